@@ -1,0 +1,356 @@
+"""Benchmark: standalone 2D nodal Helmholtz solves (2049x1025, 9-point, rtol 1e-8).
+
+One step = one projection solve of one seeded synthetic system: the
+reference-packed operands are turned into device flux planes
+(bella_op2d_set) and solved with the mixed-precision BiCGStab (FP32 stencil
+and vector updates, FP64 inner products / iterative-refinement residual /
+accumulated solution) to a true relative residual of 1e-8.  Seeds cycle over
+up to 64 pre-generated systems resident in HBM; the L2 is flushed (256 MB
+write) before every step.
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  Under torchrun (N > 1) each rank solves its
+own seeds (independent replicas, weak scaling) and the time is the max over
+ranks.  ``--impl reference`` times the reference algorithm on the host cores
+(the CPU restatement of the reference path: NumPy stencil + SciPy BiCGStab,
+FP64) on the same configuration.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX, NY = 2049, 1025
+TOL = 1e-8
+MAXIT = 30000
+METRIC = "solves/s to 1e-8 residual: learned-precond vs plain BiCGStab, 1 GB300"
+WORKLOAD = "2D nodal Helmholtz 9-point solve, 2049x1025 nodes, pseudo-incompressible, rtol 1e-8, 64 seeds"
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--seeds", type=int, default=64)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    return ap.parse_args()
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, name in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# --------------------------------------------------------------------------
+# CPU side (reference algorithm restated; bounded sample)
+# --------------------------------------------------------------------------
+def cpu_sample(w_np, iters_per_solve, seconds):
+    """Time the FP64 NumPy/SciPy restatement of the reference solve on this host.
+
+    Runs scipy BiCGStab with the oracle's vectorised lap2D_gather_new for a
+    bounded number of iterations and converts the time per iteration to
+    solves/s with the iteration count of one full FP64 solve.
+    """
+    import scipy.sparse.linalg as spla
+    from oracle import nodal2d as n2
+    op = w_np
+    n = op["nx"] * op["ny"]
+    mv = lambda v: n2.lap2d_gather(v, op)
+    t0 = time.perf_counter()
+    mv(op["b"])
+    t_mv = time.perf_counter() - t0
+    it = max(3, int(seconds / (2.2 * t_mv)))
+    A = spla.LinearOperator((n, n), matvec=mv, dtype=np.float64)
+    cnt = [0]
+    t0 = time.perf_counter()
+    spla.bicgstab(A, op["b"], rtol=1e-30, atol=0.0, maxiter=it, callback=lambda xk: cnt.__setitem__(0, cnt[0] + 1))
+    dt = time.perf_counter() - t0
+    per_iter = dt / max(cnt[0], 1)
+    return 1.0 / (per_iter * iters_per_solve), per_iter, cnt[0], dt
+
+
+def _to_np(w):
+    import torch
+    out = {}
+    for k, v in w.items():
+        if isinstance(v, torch.Tensor):
+            out[k] = v.cpu().numpy()
+        elif isinstance(v, tuple):
+            out[k] = tuple(None if t is None else t.cpu().numpy() for t in v)
+        else:
+            out[k] = v
+    nc = (out["nx"] + 1) * (out["ny"] + 1)
+    cxx, cyy, cxy, cyx = out["cor"]
+    z = np.zeros(nc)
+    out["cor"] = (cxx, cyy, z if cxy is None else cxy, z if cyx is None else cyx)
+    out["hcenter"] = np.zeros(out["nx"] * out["ny"]) if out["hcenter"] is None else out["hcenter"]
+    return out
+
+
+def run_reference(args):
+    """``--impl reference``: the reference algorithm on the host cores."""
+    ws, rank, local = _dist()
+    if ws > 1 and rank != 0:
+        return
+    from oracle import cases
+    w = cases.stratified_2d(seed=0, inx=NX, iny=NY)
+    w_np = dict(w["op"])
+    w_np["b"] = w["b"]
+    # iterations of one full FP64 solve: measured once on a smaller grid of the
+    # same construction and scaled with the grid size (BiCGStab iterations on
+    # this operator grow linearly with the node count per dimension)
+    from oracle.krylov import bicgstab_legacy
+    ws_small = cases.stratified_2d(seed=0, inx=257, iny=129)
+    _, info, it_small = bicgstab_legacy(ws_small["op"], ws_small["b"], TOL, MAXIT)
+    iters_est = it_small * (NX - 1) / 256.0
+    vals = []
+    t_all0 = time.perf_counter()
+    for s in range(args.warmup + args.steps):
+        v, per_iter, n_it, dt = cpu_sample(w_np, iters_est, max(2.0, args.cpu_seconds / 4))
+        if s >= args.warmup:
+            vals.append(v)
+    wall = time.perf_counter() - t_all0
+    value = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "rtol": TOL,
+                                           "l2": "inputs resident on host"},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": 1, "kind": "port",
+                             "sample": "NumPy lap2D_gather_new restatement + scipy bicgstab (FP64), "
+                                       "bounded iteration samples on seed 0; solves/s = 1/(s per iteration x "
+                                       "%.0f iterations per solve, from a 257x129 solve scaled by grid size)"
+                                       % iters_est},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": wall}
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------
+# GPU side
+# --------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+    from pybella_gb300 import linalg, workloads, _lib
+
+    world, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+
+    nseeds = max(1, min(args.seeds, args.steps + args.warmup))
+    systems = [workloads.stratified_2d(seed=1000 * rank + s, nx=NX, ny=NY, device=dev) for s in range(nseeds)]
+    ws = _lib.Workspace(local)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    xbuf = torch.empty(NX * NY, dtype=torch.float64, device=dev)
+
+    def step(i, stats):
+        w = systems[i % nseeds]
+        flush.fill_(float(i))
+        A = linalg.NodalHelmholtz2D(w["hplusx"], w["hplusy"], w["hcenter"], w["cor"], w["diag_inv"],
+                                    NX, NY, w["dx"], w["dy"], w["x_wall"], w["y_wall"], ws=ws)
+        x, st = A.solve(w["b"], tol=TOL, maxiter=MAXIT, precision="mixed", out=xbuf)
+        stats.append(st)
+
+    warm = []
+    for i in range(args.warmup):
+        step(i, warm)
+    # one FP64 solve of the first system: iteration count of the scipy-path algorithm
+    w0 = systems[0]
+    A0 = linalg.NodalHelmholtz2D(w0["hplusx"], w0["hplusy"], w0["hcenter"], w0["cor"], w0["diag_inv"],
+                                 NX, NY, w0["dx"], w0["dy"], w0["x_wall"], w0["y_wall"], ws=ws)
+    _, st64 = A0.solve(w0["b"], tol=TOL, maxiter=MAXIT, precision="fp64")
+
+    ws.profile(True)
+    launches0 = ws.launches
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    ev0.record()
+    stats = []
+    for i in range(args.steps):
+        step(args.warmup + i, stats)
+    ev1.record()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    launches = ws.launches - launches0
+    kt = {k: ws.kernel_time(k) for k in range(4)}
+    ws.profile(False)
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    total_solves = args.steps * world
+    value = total_solves / (ms / 1000.0)
+
+    # ---- end to end through the drop-in API with host buffers ----
+    host = [_to_np(systems[i % nseeds]) for i in range(min(nseeds, 4))]
+    e2e_stats = []
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    te0 = time.perf_counter()
+    for i in range(args.steps):
+        h = host[i % len(host)]
+        A = linalg.NodalHelmholtz2D(h["hplusx"], h["hplusy"], h["hcenter"], h["cor"], h["diag_inv"],
+                                    NX, NY, h["dx"], h["dy"], h["x_wall"], h["y_wall"], ws=ws)
+        x, info = linalg.bicgstab(linalg.LinearOperator(A.shape, A), h["b"], tol=TOL, maxiter=MAXIT,
+                                  precision="mixed")
+        e2e_stats.append(info)
+    torch.cuda.synchronize()
+    te = time.perf_counter() - te0
+    if dist is not None:
+        t = torch.tensor([te], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        te = float(t.item())
+    e2e_value = total_solves / te
+    nnode = NX * NY
+    ncell = (NX + 1) * (NY + 1)
+    h2d = 8 * (4 * ncell + 2 * nnode) + 8 * nnode   # hplusx, hplusy, cxx, cyy, diag_inv, hcenter, b
+    d2h = 8 * nnode
+
+    # ---- roofline of the dominant kernel (p-direction stencil, FP32) ----
+    peak, peak_kind = _peaks()
+    names = {0: "stencil_pdir", 1: "stencil_sdir", 2: "vector_update", 3: "resid_fp64"}
+    share = {names[k]: kt[k][0] for k in kt}
+    tot_k = sum(share.values()) or 1.0
+    pd_ms, pd_n = kt[0]
+    # algorithmic bytes per launch: r, p_old, v_old, r^ read; p_new, v_new written;
+    # Axx, Ayy per cell; diag_inv per node  -> 9 FP32 words per node
+    alg_bytes = 4.0 * (7 * nnode + 2 * ncell)
+    achieved = alg_bytes / (pd_ms / pd_n / 1000.0) / 1e9 if pd_n else None
+    iters = [s["iterations"] for s in stats]
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "rtol": TOL, "precision": "mixed",
+                   "l2": "flushed (256 MB write) before every step", "seeds": nseeds,
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "path": "pybella_gb300.linalg.bicgstab on NumPy operands"},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "kernel": "k_stencil2d<float, PDIR>", "peak_source": peak_kind,
+                     "alg_bytes_per_launch": alg_bytes},
+        "clocks": clk,
+        "solver": {"iterations_mean": float(np.mean(iters)), "outer_mean": float(np.mean([s["outer"] for s in stats])),
+                   "relres_max": max(s["relres"] for s in stats), "status": sorted(set(s["status"] for s in stats)),
+                   "fp64_path_iterations": st64["iterations"], "fp64_path_relres": st64["relres"],
+                   "e2e_info": sorted(set(e2e_stats))},
+        "kernel_ms_share": {k: v / tot_k for k, v in share.items()},
+        "kernel_ms_per_launch": {names[k]: (kt[k][0] / kt[k][1] if kt[k][1] else None) for k in kt},
+        "wall_s": wall,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        w_np = _to_np(systems[0])
+        v, per_iter, n_it, dt = cpu_sample(w_np, st64["iterations"], args.cpu_seconds)
+        line["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": 1, "kind": "port",
+                                "sample": "%d FP64 BiCGStab iterations (NumPy lap2D_gather_new restatement + scipy) "
+                                          "on seed 0 in %.1f s; solves/s = 1/(%.3f s/iter x %d iterations of the "
+                                          "FP64 solve)" % (n_it, dt, per_iter, st64["iterations"])}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = _args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

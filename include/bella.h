@@ -1,0 +1,121 @@
+/*
+ * bella.h -- C ABI of libbella_gb300.so, the GB300 (sm_103a) implicit nodal
+ * pressure projection of pyBELLA.
+ *
+ * Plain C: device pointers, sizes, doubles and an opaque workspace.  No
+ * framework types cross this boundary.  Every call returns an int status
+ * (BELLA_OK == 0); no exceptions cross the ABI.  `stream` is a cudaStream_t
+ * passed as void* (NULL = legacy default stream).
+ *
+ * Ownership: the caller allocates and owns every input/output buffer (device
+ * memory).  The library owns only what hangs off a bella_ws workspace
+ * (prepared operator planes, Krylov vectors, reduction partials), created
+ * with bella_ws_create and freed with bella_ws_destroy.  One workspace must
+ * not be used from two host threads at the same time.
+ *
+ * Vector layout (identical to the reference's solver vectors):
+ *   2D: inner nodes, y-major, idx = j*nx + i  (second_projection.py:174,214,245)
+ *   3D: inner nodes, C order over (x,y,z), idx = (i*ny + j)*nz + k
+ *       (second_projection.py:224,268)
+ */
+#ifndef BELLA_H
+#define BELLA_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define BELLA_OK          0   /* converged / done                              */
+#define BELLA_MAXITER     1   /* iteration limit reached without convergence    */
+#define BELLA_BREAKDOWN   2   /* rho or omega (or <r^,v>) below breakdown limit */
+#define BELLA_NONFINITE   3   /* NaN/Inf met in a residual norm                 */
+#define BELLA_TIMEOUT     4   /* wall-clock limit of the host loop exceeded     */
+#define BELLA_EINVAL    (-1)  /* invalid argument                               */
+#define BELLA_ECUDA     (-2)  /* CUDA runtime error (see bella_last_error)      */
+#define BELLA_ENOOP     (-3)  /* workspace has no operator set                  */
+
+typedef struct bella_ws bella_ws;   /* opaque workspace */
+
+/*
+ * 2D 9-point nodal operator, operands exactly as packed by the reference's
+ * stencil_9pt_numba_test (laplacian.py:496-528) and consumed by
+ * lap2D_gather_new (laplacian.py:546-746):
+ *   hplusx, hplusy, cxx, cyy, cxy, cyx : (ny+1)*(nx+1) cell values, row stride nx+1
+ *   hcenter, diag_inv                  : ny*nx node values
+ * All FP64 device pointers.  hcenter, cxy, cyx may be NULL (== all zero).
+ * x_wall / y_wall: 1 zeroes the hplus of the outer cell column / row
+ * (the reference's wall handling, laplacian.py:691-713); periodic wrap with
+ * the duplicated seam (wrap distance n-1, laplacian.py:595-638) is always on.
+ */
+typedef struct bella_op2d {
+    int nx, ny;
+    int x_wall, y_wall;
+    double dx, dy;
+    const double *hplusx, *hplusy, *hcenter;
+    const double *cxx, *cyy, *cxy, *cyx;
+    const double *diag_inv;
+} bella_op2d;
+
+/* Solver options.  tol/atol follow the reference's scipy call
+ * (second_projection.py:230, scipy 1.7 legacy `tol`): converged when
+ * ||b - A x|| <= max(atol, tol*||b||); ||b|| <= tol returns x = 0 at once. */
+typedef struct bella_solve_opts {
+    double tol;              /* relative tolerance on ||b - A x||            */
+    double atol;             /* absolute floor (0 = none)                    */
+    int    maxiter;          /* inner BiCGStab iteration limit (total)       */
+    int    precision;        /* 0: FP64 BiCGStab;  1: FP32 inner + FP64 IR   */
+    int    x0_zero;          /* 1: start from x = 0 (x is output only)       */
+    int    project_null;     /* 1: keep x orthogonal to the left null vector
+                                (pseudo-incompressible operator)           */
+    double inner_tol;        /* IR: inner relative residual reduction        */
+    int    max_outer;        /* IR: outer iteration limit                    */
+    int    check_every;      /* iterations per captured graph block          */
+    double timeout_s;        /* host wall-clock limit (0 = none)             */
+} bella_solve_opts;
+
+typedef struct bella_solve_stats {
+    int    status;           /* BELLA_OK, BELLA_MAXITER, ...                 */
+    int    iterations;       /* BiCGStab iterations (all inner solves)       */
+    int    outer;            /* IR outer iterations (0 for precision 0)      */
+    int    matvecs;          /* operator applications                        */
+    double relres;           /* final FP64 ||b - A x|| / ||b||               */
+    double bnorm;            /* ||b||                                        */
+    double seconds;          /* host wall time of the call                   */
+} bella_solve_stats;
+
+/* ---- workspace --------------------------------------------------------- */
+int  bella_ws_create(bella_ws **ws, int device);
+int  bella_ws_destroy(bella_ws *ws);
+const char *bella_last_error(void);
+const char *bella_status_string(int status);
+int  bella_version(void);
+/* number of library kernel launches issued through this workspace */
+long long bella_ws_launches(const bella_ws *ws);
+/* per-kernel CUDA-event timing of the solver kernels (0 = off).  kind:
+ * 0 = p-direction stencil (v = A p), 1 = s-direction stencil (t = A s),
+ * 2 = vector update, 3 = FP64 residual stencil.  Totals since enable. */
+int  bella_ws_profile(bella_ws *ws, int enable);
+int  bella_ws_kernel_time(bella_ws *ws, int kind, double *total_ms, long long *count);
+
+/* ---- 2D operator (replaces the closure returned by stencil_9pt_numba_test,
+ *      laplacian.py:496-528, wrapped as LinearOperator at
+ *      second_projection.py:205) ----------------------------------------- */
+int bella_op2d_set(bella_ws *ws, const bella_op2d *op, void *stream);
+
+/* y = A x with the prepared operator: FP64 (parity path) and FP32 planes.
+ * Replaces one call of lap2D_gather_new (laplacian.py:546-746). */
+int bella_apply_f64(bella_ws *ws, const double *x, double *y, void *stream);
+int bella_apply_f32(bella_ws *ws, const float *x, float *y, void *stream);
+
+/* ---- solver (replaces scipy.sparse.linalg.bicgstab at
+ *      second_projection.py:230) ---------------------------------------- */
+void bella_solve_opts_default(bella_solve_opts *o);
+int  bella_bicgstab(bella_ws *ws, const double *b, double *x,
+                    const bella_solve_opts *opts, bella_solve_stats *stats,
+                    void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BELLA_H */

@@ -1,0 +1,141 @@
+"""ctypes binding of libbella_gb300.so (the C ABI declared in include/bella.h).
+
+The library is the only compute path: if it is missing this module raises,
+it never falls back to a CPU implementation.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libbella_gb300.so")
+
+BELLA_OK = 0
+BELLA_MAXITER = 1
+BELLA_BREAKDOWN = 2
+BELLA_NONFINITE = 3
+BELLA_TIMEOUT = 4
+BELLA_EINVAL = -1
+BELLA_ECUDA = -2
+BELLA_ENOOP = -3
+
+_dp = ctypes.c_void_p
+
+
+class Op2D(ctypes.Structure):
+    """``bella_op2d``: reference-packed 2D operands (device pointers)."""
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int),
+                ("x_wall", ctypes.c_int), ("y_wall", ctypes.c_int),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double),
+                ("hplusx", _dp), ("hplusy", _dp), ("hcenter", _dp),
+                ("cxx", _dp), ("cyy", _dp), ("cxy", _dp), ("cyx", _dp),
+                ("diag_inv", _dp)]
+
+
+class SolveOpts(ctypes.Structure):
+    """``bella_solve_opts``."""
+    _fields_ = [("tol", ctypes.c_double), ("atol", ctypes.c_double),
+                ("maxiter", ctypes.c_int), ("precision", ctypes.c_int),
+                ("x0_zero", ctypes.c_int), ("project_null", ctypes.c_int),
+                ("inner_tol", ctypes.c_double), ("max_outer", ctypes.c_int),
+                ("check_every", ctypes.c_int), ("timeout_s", ctypes.c_double)]
+
+
+class SolveStats(ctypes.Structure):
+    """``bella_solve_stats``."""
+    _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int),
+                ("outer", ctypes.c_int), ("matvecs", ctypes.c_int),
+                ("relres", ctypes.c_double), ("bnorm", ctypes.c_double),
+                ("seconds", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# exported symbol -> (restype, argtypes); also the list checked by the tests
+SIGNATURES = {
+    "bella_ws_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]),
+    "bella_ws_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "bella_last_error": (ctypes.c_char_p, []),
+    "bella_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "bella_version": (ctypes.c_int, []),
+    "bella_ws_launches": (ctypes.c_longlong, [ctypes.c_void_p]),
+    "bella_ws_profile": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "bella_ws_kernel_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                            ctypes.POINTER(ctypes.c_longlong)]),
+    "bella_op2d_set": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Op2D), ctypes.c_void_p]),
+    "bella_apply_f64": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, ctypes.c_void_p]),
+    "bella_apply_f32": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, ctypes.c_void_p]),
+    "bella_solve_opts_default": (None, [ctypes.POINTER(SolveOpts)]),
+    "bella_bicgstab": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, ctypes.POINTER(SolveOpts),
+                                      ctypes.POINTER(SolveStats), ctypes.c_void_p]),
+}
+
+_lib = None
+
+
+def load():
+    """Load the library (once).  Raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            "libbella_gb300.so is not built (%s); run `python -m pybella_gb300.build` "
+            "(needs nvcc).  There is no CPU fallback." % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class BellaError(RuntimeError):
+    pass
+
+
+def check(rc, what):
+    """Raise :class:`BellaError` for a negative (error) return code."""
+    if rc < 0:
+        lib = load()
+        raise BellaError("%s failed (%d: %s): %s" % (
+            what, rc, lib.bella_status_string(rc).decode(), lib.bella_last_error().decode()))
+    return rc
+
+
+class Workspace:
+    """Owns one ``bella_ws`` handle on a CUDA device."""
+
+    def __init__(self, device=0):
+        self._lib = load()
+        h = ctypes.c_void_p()
+        check(self._lib.bella_ws_create(ctypes.byref(h), int(device)), "bella_ws_create")
+        self.handle = h
+        self.device = int(device)
+
+    @property
+    def launches(self):
+        return int(self._lib.bella_ws_launches(self.handle))
+
+    def profile(self, enable=True):
+        check(self._lib.bella_ws_profile(self.handle, int(bool(enable))), "bella_ws_profile")
+
+    def kernel_time(self, kind):
+        """(total ms, launches) of one solver kernel kind since profiling was enabled."""
+        t = ctypes.c_double()
+        c = ctypes.c_longlong()
+        check(self._lib.bella_ws_kernel_time(self.handle, int(kind), ctypes.byref(t), ctypes.byref(c)),
+              "bella_ws_kernel_time")
+        return t.value, c.value
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            self._lib.bella_ws_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,233 @@
+// bella_common.cuh -- shared device helpers and the workspace layout of
+// libbella_gb300 (GB300 / sm_103a implicit nodal pressure projection).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <math.h>
+
+#include "../../include/bella.h"
+
+namespace bella {
+
+// --------------------------------------------------------------------------
+// launch geometry of the 2D stencil tiles
+// --------------------------------------------------------------------------
+constexpr int TX = 64;          // tile width  (nodes, x)  = 2 warps
+constexpr int TY = 16;          // tile height (nodes, y)
+constexpr int BX = 64;          // threads in x
+constexpr int BY = 4;           // threads in y  -> 256 threads, 4 rows each
+constexpr int NTHREADS = BX * BY;
+constexpr int NSM = 152;        // GB300 SMs (grid sizes are multiples of this)
+constexpr int VEC_BLOCK = 256;  // block size of the streaming vector kernels
+constexpr int NQ = 8;           // reduction quantities per kernel (max)
+constexpr int MAXNULL = 8;      // null-space modes handled by the projection
+
+// --------------------------------------------------------------------------
+// device-resident Krylov state.  Written only by the last block of a kernel
+// (last-block-done reduction) and read by every block of the next kernel.
+// --------------------------------------------------------------------------
+struct KState {
+    double rho;        // <r^, r> of the current residual
+    double rho_prev;
+    double alpha;
+    double omega;
+    double beta;
+    double rr;         // ||r||^2
+    double ss;         // ||s||^2
+    double atol;       // absolute stopping threshold on ||r|| (and ||s||)
+    double rhotol;     // rho / omega breakdown limit
+    double scale;      // IR: inner system = outer residual / scale
+    double dot_aux;    // result of the generic FP64 dot kernel
+    double dot_aux2;
+    int    iter;       // iterations done in this (inner) solve
+    int    maxiter;    // iteration limit of this (inner) solve
+    int    done;       // 1 once converged / failed: later kernels return at once
+    int    status;     // BELLA_* status of the (inner) solve
+    int    early;      // ||s|| < atol met inside the current iteration
+    int    pad[3];
+    double nd[MAXNULL];     // <z_k, x> of the null-space projection
+    double cnull[MAXNULL];  // coefficients removed along the null modes
+};
+
+// --------------------------------------------------------------------------
+// null space of the pseudo-incompressible operator (hcenter = 0, no cross
+// terms): sign-pattern modes e(i,j,k) = sx^i sy^j sz^k (constants and the
+// checkerboards the cell-averaged differences cannot see).  The left null
+// vectors are z_k = D w e_k with D = 1/diag_inv and w the trapezoid weights
+// (1/2 on a duplicated periodic seam).  ginv = inverse Gram matrix
+// G_kl = <z_k, e_l>.
+// --------------------------------------------------------------------------
+struct NullSpace {
+    int nm;
+    int ndim, nx, ny, nz;
+    signed char sx[MAXNULL], sy[MAXNULL], sz[MAXNULL];
+    double ginv[MAXNULL * MAXNULL];
+};
+
+__device__ __forceinline__ double null_mode(const NullSpace &ns, int m, long long g) {
+    long long i, j, k;
+    if (ns.ndim == 2) { j = g / ns.nx; i = g - j * ns.nx; k = 0; }
+    else { k = g % ns.nz; long long t = g / ns.nz; j = t % ns.ny; i = t / ns.ny; }
+    int par = 0;
+    if (ns.sx[m] < 0) par ^= (int)(i & 1);
+    if (ns.sy[m] < 0) par ^= (int)(j & 1);
+    if (ns.sz[m] < 0) par ^= (int)(k & 1);
+    return par ? -1.0 : 1.0;
+}
+
+// --------------------------------------------------------------------------
+// double-float accumulation of FP32 products (error-free transformations):
+// each product a*b = p + e exactly (fmaf), and the running sum keeps a
+// compensated low word.  Converted to FP64 at the warp level, so the FP32
+// Krylov inner products are accurate to ~1e-14 without per-element FP64
+// arithmetic (GB300's FP64 pipe is narrow).
+// --------------------------------------------------------------------------
+struct DF {
+    float hi, lo;
+    __device__ __forceinline__ void zero() { hi = 0.f; lo = 0.f; }
+    __device__ __forceinline__ void add_prod(float a, float b) {
+        float p = a * b;
+        float e = fmaf(a, b, -p);
+        float s = hi + p;
+        float bb = s - hi;
+        float err = (hi - (s - bb)) + (p - bb);
+        hi = s;
+        lo += err + e;
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+struct DD {
+    double v;
+    __device__ __forceinline__ void zero() { v = 0.0; }
+    __device__ __forceinline__ void add_prod(double a, double b) { v = fma(a, b, v); }
+    __device__ __forceinline__ double value() const { return v; }
+};
+
+template <typename T> struct Acc;
+template <> struct Acc<float>  { using type = DF; };
+template <> struct Acc<double> { using type = DD; };
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum of NQ values (fixed tree order -> deterministic).  `red`
+// must hold 32*NQ doubles of shared memory.  Result valid in thread 0.
+template <int Q>
+__device__ __forceinline__ void block_sum(double (&v)[Q], double *red) {
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+    const int nthreads = blockDim.x * blockDim.y;
+    const int lane = tid & 31, wid = tid >> 5, nw = (nthreads + 31) >> 5;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) v[q] = warp_sum(v[q]);
+    if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) red[wid * Q + q] = v[q];
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) v[q] = (lane < nw) ? red[lane * Q + q] : 0.0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) v[q] = warp_sum(v[q]);
+    }
+    __syncthreads();
+}
+
+// Last-block-done grid reduction.  Every block writes its Q partial sums,
+// the last block to arrive sums all partials in block order (deterministic)
+// and returns true with the totals in `tot` (valid in every thread of that
+// block).  `counter` is reset to 0 by the last block.
+template <int Q>
+__device__ __forceinline__ bool grid_sum(double (&v)[Q], double *partials, unsigned *counter,
+                                         double (&tot)[Q]) {
+    __shared__ double red[32 * NQ];
+    __shared__ bool last;
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+    const int nthreads = blockDim.x * blockDim.y;
+    block_sum<Q>(v, red);
+    if (tid == 0) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) partials[(size_t)blockIdx.x * NQ + q] = v[q];
+        __threadfence();
+        unsigned prev = atomicAdd(counter, 1u);
+        last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double s[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) s[q] = 0.0;
+    for (int b = tid; b < (int)gridDim.x; b += nthreads) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) s[q] += __ldcg(&partials[(size_t)b * NQ + q]);
+    }
+    block_sum<Q>(s, red);
+    __shared__ double out[NQ];
+    if (tid == 0) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) out[q] = s[q];
+        *counter = 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < Q; ++q) tot[q] = out[q];
+    return true;
+}
+
+// --------------------------------------------------------------------------
+// prepared 2D operator (device pointers into the workspace)
+//   cell planes (ny+1)*(nx+1): Axx = 0.5/dx^2 cxx hplusx, Ayy = 0.5/dy^2 cyy hplusy,
+//   Axy = 0.5/(dx dy) cxy hplusy, Ayx = 0.5/(dx dy) cyx hplusx  (walls zeroed)
+//   node planes ny*nx: dinv, hc
+// --------------------------------------------------------------------------
+template <typename T>
+struct Op2D {
+    int nx, ny;
+    const T *axx, *ayy, *axy, *ayx;
+    const T *dinv, *hc;
+};
+
+}  // namespace bella
+
+// --------------------------------------------------------------------------
+// workspace (opaque to C callers)
+// --------------------------------------------------------------------------
+struct bella_ws {
+    int device;
+    int ndim;                 // 0: no operator yet
+    // operator geometry (nz == 1 in 2D)
+    int nx, ny, nz;
+    long long n;              // unknowns
+    int cross, has_hc, singular;
+    double *a64;              // 4 cell planes
+    float  *a32;
+    double *dinv64, *hc64, *z64;
+    float  *dinv32, *hc32;
+    bella::NullSpace ns;      // null modes (nm == 0: nonsingular)
+    // Krylov storage
+    long long cap;            // capacity (elements) of each vector below
+    void *vbase;              // one allocation for all vectors
+    double *r64, *x64v;       // IR outer residual, FP64 scratch
+    float  *r32, *rh32, *p32[2], *v32[2], *t32, *x32;
+    double *r64k, *rh64, *p64[2], *v64[2], *t64;
+    double *partials;
+    unsigned *counter;
+    bella::KState *ks;        // device
+    bella::KState *ks_host;   // pinned mirror
+    int grid_stencil, grid_vec;
+    long long launches;
+    // optional per-kernel timing with CUDA events (bella_ws_profile)
+    int prof;
+    struct Prof {
+        cudaEvent_t ev[2 * 256];
+        int pending;            // recorded pairs not yet harvested
+        double total_ms;
+        long long count;
+    } profk[4];
+};

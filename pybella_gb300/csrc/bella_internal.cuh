@@ -1,0 +1,65 @@
+// bella_internal.cuh -- declarations shared by the translation units of
+// libbella_gb300 (not part of the C ABI).
+#pragma once
+#include "bella_common.cuh"
+
+namespace bella {
+
+enum { M_APPLY = 0, M_RESID = 1, M_PDIR = 2, M_SDIR = 3 };
+
+// ---- last-block finalisers of one BiCGStab iteration -----------------------
+// The control flow and breakdown tests follow scipy's bicgstab, which the
+// reference calls (second_projection.py:230): rho/omega breakdown below
+// eps^2, early exit when ||s|| meets the tolerance, convergence on ||r||.
+
+// after v = A p:  alpha = rho / <r^, v>
+__device__ __forceinline__ void finalize_pdir(KState *ks, double rv) {
+    if (!isfinite(rv)) { ks->status = BELLA_NONFINITE; ks->done = 1; return; }
+    if (rv == 0.0) { ks->status = BELLA_BREAKDOWN; ks->done = 1; return; }
+    ks->alpha = ks->rho / rv;
+}
+
+// after t = A s:  omega = <t,s>/<t,t>, early exit on ||s||
+__device__ __forceinline__ void finalize_sdir(KState *ks, double ts, double tt, double ss) {
+    ks->ss = ss;
+    if (!isfinite(ss) || !isfinite(ts) || !isfinite(tt)) {
+        ks->status = BELLA_NONFINITE; ks->done = 1; return;
+    }
+    if (sqrt(ss) <= ks->atol) { ks->early = 1; ks->omega = 0.0; return; }
+    if (!(tt > 0.0)) { ks->status = BELLA_BREAKDOWN; ks->done = 1; return; }
+    ks->omega = ts / tt;
+}
+
+// after x += alpha p + omega s, r = s - omega t
+__device__ __forceinline__ void finalize_update(KState *ks, double rho_new, double rr) {
+    ks->iter += 1;
+    if (ks->early) { ks->status = BELLA_OK; ks->done = 1; ks->rr = ks->ss; return; }
+    ks->rr = rr;
+    if (!isfinite(rr) || !isfinite(rho_new)) { ks->status = BELLA_NONFINITE; ks->done = 1; }
+    else if (sqrt(rr) <= ks->atol) { ks->status = BELLA_OK; ks->done = 1; }
+    else if (ks->iter >= ks->maxiter) { ks->status = BELLA_MAXITER; ks->done = 1; }
+    else if (fabs(rho_new) < ks->rhotol) { ks->status = BELLA_BREAKDOWN; ks->done = 1; }
+    else if (fabs(ks->omega) < ks->rhotol) { ks->status = BELLA_BREAKDOWN; ks->done = 1; }
+    else {
+        ks->beta = (rho_new / ks->rho) * (ks->alpha / ks->omega);
+        ks->rho_prev = ks->rho;
+        ks->rho = rho_new;
+    }
+}
+
+// ---- per-kernel event timing (host) -------------------------------------------
+enum { PK_PDIR = 0, PK_SDIR = 1, PK_UPDATE = 2, PK_RESID = 3 };
+void prof_begin(bella_ws *ws, int kind, cudaStream_t s);
+void prof_end(bella_ws *ws, int kind, cudaStream_t s);
+void prof_harvest(bella_ws *ws);
+
+// ---- launchers (host) --------------------------------------------------------
+int  stencil_grid(int nx, int ny);
+int  vec_grid(long long n);
+int  op2d_pack(bella_ws *ws, const bella_op2d *op, cudaStream_t s);
+void op2d_apply(bella_ws *ws, int prec, const void *x, void *y, cudaStream_t s);
+void op2d_resid(bella_ws *ws, int prec, const void *x, const void *b, void *r, cudaStream_t s);
+void op2d_iteration(bella_ws *ws, int prec, cudaStream_t s);
+template <typename T> void launch_update(bella_ws *ws, cudaStream_t s);
+
+}  // namespace bella

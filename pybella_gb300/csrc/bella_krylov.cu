@@ -1,0 +1,658 @@
+// bella_krylov.cu -- streaming Krylov kernels, the BiCGStab / mixed-precision
+// iterative-refinement driver and the C ABI of libbella_gb300.
+//
+// Solver contract: the reference's scipy call
+//   p2, _ = scipy.sparse.linalg.bicgstab(lap, rhs_inner, tol=ud.tol,
+//                                        maxiter=ud.max_iterations, callback=counter)
+// (second_projection.py:230), with scipy 1.7 legacy `tol` semantics.
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "bella_internal.cuh"
+
+namespace bella {
+
+static thread_local std::string g_err;
+
+static int set_err(int code, const char *what) {
+    g_err = what;
+    return code;
+}
+
+static int cuda_check(cudaError_t e, const char *where) {
+    if (e == cudaSuccess) return BELLA_OK;
+    g_err = std::string(where) + ": " + cudaGetErrorString(e);
+    return BELLA_ECUDA;
+}
+
+#define BELLA_CUDA(call)                                             \
+    do {                                                             \
+        int _rc = cuda_check((call), #call);                         \
+        if (_rc != BELLA_OK) return _rc;                             \
+    } while (0)
+
+int vec_grid(long long n) {
+    long long g = (n + VEC_BLOCK - 1) / VEC_BLOCK;
+    const long long cap = (long long)NSM * 8;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+// --------------------------------------------------------------------------
+// vector kernels
+// --------------------------------------------------------------------------
+// x += alpha p + omega s,  r = s - omega t  (s = r - alpha v recomputed),
+// with <r^, r> and ||r||^2 of the new residual.
+template <typename T>
+__global__ void __launch_bounds__(VEC_BLOCK)
+k_update(long long n, T *x, const T *p0, const T *p1, T *r, const T *v0, const T *v1, const T *t,
+         const T *rh, KState *ks, double *partials, unsigned *counter) {
+    using AccT = typename Acc<T>::type;
+    if (ks->done) return;
+    const int par = ks->iter & 1;
+    const T *p = par ? p0 : p1;   // p/v written by this iteration's PDIR kernel
+    const T *v = par ? v0 : v1;
+    const T alpha = (T)ks->alpha, omega = (T)ks->omega;
+    const bool early = ks->early != 0;
+    AccT a0, a1;
+    a0.zero(); a1.zero();
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+         g += (long long)gridDim.x * blockDim.x) {
+        const T pg = p[g];
+        if (early) {
+            x[g] += alpha * pg;
+        } else {
+            const T s = r[g] - alpha * v[g];
+            x[g] += alpha * pg + omega * s;
+            const T rn = s - omega * t[g];
+            r[g] = rn;
+            a0.add_prod(rh[g], rn);
+            a1.add_prod(rn, rn);
+        }
+    }
+    double vv[2] = {a0.value(), a1.value()}, tot[2];
+    if (!grid_sum<2>(vv, partials, counter, tot)) return;
+    if (threadIdx.x == 0) finalize_update(ks, tot[0], tot[1]);
+}
+
+void prof_begin(bella_ws *ws, int kind, cudaStream_t s) {
+    if (!ws->prof) return;
+    bella_ws::Prof &p = ws->profk[kind];
+    if (p.pending == 256) prof_harvest(ws);
+    cudaEventRecord(p.ev[2 * p.pending], s);
+}
+
+void prof_end(bella_ws *ws, int kind, cudaStream_t s) {
+    if (!ws->prof) return;
+    bella_ws::Prof &p = ws->profk[kind];
+    cudaEventRecord(p.ev[2 * p.pending + 1], s);
+    p.pending++;
+}
+
+void prof_harvest(bella_ws *ws) {
+    if (!ws->prof) return;
+    for (int k = 0; k < 4; ++k) {
+        bella_ws::Prof &p = ws->profk[k];
+        for (int i = 0; i < p.pending; ++i) {
+            float ms = 0.f;
+            cudaEventSynchronize(p.ev[2 * i + 1]);
+            if (cudaEventElapsedTime(&ms, p.ev[2 * i], p.ev[2 * i + 1]) == cudaSuccess) {
+                p.total_ms += ms;
+                p.count++;
+            }
+        }
+        p.pending = 0;
+    }
+}
+
+template <typename T>
+void launch_update(bella_ws *ws, cudaStream_t s) {
+    prof_begin(ws, PK_UPDATE, s);
+    if (sizeof(T) == 8) {
+        k_update<double><<<ws->grid_vec, VEC_BLOCK, 0, s>>>(ws->n, ws->x64v, ws->p64[0], ws->p64[1], ws->r64k,
+                                                          ws->v64[0], ws->v64[1], ws->t64, ws->rh64,
+                                                          ws->ks, ws->partials, ws->counter);
+    } else {
+        k_update<float><<<ws->grid_vec, VEC_BLOCK, 0, s>>>(ws->n, ws->x32, ws->p32[0], ws->p32[1], ws->r32,
+                                                         ws->v32[0], ws->v32[1], ws->t32, ws->rh32,
+                                                         ws->ks, ws->partials, ws->counter);
+    }
+    prof_end(ws, PK_UPDATE, s);
+    ws->launches++;
+}
+template void launch_update<float>(bella_ws *, cudaStream_t);
+template void launch_update<double>(bella_ws *, cudaStream_t);
+
+static __device__ void init_state(KState *ks, double rr, double atol, double rhotol, int maxiter) {
+    ks->rho = rr;           // r^ = r  ->  rho = ||r||^2
+    ks->rho_prev = 1.0;
+    ks->rr = rr;
+    ks->alpha = 1.0;
+    ks->omega = 1.0;
+    ks->beta = 0.0;
+    ks->atol = atol;
+    ks->rhotol = rhotol;
+    ks->iter = 0;
+    ks->maxiter = maxiter;
+    ks->early = 0;
+    ks->done = 0;
+    ks->status = BELLA_MAXITER;
+    if (!isfinite(rr)) { ks->status = BELLA_NONFINITE; ks->done = 1; }
+    else if (sqrt(rr) <= atol) { ks->status = BELLA_OK; ks->done = 1; }
+    else if (maxiter <= 0) { ks->status = BELLA_MAXITER; ks->done = 1; }
+    else if (fabs(rr) < rhotol) { ks->status = BELLA_BREAKDOWN; ks->done = 1; }
+}
+
+// FP64 solve start.  x_given = 0: x = 0, r = b.  x_given = 1: r already
+// holds b - A x.  r^ = r.  atol = max(atol_user, tol*||b||) and the scipy
+// 1.7 legacy exit ||b|| <= tol -> x = 0 (x0 = 0 only).
+__global__ void __launch_bounds__(VEC_BLOCK)
+k_init64(long long n, const double *b, double *x, double *r, double *rh, int x_given, double tol,
+         double atol_user, int maxiter, KState *ks, double *partials, unsigned *counter) {
+    DD a0, a1;
+    a0.zero(); a1.zero();
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+         g += (long long)gridDim.x * blockDim.x) {
+        const double bg = b[g];
+        double rg;
+        if (!x_given) { x[g] = 0.0; rg = bg; r[g] = rg; }
+        else rg = r[g];
+        rh[g] = rg;
+        a0.add_prod(rg, rg);
+        a1.add_prod(bg, bg);
+    }
+    double vv[2] = {a0.value(), a1.value()}, tot[2];
+    if (!grid_sum<2>(vv, partials, counter, tot)) return;
+    if (threadIdx.x != 0) return;
+    const double bnorm = sqrt(tot[1]);
+    double atol = tol * bnorm;
+    if (atol_user > atol) atol = atol_user;
+    init_state(ks, tot[0], atol, 4.930380657631324e-32 /* eps64^2 */, maxiter);
+    ks->dot_aux = bnorm;
+    if (bnorm == 0.0 || (!x_given && bnorm <= tol)) { ks->status = BELLA_OK; ks->done = 1; }
+}
+
+// FP32 inner solve start (iterative refinement): r32 = r64 / scale, r^ = r32, x32 = 0.
+__global__ void __launch_bounds__(VEC_BLOCK)
+k_init32(long long n, const double *r64, double inv_scale, float *r, float *rh, float *x,
+         double atol, int maxiter, KState *ks, double *partials, unsigned *counter) {
+    DF a0;
+    a0.zero();
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+         g += (long long)gridDim.x * blockDim.x) {
+        const float rg = (float)(r64[g] * inv_scale);
+        r[g] = rg;
+        rh[g] = rg;
+        x[g] = 0.f;
+        a0.add_prod(rg, rg);
+    }
+    double vv[1] = {a0.value()}, tot[1];
+    if (!grid_sum<1>(vv, partials, counter, tot)) return;
+    if (threadIdx.x == 0) init_state(ks, tot[0], atol, 4.930380657631324e-32, maxiter);
+}
+
+// x64 += scale * x32, and <z_k, x64> for every null mode (projection).
+__global__ void __launch_bounds__(VEC_BLOCK)
+k_ir_update(long long n, double *x64, const float *x32, double scale, const double *z, NullSpace ns,
+            KState *ks, double *partials, unsigned *counter) {
+    double acc[MAXNULL];
+#pragma unroll
+    for (int m = 0; m < MAXNULL; ++m) acc[m] = 0.0;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+         g += (long long)gridDim.x * blockDim.x) {
+        const double xn = x64[g] + scale * (double)x32[g];
+        x64[g] = xn;
+        if (ns.nm) {
+            const double zx = z[g] * xn;
+#pragma unroll
+            for (int m = 0; m < MAXNULL; ++m)
+                if (m < ns.nm) acc[m] += null_mode(ns, m, g) * zx;
+        }
+    }
+    if (!ns.nm) return;
+    double tot[MAXNULL];
+    if (!grid_sum<MAXNULL>(acc, partials, counter, tot)) return;
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < ns.nm; ++k) {
+            ks->nd[k] = tot[k];
+            double c = 0.0;
+            for (int l = 0; l < ns.nm; ++l) c += ns.ginv[k * MAXNULL + l] * tot[l];
+            ks->cnull[k] = c;
+        }
+    }
+}
+
+// x64 -= sum_l c_l e_l: removes the null-space component, keeping x in the
+// operator's range where the exact Krylov solution from x0 = 0 lies.
+__global__ void k_null_shift(long long n, double *x64, const KState *ks, NullSpace ns) {
+    double c[MAXNULL];
+#pragma unroll
+    for (int m = 0; m < MAXNULL; ++m) c[m] = (m < ns.nm) ? ks->cnull[m] : 0.0;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+         g += (long long)gridDim.x * blockDim.x) {
+        double d = 0.0;
+#pragma unroll
+        for (int m = 0; m < MAXNULL; ++m)
+            if (m < ns.nm) d += c[m] * null_mode(ns, m, g);
+        x64[g] -= d;
+    }
+}
+
+// Gram entry G_kl = <z, e_k e_l> -> ks->dot_aux
+__global__ void __launch_bounds__(VEC_BLOCK)
+k_null_gram(long long n, const double *z, NullSpace ns, int k, int l, KState *ks, double *partials,
+            unsigned *counter) {
+    double a[1] = {0.0};
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+         g += (long long)gridDim.x * blockDim.x)
+        a[0] += z[g] * null_mode(ns, k, g) * null_mode(ns, l, g);
+    double tot[1];
+    if (!grid_sum<1>(a, partials, counter, tot)) return;
+    if (threadIdx.x == 0) ks->dot_aux = tot[0];
+}
+
+// generic FP64 dot -> ks->dot_aux
+__global__ void __launch_bounds__(VEC_BLOCK)
+k_dot64(long long n, const double *a, const double *b, KState *ks, double *partials, unsigned *counter) {
+    DD a0;
+    a0.zero();
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+         g += (long long)gridDim.x * blockDim.x)
+        a0.add_prod(a[g], b ? b[g] : 1.0);
+    double vv[1] = {a0.value()}, tot[1];
+    if (!grid_sum<1>(vv, partials, counter, tot)) return;
+    if (threadIdx.x == 0) ks->dot_aux = tot[0];
+}
+
+}  // namespace bella
+
+// ============================================================================
+// C ABI
+// ============================================================================
+using namespace bella;
+
+extern "C" {
+
+const char *bella_last_error(void) { return g_err.c_str(); }
+
+const char *bella_status_string(int st) {
+    switch (st) {
+        case BELLA_OK: return "converged";
+        case BELLA_MAXITER: return "iteration limit reached";
+        case BELLA_BREAKDOWN: return "breakdown (rho or omega below limit)";
+        case BELLA_NONFINITE: return "non-finite residual";
+        case BELLA_TIMEOUT: return "timeout";
+        case BELLA_EINVAL: return "invalid argument";
+        case BELLA_ECUDA: return "CUDA error";
+        case BELLA_ENOOP: return "no operator set";
+        default: return "unknown status";
+    }
+}
+
+int bella_version(void) { return 100; }
+
+long long bella_ws_launches(const bella_ws *ws) { return ws ? ws->launches : 0; }
+
+int bella_ws_create(bella_ws **out, int device) {
+    if (!out) return set_err(BELLA_EINVAL, "bella_ws_create: null output pointer");
+    *out = nullptr;
+    BELLA_CUDA(cudaSetDevice(device));
+    bella_ws *ws = (bella_ws *)calloc(1, sizeof(bella_ws));
+    if (!ws) return set_err(BELLA_EINVAL, "bella_ws_create: out of host memory");
+    ws->device = device;
+    int rc = cuda_check(cudaMalloc(&ws->ks, sizeof(KState)), "cudaMalloc(ks)");
+    if (rc == BELLA_OK) rc = cuda_check(cudaMallocHost(&ws->ks_host, sizeof(KState)), "cudaMallocHost(ks)");
+    if (rc == BELLA_OK) rc = cuda_check(cudaMalloc(&ws->counter, 64), "cudaMalloc(counter)");
+    if (rc == BELLA_OK) rc = cuda_check(cudaMemset(ws->counter, 0, 64), "cudaMemset(counter)");
+    if (rc == BELLA_OK)
+        rc = cuda_check(cudaMalloc(&ws->partials, sizeof(double) * NQ * NSM * 8), "cudaMalloc(partials)");
+    if (rc == BELLA_OK) rc = cuda_check(cudaMemset(ws->ks, 0, sizeof(KState)), "cudaMemset(ks)");
+    if (rc != BELLA_OK) {
+        bella_ws_destroy(ws);
+        return rc;
+    }
+    *out = ws;
+    return BELLA_OK;
+}
+
+static void free_op(bella_ws *ws) {
+    cudaFree(ws->a64); cudaFree(ws->a32);
+    cudaFree(ws->dinv64); cudaFree(ws->hc64); cudaFree(ws->z64);
+    cudaFree(ws->dinv32); cudaFree(ws->hc32);
+    ws->a64 = nullptr; ws->a32 = nullptr; ws->dinv64 = ws->hc64 = ws->z64 = nullptr;
+    ws->dinv32 = ws->hc32 = nullptr;
+}
+
+int bella_ws_destroy(bella_ws *ws) {
+    if (!ws) return BELLA_OK;
+    cudaSetDevice(ws->device);
+    if (ws->prof) bella_ws_profile(ws, 0);
+    free_op(ws);
+    cudaFree(ws->vbase);
+    cudaFree(ws->partials);
+    cudaFree(ws->counter);
+    cudaFree(ws->ks);
+    if (ws->ks_host) cudaFreeHost(ws->ks_host);
+    free(ws);
+    return BELLA_OK;
+}
+
+// carve the Krylov vectors for n unknowns out of one allocation
+static int ensure_vectors(bella_ws *ws, long long n) {
+    if (ws->cap >= n && ws->vbase) return BELLA_OK;
+    cudaFree(ws->vbase);
+    ws->vbase = nullptr;
+    const long long np = (n + 63) / 64 * 64;   // 256-byte aligned slices
+    const size_t bytes = (size_t)np * (8 * 9 + 4 * 8);
+    BELLA_CUDA(cudaMalloc(&ws->vbase, bytes));
+    char *p = (char *)ws->vbase;
+    auto take64 = [&](double **d) { *d = (double *)p; p += np * 8; };
+    auto take32 = [&](float **f) { *f = (float *)p; p += np * 4; };
+    take64(&ws->r64); take64(&ws->x64v); take64(&ws->r64k); take64(&ws->rh64);
+    take64(&ws->p64[0]); take64(&ws->p64[1]); take64(&ws->v64[0]); take64(&ws->v64[1]); take64(&ws->t64);
+    take32(&ws->r32); take32(&ws->rh32); take32(&ws->p32[0]); take32(&ws->p32[1]);
+    take32(&ws->v32[0]); take32(&ws->v32[1]); take32(&ws->t32); take32(&ws->x32);
+    ws->cap = n;
+    return BELLA_OK;
+}
+
+// Null modes of a singular (pseudo-incompressible) operator and the inverse of
+// their Gram matrix.  A checkerboard on a periodic axis needs an even period.
+static int setup_null_space(bella_ws *ws, cudaStream_t s, int xper, int yper, int zper) {
+    NullSpace &ns = ws->ns;
+    memset(&ns, 0, sizeof(ns));
+    ns.ndim = ws->ndim;
+    ns.nx = ws->nx; ns.ny = ws->ny; ns.nz = ws->nz > 0 ? ws->nz : 1;
+    if (!ws->singular) return BELLA_OK;
+    const int nn[3] = {ws->nx, ws->ny, ws->nz};
+    const int per[3] = {xper, yper, zper};
+    auto ok = [&](int axis) { return !per[axis] || ((nn[axis] - 1) % 2 == 0); };
+    auto add = [&](int a, int b, int c) {
+        ns.sx[ns.nm] = (signed char)a; ns.sy[ns.nm] = (signed char)b; ns.sz[ns.nm] = (signed char)c; ns.nm++;
+    };
+    add(1, 1, 1);
+    if (ws->ndim == 2) {
+        if (ok(0) && ok(1)) add(-1, -1, 1);
+    } else {
+        if (ok(0) && ok(1)) add(-1, -1, 1);
+        if (ok(0) && ok(2)) add(-1, 1, -1);
+        if (ok(1) && ok(2)) add(1, -1, -1);
+        if (ok(0) && ok(1) && ok(2)) add(-1, -1, -1);
+    }
+    const int nm = ns.nm;
+    double G[MAXNULL * MAXNULL];
+    for (int k = 0; k < nm; ++k)
+        for (int l = 0; l < nm; ++l) {
+            k_null_gram<<<ws->grid_vec, VEC_BLOCK, 0, s>>>(ws->n, ws->z64, ns, k, l, ws->ks, ws->partials,
+                                                           ws->counter);
+            ws->launches++;
+            BELLA_CUDA(cudaGetLastError());
+            BELLA_CUDA(cudaMemcpyAsync(ws->ks_host, ws->ks, sizeof(KState), cudaMemcpyDeviceToHost, s));
+            BELLA_CUDA(cudaStreamSynchronize(s));
+            G[k * nm + l] = ws->ks_host->dot_aux;
+        }
+    // Gauss-Jordan inverse with partial pivoting (nm <= 8)
+    double A[MAXNULL][2 * MAXNULL];
+    for (int r = 0; r < nm; ++r)
+        for (int c = 0; c < 2 * nm; ++c) A[r][c] = c < nm ? G[r * nm + c] : (c - nm == r ? 1.0 : 0.0);
+    for (int c = 0; c < nm; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < nm; ++r) if (fabs(A[r][c]) > fabs(A[piv][c])) piv = r;
+        if (A[piv][c] == 0.0) return set_err(BELLA_EINVAL, "null-space Gram matrix is singular");
+        if (piv != c) for (int q = 0; q < 2 * nm; ++q) { double t = A[c][q]; A[c][q] = A[piv][q]; A[piv][q] = t; }
+        const double d = A[c][c];
+        for (int q = 0; q < 2 * nm; ++q) A[c][q] /= d;
+        for (int r = 0; r < nm; ++r) {
+            if (r == c) continue;
+            const double f = A[r][c];
+            if (f != 0.0) for (int q = 0; q < 2 * nm; ++q) A[r][q] -= f * A[c][q];
+        }
+    }
+    for (int r = 0; r < nm; ++r)
+        for (int c = 0; c < nm; ++c) ns.ginv[r * MAXNULL + c] = A[r][nm + c];
+    return BELLA_OK;
+}
+
+int bella_op2d_set(bella_ws *ws, const bella_op2d *op, void *stream) {
+    if (!ws || !op) return set_err(BELLA_EINVAL, "bella_op2d_set: null argument");
+    if (op->nx < 3 || op->ny < 3) return set_err(BELLA_EINVAL, "bella_op2d_set: nx, ny must be >= 3");
+    if (!op->hplusx || !op->hplusy || !op->cxx || !op->cyy || !op->diag_inv)
+        return set_err(BELLA_EINVAL, "bella_op2d_set: hplusx, hplusy, cxx, cyy, diag_inv are required");
+    if (!(op->dx > 0.0) || !(op->dy > 0.0)) return set_err(BELLA_EINVAL, "bella_op2d_set: dx, dy must be > 0");
+    BELLA_CUDA(cudaSetDevice(ws->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    const long long n = (long long)op->nx * op->ny;
+    const size_t ncell = (size_t)(op->nx + 1) * (op->ny + 1);
+    if (ws->ndim != 2 || ws->nx != op->nx || ws->ny != op->ny) {
+        free_op(ws);
+        BELLA_CUDA(cudaMalloc(&ws->a64, 4 * ncell * sizeof(double)));
+        BELLA_CUDA(cudaMalloc(&ws->a32, 4 * ncell * sizeof(float)));
+        BELLA_CUDA(cudaMalloc(&ws->dinv64, n * sizeof(double)));
+        BELLA_CUDA(cudaMalloc(&ws->hc64, n * sizeof(double)));
+        BELLA_CUDA(cudaMalloc(&ws->z64, n * sizeof(double)));
+        BELLA_CUDA(cudaMalloc(&ws->dinv32, n * sizeof(float)));
+        BELLA_CUDA(cudaMalloc(&ws->hc32, n * sizeof(float)));
+    }
+    int rc = ensure_vectors(ws, n);
+    if (rc != BELLA_OK) return rc;
+    ws->ndim = 2;
+    ws->nz = 1;
+    ws->nx = op->nx;
+    ws->ny = op->ny;
+    ws->n = n;
+    ws->cross = (op->cxy != nullptr || op->cyx != nullptr) ? 1 : 0;
+    ws->has_hc = op->hcenter != nullptr ? 1 : 0;
+    ws->singular = (!ws->has_hc && !ws->cross) ? 1 : 0;
+    ws->grid_stencil = stencil_grid(op->nx, op->ny);
+    ws->grid_vec = vec_grid(n);
+    rc = op2d_pack(ws, op, s);
+    if (rc != BELLA_OK) return cuda_check(cudaGetLastError(), "op2d_pack");
+    rc = setup_null_space(ws, s, op->x_wall ? 0 : 1, op->y_wall ? 0 : 1, 0);
+    if (rc != BELLA_OK) return rc;
+    return BELLA_OK;
+}
+
+int bella_apply_f64(bella_ws *ws, const double *x, double *y, void *stream) {
+    if (!ws || !x || !y) return set_err(BELLA_EINVAL, "bella_apply_f64: null argument");
+    if (ws->ndim == 0) return set_err(BELLA_ENOOP, "bella_apply_f64: no operator set");
+    op2d_apply(ws, 0, x, y, (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "bella_apply_f64");
+}
+
+int bella_apply_f32(bella_ws *ws, const float *x, float *y, void *stream) {
+    if (!ws || !x || !y) return set_err(BELLA_EINVAL, "bella_apply_f32: null argument");
+    if (ws->ndim == 0) return set_err(BELLA_ENOOP, "bella_apply_f32: no operator set");
+    op2d_apply(ws, 1, x, y, (cudaStream_t)stream);
+    return cuda_check(cudaGetLastError(), "bella_apply_f32");
+}
+
+void bella_solve_opts_default(bella_solve_opts *o) {
+    if (!o) return;
+    memset(o, 0, sizeof(*o));
+    o->tol = 1e-8;
+    o->atol = 0.0;
+    o->maxiter = 6000;
+    o->precision = 1;
+    o->x0_zero = 1;
+    o->project_null = 1;
+    o->inner_tol = 1e-5;
+    o->max_outer = 30;
+    o->check_every = 16;
+    o->timeout_s = 0.0;
+}
+
+static int sync_state(bella_ws *ws, cudaStream_t s) {
+    BELLA_CUDA(cudaMemcpyAsync(ws->ks_host, ws->ks, sizeof(KState), cudaMemcpyDeviceToHost, s));
+    BELLA_CUDA(cudaStreamSynchronize(s));
+    prof_harvest(ws);
+    return BELLA_OK;
+}
+
+int bella_ws_profile(bella_ws *ws, int enable) {
+    if (!ws) return set_err(BELLA_EINVAL, "bella_ws_profile: null workspace");
+    BELLA_CUDA(cudaSetDevice(ws->device));
+    if (enable && !ws->prof) {
+        for (int k = 0; k < 4; ++k)
+            for (int i = 0; i < 2 * 256; ++i) BELLA_CUDA(cudaEventCreate(&ws->profk[k].ev[i]));
+    }
+    if (!enable && ws->prof) {
+        prof_harvest(ws);
+        for (int k = 0; k < 4; ++k)
+            for (int i = 0; i < 2 * 256; ++i) cudaEventDestroy(ws->profk[k].ev[i]);
+    }
+    ws->prof = enable ? 1 : 0;
+    for (int k = 0; k < 4; ++k) { ws->profk[k].pending = 0; ws->profk[k].total_ms = 0.0; ws->profk[k].count = 0; }
+    return BELLA_OK;
+}
+
+int bella_ws_kernel_time(bella_ws *ws, int kind, double *total_ms, long long *count) {
+    if (!ws || kind < 0 || kind > 3 || !total_ms || !count)
+        return set_err(BELLA_EINVAL, "bella_ws_kernel_time: bad argument");
+    prof_harvest(ws);
+    *total_ms = ws->profk[kind].total_ms;
+    *count = ws->profk[kind].count;
+    return BELLA_OK;
+}
+
+// run BiCGStab iterations (precision prec) until the device state is done
+static int run_inner(bella_ws *ws, int prec, const bella_solve_opts *o, cudaStream_t s,
+                     std::chrono::steady_clock::time_point t0, int *timed_out) {
+    const int blk = o->check_every > 0 ? o->check_every : 16;
+    *timed_out = 0;
+    for (;;) {
+        int rc = sync_state(ws, s);
+        if (rc != BELLA_OK) return rc;
+        if (ws->ks_host->done) return BELLA_OK;
+        if (o->timeout_s > 0.0) {
+            const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (el > o->timeout_s) { *timed_out = 1; return BELLA_OK; }
+        }
+        for (int k = 0; k < blk; ++k) op2d_iteration(ws, prec, s);
+        BELLA_CUDA(cudaGetLastError());
+    }
+}
+
+int bella_bicgstab(bella_ws *ws, const double *b, double *x, const bella_solve_opts *opts,
+                   bella_solve_stats *stats, void *stream) {
+    if (!ws || !b || !x) return set_err(BELLA_EINVAL, "bella_bicgstab: null argument");
+    if (ws->ndim == 0) return set_err(BELLA_ENOOP, "bella_bicgstab: no operator set");
+    bella_solve_opts o;
+    if (opts) o = *opts; else bella_solve_opts_default(&o);
+    if (!(o.tol >= 0.0) || o.maxiter < 0) return set_err(BELLA_EINVAL, "bella_bicgstab: bad tol/maxiter");
+    BELLA_CUDA(cudaSetDevice(ws->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    const auto t0 = std::chrono::steady_clock::now();
+    bella_solve_stats st;
+    memset(&st, 0, sizeof(st));
+    const long long n = ws->n;
+    const int gv = ws->grid_vec;
+    int rc, timed_out = 0;
+
+    if (o.precision == 0) {
+        // ---- FP64 BiCGStab, scipy control flow, solution in place in x ----
+        double *xs = x;
+        if (!o.x0_zero) {
+            op2d_resid(ws, 0, x, b, ws->r64k, s);
+        }
+        k_init64<<<gv, VEC_BLOCK, 0, s>>>(n, b, xs, ws->r64k, ws->rh64, o.x0_zero ? 0 : 1, o.tol, o.atol,
+                                          o.maxiter, ws->ks, ws->partials, ws->counter);
+        ws->launches++;
+        BELLA_CUDA(cudaGetLastError());
+        // the fused update kernel writes ws->x64v: alias it to the caller's x
+        double *saved = ws->x64v;
+        ws->x64v = xs;
+        rc = run_inner(ws, 0, &o, s, t0, &timed_out);
+        ws->x64v = saved;
+        if (rc != BELLA_OK) return rc;
+        st.iterations = ws->ks_host->iter;
+        st.status = timed_out ? BELLA_TIMEOUT : ws->ks_host->status;
+        st.bnorm = ws->ks_host->dot_aux;
+        st.matvecs = 2 * st.iterations + (o.x0_zero ? 0 : 1);
+    } else {
+        // ---- FP32 BiCGStab inner solves in FP64 iterative refinement ----
+        k_dot64<<<gv, VEC_BLOCK, 0, s>>>(n, b, b, ws->ks, ws->partials, ws->counter);
+        ws->launches++;
+        rc = sync_state(ws, s);
+        if (rc != BELLA_OK) return rc;
+        const double bnorm = sqrt(ws->ks_host->dot_aux);
+        st.bnorm = bnorm;
+        double target = o.tol * bnorm;
+        if (o.atol > target) target = o.atol;
+        if (o.x0_zero) {
+            BELLA_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
+            if (bnorm == 0.0 || bnorm <= o.tol) {   // scipy 1.7 legacy exit
+                st.status = BELLA_OK;
+                st.relres = 0.0;
+                goto done;
+            }
+        }
+        {
+            NullSpace ns = ws->ns;
+            if (!o.project_null) ns.nm = 0;
+            const bool proj = ns.nm > 0;
+            op2d_resid(ws, 0, x, b, ws->r64, s);
+            rc = sync_state(ws, s);
+            if (rc != BELLA_OK) return rc;
+            double rnorm = sqrt(ws->ks_host->dot_aux2);
+            st.matvecs = 1;
+            st.status = BELLA_MAXITER;
+            int total = 0;
+            for (int outer = 0;; ++outer) {
+                if (!isfinite(rnorm)) { st.status = BELLA_NONFINITE; break; }
+                if (rnorm <= target) { st.status = BELLA_OK; break; }
+                if (total >= o.maxiter) { st.status = BELLA_MAXITER; break; }
+                if (outer >= o.max_outer) { st.status = BELLA_MAXITER; break; }
+                if (timed_out) { st.status = BELLA_TIMEOUT; break; }
+                double rel = o.inner_tol;
+                const double need = 0.5 * target / rnorm;
+                if (need > rel) rel = need;
+                k_init32<<<gv, VEC_BLOCK, 0, s>>>(n, ws->r64, 1.0 / rnorm, ws->r32, ws->rh32, ws->x32, rel,
+                                                  o.maxiter - total, ws->ks, ws->partials, ws->counter);
+                ws->launches++;
+                rc = run_inner(ws, 1, &o, s, t0, &timed_out);
+                if (rc != BELLA_OK) return rc;
+                const int it = ws->ks_host->iter;
+                const int inner_status = ws->ks_host->status;
+                total += it;
+                st.matvecs += 2 * it + 1;
+                k_ir_update<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->x32, rnorm, ws->z64, ns, ws->ks,
+                                                     ws->partials, ws->counter);
+                ws->launches++;
+                if (proj) {
+                    k_null_shift<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->ks, ns);
+                    ws->launches++;
+                }
+                op2d_resid(ws, 0, x, b, ws->r64, s);
+                rc = sync_state(ws, s);
+                if (rc != BELLA_OK) return rc;
+                const double rnew = sqrt(ws->ks_host->dot_aux2);
+                st.outer = outer + 1;
+                if (inner_status == BELLA_BREAKDOWN && !(rnew < rnorm)) { rnorm = rnew; st.status = BELLA_BREAKDOWN; break; }
+                if (inner_status == BELLA_NONFINITE) { rnorm = rnew; st.status = BELLA_NONFINITE; break; }
+                if (it == 0 && !(rnew < rnorm)) { rnorm = rnew; st.status = BELLA_BREAKDOWN; break; }
+                rnorm = rnew;
+            }
+            st.iterations = total;
+            st.relres = bnorm > 0 ? rnorm / bnorm : rnorm;
+        }
+    }
+done:
+    if (o.precision == 0) {
+        // true FP64 residual of the returned x
+        op2d_resid(ws, 0, x, b, ws->r64, s);
+        rc = sync_state(ws, s);
+        if (rc != BELLA_OK) return rc;
+        const double rn = sqrt(ws->ks_host->dot_aux2);
+        st.relres = st.bnorm > 0 ? rn / st.bnorm : rn;
+    }
+    BELLA_CUDA(cudaGetLastError());
+    st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (stats) *stats = st;
+    return BELLA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,119 @@
+"""Synthetic inputs of the standalone solve workloads, generated on the GPU.
+
+``stratified_2d`` builds the operands of one 2049x1025 9-point solve in the
+reference's packed layout (laplacian.py:517-527): a stably stratified
+background (Brunt-Vaisala N = 0.01 1/s, theta0 = 300 K, hydrostatic Exner
+pressure) gives the pseudo-incompressible coefficients of
+``operator_coefficients_nodes`` (second_projection.py:308-356) and the
+Coriolis/buoyancy factors of ``multiply_inverse_coriolis``
+(second_projection.py:604-652); every cell coefficient is multiplied by a
+seeded log-normal factor (sigma 0.1).  The right-hand side is a seeded
+zero-mean Gaussian random field with a k^-3 power spectrum, made compatible
+with the singular operator (no component along its null modes) and scaled by
+the Jacobi diagonal ``precon_diag_prepare`` (laplacian.py:1284-1356).
+
+These stand in for the reference's configuration; the reference ships no
+such input data.  Values are drawn with torch's CUDA generator, so they are
+reproducible per seed on a given torch build.
+"""
+import math
+
+import torch
+
+R_GAS, GAMM, T_REF, H_REF = 287.4, 1.4, 300.0, 10000.0
+
+
+def _consts(grav=9.81, t_ref=1000.0):
+    u_ref = H_REF / t_ref
+    Msq = u_ref * u_ref / (R_GAS * T_REF)
+    g = grav * H_REF / (R_GAS * T_REF)
+    return Msq, g
+
+
+def _profile(y, g, N=0.01, grav=9.81):
+    a = N * N * H_REF / grav
+    Gamma = (GAMM - 1.0) / GAMM
+    Y = torch.exp(a * y)
+    pi = 1.0 - Gamma * g * (1.0 - torch.exp(-a * y)) / a
+    P = pi ** (1.0 / (GAMM - 1.0))
+    return Y, P
+
+
+def _kminus3(shape, gen, device):
+    white = torch.randn(shape, generator=gen, device=device, dtype=torch.float64)
+    F = torch.fft.rfftn(white)
+    kx = torch.fft.fftfreq(shape[0], device=device, dtype=torch.float64) * shape[0]
+    ky = torch.fft.rfftfreq(shape[1], device=device, dtype=torch.float64) * shape[1]
+    K = torch.sqrt(kx[:, None] ** 2 + ky[None, :] ** 2)
+    amp = torch.where(K > 0, K.clamp_min(1e-30) ** -1.5, torch.zeros_like(K))
+    f = torch.fft.irfftn(F * amp, s=shape)
+    f = f - f.mean()
+    return f / f.std()
+
+
+def null_modes_2d(nx, ny, x_periodic, y_periodic, device):
+    """Constant and checkerboard null modes (shape (k, nx, ny)) and trapezoid weights."""
+    i = torch.arange(nx, device=device)[:, None]
+    j = torch.arange(ny, device=device)[None, :]
+    modes = [torch.ones(nx, ny, dtype=torch.float64, device=device)]
+    if not ((x_periodic and (nx - 1) % 2) or (y_periodic and (ny - 1) % 2)):
+        modes.append((1.0 - 2.0 * ((i + j) % 2)).to(torch.float64).expand(nx, ny).clone())
+    wx = torch.ones(nx, dtype=torch.float64, device=device)
+    wy = torch.ones(ny, dtype=torch.float64, device=device)
+    if x_periodic:
+        wx[0] = wx[-1] = 0.5
+    if y_periodic:
+        wy[0] = wy[-1] = 0.5
+    return torch.stack(modes), wx[:, None] * wy[None, :]
+
+
+def stratified_2d(seed, nx=2049, ny=1025, sigma=0.1, dt=0.01, device="cuda"):
+    """Operands of one pseudo-incompressible 9-point solve (flat, reference packing)."""
+    dev = torch.device(device)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(int(seed))
+    Msq, g = _consts()
+    dx = 2.0 / (nx - 1)
+    dy = 1.0 / (ny - 1)
+    ecx, ecy = nx + 3, ny + 3
+    ey = -2 * dy + 0.5 * dy + dy * torch.arange(ecy, device=dev, dtype=torch.float64)
+    ny_ = -2 * dy + dy * torch.arange(ny + 4, device=dev, dtype=torch.float64)
+    Yc, Pc = _profile(ey, g)
+    Yn, _ = _profile(ny_, g)
+    Gammainv = GAMM / (GAMM - 1.0)
+    coeff = (Gammainv * Pc * Yc)[None, :].expand(ecx, ecy)
+    fac = torch.exp(sigma * torch.randn(ecx, ecy, generator=gen, device=dev, dtype=torch.float64))
+    fac[:2] = fac[-4:-2].clone()
+    fac[-2:] = fac[2:4].clone()
+    wplus = coeff * fac                                     # (ecx, ecy), both directions
+    S0 = 1.0 / Yn
+    dSdy = (S0[1:] - S0[:-1]) / dy                          # cell rows
+    nu = -dt * dt * (g / Msq) * dSdy * Yc                   # (ecy,)
+    cxx = torch.ones(ecy, ecx, dtype=torch.float64, device=dev)
+    cyy = (1.0 / (nu + 1.0))[:, None].expand(ecy, ecx)
+    box = wplus[:-1, :-1] + wplus[1:, :-1] + wplus[:-1, 1:] + wplus[1:, 1:]
+    c = 0.75
+    diag = -(c / dx ** 2) * box - (c / dy ** 2) * box - (c / (dx * dy)) * box - (c / (dy * dx)) * box
+    diag_inv = 1.0 / diag                                    # node.isc (nx+2, ny+2)
+    s = (slice(1, -1), slice(1, -1))
+    hplus = wplus[s].T.contiguous().reshape(-1)
+    dinv = diag_inv[s].T.contiguous().reshape(-1)
+    f = _kminus3((nx - 1, 2 * (ny - 1)), gen, dev)[:, :ny]
+    b = torch.cat([f, f[:1]], dim=0)                        # seam column duplicated
+    E, w = null_modes_2d(nx, ny, True, False, dev)
+    G = torch.stack([torch.stack([(w * ek * el).sum() for el in E]) for ek in E])
+    r = torch.stack([(w * ek * b).sum() for ek in E])
+    cf = torch.linalg.solve(G, r)
+    b = b - torch.tensordot(cf, E, dims=1)
+    b_flat = b.T.contiguous().reshape(-1)
+    return dict(hplusx=hplus, hplusy=hplus.clone(), hcenter=None,
+                cor=(cxx[s].contiguous().reshape(-1), cyy[s].contiguous().reshape(-1), None, None),
+                diag_inv=dinv, b=b_flat * dinv, nx=nx, ny=ny, dx=dx, dy=dy, x_wall=False, y_wall=True,
+                seed=int(seed))
+
+
+def operator_bytes_2d(w):
+    """Host<->device bytes of the operands of one solve (FP64)."""
+    n = w["nx"] * w["ny"]
+    nc = (w["nx"] + 1) * (w["ny"] + 1)
+    return 8 * (4 * nc + 2 * n)

@@ -1,0 +1,215 @@
+"""Generate the golden fixtures under tests/golden/ from the pyBELLA reference.
+
+Run in a container where the reference is checked out (it is not needed at
+test time; the fixtures are committed):
+
+    python tests/golden/make_golden.py /path/to/pyBELLA
+
+It imports the reference through ``refshim`` (numba, h5py, ... stubbed; SciPy
+``tol=`` keyword restored) and records:
+
+* ``lap2d_kat.npz``   -- ``lap2D_gather_new`` (laplacian.py:546-746) on random
+  operands for three grids / boundary combinations, incl. Coriolis cross terms;
+* ``diag_kat.npz``    -- ``precon_diag_prepare`` (laplacian.py:1284-1356);
+* ``pieces_kat.npz``  -- ``divergence_nodes``, ``correction_nodes``,
+  ``set_ghostnodes_p2`` and ``set_explicit_boundary_data`` on a random state;
+* ``rising_bubble_step0.npz`` -- inputs and outputs of the two non-trivial
+  ``euler_backward_non_advective_impl_part`` calls of the first rising-bubble
+  time step (160x80 cells, pseudo-incompressible, tol 1e-10): the full-step
+  call (no ``Sol0``) and the next half-step call (with ``Sol0``).
+"""
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import refshim  # noqa: E402
+
+FIELDS = ["rho", "rhou", "rhov", "rhow", "rhoY", "rhoX"]
+
+
+def _ud_rising_bubble():
+    import utils.user_data as user_data
+    import inputs.rising_bubble as rb
+    ud = user_data.UserDataInit()
+    for k, v in vars(rb.UserData()).items():
+        setattr(ud, k, v)
+    ud.is_compressible = 0
+    ud.compressibility = 0.0
+    ud.tol = 1e-10
+    ud.coriolis_strength = np.array(ud.coriolis_strength)
+    return ud
+
+
+def lap2d_kat(out):
+    import dycore.physics.low_mach.laplacian as lm_lp
+    rng = np.random.default_rng(1234)
+    cases = [(9, 7, False, True), (12, 10, False, False), (10, 8, True, True)]
+    rec = {}
+    for ci, (nx, ny, x_wall, y_wall) in enumerate(cases):
+        nc = (nx + 1) * (ny + 1)
+        hx = rng.uniform(0.5, 2.0, nc)
+        hy = rng.uniform(0.5, 2.0, nc)
+        hc = rng.uniform(-1.0, 0.0, nx * ny)
+        cor = tuple(rng.uniform(-0.5, 1.5, nc) for _ in range(4))
+        dinv = rng.uniform(-2.0, -0.5, nx * ny)
+        p = rng.standard_normal(nx * ny)
+        dx, dy = 0.1 + 0.05 * ci, 0.07 + 0.02 * ci
+        y = lm_lp.lap2D_gather_new(p.copy(), nx, ny, (hx, hy, hc), dx, dy, False, x_wall, y_wall,
+                                   dinv, cor)
+        for k, v in dict(hx=hx, hy=hy, hc=hc, cxx=cor[0], cyy=cor[1], cxy=cor[2], cyx=cor[3],
+                         dinv=dinv, p=p, y=y,
+                         meta=np.array([nx, ny, int(x_wall), int(y_wall), dx, dy])).items():
+            rec["c%d_%s" % (ci, k)] = v
+    np.savez_compressed(os.path.join(out, "lap2d_kat.npz"), **rec)
+
+
+def diag_kat(out):
+    import dycore.physics.low_mach.laplacian as lm_lp
+    import dycore.utils.options as opts
+    rng = np.random.default_rng(99)
+    nx, ny = 15, 9
+    wplus = rng.uniform(0.5, 2.0, (2, nx + 3, ny + 3))
+    wcenter = rng.uniform(-1.0, 0.0, (nx + 2, ny + 2))
+    mpv = types.SimpleNamespace(wplus=wplus, wcenter=wcenter)
+    node = types.SimpleNamespace(dx=0.1, dy=0.07, dz=1.0, igs=[2, 2, 0])
+    elem = types.SimpleNamespace(ndim=2)
+    ud = types.SimpleNamespace(bdry_type=[opts.BdryType.PERIODIC, opts.BdryType.WALL, opts.BdryType.WALL])
+    d = lm_lp.precon_diag_prepare(mpv, elem, node, ud, None)
+    np.savez_compressed(os.path.join(out, "diag_kat.npz"), wplus=wplus, wcenter=wcenter, diag_inv=d,
+                        meta=np.array([0.1, 0.07]))
+
+
+def _rb_setup():
+    import dycore.discretisation.grid as dis_grid
+    import dycore.utils.variable as var
+    import dycore.physics.low_mach.mpv as lm_var
+    import dycore.physics.gas_dynamics.thermodynamic as gd_thermodynamics
+    import inputs.rising_bubble as rb
+    ud = _ud_rising_bubble()
+    elem, node = dis_grid.grid_init(ud)
+    Sol = var.Vars(elem.sc, ud)
+    th = gd_thermodynamics.init(ud)
+    mpv = lm_var.MPV(elem, node, ud)
+    Sol = rb.sol_init(Sol, mpv, elem, node, th, ud)
+    ud.nonhydrostasy = 1.0
+    return ud, elem, node, Sol, th, mpv
+
+
+def pieces_kat(out):
+    """Reference helpers on a random perturbation of a small rising-bubble state."""
+    import dycore.discretisation.grid as dis_grid
+    import dycore.utils.variable as var
+    import dycore.physics.low_mach.mpv as lm_var
+    import dycore.physics.gas_dynamics.thermodynamic as gd_thermodynamics
+    import dycore.physics.low_mach.second_projection as lm_sp
+    import dycore.utils.boundary as bdry
+    import inputs.rising_bubble as rb
+    rng = np.random.default_rng(7)
+    ud = _ud_rising_bubble()
+    ud.inx, ud.iny = 17, 11
+    elem, node = dis_grid.grid_init(ud)
+    Sol = var.Vars(elem.sc, ud)
+    th = gd_thermodynamics.init(ud)
+    mpv = lm_var.MPV(elem, node, ud)
+    Sol = rb.sol_init(Sol, mpv, elem, node, th, ud)
+    ud.nonhydrostasy = 1.0
+    for k in ("rhou", "rhov", "rhoX"):
+        setattr(Sol, k, 0.01 * rng.standard_normal(elem.sc[:2]))
+    Sol.rho = Sol.rho * (1.0 + 0.01 * rng.standard_normal(elem.sc[:2]))
+    rec = {("in_" + k): np.copy(getattr(Sol, k)) for k in FIELDS}
+    p = rng.standard_normal(node.sc[:2])
+    rec["p"] = np.copy(p)
+    dt = 0.01
+    # set_explicit_boundary_data
+    bdry.set_explicit_boundary_data(Sol, elem, ud, th, mpv)
+    for k in FIELDS:
+        rec["bd_" + k] = np.copy(getattr(Sol, k))
+    # divergence_nodes (mutates ghost rows of the momenta)
+    rhs = np.zeros(node.isc[:2])
+    rhs = lm_sp.divergence_nodes(rhs, elem, node, Sol, ud)
+    rec["div"] = np.copy(rhs)
+    for k in FIELDS:
+        rec["dv_" + k] = np.copy(getattr(Sol, k))
+    # correction_nodes with updt_chi = 1
+    lm_sp.correction_nodes(Sol, elem, node, mpv, p, dt, ud, th, 1)
+    for k in FIELDS:
+        rec["cr_" + k] = np.copy(getattr(Sol, k))
+    # ghost nodes, periodic x / wall y and wall x / periodic y
+    q = np.copy(p)
+    bdry.set_ghostnodes_p2(q, node, ud)
+    rec["gn_pw"] = q
+    import dycore.utils.options as opts
+    ud2 = types.SimpleNamespace(bdry_type=[opts.BdryType.WALL, opts.BdryType.PERIODIC, opts.BdryType.WALL])
+    q2 = np.copy(p)
+    bdry.set_ghostnodes_p2(q2, node, ud2)
+    rec["gn_wp"] = q2
+    rec["meta"] = np.array([ud.inx, ud.iny, dt])
+    np.savez_compressed(os.path.join(out, "pieces_kat.npz"), **rec)
+
+
+def rising_bubble_step0(out):
+    import dycore.discretisation.time_update as dis_time_update
+    import dycore.physics.low_mach.second_projection as lm_sp
+    import dycore.utils.variable as var
+    from data_assimilation import blending as da_blending
+    ud, elem, node, Sol, th, mpv = _rb_setup()
+    flux = np.empty((3), dtype=object)
+    flux[0] = var.States(elem.sfx, ud)
+    flux[1] = var.States(elem.sfy, ud)
+    bld = da_blending.Blend(ud)
+    calls = []
+    orig = lm_sp.euler_backward_non_advective_impl_part
+
+    def wrapped(Sol, mpv, elem, node, ud, th, t, dt, alpha_diff, Sol0=None, writer=None,
+                label=None, debug=False):
+        rec = dict(dt=dt, sol_in={k: np.copy(getattr(Sol, k)) for k in FIELDS},
+                   sol0_in=None if Sol0 is None else {k: np.copy(getattr(Sol0, k)) for k in FIELDS},
+                   p2_in=np.copy(mpv.p2_nodes))
+        n0 = lm_sp.total_iter
+        orig(Sol, mpv, elem, node, ud, th, t, dt, alpha_diff, Sol0=Sol0, writer=writer, label=label,
+             debug=debug)
+        rec["niter"] = lm_sp.total_iter - n0
+        rec["sol_out"] = {k: np.copy(getattr(Sol, k)) for k in FIELDS}
+        rec["p2_out"] = np.copy(mpv.p2_nodes)
+        rec["rhs"] = np.copy(mpv.rhs)
+        calls.append(rec)
+        print("impl_part call %d: dt=%g niter=%d" % (len(calls), dt, rec["niter"]), flush=True)
+
+    lm_sp.euler_backward_non_advective_impl_part = wrapped
+    dis_time_update.do(Sol, flux, mpv, 0.0, ud.tout[0], ud, elem, node, [0, 0], th, bld, None, False)
+    rec = {}
+    for tag, ci in (("full", 1), ("half", 2)):
+        c = calls[ci]
+        rec[tag + "_dt"] = np.array(c["dt"])
+        rec[tag + "_niter"] = np.array(c["niter"])
+        rec[tag + "_p2_in"] = c["p2_in"]
+        rec[tag + "_p2_out"] = c["p2_out"]
+        rec[tag + "_rhs"] = c["rhs"]
+        for k in FIELDS:
+            rec[tag + "_in_" + k] = c["sol_in"][k]
+            rec[tag + "_out_" + k] = c["sol_out"][k]
+            if c["sol0_in"] is not None:
+                rec[tag + "_sol0_" + k] = c["sol0_in"][k]
+    rec["hydro_n_S0"] = np.copy(mpv.HydroState_n.S0)
+    rec["hydro_c_rhoY0"] = np.copy(mpv.HydroState.rhoY0)
+    rec["scalars"] = np.array([ud.Msq, ud.gravity_strength[1], th.gamm])
+    np.savez_compressed(os.path.join(out, "rising_bubble_step0.npz"), **rec)
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    refshim.install(ref)
+    out = HERE
+    lap2d_kat(out)
+    diag_kat(out)
+    pieces_kat(out)
+    rising_bubble_step0(out)
+    print("fixtures written to", out)
+
+
+if __name__ == "__main__":
+    main()

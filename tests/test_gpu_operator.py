@@ -1,0 +1,89 @@
+"""GPU parity of the 2D nodal operator (libbella_gb300) against the oracle / reference."""
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle import cases, nodal2d as n2
+
+pytestmark = pytest.mark.gpu
+
+
+def _op_from_pack(op, device=0):
+    from pybella_gb300.linalg import NodalHelmholtz2D
+    return NodalHelmholtz2D(op["hplusx"], op["hplusy"], op["hcenter"], op["cor"], op["diag_inv"],
+                            op["nx"], op["ny"], op["dx"], op["dy"], op["x_wall"], op["y_wall"], device=device)
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def test_apply_f64_matches_reference_kat():
+    d = np.load(golden("lap2d_kat.npz"))
+    for c in range(3):
+        g = lambda k: d["c%d_%s" % (c, k)]
+        nx, ny, xw, yw, dx, dy = g("meta")
+        op = dict(hplusx=g("hx"), hplusy=g("hy"), hcenter=g("hc"),
+                  cor=(g("cxx"), g("cyy"), g("cxy"), g("cyx")), diag_inv=g("dinv"),
+                  nx=int(nx), ny=int(ny), dx=dx, dy=dy, x_wall=bool(xw), y_wall=bool(yw))
+        A = _op_from_pack(op)
+        y = A.matvec(g("p"))
+        assert _rel(y, g("y")) < 1e-13, c
+
+
+def _rb_operator():
+    d = np.load(golden("rising_bubble_step0.npz"))
+    grid, prm, _, _, hn, hc, sf = cases.rising_bubble()
+    fields = ["rho", "rhou", "rhov", "rhow", "rhoY", "rhoX"]
+    Sol = {k: d["full_in_" + k].copy() for k in fields}
+    p2 = d["full_p2_in"].copy()
+    captured = {}
+
+    def solver(op, b, tol, maxiter):
+        captured["op"], captured["b"] = op, b
+        from oracle.krylov import bicgstab_legacy
+        return bicgstab_legacy(op, b, tol, maxiter)
+
+    n2.impl_part(Sol, p2, hn["S0"], hc, sf, grid, prm, float(d["full_dt"]), solver=solver)
+    return captured["op"], captured["b"], grid
+
+
+def test_apply_rising_bubble_operator_f64_f32():
+    import torch
+    op, b, grid = _rb_operator()
+    A = _op_from_pack(op)
+    rng = np.random.default_rng(0)
+    p = rng.standard_normal(op["nx"] * op["ny"])
+    ref = n2.lap2d_gather(p, op)
+    assert _rel(A.matvec(p), ref) < 1e-13
+    y32 = A.matvec_f32(torch.tensor(p, dtype=torch.float32, device="cuda")).double().cpu().numpy()
+    assert _rel(y32, ref) < 2e-6
+
+
+def test_apply_full_size_stratified():
+    w = cases.stratified_2d(seed=1)
+    A = _op_from_pack(w["op"])
+    rng = np.random.default_rng(1)
+    p = rng.standard_normal(A.n)
+    assert _rel(A.matvec(p), n2.lap2d_gather(p, w["op"])) < 1e-13
+
+
+def test_null_modes_exact_on_device():
+    import torch
+    w = cases.stratified_2d(seed=2, inx=129, iny=65)
+    A = _op_from_pack(w["op"])
+    for e in cases.null_modes_2d(w["grid"]):
+        v = e.T.reshape(-1)
+        assert np.abs(A.matvec(v)).max() == 0.0
+        y32 = A.matvec_f32(torch.tensor(v, dtype=torch.float32, device="cuda"))
+        assert float(y32.abs().max()) == 0.0
+
+
+def test_seam_consistency_preserved():
+    w = cases.stratified_2d(seed=3, inx=129, iny=65)
+    A = _op_from_pack(w["op"])
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal((w["grid"].iny, w["grid"].inx))
+    x[:, -1] = x[:, 0]
+    y = A.matvec(x.reshape(-1)).reshape(x.shape)
+    np.testing.assert_array_equal(y[:, 0], y[:, -1])

@@ -1,0 +1,123 @@
+"""Pin the CPU oracle against the reference's own outputs (committed fixtures).
+
+The fixtures were produced by importing the pyBELLA reference
+(tests/golden/make_golden.py).  The oracle restates the reference's FP64
+arithmetic in the same operation order, so most comparisons are exact.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle import cases, nodal2d as n2
+from oracle.krylov import bicgstab_legacy, true_relres
+
+FIELDS = ["rho", "rhou", "rhov", "rhow", "rhoY", "rhoX"]
+
+
+def test_lap2d_matches_reference_kat():
+    d = np.load(golden("lap2d_kat.npz"))
+    for c in range(3):
+        g = lambda k: d["c%d_%s" % (c, k)]
+        nx, ny, xw, yw, dx, dy = g("meta")
+        op = dict(hplusx=g("hx"), hplusy=g("hy"), hcenter=g("hc"),
+                  cor=(g("cxx"), g("cyy"), g("cxy"), g("cyx")), diag_inv=g("dinv"),
+                  nx=int(nx), ny=int(ny), dx=dx, dy=dy, x_wall=bool(xw), y_wall=bool(yw))
+        y = n2.lap2d_gather(g("p"), op)
+        np.testing.assert_array_equal(y, g("y"))
+
+
+def test_precon_diag_matches_reference_kat():
+    d = np.load(golden("diag_kat.npz"))
+    dx, dy = d["meta"]
+    out = n2.precon_diag_prepare(d["wplus"], d["wcenter"], dx, dy)
+    np.testing.assert_array_equal(out, d["diag_inv"])
+
+
+def _small_rb_state():
+    d = np.load(golden("pieces_kat.npz"))
+    inx, iny, dt = d["meta"]
+    grid, prm, Sol, p2, hn, hc, sf = cases.rising_bubble(inx=int(inx), iny=int(iny))
+    return d, grid, prm, hn, hc, sf, dt
+
+
+def test_projection_pieces_match_reference_kat():
+    d, grid, prm, hn, hc, sf, dt = _small_rb_state()
+    Sol = {k: d["in_" + k].copy() for k in FIELDS}
+    n2.set_explicit_boundary_data(Sol, grid, prm, hc, sf)
+    for k in FIELDS:
+        np.testing.assert_array_equal(Sol[k], d["bd_" + k], err_msg="boundary " + k)
+    div = n2.divergence_nodes(Sol, grid)
+    np.testing.assert_array_equal(div, d["div"])
+    for k in FIELDS:
+        np.testing.assert_array_equal(Sol[k], d["dv_" + k], err_msg="divergence side effect " + k)
+    n2.correction_nodes(Sol, d["p"], hn["S0"], grid, prm, dt, 1)
+    for k in FIELDS:
+        np.testing.assert_allclose(Sol[k], d["cr_" + k], rtol=0, atol=1e-15, err_msg="correction " + k)
+    q = d["p"].copy()
+    n2.set_ghostnodes_p2(q, grid)
+    np.testing.assert_array_equal(q, d["gn_pw"])
+    g2 = n2.Grid2D(grid.inx, grid.iny, -1.0, 1.0, 0.0, 1.0, (n2.WALL, n2.PERIODIC))
+    q2 = d["p"].copy()
+    n2.set_ghostnodes_p2(q2, g2)
+    np.testing.assert_array_equal(q2, d["gn_wp"])
+
+
+def test_rising_bubble_background_matches_reference():
+    d = np.load(golden("rising_bubble_step0.npz"))
+    grid, prm, Sol, p2, hn, hc, sf = cases.rising_bubble()
+    np.testing.assert_array_equal(hn["S0"], d["hydro_n_S0"])
+    np.testing.assert_array_equal(hc["rhoY0"], d["hydro_c_rhoY0"])
+    Msq, g, gamm = d["scalars"]
+    assert prm.Msq == Msq and prm.g == g and prm.gamm == gamm
+
+
+@pytest.mark.parametrize("tag", ["full", "half"])
+def test_impl_part_matches_reference_rising_bubble(tag):
+    d = np.load(golden("rising_bubble_step0.npz"))
+    grid, prm, _, _, hn, hc, sf = cases.rising_bubble()
+    Sol = {k: d["%s_in_%s" % (tag, k)].copy() for k in FIELDS}
+    Sol0 = None
+    if ("%s_sol0_rho" % tag) in d:
+        Sol0 = {k: d["%s_sol0_%s" % (tag, k)].copy() for k in FIELDS}
+    p2 = d[tag + "_p2_in"].copy()
+    out = n2.impl_part(Sol, p2, hn["S0"], hc, sf, grid, prm, float(d[tag + "_dt"]), Sol0=Sol0)
+    assert out["niter"] == int(d[tag + "_niter"])
+    np.testing.assert_array_equal(out["rhs"], d[tag + "_rhs"])
+    np.testing.assert_array_equal(p2, d[tag + "_p2_out"])
+    for k in FIELDS:
+        np.testing.assert_array_equal(Sol[k], d["%s_out_%s" % (tag, k)], err_msg=k)
+    assert true_relres(out["op"], out["x"], out["rhs_inner"]) <= prm.tol
+
+
+def test_oracle_operator_left_null_vector():
+    """Seam-consistent vectors: the trapezoid weights annihilate the range.
+
+    For x with equal values on the duplicated periodic seam, the pseudo-
+    incompressible operator's output satisfies <w, D A x> = 0 with w the
+    trapezoid weights (1/2 on the seam columns) and D = 1/diag_inv.
+    """
+    rng = np.random.default_rng(3)
+    grid = n2.Grid2D(33, 17, -1.0, 1.0, 0.0, 1.0, (n2.PERIODIC, n2.WALL))
+    cells = rng.uniform(0.5, 2.0, grid.elem_sc)
+    cells[:2] = cells[-4:-2]
+    cells[-2:] = cells[2:4]
+    wplus = np.stack([cells, cells])
+    wcenter = np.zeros(grid.node_isc)
+    cor = tuple(np.broadcast_to(v, grid.elem_sc).T.copy() for v in (1.0, 0.9, 0.0, 0.0))
+    dinv = n2.precon_diag_prepare(wplus, wcenter, grid.dx, grid.dy)
+    op = n2.pack_9pt(wplus, wcenter, cor, dinv, grid)
+    x = rng.standard_normal((grid.iny, grid.inx))
+    x[:, -1] = x[:, 0]
+    y = n2.lap2d_gather(x.reshape(-1), op)
+    w = cases.null_weights_2d(grid).T.reshape(-1) / op["diag_inv"]
+    assert abs(np.dot(w, y)) < 1e-10 * np.abs(w * y).sum()
+    # constants are in the null space
+    assert np.abs(n2.lap2d_gather(np.ones(grid.inx * grid.iny), op)).max() < 1e-9
+
+
+def test_stratified_rhs_is_consistent():
+    """The synthetic 2049x1025-type RHS is compatible (small grid for speed)."""
+    w = cases.stratified_2d(seed=0, inx=65, iny=33)
+    x, info, it = bicgstab_legacy(w["op"], w["b"], 1e-8, 5000)
+    assert info == 0
+    assert true_relres(w["op"], x, w["b"]) <= 1e-8
