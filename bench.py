@@ -2,11 +2,11 @@
 
 One step = one projection solve of one seeded synthetic system: the
 reference-packed operands are turned into device flux planes
-(bella_op2d_set) and solved with the mixed-precision BiCGStab (FP32 stencil
-and vector updates, FP64 inner products / iterative-refinement residual /
-accumulated solution) to a true relative residual of 1e-8.  Seeds cycle over
-up to 64 pre-generated systems resident in HBM; the L2 is flushed (256 MB
-write) before every step.
+(bella_op2d_set) and solved by BiCGStab on the GPU (``--precision fp64``,
+the default: the reference algorithm in FP64; ``mixed``: FP32 inner solves
+in FP64 refinement with FP64 fallback) to a true relative residual of 1e-8.
+Seeds cycle over up to 64 pre-generated systems resident in HBM; the L2 is
+flushed (256 MB write) before every step.
 
     python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 
@@ -44,7 +44,11 @@ def _args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--seeds", type=int, default=64)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--nx", type=int, default=NX)
+    ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     return ap.parse_args()
 
@@ -204,6 +208,8 @@ def run_reference(args):
 # GPU side
 # --------------------------------------------------------------------------
 def run_gpu(args):
+    global NX, NY
+    NX, NY = args.nx, args.ny
     import torch
     from pybella_gb300 import linalg, workloads, _lib
 
@@ -226,7 +232,7 @@ def run_gpu(args):
         flush.fill_(float(i))
         A = linalg.NodalHelmholtz2D(w["hplusx"], w["hplusy"], w["hcenter"], w["cor"], w["diag_inv"],
                                     NX, NY, w["dx"], w["dy"], w["x_wall"], w["y_wall"], ws=ws)
-        x, st = A.solve(w["b"], tol=TOL, maxiter=MAXIT, precision="mixed", out=xbuf)
+        x, st = A.solve(w["b"], tol=TOL, maxiter=MAXIT, precision=args.precision, out=xbuf)
         stats.append(st)
 
     warm = []
@@ -270,18 +276,18 @@ def run_gpu(args):
     value = total_solves / (ms / 1000.0)
 
     # ---- end to end through the drop-in API with host buffers ----
-    host = [_to_np(systems[i % nseeds]) for i in range(min(nseeds, 4))]
+    host = [] if args.no_e2e else [_to_np(systems[i % nseeds]) for i in range(min(nseeds, 4))]
     e2e_stats = []
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
     te0 = time.perf_counter()
-    for i in range(args.steps):
+    for i in range(args.steps if host else 0):
         h = host[i % len(host)]
         A = linalg.NodalHelmholtz2D(h["hplusx"], h["hplusy"], h["hcenter"], h["cor"], h["diag_inv"],
                                     NX, NY, h["dx"], h["dy"], h["x_wall"], h["y_wall"], ws=ws)
         x, info = linalg.bicgstab(linalg.LinearOperator(A.shape, A), h["b"], tol=TOL, maxiter=MAXIT,
-                                  precision="mixed")
+                                  precision=args.precision)
         e2e_stats.append(info)
     torch.cuda.synchronize()
     te = time.perf_counter() - te0
@@ -289,7 +295,7 @@ def run_gpu(args):
         t = torch.tensor([te], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         te = float(t.item())
-    e2e_value = total_solves / te
+    e2e_value = total_solves / te if host else None
     nnode = NX * NY
     ncell = (NX + 1) * (NY + 1)
     h2d = 8 * (4 * ncell + 2 * nnode) + 8 * nnode   # hplusx, hplusy, cxx, cyy, diag_inv, hcenter, b
@@ -310,9 +316,9 @@ def run_gpu(args):
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "rtol": TOL, "precision": "mixed",
+        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "rtol": TOL, "precision": args.precision,
                    "l2": "flushed (256 MB write) before every step", "seeds": nseeds,
                    "parallelism": "replicas" if world > 1 else "single"},
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d,

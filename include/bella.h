@@ -64,7 +64,8 @@ typedef struct bella_solve_opts {
     double tol;              /* relative tolerance on ||b - A x||            */
     double atol;             /* absolute floor (0 = none)                    */
     int    maxiter;          /* inner BiCGStab iteration limit (total)       */
-    int    precision;        /* 0: FP64 BiCGStab;  1: FP32 inner + FP64 IR   */
+    int    precision;        /* 0: FP64 BiCGStab;  1: FP32 inner solves in FP64
+                                iterative refinement, FP64 fallback           */
     int    x0_zero;          /* 1: start from x = 0 (x is output only)       */
     int    project_null;     /* 1: keep x orthogonal to the left null vector
                                 (pseudo-incompressible operator)           */
@@ -82,6 +83,10 @@ typedef struct bella_solve_stats {
     double relres;           /* final FP64 ||b - A x|| / ||b||               */
     double bnorm;            /* ||b||                                        */
     double seconds;          /* host wall time of the call                   */
+    int    fallback;         /* 1: the FP32 inner solves failed (non-finite,
+                                breakdown or no progress) and the solve was
+                                finished by FP64 BiCGStab from the FP64 iterate */
+    int    pad_;
 } bella_solve_stats;
 
 /* ---- workspace --------------------------------------------------------- */
@@ -109,7 +114,9 @@ int bella_apply_f64(bella_ws *ws, const double *x, double *y, void *stream);
 int bella_apply_f32(bella_ws *ws, const float *x, float *y, void *stream);
 
 /* ---- solver (replaces scipy.sparse.linalg.bicgstab at
- *      second_projection.py:230) ---------------------------------------- */
+ *      second_projection.py:230) ----------------------------------------
+ * Returns the solver status (BELLA_OK, BELLA_MAXITER, BELLA_BREAKDOWN,
+ * BELLA_NONFINITE, BELLA_TIMEOUT; also in stats->status) or a negative error. */
 void bella_solve_opts_default(bella_solve_opts *o);
 int  bella_bicgstab(bella_ws *ws, const double *b, double *x,
                     const bella_solve_opts *opts, bella_solve_stats *stats,

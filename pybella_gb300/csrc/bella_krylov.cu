@@ -536,6 +536,30 @@ static int run_inner(bella_ws *ws, int prec, const bella_solve_opts *o, cudaStre
     }
 }
 
+// FP64 BiCGStab with scipy's control flow; x is the solution in place.
+// x_given = 0 starts from x = 0.  Fills iterations/status/bnorm/matvecs.
+static int solve_fp64(bella_ws *ws, const double *b, double *x, const bella_solve_opts &o, int x_given,
+                      int maxiter, bella_solve_stats *st, cudaStream_t s,
+                      std::chrono::steady_clock::time_point t0) {
+    const long long n = ws->n;
+    int timed_out = 0;
+    if (x_given) op2d_resid(ws, 0, x, b, ws->r64k, s);
+    k_init64<<<ws->grid_vec, VEC_BLOCK, 0, s>>>(n, b, x, ws->r64k, ws->rh64, x_given, o.tol, o.atol, maxiter,
+                                                ws->ks, ws->partials, ws->counter);
+    ws->launches++;
+    BELLA_CUDA(cudaGetLastError());
+    double *saved = ws->x64v;            // the update kernel writes ws->x64v
+    ws->x64v = x;
+    int rc = run_inner(ws, 0, &o, s, t0, &timed_out);
+    ws->x64v = saved;
+    if (rc != BELLA_OK) return rc;
+    st->iterations += ws->ks_host->iter;
+    st->status = timed_out ? BELLA_TIMEOUT : ws->ks_host->status;
+    st->bnorm = ws->ks_host->dot_aux;
+    st->matvecs += 2 * ws->ks_host->iter + (x_given ? 1 : 0);
+    return BELLA_OK;
+}
+
 int bella_bicgstab(bella_ws *ws, const double *b, double *x, const bella_solve_opts *opts,
                    bella_solve_stats *stats, void *stream) {
     if (!ws || !b || !x) return set_err(BELLA_EINVAL, "bella_bicgstab: null argument");
@@ -553,25 +577,8 @@ int bella_bicgstab(bella_ws *ws, const double *b, double *x, const bella_solve_o
     int rc, timed_out = 0;
 
     if (o.precision == 0) {
-        // ---- FP64 BiCGStab, scipy control flow, solution in place in x ----
-        double *xs = x;
-        if (!o.x0_zero) {
-            op2d_resid(ws, 0, x, b, ws->r64k, s);
-        }
-        k_init64<<<gv, VEC_BLOCK, 0, s>>>(n, b, xs, ws->r64k, ws->rh64, o.x0_zero ? 0 : 1, o.tol, o.atol,
-                                          o.maxiter, ws->ks, ws->partials, ws->counter);
-        ws->launches++;
-        BELLA_CUDA(cudaGetLastError());
-        // the fused update kernel writes ws->x64v: alias it to the caller's x
-        double *saved = ws->x64v;
-        ws->x64v = xs;
-        rc = run_inner(ws, 0, &o, s, t0, &timed_out);
-        ws->x64v = saved;
+        rc = solve_fp64(ws, b, x, o, o.x0_zero ? 0 : 1, o.maxiter, &st, s, t0);
         if (rc != BELLA_OK) return rc;
-        st.iterations = ws->ks_host->iter;
-        st.status = timed_out ? BELLA_TIMEOUT : ws->ks_host->status;
-        st.bnorm = ws->ks_host->dot_aux;
-        st.matvecs = 2 * st.iterations + (o.x0_zero ? 0 : 1);
     } else {
         // ---- FP32 BiCGStab inner solves in FP64 iterative refinement ----
         k_dot64<<<gv, VEC_BLOCK, 0, s>>>(n, b, b, ws->ks, ws->partials, ws->counter);
@@ -582,11 +589,11 @@ int bella_bicgstab(bella_ws *ws, const double *b, double *x, const bella_solve_o
         st.bnorm = bnorm;
         double target = o.tol * bnorm;
         if (o.atol > target) target = o.atol;
+        if (!isfinite(bnorm)) { st.status = BELLA_NONFINITE; goto done; }
         if (o.x0_zero) {
             BELLA_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
             if (bnorm == 0.0 || bnorm <= o.tol) {   // scipy 1.7 legacy exit
                 st.status = BELLA_OK;
-                st.relres = 0.0;
                 goto done;
             }
         }
@@ -601,11 +608,12 @@ int bella_bicgstab(bella_ws *ws, const double *b, double *x, const bella_solve_o
             st.matvecs = 1;
             st.status = BELLA_MAXITER;
             int total = 0;
+            bool failed = false;
             for (int outer = 0;; ++outer) {
                 if (!isfinite(rnorm)) { st.status = BELLA_NONFINITE; break; }
                 if (rnorm <= target) { st.status = BELLA_OK; break; }
                 if (total >= o.maxiter) { st.status = BELLA_MAXITER; break; }
-                if (outer >= o.max_outer) { st.status = BELLA_MAXITER; break; }
+                if (outer >= o.max_outer) { failed = true; break; }
                 if (timed_out) { st.status = BELLA_TIMEOUT; break; }
                 double rel = o.inner_tol;
                 const double need = 0.5 * target / rnorm;
@@ -618,41 +626,58 @@ int bella_bicgstab(bella_ws *ws, const double *b, double *x, const bella_solve_o
                 const int it = ws->ks_host->iter;
                 const int inner_status = ws->ks_host->status;
                 total += it;
-                st.matvecs += 2 * it + 1;
+                st.matvecs += 2 * it;
+                st.outer = outer + 1;
+                // a non-finite inner iterate is never applied
+                if (inner_status == BELLA_NONFINITE || it == 0) { failed = true; break; }
                 k_ir_update<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->x32, rnorm, ws->z64, ns, ws->ks,
                                                      ws->partials, ws->counter);
                 ws->launches++;
-                if (proj) {
-                    k_null_shift<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->ks, ns);
-                    ws->launches++;
-                }
                 op2d_resid(ws, 0, x, b, ws->r64, s);
+                st.matvecs += 1;
                 rc = sync_state(ws, s);
                 if (rc != BELLA_OK) return rc;
                 const double rnew = sqrt(ws->ks_host->dot_aux2);
-                st.outer = outer + 1;
-                if (inner_status == BELLA_BREAKDOWN && !(rnew < rnorm)) { rnorm = rnew; st.status = BELLA_BREAKDOWN; break; }
-                if (inner_status == BELLA_NONFINITE) { rnorm = rnew; st.status = BELLA_NONFINITE; break; }
-                if (it == 0 && !(rnew < rnorm)) { rnorm = rnew; st.status = BELLA_BREAKDOWN; break; }
+                if (!(rnew < rnorm)) {
+                    // no progress: take the correction back and stop refining
+                    NullSpace none = ns;
+                    none.nm = 0;
+                    k_ir_update<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->x32, -rnorm, ws->z64, none, ws->ks,
+                                                         ws->partials, ws->counter);
+                    ws->launches++;
+                    failed = true;
+                    break;
+                }
+                if (proj) {   // keep x in the operator's range (A e_k = 0 exactly)
+                    k_null_shift<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->ks, ns);
+                    ws->launches++;
+                }
                 rnorm = rnew;
             }
             st.iterations = total;
-            st.relres = bnorm > 0 ? rnorm / bnorm : rnorm;
+            if (failed) {
+                // FP64 fallback from the FP64 iterate, reported in stats.fallback
+                st.fallback = 1;
+                const int left = o.maxiter - total;
+                rc = solve_fp64(ws, b, x, o, 1, left > 0 ? left : 0, &st, s, t0);
+                if (rc != BELLA_OK) return rc;
+            }
         }
     }
 done:
-    if (o.precision == 0) {
+    {
         // true FP64 residual of the returned x
         op2d_resid(ws, 0, x, b, ws->r64, s);
         rc = sync_state(ws, s);
         if (rc != BELLA_OK) return rc;
         const double rn = sqrt(ws->ks_host->dot_aux2);
         st.relres = st.bnorm > 0 ? rn / st.bnorm : rn;
+        if (!isfinite(rn)) st.status = BELLA_NONFINITE;
     }
     BELLA_CUDA(cudaGetLastError());
     st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (stats) *stats = st;
-    return BELLA_OK;
+    return st.status;
 }
 
 }  // extern "C"

@@ -126,13 +126,15 @@ class NodalHelmholtz2D:
         return y
 
     # -- solve -------------------------------------------------------------
-    def solve(self, b, x0=None, tol=1e-8, atol=0.0, maxiter=6000, precision="mixed", inner_tol=1e-5,
+    def solve(self, b, x0=None, tol=1e-8, atol=0.0, maxiter=6000, precision="fp64", inner_tol=1e-5,
               project_null=True, check_every=16, timeout_s=0.0, out=None):
         """Solve ``A x = b``; returns ``(x, stats)`` with ``x`` a CUDA float64 tensor.
 
-        ``precision='fp64'`` is BiCGStab in FP64 with scipy's control flow;
-        ``'mixed'`` runs FP32 BiCGStab inner solves inside FP64 iterative
-        refinement (FP64 residuals, FP64 accumulated solution).
+        ``precision='fp64'`` (default) is BiCGStab in FP64 with scipy's
+        control flow.  ``'mixed'`` runs FP32 BiCGStab inner solves inside FP64
+        iterative refinement (FP64 residuals, FP64 accumulated solution); if an
+        inner solve fails (non-finite, breakdown, no progress) the solve is
+        finished by FP64 BiCGStab and ``stats['fallback'] == 1``.
         """
         bd = _to_dev(b, self.dev)
         if bd.numel() != self.n:
@@ -190,7 +192,7 @@ class LinearOperator:
 
 
 def bicgstab(A, b, x0=None, tol=None, maxiter=None, M=None, callback=None, atol=None, rtol=None,
-             *, precision="mixed", stats=None, inner_tol=1e-5):
+             *, precision="fp64", stats=None, inner_tol=1e-5):
     """scipy-compatible ``bicgstab`` (scipy 1.7 keyword semantics, which the reference uses).
 
     Returns ``(x, info)``: ``info == 0`` converged, ``> 0`` iteration count
@@ -225,7 +227,7 @@ def bicgstab(A, b, x0=None, tol=None, maxiter=None, M=None, callback=None, atol=
     if stats is not None:
         stats.update(st)
         stats["info"] = info
-        stats["fallback_used"] = False
+        stats["fallback_used"] = bool(st["fallback"])
     xo = x if is_torch else x.cpu().numpy()
     if callback is not None:
         for _ in range(int(st["iterations"])):
