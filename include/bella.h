@@ -86,7 +86,8 @@ typedef struct bella_solve_stats {
     int    fallback;         /* 1: the FP32 inner solves failed (non-finite,
                                 breakdown or no progress) and the solve was
                                 finished by FP64 BiCGStab from the FP64 iterate */
-    int    pad_;
+    int    detail;           /* breakdown test that fired: 1 rho, 2 omega,
+                                3 <r^,A p> == 0, 4 ||A s|| == 0 (0: none)   */
 } bella_solve_stats;
 
 /* ---- workspace --------------------------------------------------------- */

@@ -45,10 +45,10 @@ class SolveStats(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int),
                 ("outer", ctypes.c_int), ("matvecs", ctypes.c_int),
                 ("relres", ctypes.c_double), ("bnorm", ctypes.c_double),
-                ("seconds", ctypes.c_double), ("fallback", ctypes.c_int), ("pad_", ctypes.c_int)]
+                ("seconds", ctypes.c_double), ("fallback", ctypes.c_int), ("detail", ctypes.c_int)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad_"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 # exported symbol -> (restype, argtypes); also the list checked by the tests

@@ -37,6 +37,7 @@ struct KState {
     double ss;         // ||s||^2
     double atol;       // absolute stopping threshold on ||r|| (and ||s||)
     double rhotol;     // rho / omega breakdown limit
+    double rho0;       // <r^, r0>: scale of the relative rho breakdown test
     double scale;      // IR: inner system = outer residual / scale
     double dot_aux;    // result of the generic FP64 dot kernel
     double dot_aux2;
@@ -45,7 +46,7 @@ struct KState {
     int    done;       // 1 once converged / failed: later kernels return at once
     int    status;     // BELLA_* status of the (inner) solve
     int    early;      // ||s|| < atol met inside the current iteration
-    int    pad[3];
+    int    pad[3];     // pad[0]: breakdown reason (1 rho, 2 omega, 3 <r^,v>, 4 ||t||)
     double nd[MAXNULL];     // <z_k, x> of the null-space projection
     double cnull[MAXNULL];  // coefficients removed along the null modes
 };

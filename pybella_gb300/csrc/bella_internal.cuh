@@ -8,14 +8,17 @@ namespace bella {
 enum { M_APPLY = 0, M_RESID = 1, M_PDIR = 2, M_SDIR = 3 };
 
 // ---- last-block finalisers of one BiCGStab iteration -----------------------
-// The control flow and breakdown tests follow scipy's bicgstab, which the
-// reference calls (second_projection.py:230): rho/omega breakdown below
-// eps^2, early exit when ||s|| meets the tolerance, convergence on ||r||.
+// The control flow follows scipy's bicgstab, which the reference calls
+// (second_projection.py:230): early exit when ||s|| meets the tolerance,
+// convergence on ||r||, rho and omega breakdown below eps^2.  One deviation:
+// the rho test is relative, |<r^,r>| < eps^2 <r^,r0>, where scipy's is
+// absolute; scipy's absolute test stops solves with a small-norm right-hand
+// side (||b|| ~ 4e-5 at 2049x1025) near convergence for no numerical reason.
 
 // after v = A p:  alpha = rho / <r^, v>
 __device__ __forceinline__ void finalize_pdir(KState *ks, double rv) {
     if (!isfinite(rv)) { ks->status = BELLA_NONFINITE; ks->done = 1; return; }
-    if (rv == 0.0) { ks->status = BELLA_BREAKDOWN; ks->done = 1; return; }
+    if (rv == 0.0) { ks->status = BELLA_BREAKDOWN; ks->pad[0] = 3; ks->done = 1; return; }
     ks->alpha = ks->rho / rv;
 }
 
@@ -26,7 +29,7 @@ __device__ __forceinline__ void finalize_sdir(KState *ks, double ts, double tt, 
         ks->status = BELLA_NONFINITE; ks->done = 1; return;
     }
     if (sqrt(ss) <= ks->atol) { ks->early = 1; ks->omega = 0.0; return; }
-    if (!(tt > 0.0)) { ks->status = BELLA_BREAKDOWN; ks->done = 1; return; }
+    if (!(tt > 0.0)) { ks->status = BELLA_BREAKDOWN; ks->pad[0] = 4; ks->done = 1; return; }
     ks->omega = ts / tt;
 }
 
@@ -38,8 +41,8 @@ __device__ __forceinline__ void finalize_update(KState *ks, double rho_new, doub
     if (!isfinite(rr) || !isfinite(rho_new)) { ks->status = BELLA_NONFINITE; ks->done = 1; }
     else if (sqrt(rr) <= ks->atol) { ks->status = BELLA_OK; ks->done = 1; }
     else if (ks->iter >= ks->maxiter) { ks->status = BELLA_MAXITER; ks->done = 1; }
-    else if (fabs(rho_new) < ks->rhotol) { ks->status = BELLA_BREAKDOWN; ks->done = 1; }
-    else if (fabs(ks->omega) < ks->rhotol) { ks->status = BELLA_BREAKDOWN; ks->done = 1; }
+    else if (fabs(rho_new) < ks->rhotol * ks->rho0) { ks->status = BELLA_BREAKDOWN; ks->pad[0] = 1; ks->done = 1; }
+    else if (fabs(ks->omega) < ks->rhotol) { ks->status = BELLA_BREAKDOWN; ks->pad[0] = 2; ks->done = 1; }
     else {
         ks->beta = (rho_new / ks->rho) * (ks->alpha / ks->omega);
         ks->rho_prev = ks->rho;

@@ -129,6 +129,7 @@ template void launch_update<double>(bella_ws *, cudaStream_t);
 
 static __device__ void init_state(KState *ks, double rr, double atol, double rhotol, int maxiter) {
     ks->rho = rr;           // r^ = r  ->  rho = ||r||^2
+    ks->rho0 = rr;
     ks->rho_prev = 1.0;
     ks->rr = rr;
     ks->alpha = 1.0;
@@ -141,10 +142,11 @@ static __device__ void init_state(KState *ks, double rr, double atol, double rho
     ks->early = 0;
     ks->done = 0;
     ks->status = BELLA_MAXITER;
+    ks->pad[0] = 0;
     if (!isfinite(rr)) { ks->status = BELLA_NONFINITE; ks->done = 1; }
     else if (sqrt(rr) <= atol) { ks->status = BELLA_OK; ks->done = 1; }
     else if (maxiter <= 0) { ks->status = BELLA_MAXITER; ks->done = 1; }
-    else if (fabs(rr) < rhotol) { ks->status = BELLA_BREAKDOWN; ks->done = 1; }
+    else if (!(rr > 0.0)) { ks->status = BELLA_BREAKDOWN; ks->done = 1; }
 }
 
 // FP64 solve start.  x_given = 0: x = 0, r = b.  x_given = 1: r already
@@ -557,6 +559,7 @@ static int solve_fp64(bella_ws *ws, const double *b, double *x, const bella_solv
     st->status = timed_out ? BELLA_TIMEOUT : ws->ks_host->status;
     st->bnorm = ws->ks_host->dot_aux;
     st->matvecs += 2 * ws->ks_host->iter + (x_given ? 1 : 0);
+    st->detail = ws->ks_host->pad[0];
     return BELLA_OK;
 }
 
@@ -625,6 +628,7 @@ int bella_bicgstab(bella_ws *ws, const double *b, double *x, const bella_solve_o
                 if (rc != BELLA_OK) return rc;
                 const int it = ws->ks_host->iter;
                 const int inner_status = ws->ks_host->status;
+                st.detail = ws->ks_host->pad[0];
                 total += it;
                 st.matvecs += 2 * it;
                 st.outer = outer + 1;

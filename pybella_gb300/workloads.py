@@ -16,8 +16,7 @@ These stand in for the reference's configuration; the reference ships no
 such input data.  Values are drawn with torch's CUDA generator, so they are
 reproducible per seed on a given torch build.
 """
-import math
-
+import numpy as np
 import torch
 
 R_GAS, GAMM, T_REF, H_REF = 287.4, 1.4, 300.0, 10000.0
@@ -101,9 +100,10 @@ def stratified_2d(seed, nx=2049, ny=1025, sigma=0.1, dt=0.01, device="cuda"):
     f = _kminus3((nx - 1, 2 * (ny - 1)), gen, dev)[:, :ny]
     b = torch.cat([f, f[:1]], dim=0)                        # seam column duplicated
     E, w = null_modes_2d(nx, ny, True, False, dev)
-    G = torch.stack([torch.stack([(w * ek * el).sum() for el in E]) for ek in E])
-    r = torch.stack([(w * ek * b).sum() for ek in E])
-    cf = torch.linalg.solve(G, r)
+    # tiny Gram system solved on the host (no device linear-algebra library needed)
+    G = torch.stack([torch.stack([(w * ek * el).sum() for el in E]) for ek in E]).cpu().numpy()
+    r = torch.stack([(w * ek * b).sum() for ek in E]).cpu().numpy()
+    cf = torch.from_numpy(np.linalg.solve(G, r)).to(dev)
     b = b - torch.tensordot(cf, E, dims=1)
     b_flat = b.T.contiguous().reshape(-1)
     return dict(hplusx=hplus, hplusy=hplus.clone(), hcenter=None,
