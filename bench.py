@@ -307,9 +307,10 @@ def run_gpu(args):
     share = {names[k]: kt[k][0] for k in kt}
     tot_k = sum(share.values()) or 1.0
     pd_ms, pd_n = kt[0]
-    # algorithmic bytes per launch: r, p_old, v_old, r^ read; p_new, v_new written;
-    # Axx, Ayy per cell; diag_inv per node  -> 9 FP32 words per node
-    alg_bytes = 4.0 * (7 * nnode + 2 * ncell)
+    # algorithmic bytes per launch of the p-direction stencil: r, p_old, v_old, r^
+    # read, p_new, v_new written, diag_inv (7 node words) + Axx, Ayy (2 cell words)
+    word = 8.0 if args.precision == "fp64" else 4.0
+    alg_bytes = word * (7 * nnode + 2 * ncell)
     achieved = alg_bytes / (pd_ms / pd_n / 1000.0) / 1e9 if pd_n else None
     iters = [s["iterations"] for s in stats]
 
@@ -326,7 +327,8 @@ def run_gpu(args):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": None,
-                     "kernel": "k_stencil2d<float, PDIR>", "peak_source": peak_kind,
+                     "kernel": "k_stencil2d<%s, PDIR>" % ("double" if args.precision == "fp64" else "float"),
+                     "peak_source": peak_kind,
                      "alg_bytes_per_launch": alg_bytes},
         "clocks": clk,
         "solver": {"iterations_mean": float(np.mean(iters)), "outer_mean": float(np.mean([s["outer"] for s in stats])),
