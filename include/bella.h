@@ -123,6 +123,25 @@ int  bella_bicgstab(bella_ws *ws, const double *b, double *x,
                     const bella_solve_opts *opts, bella_solve_stats *stats,
                     void *stream);
 
+/* ---- allocation-free variant (no counterpart in the reference) ----------
+ * FP64 BiCGStab of bella_bicgstab (precision 0 only) on the reference-packed
+ * 2D operands, for callers that cannot allocate device memory while they run
+ * (a host model that owns the whole GPU through its own memory pool, or a
+ * time loop that cannot take the device-wide stall a cudaMalloc/cudaFree can
+ * cause).  Needs no workspace: all scratch lives in one fixed device array
+ * inside the library (about 13 MB, held by every GPU that loads the library
+ * until the process exits).  Limits: nx*ny <= 65536 nodes and
+ * (nx+1)*(ny+1) <= 131072 cells; larger grids return BELLA_EINVAL.
+ * The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any stream
+ * capture.  Every call reuses the same array: calls that overlap on the GPU
+ * (other streams, other host threads, same device) race and must not be
+ * issued.  The caller passes b and x (device, FP64).  Returns the solver
+ * status or a negative error. */
+int bella_bicgstab2d_noalloc(const bella_op2d *op, const double *b, double *x,
+                             const bella_solve_opts *opts, bella_solve_stats *stats,
+                             void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -68,6 +68,8 @@ SIGNATURES = {
     "bella_solve_opts_default": (None, [ctypes.POINTER(SolveOpts)]),
     "bella_bicgstab": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, ctypes.POINTER(SolveOpts),
                                       ctypes.POINTER(SolveStats), ctypes.c_void_p]),
+    "bella_bicgstab2d_noalloc": (ctypes.c_int, [ctypes.POINTER(Op2D), _dp, _dp, ctypes.POINTER(SolveOpts),
+                                                ctypes.POINTER(SolveStats), ctypes.c_void_p]),
 }
 
 _lib = None

@@ -685,3 +685,137 @@ done:
 }
 
 }  // extern "C"
+
+// ============================================================================
+// Allocation-free FP64 BiCGStab for small 2D systems.
+//
+// Some callers cannot allocate device memory while they run: a model that
+// reserves the whole GPU for its own memory pool at start-up and forbids any
+// later cudaMalloc, or a time loop that cannot afford the device-wide
+// synchronisation a cudaMalloc/cudaFree may cause.  For them this entry point
+// keeps every byte of its scratch (packed operator planes, Krylov vectors,
+// reduction partials, Krylov state) in one file-scope device array of fixed
+// size, created when the library's device code is loaded on a GPU and held by
+// every GPU that loads the library until the process exits.
+// ============================================================================
+#include <mutex>
+
+namespace bella {
+
+constexpr long long NOALLOC_MAX_NODES = 65536;                   // nx*ny
+constexpr long long NOALLOC_MAX_CELLS = 2 * NOALLOC_MAX_NODES;   // (nx+1)*(ny+1)
+constexpr long long NOALLOC_PARTIALS = (long long)NQ * NSM * 8;
+// doubles: 4 FP64 cell planes + 4 FP32 cell planes (as 2 doubles' worth),
+// dinv/hc/z (FP64) + dinv/hc (FP32, one double's worth), 9 FP64 vectors,
+// partials, counter word and the Krylov state
+constexpr long long NOALLOC_DOUBLES =
+    6 * NOALLOC_MAX_CELLS + 4 * NOALLOC_MAX_NODES + 9 * NOALLOC_MAX_NODES + NOALLOC_PARTIALS + 8 +
+    (long long)((sizeof(KState) + 7) / 8);
+
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_DOUBLES];
+
+static std::mutex g_noalloc_mu;
+static double *g_noalloc_ptr[256];   // device address of g_noalloc_scratch per device
+
+// Device address of the scratch array on the current device (looked up once
+// per device with that device current; the array's host-side name is not a
+// device address).
+static int noalloc_scratch(int dev, double **out) {
+    if (dev < 0 || dev >= 256) return set_err(BELLA_EINVAL, "bella_bicgstab2d_noalloc: device id out of range");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        double *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress((void **)&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_check(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return BELLA_OK;
+}
+
+}  // namespace bella
+
+extern "C" int bella_bicgstab2d_noalloc(const bella_op2d *op, const double *b, double *x,
+                                        const bella_solve_opts *opts, bella_solve_stats *stats,
+                                        void *stream) {
+    using namespace bella;
+    if (!op || !b || !x) return set_err(BELLA_EINVAL, "bella_bicgstab2d_noalloc: null argument");
+    if (op->nx < 3 || op->ny < 3) return set_err(BELLA_EINVAL, "bella_bicgstab2d_noalloc: nx, ny must be >= 3");
+    const long long n = (long long)op->nx * op->ny;
+    const long long nc = (long long)(op->nx + 1) * (op->ny + 1);
+    if (n > NOALLOC_MAX_NODES || nc > NOALLOC_MAX_CELLS)
+        return set_err(BELLA_EINVAL, "bella_bicgstab2d_noalloc: grid too large for the fixed scratch "
+                                     "(at most 65536 nodes and 131072 cells); use bella_bicgstab");
+    if (!op->hplusx || !op->hplusy || !op->cxx || !op->cyy || !op->diag_inv)
+        return set_err(BELLA_EINVAL, "bella_bicgstab2d_noalloc: hplusx, hplusy, cxx, cyy, diag_inv are required");
+    if (!(op->dx > 0.0) || !(op->dy > 0.0)) return set_err(BELLA_EINVAL, "bella_bicgstab2d_noalloc: dx, dy must be > 0");
+    bella_solve_opts o;
+    if (opts) o = *opts; else bella_solve_opts_default(&o);
+    if (!(o.tol >= 0.0) || o.maxiter < 0) return set_err(BELLA_EINVAL, "bella_bicgstab2d_noalloc: bad tol/maxiter");
+    if (o.precision != 0)
+        return set_err(BELLA_EINVAL, "bella_bicgstab2d_noalloc: only precision 0 (FP64 BiCGStab) is available");
+    int dev = 0;
+    BELLA_CUDA(cudaGetDevice(&dev));
+    double *base = nullptr;
+    int rc = noalloc_scratch(dev, &base);
+    if (rc != BELLA_OK) return rc;
+
+    // a workspace view onto the fixed scratch; lives on this call's stack
+    bella_ws w;
+    memset(&w, 0, sizeof(w));
+    KState ks_host;
+    w.device = dev;
+    w.ndim = 2;
+    w.nx = op->nx; w.ny = op->ny; w.nz = 1;
+    w.n = n;
+    w.cross = (op->cxy != nullptr || op->cyx != nullptr) ? 1 : 0;
+    w.has_hc = op->hcenter != nullptr ? 1 : 0;
+    w.singular = 0;            // no null-space projection on the FP64 path
+    w.grid_stencil = stencil_grid(op->nx, op->ny);
+    w.grid_vec = vec_grid(n);
+    double *p = base;
+    w.a64 = p;                 p += 4 * NOALLOC_MAX_CELLS;
+    w.a32 = (float *)p;        p += 2 * NOALLOC_MAX_CELLS;
+    w.dinv64 = p;              p += NOALLOC_MAX_NODES;
+    w.hc64 = p;                p += NOALLOC_MAX_NODES;
+    w.z64 = p;                 p += NOALLOC_MAX_NODES;
+    w.dinv32 = (float *)p;     // dinv32 and hc32 share one slab of MAX_NODES doubles
+    w.hc32 = w.dinv32 + NOALLOC_MAX_NODES;
+    p += NOALLOC_MAX_NODES;
+    w.r64 = p;                 p += NOALLOC_MAX_NODES;
+    w.x64v = p;                p += NOALLOC_MAX_NODES;
+    w.r64k = p;                p += NOALLOC_MAX_NODES;
+    w.rh64 = p;                p += NOALLOC_MAX_NODES;
+    w.p64[0] = p;              p += NOALLOC_MAX_NODES;
+    w.p64[1] = p;              p += NOALLOC_MAX_NODES;
+    w.v64[0] = p;              p += NOALLOC_MAX_NODES;
+    w.v64[1] = p;              p += NOALLOC_MAX_NODES;
+    w.t64 = p;                 p += NOALLOC_MAX_NODES;
+    w.partials = p;            p += NOALLOC_PARTIALS;
+    w.counter = (unsigned *)p; p += 8;
+    w.ks = (KState *)p;
+    w.ks_host = &ks_host;
+    w.cap = n;
+
+    cudaStream_t s = (cudaStream_t)stream;
+    const auto t0 = std::chrono::steady_clock::now();
+    // the array keeps the previous call's contents: the grid-reduction counter
+    // must start at zero
+    BELLA_CUDA(cudaMemsetAsync(w.counter, 0, 8 * sizeof(double), s));
+    rc = op2d_pack(&w, op, s);
+    if (rc != BELLA_OK) return cuda_check(cudaGetLastError(), "bella_bicgstab2d_noalloc: pack");
+    bella_solve_stats st;
+    memset(&st, 0, sizeof(st));
+    rc = solve_fp64(&w, b, x, o, o.x0_zero ? 0 : 1, o.maxiter, &st, s, t0);
+    if (rc != BELLA_OK) return rc;
+    op2d_resid(&w, 0, x, b, w.r64, s);
+    rc = sync_state(&w, s);
+    if (rc != BELLA_OK) return rc;
+    const double rn = sqrt(ks_host.dot_aux2);
+    st.relres = st.bnorm > 0 ? rn / st.bnorm : rn;
+    if (!isfinite(rn)) st.status = BELLA_NONFINITE;
+    BELLA_CUDA(cudaGetLastError());
+    st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (stats) *stats = st;
+    return st.status;
+}
