@@ -44,7 +44,7 @@ def _args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--seeds", type=int, default=64)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="df64", choices=["fp64", "mixed", "df64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--nx", type=int, default=NX)
@@ -309,7 +309,7 @@ def run_gpu(args):
     pd_ms, pd_n = kt[0]
     # algorithmic bytes per launch of the p-direction stencil: r, p_old, v_old, r^
     # read, p_new, v_new written, diag_inv (7 node words) + Axx, Ayy (2 cell words)
-    word = 8.0 if args.precision == "fp64" else 4.0
+    word = 4.0 if args.precision == "mixed" else 8.0
     alg_bytes = word * (7 * nnode + 2 * ncell)
     achieved = alg_bytes / (pd_ms / pd_n / 1000.0) / 1e9 if pd_n else None
     iters = [s["iterations"] for s in stats]
@@ -317,7 +317,7 @@ def run_gpu(args):
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "scaling": "weak", "vs_baseline": None, "dtype": {"fp64": "f64", "mixed": "f32+f64", "df64": "f32x2 (double-float)"}[args.precision],
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "rtol": TOL, "precision": args.precision,
                    "l2": "flushed (256 MB write) before every step", "seeds": nseeds,
@@ -327,7 +327,7 @@ def run_gpu(args):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": None,
-                     "kernel": "k_stencil2d<%s, PDIR>" % ("double" if args.precision == "fp64" else "float"),
+                     "kernel": "k_stencil2d<%s, PDIR>" % {"fp64": "double", "mixed": "float", "df64": "dfloat"}[args.precision],
                      "peak_source": peak_kind,
                      "alg_bytes_per_launch": alg_bytes},
         "clocks": clk,

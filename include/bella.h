@@ -65,7 +65,9 @@ typedef struct bella_solve_opts {
     double atol;             /* absolute floor (0 = none)                    */
     int    maxiter;          /* inner BiCGStab iteration limit (total)       */
     int    precision;        /* 0: FP64 BiCGStab;  1: FP32 inner solves in FP64
-                                iterative refinement, FP64 fallback           */
+                                iterative refinement, FP64 fallback;
+                                2: double-float BiCGStab (FP32-pair vectors
+                                and arithmetic, ~48-bit, on the FP32 pipe)   */
     int    x0_zero;          /* 1: start from x = 0 (x is output only)       */
     int    project_null;     /* 1: keep x orthogonal to the left null vector
                                 (pseudo-incompressible operator)           */

@@ -7,20 +7,33 @@
 #include <math.h>
 
 #include "../../include/bella.h"
+#include "bella_df.cuh"
 
 namespace bella {
 
 // --------------------------------------------------------------------------
 // launch geometry of the 2D stencil tiles
 // --------------------------------------------------------------------------
+#ifndef BELLA_TY
+#define BELLA_TY 16
+#endif
+#ifndef BELLA_MINB
+#define BELLA_MINB 5            // measured best on GB300 (2049x1025, double-float)
+#endif
+#ifndef BELLA_GRID_PER_SM
+#define BELLA_GRID_PER_SM 8
+#endif
 constexpr int TX = 64;          // tile width  (nodes, x)  = 2 warps
-constexpr int TY = 16;          // tile height (nodes, y)
+constexpr int TY = BELLA_TY;    // tile height (nodes, y)
+constexpr int MINB = BELLA_MINB;            // __launch_bounds__ min CTAs/SM of the stencil
+constexpr int GRID_PER_SM = BELLA_GRID_PER_SM;
 constexpr int BX = 64;          // threads in x
 constexpr int BY = 4;           // threads in y  -> 256 threads, 4 rows each
 constexpr int NTHREADS = BX * BY;
 constexpr int NSM = 152;        // GB300 SMs (grid sizes are multiples of this)
 constexpr int VEC_BLOCK = 256;  // block size of the streaming vector kernels
 constexpr int NQ = 8;           // reduction quantities per kernel (max)
+constexpr int MAXGRID = NSM * 8;  // largest grid of any reduction kernel (partials capacity)
 constexpr int MAXNULL = 8;      // null-space modes handled by the projection
 
 // --------------------------------------------------------------------------
@@ -109,6 +122,7 @@ struct DD {
 template <typename T> struct Acc;
 template <> struct Acc<float>  { using type = DF; };
 template <> struct Acc<double> { using type = DD; };
+template <> struct Acc<dfloat> { using type = DFAcc; };
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -217,6 +231,8 @@ struct bella_ws {
     double *r64, *x64v;       // IR outer residual, FP64 scratch
     float  *r32, *rh32, *p32[2], *v32[2], *t32, *x32;
     double *r64k, *rh64, *p64[2], *v64[2], *t64;
+    bella::dfloat *rdf, *rhdf, *pdf[2], *vdf[2], *tdf, *xdf;   // double-float Krylov vectors
+    bella::dfloat *adf, *dinvdf, *hcdf;                         // double-float operator planes
     double *partials;
     unsigned *counter;
     bella::KState *ks;        // device

@@ -33,21 +33,24 @@ __device__ __forceinline__ void finalize_sdir(KState *ks, double ts, double tt, 
     ks->omega = ts / tt;
 }
 
-// after x += alpha p + omega s, r = s - omega t
+// after x += alpha p + omega s, r = s - omega t.  rho/beta are advanced even
+// when the solve stops here, so a residual replacement can continue the
+// same Krylov process (k_replace_df).
 __device__ __forceinline__ void finalize_update(KState *ks, double rho_new, double rr) {
     ks->iter += 1;
     if (ks->early) { ks->status = BELLA_OK; ks->done = 1; ks->rr = ks->ss; return; }
     ks->rr = rr;
-    if (!isfinite(rr) || !isfinite(rho_new)) { ks->status = BELLA_NONFINITE; ks->done = 1; }
-    else if (sqrt(rr) <= ks->atol) { ks->status = BELLA_OK; ks->done = 1; }
-    else if (ks->iter >= ks->maxiter) { ks->status = BELLA_MAXITER; ks->done = 1; }
-    else if (fabs(rho_new) < ks->rhotol * ks->rho0) { ks->status = BELLA_BREAKDOWN; ks->pad[0] = 1; ks->done = 1; }
-    else if (fabs(ks->omega) < ks->rhotol) { ks->status = BELLA_BREAKDOWN; ks->pad[0] = 2; ks->done = 1; }
-    else {
+    const bool finite = isfinite(rr) && isfinite(rho_new);
+    if (finite && ks->omega != 0.0) {
         ks->beta = (rho_new / ks->rho) * (ks->alpha / ks->omega);
         ks->rho_prev = ks->rho;
         ks->rho = rho_new;
     }
+    if (!finite) { ks->status = BELLA_NONFINITE; ks->done = 1; }
+    else if (sqrt(rr) <= ks->atol) { ks->status = BELLA_OK; ks->done = 1; }
+    else if (ks->iter >= ks->maxiter) { ks->status = BELLA_MAXITER; ks->done = 1; }
+    else if (fabs(rho_new) < ks->rhotol * ks->rho0) { ks->status = BELLA_BREAKDOWN; ks->pad[0] = 1; ks->done = 1; }
+    else if (fabs(ks->omega) < ks->rhotol) { ks->status = BELLA_BREAKDOWN; ks->pad[0] = 2; ks->done = 1; }
 }
 
 // ---- per-kernel event timing (host) -------------------------------------------

@@ -10,6 +10,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <type_traits>
 
 #include "bella_internal.cuh"
 
@@ -112,7 +113,11 @@ void prof_harvest(bella_ws *ws) {
 template <typename T>
 void launch_update(bella_ws *ws, cudaStream_t s) {
     prof_begin(ws, PK_UPDATE, s);
-    if (sizeof(T) == 8) {
+    if (std::is_same<T, dfloat>::value) {
+        k_update<dfloat><<<ws->grid_vec, VEC_BLOCK, 0, s>>>(ws->n, ws->xdf, ws->pdf[0], ws->pdf[1], ws->rdf,
+                                                          ws->vdf[0], ws->vdf[1], ws->tdf, ws->rhdf,
+                                                          ws->ks, ws->partials, ws->counter);
+    } else if (std::is_same<T, double>::value) {
         k_update<double><<<ws->grid_vec, VEC_BLOCK, 0, s>>>(ws->n, ws->x64v, ws->p64[0], ws->p64[1], ws->r64k,
                                                           ws->v64[0], ws->v64[1], ws->t64, ws->rh64,
                                                           ws->ks, ws->partials, ws->counter);
@@ -126,6 +131,7 @@ void launch_update(bella_ws *ws, cudaStream_t s) {
 }
 template void launch_update<float>(bella_ws *, cudaStream_t);
 template void launch_update<double>(bella_ws *, cudaStream_t);
+template void launch_update<dfloat>(bella_ws *, cudaStream_t);
 
 static __device__ void init_state(KState *ks, double rr, double atol, double rhotol, int maxiter) {
     ks->rho = rr;           // r^ = r  ->  rho = ||r||^2
@@ -143,6 +149,7 @@ static __device__ void init_state(KState *ks, double rr, double atol, double rho
     ks->done = 0;
     ks->status = BELLA_MAXITER;
     ks->pad[0] = 0;
+    ks->pad[1] = 0;
     if (!isfinite(rr)) { ks->status = BELLA_NONFINITE; ks->done = 1; }
     else if (sqrt(rr) <= atol) { ks->status = BELLA_OK; ks->done = 1; }
     else if (maxiter <= 0) { ks->status = BELLA_MAXITER; ks->done = 1; }
@@ -176,6 +183,73 @@ k_init64(long long n, const double *b, double *x, double *r, double *rh, int x_g
     init_state(ks, tot[0], atol, 4.930380657631324e-32 /* eps64^2 */, maxiter);
     ks->dot_aux = bnorm;
     if (bnorm == 0.0 || (!x_given && bnorm <= tol)) { ks->status = BELLA_OK; ks->done = 1; }
+}
+
+// Double-float solve start.  x_given = 0: x = 0, r = b.  x_given = 1: r64 holds
+// b - A x (FP64) and x is the FP64 start.  r^ = r.  Same thresholds as k_init64.
+__global__ void __launch_bounds__(VEC_BLOCK)
+k_init_df(long long n, const double *b, const double *x64, const double *r64, dfloat *x, dfloat *r,
+          dfloat *rh, int x_given, double tol, double atol_user, int maxiter, KState *ks, double *partials,
+          unsigned *counter) {
+    DD a0, a1;
+    a0.zero(); a1.zero();
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+         g += (long long)gridDim.x * blockDim.x) {
+        const double bg = b[g];
+        const double rg = x_given ? r64[g] : bg;
+        const dfloat rd(rg);
+        r[g] = rd;
+        rh[g] = rd;
+        x[g] = x_given ? dfloat(x64[g]) : dfloat(0.f, 0.f);
+        a0.add_prod(rg, rg);
+        a1.add_prod(bg, bg);
+    }
+    double vv[2] = {a0.value(), a1.value()}, tot[2];
+    if (!grid_sum<2>(vv, partials, counter, tot)) return;
+    if (threadIdx.x != 0) return;
+    const double bnorm = sqrt(tot[1]);
+    double atol = tol * bnorm;
+    if (atol_user > atol) atol = atol_user;
+    init_state(ks, tot[0], atol, 4.930380657631324e-32, maxiter);
+    ks->dot_aux = bnorm;
+    if (bnorm == 0.0 || (!x_given && bnorm <= tol)) { ks->status = BELLA_OK; ks->done = 1; }
+}
+
+// Residual replacement (reliable update): r = b - A x computed in FP64
+// replaces the recursive double-float residual and the iteration continues
+// with the same r^ and p; rho and beta are recomputed from the new r.  After
+// an early (||s||) exit the omega step is missing, so the caller restarts.
+__global__ void __launch_bounds__(VEC_BLOCK)
+k_replace_df(long long n, const double *r64, dfloat *r, const dfloat *rh, KState *ks, double *partials,
+             unsigned *counter) {
+    DFAcc a0, a1;
+    a0.zero(); a1.zero();
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+         g += (long long)gridDim.x * blockDim.x) {
+        const dfloat rd(r64[g]);
+        r[g] = rd;
+        a0.add_prod(rh[g], rd);
+        a1.add_prod(rd, rd);
+    }
+    double vv[2] = {a0.value(), a1.value()}, tot[2];
+    if (!grid_sum<2>(vv, partials, counter, tot)) return;
+    if (threadIdx.x != 0) return;
+    ks->rr = tot[1];
+    ks->done = 0;
+    ks->status = BELLA_MAXITER;
+    ks->pad[0] = 0;
+    if (ks->early || ks->omega == 0.0 || !isfinite(tot[0])) { ks->pad[1] = 1; ks->done = 1; return; }
+    ks->rho = tot[0];
+    ks->beta = (ks->rho / ks->rho_prev) * (ks->alpha / ks->omega);
+    if (sqrt(tot[1]) <= ks->atol) { ks->status = BELLA_OK; ks->done = 1; }
+    else if (ks->iter >= ks->maxiter) { ks->status = BELLA_MAXITER; ks->done = 1; }
+}
+
+// x (FP64 output) = double-float solution
+__global__ void k_df_to_f64(long long n, const dfloat *xd, double *x) {
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+         g += (long long)gridDim.x * blockDim.x)
+        x[g] = xd[g].to_double();
 }
 
 // FP32 inner solve start (iterative refinement): r32 = r64 / scale, r^ = r32, x32 = 0.
@@ -325,8 +399,10 @@ static void free_op(bella_ws *ws) {
     cudaFree(ws->a64); cudaFree(ws->a32);
     cudaFree(ws->dinv64); cudaFree(ws->hc64); cudaFree(ws->z64);
     cudaFree(ws->dinv32); cudaFree(ws->hc32);
+    cudaFree(ws->adf); cudaFree(ws->dinvdf); cudaFree(ws->hcdf);
     ws->a64 = nullptr; ws->a32 = nullptr; ws->dinv64 = ws->hc64 = ws->z64 = nullptr;
     ws->dinv32 = ws->hc32 = nullptr;
+    ws->adf = ws->dinvdf = ws->hcdf = nullptr;
 }
 
 int bella_ws_destroy(bella_ws *ws) {
@@ -349,7 +425,7 @@ static int ensure_vectors(bella_ws *ws, long long n) {
     cudaFree(ws->vbase);
     ws->vbase = nullptr;
     const long long np = (n + 63) / 64 * 64;   // 256-byte aligned slices
-    const size_t bytes = (size_t)np * (8 * 9 + 4 * 8);
+    const size_t bytes = (size_t)np * (8 * 9 + 4 * 8 + 8 * 8);
     BELLA_CUDA(cudaMalloc(&ws->vbase, bytes));
     char *p = (char *)ws->vbase;
     auto take64 = [&](double **d) { *d = (double *)p; p += np * 8; };
@@ -358,6 +434,9 @@ static int ensure_vectors(bella_ws *ws, long long n) {
     take64(&ws->p64[0]); take64(&ws->p64[1]); take64(&ws->v64[0]); take64(&ws->v64[1]); take64(&ws->t64);
     take32(&ws->r32); take32(&ws->rh32); take32(&ws->p32[0]); take32(&ws->p32[1]);
     take32(&ws->v32[0]); take32(&ws->v32[1]); take32(&ws->t32); take32(&ws->x32);
+    auto takedf = [&](dfloat **d) { *d = (dfloat *)p; p += np * 8; };
+    takedf(&ws->rdf); takedf(&ws->rhdf); takedf(&ws->pdf[0]); takedf(&ws->pdf[1]);
+    takedf(&ws->vdf[0]); takedf(&ws->vdf[1]); takedf(&ws->tdf); takedf(&ws->xdf);
     ws->cap = n;
     return BELLA_OK;
 }
@@ -438,6 +517,9 @@ int bella_op2d_set(bella_ws *ws, const bella_op2d *op, void *stream) {
         BELLA_CUDA(cudaMalloc(&ws->z64, n * sizeof(double)));
         BELLA_CUDA(cudaMalloc(&ws->dinv32, n * sizeof(float)));
         BELLA_CUDA(cudaMalloc(&ws->hc32, n * sizeof(float)));
+        BELLA_CUDA(cudaMalloc(&ws->adf, 4 * ncell * sizeof(dfloat)));
+        BELLA_CUDA(cudaMalloc(&ws->dinvdf, n * sizeof(dfloat)));
+        BELLA_CUDA(cudaMalloc(&ws->hcdf, n * sizeof(dfloat)));
     }
     int rc = ensure_vectors(ws, n);
     if (rc != BELLA_OK) return rc;
@@ -563,6 +645,70 @@ static int solve_fp64(bella_ws *ws, const double *b, double *x, const bella_solv
     return BELLA_OK;
 }
 
+// Double-float BiCGStab (scipy control flow) on the FP32 pipe; x in/out FP64.
+// Convergence is only accepted on the FP64 true residual: when the recursive
+// double-float residual meets the tolerance, b - A x is recomputed in FP64 and,
+// if it is still too large, replaces the recursive one (reliable update) and
+// the iteration goes on (restarting after an early ||s|| exit).
+static int solve_df(bella_ws *ws, const double *b, double *x, const bella_solve_opts &o, int x_given,
+                    int maxiter, bella_solve_stats *st, cudaStream_t s,
+                    std::chrono::steady_clock::time_point t0) {
+    const long long n = ws->n;
+    const int gv = ws->grid_vec;
+    int timed_out = 0;
+    if (x_given) op2d_resid(ws, 0, x, b, ws->r64, s);
+    k_init_df<<<gv, VEC_BLOCK, 0, s>>>(n, b, x, ws->r64, ws->xdf, ws->rdf, ws->rhdf, x_given, o.tol, o.atol,
+                                       maxiter, ws->ks, ws->partials, ws->counter);
+    ws->launches++;
+    BELLA_CUDA(cudaGetLastError());
+    int rc, replaced = 0, restarts = 0, iters_before = 0;
+    bool true_too_large = false;
+    st->matvecs += x_given ? 1 : 0;
+    for (;;) {
+        rc = run_inner(ws, 2, &o, s, t0, &timed_out);
+        if (rc != BELLA_OK) return rc;
+        k_df_to_f64<<<gv, VEC_BLOCK, 0, s>>>(n, ws->xdf, x);
+        ws->launches++;
+        const KState k = *ws->ks_host;
+        st->detail = k.pad[0];
+        if (timed_out || k.status != BELLA_OK || k.iter >= maxiter) break;
+        const double bnorm = k.dot_aux, atol = k.atol;
+        op2d_resid(ws, 0, x, b, ws->r64, s);
+        st->matvecs += 1;
+        rc = sync_state(ws, s);
+        if (rc != BELLA_OK) return rc;
+        const double rn = sqrt(ws->ks_host->dot_aux2);
+        ws->ks_host->dot_aux = bnorm;
+        if (rn <= atol) break;
+        if (replaced >= 16) { true_too_large = true; break; }
+        replaced++;
+        k_replace_df<<<gv, VEC_BLOCK, 0, s>>>(n, ws->r64, ws->rdf, ws->rhdf, ws->ks, ws->partials, ws->counter);
+        ws->launches++;
+        rc = sync_state(ws, s);
+        if (rc != BELLA_OK) return rc;
+        if (ws->ks_host->pad[1]) {   // early exit: restart the Krylov process from x
+            restarts++;
+            iters_before += ws->ks_host->iter;
+            const int left = maxiter - iters_before;
+            if (left <= 0) break;
+            k_init_df<<<gv, VEC_BLOCK, 0, s>>>(n, b, x, ws->r64, ws->xdf, ws->rdf, ws->rhdf, 1, o.tol, o.atol, left,
+                                               ws->ks, ws->partials, ws->counter);
+            ws->launches++;
+            rc = sync_state(ws, s);
+            if (rc != BELLA_OK) return rc;
+            ws->ks_host->dot_aux = bnorm;
+        }
+    }
+    const KState k = *ws->ks_host;
+    st->iterations += iters_before + k.iter;
+    st->status = timed_out ? BELLA_TIMEOUT : k.status;
+    if (st->status == BELLA_OK && true_too_large) st->status = BELLA_MAXITER;   // never on the recursive residual alone
+    st->bnorm = k.dot_aux;
+    st->matvecs += 2 * (iters_before + k.iter);
+    st->outer = replaced;
+    return BELLA_OK;
+}
+
 int bella_bicgstab(bella_ws *ws, const double *b, double *x, const bella_solve_opts *opts,
                    bella_solve_stats *stats, void *stream) {
     if (!ws || !b || !x) return set_err(BELLA_EINVAL, "bella_bicgstab: null argument");
@@ -581,6 +727,9 @@ int bella_bicgstab(bella_ws *ws, const double *b, double *x, const bella_solve_o
 
     if (o.precision == 0) {
         rc = solve_fp64(ws, b, x, o, o.x0_zero ? 0 : 1, o.maxiter, &st, s, t0);
+        if (rc != BELLA_OK) return rc;
+    } else if (o.precision == 2) {
+        rc = solve_df(ws, b, x, o, o.x0_zero ? 0 : 1, o.maxiter, &st, s, t0);
         if (rc != BELLA_OK) return rc;
     } else {
         // ---- FP32 BiCGStab inner solves in FP64 iterative refinement ----

@@ -34,7 +34,7 @@ struct StArgs {
 // --------------------------------------------------------------------------
 // operator packing: reference operands -> cell planes (FP64 and FP32)
 // --------------------------------------------------------------------------
-__global__ void k_pack2d_cells(bella_op2d op, double *a64, float *a32, int cross) {
+__global__ void k_pack2d_cells(bella_op2d op, double *a64, float *a32, dfloat *adf, int cross) {
     const int nx = op.nx, ny = op.ny;
     const size_t ncell = (size_t)(nx + 1) * (ny + 1);
     const double oodx = 1.0 / op.dx, oody = 1.0 / op.dy;
@@ -52,6 +52,10 @@ __global__ void k_pack2d_cells(bella_op2d op, double *a64, float *a32, int cross
         a64[c] = axx; a64[ncell + c] = ayy; a64[2 * ncell + c] = axy; a64[3 * ncell + c] = ayx;
         a32[c] = (float)axx; a32[ncell + c] = (float)ayy;
         a32[2 * ncell + c] = (float)axy; a32[3 * ncell + c] = (float)ayx;
+        if (adf) {   // double-float planes (absent in the allocation-free path)
+            adf[c] = dfloat(axx); adf[ncell + c] = dfloat(ayy);
+            adf[2 * ncell + c] = dfloat(axy); adf[3 * ncell + c] = dfloat(ayx);
+        }
     }
 }
 
@@ -59,7 +63,7 @@ __global__ void k_pack2d_cells(bella_op2d op, double *a64, float *a32, int cross
 // duplicated periodic seam), used to project the pseudo-incompressible
 // solution onto the operator's range.
 __global__ void k_pack2d_nodes(bella_op2d op, double *dinv64, float *dinv32, double *hc64,
-                               float *hc32, double *z64) {
+                               float *hc32, double *z64, dfloat *dinvdf, dfloat *hcdf) {
     const int nx = op.nx, ny = op.ny;
     const size_t n = (size_t)nx * ny;
     for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < n;
@@ -69,6 +73,7 @@ __global__ void k_pack2d_nodes(bella_op2d op, double *dinv64, float *dinv32, dou
         const double h = op.hcenter ? op.hcenter[g] : 0.0;
         dinv64[g] = d; dinv32[g] = (float)d;
         hc64[g] = h;   hc32[g] = (float)h;
+        if (dinvdf) { dinvdf[g] = dfloat(d); hcdf[g] = dfloat(h); }
         double w = 1.0;
         if (!op.x_wall && (i == 0 || i == nx - 1)) w *= 0.5;
         if (!op.y_wall && (j == 0 || j == ny - 1)) w *= 0.5;
@@ -80,7 +85,7 @@ __global__ void k_pack2d_nodes(bella_op2d op, double *dinv64, float *dinv32, dou
 // fused stencil kernel
 // --------------------------------------------------------------------------
 template <typename T, int MODE, bool CROSS, bool HC>
-__global__ void __launch_bounds__(NTHREADS)
+__global__ void __launch_bounds__(NTHREADS, MINB)
 k_stencil2d(Op2D<T> op, StArgs<T> a, KState *ks, double *partials, unsigned *counter) {
     using AccT = typename Acc<T>::type;
     __shared__ T su[TY + 2][TX + 2];
@@ -116,6 +121,7 @@ k_stencil2d(Op2D<T> op, StArgs<T> a, KState *ks, double *partials, unsigned *cou
         const int tyi = tile / tilesx, txi = tile - tyi * tilesx;
         const int j0 = tyi * TY, i0 = txi * TX;
         // 1. stencil input u on the tile + one-node halo (wrap: duplicated seam)
+#pragma unroll
         for (int e = tid; e < (TY + 2) * (TX + 2); e += NTHREADS) {
             const int la = e / (TX + 2), lb = e - la * (TX + 2);
             int gj = j0 - 1 + la, gi = i0 - 1 + lb;
@@ -140,6 +146,7 @@ k_stencil2d(Op2D<T> op, StArgs<T> a, KState *ks, double *partials, unsigned *cou
         }
         __syncthreads();
         // 2. cell fluxes
+#pragma unroll
         for (int e = tid; e < (TY + 1) * (TX + 1); e += NTHREADS) {
             const int la = e / (TX + 1), lb = e - la * (TX + 1);
             const int cj = j0 + la, ci = i0 + lb;
@@ -221,6 +228,16 @@ Op2D<double> make_op<double>(bella_ws *ws) {
 }
 
 template <>
+Op2D<dfloat> make_op<dfloat>(bella_ws *ws) {
+    const size_t nc = (size_t)(ws->nx + 1) * (ws->ny + 1);
+    Op2D<dfloat> o;
+    o.nx = ws->nx; o.ny = ws->ny;
+    o.axx = ws->adf; o.ayy = ws->adf + nc; o.axy = ws->adf + 2 * nc; o.ayx = ws->adf + 3 * nc;
+    o.dinv = ws->dinvdf; o.hc = ws->hcdf;
+    return o;
+}
+
+template <>
 Op2D<float> make_op<float>(bella_ws *ws) {
     const size_t nc = (size_t)(ws->nx + 1) * (ws->ny + 1);
     Op2D<float> o;
@@ -232,7 +249,7 @@ Op2D<float> make_op<float>(bella_ws *ws) {
 
 int stencil_grid(int nx, int ny) {
     const int tiles = ((nx + TX - 1) / TX) * ((ny + TY - 1) / TY);
-    const int cap = NSM * 4;
+    const int cap = NSM * (GRID_PER_SM < 8 ? GRID_PER_SM : 8);   // partials hold NSM*8 CTAs
     return tiles < cap ? tiles : cap;
 }
 
@@ -258,8 +275,9 @@ int op2d_pack(bella_ws *ws, const bella_op2d *op, cudaStream_t s) {
     const size_t ncell = (size_t)(op->nx + 1) * (op->ny + 1);
     int g = (int)((ncell + 255) / 256);
     if (g > NSM * 8) g = NSM * 8;
-    k_pack2d_cells<<<g, 256, 0, s>>>(*op, ws->a64, ws->a32, ws->cross);
-    k_pack2d_nodes<<<g, 256, 0, s>>>(*op, ws->dinv64, ws->dinv32, ws->hc64, ws->hc32, ws->z64);
+    k_pack2d_cells<<<g, 256, 0, s>>>(*op, ws->a64, ws->a32, ws->adf, ws->cross);
+    k_pack2d_nodes<<<g, 256, 0, s>>>(*op, ws->dinv64, ws->dinv32, ws->hc64, ws->hc32, ws->z64, ws->dinvdf,
+                                     ws->hcdf);
     ws->launches += 2;
     return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
 }
@@ -289,8 +307,16 @@ void op2d_resid(bella_ws *ws, int prec, const void *x, const void *b, void *r, c
 }
 
 // one BiCGStab iteration: PDIR stencil, SDIR stencil, vector update
+// prec: 0 FP64, 1 FP32, 2 double-float
 void op2d_iteration(bella_ws *ws, int prec, cudaStream_t s) {
-    if (prec == 0) {
+    if (prec == 2) {
+        StArgs<dfloat> a = {};
+        a.r = ws->rdf; a.rh = ws->rhdf; a.y = ws->tdf;
+        a.p0 = ws->pdf[0]; a.p1 = ws->pdf[1]; a.v0 = ws->vdf[0]; a.v1 = ws->vdf[1];
+        launch_mode<dfloat, M_PDIR>(ws, a, s);
+        launch_mode<dfloat, M_SDIR>(ws, a, s);
+        launch_update<dfloat>(ws, s);
+    } else if (prec == 0) {
         StArgs<double> a = {};
         a.r = ws->r64k; a.rh = ws->rh64; a.y = ws->t64;
         a.p0 = ws->p64[0]; a.p1 = ws->p64[1]; a.v0 = ws->v64[0]; a.v1 = ws->v64[1];

@@ -25,7 +25,7 @@ import torch
 
 from . import _lib
 
-PRECISIONS = {"fp64": 0, "mixed": 1}
+PRECISIONS = {"fp64": 0, "mixed": 1, "df64": 2}
 _INFO = {_lib.BELLA_OK: 0, _lib.BELLA_BREAKDOWN: -10, _lib.BELLA_NONFINITE: -12}
 
 

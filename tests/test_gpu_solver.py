@@ -33,7 +33,7 @@ def _rb_system(tag):
 
 
 @pytest.mark.parametrize("tag", ["full", "half"])
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "df64", "mixed"])
 def test_rising_bubble_solve_matches_reference(tag, precision):
     """Same scaled system and tol (1e-10) as the reference's scipy solve."""
     from pybella_gb300 import linalg
@@ -70,6 +70,30 @@ def test_stratified_full_size_fp64_converges():
     assert true_relres(w["op"], xn, w["b"]) <= 1e-8
     assert st["relres"] <= 1e-8
     assert isinstance(x, torch.Tensor) and x.is_cuda
+
+
+def test_stratified_full_size_df64_converges():
+    """Double-float Krylov (FP32 pipe) reaches the FP64 true residual 1e-8."""
+    w = cases.stratified_2d(seed=0)
+    A = _op(w["op"])
+    x, st = A.solve(w["b"], tol=1e-8, maxiter=20000, precision="df64")
+    assert st["status"] == 0, st
+    xn = x.cpu().numpy()
+    assert true_relres(w["op"], xn, w["b"]) <= 1e-8
+    x64, s64 = A.solve(w["b"], tol=1e-8, maxiter=20000, precision="fp64")
+    assert s64["status"] == 0
+    assert _rel(xn, x64.cpu().numpy()) < 1e-6
+
+
+def test_df64_small_matches_scipy_tight():
+    from pybella_gb300 import linalg
+    w = cases.stratified_2d(seed=5, inx=257, iny=129)
+    A = _op(w["op"])
+    x_ref, info_ref, it_ref = bicgstab_legacy(w["op"], w["b"], 1e-11, 20000)
+    x, info = linalg.bicgstab(A, w["b"], tol=1e-11, maxiter=20000, precision="df64")
+    assert info == 0 and info_ref == 0
+    assert true_relres(w["op"], x, w["b"]) <= 1e-11
+    assert _rel(x, x_ref) < 1e-8
 
 
 def test_stratified_full_size_mixed_never_silent():
@@ -117,6 +141,10 @@ def test_status_codes_are_reported():
     assert info == -12
     _, info = linalg.bicgstab(A, b, tol=1e-8, maxiter=50, precision="mixed")
     assert info == -12
+    _, info = linalg.bicgstab(A, b, tol=1e-8, maxiter=50, precision="df64")
+    assert info == -12
+    _, info = linalg.bicgstab(A, w["b"], tol=1e-12, maxiter=3, precision="df64")
+    assert info > 0
 
 
 def test_callback_counts_iterations():
