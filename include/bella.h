@@ -57,6 +57,25 @@ typedef struct bella_op2d {
     const double *diag_inv;
 } bella_op2d;
 
+/*
+ * 3D 27-point nodal operator: the arithmetic of the reference's lap3D
+ * (laplacian.py:898-1026) with the 2D path's boundary conventions (the
+ * reference's own 3D glue, second_projection.py:183-203, cannot run):
+ *   hplusx, hplusy, hplusz : (nx+1)*(ny+1)*(nz+1) cells, C order (z fastest)
+ *   hcenter, diag_inv      : nx*ny*nz inner nodes, C order (z fastest)
+ * corrf = dt * coriolis_strength[0] (laplacian.py:894); 0 drops the cross
+ * terms.  hcenter may be NULL (== 0).  A wall axis zeroes the outer cell
+ * planes; a periodic axis wraps with the duplicated seam.
+ */
+typedef struct bella_op3d {
+    int nx, ny, nz;
+    int x_wall, y_wall, z_wall;
+    double dx, dy, dz;
+    double corrf;
+    const double *hplusx, *hplusy, *hplusz, *hcenter;
+    const double *diag_inv;
+} bella_op3d;
+
 /* Solver options.  tol/atol follow the reference's scipy call
  * (second_projection.py:230, scipy 1.7 legacy `tol`): converged when
  * ||b - A x|| <= max(atol, tol*||b||); ||b|| <= tol returns x = 0 at once. */
@@ -111,7 +130,11 @@ int  bella_ws_kernel_time(bella_ws *ws, int kind, double *total_ms, long long *c
  *      second_projection.py:205) ----------------------------------------- */
 int bella_op2d_set(bella_ws *ws, const bella_op2d *op, void *stream);
 
-/* y = A x with the prepared operator: FP64 (parity path) and FP32 planes.
+/* ---- 3D operator (replaces the closure returned by stencil_27pt,
+ *      laplacian.py:872-896) -------------------------------------------- */
+int bella_op3d_set(bella_ws *ws, const bella_op3d *op, void *stream);
+
+/* y = A x with the prepared operator (2D or 3D): FP64 (parity path) and FP32 planes.
  * Replaces one call of lap2D_gather_new (laplacian.py:546-746). */
 int bella_apply_f64(bella_ws *ws, const double *x, double *y, void *stream);
 int bella_apply_f32(bella_ws *ws, const float *x, float *y, void *stream);

@@ -78,15 +78,15 @@ def rising_bubble(inx=161, iny=81, delth=2.0, x0=0.0, y0=0.2, r0=0.2, tol=1e-10)
 # --------------------------------------------------------------------------
 # standalone solves on a stratified background
 # --------------------------------------------------------------------------
-def _kminus3_field(shape, rng):
-    """Zero-mean Gaussian random field with power spectrum ~ k^-3 (k=0 removed)."""
+def _kminus3_field(shape, rng, power=3.0):
+    """Zero-mean Gaussian random field with power spectrum ~ k^-power (k=0 removed)."""
     white = rng.standard_normal(shape)
     F = np.fft.rfftn(white)
     ks = [np.fft.fftfreq(n) * n for n in shape[:-1]] + [np.fft.rfftfreq(shape[-1]) * shape[-1]]
     K = np.sqrt(sum(np.meshgrid(*[k ** 2 for k in ks], indexing="ij")))
     amp = np.zeros_like(K)
     nz = K > 0
-    amp[nz] = K[nz] ** -1.5
+    amp[nz] = K[nz] ** (-0.5 * power)
     f = np.fft.irfftn(F * amp, s=shape)
     f -= f.mean()
     return f / f.std()
@@ -186,3 +186,84 @@ def null_weights_2d(grid):
     if grid.bdry[1] == n2.PERIODIC:
         wy[0] = wy[-1] = 0.5
     return np.outer(wx, wy)
+
+
+# --------------------------------------------------------------------------
+# 3D standalone solve (27-point), same construction as the 2D case
+# --------------------------------------------------------------------------
+SIGN_MODES_3D = ((1, 1, 1), (-1, -1, 1), (-1, 1, -1), (1, -1, -1), (-1, -1, -1))
+
+
+def null_modes_3d(shape, periodic):
+    """Sign-pattern null vectors of the pseudo-incompressible 27-point operator."""
+    nx, ny, nz = shape
+    i, j, k = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    out = []
+    for sx, sy, sz in SIGN_MODES_3D:
+        ok = all(not (per and s < 0 and (n - 1) % 2) for per, s, n in zip(periodic, (sx, sy, sz), shape))
+        if ok:
+            e = np.ones(shape)
+            if sx < 0:
+                e = e * (-1.0) ** i
+            if sy < 0:
+                e = e * (-1.0) ** j
+            if sz < 0:
+                e = e * (-1.0) ** k
+            out.append(e)
+    return np.stack(out)
+
+
+def trapezoid_weights(shape, periodic):
+    ws = []
+    for n, per in zip(shape, periodic):
+        w = np.ones(n)
+        if per:
+            w[0] = w[-1] = 0.5
+        ws.append(w)
+    return np.einsum("i,j,k->ijk", *ws)
+
+
+def stratified_3d(seed, nx=257, ny=129, nz=257, sigma=0.1, walls=(False, True, True)):
+    """Operands of one 3D 27-point pseudo-incompressible solve (C order, z fastest)."""
+    from oracle import nodal3d as n3
+    rng = np.random.default_rng(seed)
+    Msq, g, cor = _derived(grav=9.81, t_ref=1000.0)
+    prm = n2.Params(Msq=Msq, g=g, gamm=GAMM)
+    dx, dy, dz = 2.0 / (nx - 1), 1.0 / (ny - 1), 2.0 / (nz - 1)
+    yc = (np.arange(ny + 1) - 0.5) * dy
+    Yc, Pc = _stratified_profile(yc, prm)
+    coeff = prm.Gammainv * Pc * Yc
+    fac = np.exp(sigma * rng.standard_normal((nx + 1, ny + 1, nz + 1)))
+    for ax, wall in enumerate(walls):
+        if not wall:
+            n = fac.shape[ax] - 1
+            sl, src = [slice(None)] * 3, [slice(None)] * 3
+            sl[ax], src[ax] = 0, n - 1
+            fac[tuple(sl)] = fac[tuple(src)]
+            sl[ax], src[ax] = n, 1
+            fac[tuple(sl)] = fac[tuple(src)]
+    h = coeff[None, :, None] * fac
+    hc = np.zeros((nx, ny, nz))
+    dinv = n3.precon_diag_3d(h, h, h, hc, dx, dy, dz)
+    periodic = tuple(not w for w in walls)
+    # right-hand side: nodal divergence of a seeded Gaussian cell flux field
+    # with power ~k^-5 per component, so the divergence has ~k^-3 power; the
+    # divergence form makes it compatible with the operator's large null space
+    cshape = (nx + 1, ny + 1, nz + 1)
+    F = []
+    for _ in range(3):
+        f = _kminus3_field(cshape, rng, power=5.0)
+        for ax, per in enumerate(periodic):
+            if per:
+                n = cshape[ax] - 1
+                sl, src = [slice(None)] * 3, [slice(None)] * 3
+                sl[ax], src[ax] = 0, n - 1
+                f[tuple(sl)] = f[tuple(src)]
+                sl[ax], src[ax] = n, 1
+                f[tuple(sl)] = f[tuple(src)]
+        F.append(f)
+    b = n3.node_divergence(F[0], F[1], F[2], walls)
+    b = b / np.sqrt(np.mean(b * b))
+    op = n3.pack_27pt(h, h, h, hc, dinv, nx, ny, nz, dx, dy, dz, walls=walls)
+    return dict(op=op, b=b.reshape(-1) * dinv.reshape(-1), b_unscaled=b.reshape(-1), walls=walls,
+                periodic=periodic, seed=seed)

@@ -31,6 +31,15 @@ class Op2D(ctypes.Structure):
                 ("diag_inv", _dp)]
 
 
+class Op3D(ctypes.Structure):
+    """``bella_op3d``: 3D 27-point operands (device pointers, C order, z fastest)."""
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("x_wall", ctypes.c_int), ("y_wall", ctypes.c_int), ("z_wall", ctypes.c_int),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
+                ("corrf", ctypes.c_double),
+                ("hplusx", _dp), ("hplusy", _dp), ("hplusz", _dp), ("hcenter", _dp), ("diag_inv", _dp)]
+
+
 class SolveOpts(ctypes.Structure):
     """``bella_solve_opts``."""
     _fields_ = [("tol", ctypes.c_double), ("atol", ctypes.c_double),
@@ -63,6 +72,7 @@ SIGNATURES = {
     "bella_ws_kernel_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                             ctypes.POINTER(ctypes.c_longlong)]),
     "bella_op2d_set": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Op2D), ctypes.c_void_p]),
+    "bella_op3d_set": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Op3D), ctypes.c_void_p]),
     "bella_apply_f64": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, ctypes.c_void_p]),
     "bella_apply_f32": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, ctypes.c_void_p]),
     "bella_solve_opts_default": (None, [ctypes.POINTER(SolveOpts)]),

@@ -66,6 +66,22 @@ int  op2d_pack(bella_ws *ws, const bella_op2d *op, cudaStream_t s);
 void op2d_apply(bella_ws *ws, int prec, const void *x, void *y, cudaStream_t s);
 void op2d_resid(bella_ws *ws, int prec, const void *x, const void *b, void *r, cudaStream_t s);
 void op2d_iteration(bella_ws *ws, int prec, cudaStream_t s);
+int  stencil3d_grid(int nx, int ny, int nz);
+int  op3d_pack(bella_ws *ws, const bella_op3d *op, cudaStream_t s);
+void op3d_apply(bella_ws *ws, int prec, const void *x, void *y, cudaStream_t s);
+void op3d_resid(bella_ws *ws, int prec, const void *x, const void *b, void *r, cudaStream_t s);
+void op3d_iteration(bella_ws *ws, int prec, cudaStream_t s);
+
+// dimension dispatch of the prepared operator
+inline void op_apply(bella_ws *ws, int prec, const void *x, void *y, cudaStream_t s) {
+    if (ws->ndim == 3) op3d_apply(ws, prec, x, y, s); else op2d_apply(ws, prec, x, y, s);
+}
+inline void op_resid(bella_ws *ws, int prec, const void *x, const void *b, void *r, cudaStream_t s) {
+    if (ws->ndim == 3) op3d_resid(ws, prec, x, b, r, s); else op2d_resid(ws, prec, x, b, r, s);
+}
+inline void op_iteration(bella_ws *ws, int prec, cudaStream_t s) {
+    if (ws->ndim == 3) op3d_iteration(ws, prec, s); else op2d_iteration(ws, prec, s);
+}
 template <typename T> void launch_update(bella_ws *ws, cudaStream_t s);
 
 }  // namespace bella

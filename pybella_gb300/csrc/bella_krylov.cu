@@ -540,17 +540,56 @@ int bella_op2d_set(bella_ws *ws, const bella_op2d *op, void *stream) {
     return BELLA_OK;
 }
 
+int bella_op3d_set(bella_ws *ws, const bella_op3d *op, void *stream) {
+    if (!ws || !op) return set_err(BELLA_EINVAL, "bella_op3d_set: null argument");
+    if (op->nx < 3 || op->ny < 3 || op->nz < 3) return set_err(BELLA_EINVAL, "bella_op3d_set: nx, ny, nz must be >= 3");
+    if (!op->hplusx || !op->hplusy || !op->hplusz || !op->diag_inv)
+        return set_err(BELLA_EINVAL, "bella_op3d_set: hplusx, hplusy, hplusz, diag_inv are required");
+    if (!(op->dx > 0.0) || !(op->dy > 0.0) || !(op->dz > 0.0))
+        return set_err(BELLA_EINVAL, "bella_op3d_set: dx, dy, dz must be > 0");
+    BELLA_CUDA(cudaSetDevice(ws->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    const long long n = (long long)op->nx * op->ny * op->nz;
+    const size_t ncell = (size_t)(op->nx + 1) * (op->ny + 1) * (op->nz + 1);
+    if (ws->ndim != 3 || ws->nx != op->nx || ws->ny != op->ny || ws->nz != op->nz) {
+        free_op(ws);
+        BELLA_CUDA(cudaMalloc(&ws->a64, 5 * ncell * sizeof(double)));
+        BELLA_CUDA(cudaMalloc(&ws->a32, 5 * ncell * sizeof(float)));
+        BELLA_CUDA(cudaMalloc(&ws->adf, 5 * ncell * sizeof(dfloat)));
+        BELLA_CUDA(cudaMalloc(&ws->dinv64, n * sizeof(double)));
+        BELLA_CUDA(cudaMalloc(&ws->hc64, n * sizeof(double)));
+        BELLA_CUDA(cudaMalloc(&ws->z64, n * sizeof(double)));
+        BELLA_CUDA(cudaMalloc(&ws->dinv32, n * sizeof(float)));
+        BELLA_CUDA(cudaMalloc(&ws->hc32, n * sizeof(float)));
+        BELLA_CUDA(cudaMalloc(&ws->dinvdf, n * sizeof(dfloat)));
+        BELLA_CUDA(cudaMalloc(&ws->hcdf, n * sizeof(dfloat)));
+    }
+    int rc = ensure_vectors(ws, n);
+    if (rc != BELLA_OK) return rc;
+    ws->ndim = 3;
+    ws->nx = op->nx; ws->ny = op->ny; ws->nz = op->nz;
+    ws->n = n;
+    ws->cross = op->corrf != 0.0 ? 1 : 0;
+    ws->has_hc = op->hcenter != nullptr ? 1 : 0;
+    ws->singular = (!ws->has_hc && !ws->cross) ? 1 : 0;
+    ws->grid_stencil = stencil3d_grid(op->nx, op->ny, op->nz);
+    ws->grid_vec = vec_grid(n);
+    rc = op3d_pack(ws, op, s);
+    if (rc != BELLA_OK) return cuda_check(cudaGetLastError(), "op3d_pack");
+    return setup_null_space(ws, s, op->x_wall ? 0 : 1, op->y_wall ? 0 : 1, op->z_wall ? 0 : 1);
+}
+
 int bella_apply_f64(bella_ws *ws, const double *x, double *y, void *stream) {
     if (!ws || !x || !y) return set_err(BELLA_EINVAL, "bella_apply_f64: null argument");
     if (ws->ndim == 0) return set_err(BELLA_ENOOP, "bella_apply_f64: no operator set");
-    op2d_apply(ws, 0, x, y, (cudaStream_t)stream);
+    op_apply(ws, 0, x, y, (cudaStream_t)stream);
     return cuda_check(cudaGetLastError(), "bella_apply_f64");
 }
 
 int bella_apply_f32(bella_ws *ws, const float *x, float *y, void *stream) {
     if (!ws || !x || !y) return set_err(BELLA_EINVAL, "bella_apply_f32: null argument");
     if (ws->ndim == 0) return set_err(BELLA_ENOOP, "bella_apply_f32: no operator set");
-    op2d_apply(ws, 1, x, y, (cudaStream_t)stream);
+    op_apply(ws, 1, x, y, (cudaStream_t)stream);
     return cuda_check(cudaGetLastError(), "bella_apply_f32");
 }
 
@@ -615,7 +654,7 @@ static int run_inner(bella_ws *ws, int prec, const bella_solve_opts *o, cudaStre
             const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
             if (el > o->timeout_s) { *timed_out = 1; return BELLA_OK; }
         }
-        for (int k = 0; k < blk; ++k) op2d_iteration(ws, prec, s);
+        for (int k = 0; k < blk; ++k) op_iteration(ws, prec, s);
         BELLA_CUDA(cudaGetLastError());
     }
 }
@@ -627,7 +666,7 @@ static int solve_fp64(bella_ws *ws, const double *b, double *x, const bella_solv
                       std::chrono::steady_clock::time_point t0) {
     const long long n = ws->n;
     int timed_out = 0;
-    if (x_given) op2d_resid(ws, 0, x, b, ws->r64k, s);
+    if (x_given) op_resid(ws, 0, x, b, ws->r64k, s);
     k_init64<<<ws->grid_vec, VEC_BLOCK, 0, s>>>(n, b, x, ws->r64k, ws->rh64, x_given, o.tol, o.atol, maxiter,
                                                 ws->ks, ws->partials, ws->counter);
     ws->launches++;
@@ -656,7 +695,7 @@ static int solve_df(bella_ws *ws, const double *b, double *x, const bella_solve_
     const long long n = ws->n;
     const int gv = ws->grid_vec;
     int timed_out = 0;
-    if (x_given) op2d_resid(ws, 0, x, b, ws->r64, s);
+    if (x_given) op_resid(ws, 0, x, b, ws->r64, s);
     k_init_df<<<gv, VEC_BLOCK, 0, s>>>(n, b, x, ws->r64, ws->xdf, ws->rdf, ws->rhdf, x_given, o.tol, o.atol,
                                        maxiter, ws->ks, ws->partials, ws->counter);
     ws->launches++;
@@ -673,7 +712,7 @@ static int solve_df(bella_ws *ws, const double *b, double *x, const bella_solve_
         st->detail = k.pad[0];
         if (timed_out || k.status != BELLA_OK || k.iter >= maxiter) break;
         const double bnorm = k.dot_aux, atol = k.atol;
-        op2d_resid(ws, 0, x, b, ws->r64, s);
+        op_resid(ws, 0, x, b, ws->r64, s);
         st->matvecs += 1;
         rc = sync_state(ws, s);
         if (rc != BELLA_OK) return rc;
@@ -753,7 +792,7 @@ int bella_bicgstab(bella_ws *ws, const double *b, double *x, const bella_solve_o
             NullSpace ns = ws->ns;
             if (!o.project_null) ns.nm = 0;
             const bool proj = ns.nm > 0;
-            op2d_resid(ws, 0, x, b, ws->r64, s);
+            op_resid(ws, 0, x, b, ws->r64, s);
             rc = sync_state(ws, s);
             if (rc != BELLA_OK) return rc;
             double rnorm = sqrt(ws->ks_host->dot_aux2);
@@ -786,7 +825,7 @@ int bella_bicgstab(bella_ws *ws, const double *b, double *x, const bella_solve_o
                 k_ir_update<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->x32, rnorm, ws->z64, ns, ws->ks,
                                                      ws->partials, ws->counter);
                 ws->launches++;
-                op2d_resid(ws, 0, x, b, ws->r64, s);
+                op_resid(ws, 0, x, b, ws->r64, s);
                 st.matvecs += 1;
                 rc = sync_state(ws, s);
                 if (rc != BELLA_OK) return rc;
@@ -820,7 +859,7 @@ int bella_bicgstab(bella_ws *ws, const double *b, double *x, const bella_solve_o
 done:
     {
         // true FP64 residual of the returned x
-        op2d_resid(ws, 0, x, b, ws->r64, s);
+        op_resid(ws, 0, x, b, ws->r64, s);
         rc = sync_state(ws, s);
         if (rc != BELLA_OK) return rc;
         const double rn = sqrt(ws->ks_host->dot_aux2);

@@ -58,46 +58,12 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
 
 
-class NodalHelmholtz2D:
-    """Device-resident 9-point nodal operator (the reference's ``lap2D_gather_new``).
+class _NodalOperator:
+    """Device-resident nodal operator: matvec and solves through libbella_gb300."""
 
-    Operands are the reference's packed arrays (laplacian.py:517-527):
-    ``hplusx, hplusy`` and the four Coriolis coefficient arrays on
-    ``(ny+1)*(nx+1)`` cells, ``hcenter`` and ``diag_inv`` on ``ny*nx`` nodes,
-    all flattened y-major.  NumPy or torch inputs are accepted; they are copied
-    once to the GPU and packed into flux planes (FP64 and FP32).
-    """
-
-    def __init__(self, hplusx, hplusy, hcenter, coriolis, diag_inv, nx, ny, dx, dy,
-                 x_wall, y_wall, device=None, ws=None):
-        self.dev = _device(device) if ws is None else torch.device("cuda", ws.device)
-        self.nx, self.ny = int(nx), int(ny)
-        self.n = self.nx * self.ny
-        self.shape = (self.n, self.n)
-        self.dtype = np.dtype(np.float64)
-        cxx, cyy, cxy, cyx = coriolis
-        d = self.dev
-        self._hx = _to_dev(hplusx, d)
-        self._hy = _to_dev(hplusy, d)
-        self._hc = None if _all_zero(hcenter) else _to_dev(hcenter, d)
-        self._cxx = _to_dev(cxx, d)
-        self._cyy = _to_dev(cyy, d)
-        self._cxy = None if (_all_zero(cxy) and _all_zero(cyx)) else _to_dev(cxy, d)
-        self._cyx = None if self._cxy is None else _to_dev(cyx, d)
-        self._dinv = _to_dev(diag_inv, d)
-        nc = (self.nx + 1) * (self.ny + 1)
-        for t, m, name in ((self._hx, nc, "hplusx"), (self._hy, nc, "hplusy"), (self._cxx, nc, "cxx"),
-                           (self._cyy, nc, "cyy"), (self._dinv, self.n, "diag_inv")):
-            if t.numel() != m:
-                raise ValueError("%s has %d entries, expected %d" % (name, t.numel(), m))
-        self.singular = self._hc is None and self._cxy is None
-        self.ws = _lib.Workspace(d.index) if ws is None else ws
-        self._op = _lib.Op2D(self.nx, self.ny, int(bool(x_wall)), int(bool(y_wall)), float(dx), float(dy),
-                             _ptr(self._hx), _ptr(self._hy), _ptr(self._hc), _ptr(self._cxx),
-                             _ptr(self._cyy), _ptr(self._cxy), _ptr(self._cyx), _ptr(self._dinv))
-        with torch.cuda.device(d):
-            _lib.check(self.ws._lib.bella_op2d_set(self.ws.handle, ctypes.byref(self._op), _stream(d)),
-                       "bella_op2d_set")
+    dev = None
+    n = 0
+    ws = None
 
     # -- matvec ------------------------------------------------------------
     def matvec(self, p):
@@ -161,6 +127,85 @@ class NodalHelmholtz2D:
             _lib.check(self.ws._lib.bella_bicgstab(self.ws.handle, _ptr(bd), _ptr(x), ctypes.byref(o),
                                                    ctypes.byref(st), _stream(self.dev)), "bella_bicgstab")
         return x, st.as_dict()
+
+
+class NodalHelmholtz2D(_NodalOperator):
+    """Device-resident 9-point nodal operator (the reference's ``lap2D_gather_new``).
+
+    Operands are the reference's packed arrays (laplacian.py:517-527):
+    ``hplusx, hplusy`` and the four Coriolis coefficient arrays on
+    ``(ny+1)*(nx+1)`` cells, ``hcenter`` and ``diag_inv`` on ``ny*nx`` nodes,
+    all flattened y-major.  NumPy or torch inputs are accepted; they are copied
+    once to the GPU and packed into flux planes (FP64, FP32, double-float).
+    """
+
+    def __init__(self, hplusx, hplusy, hcenter, coriolis, diag_inv, nx, ny, dx, dy,
+                 x_wall, y_wall, device=None, ws=None):
+        self.dev = _device(device) if ws is None else torch.device("cuda", ws.device)
+        self.nx, self.ny = int(nx), int(ny)
+        self.n = self.nx * self.ny
+        self.shape = (self.n, self.n)
+        self.dtype = np.dtype(np.float64)
+        cxx, cyy, cxy, cyx = coriolis
+        d = self.dev
+        self._hx = _to_dev(hplusx, d)
+        self._hy = _to_dev(hplusy, d)
+        self._hc = None if _all_zero(hcenter) else _to_dev(hcenter, d)
+        self._cxx = _to_dev(cxx, d)
+        self._cyy = _to_dev(cyy, d)
+        self._cxy = None if (_all_zero(cxy) and _all_zero(cyx)) else _to_dev(cxy, d)
+        self._cyx = None if self._cxy is None else _to_dev(cyx, d)
+        self._dinv = _to_dev(diag_inv, d)
+        nc = (self.nx + 1) * (self.ny + 1)
+        for t, m, name in ((self._hx, nc, "hplusx"), (self._hy, nc, "hplusy"), (self._cxx, nc, "cxx"),
+                           (self._cyy, nc, "cyy"), (self._dinv, self.n, "diag_inv")):
+            if t.numel() != m:
+                raise ValueError("%s has %d entries, expected %d" % (name, t.numel(), m))
+        self.singular = self._hc is None and self._cxy is None
+        self.ws = _lib.Workspace(d.index) if ws is None else ws
+        self._op = _lib.Op2D(self.nx, self.ny, int(bool(x_wall)), int(bool(y_wall)), float(dx), float(dy),
+                             _ptr(self._hx), _ptr(self._hy), _ptr(self._hc), _ptr(self._cxx),
+                             _ptr(self._cyy), _ptr(self._cxy), _ptr(self._cyx), _ptr(self._dinv))
+        with torch.cuda.device(d):
+            _lib.check(self.ws._lib.bella_op2d_set(self.ws.handle, ctypes.byref(self._op), _stream(d)),
+                       "bella_op2d_set")
+
+
+class NodalHelmholtz3D(_NodalOperator):
+    """Device-resident 27-point nodal operator (the arithmetic of the reference's ``lap3D``).
+
+    Operands: ``hplusx, hplusy, hplusz`` on ``(nx+1)(ny+1)(nz+1)`` cells and
+    ``hcenter``, ``diag_inv`` on ``nx*ny*nz`` inner nodes, C order over
+    (x, y, z) (second_projection.py:224); ``corrf = dt*coriolis_strength[0]``
+    (laplacian.py:894).  Walls per axis; other axes wrap with the duplicated seam.
+    """
+
+    def __init__(self, hplusx, hplusy, hplusz, hcenter, diag_inv, nx, ny, nz, dx, dy, dz,
+                 walls=(False, True, True), corrf=0.0, device=None, ws=None):
+        self.dev = _device(device) if ws is None else torch.device("cuda", ws.device)
+        self.nx, self.ny, self.nz = int(nx), int(ny), int(nz)
+        self.n = self.nx * self.ny * self.nz
+        self.shape = (self.n, self.n)
+        self.dtype = np.dtype(np.float64)
+        d = self.dev
+        self._hx = _to_dev(hplusx, d)
+        self._hy = _to_dev(hplusy, d)
+        self._hz = _to_dev(hplusz, d)
+        self._hc = None if _all_zero(hcenter) else _to_dev(hcenter, d)
+        self._dinv = _to_dev(diag_inv, d)
+        nc = (self.nx + 1) * (self.ny + 1) * (self.nz + 1)
+        for t, m, name in ((self._hx, nc, "hplusx"), (self._hy, nc, "hplusy"), (self._hz, nc, "hplusz"),
+                           (self._dinv, self.n, "diag_inv")):
+            if t.numel() != m:
+                raise ValueError("%s has %d entries, expected %d" % (name, t.numel(), m))
+        self.singular = self._hc is None and float(corrf) == 0.0
+        self.ws = _lib.Workspace(d.index) if ws is None else ws
+        self._op = _lib.Op3D(self.nx, self.ny, self.nz, int(bool(walls[0])), int(bool(walls[1])),
+                             int(bool(walls[2])), float(dx), float(dy), float(dz), float(corrf),
+                             _ptr(self._hx), _ptr(self._hy), _ptr(self._hz), _ptr(self._hc), _ptr(self._dinv))
+        with torch.cuda.device(d):
+            _lib.check(self.ws._lib.bella_op3d_set(self.ws.handle, ctypes.byref(self._op), _stream(d)),
+                       "bella_op3d_set")
 
 
 class LinearOperator:

@@ -117,3 +117,80 @@ def operator_bytes_2d(w):
     n = w["nx"] * w["ny"]
     nc = (w["nx"] + 1) * (w["ny"] + 1)
     return 8 * (4 * nc + 2 * n)
+
+
+def _power_field(shape, power, gen, device):
+    """Zero-mean Gaussian random field with power spectrum ~ k^-power (k = 0 removed)."""
+    white = torch.randn(shape, generator=gen, device=device, dtype=torch.float64)
+    F = torch.fft.rfftn(white)
+    ks = [torch.fft.fftfreq(n, device=device, dtype=torch.float64) * n for n in shape[:-1]]
+    ks.append(torch.fft.rfftfreq(shape[-1], device=device, dtype=torch.float64) * shape[-1])
+    grids = torch.meshgrid(*ks, indexing="ij")
+    K = torch.sqrt(sum(g * g for g in grids))
+    amp = torch.where(K > 0, K.clamp_min(1e-30) ** (-0.5 * power), torch.zeros_like(K))
+    f = torch.fft.irfftn(F * amp, s=shape)
+    f = f - f.mean()
+    return f / f.std()
+
+
+def _box3(a):
+    return (a[:-1, :-1, :-1] + a[1:, :-1, :-1] + a[:-1, 1:, :-1] + a[1:, 1:, :-1]
+            + a[:-1, :-1, 1:] + a[1:, :-1, 1:] + a[:-1, 1:, 1:] + a[1:, 1:, 1:])
+
+
+def stratified_3d(seed, nx=257, ny=129, nz=257, sigma=0.1, walls=(False, True, True), device="cuda"):
+    """Operands of one 3D 27-point solve (257x129x257 by default), C order (z fastest).
+
+    Cells carry the stratified pseudo-incompressible coefficient (same
+    background as :func:`stratified_2d`) times a seeded log-normal factor;
+    the right-hand side is the nodal divergence (the operator's own node sums)
+    of three seeded Gaussian cell flux fields with power ~k^-5, i.e. a field
+    with ~k^-3 power that is compatible with the 27-point operator's null
+    space (constants and hourglass modes).  Scaled by the 3D Jacobi diagonal
+    of ``precon_diag_prepare`` (laplacian.py:1323-1356).
+    """
+    dev = torch.device(device)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(int(seed))
+    Msq, g = _consts()
+    dx, dy, dz = 2.0 / (nx - 1), 1.0 / (ny - 1), 2.0 / (nz - 1)
+    yc = (torch.arange(ny + 1, device=dev, dtype=torch.float64) - 0.5) * dy
+    Yc, Pc = _profile(yc, g)
+    coeff = GAMM / (GAMM - 1.0) * Pc * Yc
+    cshape = (nx + 1, ny + 1, nz + 1)
+
+    def periodic_copy(f):
+        for ax, wall in enumerate(walls):
+            if not wall:
+                n = cshape[ax] - 1
+                f.index_copy_(ax, torch.tensor([0, n], device=dev),
+                              f.index_select(ax, torch.tensor([n - 1, 1], device=dev)))
+        return f
+
+    fac = periodic_copy(torch.exp(sigma * torch.randn(cshape, generator=gen, device=dev, dtype=torch.float64)))
+    h = (coeff[None, :, None] * fac).contiguous()
+    c = 0.0625
+    S = _box3(h)
+    diag = -(c / dx ** 2) * S - (c / dy ** 2) * S - (c / (dx * dy)) * S - (c / (dy * dx)) * S - (c / dz ** 2) * S
+    dinv = 1.0 / diag
+    F = []
+    for _ in range(3):
+        f = periodic_copy(_power_field(cshape, 5.0, gen, dev))
+        for ax, wall in enumerate(walls):
+            if wall:
+                f.index_fill_(ax, torch.tensor([0, cshape[ax] - 1], device=dev), 0.0)
+        F.append(f)
+    fx, fy, fz = F
+    xs = (fx[1:, :-1, :-1] + fx[1:, :-1, 1:] + fx[1:, 1:, :-1] + fx[1:, 1:, 1:]) - \
+         (fx[:-1, :-1, :-1] + fx[:-1, :-1, 1:] + fx[:-1, 1:, :-1] + fx[:-1, 1:, 1:])
+    ys = (fy[:-1, 1:, :-1] + fy[1:, 1:, :-1] + fy[:-1, 1:, 1:] + fy[1:, 1:, 1:]) - \
+         (fy[:-1, :-1, :-1] + fy[1:, :-1, :-1] + fy[:-1, :-1, 1:] + fy[1:, :-1, 1:])
+    zs = (fz[:-1, :-1, 1:] + fz[:-1, 1:, 1:] + fz[1:, :-1, 1:] + fz[1:, 1:, 1:]) - \
+         (fz[:-1, :-1, :-1] + fz[:-1, 1:, :-1] + fz[1:, :-1, :-1] + fz[1:, 1:, :-1])
+    b = xs + ys + zs
+    b = b / torch.sqrt(torch.mean(b * b))
+    dflat = dinv.reshape(-1).contiguous()
+    hf = h.reshape(-1)
+    return dict(hplusx=hf, hplusy=hf, hplusz=hf, hcenter=None, diag_inv=dflat,
+                b=(b.reshape(-1) * dflat).contiguous(), nx=nx, ny=ny, nz=nz, dx=dx, dy=dy, dz=dz,
+                walls=tuple(walls), corrf=0.0, seed=int(seed))

@@ -1,0 +1,98 @@
+"""GPU parity of the 3D 27-point operator and solves against the 3D oracle.
+
+The reference's 3D glue cannot run, so these comparisons are against the
+oracle's restatement of lap3D (parity unpinned, see oracle/nodal3d.py).
+"""
+import numpy as np
+import pytest
+
+from oracle import cases, nodal3d as n3
+from oracle.krylov import bicgstab_legacy, true_relres
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def _dev_op(op):
+    from pybella_gb300.linalg import NodalHelmholtz3D
+    return NodalHelmholtz3D(op["hplusx"], op["hplusy"], op["hplusz"], op["hcenter"], op["diag_inv"],
+                            op["nx"], op["ny"], op["nz"], op["dx"], op["dy"], op["dz"],
+                            walls=op["walls"], corrf=op["corrf"])
+
+
+def _random_op(rng, nx, ny, nz, walls, corrf=0.0, hc=False):
+    shp = (nx + 1, ny + 1, nz + 1)
+    hx, hy, hz = (rng.uniform(0.5, 2.0, shp) for _ in range(3))
+    hcen = -rng.uniform(0.1, 1.0, (nx, ny, nz)) if hc else np.zeros((nx, ny, nz))
+    dinv = n3.precon_diag_3d(hx, hy, hz, hcen, 0.2, 0.3, 0.25)
+    return n3.pack_27pt(hx, hy, hz, hcen, dinv, nx, ny, nz, 0.2, 0.3, 0.25, walls=walls, corrf=corrf)
+
+
+@pytest.mark.parametrize("shape,walls,corrf,hc", [
+    ((9, 7, 11), (False, True, True), 0.0, False),
+    ((13, 10, 40), (False, True, False), 0.4, True),
+    ((37, 20, 70), (True, True, True), 0.0, True),
+])
+def test_apply3d_f64_f32_vs_oracle(shape, walls, corrf, hc):
+    import torch
+    rng = np.random.default_rng(sum(shape))
+    op = _random_op(rng, *shape, walls, corrf, hc)
+    A = _dev_op(op)
+    p = rng.standard_normal(A.n)
+    ref = n3.lap3d(p, op)
+    assert _rel(A.matvec(p), ref) < 1e-13
+    y32 = A.matvec_f32(torch.tensor(p, dtype=torch.float32, device="cuda")).double().cpu().numpy()
+    assert _rel(y32, ref) < 5e-6
+
+
+def test_null_modes_3d_exact_on_device():
+    rng = np.random.default_rng(4)
+    nx, ny, nz = 17, 10, 33
+    op = _random_op(rng, nx, ny, nz, (False, True, True))
+    A = _dev_op(op)
+    i, j, k = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    f = rng.standard_normal(nx)
+    f[-1] = f[0]
+    for e in (np.ones((nx, ny, nz)), (-1.0) ** (i + j + k), f[i] * (-1.0) ** (j + k)):
+        assert np.abs(A.matvec(e.reshape(-1))).max() == 0.0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "df64", "mixed"])
+def test_solve3d_small_vs_scipy(precision):
+    w = cases.stratified_3d(1, 33, 17, 33)
+    A = _dev_op(w["op"])
+    x_ref, info_ref, _ = bicgstab_legacy(w["op"], w["b"], 1e-10, 20000)
+    x, st = A.solve(w["b"], tol=1e-10, maxiter=20000, precision=precision)
+    assert st["status"] == 0, st
+    xn = x.cpu().numpy()
+    assert true_relres(w["op"], xn, w["b"]) <= 1e-10
+    if precision != "mixed" or st["fallback"]:
+        assert _rel(xn, x_ref) < 1e-6
+
+
+def test_solve3d_mid_size_df64_converges():
+    """129x65x129: the device solve reaches the FP64 true residual 1e-8."""
+    from pybella_gb300 import workloads
+    w = workloads.stratified_3d(0, 129, 65, 129)
+    A = _dev_op(w)
+    x, st = A.solve(w["b"], tol=1e-8, maxiter=60000, precision="df64")
+    assert st["status"] == 0, st
+    assert st["relres"] <= 1e-8
+
+
+def test_solve3d_full_size_progress_is_reported():
+    """257x129x257: a bounded plain BiCGStab run reports its true residual honestly.
+
+    Plain BiCGStab needs tens of thousands of iterations here (the 27-point
+    operator's hourglass null space); the test bounds the run and checks that
+    the status says 'not converged' with a finite, reduced FP64 residual.
+    """
+    from pybella_gb300 import workloads
+    w = workloads.stratified_3d(0)
+    A = _dev_op(w)
+    x, st = A.solve(w["b"], tol=1e-8, maxiter=2000, precision="df64")
+    assert st["status"] in (0, 1), st
+    assert np.isfinite(st["relres"]) and st["relres"] < 1.0

@@ -1,0 +1,81 @@
+"""Self-consistency of the 3D 27-point oracle (the reference's 3D path cannot run).
+
+Parity of the 3D operator is unpinned: these tests pin it to the reference's
+working 2D operator and to structural properties instead.
+"""
+import numpy as np
+
+from oracle import nodal2d as n2
+from oracle import nodal3d as n3
+
+
+def _rand_cells(rng, shape):
+    return rng.uniform(0.5, 2.0, shape)
+
+
+def test_z_invariant_field_reproduces_2d_operator():
+    rng = np.random.default_rng(0)
+    nx, ny, nz = 9, 7, 5
+    dx, dy, dz = 0.3, 0.2, 0.25
+    hx2 = _rand_cells(rng, (ny + 1, nx + 1))
+    hy2 = _rand_cells(rng, (ny + 1, nx + 1))
+    op2 = dict(hplusx=hx2.reshape(-1), hplusy=hy2.reshape(-1), hcenter=np.zeros(nx * ny),
+               cor=(np.ones(hx2.size), np.ones(hx2.size), np.zeros(hx2.size), np.zeros(hx2.size)),
+               diag_inv=np.ones(nx * ny), nx=nx, ny=ny, dx=dx, dy=dy, x_wall=False, y_wall=True)
+    hx3 = np.repeat(hx2.T[:, :, None], nz + 1, axis=2)
+    hy3 = np.repeat(hy2.T[:, :, None], nz + 1, axis=2)
+    hz3 = _rand_cells(rng, (nx + 1, ny + 1, 1)).repeat(nz + 1, axis=2)
+    op3 = n3.pack_27pt(hx3, hy3, hz3, np.zeros(nx * ny * nz), np.ones(nx * ny * nz), nx, ny, nz, dx, dy, dz,
+                       walls=(False, True, False), corrf=0.3)
+    p2 = rng.standard_normal((ny, nx))
+    p3 = np.repeat(p2.T[:, :, None], nz, axis=2)
+    y2 = n2.lap2d_gather(p2.reshape(-1), op2).reshape(ny, nx)
+    y3 = n3.lap3d(p3.reshape(-1), op3).reshape(nx, ny, nz)
+    for k in range(nz):
+        np.testing.assert_allclose(y3[:, :, k], y2.T, rtol=1e-12, atol=1e-12 * np.abs(y2).max())
+
+
+def _op3(rng, nx, ny, nz, walls, corrf=0.0, hc=False):
+    shp = (nx + 1, ny + 1, nz + 1)
+    hx, hy, hz = (_rand_cells(rng, shp) for _ in range(3))
+    for h in (hx, hy, hz):            # periodic copies of the ghost-like cells
+        for ax, w in enumerate(walls):
+            if not w:
+                n = shp[ax] - 1
+                sl = [slice(None)] * 3
+                src = [slice(None)] * 3
+                sl[ax], src[ax] = 0, n - 1
+                h[tuple(sl)] = h[tuple(src)]
+                sl[ax], src[ax] = n, 1
+                h[tuple(sl)] = h[tuple(src)]
+    hcen = -rng.uniform(0.1, 1.0, nx * ny * nz) if hc else np.zeros(nx * ny * nz)
+    dinv = n3.precon_diag_3d(hx, hy, hz, hcen.reshape(nx, ny, nz), 0.2, 0.3, 0.25)
+    return n3.pack_27pt(hx, hy, hz, hcen, dinv, nx, ny, nz, 0.2, 0.3, 0.25, walls=walls, corrf=corrf)
+
+
+def test_null_modes_of_pseudo_incompressible_3d():
+    rng = np.random.default_rng(1)
+    nx, ny, nz = 9, 6, 7
+    op = _op3(rng, nx, ny, nz, (False, True, True))
+    i, j, k = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    for e in (np.ones((nx, ny, nz)), (-1.0) ** (i + j), (-1.0) ** (i + k), (-1.0) ** (j + k),
+              (-1.0) ** (i + j + k)):
+        assert np.abs(n3.lap3d(e.reshape(-1), op)).max() < 1e-12
+    assert np.abs(n3.lap3d(((-1.0) ** i).reshape(-1), op)).max() > 1.0
+
+
+def test_unscaled_operator_is_weighted_symmetric_on_seam_consistent_vectors():
+    rng = np.random.default_rng(2)
+    nx, ny, nz = 9, 6, 7
+    op = _op3(rng, nx, ny, nz, (False, True, True))
+    op["diag_inv"] = np.ones(nx * ny * nz)
+    w = np.ones((nx, ny, nz))
+    w[0] = w[-1] = 0.5
+    u = rng.standard_normal((nx, ny, nz))
+    v = rng.standard_normal((nx, ny, nz))
+    u[-1] = u[0]
+    v[-1] = v[0]
+    Au = n3.lap3d(u.reshape(-1), op).reshape(u.shape)
+    Av = n3.lap3d(v.reshape(-1), op).reshape(v.shape)
+    a, b = np.sum(w * v * Au), np.sum(w * u * Av)
+    assert abs(a - b) < 1e-11 * (abs(a) + abs(b))
