@@ -148,6 +148,33 @@ int  bella_bicgstab(bella_ws *ws, const double *b, double *x,
                     const bella_solve_opts *opts, bella_solve_stats *stats,
                     void *stream);
 
+/* ---- the whole 2D projection on the device (replaces
+ *      euler_backward_non_advective_impl_part, second_projection.py:97-277):
+ * cell boundary data, coefficients, Coriolis factors, Jacobi diagonal, nodal
+ * divergence right-hand side, the solve, ghost nodes, momentum / rhoX
+ * correction and p2 update, all on device arrays in the reference's layout
+ * (NumPy C order over (x, y); cells (inx+3)x(iny+3), nodes (inx+4)x(iny+4)).
+ * Sol (and Sol0, whose ghost cells are refreshed) and p2 are updated in
+ * place.  Returns the solver status or a negative error. */
+typedef struct bella_proj2d {
+    int inx, iny;                 /* grid nodes per direction (ud.inx, ud.iny)       */
+    int x_wall, y_wall;           /* 0: periodic, 1: wall                              */
+    double dx, dy, dt;
+    double Msq, g, gamm, nonhydro, compressibility;
+    double coriolis[3];           /* ud.coriolis_strength                             */
+    int is_compressible;
+    int pad_;
+    double *rho, *rhou, *rhov, *rhow, *rhoY, *rhoX;          /* Sol                    */
+    double *rho0, *rhou0, *rhov0, *rhow0, *rhoY0, *rhoX0;    /* Sol0 or all NULL       */
+    double *p2;                   /* mpv.p2_nodes                                     */
+    const double *hydro_rhoY0;    /* mpv.HydroState.rhoY0 (iny+3 cell rows)            */
+    const double *S0n;            /* mpv.HydroState_n.S0 (iny+4 node rows)             */
+    const double *strat_inv;      /* 1/ud.stratification(elem.y) (iny+3)               */
+    double *rhs_out;              /* mpv.rhs (inx+2)x(iny+2) or NULL                   */
+} bella_proj2d;
+int bella_projection2d(bella_ws *ws, const bella_proj2d *args, const bella_solve_opts *opts,
+                       bella_solve_stats *stats, void *stream);
+
 /* ---- allocation-free variant (no counterpart in the reference) ----------
  * FP64 BiCGStab of bella_bicgstab (precision 0 only) on the reference-packed
  * 2D operands, for callers that cannot allocate device memory while they run

@@ -40,6 +40,18 @@ class Op3D(ctypes.Structure):
                 ("hplusx", _dp), ("hplusy", _dp), ("hplusz", _dp), ("hcenter", _dp), ("diag_inv", _dp)]
 
 
+class Proj2D(ctypes.Structure):
+    """``bella_proj2d``: device arrays of one 2D projection (reference layout)."""
+    _fields_ = [("inx", ctypes.c_int), ("iny", ctypes.c_int), ("x_wall", ctypes.c_int), ("y_wall", ctypes.c_int),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dt", ctypes.c_double),
+                ("Msq", ctypes.c_double), ("g", ctypes.c_double), ("gamm", ctypes.c_double),
+                ("nonhydro", ctypes.c_double), ("compressibility", ctypes.c_double),
+                ("coriolis", ctypes.c_double * 3), ("is_compressible", ctypes.c_int), ("pad_", ctypes.c_int)] + \
+        [(k, _dp) for k in ("rho", "rhou", "rhov", "rhow", "rhoY", "rhoX",
+                            "rho0", "rhou0", "rhov0", "rhow0", "rhoY0", "rhoX0",
+                            "p2", "hydro_rhoY0", "S0n", "strat_inv", "rhs_out")]
+
+
 class SolveOpts(ctypes.Structure):
     """``bella_solve_opts``."""
     _fields_ = [("tol", ctypes.c_double), ("atol", ctypes.c_double),
@@ -78,6 +90,8 @@ SIGNATURES = {
     "bella_solve_opts_default": (None, [ctypes.POINTER(SolveOpts)]),
     "bella_bicgstab": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, ctypes.POINTER(SolveOpts),
                                       ctypes.POINTER(SolveStats), ctypes.c_void_p]),
+    "bella_projection2d": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Proj2D), ctypes.POINTER(SolveOpts),
+                                          ctypes.POINTER(SolveStats), ctypes.c_void_p]),
     "bella_bicgstab2d_noalloc": (ctypes.c_int, [ctypes.POINTER(Op2D), _dp, _dp, ctypes.POINTER(SolveOpts),
                                                 ctypes.POINTER(SolveStats), ctypes.c_void_p]),
 }

@@ -239,6 +239,9 @@ struct bella_ws {
     bella::KState *ks_host;   // pinned mirror
     int grid_stencil, grid_vec;
     long long launches;
+    // scratch of the device projection (bella_projection2d)
+    double *proj_buf;
+    size_t proj_cap;
     // optional per-kernel timing with CUDA events (bella_ws_profile)
     int prof;
     struct Prof {

@@ -410,6 +410,7 @@ int bella_ws_destroy(bella_ws *ws) {
     cudaSetDevice(ws->device);
     if (ws->prof) bella_ws_profile(ws, 0);
     free_op(ws);
+    cudaFree(ws->proj_buf);
     cudaFree(ws->vbase);
     cudaFree(ws->partials);
     cudaFree(ws->counter);

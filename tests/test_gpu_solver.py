@@ -2,7 +2,7 @@
 import numpy as np
 import pytest
 
-from conftest import golden
+from conftest import golden, rb_background
 from oracle import cases, nodal2d as n2
 from oracle.krylov import bicgstab_legacy, true_relres
 
@@ -21,7 +21,7 @@ def _op(op):
 
 def _rb_system(tag):
     d = np.load(golden("rising_bubble_step0.npz"))
-    grid, prm, _, _, hn, hc, sf = cases.rising_bubble()
+    grid, prm, hn, hc, sf = rb_background(d)
     fields = ["rho", "rhou", "rhov", "rhow", "rhoY", "rhoX"]
     Sol = {k: d["%s_in_%s" % (tag, k)].copy() for k in fields}
     Sol0 = None

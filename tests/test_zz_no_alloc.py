@@ -14,7 +14,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from conftest import golden
+from conftest import golden, rb_background
 from oracle import cases, nodal2d as n2
 from oracle.krylov import true_relres
 
@@ -23,7 +23,7 @@ pytestmark = pytest.mark.gpu
 
 def _system():
     d = np.load(golden("rising_bubble_step0.npz"))
-    grid, prm, _, _, hn, hc, sf = cases.rising_bubble()
+    grid, prm, hn, hc, sf = rb_background(d)
     fields = ["rho", "rhou", "rhov", "rhow", "rhoY", "rhoX"]
     Sol = {k: d["full_in_" + k].copy() for k in fields}
     p2 = d["full_p2_in"].copy()
