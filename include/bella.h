@@ -175,6 +175,22 @@ typedef struct bella_proj2d {
 int bella_projection2d(bella_ws *ws, const bella_proj2d *args, const bella_solve_opts *opts,
                        bella_solve_stats *stats, void *stream);
 
+/* ---- learned preconditioner: 6-layer 3x3x3 CNN, 32 channels, BF16 weights and
+ *      activations, FP32 accumulation, tensor-core implicit GEMM (no counterpart
+ *      in the reference, which has no learned component) ------------------- */
+typedef struct bella_cnn bella_cnn;
+int       bella_cnn_create(bella_cnn **net, int device, long long max_voxels);
+int       bella_cnn_destroy(bella_cnn *net);
+long long bella_cnn_param_count(void);
+/* FP32 parameters, layer by layer W[27][cin][cout] (tap = (dx+1)*9+(dy+1)*3+(dz+1)) then b[cout];
+ * host or device pointer */
+int       bella_cnn_set_params(bella_cnn *net, const float *params, void *stream);
+int       bella_cnn_get_params(bella_cnn *net, float *params, void *stream);
+/* out = CNN(in * in_scale) / in_scale on an nx x ny x nz grid (C order, z fastest) */
+int       bella_cnn_forward(bella_cnn *net, int nx, int ny, int nz, const float *in, float *out,
+                            float in_scale, void *stream);
+long long bella_cnn_launches(const bella_cnn *net);
+
 /* ---- allocation-free variant (no counterpart in the reference) ----------
  * FP64 BiCGStab of bella_bicgstab (precision 0 only) on the reference-packed
  * 2D operands, for callers that cannot allocate device memory while they run

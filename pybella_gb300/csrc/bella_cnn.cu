@@ -1,0 +1,528 @@
+// bella_cnn.cu -- the learned preconditioner's CNN on the tensor cores.
+//
+// Six 3x3x3 convolutions with zero padding, 1 -> 32 -> 32 -> 32 -> 32 -> 32 -> 1
+// channels, ReLU after the first five; BF16 weights and activations, FP32
+// accumulation.  Every layer is an implicit GEMM
+//   out[v, co] = sum_{tap, ci} in[v + off(tap), ci] * W[tap, ci, co]
+// (M = voxels, N = output channels, K = 27 taps x input channels) run with
+// mma.sync m16n8k16 BF16 tensor-core instructions.  A persistent CTA keeps the
+// layer's weights in shared memory ([tap][co][ci], swizzled for ldmatrix) and
+// loops over 4x4x16-voxel tiles: it stages the tile plus a one-voxel halo of
+// the channels-last input (swizzled 16-byte chunks), each warp owns two 16-voxel
+// rows along z and accumulates 16 x COUT in registers, then adds the bias,
+// applies ReLU and stores BF16 (or FP32 for the last layer).  The input layer
+// pads 1 channel to 16 and the output layer 1 channel to 8 (tensor-core shapes).
+// Gradients for training: input gradients reuse the forward kernel with the
+// taps mirrored and (ci, co) swapped; weight gradients are FP32 reductions on
+// the CUDA cores.
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cuda_bf16.h>
+
+#include "bella_internal.cuh"
+
+namespace bella {
+
+constexpr int CT_X = 4, CT_Y = 4, CT_Z = 16;                // output tile (voxels)
+constexpr int CH_X = CT_X + 2, CH_Y = CT_Y + 2, CH_Z = CT_Z + 2;
+constexpr int CH_VOX = CH_X * CH_Y * CH_Z;                    // 648 halo voxels
+constexpr int CNN_THREADS = 256;                              // 8 warps x 2 m-tiles = 16 rows of 16 voxels
+
+__device__ __forceinline__ int tap_of(int dx, int dy, int dz) { return (dx + 1) * 9 + (dy + 1) * 3 + (dz + 1); }
+
+// byte offset of (row, 16-byte chunk) in a swizzled [rows][CIN] bf16 array
+template <int CIN>
+__device__ __forceinline__ uint32_t swz(int row, int chunk) {
+    constexpr int NCH = CIN / 8;             // 16-byte chunks per row (2 or 4)
+    const int p = (NCH == 4) ? (chunk ^ ((row >> 1) & 3)) : (chunk ^ ((row >> 2) & 1));
+    return (uint32_t)(row * (CIN * 2) + p * 16);
+}
+
+__device__ __forceinline__ void ldmatrix_x4(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(addr));
+}
+
+__device__ __forceinline__ void ldmatrix_x2(uint32_t addr, uint32_t &r0, uint32_t &r1) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n" : "=r"(r0), "=r"(r1) : "r"(addr));
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1) {
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+                 "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// Implicit-GEMM 3x3x3 convolution.  in: [nvox][CIN] bf16 (channels-last),
+// W: [27][COUT][CIN] bf16, bias: [COUT] f32.  out: [nvox][COUT] bf16, or
+// [nvox] f32 (channel 0 only, scaled by out_scale) when OUTF32.
+// FLIP mirrors the taps (input-gradient pass).  mask (optional, [nvox][COUT]
+// bf16): the output is multiplied by (mask > 0) -- the ReLU derivative.
+template <int CIN, int COUT, bool RELU, bool OUTF32, bool FLIP>
+__global__ void __launch_bounds__(CNN_THREADS)
+k_conv3d(int nx, int ny, int nz, int xseg, const __nv_bfloat16 *__restrict__ in, const __nv_bfloat16 *__restrict__ W,
+         const float *__restrict__ bias, void *out, float out_scale, const __nv_bfloat16 *__restrict__ mask) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    unsigned char *sW = smem;                                   // 27 * COUT * CIN * 2 bytes
+    unsigned char *sIn = smem + 27 * COUT * CIN * 2;            // CH_VOX * CIN * 2 bytes
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // weights -> shared memory (swizzled rows = (tap, co))
+    for (int e = tid; e < 27 * COUT * (CIN / 8); e += CNN_THREADS) {
+        const int row = e / (CIN / 8), ch = e - row * (CIN / 8);
+        const uint4 v = *reinterpret_cast<const uint4 *>(W + (size_t)row * CIN + ch * 8);
+        *reinterpret_cast<uint4 *>(sW + swz<CIN>(row, ch)) = v;
+    }
+    const int tx = (nx + CT_X - 1) / CT_X, ty = (ny + CT_Y - 1) / CT_Y, tz = (nz + CT_Z - 1) / CT_Z;
+    const long long ntiles = (long long)tx * ty * tz;
+    const uint32_t sW_base = (uint32_t)__cvta_generic_to_shared(sW);
+    const uint32_t sIn_base = (uint32_t)__cvta_generic_to_shared(sIn);
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int tzi = (int)(tile % tz);
+        const long long rest = tile / tz;
+        const int tyi = (int)(rest % ty), txi = (int)(rest / ty);
+        const int i0 = txi * CT_X, j0 = tyi * CT_Y, k0 = tzi * CT_Z;
+        __syncthreads();   // previous tile's reads of sIn are done (and sW is written)
+        // halo tile of the input (zero outside the domain)
+        for (int e = tid; e < CH_VOX * (CIN / 8); e += CNN_THREADS) {
+            const int vox = e / (CIN / 8), ch = e - vox * (CIN / 8);
+            const int la = vox / (CH_Y * CH_Z), rem = vox - la * (CH_Y * CH_Z), lb = rem / CH_Z, lc = rem - lb * CH_Z;
+            const int gi = i0 - 1 + la, gj = j0 - 1 + lb, gk = k0 - 1 + lc;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            // a batch of crops lies along x in segments of xseg voxels (multiple of the tile
+            // width): the halo never reaches into a neighbouring crop
+            const bool same_seg = gi >= 0 && (gi / xseg) == (i0 / xseg);
+            if (same_seg && gi < nx && gj >= 0 && gj < ny && gk >= 0 && gk < nz) {
+                const size_t g = ((size_t)gi * ny + gj) * nz + gk;
+                v = *reinterpret_cast<const uint4 *>(in + g * CIN + ch * 8);
+            }
+            *reinterpret_cast<uint4 *>(sIn + swz<CIN>(vox, ch)) = v;
+        }
+        __syncthreads();
+        // warp -> two m-tiles (16 z-voxels each) of the 4x4 (x, y) rows
+        float acc[2][COUT / 8][4];
+#pragma unroll
+        for (int m = 0; m < 2; ++m)
+#pragma unroll
+            for (int n = 0; n < COUT / 8; ++n)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[m][n][q] = 0.f;
+        const int rowA = (lane & 7) + ((lane >> 3) & 1) * 8;   // ldmatrix row supplied by this lane
+        const int chA = lane >> 4;                              // k half supplied by this lane
+#pragma unroll 1
+        for (int tap = 0; tap < 27; ++tap) {
+            const int dx = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dz = tap % 3 - 1;
+            const int wtap = FLIP ? tap_of(-dx, -dy, -dz) : tap;
+#pragma unroll
+            for (int ks = 0; ks < CIN / 16; ++ks) {
+                // B fragments for all n-tiles of this (tap, k-step)
+                uint32_t b[COUT / 8][2];
+                if (COUT >= 16) {
+#pragma unroll
+                    for (int np = 0; np < COUT / 16; ++np) {
+                        const int brow = wtap * COUT + np * 16 + (lane & 7) + ((lane >> 4) & 1) * 8;
+                        const int bch = ks * 2 + ((lane >> 3) & 1);
+                        ldmatrix_x4(sW_base + swz<CIN>(brow, bch), b[2 * np][0], b[2 * np][1], b[2 * np + 1][0],
+                                    b[2 * np + 1][1]);
+                    }
+                } else {
+                    const int brow = wtap * COUT + (lane & 7);
+                    const int bch = ks * 2 + ((lane >> 3) & 1);
+                    ldmatrix_x2(sW_base + swz<CIN>(brow, bch), b[0][0], b[0][1]);
+                }
+#pragma unroll
+                for (int m = 0; m < 2; ++m) {
+                    const int mt = warp * 2 + m;                  // 0..15 -> (x, y) row of the tile
+                    const int la = mt / CT_Y, lb = mt - la * CT_Y;
+                    const int vox = ((la + 1 + dx) * CH_Y + (lb + 1 + dy)) * CH_Z + (1 + dz) + rowA;
+                    uint32_t a0, a1, a2, a3;
+                    ldmatrix_x4(sIn_base + swz<CIN>(vox, ks * 2 + chA), a0, a1, a2, a3);
+#pragma unroll
+                    for (int n = 0; n < COUT / 8; ++n) mma_bf16(acc[m][n], a0, a1, a2, a3, b[n][0], b[n][1]);
+                }
+            }
+        }
+        // epilogue: bias, ReLU (or ReLU-derivative mask), store
+#pragma unroll
+        for (int m = 0; m < 2; ++m) {
+            const int mt = warp * 2 + m;
+            const int la = mt / CT_Y, lb = mt - la * CT_Y;
+            const int gi = i0 + la, gj = j0 + lb;
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                const int gk = k0 + (lane >> 2) + half * 8;
+                if (gi >= nx || gj >= ny || gk >= nz) continue;
+                const size_t g = ((size_t)gi * ny + gj) * nz + gk;
+#pragma unroll
+                for (int n = 0; n < COUT / 8; ++n) {
+                    const int co = n * 8 + (lane & 3) * 2;
+                    float v0 = acc[m][n][half * 2 + 0], v1 = acc[m][n][half * 2 + 1];
+                    if (bias) { v0 += bias[co]; v1 += bias[co + 1]; }
+                    if (RELU) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
+                    if (mask) {
+                        const __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162 *>(mask + g * COUT + co);
+                        if (!(__bfloat162float(mk.x) > 0.f)) v0 = 0.f;
+                        if (!(__bfloat162float(mk.y) > 0.f)) v1 = 0.f;
+                    }
+                    if (OUTF32) {
+                        if (co == 0) reinterpret_cast<float *>(out)[g] = v0 * out_scale;
+                    } else {
+                        *reinterpret_cast<__nv_bfloat162 *>(reinterpret_cast<__nv_bfloat16 *>(out) + g * COUT + co) =
+                            __floats2bfloat162_rn(v0, v1);
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <int CIN, int COUT>
+constexpr size_t conv_smem() { return (size_t)27 * COUT * CIN * 2 + (size_t)CH_VOX * CIN * 2; }
+
+// residual (f32) -> channels-last bf16 with 16 channels (channel 0 = in * scale)
+__global__ void k_pack_in(long long n, const float *in, float scale, __nv_bfloat16 *out) {
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
+        uint4 z = make_uint4(0u, 0u, 0u, 0u);
+        uint4 *o = reinterpret_cast<uint4 *>(out + v * 16);
+        __nv_bfloat16 h = __float2bfloat16_rn(in[v] * scale);
+        uint4 first = z;
+        first.x = (uint32_t)__bfloat16_as_ushort(h);
+        o[0] = first;
+        o[1] = z;
+    }
+}
+
+// ---- training kernels (FP32 on the CUDA cores) ------------------------------------
+// Weight gradients dW[tap][ci][co] = sum_v in[v + off(tap)][ci] * g[v][co] and bias
+// gradients db[co] = sum_v g[v][co].  A persistent CTA stages a 4x4x16 tile of the
+// gradient and the one-voxel halo of the input in shared memory (FP32) and keeps
+// the 27 taps x (its ci, co pairs) in registers; partial sums are added to the
+// global gradient once per CTA.
+template <int CIN, int CINR, int COUT, int COUTR, typename GT>
+__global__ void __launch_bounds__(256)
+k_wgrad(int nx, int ny, int nz, int xseg, const __nv_bfloat16 *__restrict__ in, const GT *__restrict__ g,
+        float *dW, float *db) {
+    extern __shared__ __align__(16) float fsm[];
+    float *sIn = fsm;                         // [CH_VOX][CINR]
+    float *sG = fsm + CH_VOX * CINR;          // [256][COUTR]
+    constexpr int NP = CINR * COUTR;          // (ci, co) pairs
+    constexpr int PPT = (NP + 255) / 256;     // pairs per thread
+    const int tid = threadIdx.x;
+    float acc[PPT][27];
+    float accb[PPT];
+#pragma unroll
+    for (int q = 0; q < PPT; ++q) {
+        accb[q] = 0.f;
+#pragma unroll
+        for (int t = 0; t < 27; ++t) acc[q][t] = 0.f;
+    }
+    const int tx = (nx + CT_X - 1) / CT_X, ty = (ny + CT_Y - 1) / CT_Y, tz = (nz + CT_Z - 1) / CT_Z;
+    const long long ntiles = (long long)tx * ty * tz;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int tzi = (int)(tile % tz);
+        const long long rest = tile / tz;
+        const int tyi = (int)(rest % ty), txi = (int)(rest / ty);
+        const int i0 = txi * CT_X, j0 = tyi * CT_Y, k0 = tzi * CT_Z;
+        __syncthreads();
+        for (int e = tid; e < CH_VOX * CINR; e += 256) {
+            const int vox = e / CINR, ci = e - vox * CINR;
+            const int la = vox / (CH_Y * CH_Z), rem = vox - la * (CH_Y * CH_Z), lb = rem / CH_Z, lc = rem - lb * CH_Z;
+            const int gi = i0 - 1 + la, gj = j0 - 1 + lb, gk = k0 - 1 + lc;
+            float v = 0.f;
+            if (gi >= 0 && (gi / xseg) == (i0 / xseg) && gi < nx && gj >= 0 && gj < ny && gk >= 0 && gk < nz)
+                v = __bfloat162float(in[(((size_t)gi * ny + gj) * nz + gk) * CIN + ci]);
+            sIn[e] = v;
+        }
+        for (int e = tid; e < 256 * COUTR; e += 256) {
+            const int vox = e / COUTR, co = e - vox * COUTR;
+            const int la = vox / (CT_Y * CT_Z), rem = vox - la * (CT_Y * CT_Z), lb = rem / CT_Z, lc = rem - lb * CT_Z;
+            const int gi = i0 + la, gj = j0 + lb, gk = k0 + lc;
+            float v = 0.f;
+            if (gi < nx && gj < ny && gk < nz) {
+                const size_t gg = (((size_t)gi * ny + gj) * nz + gk) * COUT + co;
+                if constexpr (sizeof(GT) == 2) v = __bfloat162float(g[gg]); else v = (float)g[gg];
+            }
+            sG[e] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) {
+            const int pr = tid + q * 256;
+            if (pr >= NP) break;
+            const int ci = pr / COUTR, co = pr - ci * COUTR;
+            for (int vox = 0; vox < 256; ++vox) {
+                const int la = vox / (CT_Y * CT_Z), rem = vox - la * (CT_Y * CT_Z), lb = rem / CT_Z, lc = rem - lb * CT_Z;
+                const float gv = sG[vox * COUTR + co];
+                accb[q] += gv;
+                const int hb = ((la + 1) * CH_Y + (lb + 1)) * CH_Z + (lc + 1);
+#pragma unroll
+                for (int t = 0; t < 27; ++t) {
+                    const int dx = t / 9 - 1, dy = (t / 3) % 3 - 1, dz = t % 3 - 1;
+                    acc[q][t] = fmaf(sIn[(hb + (dx * CH_Y + dy) * CH_Z + dz) * CINR + ci], gv, acc[q][t]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < PPT; ++q) {
+        const int pr = tid + q * 256;
+        if (pr >= NP) break;
+        const int ci = pr / COUTR, co = pr - ci * COUTR;
+#pragma unroll
+        for (int t = 0; t < 27; ++t) atomicAdd(&dW[((size_t)t * CINR + ci) * COUTR + co], acc[q][t]);
+        if (ci == 0 && db) atomicAdd(&db[co], accb[q]);
+    }
+}
+
+template <int CINR, int COUTR>
+constexpr size_t wgrad_smem() { return sizeof(float) * ((size_t)CH_VOX * CINR + 256 * COUTR); }
+
+// gradient through the last layer (32 -> 1): d5[v][ci] = (act5[v][ci] > 0) *
+// sum_tap g6[v - off(tap)] * W5[tap][ci]  (bf16 weights as in the forward pass)
+__global__ void k_last_dgrad(int nx, int ny, int nz, int xseg, const float *g6, const __nv_bfloat16 *wk5,
+                             const __nv_bfloat16 *act5, __nv_bfloat16 *d5) {
+    const long long n = (long long)nx * ny * nz;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(v % nz);
+        const long long t0 = v / nz;
+        const int j = (int)(t0 % ny), i = (int)(t0 / ny);
+        float acc[32];
+#pragma unroll
+        for (int c = 0; c < 32; ++c) acc[c] = 0.f;
+        for (int t = 0; t < 27; ++t) {
+            const int dx = t / 9 - 1, dy = (t / 3) % 3 - 1, dz = t % 3 - 1;
+            const int si = i - dx, sj = j - dy, sk = k - dz;
+            if (si < 0 || si >= nx || (si / xseg) != (i / xseg) || sj < 0 || sj >= ny || sk < 0 || sk >= nz) continue;
+            const float gv = g6[((long long)si * ny + sj) * nz + sk];
+            const __nv_bfloat16 *w = wk5 + (size_t)t * 8 * 32;      // [tap][co=0..7][ci]: row co = 0
+#pragma unroll
+            for (int c = 0; c < 32; ++c) acc[c] = fmaf(gv, __bfloat162float(w[c]), acc[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < 32; c += 2) {
+            const __nv_bfloat162 a = *reinterpret_cast<const __nv_bfloat162 *>(act5 + v * 32 + c);
+            const float x0 = __bfloat162float(a.x) > 0.f ? acc[c] : 0.f;
+            const float x1 = __bfloat162float(a.y) > 0.f ? acc[c + 1] : 0.f;
+            *reinterpret_cast<__nv_bfloat162 *>(d5 + v * 32 + c) = __floats2bfloat162_rn(x0, x1);
+        }
+    }
+}
+
+// per-sample normalised squared error: L = (1/B) sum_s ||y_s - e_s||^2 / ||e_s||^2,
+// g = dL/dy; samples are contiguous blocks of nsv voxels
+__global__ void k_loss(long long n, long long nsv, int B, const float *y, const float *e, const float *inv_e2,
+                       float *g, float *loss) {
+    float l = 0.f;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
+        const int smp = (int)(v / nsv);
+        const float d = y[v] - e[v];
+        g[v] = 2.f * d * inv_e2[smp] / (float)B;
+        l += d * d * inv_e2[smp] / (float)B;
+    }
+    l = warp_sum((double)l);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, l);
+}
+
+// Adam (Kingma & Ba) on the FP32 master parameters
+__global__ void k_adam(long long n, float *p, const float *g, float *m, float *v, float lr, float b1, float b2,
+                       float eps, float bc1, float bc2) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+    }
+}
+
+}  // namespace bella
+
+// ============================================================================
+// C ABI
+// ============================================================================
+using namespace bella;
+
+struct bella_cnn {
+    int device;
+    long long max_vox;
+    // FP32 master parameters in the oracle layout W[l][27][cin][cout], b[l][cout]
+    float *params;            // device
+    long long nparams;
+    // BF16 kernel weights [27][coutp][cinp] (and mirrored/transposed for input gradients)
+    __nv_bfloat16 *wk[6], *wkT[6];
+    float *bias[6];           // padded biases
+    __nv_bfloat16 *act[6];    // act[0]: packed input (16 ch); act[l]: output of layer l-1 (32 ch)
+    __nv_bfloat16 *gact[2];   // gradient ping-pong buffers (32 ch, bf16)
+    float *gtmp;              // f32 gradient of the current layer output [nvox][32]
+    float *out_tmp;
+    long long launches;
+};
+
+static const int CIN_L[6] = {1, 32, 32, 32, 32, 32};
+static const int COUT_L[6] = {32, 32, 32, 32, 32, 1};
+static const int CINP_L[6] = {16, 32, 32, 32, 32, 32};
+static const int COUTP_L[6] = {32, 32, 32, 32, 32, 8};
+
+static long long param_count() {
+    long long n = 0;
+    for (int l = 0; l < 6; ++l) n += 27LL * CIN_L[l] * COUT_L[l] + COUT_L[l];
+    return n;
+}
+
+static long long w_off(int l) {
+    long long n = 0;
+    for (int k = 0; k < l; ++k) n += 27LL * CIN_L[k] * COUT_L[k] + COUT_L[k];
+    return n;
+}
+
+// master f32 [27][cin][cout] -> kernel bf16 [27][coutp][cinp] and the mirrored
+// transpose [27][cinp][coutp] used by the input-gradient pass
+__global__ void k_cast_weights(const float *W, int cin, int cout, int cinp, int coutp, __nv_bfloat16 *wk,
+                               __nv_bfloat16 *wkT) {
+    const int total = 27 * cinp * coutp;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        const int tap = e / (cinp * coutp), r = e - tap * cinp * coutp, co = r / cinp, ci = r - co * cinp;
+        float v = 0.f;
+        if (ci < cin && co < cout) v = W[((size_t)tap * cin + ci) * cout + co];
+        wk[((size_t)tap * coutp + co) * cinp + ci] = __float2bfloat16_rn(v);
+        // transpose: rows (tap, ci) of length coutp -> used as [27][CIN'=coutp][COUT'=cinp]
+        wkT[((size_t)tap * cinp + ci) * coutp + co] = __float2bfloat16_rn(v);
+    }
+}
+
+__global__ void k_cast_bias(const float *b, int cout, int coutp, float *bp) {
+    for (int e = threadIdx.x; e < coutp; e += blockDim.x) bp[e] = e < cout ? b[e] : 0.f;
+}
+
+static std::string g_cnn_err;
+
+extern "C" {
+
+int bella_cnn_create(bella_cnn **out, int device, long long max_voxels) {
+    if (!out || max_voxels <= 0) return BELLA_EINVAL;
+    if (cudaSetDevice(device) != cudaSuccess) return BELLA_ECUDA;
+    bella_cnn *net = new bella_cnn();
+    memset(net, 0, sizeof(*net));
+    net->device = device;
+    net->max_vox = max_voxels;
+    net->nparams = param_count();
+    bool ok = cudaMalloc(&net->params, net->nparams * sizeof(float)) == cudaSuccess;
+    for (int l = 0; l < 6 && ok; ++l) {
+        const size_t nw = 27ULL * CINP_L[l] * COUTP_L[l];
+        ok = cudaMalloc(&net->wk[l], nw * 2) == cudaSuccess && cudaMalloc(&net->wkT[l], nw * 2) == cudaSuccess &&
+             cudaMalloc(&net->bias[l], 32 * sizeof(float)) == cudaSuccess;
+    }
+    ok = ok && cudaMalloc(&net->act[0], (size_t)max_voxels * 16 * 2) == cudaSuccess;
+    for (int l = 1; l < 6 && ok; ++l) ok = cudaMalloc(&net->act[l], (size_t)max_voxels * 32 * 2) == cudaSuccess;
+    for (int k = 0; k < 2 && ok; ++k) ok = cudaMalloc(&net->gact[k], (size_t)max_voxels * 32 * 2) == cudaSuccess;
+    ok = ok && cudaMalloc(&net->gtmp, (size_t)max_voxels * 32 * sizeof(float)) == cudaSuccess;
+    ok = ok && cudaMalloc(&net->out_tmp, (size_t)max_voxels * sizeof(float)) == cudaSuccess;
+    ok = ok && cudaMemset(net->params, 0, net->nparams * sizeof(float)) == cudaSuccess;
+    if (ok) {
+        ok = cudaFuncSetAttribute(k_conv3d<16, 32, true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)conv_smem<16, 32>()) == cudaSuccess &&
+             cudaFuncSetAttribute(k_conv3d<32, 32, true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)conv_smem<32, 32>()) == cudaSuccess &&
+             cudaFuncSetAttribute(k_conv3d<32, 8, false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)conv_smem<32, 8>()) == cudaSuccess &&
+             cudaFuncSetAttribute(k_conv3d<32, 32, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)conv_smem<32, 32>()) == cudaSuccess &&
+             cudaFuncSetAttribute(k_conv3d<16, 32, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)conv_smem<16, 32>()) == cudaSuccess;
+    }
+    if (!ok) {
+        g_cnn_err = "bella_cnn_create: allocation or attribute failed";
+        // best-effort cleanup
+        cudaFree(net->params);
+        for (int l = 0; l < 6; ++l) { cudaFree(net->wk[l]); cudaFree(net->wkT[l]); cudaFree(net->bias[l]); cudaFree(net->act[l]); }
+        cudaFree(net->gact[0]); cudaFree(net->gact[1]); cudaFree(net->gtmp); cudaFree(net->out_tmp);
+        delete net;
+        return BELLA_ECUDA;
+    }
+    *out = net;
+    return BELLA_OK;
+}
+
+int bella_cnn_destroy(bella_cnn *net) {
+    if (!net) return BELLA_OK;
+    cudaSetDevice(net->device);
+    cudaFree(net->params);
+    for (int l = 0; l < 6; ++l) { cudaFree(net->wk[l]); cudaFree(net->wkT[l]); cudaFree(net->bias[l]); cudaFree(net->act[l]); }
+    cudaFree(net->gact[0]); cudaFree(net->gact[1]); cudaFree(net->gtmp); cudaFree(net->out_tmp);
+    delete net;
+    return BELLA_OK;
+}
+
+long long bella_cnn_param_count(void) { return param_count(); }
+
+// refresh the BF16 kernel weights from the FP32 master parameters (device)
+static int cnn_sync_weights(bella_cnn *net, cudaStream_t s) {
+    for (int l = 0; l < 6; ++l) {
+        const float *W = net->params + w_off(l);
+        const float *b = W + 27LL * CIN_L[l] * COUT_L[l];
+        k_cast_weights<<<64, 256, 0, s>>>(W, CIN_L[l], COUT_L[l], CINP_L[l], COUTP_L[l], net->wk[l], net->wkT[l]);
+        k_cast_bias<<<1, 32, 0, s>>>(b, COUT_L[l], COUTP_L[l], net->bias[l]);
+        net->launches += 2;
+    }
+    return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
+}
+
+// params: host or device FP32 array of bella_cnn_param_count() values, layer by
+// layer W[27][cin][cout] then b[cout]
+int bella_cnn_set_params(bella_cnn *net, const float *params, void *stream) {
+    if (!net || !params) return BELLA_EINVAL;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (cudaMemcpyAsync(net->params, params, net->nparams * sizeof(float), cudaMemcpyDefault, s) != cudaSuccess)
+        return BELLA_ECUDA;
+    return cnn_sync_weights(net, s);
+}
+
+int bella_cnn_get_params(bella_cnn *net, float *params, void *stream) {
+    if (!net || !params) return BELLA_EINVAL;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (cudaMemcpyAsync(params, net->params, net->nparams * sizeof(float), cudaMemcpyDefault, s) != cudaSuccess)
+        return BELLA_ECUDA;
+    return BELLA_OK;
+}
+
+static int conv_grid(int nx, int ny, int nz) {
+    const long long tiles = (long long)((nx + CT_X - 1) / CT_X) * ((ny + CT_Y - 1) / CT_Y) * ((nz + CT_Z - 1) / CT_Z);
+    const long long cap = (long long)NSM * 2;
+    return (int)(tiles < cap ? tiles : cap);
+}
+
+static void cnn_forward_layers(bella_cnn *net, int nx, int ny, int nz, int xseg, float *out, float out_scale,
+                               cudaStream_t s) {
+    const int g = conv_grid(nx, ny, nz);
+    k_conv3d<16, 32, true, false, false><<<g, CNN_THREADS, conv_smem<16, 32>(), s>>>(
+        nx, ny, nz, xseg, net->act[0], net->wk[0], net->bias[0], net->act[1], 1.f, nullptr);
+    for (int l = 1; l <= 4; ++l)
+        k_conv3d<32, 32, true, false, false><<<g, CNN_THREADS, conv_smem<32, 32>(), s>>>(
+            nx, ny, nz, xseg, net->act[l], net->wk[l], net->bias[l], net->act[l + 1], 1.f, nullptr);
+    k_conv3d<32, 8, false, true, false><<<g, CNN_THREADS, conv_smem<32, 8>(), s>>>(
+        nx, ny, nz, xseg, net->act[5], net->wk[5], net->bias[5], out, out_scale, nullptr);
+    net->launches += 6;
+}
+
+// out = CNN(in * in_scale) / in_scale on an (nx, ny, nz) grid (C order, z fastest)
+int bella_cnn_forward(bella_cnn *net, int nx, int ny, int nz, const float *in, float *out, float in_scale,
+                      void *stream) {
+    if (!net || !in || !out || nx < 1 || ny < 1 || nz < 1 || !(in_scale > 0.f)) return BELLA_EINVAL;
+    const long long n = (long long)nx * ny * nz;
+    if (n > net->max_vox) return BELLA_EINVAL;
+    cudaStream_t s = (cudaStream_t)stream;
+    k_pack_in<<<vec_grid(n), 256, 0, s>>>(n, in, in_scale, net->act[0]);
+    cnn_forward_layers(net, nx, ny, nz, nx, out, 1.f / in_scale, s);
+    net->launches += 1;
+    if (cudaGetLastError() != cudaSuccess) return BELLA_ECUDA;
+    return BELLA_OK;
+}
+
+long long bella_cnn_launches(const bella_cnn *net) { return net ? net->launches : 0; }
+
+}  // extern "C"
