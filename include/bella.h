@@ -177,18 +177,33 @@ int bella_projection2d(bella_ws *ws, const bella_proj2d *args, const bella_solve
 
 /* ---- learned preconditioner: 6-layer 3x3x3 CNN, 32 channels, BF16 weights and
  *      activations, FP32 accumulation, tensor-core implicit GEMM (no counterpart
- *      in the reference, which has no learned component) ------------------- */
+ *      in the reference, which has no learned component) -------------------
+ * block = 1: the convolutions run on the node grid (1 input, 1 output channel).
+ * block = 2: they run on the grid of 2x2x2 node blocks, the 8 nodes of a block
+ *   being 8 channels (sub-node ((a*2+b)*2+d) for offsets (a,b,d)).
+ * capacity: voxels of the grid the convolutions run on, summed over the samples
+ *   of a training batch (ceil(nx/block)*ceil(ny/block)*ceil(nz/block)*nsamples). */
 typedef struct bella_cnn bella_cnn;
-int       bella_cnn_create(bella_cnn **net, int device, long long max_voxels);
+int       bella_cnn_create(bella_cnn **net, int device, int block, long long capacity);
 int       bella_cnn_destroy(bella_cnn *net);
-long long bella_cnn_param_count(void);
+long long bella_cnn_param_count(int block);
+int       bella_cnn_block(const bella_cnn *net);
 /* FP32 parameters, layer by layer W[27][cin][cout] (tap = (dx+1)*9+(dy+1)*3+(dz+1)) then b[cout];
- * host or device pointer */
+ * host or device pointer; set_params resets the Adam state */
 int       bella_cnn_set_params(bella_cnn *net, const float *params, void *stream);
 int       bella_cnn_get_params(bella_cnn *net, float *params, void *stream);
-/* out = CNN(in * in_scale) / in_scale on an nx x ny x nz grid (C order, z fastest) */
+/* out = CNN(in * in_scale) / in_scale on the nodes of an nx x ny x nz grid (C order,
+ * z fastest); device FP32 arrays */
 int       bella_cnn_forward(bella_cnn *net, int nx, int ny, int nz, const float *in, float *out,
                             float in_scale, void *stream);
+/* grads = d/dparams sum(gout * CNN(in)); out (optional) = CNN(in); device FP32 arrays */
+int       bella_cnn_gradients(bella_cnn *net, int nx, int ny, int nz, const float *in, const float *gout,
+                              float *grads, float *out, void *stream);
+/* one Adam step on nsamples (in, target) pairs stacked as [nsamples][nx][ny][nz];
+ * loss = mean_s ||CNN(in_s) - target_s||^2 / ||target_s||^2 (before the step, optional,
+ * synchronises); nx, ny, nz multiples of block, nx/block a multiple of 4 when nsamples > 1 */
+int       bella_cnn_train_step(bella_cnn *net, int nsamples, int nx, int ny, int nz, const float *in,
+                               const float *target, float lr, double *loss, void *stream);
 long long bella_cnn_launches(const bella_cnn *net);
 
 /* ---- allocation-free variant (no counterpart in the reference) ----------

@@ -92,13 +92,20 @@ SIGNATURES = {
                                       ctypes.POINTER(SolveStats), ctypes.c_void_p]),
     "bella_projection2d": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Proj2D), ctypes.POINTER(SolveOpts),
                                           ctypes.POINTER(SolveStats), ctypes.c_void_p]),
-    "bella_cnn_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_longlong]),
+    "bella_cnn_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_longlong]),
     "bella_cnn_destroy": (ctypes.c_int, [ctypes.c_void_p]),
-    "bella_cnn_param_count": (ctypes.c_longlong, []),
+    "bella_cnn_param_count": (ctypes.c_longlong, [ctypes.c_int]),
+    "bella_cnn_block": (ctypes.c_int, [ctypes.c_void_p]),
     "bella_cnn_set_params": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_void_p]),
     "bella_cnn_get_params": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_void_p]),
     "bella_cnn_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp,
                                          ctypes.c_float, ctypes.c_void_p]),
+    "bella_cnn_gradients": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp,
+                                           _dp, ctypes.c_void_p]),
+    "bella_cnn_train_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            _dp, _dp, ctypes.c_float, ctypes.POINTER(ctypes.c_double),
+                                            ctypes.c_void_p]),
     "bella_cnn_launches": (ctypes.c_longlong, [ctypes.c_void_p]),
     "bella_bicgstab2d_noalloc": (ctypes.c_int, [ctypes.POINTER(Op2D), _dp, _dp, ctypes.POINTER(SolveOpts),
                                                 ctypes.POINTER(SolveStats), ctypes.c_void_p]),

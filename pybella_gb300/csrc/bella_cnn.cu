@@ -60,7 +60,7 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1
 
 // Implicit-GEMM 3x3x3 convolution.  in: [nvox][CIN] bf16 (channels-last),
 // W: [27][COUT][CIN] bf16, bias: [COUT] f32.  out: [nvox][COUT] bf16, or
-// [nvox] f32 (channel 0 only, scaled by out_scale) when OUTF32.
+// [nvox][COUT] f32 scaled by out_scale when OUTF32.
 // FLIP mirrors the taps (input-gradient pass).  mask (optional, [nvox][COUT]
 // bf16): the output is multiplied by (mask > 0) -- the ReLU derivative.
 template <int CIN, int COUT, bool RELU, bool OUTF32, bool FLIP>
@@ -169,7 +169,8 @@ k_conv3d(int nx, int ny, int nz, int xseg, const __nv_bfloat16 *__restrict__ in,
                         if (!(__bfloat162float(mk.y) > 0.f)) v1 = 0.f;
                     }
                     if (OUTF32) {
-                        if (co == 0) reinterpret_cast<float *>(out)[g] = v0 * out_scale;
+                        *reinterpret_cast<float2 *>(reinterpret_cast<float *>(out) + g * COUT + co) =
+                            make_float2(v0 * out_scale, v1 * out_scale);
                     } else {
                         *reinterpret_cast<__nv_bfloat162 *>(reinterpret_cast<__nv_bfloat16 *>(out) + g * COUT + co) =
                             __floats2bfloat162_rn(v0, v1);
@@ -183,16 +184,94 @@ k_conv3d(int nx, int ny, int nz, int xseg, const __nv_bfloat16 *__restrict__ in,
 template <int CIN, int COUT>
 constexpr size_t conv_smem() { return (size_t)27 * COUT * CIN * 2 + (size_t)CH_VOX * CIN * 2; }
 
-// residual (f32) -> channels-last bf16 with 16 channels (channel 0 = in * scale)
-__global__ void k_pack_in(long long n, const float *in, float scale, __nv_bfloat16 *out) {
+// Node grid <-> net grid.  Samples are stacked along x: node (s, i, j, k) of a
+// [B][nx][ny][nz] array maps to net voxel ((s*cx + i/b)*cy + j/b)*cz + k/b and
+// sub-node channel ((i%b)*b + j%b)*b + k%b, with cx = ceil(nx/b) etc.
+struct BlockMap {
+    int B, nx, ny, nz, b, cx, cy, cz;
+    __host__ __device__ long long nvox() const { return (long long)B * cx * cy * cz; }
+};
+
+static BlockMap make_map(int B, int nx, int ny, int nz, int b) {
+    return BlockMap{B, nx, ny, nz, b, (nx + b - 1) / b, (ny + b - 1) / b, (nz + b - 1) / b};
+}
+
+// node values (f32, times scale) -> channels-last bf16 with 16 channels
+__global__ void k_pack_in(BlockMap m, const float *in, float scale, __nv_bfloat16 *out) {
+    const long long n = m.nvox();
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
-        uint4 z = make_uint4(0u, 0u, 0u, 0u);
+        const int ck = (int)(v % m.cz);
+        const long long t = v / m.cz;
+        const int cj = (int)(t % m.cy);
+        const long long sx = t / m.cy;
+        const int s = (int)(sx / m.cx), ci = (int)(sx % m.cx);
+        float c[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) c[q] = 0.f;
+        for (int q = 0; q < m.b * m.b * m.b; ++q) {
+            const int a = q / (m.b * m.b), bb = (q / m.b) % m.b, d = q % m.b;
+            const int i = ci * m.b + a, j = cj * m.b + bb, k = ck * m.b + d;
+            if (i < m.nx && j < m.ny && k < m.nz)
+                c[q] = in[(((long long)s * m.nx + i) * m.ny + j) * m.nz + k] * scale;
+        }
+        uint32_t w[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const __nv_bfloat162 h = __floats2bfloat162_rn(c[2 * q], c[2 * q + 1]);
+            w[q] = *reinterpret_cast<const uint32_t *>(&h);
+        }
         uint4 *o = reinterpret_cast<uint4 *>(out + v * 16);
-        __nv_bfloat16 h = __float2bfloat16_rn(in[v] * scale);
-        uint4 first = z;
-        first.x = (uint32_t)__bfloat16_as_ushort(h);
-        o[0] = first;
-        o[1] = z;
+        o[0] = make_uint4(w[0], w[1], w[2], w[3]);
+        o[1] = make_uint4(w[4], w[5], w[6], w[7]);
+    }
+}
+
+// node values (f32) -> net-grid f32 with 8 channels (training targets, output gradients)
+__global__ void k_pack_f32(BlockMap m, const float *in, float scale, float *out) {
+    const long long n = m.nvox();
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
+        const int ck = (int)(v % m.cz);
+        const long long t = v / m.cz;
+        const int cj = (int)(t % m.cy);
+        const long long sx = t / m.cy;
+        const int s = (int)(sx / m.cx), ci = (int)(sx % m.cx);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            float c = 0.f;
+            if (q < m.b * m.b * m.b) {
+                const int a = q / (m.b * m.b), bb = (q / m.b) % m.b, d = q % m.b;
+                const int i = ci * m.b + a, j = cj * m.b + bb, k = ck * m.b + d;
+                if (i < m.nx && j < m.ny && k < m.nz) c = in[(((long long)s * m.nx + i) * m.ny + j) * m.nz + k] * scale;
+            }
+            out[v * 8 + q] = c;
+        }
+    }
+}
+
+// net-grid f32 [nvox][8] -> node values
+__global__ void k_unpack(BlockMap m, const float *y8, float *out) {
+    const long long n = (long long)m.B * m.nx * m.ny * m.nz;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(e % m.nz);
+        const long long t = e / m.nz;
+        const int j = (int)(t % m.ny);
+        const long long si = t / m.ny;
+        const int s = (int)(si / m.nx), i = (int)(si % m.nx);
+        const long long v = (((long long)s * m.cx + i / m.b) * m.cy + j / m.b) * m.cz + k / m.b;
+        const int q = ((i % m.b) * m.b + j % m.b) * m.b + k % m.b;
+        out[e] = y8[v * 8 + q];
+    }
+}
+
+// f32 [nvox][8] -> bf16 [nvox][16] (zero-padded), input of the last layer's gradient pass
+__global__ void k_g8_to_bf16(long long n, const float *g8, __nv_bfloat16 *g16) {
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
+        const float4 a = reinterpret_cast<const float4 *>(g8)[2 * v], b = reinterpret_cast<const float4 *>(g8)[2 * v + 1];
+        __nv_bfloat162 h[4] = {__floats2bfloat162_rn(a.x, a.y), __floats2bfloat162_rn(a.z, a.w),
+                               __floats2bfloat162_rn(b.x, b.y), __floats2bfloat162_rn(b.z, b.w)};
+        uint4 *o = reinterpret_cast<uint4 *>(g16 + v * 16);
+        o[0] = *reinterpret_cast<uint4 *>(h);
+        o[1] = make_uint4(0u, 0u, 0u, 0u);
     }
 }
 
@@ -281,49 +360,29 @@ k_wgrad(int nx, int ny, int nz, int xseg, const __nv_bfloat16 *__restrict__ in, 
 template <int CINR, int COUTR>
 constexpr size_t wgrad_smem() { return sizeof(float) * ((size_t)CH_VOX * CINR + 256 * COUTR); }
 
-// gradient through the last layer (32 -> 1): d5[v][ci] = (act5[v][ci] > 0) *
-// sum_tap g6[v - off(tap)] * W5[tap][ci]  (bf16 weights as in the forward pass)
-__global__ void k_last_dgrad(int nx, int ny, int nz, int xseg, const float *g6, const __nv_bfloat16 *wk5,
-                             const __nv_bfloat16 *act5, __nv_bfloat16 *d5) {
-    const long long n = (long long)nx * ny * nz;
-    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(v % nz);
-        const long long t0 = v / nz;
-        const int j = (int)(t0 % ny), i = (int)(t0 / ny);
-        float acc[32];
-#pragma unroll
-        for (int c = 0; c < 32; ++c) acc[c] = 0.f;
-        for (int t = 0; t < 27; ++t) {
-            const int dx = t / 9 - 1, dy = (t / 3) % 3 - 1, dz = t % 3 - 1;
-            const int si = i - dx, sj = j - dy, sk = k - dz;
-            if (si < 0 || si >= nx || (si / xseg) != (i / xseg) || sj < 0 || sj >= ny || sk < 0 || sk >= nz) continue;
-            const float gv = g6[((long long)si * ny + sj) * nz + sk];
-            const __nv_bfloat16 *w = wk5 + (size_t)t * 8 * 32;      // [tap][co=0..7][ci]: row co = 0
-#pragma unroll
-            for (int c = 0; c < 32; ++c) acc[c] = fmaf(gv, __bfloat162float(w[c]), acc[c]);
-        }
-#pragma unroll
-        for (int c = 0; c < 32; c += 2) {
-            const __nv_bfloat162 a = *reinterpret_cast<const __nv_bfloat162 *>(act5 + v * 32 + c);
-            const float x0 = __bfloat162float(a.x) > 0.f ? acc[c] : 0.f;
-            const float x1 = __bfloat162float(a.y) > 0.f ? acc[c + 1] : 0.f;
-            *reinterpret_cast<__nv_bfloat162 *>(d5 + v * 32 + c) = __floats2bfloat162_rn(x0, x1);
-        }
-    }
+// per-sample squared norms of the targets: one block per sample of nsv values
+__global__ void k_sample_norm(long long nsv, const float *e, float *inv_e2) {
+    __shared__ double red[32 * NQ];
+    const float *p = e + (long long)blockIdx.x * nsv;
+    double acc[1] = {0.0};
+    for (long long i = threadIdx.x; i < nsv; i += blockDim.x) acc[0] += (double)p[i] * p[i];
+    block_sum<1>(acc, red);
+    if (threadIdx.x == 0) inv_e2[blockIdx.x] = acc[0] > 0.0 ? (float)(1.0 / acc[0]) : 0.f;
 }
 
 // per-sample normalised squared error: L = (1/B) sum_s ||y_s - e_s||^2 / ||e_s||^2,
-// g = dL/dy; samples are contiguous blocks of nsv voxels
+// g = dL/dy; samples are contiguous blocks of nsv values
 __global__ void k_loss(long long n, long long nsv, int B, const float *y, const float *e, const float *inv_e2,
-                       float *g, float *loss) {
-    float l = 0.f;
+                       float *g, double *loss) {
+    double l = 0.0;
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
         const int smp = (int)(v / nsv);
         const float d = y[v] - e[v];
-        g[v] = 2.f * d * inv_e2[smp] / (float)B;
-        l += d * d * inv_e2[smp] / (float)B;
+        const float w = inv_e2[smp] / (float)B;
+        g[v] = 2.f * d * w;
+        l += (double)d * d * w;
     }
-    l = warp_sum((double)l);
+    l = warp_sum(l);
     if ((threadIdx.x & 31) == 0) atomicAdd(loss, l);
 }
 
@@ -347,51 +406,56 @@ __global__ void k_adam(long long n, float *p, const float *g, float *m, float *v
 // ============================================================================
 using namespace bella;
 
+// Layer shapes: real channels (cin, cout) and the padded kernel shapes (cinp, coutp);
+// layer 0 takes block^3 sub-node channels (padded to 16), layer 5 returns block^3
+// channels (padded to 8; to 16 for its mirrored input-gradient pass).
 struct bella_cnn {
-    int device;
-    long long max_vox;
-    // FP32 master parameters in the oracle layout W[l][27][cin][cout], b[l][cout]
-    float *params;            // device
+    int device, block;
+    long long cap;            // net-grid voxel capacity
+    int cin[6], cout[6];
+    float *params, *grads, *adam_m, *adam_v;   // FP32, layout W[l][27][cin][cout], b[l][cout]
     long long nparams;
-    // BF16 kernel weights [27][coutp][cinp] (and mirrored/transposed for input gradients)
-    __nv_bfloat16 *wk[6], *wkT[6];
-    float *bias[6];           // padded biases
+    long long adam_t;
+    __nv_bfloat16 *wk[6], *wkT[6];   // [27][coutp][cinp] and mirrored [27][cinp][coutpT]
+    float *bias[6];
     __nv_bfloat16 *act[6];    // act[0]: packed input (16 ch); act[l]: output of layer l-1 (32 ch)
-    __nv_bfloat16 *gact[2];   // gradient ping-pong buffers (32 ch, bf16)
-    float *gtmp;              // f32 gradient of the current layer output [nvox][32]
-    float *out_tmp;
+    __nv_bfloat16 *gact[2];   // gradient ping-pong (32 ch; gact[1] also holds the 16-ch output gradient)
+    float *y8, *t8, *g8;      // net output, target, output gradient [cap][8]
+    float *inv_e2;            // per-sample 1/||target||^2 [cap]
+    double *loss;
     long long launches;
 };
 
-static const int CIN_L[6] = {1, 32, 32, 32, 32, 32};
-static const int COUT_L[6] = {32, 32, 32, 32, 32, 1};
 static const int CINP_L[6] = {16, 32, 32, 32, 32, 32};
 static const int COUTP_L[6] = {32, 32, 32, 32, 32, 8};
+static const int COUTPT_L[6] = {32, 32, 32, 32, 32, 16};
 
-static long long param_count() {
+static long long param_count_b(int block) {
+    const int b3 = block * block * block;
+    const int cin[6] = {b3, 32, 32, 32, 32, 32}, cout[6] = {32, 32, 32, 32, 32, b3};
     long long n = 0;
-    for (int l = 0; l < 6; ++l) n += 27LL * CIN_L[l] * COUT_L[l] + COUT_L[l];
+    for (int l = 0; l < 6; ++l) n += 27LL * cin[l] * cout[l] + cout[l];
     return n;
 }
 
-static long long w_off(int l) {
+static long long w_off(const bella_cnn *net, int l) {
     long long n = 0;
-    for (int k = 0; k < l; ++k) n += 27LL * CIN_L[k] * COUT_L[k] + COUT_L[k];
+    for (int k = 0; k < l; ++k) n += 27LL * net->cin[k] * net->cout[k] + net->cout[k];
     return n;
 }
 
 // master f32 [27][cin][cout] -> kernel bf16 [27][coutp][cinp] and the mirrored
-// transpose [27][cinp][coutp] used by the input-gradient pass
-__global__ void k_cast_weights(const float *W, int cin, int cout, int cinp, int coutp, __nv_bfloat16 *wk,
-                               __nv_bfloat16 *wkT) {
-    const int total = 27 * cinp * coutp;
+// transpose [27][cinp][coutpT] used by the input-gradient pass
+__global__ void k_cast_weights(const float *W, int cin, int cout, int cinp, int coutp, int coutpT,
+                               __nv_bfloat16 *wk, __nv_bfloat16 *wkT) {
+    const int total = 27 * cinp * coutpT;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-        const int tap = e / (cinp * coutp), r = e - tap * cinp * coutp, co = r / cinp, ci = r - co * cinp;
+        const int tap = e / (cinp * coutpT), r = e - tap * cinp * coutpT, co = r / cinp, ci = r - co * cinp;
         float v = 0.f;
         if (ci < cin && co < cout) v = W[((size_t)tap * cin + ci) * cout + co];
-        wk[((size_t)tap * coutp + co) * cinp + ci] = __float2bfloat16_rn(v);
-        // transpose: rows (tap, ci) of length coutp -> used as [27][CIN'=coutp][COUT'=cinp]
-        wkT[((size_t)tap * cinp + ci) * coutp + co] = __float2bfloat16_rn(v);
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        if (co < coutp) wk[((size_t)tap * coutp + co) * cinp + ci] = h;
+        wkT[((size_t)tap * cinp + ci) * coutpT + co] = h;
     }
 }
 
@@ -399,48 +463,141 @@ __global__ void k_cast_bias(const float *b, int cout, int coutp, float *bp) {
     for (int e = threadIdx.x; e < coutp; e += blockDim.x) bp[e] = e < cout ? b[e] : 0.f;
 }
 
+static void cnn_free(bella_cnn *net) {
+    cudaFree(net->params); cudaFree(net->grads); cudaFree(net->adam_m); cudaFree(net->adam_v);
+    for (int l = 0; l < 6; ++l) { cudaFree(net->wk[l]); cudaFree(net->wkT[l]); cudaFree(net->bias[l]); cudaFree(net->act[l]); }
+    cudaFree(net->gact[0]); cudaFree(net->gact[1]);
+    cudaFree(net->y8); cudaFree(net->t8); cudaFree(net->g8); cudaFree(net->inv_e2); cudaFree(net->loss);
+}
+
+template <typename K>
+static bool big_smem(K kernel, size_t bytes) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess;
+}
+
+static int conv_grid(const BlockMap &m) {
+    const long long tiles = (long long)m.B * ((m.cx + CT_X - 1) / CT_X) * ((m.cy + CT_Y - 1) / CT_Y) *
+                            ((m.cz + CT_Z - 1) / CT_Z);
+    const long long cap = (long long)NSM * 2;
+    return (int)(tiles < cap ? tiles : cap);
+}
+
+// the conv kernels see the stacked samples as one (B*cx, cy, cz) grid cut into
+// x segments of cx voxels; B > 1 needs cx to be a multiple of the tile width
+static bool map_ok(const bella_cnn *net, const BlockMap &m) {
+    return m.nvox() <= net->cap && (m.B == 1 || m.cx % CT_X == 0);
+}
+
+static void forward_layers(bella_cnn *net, const BlockMap &m, float out_scale, cudaStream_t s) {
+    const int g = conv_grid(m);
+    const int nx = m.B * m.cx, ny = m.cy, nz = m.cz, xs = m.cx;
+    k_conv3d<16, 32, true, false, false><<<g, CNN_THREADS, conv_smem<16, 32>(), s>>>(
+        nx, ny, nz, xs, net->act[0], net->wk[0], net->bias[0], net->act[1], 1.f, nullptr);
+    for (int l = 1; l <= 4; ++l)
+        k_conv3d<32, 32, true, false, false><<<g, CNN_THREADS, conv_smem<32, 32>(), s>>>(
+            nx, ny, nz, xs, net->act[l], net->wk[l], net->bias[l], net->act[l + 1], 1.f, nullptr);
+    k_conv3d<32, 8, false, true, false><<<g, CNN_THREADS, conv_smem<32, 8>(), s>>>(
+        nx, ny, nz, xs, net->act[5], net->wk[5], net->bias[5], net->y8, out_scale, nullptr);
+    net->launches += 6;
+}
+
+// gradients of sum(g8 * y8) into net->grads (zeroed here), from the stored activations
+static void backward_layers(bella_cnn *net, const BlockMap &m, cudaStream_t s) {
+    const int g = conv_grid(m);
+    const int nx = m.B * m.cx, ny = m.cy, nz = m.cz, xs = m.cx;
+    const long long n = m.nvox();
+    const int gw = g < NSM ? g : NSM;
+    cudaMemsetAsync(net->grads, 0, net->nparams * sizeof(float), s);
+    float *dW[6], *db[6];
+    for (int l = 0; l < 6; ++l) {
+        dW[l] = net->grads + w_off(net, l);
+        db[l] = dW[l] + 27LL * net->cin[l] * net->cout[l];
+    }
+    // layer 5 (32 -> block^3): weight gradient from the FP32 output gradient
+    if (net->block == 2)
+        k_wgrad<32, 32, 8, 8, float><<<gw, 256, wgrad_smem<32, 8>(), s>>>(nx, ny, nz, xs, net->act[5], net->g8, dW[5], db[5]);
+    else
+        k_wgrad<32, 32, 8, 1, float><<<gw, 256, wgrad_smem<32, 1>(), s>>>(nx, ny, nz, xs, net->act[5], net->g8, dW[5], db[5]);
+    k_g8_to_bf16<<<vec_grid(n), 256, 0, s>>>(n, net->g8, net->gact[1]);
+    // input gradient of layer 5, masked by ReLU'(layer-4 output)
+    k_conv3d<16, 32, false, false, true><<<g, CNN_THREADS, conv_smem<16, 32>(), s>>>(
+        nx, ny, nz, xs, net->gact[1], net->wkT[5], nullptr, net->gact[0], 1.f, net->act[5]);
+    int cur = 0;
+    for (int l = 4; l >= 1; --l) {
+        k_wgrad<32, 32, 32, 32, __nv_bfloat16><<<gw, 256, wgrad_smem<32, 32>(), s>>>(
+            nx, ny, nz, xs, net->act[l], net->gact[cur], dW[l], db[l]);
+        k_conv3d<32, 32, false, false, true><<<g, CNN_THREADS, conv_smem<32, 32>(), s>>>(
+            nx, ny, nz, xs, net->gact[cur], net->wkT[l], nullptr, net->gact[cur ^ 1], 1.f, net->act[l]);
+        cur ^= 1;
+    }
+    if (net->block == 2)
+        k_wgrad<16, 8, 32, 32, __nv_bfloat16><<<gw, 256, wgrad_smem<8, 32>(), s>>>(
+            nx, ny, nz, xs, net->act[0], net->gact[cur], dW[0], db[0]);
+    else
+        k_wgrad<16, 1, 32, 32, __nv_bfloat16><<<gw, 256, wgrad_smem<1, 32>(), s>>>(
+            nx, ny, nz, xs, net->act[0], net->gact[cur], dW[0], db[0]);
+    net->launches += 2 + 2 + 2 * 4 + 1;
+}
+
+// refresh the BF16 kernel weights from the FP32 master parameters (device)
+static int cnn_sync_weights(bella_cnn *net, cudaStream_t s) {
+    for (int l = 0; l < 6; ++l) {
+        const float *W = net->params + w_off(net, l);
+        const float *b = W + 27LL * net->cin[l] * net->cout[l];
+        k_cast_weights<<<64, 256, 0, s>>>(W, net->cin[l], net->cout[l], CINP_L[l], COUTP_L[l], COUTPT_L[l],
+                                          net->wk[l], net->wkT[l]);
+        k_cast_bias<<<1, 32, 0, s>>>(b, net->cout[l], COUTP_L[l], net->bias[l]);
+        net->launches += 2;
+    }
+    return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
+}
+
 static std::string g_cnn_err;
 
 extern "C" {
 
-int bella_cnn_create(bella_cnn **out, int device, long long max_voxels) {
-    if (!out || max_voxels <= 0) return BELLA_EINVAL;
+int bella_cnn_create(bella_cnn **out, int device, int block, long long capacity) {
+    if (!out || capacity <= 0 || (block != 1 && block != 2)) return BELLA_EINVAL;
     if (cudaSetDevice(device) != cudaSuccess) return BELLA_ECUDA;
     bella_cnn *net = new bella_cnn();
     memset(net, 0, sizeof(*net));
     net->device = device;
-    net->max_vox = max_voxels;
-    net->nparams = param_count();
-    bool ok = cudaMalloc(&net->params, net->nparams * sizeof(float)) == cudaSuccess;
+    net->block = block;
+    net->cap = capacity;
+    const int b3 = block * block * block;
+    for (int l = 0; l < 6; ++l) { net->cin[l] = l == 0 ? b3 : 32; net->cout[l] = l == 5 ? b3 : 32; }
+    net->nparams = param_count_b(block);
+    const size_t C = (size_t)capacity;
+    bool ok = true;
+    for (float **p : {&net->params, &net->grads, &net->adam_m, &net->adam_v})
+        ok = ok && cudaMalloc(p, net->nparams * sizeof(float)) == cudaSuccess;
     for (int l = 0; l < 6 && ok; ++l) {
-        const size_t nw = 27ULL * CINP_L[l] * COUTP_L[l];
-        ok = cudaMalloc(&net->wk[l], nw * 2) == cudaSuccess && cudaMalloc(&net->wkT[l], nw * 2) == cudaSuccess &&
+        ok = cudaMalloc(&net->wk[l], 27ULL * CINP_L[l] * COUTP_L[l] * 2) == cudaSuccess &&
+             cudaMalloc(&net->wkT[l], 27ULL * CINP_L[l] * COUTPT_L[l] * 2) == cudaSuccess &&
              cudaMalloc(&net->bias[l], 32 * sizeof(float)) == cudaSuccess;
     }
-    ok = ok && cudaMalloc(&net->act[0], (size_t)max_voxels * 16 * 2) == cudaSuccess;
-    for (int l = 1; l < 6 && ok; ++l) ok = cudaMalloc(&net->act[l], (size_t)max_voxels * 32 * 2) == cudaSuccess;
-    for (int k = 0; k < 2 && ok; ++k) ok = cudaMalloc(&net->gact[k], (size_t)max_voxels * 32 * 2) == cudaSuccess;
-    ok = ok && cudaMalloc(&net->gtmp, (size_t)max_voxels * 32 * sizeof(float)) == cudaSuccess;
-    ok = ok && cudaMalloc(&net->out_tmp, (size_t)max_voxels * sizeof(float)) == cudaSuccess;
-    ok = ok && cudaMemset(net->params, 0, net->nparams * sizeof(float)) == cudaSuccess;
-    if (ok) {
-        ok = cudaFuncSetAttribute(k_conv3d<16, 32, true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)conv_smem<16, 32>()) == cudaSuccess &&
-             cudaFuncSetAttribute(k_conv3d<32, 32, true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)conv_smem<32, 32>()) == cudaSuccess &&
-             cudaFuncSetAttribute(k_conv3d<32, 8, false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)conv_smem<32, 8>()) == cudaSuccess &&
-             cudaFuncSetAttribute(k_conv3d<32, 32, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)conv_smem<32, 32>()) == cudaSuccess &&
-             cudaFuncSetAttribute(k_conv3d<16, 32, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)conv_smem<16, 32>()) == cudaSuccess;
-    }
+    ok = ok && cudaMalloc(&net->act[0], C * 16 * 2) == cudaSuccess;
+    for (int l = 1; l < 6 && ok; ++l) ok = cudaMalloc(&net->act[l], C * 32 * 2) == cudaSuccess;
+    for (int k = 0; k < 2 && ok; ++k) ok = cudaMalloc(&net->gact[k], C * 32 * 2) == cudaSuccess;
+    for (float **p : {&net->y8, &net->t8, &net->g8}) ok = ok && cudaMalloc(p, C * 8 * sizeof(float)) == cudaSuccess;
+    ok = ok && cudaMalloc(&net->inv_e2, C * sizeof(float)) == cudaSuccess;
+    ok = ok && cudaMalloc(&net->loss, sizeof(double)) == cudaSuccess;
+    for (float *p : {net->params, net->grads, net->adam_m, net->adam_v})
+        ok = ok && cudaMemset(p, 0, net->nparams * sizeof(float)) == cudaSuccess;
+    ok = ok && big_smem(k_conv3d<16, 32, true, false, false>, conv_smem<16, 32>()) &&
+         big_smem(k_conv3d<32, 32, true, false, false>, conv_smem<32, 32>()) &&
+         big_smem(k_conv3d<32, 8, false, true, false>, conv_smem<32, 8>()) &&
+         big_smem(k_conv3d<32, 32, false, false, true>, conv_smem<32, 32>()) &&
+         big_smem(k_conv3d<16, 32, false, false, true>, conv_smem<16, 32>()) &&
+         big_smem(k_wgrad<32, 32, 8, 8, float>, wgrad_smem<32, 8>()) &&
+         big_smem(k_wgrad<32, 32, 8, 1, float>, wgrad_smem<32, 1>()) &&
+         big_smem(k_wgrad<32, 32, 32, 32, __nv_bfloat16>, wgrad_smem<32, 32>()) &&
+         big_smem(k_wgrad<16, 8, 32, 32, __nv_bfloat16>, wgrad_smem<8, 32>()) &&
+         big_smem(k_wgrad<16, 1, 32, 32, __nv_bfloat16>, wgrad_smem<1, 32>());
+    if (ok) ok = cnn_sync_weights(net, 0) == BELLA_OK && cudaDeviceSynchronize() == cudaSuccess;
     if (!ok) {
         g_cnn_err = "bella_cnn_create: allocation or attribute failed";
-        // best-effort cleanup
-        cudaFree(net->params);
-        for (int l = 0; l < 6; ++l) { cudaFree(net->wk[l]); cudaFree(net->wkT[l]); cudaFree(net->bias[l]); cudaFree(net->act[l]); }
-        cudaFree(net->gact[0]); cudaFree(net->gact[1]); cudaFree(net->gtmp); cudaFree(net->out_tmp);
+        cnn_free(net);
         delete net;
         return BELLA_ECUDA;
     }
@@ -451,34 +608,23 @@ int bella_cnn_create(bella_cnn **out, int device, long long max_voxels) {
 int bella_cnn_destroy(bella_cnn *net) {
     if (!net) return BELLA_OK;
     cudaSetDevice(net->device);
-    cudaFree(net->params);
-    for (int l = 0; l < 6; ++l) { cudaFree(net->wk[l]); cudaFree(net->wkT[l]); cudaFree(net->bias[l]); cudaFree(net->act[l]); }
-    cudaFree(net->gact[0]); cudaFree(net->gact[1]); cudaFree(net->gtmp); cudaFree(net->out_tmp);
+    cnn_free(net);
     delete net;
     return BELLA_OK;
 }
 
-long long bella_cnn_param_count(void) { return param_count(); }
+long long bella_cnn_param_count(int block) { return (block == 1 || block == 2) ? param_count_b(block) : -1; }
 
-// refresh the BF16 kernel weights from the FP32 master parameters (device)
-static int cnn_sync_weights(bella_cnn *net, cudaStream_t s) {
-    for (int l = 0; l < 6; ++l) {
-        const float *W = net->params + w_off(l);
-        const float *b = W + 27LL * CIN_L[l] * COUT_L[l];
-        k_cast_weights<<<64, 256, 0, s>>>(W, CIN_L[l], COUT_L[l], CINP_L[l], COUTP_L[l], net->wk[l], net->wkT[l]);
-        k_cast_bias<<<1, 32, 0, s>>>(b, COUT_L[l], COUTP_L[l], net->bias[l]);
-        net->launches += 2;
-    }
-    return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
-}
-
-// params: host or device FP32 array of bella_cnn_param_count() values, layer by
-// layer W[27][cin][cout] then b[cout]
+// params: host or device FP32 array of bella_cnn_param_count(block) values, layer
+// by layer W[27][cin][cout] then b[cout].  Resets the Adam state.
 int bella_cnn_set_params(bella_cnn *net, const float *params, void *stream) {
     if (!net || !params) return BELLA_EINVAL;
     cudaStream_t s = (cudaStream_t)stream;
     if (cudaMemcpyAsync(net->params, params, net->nparams * sizeof(float), cudaMemcpyDefault, s) != cudaSuccess)
         return BELLA_ECUDA;
+    cudaMemsetAsync(net->adam_m, 0, net->nparams * sizeof(float), s);
+    cudaMemsetAsync(net->adam_v, 0, net->nparams * sizeof(float), s);
+    net->adam_t = 0;
     return cnn_sync_weights(net, s);
 }
 
@@ -490,38 +636,81 @@ int bella_cnn_get_params(bella_cnn *net, float *params, void *stream) {
     return BELLA_OK;
 }
 
-static int conv_grid(int nx, int ny, int nz) {
-    const long long tiles = (long long)((nx + CT_X - 1) / CT_X) * ((ny + CT_Y - 1) / CT_Y) * ((nz + CT_Z - 1) / CT_Z);
-    const long long cap = (long long)NSM * 2;
-    return (int)(tiles < cap ? tiles : cap);
-}
-
-static void cnn_forward_layers(bella_cnn *net, int nx, int ny, int nz, int xseg, float *out, float out_scale,
-                               cudaStream_t s) {
-    const int g = conv_grid(nx, ny, nz);
-    k_conv3d<16, 32, true, false, false><<<g, CNN_THREADS, conv_smem<16, 32>(), s>>>(
-        nx, ny, nz, xseg, net->act[0], net->wk[0], net->bias[0], net->act[1], 1.f, nullptr);
-    for (int l = 1; l <= 4; ++l)
-        k_conv3d<32, 32, true, false, false><<<g, CNN_THREADS, conv_smem<32, 32>(), s>>>(
-            nx, ny, nz, xseg, net->act[l], net->wk[l], net->bias[l], net->act[l + 1], 1.f, nullptr);
-    k_conv3d<32, 8, false, true, false><<<g, CNN_THREADS, conv_smem<32, 8>(), s>>>(
-        nx, ny, nz, xseg, net->act[5], net->wk[5], net->bias[5], out, out_scale, nullptr);
-    net->launches += 6;
-}
-
-// out = CNN(in * in_scale) / in_scale on an (nx, ny, nz) grid (C order, z fastest)
+// out = CNN(in * in_scale) / in_scale on the nodes of an (nx, ny, nz) grid (C
+// order, z fastest); in and out are device FP32 arrays and may not alias
 int bella_cnn_forward(bella_cnn *net, int nx, int ny, int nz, const float *in, float *out, float in_scale,
                       void *stream) {
     if (!net || !in || !out || nx < 1 || ny < 1 || nz < 1 || !(in_scale > 0.f)) return BELLA_EINVAL;
-    const long long n = (long long)nx * ny * nz;
-    if (n > net->max_vox) return BELLA_EINVAL;
+    const BlockMap m = make_map(1, nx, ny, nz, net->block);
+    if (!map_ok(net, m)) return BELLA_EINVAL;
     cudaStream_t s = (cudaStream_t)stream;
-    k_pack_in<<<vec_grid(n), 256, 0, s>>>(n, in, in_scale, net->act[0]);
-    cnn_forward_layers(net, nx, ny, nz, nx, out, 1.f / in_scale, s);
-    net->launches += 1;
-    if (cudaGetLastError() != cudaSuccess) return BELLA_ECUDA;
-    return BELLA_OK;
+    k_pack_in<<<vec_grid(m.nvox()), 256, 0, s>>>(m, in, in_scale, net->act[0]);
+    forward_layers(net, m, 1.f / in_scale, s);
+    k_unpack<<<vec_grid((long long)nx * ny * nz), 256, 0, s>>>(m, net->y8, out);
+    net->launches += 2;
+    return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
 }
+
+// Parameter gradients of sum(gout * CNN(in)) (nodes of an (nx, ny, nz) grid,
+// device FP32) into grads (device FP32, parameter layout).  Also leaves the
+// forward output in `out` when non-null.
+int bella_cnn_gradients(bella_cnn *net, int nx, int ny, int nz, const float *in, const float *gout, float *grads,
+                        float *out, void *stream) {
+    if (!net || !in || !gout || !grads || nx < 1 || ny < 1 || nz < 1) return BELLA_EINVAL;
+    const BlockMap m = make_map(1, nx, ny, nz, net->block);
+    if (!map_ok(net, m)) return BELLA_EINVAL;
+    cudaStream_t s = (cudaStream_t)stream;
+    k_pack_in<<<vec_grid(m.nvox()), 256, 0, s>>>(m, in, 1.f, net->act[0]);
+    forward_layers(net, m, 1.f, s);
+    if (out) k_unpack<<<vec_grid((long long)nx * ny * nz), 256, 0, s>>>(m, net->y8, out);
+    k_pack_f32<<<vec_grid(m.nvox()), 256, 0, s>>>(m, gout, 1.f, net->g8);
+    backward_layers(net, m, s);
+    cudaMemcpyAsync(grads, net->grads, net->nparams * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    net->launches += 3;
+    return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
+}
+
+// One Adam step on a batch of nsamples (input, target) pairs of (nx, ny, nz)
+// nodes each, stacked as [nsamples][nx][ny][nz] device FP32 arrays.  The loss
+// is the mean over samples of ||CNN(in_s) - target_s||^2 / ||target_s||^2; the
+// caller normalises each pair (the solver feeds the net unit-RMS inputs).
+// nx, ny, nz must be multiples of the block size and, for nsamples > 1,
+// nx / block a multiple of 4.  *loss (host, optional) receives the batch loss
+// before the step, which synchronises the stream.
+int bella_cnn_train_step(bella_cnn *net, int nsamples, int nx, int ny, int nz, const float *in, const float *target,
+                         float lr, double *loss, void *stream) {
+    if (!net || !in || !target || nsamples < 1 || nx < 1 || ny < 1 || nz < 1 || !(lr > 0.f)) return BELLA_EINVAL;
+    const int b = net->block;
+    if (nx % b || ny % b || nz % b) return BELLA_EINVAL;
+    const BlockMap m = make_map(nsamples, nx, ny, nz, b);
+    if (!map_ok(net, m)) return BELLA_EINVAL;
+    cudaStream_t s = (cudaStream_t)stream;
+    const long long n = m.nvox();
+    const long long nsv = (long long)m.cx * m.cy * m.cz * 8;
+    k_pack_in<<<vec_grid(n), 256, 0, s>>>(m, in, 1.f, net->act[0]);
+    k_pack_f32<<<vec_grid(n), 256, 0, s>>>(m, target, 1.f, net->t8);
+    k_sample_norm<<<nsamples, 256, 0, s>>>(nsv, net->t8, net->inv_e2);
+    forward_layers(net, m, 1.f, s);
+    cudaMemsetAsync(net->loss, 0, sizeof(double), s);
+    k_loss<<<vec_grid(n * 8), 256, 0, s>>>(n * 8, nsv, nsamples, net->y8, net->t8, net->inv_e2, net->g8, net->loss);
+    backward_layers(net, m, s);
+    net->adam_t += 1;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float bc1 = 1.f - powf(b1, (float)net->adam_t), bc2 = 1.f - powf(b2, (float)net->adam_t);
+    k_adam<<<vec_grid(net->nparams), 256, 0, s>>>(net->nparams, net->params, net->grads, net->adam_m, net->adam_v, lr,
+                                                  b1, b2, 1e-8f, bc1, bc2);
+    net->launches += 5;
+    const int rc = cnn_sync_weights(net, s);
+    if (rc != BELLA_OK) return rc;
+    if (loss) {
+        if (cudaMemcpyAsync(loss, net->loss, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return BELLA_ECUDA;
+    }
+    return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
+}
+
+int bella_cnn_block(const bella_cnn *net) { return net ? net->block : 0; }
 
 long long bella_cnn_launches(const bella_cnn *net) { return net ? net->launches : 0; }
 
