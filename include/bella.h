@@ -188,6 +188,9 @@ int       bella_cnn_create(bella_cnn **net, int device, int block, long long cap
 int       bella_cnn_destroy(bella_cnn *net);
 long long bella_cnn_param_count(int block);
 int       bella_cnn_block(const bella_cnn *net);
+/* mode 0: ReLU network with biases; 1: linear (no ReLU, no biases); 2: ReLU without biases
+ * (positively homogeneous); biases must be zero for modes 1 and 2 and stay zero in training */
+int       bella_cnn_set_mode(bella_cnn *net, int mode);
 /* FP32 parameters, layer by layer W[27][cin][cout] (tap = (dx+1)*9+(dy+1)*3+(dz+1)) then b[cout];
  * host or device pointer; set_params resets the Adam state */
 int       bella_cnn_set_params(bella_cnn *net, const float *params, void *stream);
@@ -204,7 +207,30 @@ int       bella_cnn_gradients(bella_cnn *net, int nx, int ny, int nz, const floa
  * synchronises); nx, ny, nz multiples of block, nx/block a multiple of 4 when nsamples > 1 */
 int       bella_cnn_train_step(bella_cnn *net, int nsamples, int nx, int ny, int nz, const float *in,
                                const float *target, float lr, double *loss, void *stream);
+/* one Adam step on the operator residual of the predicted error over nsamples crops of
+ * S^3 nodes: loss = mean_s ||interior(A_s(CNN(in_s) - target_s))||^2 / ||interior(in_s)||^2,
+ * A_s the 27-point operator (hplusx = hplusy = hplusz = hcell, no hcenter/Coriolis term)
+ * on the crop with zero values outside it; hcell [nsamples][(S+1)^3] cell coefficients,
+ * dinv [nsamples][S^3]; device FP32 arrays */
+int       bella_cnn_train_step_op(bella_cnn *net, int nsamples, int S, const float *in, const float *target,
+                                  const float *hcell, const float *dinv, double dx, double dy, double dz,
+                                  float lr, double *loss, void *stream);
+/* y = A_crop u for the crop operator above (interior != 0 zeroes the crop's face nodes);
+ * flux: scratch of nsamples*(S+1)^3*3 floats */
+int       bella_crop_apply(int nsamples, int S, const float *u, const float *hcell, const float *dinv,
+                           double dx, double dy, double dz, int interior, float *flux, float *y, void *stream);
 long long bella_cnn_launches(const bella_cnn *net);
+/* Flexible BiCGStab on the 3D operator of ws, right-preconditioned by net: the
+ * preconditioner slot of scipy's bicgstab (its M argument), which the reference
+ * leaves empty at second_projection.py:230.  FP32 inner iterations (FP32 stencil,
+ * FP64 reductions) inside FP64 iterative refinement on the true residual; tol,
+ * atol, maxiter, x0_zero, project_null, inner_tol, max_outer, check_every and
+ * timeout_s as for bella_bicgstab (precision is ignored); each inner solve is
+ * capped at maxiter/max_outer iterations (at least 100).  When the learned
+ * iteration fails (no progress, non-finite, max_outer) the plain double-float
+ * BiCGStab continues from the current iterate and stats->fallback = 1. */
+int       bella_fbicgstab(bella_ws *ws, bella_cnn *net, const double *b, double *x,
+                          const bella_solve_opts *opts, bella_solve_stats *stats, void *stream);
 
 /* ---- allocation-free variant (no counterpart in the reference) ----------
  * FP64 BiCGStab of bella_bicgstab (precision 0 only) on the reference-packed

@@ -64,20 +64,21 @@ def unblocked(y, shape, block):
     return np.ascontiguousarray(x[:shape[0], :shape[1], :shape[2]])
 
 
-def forward(r, params, block=1, rounding=True):
+def forward(r, params, block=1, rounding=True, linear=False):
     """r: (nx,ny,nz) float -> (output on the same grid, activations list on the net grid).
 
     ``rounding=False`` evaluates the same network in float64 throughout (for
-    finite-difference checks of ``backward``)."""
+    finite-difference checks of ``backward``).  ``linear=True``: no ReLU and no
+    biases (the linear preconditioner mode)."""
     rnd = bf16 if rounding else (lambda a: np.asarray(a, np.float64))
     a = rnd(blocked(np.asarray(r, np.float32 if rounding else np.float64), block))
     acts = [a]
     for layer in range(6):
         W, b = params["W%d" % layer], params["b%d" % layer]
         W = rnd(W)
-        z = conv(acts[-1], W, b)
+        z = conv(acts[-1], W, 0.0 * b if linear else b)
         if layer < 5:
-            a = rnd(np.maximum(z, 0.0).astype(np.float32 if rounding else np.float64))
+            a = rnd((z if linear else np.maximum(z, 0.0)).astype(np.float32 if rounding else np.float64))
         else:
             a = z.astype(np.float32 if rounding else np.float64)
         acts.append(a)
@@ -101,7 +102,7 @@ def weight_grad(x, g):
     return out
 
 
-def backward(acts, params, gout, block=1, rounding=True):
+def backward(acts, params, gout, block=1, rounding=True, linear=False):
     """Gradients of sum(gout * output) w.r.t. all weights and biases (gout on the node grid)."""
     grads = {}
     g = blocked(np.asarray(gout, np.float64), block)
@@ -112,7 +113,7 @@ def backward(acts, params, gout, block=1, rounding=True):
         grads["b%d" % layer] = g.sum(axis=(0, 1, 2))
         if layer > 0:
             gin = conv_transpose(g, W)
-            g = gin * (acts[layer] > 0)
+            g = gin if linear else gin * (acts[layer] > 0)
     return grads
 
 

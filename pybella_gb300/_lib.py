@@ -97,6 +97,14 @@ SIGNATURES = {
     "bella_cnn_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "bella_cnn_param_count": (ctypes.c_longlong, [ctypes.c_int]),
     "bella_cnn_block": (ctypes.c_int, [ctypes.c_void_p]),
+    "bella_cnn_set_mode": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "bella_cnn_train_step_op": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp,
+                                               ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_float,
+                                               ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
+    "bella_crop_apply": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_int, _dp, _dp, ctypes.c_void_p]),
+    "bella_fbicgstab": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, _dp, _dp, ctypes.POINTER(SolveOpts),
+                                       ctypes.POINTER(SolveStats), ctypes.c_void_p]),
     "bella_cnn_set_params": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_void_p]),
     "bella_cnn_get_params": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_void_p]),
     "bella_cnn_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp,

@@ -196,9 +196,17 @@ static BlockMap make_map(int B, int nx, int ny, int nz, int b) {
     return BlockMap{B, nx, ny, nz, b, (nx + b - 1) / b, (ny + b - 1) / b, (nz + b - 1) / b};
 }
 
-// node values (f32, times scale) -> channels-last bf16 with 16 channels
-__global__ void k_pack_in(BlockMap m, const float *in, float scale, __nv_bfloat16 *out) {
+// scale of a unit-RMS normalisation from a device sum of squares of nn values
+__device__ __forceinline__ float rms_scale(const double *sumsq, long long nn) {
+    const double q = *sumsq;
+    return (q > 0.0 && isfinite(q)) ? (float)(1.0 / sqrt(q / (double)nn)) : 1.f;
+}
+
+// node values (f32, times scale -- or 1/RMS from sumsq when given) -> channels-last
+// bf16 with 16 channels
+__global__ void k_pack_in(BlockMap m, const float *in, float scale, __nv_bfloat16 *out, const double *sumsq) {
     const long long n = m.nvox();
+    if (sumsq) scale = rms_scale(sumsq, (long long)m.B * m.nx * m.ny * m.nz);
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
         const int ck = (int)(v % m.cz);
         const long long t = v / m.cz;
@@ -248,9 +256,10 @@ __global__ void k_pack_f32(BlockMap m, const float *in, float scale, float *out)
     }
 }
 
-// net-grid f32 [nvox][8] -> node values
-__global__ void k_unpack(BlockMap m, const float *y8, float *out) {
+// net-grid f32 [nvox][8] -> node values (times RMS from sumsq when given)
+__global__ void k_unpack(BlockMap m, const float *y8, float *out, const double *sumsq) {
     const long long n = (long long)m.B * m.nx * m.ny * m.nz;
+    const float mul = sumsq ? 1.f / rms_scale(sumsq, n) : 1.f;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
         const int k = (int)(e % m.nz);
         const long long t = e / m.nz;
@@ -259,7 +268,7 @@ __global__ void k_unpack(BlockMap m, const float *y8, float *out) {
         const int s = (int)(si / m.nx), i = (int)(si % m.nx);
         const long long v = (((long long)s * m.cx + i / m.b) * m.cy + j / m.b) * m.cz + k / m.b;
         const int q = ((i % m.b) * m.b + j % m.b) * m.b + k % m.b;
-        out[e] = y8[v * 8 + q];
+        out[e] = y8[v * 8 + q] * mul;
     }
 }
 
@@ -399,6 +408,118 @@ __global__ void k_adam(long long n, float *p, const float *g, float *m, float *v
     }
 }
 
+// ---- the 27-point operator on batches of crops (training loss) ---------------
+// A crop is S^3 nodes with the S+1 cell planes around them; crop cell c spans
+// crop nodes c-1 and c, nodes outside the crop are zero.  Per cell the edge
+// differences of the node values are summed over the cell's four edges along
+// each axis and weighted by the cell's hplus (the arithmetic of lap3D,
+// laplacian.py:968-1015, with hplusx = hplusy = hplusz and no Coriolis or
+// hcenter term); a node receives the four + side cells minus the four - side
+// cells per axis, times 1/16 and 1/d^2, then diag_inv.  On nodes at least one
+// node away from the crop faces this equals the full-grid operator.
+__device__ __forceinline__ float crop_u(const float *u, const float *us, int S, int i, int j, int k) {
+    if (i < 0 || j < 0 || k < 0 || i >= S || j >= S || k >= S) return 0.f;
+    const int g = (i * S + j) * S + k;
+    return us ? u[g] * us[g] : u[g];
+}
+
+__global__ void k_crop_flux(int B, int S, const float *u, const float *us, const float *h, float *F) {
+    const int C = S + 1;
+    const long long n = (long long)B * C * C * C;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int f = (int)(e % C);
+        const long long t = e / C;
+        const int d = (int)(t % C);
+        const long long t2 = t / C;
+        const int c = (int)(t2 % C), b = (int)(t2 / C);
+        const float *ub = u + (long long)b * S * S * S;
+        const float *usb = us ? us + (long long)b * S * S * S : nullptr;
+        float U[2][2][2];
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int bb = 0; bb < 2; ++bb)
+#pragma unroll
+                for (int q = 0; q < 2; ++q) U[a][bb][q] = crop_u(ub, usb, S, c - 1 + a, d - 1 + bb, f - 1 + q);
+        float xf = 0.f, yf = 0.f, zf = 0.f;
+#pragma unroll
+        for (int p = 0; p < 2; ++p)
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                xf += U[1][p][q] - U[0][p][q];
+                yf += U[p][1][q] - U[p][0][q];
+                zf += U[p][q][1] - U[p][q][0];
+            }
+        const float hh = h[e];
+        F[3 * e + 0] = hh * xf;
+        F[3 * e + 1] = hh * yf;
+        F[3 * e + 2] = hh * zf;
+    }
+}
+
+// out = mask * dinv * (node sums of F); interior != 0 zeroes the crop's face nodes
+__global__ void k_crop_node(int B, int S, const float *F, const float *dinv, float ox, float oy, float oz,
+                            int interior, float *out) {
+    const int C = S + 1;
+    const long long n = (long long)B * S * S * S;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(e % S);
+        const long long t = e / S;
+        const int j = (int)(t % S);
+        const long long t2 = t / S;
+        const int i = (int)(t2 % S), b = (int)(t2 / S);
+        const float *Fb = F + (long long)b * C * C * C * 3;
+        auto at = [&](int c, int d, int f, int comp) { return Fb[(((long long)c * C + d) * C + f) * 3 + comp]; };
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+        for (int p = 0; p < 2; ++p)
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                sx += at(i + 1, j + p, k + q, 0) - at(i, j + p, k + q, 0);
+                sy += at(i + p, j + 1, k + q, 1) - at(i + p, j, k + q, 1);
+                sz += at(i + p, j + q, k + 1, 2) - at(i + p, j + q, k, 2);
+            }
+        float v = 0.0625f * (ox * sx + oy * sy + oz * sz);
+        if (dinv) v *= dinv[e];
+        if (interior && (i == 0 || j == 0 || k == 0 || i == S - 1 || j == S - 1 || k == S - 1)) v = 0.f;
+        out[e] = v;
+    }
+}
+
+// d = a - b (node grid)
+__global__ void k_sub(long long n, const float *a, const float *b, float *d) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        d[i] = a[i] - b[i];
+}
+
+// per-sample weights 1/||interior(r_s)||^2 (one block per sample)
+__global__ void k_crop_rnorm(int S, const float *r, float *w) {
+    __shared__ double red[32 * NQ];
+    const long long nsv = (long long)S * S * S;
+    const float *p = r + (long long)blockIdx.x * nsv;
+    double acc[1] = {0.0};
+    for (long long e = threadIdx.x; e < nsv; e += blockDim.x) {
+        const int k = (int)(e % S), j = (int)((e / S) % S), i = (int)(e / ((long long)S * S));
+        if (i == 0 || j == 0 || k == 0 || i == S - 1 || j == S - 1 || k == S - 1) continue;
+        acc[0] += (double)p[e] * p[e];
+    }
+    block_sum<1>(acc, red);
+    if (threadIdx.x == 0) w[blockIdx.x] = acc[0] > 0.0 ? (float)(1.0 / acc[0]) : 0.f;
+}
+
+// loss += w_s ||q||^2 / B and q *= 2 w_s / B (q becomes dL/d(Ad) before the adjoint)
+__global__ void k_crop_loss(long long n, long long nsv, int B, float *q, const float *w, double *loss) {
+    double l = 0.0;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
+        const float ws = w[v / nsv] / (float)B;
+        const float qv = q[v];
+        l += (double)qv * qv * ws;
+        q[v] = 2.f * ws * qv;
+    }
+    l = warp_sum(l);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, l);
+}
+
 }  // namespace bella
 
 // ============================================================================
@@ -411,6 +532,8 @@ using namespace bella;
 // channels (padded to 8; to 16 for its mirrored input-gradient pass).
 struct bella_cnn {
     int device, block;
+    int linear;               // 1: no ReLU and no biases (a linear map)
+    int bias_free;            // 1: biases held at zero (positively homogeneous map)
     long long cap;            // net-grid voxel capacity
     int cin[6], cout[6];
     float *params, *grads, *adam_m, *adam_v;   // FP32, layout W[l][27][cin][cout], b[l][cout]
@@ -423,6 +546,9 @@ struct bella_cnn {
     float *y8, *t8, *g8;      // net output, target, output gradient [cap][8]
     float *inv_e2;            // per-sample 1/||target||^2 [cap]
     double *loss;
+    // operator-loss scratch (node grid of a batch of crops), allocated on first use
+    float *yf, *qf, *gf, *flux, *wcrop;
+    long long fine_cap, flux_cap;
     long long launches;
 };
 
@@ -468,6 +594,7 @@ static void cnn_free(bella_cnn *net) {
     for (int l = 0; l < 6; ++l) { cudaFree(net->wk[l]); cudaFree(net->wkT[l]); cudaFree(net->bias[l]); cudaFree(net->act[l]); }
     cudaFree(net->gact[0]); cudaFree(net->gact[1]);
     cudaFree(net->y8); cudaFree(net->t8); cudaFree(net->g8); cudaFree(net->inv_e2); cudaFree(net->loss);
+    cudaFree(net->yf); cudaFree(net->qf); cudaFree(net->gf); cudaFree(net->flux); cudaFree(net->wcrop);
 }
 
 template <typename K>
@@ -491,13 +618,23 @@ static bool map_ok(const bella_cnn *net, const BlockMap &m) {
 static void forward_layers(bella_cnn *net, const BlockMap &m, float out_scale, cudaStream_t s) {
     const int g = conv_grid(m);
     const int nx = m.B * m.cx, ny = m.cy, nz = m.cz, xs = m.cx;
-    k_conv3d<16, 32, true, false, false><<<g, CNN_THREADS, conv_smem<16, 32>(), s>>>(
-        nx, ny, nz, xs, net->act[0], net->wk[0], net->bias[0], net->act[1], 1.f, nullptr);
-    for (int l = 1; l <= 4; ++l)
-        k_conv3d<32, 32, true, false, false><<<g, CNN_THREADS, conv_smem<32, 32>(), s>>>(
-            nx, ny, nz, xs, net->act[l], net->wk[l], net->bias[l], net->act[l + 1], 1.f, nullptr);
-    k_conv3d<32, 8, false, true, false><<<g, CNN_THREADS, conv_smem<32, 8>(), s>>>(
-        nx, ny, nz, xs, net->act[5], net->wk[5], net->bias[5], net->y8, out_scale, nullptr);
+    if (net->linear) {
+        k_conv3d<16, 32, false, false, false><<<g, CNN_THREADS, conv_smem<16, 32>(), s>>>(
+            nx, ny, nz, xs, net->act[0], net->wk[0], nullptr, net->act[1], 1.f, nullptr);
+        for (int l = 1; l <= 4; ++l)
+            k_conv3d<32, 32, false, false, false><<<g, CNN_THREADS, conv_smem<32, 32>(), s>>>(
+                nx, ny, nz, xs, net->act[l], net->wk[l], nullptr, net->act[l + 1], 1.f, nullptr);
+        k_conv3d<32, 8, false, true, false><<<g, CNN_THREADS, conv_smem<32, 8>(), s>>>(
+            nx, ny, nz, xs, net->act[5], net->wk[5], nullptr, net->y8, out_scale, nullptr);
+    } else {
+        k_conv3d<16, 32, true, false, false><<<g, CNN_THREADS, conv_smem<16, 32>(), s>>>(
+            nx, ny, nz, xs, net->act[0], net->wk[0], net->bias[0], net->act[1], 1.f, nullptr);
+        for (int l = 1; l <= 4; ++l)
+            k_conv3d<32, 32, true, false, false><<<g, CNN_THREADS, conv_smem<32, 32>(), s>>>(
+                nx, ny, nz, xs, net->act[l], net->wk[l], net->bias[l], net->act[l + 1], 1.f, nullptr);
+        k_conv3d<32, 8, false, true, false><<<g, CNN_THREADS, conv_smem<32, 8>(), s>>>(
+            nx, ny, nz, xs, net->act[5], net->wk[5], net->bias[5], net->y8, out_scale, nullptr);
+    }
     net->launches += 6;
 }
 
@@ -520,14 +657,15 @@ static void backward_layers(bella_cnn *net, const BlockMap &m, cudaStream_t s) {
         k_wgrad<32, 32, 8, 1, float><<<gw, 256, wgrad_smem<32, 1>(), s>>>(nx, ny, nz, xs, net->act[5], net->g8, dW[5], db[5]);
     k_g8_to_bf16<<<vec_grid(n), 256, 0, s>>>(n, net->g8, net->gact[1]);
     // input gradient of layer 5, masked by ReLU'(layer-4 output)
+    const bool relu = !net->linear;
     k_conv3d<16, 32, false, false, true><<<g, CNN_THREADS, conv_smem<16, 32>(), s>>>(
-        nx, ny, nz, xs, net->gact[1], net->wkT[5], nullptr, net->gact[0], 1.f, net->act[5]);
+        nx, ny, nz, xs, net->gact[1], net->wkT[5], nullptr, net->gact[0], 1.f, relu ? net->act[5] : nullptr);
     int cur = 0;
     for (int l = 4; l >= 1; --l) {
         k_wgrad<32, 32, 32, 32, __nv_bfloat16><<<gw, 256, wgrad_smem<32, 32>(), s>>>(
             nx, ny, nz, xs, net->act[l], net->gact[cur], dW[l], db[l]);
         k_conv3d<32, 32, false, false, true><<<g, CNN_THREADS, conv_smem<32, 32>(), s>>>(
-            nx, ny, nz, xs, net->gact[cur], net->wkT[l], nullptr, net->gact[cur ^ 1], 1.f, net->act[l]);
+            nx, ny, nz, xs, net->gact[cur], net->wkT[l], nullptr, net->gact[cur ^ 1], 1.f, relu ? net->act[l] : nullptr);
         cur ^= 1;
     }
     if (net->block == 2)
@@ -537,6 +675,9 @@ static void backward_layers(bella_cnn *net, const BlockMap &m, cudaStream_t s) {
         k_wgrad<16, 1, 32, 32, __nv_bfloat16><<<gw, 256, wgrad_smem<1, 32>(), s>>>(
             nx, ny, nz, xs, net->act[0], net->gact[cur], dW[0], db[0]);
     net->launches += 2 + 2 + 2 * 4 + 1;
+    if (net->linear || net->bias_free) {   // biases stay at zero: no gradient, no Adam motion
+        for (int l = 0; l < 6; ++l) cudaMemsetAsync(db[l], 0, net->cout[l] * sizeof(float), s);
+    }
 }
 
 // refresh the BF16 kernel weights from the FP32 master parameters (device)
@@ -553,6 +694,22 @@ static int cnn_sync_weights(bella_cnn *net, cudaStream_t s) {
 }
 
 static std::string g_cnn_err;
+
+namespace bella {
+// out = CNN(in / rms) * rms with rms = sqrt(*sumsq / n) read on the device (no host
+// synchronisation); used by the flexible solver.  BELLA_EINVAL if the grid
+// exceeds the network's capacity.
+int cnn_apply_dev(bella_cnn *net, int nx, int ny, int nz, const float *in, float *out, const double *sumsq,
+                  cudaStream_t s) {
+    const BlockMap m = make_map(1, nx, ny, nz, net->block);
+    if (!map_ok(net, m)) return BELLA_EINVAL;
+    k_pack_in<<<vec_grid(m.nvox()), 256, 0, s>>>(m, in, 1.f, net->act[0], sumsq);
+    forward_layers(net, m, 1.f, s);
+    k_unpack<<<vec_grid((long long)nx * ny * nz), 256, 0, s>>>(m, net->y8, out, sumsq);
+    net->launches += 2;
+    return BELLA_OK;
+}
+}  // namespace bella
 
 extern "C" {
 
@@ -589,6 +746,8 @@ int bella_cnn_create(bella_cnn **out, int device, int block, long long capacity)
          big_smem(k_conv3d<32, 8, false, true, false>, conv_smem<32, 8>()) &&
          big_smem(k_conv3d<32, 32, false, false, true>, conv_smem<32, 32>()) &&
          big_smem(k_conv3d<16, 32, false, false, true>, conv_smem<16, 32>()) &&
+         big_smem(k_conv3d<16, 32, false, false, false>, conv_smem<16, 32>()) &&
+         big_smem(k_conv3d<32, 32, false, false, false>, conv_smem<32, 32>()) &&
          big_smem(k_wgrad<32, 32, 8, 8, float>, wgrad_smem<32, 8>()) &&
          big_smem(k_wgrad<32, 32, 8, 1, float>, wgrad_smem<32, 1>()) &&
          big_smem(k_wgrad<32, 32, 32, 32, __nv_bfloat16>, wgrad_smem<32, 32>()) &&
@@ -644,9 +803,9 @@ int bella_cnn_forward(bella_cnn *net, int nx, int ny, int nz, const float *in, f
     const BlockMap m = make_map(1, nx, ny, nz, net->block);
     if (!map_ok(net, m)) return BELLA_EINVAL;
     cudaStream_t s = (cudaStream_t)stream;
-    k_pack_in<<<vec_grid(m.nvox()), 256, 0, s>>>(m, in, in_scale, net->act[0]);
+    k_pack_in<<<vec_grid(m.nvox()), 256, 0, s>>>(m, in, in_scale, net->act[0], nullptr);
     forward_layers(net, m, 1.f / in_scale, s);
-    k_unpack<<<vec_grid((long long)nx * ny * nz), 256, 0, s>>>(m, net->y8, out);
+    k_unpack<<<vec_grid((long long)nx * ny * nz), 256, 0, s>>>(m, net->y8, out, nullptr);
     net->launches += 2;
     return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
 }
@@ -660,9 +819,9 @@ int bella_cnn_gradients(bella_cnn *net, int nx, int ny, int nz, const float *in,
     const BlockMap m = make_map(1, nx, ny, nz, net->block);
     if (!map_ok(net, m)) return BELLA_EINVAL;
     cudaStream_t s = (cudaStream_t)stream;
-    k_pack_in<<<vec_grid(m.nvox()), 256, 0, s>>>(m, in, 1.f, net->act[0]);
+    k_pack_in<<<vec_grid(m.nvox()), 256, 0, s>>>(m, in, 1.f, net->act[0], nullptr);
     forward_layers(net, m, 1.f, s);
-    if (out) k_unpack<<<vec_grid((long long)nx * ny * nz), 256, 0, s>>>(m, net->y8, out);
+    if (out) k_unpack<<<vec_grid((long long)nx * ny * nz), 256, 0, s>>>(m, net->y8, out, nullptr);
     k_pack_f32<<<vec_grid(m.nvox()), 256, 0, s>>>(m, gout, 1.f, net->g8);
     backward_layers(net, m, s);
     cudaMemcpyAsync(grads, net->grads, net->nparams * sizeof(float), cudaMemcpyDeviceToDevice, s);
@@ -687,7 +846,7 @@ int bella_cnn_train_step(bella_cnn *net, int nsamples, int nx, int ny, int nz, c
     cudaStream_t s = (cudaStream_t)stream;
     const long long n = m.nvox();
     const long long nsv = (long long)m.cx * m.cy * m.cz * 8;
-    k_pack_in<<<vec_grid(n), 256, 0, s>>>(m, in, 1.f, net->act[0]);
+    k_pack_in<<<vec_grid(n), 256, 0, s>>>(m, in, 1.f, net->act[0], nullptr);
     k_pack_f32<<<vec_grid(n), 256, 0, s>>>(m, target, 1.f, net->t8);
     k_sample_norm<<<nsamples, 256, 0, s>>>(nsv, net->t8, net->inv_e2);
     forward_layers(net, m, 1.f, s);
@@ -710,7 +869,95 @@ int bella_cnn_train_step(bella_cnn *net, int nsamples, int nx, int ny, int nz, c
     return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
 }
 
+// y = A_crop u for nsamples crops of S^3 nodes (device FP32): hcell
+// [nsamples][(S+1)^3] cell hplus, dinv [nsamples][S^3]; interior != 0 zeroes
+// the crop's face nodes.  Scratch flux: [nsamples][(S+1)^3][3] FP32.
+int bella_crop_apply(int nsamples, int S, const float *u, const float *hcell, const float *dinv, double dx, double dy,
+                     double dz, int interior, float *flux, float *y, void *stream) {
+    if (nsamples < 1 || S < 2 || !u || !hcell || !flux || !y) return BELLA_EINVAL;
+    cudaStream_t s = (cudaStream_t)stream;
+    const long long nc = (long long)nsamples * (S + 1) * (S + 1) * (S + 1), nn = (long long)nsamples * S * S * S;
+    k_crop_flux<<<vec_grid(nc), 256, 0, s>>>(nsamples, S, u, nullptr, hcell, flux);
+    k_crop_node<<<vec_grid(nn), 256, 0, s>>>(nsamples, S, flux, dinv, (float)(1.0 / (dx * dx)),
+                                             (float)(1.0 / (dy * dy)), (float)(1.0 / (dz * dz)), interior, y);
+    return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
+}
+
+// One Adam step on the operator residual of the predicted error:
+//   loss = mean_s ||interior(A_s (CNN(r_s) - e_s))||^2 / ||interior(r_s)||^2
+// for nsamples crops of S^3 nodes (r = A e on the full grid, so on interior
+// nodes A(CNN(r) - e) = A CNN(r) - r).  hcell, dinv: the crops' operator
+// coefficients as in bella_crop_apply; the gradient through A uses
+// A^T = L diag(dinv) with L the symmetric unscaled operator.
+int bella_cnn_train_step_op(bella_cnn *net, int nsamples, int S, const float *in, const float *target,
+                            const float *hcell, const float *dinv, double dx, double dy, double dz, float lr,
+                            double *loss, void *stream) {
+    if (!net || !in || !target || !hcell || !dinv || nsamples < 1 || S < 4 || !(lr > 0.f)) return BELLA_EINVAL;
+    const int b = net->block;
+    if (S % b) return BELLA_EINVAL;
+    const BlockMap m = make_map(nsamples, S, S, S, b);
+    if (!map_ok(net, m)) return BELLA_EINVAL;
+    cudaStream_t s = (cudaStream_t)stream;
+    const long long nn = (long long)nsamples * S * S * S;
+    const long long nc = (long long)nsamples * (S + 1) * (S + 1) * (S + 1);
+    if (net->fine_cap < nn) {
+        cudaFree(net->yf); cudaFree(net->qf); cudaFree(net->gf); cudaFree(net->wcrop);
+        net->yf = net->qf = net->gf = net->wcrop = nullptr;
+        net->fine_cap = 0;
+        if (cudaMalloc(&net->yf, nn * 4) != cudaSuccess || cudaMalloc(&net->qf, nn * 4) != cudaSuccess ||
+            cudaMalloc(&net->gf, nn * 4) != cudaSuccess || cudaMalloc(&net->wcrop, (nn / 64 + 1) * 4) != cudaSuccess)
+            return BELLA_ECUDA;
+        net->fine_cap = nn;
+    }
+    if (net->flux_cap < nc) {
+        cudaFree(net->flux);
+        net->flux = nullptr;
+        net->flux_cap = 0;
+        if (cudaMalloc(&net->flux, nc * 3 * 4) != cudaSuccess) return BELLA_ECUDA;
+        net->flux_cap = nc;
+    }
+    const float ox = (float)(1.0 / (dx * dx)), oy = (float)(1.0 / (dy * dy)), oz = (float)(1.0 / (dz * dz));
+    k_pack_in<<<vec_grid(m.nvox()), 256, 0, s>>>(m, in, 1.f, net->act[0], nullptr);
+    forward_layers(net, m, 1.f, s);
+    k_unpack<<<vec_grid(nn), 256, 0, s>>>(m, net->y8, net->yf, nullptr);
+    k_sub<<<vec_grid(nn), 256, 0, s>>>(nn, net->yf, target, net->gf);
+    // q = interior(A (y - e))
+    k_crop_flux<<<vec_grid(nc), 256, 0, s>>>(nsamples, S, net->gf, nullptr, hcell, net->flux);
+    k_crop_node<<<vec_grid(nn), 256, 0, s>>>(nsamples, S, net->flux, dinv, ox, oy, oz, 1, net->qf);
+    k_crop_rnorm<<<nsamples, 256, 0, s>>>(S, in, net->wcrop);
+    cudaMemsetAsync(net->loss, 0, sizeof(double), s);
+    k_crop_loss<<<vec_grid(nn), 256, 0, s>>>(nn, (long long)S * S * S, nsamples, net->qf, net->wcrop, net->loss);
+    // g = A^T q = L (dinv * q)
+    k_crop_flux<<<vec_grid(nc), 256, 0, s>>>(nsamples, S, net->qf, dinv, hcell, net->flux);
+    k_crop_node<<<vec_grid(nn), 256, 0, s>>>(nsamples, S, net->flux, nullptr, ox, oy, oz, 0, net->gf);
+    k_pack_f32<<<vec_grid(m.nvox()), 256, 0, s>>>(m, net->gf, 1.f, net->g8);
+    backward_layers(net, m, s);
+    net->adam_t += 1;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float bc1 = 1.f - powf(b1, (float)net->adam_t), bc2 = 1.f - powf(b2, (float)net->adam_t);
+    k_adam<<<vec_grid(net->nparams), 256, 0, s>>>(net->nparams, net->params, net->grads, net->adam_m, net->adam_v, lr,
+                                                  b1, b2, 1e-8f, bc1, bc2);
+    net->launches += 13;
+    const int rc = cnn_sync_weights(net, s);
+    if (rc != BELLA_OK) return rc;
+    if (loss) {
+        if (cudaMemcpyAsync(loss, net->loss, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return BELLA_ECUDA;
+    }
+    return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
+}
+
 int bella_cnn_block(const bella_cnn *net) { return net ? net->block : 0; }
+
+// mode bit 0: linear (no ReLU, no biases); bit 1: bias-free ReLU network.  The
+// biases must be zero for either (set_params); they then stay zero in training.
+int bella_cnn_set_mode(bella_cnn *net, int mode) {
+    if (!net || mode < 0 || mode > 3) return BELLA_EINVAL;
+    net->linear = mode & 1;
+    net->bias_free = (mode >> 1) & 1;
+    return BELLA_OK;
+}
 
 long long bella_cnn_launches(const bella_cnn *net) { return net ? net->launches : 0; }
 

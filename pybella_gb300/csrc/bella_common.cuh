@@ -230,6 +230,7 @@ struct bella_ws {
     void *vbase;              // one allocation for all vectors
     double *r64, *x64v;       // IR outer residual, FP64 scratch
     float  *r32, *rh32, *p32[2], *v32[2], *t32, *x32;
+    float  *s32, *ph32, *sh32;   // flexible (CNN-preconditioned) solver: s, M(p), M(s)
     double *r64k, *rh64, *p64[2], *v64[2], *t64;
     bella::dfloat *rdf, *rhdf, *pdf[2], *vdf[2], *tdf, *xdf;   // double-float Krylov vectors
     bella::dfloat *adf, *dinvdf, *hcdf;                         // double-float operator planes

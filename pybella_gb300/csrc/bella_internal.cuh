@@ -84,4 +84,8 @@ inline void op_iteration(bella_ws *ws, int prec, cudaStream_t s) {
 }
 template <typename T> void launch_update(bella_ws *ws, cudaStream_t s);
 
+// learned preconditioner (bella_cnn.cu)
+int cnn_apply_dev(bella_cnn *net, int nx, int ny, int nz, const float *in, float *out, const double *sumsq,
+                  cudaStream_t s);
+
 }  // namespace bella

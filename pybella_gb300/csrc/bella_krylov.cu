@@ -426,7 +426,7 @@ static int ensure_vectors(bella_ws *ws, long long n) {
     cudaFree(ws->vbase);
     ws->vbase = nullptr;
     const long long np = (n + 63) / 64 * 64;   // 256-byte aligned slices
-    const size_t bytes = (size_t)np * (8 * 9 + 4 * 8 + 8 * 8);
+    const size_t bytes = (size_t)np * (8 * 9 + 4 * 11 + 8 * 8);
     BELLA_CUDA(cudaMalloc(&ws->vbase, bytes));
     char *p = (char *)ws->vbase;
     auto take64 = [&](double **d) { *d = (double *)p; p += np * 8; };
@@ -435,6 +435,7 @@ static int ensure_vectors(bella_ws *ws, long long n) {
     take64(&ws->p64[0]); take64(&ws->p64[1]); take64(&ws->v64[0]); take64(&ws->v64[1]); take64(&ws->t64);
     take32(&ws->r32); take32(&ws->rh32); take32(&ws->p32[0]); take32(&ws->p32[1]);
     take32(&ws->v32[0]); take32(&ws->v32[1]); take32(&ws->t32); take32(&ws->x32);
+    take32(&ws->s32); take32(&ws->ph32); take32(&ws->sh32);
     auto takedf = [&](dfloat **d) { *d = (dfloat *)p; p += np * 8; };
     takedf(&ws->rdf); takedf(&ws->rhdf); takedf(&ws->pdf[0]); takedf(&ws->pdf[1]);
     takedf(&ws->vdf[0]); takedf(&ws->vdf[1]); takedf(&ws->tdf); takedf(&ws->xdf);
@@ -874,6 +875,256 @@ done:
 }
 
 }  // extern "C"
+
+// ============================================================================
+// Flexible BiCGStab right-preconditioned by the learned CNN (3D operators).
+//
+// scipy's bicgstab, which the reference calls without a preconditioner
+// (second_projection.py:230), takes one through its M argument and applies it
+// to p and s; here M is the CNN (nonlinear in its ReLU modes), so the
+// iteration is the flexible variant: p^ = M(p), v = A p^, s = r - alpha v,
+// s^ = M(s), t = A s^, x += alpha p^ + omega s^.  The scalar recurrences,
+// stop tests and breakdown tests are those of the plain solver (finalize_*).
+// Inner iterations keep FP32 vectors and the FP32 operator with FP64
+// reductions; FP64 iterative refinement on the true residual wraps them as in
+// the mixed plain solve.  The plain double-float BiCGStab is the fallback and
+// is reported in stats->fallback.  The CNN sees unit-RMS inputs (its scale is
+// read on the device, no host synchronisation).
+// ============================================================================
+namespace bella {
+
+__global__ void __launch_bounds__(VEC_BLOCK)
+k_flex_p(long long n, const float *r, float *p, const float *v, KState *ks, double *partials, unsigned *counter) {
+    if (ks->done) return;
+    const bool first = ks->iter == 0;
+    const float beta = (float)ks->beta, omega = (float)ks->omega;
+    double a[1] = {0.0};
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
+        const float pg = first ? r[g] : fmaf(beta, fmaf(-omega, v[g], p[g]), r[g]);
+        p[g] = pg;
+        a[0] += (double)pg * (double)pg;
+    }
+    double tot[1];
+    if (!grid_sum<1>(a, partials, counter, tot)) return;
+    if (threadIdx.x == 0) ks->dot_aux = tot[0];
+}
+
+__global__ void __launch_bounds__(VEC_BLOCK)
+k_flex_alpha(long long n, const float *rh, const float *v, KState *ks, double *partials, unsigned *counter) {
+    if (ks->done) return;
+    double a[1] = {0.0};
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x)
+        a[0] += (double)rh[g] * (double)v[g];
+    double tot[1];
+    if (!grid_sum<1>(a, partials, counter, tot)) return;
+    if (threadIdx.x == 0) finalize_pdir(ks, tot[0]);
+}
+
+// s = r - alpha v, ||s||^2 -> ks->ss and ks->dot_aux (the CNN's scale)
+__global__ void __launch_bounds__(VEC_BLOCK)
+k_flex_s(long long n, const float *r, const float *v, float *s, KState *ks, double *partials, unsigned *counter) {
+    if (ks->done) return;
+    const float alpha = (float)ks->alpha;
+    double a[1] = {0.0};
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
+        const float sg = fmaf(-alpha, v[g], r[g]);
+        s[g] = sg;
+        a[0] += (double)sg * (double)sg;
+    }
+    double tot[1];
+    if (!grid_sum<1>(a, partials, counter, tot)) return;
+    if (threadIdx.x == 0) { ks->ss = tot[0]; ks->dot_aux = tot[0]; }
+}
+
+__global__ void __launch_bounds__(VEC_BLOCK)
+k_flex_omega(long long n, const float *t, const float *s, KState *ks, double *partials, unsigned *counter) {
+    if (ks->done) return;
+    double a[2] = {0.0, 0.0};
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
+        const double tg = t[g];
+        a[0] += tg * (double)s[g];
+        a[1] += tg * tg;
+    }
+    double tot[2];
+    if (!grid_sum<2>(a, partials, counter, tot)) return;
+    if (threadIdx.x == 0) finalize_sdir(ks, tot[0], tot[1], ks->ss);
+}
+
+// x += alpha p^ + omega s^, r = s - omega t, <r^, r>, ||r||^2
+__global__ void __launch_bounds__(VEC_BLOCK)
+k_flex_update(long long n, float *x, const float *ph, const float *sh, float *r, const float *s, const float *t,
+              const float *rh, KState *ks, double *partials, unsigned *counter) {
+    if (ks->done) return;
+    const float alpha = (float)ks->alpha, omega = ks->early ? 0.f : (float)ks->omega;
+    double a[2] = {0.0, 0.0};
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
+        x[g] = fmaf(omega, sh[g], fmaf(alpha, ph[g], x[g]));
+        const float rg = fmaf(-omega, t[g], s[g]);
+        r[g] = rg;
+        a[0] += (double)rh[g] * (double)rg;
+        a[1] += (double)rg * (double)rg;
+    }
+    double tot[2];
+    if (!grid_sum<2>(a, partials, counter, tot)) return;
+    if (threadIdx.x == 0) finalize_update(ks, tot[0], tot[1]);
+}
+
+static int flex_iteration(bella_ws *ws, bella_cnn *net, cudaStream_t s) {
+    const long long n = ws->n;
+    const int gv = ws->grid_vec;
+    double *scale = &ws->ks->dot_aux;   // device address of the running sum of squares
+    k_flex_p<<<gv, VEC_BLOCK, 0, s>>>(n, ws->r32, ws->p32[0], ws->v32[0], ws->ks, ws->partials, ws->counter);
+    int rc = cnn_apply_dev(net, ws->nx, ws->ny, ws->nz, ws->p32[0], ws->ph32, scale, s);
+    if (rc != BELLA_OK) return set_err(rc, "bella_fbicgstab: grid exceeds the network's capacity");
+    op_apply(ws, 1, ws->ph32, ws->v32[0], s);
+    k_flex_alpha<<<gv, VEC_BLOCK, 0, s>>>(n, ws->rh32, ws->v32[0], ws->ks, ws->partials, ws->counter);
+    k_flex_s<<<gv, VEC_BLOCK, 0, s>>>(n, ws->r32, ws->v32[0], ws->s32, ws->ks, ws->partials, ws->counter);
+    rc = cnn_apply_dev(net, ws->nx, ws->ny, ws->nz, ws->s32, ws->sh32, scale, s);
+    if (rc != BELLA_OK) return set_err(rc, "bella_fbicgstab: grid exceeds the network's capacity");
+    op_apply(ws, 1, ws->sh32, ws->t32, s);
+    k_flex_omega<<<gv, VEC_BLOCK, 0, s>>>(n, ws->t32, ws->s32, ws->ks, ws->partials, ws->counter);
+    k_flex_update<<<gv, VEC_BLOCK, 0, s>>>(n, ws->x32, ws->ph32, ws->sh32, ws->r32, ws->s32, ws->t32, ws->rh32,
+                                           ws->ks, ws->partials, ws->counter);
+    ws->launches += 7;
+    return cuda_check(cudaGetLastError(), "flexible BiCGStab iteration");
+}
+
+static int run_flex(bella_ws *ws, bella_cnn *net, const bella_solve_opts *o, cudaStream_t s,
+                    std::chrono::steady_clock::time_point t0, int *timed_out) {
+    const int blk = o->check_every > 0 ? (o->check_every < 4 ? o->check_every : 4) : 4;
+    *timed_out = 0;
+    for (;;) {
+        int rc = sync_state(ws, s);
+        if (rc != BELLA_OK) return rc;
+        if (ws->ks_host->done) return BELLA_OK;
+        if (o->timeout_s > 0.0) {
+            const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (el > o->timeout_s) { *timed_out = 1; return BELLA_OK; }
+        }
+        for (int k = 0; k < blk; ++k) {
+            rc = flex_iteration(ws, net, s);
+            if (rc != BELLA_OK) return rc;
+        }
+    }
+}
+
+}  // namespace bella
+
+extern "C" int bella_fbicgstab(bella_ws *ws, bella_cnn *net, const double *b, double *x,
+                               const bella_solve_opts *opts, bella_solve_stats *stats, void *stream) {
+    if (!ws || !net || !b || !x) return set_err(BELLA_EINVAL, "bella_fbicgstab: null argument");
+    if (ws->ndim != 3) return set_err(ws->ndim == 0 ? BELLA_ENOOP : BELLA_EINVAL,
+                                      "bella_fbicgstab: needs a 3D operator (bella_op3d_set)");
+    bella_solve_opts o;
+    if (opts) o = *opts; else bella_solve_opts_default(&o);
+    if (!(o.tol >= 0.0) || o.maxiter < 0) return set_err(BELLA_EINVAL, "bella_fbicgstab: bad tol/maxiter");
+    BELLA_CUDA(cudaSetDevice(ws->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    const auto t0 = std::chrono::steady_clock::now();
+    bella_solve_stats st;
+    memset(&st, 0, sizeof(st));
+    const long long n = ws->n;
+    const int gv = ws->grid_vec;
+    int rc, timed_out = 0;
+    k_dot64<<<gv, VEC_BLOCK, 0, s>>>(n, b, b, ws->ks, ws->partials, ws->counter);
+    ws->launches++;
+    rc = sync_state(ws, s);
+    if (rc != BELLA_OK) return rc;
+    const double bnorm = sqrt(ws->ks_host->dot_aux);
+    st.bnorm = bnorm;
+    double target = o.tol * bnorm;
+    if (o.atol > target) target = o.atol;
+    bool failed = false;
+    if (!isfinite(bnorm)) {
+        st.status = BELLA_NONFINITE;
+    } else if (o.x0_zero && (bnorm == 0.0 || bnorm <= o.tol)) {   // scipy 1.7 legacy exit
+        BELLA_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
+        st.status = BELLA_OK;
+    } else {
+        if (o.x0_zero) BELLA_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
+        NullSpace ns = ws->ns;
+        if (!o.project_null) ns.nm = 0;
+        op_resid(ws, 0, x, b, ws->r64, s);
+        rc = sync_state(ws, s);
+        if (rc != BELLA_OK) return rc;
+        double rnorm = sqrt(ws->ks_host->dot_aux2);
+        st.matvecs = 1;
+        int total = 0;
+        for (int outer = 0;; ++outer) {
+            if (!isfinite(rnorm)) { st.status = BELLA_NONFINITE; failed = true; break; }
+            if (rnorm <= target) { st.status = BELLA_OK; break; }
+            if (total >= o.maxiter) { st.status = BELLA_MAXITER; break; }
+            if (outer >= o.max_outer) { failed = true; break; }
+            if (timed_out) { st.status = BELLA_TIMEOUT; break; }
+            double rel = o.inner_tol;
+            const double need = 0.5 * target / rnorm;
+            if (need > rel) rel = need;
+            // each inner solve is capped so that a stagnating learned iteration is
+            // judged (and, without progress, replaced by the plain method) early
+            int cap = o.maxiter / (o.max_outer > 0 ? o.max_outer : 1);
+            if (cap < 100) cap = 100;
+            if (cap > o.maxiter - total) cap = o.maxiter - total;
+            k_init32<<<gv, VEC_BLOCK, 0, s>>>(n, ws->r64, 1.0 / rnorm, ws->r32, ws->rh32, ws->x32, rel, cap, ws->ks,
+                                              ws->partials, ws->counter);
+            ws->launches++;
+            rc = run_flex(ws, net, &o, s, t0, &timed_out);
+            if (rc != BELLA_OK) return rc;
+            const int it = ws->ks_host->iter;
+            const int inner_status = ws->ks_host->status;
+            st.detail = ws->ks_host->pad[0];
+            total += it;
+            st.matvecs += 2 * it;
+            st.outer = outer + 1;
+            if (inner_status == BELLA_NONFINITE || it == 0) { failed = true; break; }
+            k_ir_update<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->x32, rnorm, ws->z64, ns, ws->ks, ws->partials,
+                                                 ws->counter);
+            ws->launches++;
+            op_resid(ws, 0, x, b, ws->r64, s);
+            st.matvecs += 1;
+            rc = sync_state(ws, s);
+            if (rc != BELLA_OK) return rc;
+            const double rnew = sqrt(ws->ks_host->dot_aux2);
+            if (!(rnew < rnorm)) {   // no progress: take the correction back, fall back
+                NullSpace none = ns;
+                none.nm = 0;
+                k_ir_update<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->x32, -rnorm, ws->z64, none, ws->ks, ws->partials,
+                                                     ws->counter);
+                ws->launches++;
+                failed = true;
+                break;
+            }
+            if (ns.nm > 0) {
+                k_null_shift<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->ks, ns);
+                ws->launches++;
+            }
+            rnorm = rnew;
+        }
+        st.iterations = total;
+        if (failed) {
+            // the plain method from the current iterate; reported, never silent
+            st.fallback = 1;
+            const int left = o.maxiter - total;
+            bella_solve_stats fs;
+            memset(&fs, 0, sizeof(fs));
+            rc = solve_df(ws, b, x, o, 1, left > 0 ? left : 0, &fs, s, t0);
+            if (rc != BELLA_OK) return rc;
+            st.status = fs.status;
+            st.iterations += fs.iterations;
+            st.matvecs += fs.matvecs;
+            st.detail = fs.detail;
+        }
+    }
+    op_resid(ws, 0, x, b, ws->r64, s);
+    rc = sync_state(ws, s);
+    if (rc != BELLA_OK) return rc;
+    const double rn = sqrt(ws->ks_host->dot_aux2);
+    st.relres = st.bnorm > 0 ? rn / st.bnorm : rn;
+    if (!isfinite(rn)) st.status = BELLA_NONFINITE;
+    BELLA_CUDA(cudaGetLastError());
+    st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (stats) *stats = st;
+    return st.status;
+}
 
 // ============================================================================
 // Allocation-free FP64 BiCGStab for small 2D systems.

@@ -30,7 +30,9 @@ def net_voxels(shape, block, nsamples=1):
 class CNN:
     """Device-resident network.  ``capacity``: largest (shape, nsamples) it must run."""
 
-    def __init__(self, shape, block=2, nsamples=1, device=None):
+    MODES = {"relu": 0, "linear": 1, "relu_nobias": 2}
+
+    def __init__(self, shape, block=2, nsamples=1, device=None, mode="relu"):
         self._lib = _lib.load()
         self.dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.block = int(block)
@@ -40,6 +42,8 @@ class CNN:
                    "bella_cnn_create")
         self.handle = h
         self.nparams = int(self._lib.bella_cnn_param_count(self.block))
+        self.mode = mode
+        _lib.check(self._lib.bella_cnn_set_mode(self.handle, self.MODES[mode]), "bella_cnn_set_mode")
 
     def _stream(self):
         return ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
@@ -62,13 +66,14 @@ class CNN:
         return t.cpu().numpy()
 
     def init(self, seed):
-        """He-normal weights (seeded), zero biases."""
+        """He-normal weights (seeded; variance 1/fan-in for the linear net), zero biases."""
         rng = np.random.default_rng(seed)
         b3 = self.block ** 3
         cin, cout = [b3, 32, 32, 32, 32, 32], [32, 32, 32, 32, 32, b3]
+        gain = 1.0 if self.mode == "linear" else 2.0
         parts = []
         for l in range(6):
-            parts.append((rng.standard_normal(27 * cin[l] * cout[l]) * np.sqrt(2.0 / (27 * cin[l]))).astype(np.float32))
+            parts.append((rng.standard_normal(27 * cin[l] * cout[l]) * np.sqrt(gain / (27 * cin[l]))).astype(np.float32))
             parts.append(np.zeros(cout[l], np.float32))
         self.set_params(np.concatenate(parts))
 
@@ -113,3 +118,137 @@ class CNN:
                 self.handle = None
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------------
+# training data and training
+# ---------------------------------------------------------------------------
+def operator_3d(w, ws=None):
+    """Device 27-point operator of a :func:`pybella_gb300.workloads.stratified_3d` workload."""
+    from .linalg import NodalHelmholtz3D
+    return NodalHelmholtz3D(w["hplusx"], w["hplusy"], w["hplusz"], w["hcenter"], w["diag_inv"], w["nx"], w["ny"],
+                            w["nz"], w["dx"], w["dy"], w["dz"], walls=w["walls"], corrf=w["corrf"], ws=ws)
+
+
+def wall_zeroed_cells(w):
+    """The cell coefficient (hplusx = hplusy = hplusz) with the wall cell planes zeroed, as the operator uses it."""
+    nx, ny, nz = w["nx"], w["ny"], w["nz"]
+    h = w["hplusx"].reshape(nx + 1, ny + 1, nz + 1).clone()
+    for ax, wall in enumerate(w["walls"]):
+        if wall:
+            h.index_fill_(ax, torch.tensor([0, h.shape[ax] - 1], device=h.device), 0.0)
+    return h
+
+
+class PairSet:
+    """Training windows on the device: residual R, error E (S^3 nodes), the window's
+    cell coefficients H ((S+1)^3) and Jacobi scaling D (S^3), FP32; grid spacing."""
+
+    def __init__(self, n, S, spacing):
+        kw = dict(dtype=torch.float32, device="cuda")
+        self.R = torch.empty((n, S, S, S), **kw)
+        self.E = torch.empty((n, S, S, S), **kw)
+        self.H = torch.empty((n, S + 1, S + 1, S + 1), **kw)
+        self.D = torch.empty((n, S, S, S), **kw)
+        self.S, self.n, self.spacing = S, 0, tuple(float(v) for v in spacing)
+
+    def add(self, r, e, h, dinv, shape, count, gen):
+        """Random windows of the node fields r, e (unit-RMS residual per window)."""
+        nx, ny, nz = shape
+        S = self.S
+        R, E, D = r.reshape(nx, ny, nz), e.reshape(nx, ny, nz), dinv.reshape(nx, ny, nz)
+        for _ in range(count):
+            i0 = int(torch.randint(0, nx - S + 1, (1,), generator=gen))
+            j0 = int(torch.randint(0, ny - S + 1, (1,), generator=gen))
+            k0 = int(torch.randint(0, nz - S + 1, (1,), generator=gen))
+            rc = R[i0:i0 + S, j0:j0 + S, k0:k0 + S]
+            sc = 1.0 / torch.sqrt(torch.mean(rc * rc)).clamp_min(1e-300)
+            q = self.n
+            self.R[q] = (rc * sc).to(torch.float32)
+            self.E[q] = (E[i0:i0 + S, j0:j0 + S, k0:k0 + S] * sc).to(torch.float32)
+            self.H[q] = h[i0:i0 + S + 1, j0:j0 + S + 1, k0:k0 + S + 1].to(torch.float32)
+            self.D[q] = D[i0:i0 + S, j0:j0 + S, k0:k0 + S].to(torch.float32)
+            self.n += 1
+
+    def trim(self):
+        for k in ("R", "E", "H", "D"):
+            setattr(self, k, getattr(self, k)[:self.n])
+        return self
+
+
+def harvest_pairs(seeds, shape=(129, 65, 129), npairs=20000, crop=32, checkpoints=(2, 8, 32, 128, 512, 2048),
+                  random_fraction=0.25, powers=(0.0, 2.0, 4.0), solve_tol=1e-9, solve_maxiter=200000,
+                  gen_seed=0, log=None):
+    """(residual, error) training windows on the device (a :class:`PairSet`).
+
+    For every seed a :func:`~pybella_gb300.workloads.stratified_3d` problem of
+    ``shape`` is solved to ``solve_tol`` (x*), then plain BiCGStab is run again
+    from x = 0 and stopped at each of ``checkpoints`` iterations: each stop
+    gives r = b - A x and e = x* - x, cut into random windows of ``crop``^3
+    nodes with their operator coefficients.  A further ``random_fraction`` of
+    the pairs are (A e, e) for seeded Gaussian fields e with power ~k^-p
+    (``powers``), covering error components the solver's own iterates leave
+    out.  A seed whose x* solve fails contributes only the latter.
+    """
+    from . import workloads
+    gen = torch.Generator(device="cpu")
+    gen.manual_seed(int(gen_seed))
+    n_rand = int(round(npairs * random_fraction))
+    n_iter = npairs - n_rand
+    per_state = max(1, -(-n_iter // (len(seeds) * len(checkpoints))))
+    per_rand = max(1, -(-n_rand // (len(seeds) * len(powers)))) if n_rand else 0
+    ps = None
+    for seed in seeds:
+        w = workloads.stratified_3d(seed, *shape)
+        if ps is None:
+            ps = PairSet(npairs, crop, (w["dx"], w["dy"], w["dz"]))
+        A = operator_3d(w)
+        h = wall_zeroed_cells(w)
+        b = w["b"]
+        xs, st = A.solve(b, tol=solve_tol, maxiter=solve_maxiter, precision="df64")
+        ok = st["status"] == 0
+        if log:
+            log("seed %d: x* %s in %d iterations (relres %.2e)" % (seed, "found" if ok else "NOT found",
+                                                                   st["iterations"], st["relres"]))
+        x, done = None, 0
+        for k in (checkpoints if ok else ()):
+            if ps.n >= n_iter:
+                break
+            x, _ = A.solve(b, x0=x, tol=1e-300, maxiter=k - done, precision="df64")
+            done = k
+            r = b - A.matvec(x)
+            ps.add(r, xs - x, h, w["diag_inv"], shape, min(per_state, n_iter - ps.n), gen)
+        if n_rand:
+            g = torch.Generator(device="cuda")
+            g.manual_seed(1000 + int(seed))
+            for p in powers:
+                if ps.n >= npairs:
+                    break
+                e = workloads._power_field(shape, p, g, torch.device("cuda")).reshape(-1)
+                ps.add(A.matvec(e), e, h, w["diag_inv"], shape, min(per_rand, npairs - ps.n), gen)
+        del A
+    return ps.trim()
+
+
+def train(net, pairs, steps=3000, batch=32, lr=1e-3, lr_final=1e-5, seed=0, log=None, log_every=250):
+    """Adam on the device with the net's own kernels and the operator-residual loss
+    (``bella_cnn_train_step_op``); cosine learning-rate decay.  Returns [(step, loss)]."""
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(int(seed))
+    losses = []
+    lib = net._lib
+    dx, dy, dz = pairs.spacing
+    for it in range(steps):
+        idx = torch.randint(0, pairs.n, (batch,), generator=gen, device="cuda")
+        lr_t = lr_final + 0.5 * (lr - lr_final) * (1.0 + np.cos(np.pi * it / max(1, steps - 1)))
+        want = (it % log_every == 0) or it == steps - 1
+        R, E, H, D = (t[idx].contiguous() for t in (pairs.R, pairs.E, pairs.H, pairs.D))
+        loss = ctypes.c_double(float("nan"))
+        _lib.check(lib.bella_cnn_train_step_op(net.handle, batch, pairs.S, _ptr(R), _ptr(E), _ptr(H), _ptr(D),
+                                               dx, dy, dz, float(lr_t), ctypes.byref(loss) if want else None,
+                                               net._stream()), "bella_cnn_train_step_op")
+        if want:
+            losses.append((it, loss.value))
+            if log:
+                log("step %d  loss %.4f  lr %.2e" % (it, loss.value, lr_t))
+    return losses

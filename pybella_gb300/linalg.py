@@ -19,6 +19,7 @@ libbella_gb300.  There is no CPU path: a matvec that is not a device nodal
 operator is rejected.
 """
 import ctypes
+import warnings
 
 import numpy as np
 import torch
@@ -93,14 +94,21 @@ class _NodalOperator:
 
     # -- solve -------------------------------------------------------------
     def solve(self, b, x0=None, tol=1e-8, atol=0.0, maxiter=6000, precision="fp64", inner_tol=1e-5,
-              project_null=True, check_every=16, timeout_s=0.0, out=None):
+              project_null=True, check_every=16, timeout_s=0.0, out=None, preconditioner=None, max_outer=30):
         """Solve ``A x = b``; returns ``(x, stats)`` with ``x`` a CUDA float64 tensor.
 
         ``precision='fp64'`` (default) is BiCGStab in FP64 with scipy's
         control flow.  ``'mixed'`` runs FP32 BiCGStab inner solves inside FP64
         iterative refinement (FP64 residuals, FP64 accumulated solution); if an
         inner solve fails (non-finite, breakdown, no progress) the solve is
-        finished by FP64 BiCGStab and ``stats['fallback'] == 1``.
+        finished by FP64 BiCGStab and ``stats['fallback'] == 1``.  ``'df64'``
+        is double-float BiCGStab with FP64 reliable updates.
+
+        ``preconditioner`` (a :class:`pybella_gb300.learned.CNN`, 3D only)
+        selects flexible BiCGStab right-preconditioned by the network (FP32
+        inner iterations in FP64 refinement, ``precision`` ignored); a failed
+        learned solve is finished by the plain double-float method, reported
+        in ``stats['fallback']`` and by a warning.
         """
         bd = _to_dev(b, self.dev)
         if bd.numel() != self.n:
@@ -122,10 +130,19 @@ class _NodalOperator:
         o.inner_tol = float(inner_tol)
         o.check_every = int(check_every)
         o.timeout_s = float(timeout_s)
+        o.max_outer = int(max_outer)
         st = _lib.SolveStats()
         with torch.cuda.device(self.dev):
-            _lib.check(self.ws._lib.bella_bicgstab(self.ws.handle, _ptr(bd), _ptr(x), ctypes.byref(o),
-                                                   ctypes.byref(st), _stream(self.dev)), "bella_bicgstab")
+            if preconditioner is None:
+                _lib.check(self.ws._lib.bella_bicgstab(self.ws.handle, _ptr(bd), _ptr(x), ctypes.byref(o),
+                                                       ctypes.byref(st), _stream(self.dev)), "bella_bicgstab")
+            else:
+                _lib.check(self.ws._lib.bella_fbicgstab(self.ws.handle, preconditioner.handle, _ptr(bd), _ptr(x),
+                                                        ctypes.byref(o), ctypes.byref(st), _stream(self.dev)),
+                           "bella_fbicgstab")
+                if st.fallback:
+                    warnings.warn("learned-preconditioner solve failed; finished by plain BiCGStab "
+                                  "(status %d, relres %.3e)" % (st.status, st.relres), RuntimeWarning)
         return x, st.as_dict()
 
 
@@ -248,11 +265,12 @@ def bicgstab(A, b, x0=None, tol=None, maxiter=None, M=None, callback=None, atol=
     second_projection.py:11-20); it is invoked once per BiCGStab iteration
     after the solve, each time with the final iterate (per-iteration
     iterates stay on the device).  ``M`` (preconditioner) is not supported on
-    this path.  ``stats`` (a dict) receives iterations, outer refinement
+    this path unless it is a :class:`pybella_gb300.learned.CNN` (3D operators),
+    which selects the flexible solver.  ``stats`` (a dict) receives iterations, outer refinement
     steps, true relative residual, status and time.
     """
-    if M is not None:
-        raise NotImplementedError("bicgstab: M is not supported; use the flexible solver for preconditioning")
+    if M is not None and not hasattr(M, "train_step"):
+        raise NotImplementedError("bicgstab: M must be a pybella_gb300.learned.CNN (flexible BiCGStab)")
     op = A.op if isinstance(A, LinearOperator) else A
     if not hasattr(op, "solve"):
         raise TypeError("bicgstab needs a pybella_gb300 device operator, got %r" % (A,))
@@ -263,7 +281,7 @@ def bicgstab(A, b, x0=None, tol=None, maxiter=None, M=None, callback=None, atol=
         maxiter = 10 * n
     is_torch = isinstance(b, torch.Tensor) and b.is_cuda
     x, st = op.solve(b, x0=x0, tol=tol, atol=atol or 0.0, maxiter=maxiter, precision=precision,
-                     inner_tol=inner_tol)
+                     inner_tol=inner_tol, preconditioner=M)
     status = st["status"]
     if status in (_lib.BELLA_MAXITER, _lib.BELLA_TIMEOUT):
         info = max(int(st["iterations"]), 1)

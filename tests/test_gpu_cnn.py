@@ -79,3 +79,91 @@ def test_cnn_train_step_reduces_loss(block):
     assert np.all(np.isfinite(losses))
     assert losses[-1] < 0.5 * losses[0], (losses[0], losses[-1])
     assert not np.array_equal(net.get_params(), p0)
+
+
+@pytest.mark.parametrize("block,shape", [(2, (10, 8, 18))])
+def test_cnn_linear_mode_gradients_match_oracle(block, shape):
+    """Linear mode (no ReLU, no biases): forward and weight gradients against the oracle;
+    bias gradients are held at zero."""
+    import torch
+    from pybella_gb300.learned import CNN
+    rng = np.random.default_rng(21)
+    params = ocnn.init_params(6, block)
+    r = rng.standard_normal(shape).astype(np.float32)
+    gout = rng.standard_normal(shape).astype(np.float32)
+    yref, acts = ocnn.forward(r, params, block, linear=True)
+    ref = ocnn.backward(acts, params, gout, block, linear=True)
+    net = CNN(shape, block=block, mode="linear")
+    net.set_params(params)
+    g, y = net.gradients(torch.tensor(r.ravel(), device="cuda"), torch.tensor(gout.ravel(), device="cuda"), shape)
+    assert _rel(y.cpu().numpy().reshape(shape), yref) < 2e-2
+    got = ocnn.unflatten(g.cpu().numpy(), block)
+    for l in range(6):
+        assert _rel(got["W%d" % l], ref["W%d" % l]) < 3e-2, (l, _rel(got["W%d" % l], ref["W%d" % l]))
+        assert np.all(got["b%d" % l] == 0.0)
+    # linearity of the map: M(a + 2b) = M(a) + 2 M(b) up to BF16 rounding
+    a = torch.randn(int(np.prod(shape)), device="cuda")
+    b = torch.randn_like(a)
+    lhs = net.forward(a + 2 * b, shape, scale=1.0)
+    rhs = net.forward(a, shape, scale=1.0) + 2 * net.forward(b, shape, scale=1.0)
+    assert float(torch.linalg.norm(lhs - rhs) / torch.linalg.norm(rhs)) < 2e-2
+
+
+def test_crop_operator_matches_full_operator():
+    """The batched crop operator of the training loss equals the device 27-point
+    operator on the crop's interior nodes."""
+    import ctypes
+    import torch
+    from pybella_gb300 import _lib, learned, workloads
+    shape = (33, 21, 29)
+    w = workloads.stratified_3d(3, *shape)
+    A = learned.operator_3d(w)
+    u = torch.randn(A.n, device="cuda", dtype=torch.float64)
+    Au = A.matvec(u).reshape(shape)
+    h = learned.wall_zeroed_cells(w)
+    S = 16
+    offs = [(0, 0, 0), (17, 5, 13)]
+    U = torch.stack([u.reshape(shape)[i:i + S, j:j + S, k:k + S] for i, j, k in offs]).float().contiguous()
+    H = torch.stack([h[i:i + S + 1, j:j + S + 1, k:k + S + 1] for i, j, k in offs]).float().contiguous()
+    D = torch.stack([w["diag_inv"].reshape(shape)[i:i + S, j:j + S, k:k + S] for i, j, k in offs]).float().contiguous()
+    flux = torch.empty(len(offs) * (S + 1) ** 3 * 3, device="cuda")
+    y = torch.empty_like(U)
+    lib = _lib.load()
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    _lib.check(lib.bella_crop_apply(len(offs), S, p(U), p(H), p(D), w["dx"], w["dy"], w["dz"], 1, p(flux), p(y),
+                                    None), "bella_crop_apply")
+    torch.cuda.synchronize()
+    for q, (i, j, k) in enumerate(offs):
+        got = y[q, 1:-1, 1:-1, 1:-1].double()
+        ref = Au[i + 1:i + S - 1, j + 1:j + S - 1, k + 1:k + S - 1]
+        assert float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref)) < 1e-6
+        assert float(y[q, 0].abs().max()) == 0.0          # face nodes masked
+
+
+def test_flexible_solver_reaches_tolerance_and_reports():
+    """Flexible BiCGStab with an (untrained) network: the FP64 true residual meets the
+    tolerance, either by the learned iteration or by the reported plain fallback."""
+    import torch
+    from pybella_gb300 import learned, workloads
+    shape = (33, 17, 33)
+    w = workloads.stratified_3d(2, *shape)
+    A = learned.operator_3d(w)
+    net = learned.CNN(shape, block=2, mode="linear")
+    net.init(0)
+    with _nullctx():
+        x, st = A.solve(w["b"], tol=1e-8, maxiter=20000, preconditioner=net)
+    assert st["status"] == 0, st
+    r = w["b"] - A.matvec(x)
+    assert float(torch.linalg.norm(r) / torch.linalg.norm(w["b"])) <= 1e-8
+    assert st["fallback"] in (0, 1)
+
+
+class _nullctx:
+    def __enter__(self):
+        import warnings
+        self._w = warnings.catch_warnings()
+        self._w.__enter__()
+        warnings.simplefilter("ignore", RuntimeWarning)
+
+    def __exit__(self, *a):
+        self._w.__exit__(*a)
