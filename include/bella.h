@@ -191,11 +191,14 @@ int       bella_cnn_block(const bella_cnn *net);
 /* mode 0: ReLU network with biases; 1: linear (no ReLU, no biases); 2: ReLU without biases
  * (positively homogeneous); biases must be zero for modes 1 and 2 and stay zero in training */
 int       bella_cnn_set_mode(bella_cnn *net, int mode);
+/* identity path: every map (forward, gradients, training, solver) returns omega*in + CNN(in);
+ * default 0 */
+int       bella_cnn_set_skip(bella_cnn *net, float omega);
 /* FP32 parameters, layer by layer W[27][cin][cout] (tap = (dx+1)*9+(dy+1)*3+(dz+1)) then b[cout];
  * host or device pointer; set_params resets the Adam state */
 int       bella_cnn_set_params(bella_cnn *net, const float *params, void *stream);
 int       bella_cnn_get_params(bella_cnn *net, float *params, void *stream);
-/* out = CNN(in * in_scale) / in_scale on the nodes of an nx x ny x nz grid (C order,
+/* out = omega*in + CNN(in * in_scale) / in_scale on the nodes of an nx x ny x nz grid (C order,
  * z fastest); device FP32 arrays */
 int       bella_cnn_forward(bella_cnn *net, int nx, int ny, int nz, const float *in, float *out,
                             float in_scale, void *stream);
@@ -208,17 +211,18 @@ int       bella_cnn_gradients(bella_cnn *net, int nx, int ny, int nz, const floa
 int       bella_cnn_train_step(bella_cnn *net, int nsamples, int nx, int ny, int nz, const float *in,
                                const float *target, float lr, double *loss, void *stream);
 /* one Adam step on the operator residual of the predicted error over nsamples crops of
- * S^3 nodes: loss = mean_s ||interior(A_s(CNN(in_s) - target_s))||^2 / ||interior(in_s)||^2,
- * A_s the 27-point operator (hplusx = hplusy = hplusz = hcell, no hcenter/Coriolis term)
- * on the crop with zero values outside it; hcell [nsamples][(S+1)^3] cell coefficients,
+ * S^3 nodes: loss = mean_s ||core(A_s(M(in_s) - target_s))||^2 / ||core(in_s)||^2, M the map
+ * with its identity path, core = nodes at least margin nodes inside the crop, A_s the
+ * 27-point operator (hplusx = hplusy = hplusz = hcell, no hcenter/Coriolis term) on the
+ * crop with zero values outside it; hcell [nsamples][(S+1)^3] cell coefficients,
  * dinv [nsamples][S^3]; device FP32 arrays */
 int       bella_cnn_train_step_op(bella_cnn *net, int nsamples, int S, const float *in, const float *target,
                                   const float *hcell, const float *dinv, double dx, double dy, double dz,
-                                  float lr, double *loss, void *stream);
-/* y = A_crop u for the crop operator above (interior != 0 zeroes the crop's face nodes);
+                                  int margin, float lr, double *loss, void *stream);
+/* y = A_crop u for the crop operator above, zero within margin nodes of the crop's faces;
  * flux: scratch of nsamples*(S+1)^3*3 floats */
 int       bella_crop_apply(int nsamples, int S, const float *u, const float *hcell, const float *dinv,
-                           double dx, double dy, double dz, int interior, float *flux, float *y, void *stream);
+                           double dx, double dy, double dz, int margin, float *flux, float *y, void *stream);
 long long bella_cnn_launches(const bella_cnn *net);
 /* Flexible BiCGStab on the 3D operator of ws, right-preconditioned by net: the
  * preconditioner slot of scipy's bicgstab (its M argument), which the reference

@@ -256,8 +256,10 @@ __global__ void k_pack_f32(BlockMap m, const float *in, float scale, float *out)
     }
 }
 
-// net-grid f32 [nvox][8] -> node values (times RMS from sumsq when given)
-__global__ void k_unpack(BlockMap m, const float *y8, float *out, const double *sumsq) {
+// net-grid f32 [nvox][8] -> node values (times RMS from sumsq when given), plus
+// omega * skip (the identity path of the preconditioner) when skip is given
+__global__ void k_unpack(BlockMap m, const float *y8, float *out, const double *sumsq, const float *skip = nullptr,
+                         float omega = 0.f) {
     const long long n = (long long)m.B * m.nx * m.ny * m.nz;
     const float mul = sumsq ? 1.f / rms_scale(sumsq, n) : 1.f;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
@@ -268,7 +270,9 @@ __global__ void k_unpack(BlockMap m, const float *y8, float *out, const double *
         const int s = (int)(si / m.nx), i = (int)(si % m.nx);
         const long long v = (((long long)s * m.cx + i / m.b) * m.cy + j / m.b) * m.cz + k / m.b;
         const int q = ((i % m.b) * m.b + j % m.b) * m.b + k % m.b;
-        out[e] = y8[v * 8 + q] * mul;
+        float o = y8[v * 8 + q] * mul;
+        if (skip) o = fmaf(omega, skip[e], o);
+        out[e] = o;
     }
 }
 
@@ -457,9 +461,9 @@ __global__ void k_crop_flux(int B, int S, const float *u, const float *us, const
     }
 }
 
-// out = mask * dinv * (node sums of F); interior != 0 zeroes the crop's face nodes
+// out = dinv * (node sums of F), zero on nodes within `margin` nodes of the crop's faces
 __global__ void k_crop_node(int B, int S, const float *F, const float *dinv, float ox, float oy, float oz,
-                            int interior, float *out) {
+                            int margin, float *out) {
     const int C = S + 1;
     const long long n = (long long)B * S * S * S;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
@@ -481,7 +485,7 @@ __global__ void k_crop_node(int B, int S, const float *F, const float *dinv, flo
             }
         float v = 0.0625f * (ox * sx + oy * sy + oz * sz);
         if (dinv) v *= dinv[e];
-        if (interior && (i == 0 || j == 0 || k == 0 || i == S - 1 || j == S - 1 || k == S - 1)) v = 0.f;
+        if (i < margin || j < margin || k < margin || i >= S - margin || j >= S - margin || k >= S - margin) v = 0.f;
         out[e] = v;
     }
 }
@@ -492,15 +496,16 @@ __global__ void k_sub(long long n, const float *a, const float *b, float *d) {
         d[i] = a[i] - b[i];
 }
 
-// per-sample weights 1/||interior(r_s)||^2 (one block per sample)
-__global__ void k_crop_rnorm(int S, const float *r, float *w) {
+// per-sample weights 1/||core(r_s)||^2 (one block per sample; core: nodes at least
+// `margin` nodes inside the crop)
+__global__ void k_crop_rnorm(int S, int margin, const float *r, float *w) {
     __shared__ double red[32 * NQ];
     const long long nsv = (long long)S * S * S;
     const float *p = r + (long long)blockIdx.x * nsv;
     double acc[1] = {0.0};
     for (long long e = threadIdx.x; e < nsv; e += blockDim.x) {
         const int k = (int)(e % S), j = (int)((e / S) % S), i = (int)(e / ((long long)S * S));
-        if (i == 0 || j == 0 || k == 0 || i == S - 1 || j == S - 1 || k == S - 1) continue;
+        if (i < margin || j < margin || k < margin || i >= S - margin || j >= S - margin || k >= S - margin) continue;
         acc[0] += (double)p[e] * p[e];
     }
     block_sum<1>(acc, red);
@@ -533,6 +538,7 @@ using namespace bella;
 struct bella_cnn {
     int device, block;
     int linear;               // 1: no ReLU and no biases (a linear map)
+    float omega;              // identity path: output = omega * input + network
     int bias_free;            // 1: biases held at zero (positively homogeneous map)
     long long cap;            // net-grid voxel capacity
     int cin[6], cout[6];
@@ -705,7 +711,7 @@ int cnn_apply_dev(bella_cnn *net, int nx, int ny, int nz, const float *in, float
     if (!map_ok(net, m)) return BELLA_EINVAL;
     k_pack_in<<<vec_grid(m.nvox()), 256, 0, s>>>(m, in, 1.f, net->act[0], sumsq);
     forward_layers(net, m, 1.f, s);
-    k_unpack<<<vec_grid((long long)nx * ny * nz), 256, 0, s>>>(m, net->y8, out, sumsq);
+    k_unpack<<<vec_grid((long long)nx * ny * nz), 256, 0, s>>>(m, net->y8, out, sumsq, in, net->omega);
     net->launches += 2;
     return BELLA_OK;
 }
@@ -805,7 +811,7 @@ int bella_cnn_forward(bella_cnn *net, int nx, int ny, int nz, const float *in, f
     cudaStream_t s = (cudaStream_t)stream;
     k_pack_in<<<vec_grid(m.nvox()), 256, 0, s>>>(m, in, in_scale, net->act[0], nullptr);
     forward_layers(net, m, 1.f / in_scale, s);
-    k_unpack<<<vec_grid((long long)nx * ny * nz), 256, 0, s>>>(m, net->y8, out, nullptr);
+    k_unpack<<<vec_grid((long long)nx * ny * nz), 256, 0, s>>>(m, net->y8, out, nullptr, in, net->omega);
     net->launches += 2;
     return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
 }
@@ -821,7 +827,7 @@ int bella_cnn_gradients(bella_cnn *net, int nx, int ny, int nz, const float *in,
     cudaStream_t s = (cudaStream_t)stream;
     k_pack_in<<<vec_grid(m.nvox()), 256, 0, s>>>(m, in, 1.f, net->act[0], nullptr);
     forward_layers(net, m, 1.f, s);
-    if (out) k_unpack<<<vec_grid((long long)nx * ny * nz), 256, 0, s>>>(m, net->y8, out, nullptr);
+    if (out) k_unpack<<<vec_grid((long long)nx * ny * nz), 256, 0, s>>>(m, net->y8, out, nullptr, in, net->omega);
     k_pack_f32<<<vec_grid(m.nvox()), 256, 0, s>>>(m, gout, 1.f, net->g8);
     backward_layers(net, m, s);
     cudaMemcpyAsync(grads, net->grads, net->nparams * sizeof(float), cudaMemcpyDeviceToDevice, s);
@@ -870,29 +876,34 @@ int bella_cnn_train_step(bella_cnn *net, int nsamples, int nx, int ny, int nz, c
 }
 
 // y = A_crop u for nsamples crops of S^3 nodes (device FP32): hcell
-// [nsamples][(S+1)^3] cell hplus, dinv [nsamples][S^3]; interior != 0 zeroes
-// the crop's face nodes.  Scratch flux: [nsamples][(S+1)^3][3] FP32.
+// [nsamples][(S+1)^3] cell hplus, dinv [nsamples][S^3]; y is zero on nodes
+// within `margin` nodes of the crop's faces.  Scratch flux: [nsamples][(S+1)^3][3].
 int bella_crop_apply(int nsamples, int S, const float *u, const float *hcell, const float *dinv, double dx, double dy,
-                     double dz, int interior, float *flux, float *y, void *stream) {
-    if (nsamples < 1 || S < 2 || !u || !hcell || !flux || !y) return BELLA_EINVAL;
+                     double dz, int margin, float *flux, float *y, void *stream) {
+    if (nsamples < 1 || S < 2 || margin < 0 || !u || !hcell || !flux || !y) return BELLA_EINVAL;
     cudaStream_t s = (cudaStream_t)stream;
     const long long nc = (long long)nsamples * (S + 1) * (S + 1) * (S + 1), nn = (long long)nsamples * S * S * S;
     k_crop_flux<<<vec_grid(nc), 256, 0, s>>>(nsamples, S, u, nullptr, hcell, flux);
     k_crop_node<<<vec_grid(nn), 256, 0, s>>>(nsamples, S, flux, dinv, (float)(1.0 / (dx * dx)),
-                                             (float)(1.0 / (dy * dy)), (float)(1.0 / (dz * dz)), interior, y);
+                                             (float)(1.0 / (dy * dy)), (float)(1.0 / (dz * dz)), margin, y);
     return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
 }
 
 // One Adam step on the operator residual of the predicted error:
-//   loss = mean_s ||interior(A_s (CNN(r_s) - e_s))||^2 / ||interior(r_s)||^2
-// for nsamples crops of S^3 nodes (r = A e on the full grid, so on interior
-// nodes A(CNN(r) - e) = A CNN(r) - r).  hcell, dinv: the crops' operator
-// coefficients as in bella_crop_apply; the gradient through A uses
-// A^T = L diag(dinv) with L the symmetric unscaled operator.
+//   loss = mean_s ||core(A_s (M(r_s) - e_s))||^2 / ||core(r_s)||^2
+// for nsamples crops of S^3 nodes, M the map with its identity path, core the
+// nodes at least `margin` nodes inside the crop (r = A e on the full grid, so
+// there A(M(r) - e) = A M(r) - r).  A margin of the network's reach plus one
+// keeps the loss where the network never sees the crop's zero padding, as in
+// the bulk of a solve.  hcell, dinv: the crops' operator coefficients as in
+// bella_crop_apply; the gradient through A uses A^T = L diag(dinv) with L the
+// symmetric unscaled operator.
 int bella_cnn_train_step_op(bella_cnn *net, int nsamples, int S, const float *in, const float *target,
-                            const float *hcell, const float *dinv, double dx, double dy, double dz, float lr,
-                            double *loss, void *stream) {
-    if (!net || !in || !target || !hcell || !dinv || nsamples < 1 || S < 4 || !(lr > 0.f)) return BELLA_EINVAL;
+                            const float *hcell, const float *dinv, double dx, double dy, double dz, int margin,
+                            float lr, double *loss, void *stream) {
+    if (!net || !in || !target || !hcell || !dinv || nsamples < 1 || S < 4 || margin < 1 || 2 * margin >= S ||
+        !(lr > 0.f))
+        return BELLA_EINVAL;
     const int b = net->block;
     if (S % b) return BELLA_EINVAL;
     const BlockMap m = make_map(nsamples, S, S, S, b);
@@ -919,12 +930,12 @@ int bella_cnn_train_step_op(bella_cnn *net, int nsamples, int S, const float *in
     const float ox = (float)(1.0 / (dx * dx)), oy = (float)(1.0 / (dy * dy)), oz = (float)(1.0 / (dz * dz));
     k_pack_in<<<vec_grid(m.nvox()), 256, 0, s>>>(m, in, 1.f, net->act[0], nullptr);
     forward_layers(net, m, 1.f, s);
-    k_unpack<<<vec_grid(nn), 256, 0, s>>>(m, net->y8, net->yf, nullptr);
+    k_unpack<<<vec_grid(nn), 256, 0, s>>>(m, net->y8, net->yf, nullptr, in, net->omega);
     k_sub<<<vec_grid(nn), 256, 0, s>>>(nn, net->yf, target, net->gf);
     // q = interior(A (y - e))
     k_crop_flux<<<vec_grid(nc), 256, 0, s>>>(nsamples, S, net->gf, nullptr, hcell, net->flux);
-    k_crop_node<<<vec_grid(nn), 256, 0, s>>>(nsamples, S, net->flux, dinv, ox, oy, oz, 1, net->qf);
-    k_crop_rnorm<<<nsamples, 256, 0, s>>>(S, in, net->wcrop);
+    k_crop_node<<<vec_grid(nn), 256, 0, s>>>(nsamples, S, net->flux, dinv, ox, oy, oz, margin, net->qf);
+    k_crop_rnorm<<<nsamples, 256, 0, s>>>(S, margin, in, net->wcrop);
     cudaMemsetAsync(net->loss, 0, sizeof(double), s);
     k_crop_loss<<<vec_grid(nn), 256, 0, s>>>(nn, (long long)S * S * S, nsamples, net->qf, net->wcrop, net->loss);
     // g = A^T q = L (dinv * q)
@@ -952,6 +963,13 @@ int bella_cnn_block(const bella_cnn *net) { return net ? net->block : 0; }
 
 // mode bit 0: linear (no ReLU, no biases); bit 1: bias-free ReLU network.  The
 // biases must be zero for either (set_params); they then stay zero in training.
+// identity path of the map: output = omega * input + network(input)
+int bella_cnn_set_skip(bella_cnn *net, float omega) {
+    if (!net || !isfinite(omega)) return BELLA_EINVAL;
+    net->omega = omega;
+    return BELLA_OK;
+}
+
 int bella_cnn_set_mode(bella_cnn *net, int mode) {
     if (!net || mode < 0 || mode > 3) return BELLA_EINVAL;
     net->linear = mode & 1;

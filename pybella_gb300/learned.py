@@ -32,7 +32,7 @@ class CNN:
 
     MODES = {"relu": 0, "linear": 1, "relu_nobias": 2}
 
-    def __init__(self, shape, block=2, nsamples=1, device=None, mode="relu"):
+    def __init__(self, shape, block=2, nsamples=1, device=None, mode="relu", skip=0.0):
         self._lib = _lib.load()
         self.dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.block = int(block)
@@ -44,6 +44,8 @@ class CNN:
         self.nparams = int(self._lib.bella_cnn_param_count(self.block))
         self.mode = mode
         _lib.check(self._lib.bella_cnn_set_mode(self.handle, self.MODES[mode]), "bella_cnn_set_mode")
+        self.skip = float(skip)
+        _lib.check(self._lib.bella_cnn_set_skip(self.handle, self.skip), "bella_cnn_set_skip")
 
     def _stream(self):
         return ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
@@ -65,15 +67,19 @@ class CNN:
         _lib.check(self._lib.bella_cnn_get_params(self.handle, _ptr(t), self._stream()), "bella_cnn_get_params")
         return t.cpu().numpy()
 
-    def init(self, seed):
-        """He-normal weights (seeded; variance 1/fan-in for the linear net), zero biases."""
+    def init(self, seed, last_gain=None):
+        """He-normal weights (seeded; variance 1/fan-in for the linear net), zero biases.
+        ``last_gain`` scales the output layer (small with an identity path, so that
+        training starts from the plain method)."""
         rng = np.random.default_rng(seed)
         b3 = self.block ** 3
         cin, cout = [b3, 32, 32, 32, 32, 32], [32, 32, 32, 32, 32, b3]
         gain = 1.0 if self.mode == "linear" else 2.0
         parts = []
         for l in range(6):
-            parts.append((rng.standard_normal(27 * cin[l] * cout[l]) * np.sqrt(gain / (27 * cin[l]))).astype(np.float32))
+            g = 1.0 if (l < 5 or last_gain is None) else float(last_gain)
+            parts.append((g * rng.standard_normal(27 * cin[l] * cout[l]) * np.sqrt(gain / (27 * cin[l])))
+                         .astype(np.float32))
             parts.append(np.zeros(cout[l], np.float32))
         self.set_params(np.concatenate(parts))
 
@@ -230,9 +236,17 @@ def harvest_pairs(seeds, shape=(129, 65, 129), npairs=20000, crop=32, checkpoint
     return ps.trim()
 
 
-def train(net, pairs, steps=3000, batch=32, lr=1e-3, lr_final=1e-5, seed=0, log=None, log_every=250):
+def reach(block):
+    """Nodes the network's output depends on in each direction (six 3x3x3 layers)."""
+    return 6 * block + block - 1
+
+
+def train(net, pairs, steps=3000, batch=32, lr=1e-3, lr_final=1e-5, seed=0, log=None, log_every=250, margin=None):
     """Adam on the device with the net's own kernels and the operator-residual loss
-    (``bella_cnn_train_step_op``); cosine learning-rate decay.  Returns [(step, loss)]."""
+    (``bella_cnn_train_step_op``) on each window's core (``margin``: the network's
+    reach plus one by default); cosine learning-rate decay.  Returns [(step, loss)]."""
+    if margin is None:
+        margin = reach(net.block) + 1
     gen = torch.Generator(device="cuda")
     gen.manual_seed(int(seed))
     losses = []
@@ -245,7 +259,8 @@ def train(net, pairs, steps=3000, batch=32, lr=1e-3, lr_final=1e-5, seed=0, log=
         R, E, H, D = (t[idx].contiguous() for t in (pairs.R, pairs.E, pairs.H, pairs.D))
         loss = ctypes.c_double(float("nan"))
         _lib.check(lib.bella_cnn_train_step_op(net.handle, batch, pairs.S, _ptr(R), _ptr(E), _ptr(H), _ptr(D),
-                                               dx, dy, dz, float(lr_t), ctypes.byref(loss) if want else None,
+                                               dx, dy, dz, int(margin), float(lr_t),
+                                               ctypes.byref(loss) if want else None,
                                                net._stream()), "bella_cnn_train_step_op")
         if want:
             losses.append((it, loss.value))
