@@ -267,3 +267,21 @@ def train(net, pairs, steps=3000, batch=32, lr=1e-3, lr_final=1e-5, seed=0, log=
             if log:
                 log("step %d  loss %.4f  lr %.2e" % (it, loss.value, lr_t))
     return losses
+
+
+def train_preconditioner(shape=(129, 65, 129), seeds=(1, 2, 3, 5), npairs=6000, crop=48, steps=2000, batch=32,
+                         block=2, mode="linear", skip=1.0, last_gain=0.01, random_fraction=0.25,
+                         powers=(0.0, 2.0, 4.0), lr=5e-4, seed=0, log=None):
+    """Harvest pairs, train from a seeded init on the GPU and return the flat FP32 parameters.
+
+    The defaults are the configuration measured for the 3D stratified problem:
+    a linear network on 2x2x2 node blocks with an identity path (training
+    starts from the plain method), trained on the operator residual of each
+    window's core.
+    """
+    pairs = harvest_pairs(list(seeds), shape=shape, npairs=npairs, crop=crop, random_fraction=random_fraction,
+                          powers=powers, gen_seed=seed, log=log)
+    net = CNN((crop, crop, crop), block=block, nsamples=batch, mode=mode, skip=skip)
+    net.init(seed, last_gain=last_gain)
+    losses = train(net, pairs, steps=steps, batch=batch, lr=lr, seed=seed, log=log, log_every=max(1, steps // 8))
+    return net.get_params(), losses
