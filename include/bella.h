@@ -104,11 +104,15 @@ typedef struct bella_solve_stats {
     double relres;           /* final FP64 ||b - A x|| / ||b||               */
     double bnorm;            /* ||b||                                        */
     double seconds;          /* host wall time of the call                   */
-    int    fallback;         /* 1: the FP32 inner solves failed (non-finite,
-                                breakdown or no progress) and the solve was
-                                finished by FP64 BiCGStab from the FP64 iterate */
+    int    fallback;         /* 1: the FP32 (or learned) inner solves failed
+                                (non-finite, breakdown or no progress) and the
+                                solve was finished by the plain method from the
+                                FP64 iterate                                  */
     int    detail;           /* breakdown test that fired: 1 rho, 2 omega,
-                                3 <r^,A p> == 0, 4 ||A s|| == 0 (0: none)   */
+                                3 <r^,A p> == 0, 4 ||A s|| == 0, 5 the
+                                double-float recursion diverged (x is the best
+                                iterate seen, after up to 4 restarts from it)
+                                (0: none)                                     */
 } bella_solve_stats;
 
 /* ---- workspace --------------------------------------------------------- */

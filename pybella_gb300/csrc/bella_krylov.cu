@@ -661,6 +661,40 @@ static int run_inner(bella_ws *ws, int prec, const bella_solve_opts *o, cudaStre
     }
 }
 
+// Double-float iterations with a divergence guard: at every host check the
+// iterate with the smallest recursive residual so far is kept in FP64 (xbest,
+// refreshed when the residual has halved), and the run stops with *diverged
+// set when the recursive residual norm is non-finite or has grown a
+// million-fold above that best value.
+static int run_inner_guarded(bella_ws *ws, const bella_solve_opts *o, cudaStream_t s,
+                             std::chrono::steady_clock::time_point t0, int *timed_out, int *diverged, double *xbest,
+                             double *best_rr) {
+    const int blk = o->check_every > 0 ? o->check_every : 16;
+    *timed_out = 0;
+    *diverged = 0;
+    for (;;) {
+        int rc = sync_state(ws, s);
+        if (rc != BELLA_OK) return rc;
+        const double rr = ws->ks_host->rr;
+        if (!isfinite(rr) || (isfinite(*best_rr) && rr > 1e12 * *best_rr)) {
+            *diverged = 1;
+            return BELLA_OK;
+        }
+        if (rr < 0.25 * *best_rr) {
+            k_df_to_f64<<<ws->grid_vec, VEC_BLOCK, 0, s>>>(ws->n, ws->xdf, xbest);
+            ws->launches++;
+            *best_rr = rr;
+        }
+        if (ws->ks_host->done) return BELLA_OK;
+        if (o->timeout_s > 0.0) {
+            const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (el > o->timeout_s) { *timed_out = 1; return BELLA_OK; }
+        }
+        for (int k = 0; k < blk; ++k) op_iteration(ws, 2, s);
+        BELLA_CUDA(cudaGetLastError());
+    }
+}
+
 // FP64 BiCGStab with scipy's control flow; x is the solution in place.
 // x_given = 0 starts from x = 0.  Fills iterations/status/bnorm/matvecs.
 static int solve_fp64(bella_ws *ws, const double *b, double *x, const bella_solve_opts &o, int x_given,
@@ -702,16 +736,38 @@ static int solve_df(bella_ws *ws, const double *b, double *x, const bella_solve_
                                        maxiter, ws->ks, ws->partials, ws->counter);
     ws->launches++;
     BELLA_CUDA(cudaGetLastError());
-    int rc, replaced = 0, restarts = 0, iters_before = 0;
-    bool true_too_large = false;
+    int rc, replaced = 0, restarts = 0, iters_before = 0, rescues = 0;
+    bool true_too_large = false, gave_up = false;
     st->matvecs += x_given ? 1 : 0;
+    double best_rr = INFINITY;
     for (;;) {
-        rc = run_inner(ws, 2, &o, s, t0, &timed_out);
+        int diverged = 0;
+        rc = run_inner_guarded(ws, &o, s, t0, &timed_out, &diverged, ws->x64v, &best_rr);
         if (rc != BELLA_OK) return rc;
-        k_df_to_f64<<<gv, VEC_BLOCK, 0, s>>>(n, ws->xdf, x);
-        ws->launches++;
         const KState k = *ws->ks_host;
         st->detail = k.pad[0];
+        if (diverged || (k.status == BELLA_NONFINITE && isfinite(best_rr))) {
+            // the recursion blew up: continue from the best iterate seen, with a
+            // fresh Krylov process, a few times; then return that iterate
+            const double bnorm = k.dot_aux;
+            BELLA_CUDA(cudaMemcpyAsync(x, ws->x64v, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            iters_before += k.iter;
+            const int left = maxiter - iters_before;
+            if (rescues >= 4 || left <= 0 || timed_out) { gave_up = true; break; }
+            rescues++;
+            op_resid(ws, 0, x, b, ws->r64, s);
+            st->matvecs += 1;
+            k_init_df<<<gv, VEC_BLOCK, 0, s>>>(n, b, x, ws->r64, ws->xdf, ws->rdf, ws->rhdf, 1, o.tol, o.atol, left,
+                                               ws->ks, ws->partials, ws->counter);
+            ws->launches++;
+            rc = sync_state(ws, s);
+            if (rc != BELLA_OK) return rc;
+            ws->ks_host->dot_aux = bnorm;
+            best_rr = INFINITY;
+            continue;
+        }
+        k_df_to_f64<<<gv, VEC_BLOCK, 0, s>>>(n, ws->xdf, x);
+        ws->launches++;
         if (timed_out || k.status != BELLA_OK || k.iter >= maxiter) break;
         const double bnorm = k.dot_aux, atol = k.atol;
         op_resid(ws, 0, x, b, ws->r64, s);
@@ -741,12 +797,21 @@ static int solve_df(bella_ws *ws, const double *b, double *x, const bella_solve_
         }
     }
     const KState k = *ws->ks_host;
+    if (gave_up) {
+        st->iterations += iters_before;
+        st->status = timed_out ? BELLA_TIMEOUT : BELLA_BREAKDOWN;
+        st->detail = 5;                 // the recursion diverged; x is the best iterate seen
+        st->bnorm = k.dot_aux;
+        st->matvecs += 2 * iters_before;
+        st->outer = replaced + rescues;
+        return BELLA_OK;
+    }
     st->iterations += iters_before + k.iter;
     st->status = timed_out ? BELLA_TIMEOUT : k.status;
     if (st->status == BELLA_OK && true_too_large) st->status = BELLA_MAXITER;   // never on the recursive residual alone
     st->bnorm = k.dot_aux;
     st->matvecs += 2 * (iters_before + k.iter);
-    st->outer = replaced;
+    st->outer = replaced + rescues;
     return BELLA_OK;
 }
 
@@ -824,6 +889,9 @@ int bella_bicgstab(bella_ws *ws, const double *b, double *x, const bella_solve_o
                 st.outer = outer + 1;
                 // a non-finite inner iterate is never applied
                 if (inner_status == BELLA_NONFINITE || it == 0) { failed = true; break; }
+                // keep the iterate: a rejected correction is undone by copy, not by
+                // subtracting it again (which leaves rounding garbage when it is large)
+                BELLA_CUDA(cudaMemcpyAsync(ws->x64v, x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
                 k_ir_update<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->x32, rnorm, ws->z64, ns, ws->ks,
                                                      ws->partials, ws->counter);
                 ws->launches++;
@@ -833,12 +901,8 @@ int bella_bicgstab(bella_ws *ws, const double *b, double *x, const bella_solve_o
                 if (rc != BELLA_OK) return rc;
                 const double rnew = sqrt(ws->ks_host->dot_aux2);
                 if (!(rnew < rnorm)) {
-                    // no progress: take the correction back and stop refining
-                    NullSpace none = ns;
-                    none.nm = 0;
-                    k_ir_update<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->x32, -rnorm, ws->z64, none, ws->ks,
-                                                         ws->partials, ws->counter);
-                    ws->launches++;
+                    // no progress: restore the iterate and stop refining
+                    BELLA_CUDA(cudaMemcpyAsync(x, ws->x64v, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
                     failed = true;
                     break;
                 }
@@ -1076,6 +1140,7 @@ extern "C" int bella_fbicgstab(bella_ws *ws, bella_cnn *net, const double *b, do
             st.matvecs += 2 * it;
             st.outer = outer + 1;
             if (inner_status == BELLA_NONFINITE || it == 0) { failed = true; break; }
+            BELLA_CUDA(cudaMemcpyAsync(ws->x64v, x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
             k_ir_update<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->x32, rnorm, ws->z64, ns, ws->ks, ws->partials,
                                                  ws->counter);
             ws->launches++;
@@ -1084,12 +1149,8 @@ extern "C" int bella_fbicgstab(bella_ws *ws, bella_cnn *net, const double *b, do
             rc = sync_state(ws, s);
             if (rc != BELLA_OK) return rc;
             const double rnew = sqrt(ws->ks_host->dot_aux2);
-            if (!(rnew < rnorm)) {   // no progress: take the correction back, fall back
-                NullSpace none = ns;
-                none.nm = 0;
-                k_ir_update<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->x32, -rnorm, ws->z64, none, ws->ks, ws->partials,
-                                                     ws->counter);
-                ws->launches++;
+            if (!(rnew < rnorm)) {   // no progress: restore the iterate, fall back
+                BELLA_CUDA(cudaMemcpyAsync(x, ws->x64v, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
                 failed = true;
                 break;
             }

@@ -96,3 +96,21 @@ def test_solve3d_full_size_progress_is_reported():
     x, st = A.solve(w["b"], tol=1e-8, maxiter=2000, precision="df64")
     assert st["status"] in (0, 1), st
     assert np.isfinite(st["relres"]) and st["relres"] < 1.0
+
+
+def test_df64_recovers_from_a_diverging_recursion():
+    """129x65x129 seed 4 at tol 1e-10: the double-float recursion of this solve once
+    ran away to a non-finite iterate; the guard restarts it from the best iterate and
+    the returned x is finite with the residual the status reports."""
+    import torch
+    from pybella_gb300 import learned, workloads
+    w = workloads.stratified_3d(4, 129, 65, 129)
+    A = learned.operator_3d(w)
+    x, st = A.solve(w["b"], tol=1e-10, maxiter=200000, precision="df64", timeout_s=120)
+    assert torch.isfinite(x).all()
+    rel = float(torch.linalg.norm(w["b"] - A.matvec(x)) / torch.linalg.norm(w["b"]))
+    assert np.isfinite(st["relres"]) and abs(rel - st["relres"]) <= 1e-3 * st["relres"] + 1e-16
+    if st["status"] == 0:
+        assert rel <= 1e-10
+    else:
+        assert st["status"] in (1, 2, 4) and rel < 1e-6, st
