@@ -13,10 +13,14 @@ pytestmark = pytest.mark.gpu
 def test_trained_network_lowers_its_training_loss_and_solves_are_judged_by_true_residual(capsys):
     import torch
     from pybella_gb300 import learned, workloads
-    params, losses = learned.train_preconditioner(shape=(65, 33, 65), seeds=(1,), npairs=256, crop=32, steps=150,
-                                                  batch=16, block=2, mode="linear", skip=1.0, seed=0)
-    assert np.all(np.isfinite([l for _, l in losses]))
-    assert losses[-1][1] < losses[0][1], losses
+    pairs = learned.harvest_pairs([1], shape=(97, 49, 97), npairs=256, crop=40, random_fraction=0.25)
+    net0 = learned.CNN((40, 40, 40), block=2, nsamples=16, mode="linear", skip=1.0)
+    net0.init(0, last_gain=0.01)
+    losses = [l for _, l in learned.train(net0, pairs, steps=240, batch=16, lr=5e-4, log_every=1)]
+    params = net0.get_params()
+    assert np.all(np.isfinite(losses))
+    # per-batch losses are noisy: compare the means over the first and last 60 steps
+    assert np.mean(losses[-60:]) < np.mean(losses[:60]), (np.mean(losses[:60]), np.mean(losses[-60:]))
     ev = (41, 21, 41)
     w = workloads.stratified_3d(7, *ev)
     A = learned.operator_3d(w)
