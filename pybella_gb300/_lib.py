@@ -105,6 +105,15 @@ SIGNATURES = {
                                                ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
     "bella_crop_apply": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_int, _dp, _dp, ctypes.c_void_p]),
+    "bella_bicgstab_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.POINTER(SolveOpts), ctypes.c_int, ctypes.c_void_p,
+                                              ctypes.c_void_p]),
+    "bella_batch_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                            ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
+    "bella_batch_config_count": (ctypes.c_int, []),
+    "bella_batch_config": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                          ctypes.POINTER(ctypes.c_int)]),
     "bella_fbicgstab": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, _dp, _dp, ctypes.POINTER(SolveOpts),
                                        ctypes.POINTER(SolveStats), ctypes.c_void_p]),
     "bella_cnn_set_params": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_void_p]),

@@ -194,3 +194,78 @@ def stratified_3d(seed, nx=257, ny=129, nz=257, sigma=0.1, walls=(False, True, T
     return dict(hplusx=hf, hplusy=hf, hplusz=hf, hcenter=None, diag_inv=dflat,
                 b=(b.reshape(-1) * dflat).contiguous(), nx=nx, ny=ny, nz=nz, dx=dx, dy=dy, dz=dz,
                 walls=tuple(walls), corrf=0.0, seed=int(seed))
+
+
+def operator_2d(w, ws=None):
+    """Device 9-point operator of a 2D workload dict (its own workspace unless ``ws``)."""
+    from .linalg import NodalHelmholtz2D
+    return NodalHelmholtz2D(w["hplusx"], w["hplusy"], w["hcenter"], w["cor"], w["diag_inv"], w["nx"], w["ny"],
+                            w["dx"], w["dy"], x_wall=w["x_wall"], y_wall=w["y_wall"], ws=ws)
+
+
+ENSEMBLE_GRIDS = ((160, 80), (320, 160), (640, 320))
+
+
+def rising_bubble_member(cells, amplitude_K, centre_x, grav=10.0, r0=0.2, z0=0.2, device="cuda"):
+    """Operands of one pseudo-incompressible rising-bubble projection solve.
+
+    The rising-bubble set-up (inputs/rising_bubble.py:5-98): x in [-1, 1]
+    (periodic), z in [0, 1] (walls) in units of h_ref = 10 km, isentropic
+    background theta = 300 K with hydrostatic pressure, g = 10, and a warm
+    bubble theta' = amplitude * cos^2(pi r / 2), r = |(x, z) - (centre_x, z0)| / r0.
+    Cell coefficients as operator_coefficients_nodes (second_projection.py:
+    308-356): hplus = Gamma^-1 P theta (P the background rho*theta); isentropic,
+    so the buoyancy factor of multiply_inverse_coriolis is 1.  The right-hand
+    side is the nodal divergence of the bubble's buoyancy flux (0, P theta' g dt)
+    on cells (none through the walls), cleared of the operator's null modes and
+    scaled by the Jacobi diagonal of precon_diag_prepare (laplacian.py:1284-1356).
+    """
+    dev = torch.device(device)
+    cx, cz = cells
+    nx, ny = cx + 1, cz + 1
+    dx, dy = 2.0 / cx, 1.0 / cz
+    Msq, g = _consts(grav=grav)
+    Gamma = (GAMM - 1.0) / GAMM
+    # cell centres of the (nx+1) x (ny+1) cells around the inner nodes; x wraps
+    xc = -1.0 + (torch.arange(nx + 1, device=dev, dtype=torch.float64) - 0.5) * dx
+    xc = torch.remainder(xc + 1.0, 2.0) - 1.0
+    zc = (torch.arange(ny + 1, device=dev, dtype=torch.float64) - 0.5) * dy
+    X, Z = torch.meshgrid(xc, zc, indexing="ij")
+    pi = 1.0 - Gamma * g * Z                                # isentropic Exner pressure, theta = 1
+    P = pi.clamp_min(1e-6) ** (1.0 / (GAMM - 1.0))
+    r = torch.sqrt((X - centre_x) ** 2 + (Z - z0) ** 2) / r0
+    dth = torch.where(r < 1.0, (amplitude_K / T_REF) * torch.cos(0.5 * np.pi * r) ** 2, torch.zeros_like(r))
+    theta = 1.0 + dth
+    wplus = P * theta / Gamma                               # (nx+1, ny+1)
+    box = wplus[:-1, :-1] + wplus[1:, :-1] + wplus[:-1, 1:] + wplus[1:, 1:]
+    c = 0.75
+    diag = -(c / dx ** 2) * box - (c / dy ** 2) * box - (c / (dx * dy)) * box - (c / (dy * dx)) * box
+    dinv = 1.0 / diag                                       # (nx, ny)
+    dt = 0.5 * dx
+    Fy = P * dth * g * dt
+    Fy[:, 0] = 0.0
+    Fy[:, -1] = 0.0
+    b = 0.5 * ((Fy[:-1, 1:] + Fy[1:, 1:]) - (Fy[:-1, :-1] + Fy[1:, :-1])) / dy
+    E, w = null_modes_2d(nx, ny, True, False, dev)
+    G = torch.stack([torch.stack([(w * ek * el).sum() for el in E]) for ek in E]).cpu().numpy()
+    rr = torch.stack([(w * ek * b).sum() for ek in E]).cpu().numpy()
+    cf = torch.from_numpy(np.linalg.solve(G, rr)).to(dev)
+    b = b - torch.tensordot(cf, E, dims=1)
+    ones = torch.ones(ny + 1, nx + 1, dtype=torch.float64, device=dev).reshape(-1)
+    hplus = wplus.T.contiguous().reshape(-1)
+    dflat = dinv.T.contiguous().reshape(-1)
+    return dict(hplusx=hplus, hplusy=hplus.clone(), hcenter=None, cor=(ones, ones.clone(), None, None),
+                diag_inv=dflat, b=b.T.contiguous().reshape(-1) * dflat, nx=nx, ny=ny, dx=dx, dy=dy,
+                x_wall=False, y_wall=True, amplitude_K=float(amplitude_K), centre_x=float(centre_x))
+
+
+def rising_bubble_ensemble(seed, per_grid=16, grids=ENSEMBLE_GRIDS, device="cuda"):
+    """48 members (16 per grid by default): amplitude ~ N(2 K, 0.2 K), centre ~ N(0, 200 m), seeded."""
+    rng = np.random.default_rng(int(seed))
+    members = []
+    for cells in grids:
+        for _ in range(per_grid):
+            amp = rng.normal(2.0, 0.2)
+            x0 = rng.normal(0.0, 200.0 / H_REF)
+            members.append(rising_bubble_member(cells, amp, x0, device=device))
+    return members

@@ -1,0 +1,69 @@
+"""The ensemble's solves in one persistent launch (bella_bicgstab_batched):
+every member against its own single solve and, for the reference's rising-bubble
+system placed in the batch, against the reference's scipy solution."""
+import numpy as np
+import pytest
+
+from test_gpu_solver import _op, _rb_system, _rel
+
+pytestmark = pytest.mark.gpu
+
+
+def _members(per_grid=2, seed=3):
+    from pybella_gb300 import workloads
+    return workloads.rising_bubble_ensemble(seed, per_grid=per_grid)
+
+
+def test_batched_matches_single_solves_and_reference():
+    import torch
+    from pybella_gb300 import ensemble, workloads
+    ws = _members()
+    ops = [workloads.operator_2d(w) for w in ws]
+    bs = [w["b"] for w in ws]
+    # the reference's own rising-bubble system (scipy solution recorded in the fixtures)
+    op_ref, b_ref, x_ref, tol = _rb_system("full")
+    ops.insert(1, _op(op_ref))
+    bs.insert(1, torch.tensor(b_ref, device="cuda"))
+    xs, stats = ensemble.solve_ensemble(ops, bs, tol=1e-10, maxiter=20000, config=0)
+    for m, (op, b, x, st) in enumerate(zip(ops, bs, xs, stats)):
+        assert st["status"] == 0, (m, st)
+        bd = torch.as_tensor(b, device="cuda", dtype=torch.float64)
+        rel = float(torch.linalg.norm(bd - op.matvec(x)) / torch.linalg.norm(bd))
+        assert rel <= 1e-10 and abs(rel - st["relres"]) <= 1e-3 * rel, (m, rel, st)
+        xs1, st1 = op.solve(bd, tol=1e-10, maxiter=20000, precision="fp64")
+        # same algorithm, reductions summed in another order: a few iterations apart at most
+        assert abs(st["iterations"] - st1["iterations"]) <= max(3, 0.05 * st1["iterations"]), (m, st, st1)
+        assert _rel(x.cpu().numpy(), xs1.cpu().numpy()) < 1e-7, m
+    assert _rel(xs[1].cpu().numpy(), x_ref) < 1e-8
+
+
+@pytest.mark.parametrize("config", range(6))
+def test_every_launch_configuration_solves(config):
+    import torch
+    from pybella_gb300 import ensemble, workloads
+    ws = _members(per_grid=1, seed=5)
+    ops = [workloads.operator_2d(w) for w in ws]
+    xs, stats = ensemble.solve_ensemble(ops, [w["b"] for w in ws], tol=1e-10, maxiter=20000, config=config)
+    for op, w, x, st in zip(ops, ws, xs, stats):
+        assert st["status"] == 0 and st["outer"] == config
+        rel = float(torch.linalg.norm(w["b"] - op.matvec(x)) / torch.linalg.norm(w["b"]))
+        assert rel <= 1e-10
+
+
+def test_autotuned_configuration_is_used_and_members_stop_independently():
+    import torch
+    from pybella_gb300 import ensemble, workloads
+    ws = _members(per_grid=2, seed=9)
+    ops = [workloads.operator_2d(w) for w in ws]
+    bs = [w["b"] for w in ws]
+    choice, ms = ensemble.autotune(ops, bs, probe_iters=10)
+    assert 0 <= choice < len(ensemble.configs()) and all(np.isfinite(ms)) and ms[choice] == min(ms)
+    # a zero right-hand side stops at once (scipy 1.7 legacy exit) without holding the others
+    bs[0] = torch.zeros_like(bs[0])
+    xs, stats = ensemble.solve_ensemble(ops, bs, tol=1e-10, maxiter=20000)
+    assert stats[0]["status"] == 0 and stats[0]["iterations"] == 0 and float(xs[0].abs().max()) == 0.0
+    assert all(st["outer"] == choice for st in stats)
+    assert all(st["status"] == 0 for st in stats)
+    # a member capped by maxiter reports it while the rest converge
+    xs, stats = ensemble.solve_ensemble(ops, [w["b"] for w in ws], tol=1e-10, maxiter=5)
+    assert all(st["status"] == 1 and st["iterations"] == 5 for st in stats)
