@@ -50,6 +50,9 @@ def _args():
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--workload", default="solve2d", choices=["solve2d", "ensemble", "learned3d"])
+    ap.add_argument("--nz", type=int, default=257)
+    ap.add_argument("--train-steps", type=int, default=2000)
     return ap.parse_args()
 
 
@@ -352,10 +355,232 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+# --------------------------------------------------------------------------
+# ensemble: 48 rising-bubble members' solves in one persistent launch
+# --------------------------------------------------------------------------
+ENS_WORKLOAD = ("ensemble of 48 rising-bubble projection solves (16 each at 160x80, 320x160, 640x320 cells), "
+                "FP64 BiCGStab rtol 1e-10, one persistent launch per round")
+
+
+def _cpu_iter_seconds(w_np, iters=20):
+    """Seconds per FP64 BiCGStab iteration of the NumPy/SciPy restatement on this host (bounded sample)."""
+    import scipy.sparse.linalg as spla
+    from oracle import nodal2d as n2
+    n = w_np["nx"] * w_np["ny"]
+    A = spla.LinearOperator((n, n), matvec=lambda v: n2.lap2d_gather(v, w_np), dtype=np.float64)
+    cnt = [0]
+    t0 = time.perf_counter()
+    spla.bicgstab(A, w_np["b"], rtol=1e-30, atol=0.0, maxiter=iters, callback=lambda xk: cnt.__setitem__(0, cnt[0] + 1))
+    return (time.perf_counter() - t0) / max(cnt[0], 1)
+
+
+def run_ensemble(args):
+    import torch
+    from pybella_gb300 import ensemble, workloads
+    world, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    members = workloads.rising_bubble_ensemble(seed=17 + rank, device=dev)
+    ops = [workloads.operator_2d(w) for w in members]
+    bs = [w["b"] for w in members]
+    xs = [torch.zeros_like(b) for b in bs]
+    choice, tune_ms = ensemble.autotune(ops, bs, probe_iters=20)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    for i in range(args.warmup):
+        ensemble.solve_ensemble(ops, bs, tol=1e-10, maxiter=20000, out=xs)
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist is not None:
+        dist.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kms = []
+    stats = None
+    torch.cuda.synchronize()
+    ev0.record()
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        k0.record()
+        _, stats = ensemble.solve_ensemble(ops, bs, tol=1e-10, maxiter=20000, out=xs)
+        k1.record()
+        kms.append((k0, k1))
+    ev1.record()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    step_ms = [a.elapsed_time(b) for a, b in kms]
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = args.steps * world * len(ops) / (ms / 1000.0)
+    # end to end: host operands -> device, one round, solutions back to the host
+    def _np(v):
+        if isinstance(v, torch.Tensor):
+            return v.cpu().numpy()
+        if isinstance(v, tuple):
+            return tuple(_np(t) for t in v)
+        return v
+    host = [{k: _np(v) for k, v in w.items()} for w in members]
+    te0 = time.perf_counter()
+    h2d = d2h = 0
+    for i in range(args.steps):
+        ops_e = [workloads.operator_2d(h, ws=op.ws) for h, op in zip(host, ops)]
+        xs_e, _ = ensemble.solve_ensemble(ops_e, [h["b"] for h in host], tol=1e-10, maxiter=20000)
+        out = [x.cpu().numpy() for x in xs_e]
+    torch.cuda.synchronize()
+    te = time.perf_counter() - te0
+    for h in host:
+        nn, nc = h["nx"] * h["ny"], (h["nx"] + 1) * (h["ny"] + 1)
+        h2d += 8 * (4 * nc + 2 * nn)
+        d2h += 8 * nn
+    # roofline: FP64 words per node and iteration (two 5-word matvecs + 15-word vector chain)
+    peak, peak_kind = _peaks()
+    alg = sum(200.0 * op.n * st["iterations"] for op, st in zip(ops, stats))
+    achieved = alg / (statistics.median(step_ms) / 1000.0) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": ENS_WORKLOAD, "members": len(ops), "unknowns": int(sum(op.n for op in ops)),
+                   "rtol": 1e-10, "launch_config": ensemble.configs()[choice], "autotune_ms": tune_ms,
+                   "l2": "flushed (256 MB write) before every round",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": args.steps * world * len(ops) / te, "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "path": "pybella_gb300.ensemble.solve_ensemble on NumPy operands"},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "k_batch_bicgstab (whole round, one launch)",
+                     "peak_source": peak_kind, "alg_bytes_per_launch": alg},
+        "clocks": clk,
+        "solver": {"iterations": [st["iterations"] for st in stats], "status": sorted(set(st["status"] for st in stats)),
+                   "relres_max": max(st["relres"] for st in stats)},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        per_grid = {}
+        est = 0.0
+        for w, op, st in zip(host, ops, stats):
+            key = (w["nx"], w["ny"])
+            if key not in per_grid:
+                w_np = dict(w)
+                nc = (w["nx"] + 1) * (w["ny"] + 1)
+                w_np["cor"] = (w["cor"][0], w["cor"][1], np.zeros(nc), np.zeros(nc))
+                w_np["hcenter"] = np.zeros(w["nx"] * w["ny"])
+                per_grid[key] = _cpu_iter_seconds(w_np, iters=40)
+            est += per_grid[key] * st["iterations"]
+        line["cpu_baseline"] = {"value": len(ops) / est, "unit": "solves/s", "cores": 1, "kind": "port",
+                                "sample": "40 FP64 BiCGStab iterations per grid size (NumPy lap2D_gather_new "
+                                          "restatement + scipy); a round = sum over members of s/iteration x the "
+                                          "member's iterations"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+# --------------------------------------------------------------------------
+# learned preconditioner vs plain BiCGStab on the 3D 27-point problem
+# --------------------------------------------------------------------------
+def run_learned3d(args):
+    import torch
+    from pybella_gb300 import learned, workloads
+    world, rank, local = _dist()
+    if world > 1 and rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    shape = (args.nx, args.ny, args.nz)
+    t0 = time.perf_counter()
+    params, losses = learned.train_preconditioner(steps=args.train_steps)
+    train_s = time.perf_counter() - t0
+    w = workloads.stratified_3d(7, *shape)
+    A = learned.operator_3d(w)
+    net = learned.CNN(shape, block=2, mode="linear", skip=1.0)
+    net.set_params(params)
+    b = w["b"]
+    res = {}
+    clocks = ClockSampler(local)
+    for name, kw in (("plain", dict(precision="df64")), ("learned", dict(preconditioner=net))):
+        for _ in range(args.warmup):
+            A.solve(b, tol=1e-8, maxiter=200000, **kw)
+        if name == "learned":
+            clocks.start()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        sts = []
+        for _ in range(args.steps):
+            import warnings
+            with warnings.catch_warnings():
+                warnings.simplefilter("ignore", RuntimeWarning)
+                _, st = A.solve(b, tol=1e-8, maxiter=200000, **kw)
+            sts.append(st)
+        e1.record()
+        torch.cuda.synchronize()
+        res[name] = {"ms": e0.elapsed_time(e1) / args.steps, "stats": sts}
+    clk = clocks.stop()
+    # tensor-core rate of the network on this grid
+    x32 = torch.randn(A.n, device=dev)
+    y32 = torch.empty_like(x32)
+    for _ in range(3):
+        net.forward(x32, shape, scale=1.0, out=y32)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(10):
+        net.forward(x32, shape, scale=1.0, out=y32)
+    e1.record()
+    torch.cuda.synchronize()
+    cnn_ms = e0.elapsed_time(e1) / 10
+    nv = learned.net_voxels(shape, 2)
+    flops = nv * 2 * 27 * (16 * 32 + 4 * 32 * 32 + 32 * 8)
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            tpeak, tkind = float(json.load(f)["bf16_tflops_sustained"]), "measured (sustained)"
+    except (OSError, KeyError, ValueError):
+        tpeak, tkind = 1700.0, "fallback"
+    ach = flops / (cnn_ms / 1000.0) / 1e12
+    L, P = res["learned"], res["plain"]
+    line = {
+        "metric": METRIC, "value": 1000.0 / L["ms"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": L["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16 network + f32 inner / f64 refinement", "data": "synthetic",
+        "config": {"workload": "3D 27-point solve %s nodes, rtol 1e-8: flexible BiCGStab with the learned "
+                               "preconditioner vs plain double-float BiCGStab" % "x".join(map(str, shape)),
+                   "network": "6 layers 3x3x3, 32 channels, 2x2x2-blocked grid, linear with identity path",
+                   "train_steps": args.train_steps, "train_s": train_s, "final_loss": losses[-1][1],
+                   "l2": "inputs larger than L2 (%.0f MB of operator planes)" % (A.n * 8 * 9 / 1e6)},
+        "plain": {"solves_per_s": 1000.0 / P["ms"], "iterations": P["stats"][-1]["iterations"],
+                  "relres": P["stats"][-1]["relres"]},
+        "learned": {"solves_per_s": 1000.0 / L["ms"], "iterations": L["stats"][-1]["iterations"],
+                    "relres": L["stats"][-1]["relres"], "fallback": L["stats"][-1]["fallback"],
+                    "status": L["stats"][-1]["status"]},
+        "learned_over_plain": P["ms"] / L["ms"],
+        "e2e": None,
+        "gpu_launches": None,
+        "roofline": {"bound": "tensor", "achieved": ach, "peak": tpeak, "unit": "TFLOP/s", "frac": ach / tpeak,
+                     "traffic": None, "kernel": "k_conv3d (6 layers, one network application)",
+                     "peak_source": tkind, "flops_per_launch": flops, "ms_per_application": cnn_ms},
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = _args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "ensemble":
+        run_ensemble(args)
+    elif args.workload == "learned3d":
+        if args.nx == NX and args.ny == NY:
+            args.nx, args.ny = 257, 129
+        run_learned3d(args)
     else:
         run_gpu(args)
 
