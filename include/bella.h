@@ -183,16 +183,21 @@ int bella_projection2d(bella_ws *ws, const bella_proj2d *args, const bella_solve
  * Each member is the reference's call (second_projection.py:205-230) on its own
  * workspace (bella_op2d_set): FP64 BiCGStab, scipy 1.7 control flow, x0 = 0.
  * One cooperative kernel iterates all members (phases separated by a bounded
- * grid barrier); tol, atol, maxiter from opts.  config: index of a launch
- * configuration (tile shape, CTAs per SM), < 0 for the autotuned one.
- * stats[m].outer reports the configuration used.  Returns BELLA_OK when every
- * member converged, else the first failing member's status. */
+ * grid barrier); tol, atol, maxiter from opts; opts->precision 0: FP64
+ * arithmetic, otherwise double-float on the FP32 pipe, whose members are
+ * refined in FP64 (residual, batched correction solve, update) when their FP64
+ * true residual misses the tolerance.  config: index of a launch configuration
+ * (tile shape, CTAs per SM), < 0 for the autotuned one.  stats[m].outer reports
+ * the configuration used, stats[m].fallback the refinement rounds of member m.
+ * Returns BELLA_OK when every member converged, else the first failing
+ * member's status. */
 int bella_bicgstab_batched(bella_ws *const *ws, int nmembers, const double *const *b, double *const *x,
                            const bella_solve_opts *opts, int config, bella_solve_stats *stats, void *stream);
 /* times every launch configuration on probe_iters iterations of this batch and keeps
- * the fastest for these member sizes; ms (optional) receives the times */
+ * the fastest for these member sizes and precision (0 FP64, else double-float);
+ * ms (optional) receives the times */
 int bella_batch_autotune(bella_ws *const *ws, int nmembers, const double *const *b, double *const *x,
-                         int probe_iters, int *choice, double *ms, void *stream);
+                         int precision, int probe_iters, int *choice, double *ms, void *stream);
 int bella_batch_config_count(void);
 int bella_batch_config(int index, int *tile_x, int *tile_y, int *ctas_per_sm);
 

@@ -109,7 +109,7 @@ SIGNATURES = {
                                               ctypes.POINTER(SolveOpts), ctypes.c_int, ctypes.c_void_p,
                                               ctypes.c_void_p]),
     "bella_batch_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
-                                            ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                            ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                             ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
     "bella_batch_config_count": (ctypes.c_int, []),
     "bella_batch_config": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),

@@ -47,7 +47,10 @@ def configs():
     return out
 
 
-def autotune(ops, bs, probe_iters=20):
+PRECISIONS = {"fp64": 0, "df64": 2}
+
+
+def autotune(ops, bs, probe_iters=20, precision="df64"):
     """Time every launch configuration on this ensemble; returns (choice, ms per config)."""
     lib = _lib.load()
     dev, bd, xs = _prep(ops, bs)
@@ -56,14 +59,19 @@ def autotune(ops, bs, probe_iters=20):
     ms = (ctypes.c_double * n)()
     choice = ctypes.c_int()
     with torch.cuda.device(dev):
-        _lib.check(lib.bella_batch_autotune(W, len(ops), B, X, int(probe_iters), ctypes.byref(choice), ms,
+        _lib.check(lib.bella_batch_autotune(W, len(ops), B, X, PRECISIONS[precision], int(probe_iters),
+                                            ctypes.byref(choice), ms,
                                             ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)),
                    "bella_batch_autotune")
     return choice.value, list(ms)
 
 
-def solve_ensemble(ops, bs, tol=1e-10, atol=0.0, maxiter=6000, config=-1, out=None):
-    """Solve ``ops[m] x_m = bs[m]`` for all members in one launch; returns (xs, stats list)."""
+def solve_ensemble(ops, bs, tol=1e-10, atol=0.0, maxiter=6000, config=-1, out=None, precision="df64"):
+    """Solve ``ops[m] x_m = bs[m]`` for all members in one launch; returns (xs, stats list).
+
+    ``precision='df64'`` (default) iterates in double-float on the FP32 pipe with
+    FP64 refinement of members whose FP64 true residual misses the tolerance
+    (``stats[m]['fallback']`` counts those rounds); ``'fp64'`` iterates in FP64."""
     lib = _lib.load()
     dev, bd, xs = _prep(ops, bs)
     if out is not None:
@@ -72,6 +80,7 @@ def solve_ensemble(ops, bs, tol=1e-10, atol=0.0, maxiter=6000, config=-1, out=No
     o = _lib.SolveOpts()
     lib.bella_solve_opts_default(ctypes.byref(o))
     o.tol, o.atol, o.maxiter = float(tol), float(atol or 0.0), int(maxiter)
+    o.precision = PRECISIONS[precision]
     st = (_lib.SolveStats * len(ops))()
     with torch.cuda.device(dev):
         rc = lib.bella_bicgstab_batched(W, len(ops), B, X, ctypes.byref(o), int(config), st,
