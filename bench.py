@@ -225,7 +225,8 @@ def run_gpu(args):
         dist.init_process_group("nccl", device_id=dev)
 
     nseeds = max(1, min(args.seeds, args.steps + args.warmup))
-    systems = [workloads.stratified_2d(seed=1000 * rank + s, nx=NX, ny=NY, device=dev) for s in range(nseeds)]
+    from pybella_gb300 import replicas
+    systems = [workloads.stratified_2d(seed=sd, nx=NX, ny=NY, device=dev) for sd in replicas.seeds_for_rank(rank, nseeds)]
     ws = _lib.Workspace(local)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     xbuf = torch.empty(NX * NY, dtype=torch.float64, device=dev)
@@ -271,12 +272,9 @@ def run_gpu(args):
     launches = ws.launches - launches0
     kt = {k: ws.kernel_time(k) for k in range(4)}
     ws.profile(False)
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(ms, device=dev)
     total_solves = args.steps * world
-    value = total_solves / (ms / 1000.0)
+    value = replicas.aggregate_rate(args.steps, world, ms / 1000.0)
 
     # ---- end to end through the drop-in API with host buffers ----
     host = [] if args.no_e2e else [_to_np(systems[i % nseeds]) for i in range(min(nseeds, 4))]
