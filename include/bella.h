@@ -179,6 +179,29 @@ typedef struct bella_proj2d {
 int bella_projection2d(bella_ws *ws, const bella_proj2d *args, const bella_solve_opts *opts,
                        bella_solve_stats *stats, void *stream);
 
+/* ---- explicit parts of the projection (2D), in place on device arrays ------
+ * Arrays as in bella_proj2d (reference NumPy C order over (x, y), ghosts
+ * included).  S0c: mpv.HydroState.get_S0c(elem) on cells; S0n, hydro_rhoY0,
+ * strat_inv as in bella_proj2d. */
+typedef struct {
+    int inx, iny;                 /* node.iicx, node.iicy                              */
+    int x_wall, y_wall;
+    double dx, dy, dt;
+    double Msq, g, gamm, nonhydro, compressibility;
+    double coriolis[3];           /* ud.coriolis_strength                              */
+    double wind[3];               /* ud.u_wind_speed, v_wind_speed, w_wind_speed       */
+    int is_compressible, is_ArakawaKonor;
+    double *rho, *rhou, *rhov, *rhow, *rhoY, *rhoX;
+    double *p2;                   /* mpv.p2_nodes (forward step)                       */
+    double *rhs_out;              /* mpv.rhs, (inx+2)x(iny+2) (forward step)           */
+    const double *S0c, *S0n, *hydro_rhoY0, *strat_inv;
+} bella_expl2d;
+/* euler_forward_non_advective (second_projection.py:22-74): momenta, rhoX, p2,
+ * mpv.rhs, ghost nodes and boundary data */
+int bella_euler_forward2d(const bella_expl2d *args, void *stream);
+/* euler_backward_non_advective_expl_part (second_projection.py:77-92) */
+int bella_expl_part2d(const bella_expl2d *args, void *stream);
+
 /* ---- ensemble: the solves of many 2D members in one persistent launch ----
  * Each member is the reference's call (second_projection.py:205-230) on its own
  * workspace (bella_op2d_set): FP64 BiCGStab, scipy 1.7 control flow, x0 = 0.

@@ -52,6 +52,17 @@ class Proj2D(ctypes.Structure):
                             "p2", "hydro_rhoY0", "S0n", "strat_inv", "rhs_out")]
 
 
+class Expl2D(ctypes.Structure):
+    _fields_ = [("inx", ctypes.c_int), ("iny", ctypes.c_int), ("x_wall", ctypes.c_int), ("y_wall", ctypes.c_int),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dt", ctypes.c_double),
+                ("Msq", ctypes.c_double), ("g", ctypes.c_double), ("gamm", ctypes.c_double),
+                ("nonhydro", ctypes.c_double), ("compressibility", ctypes.c_double),
+                ("coriolis", ctypes.c_double * 3), ("wind", ctypes.c_double * 3),
+                ("is_compressible", ctypes.c_int), ("is_ArakawaKonor", ctypes.c_int)] + \
+        [(k, ctypes.c_void_p) for k in ("rho", "rhou", "rhov", "rhow", "rhoY", "rhoX", "p2", "rhs_out",
+                                         "S0c", "S0n", "hydro_rhoY0", "strat_inv")]
+
+
 class SolveOpts(ctypes.Structure):
     """``bella_solve_opts``."""
     _fields_ = [("tol", ctypes.c_double), ("atol", ctypes.c_double),
@@ -114,6 +125,8 @@ SIGNATURES = {
     "bella_batch_config_count": (ctypes.c_int, []),
     "bella_batch_config": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                           ctypes.POINTER(ctypes.c_int)]),
+    "bella_euler_forward2d": (ctypes.c_int, [ctypes.POINTER(Expl2D), ctypes.c_void_p]),
+    "bella_expl_part2d": (ctypes.c_int, [ctypes.POINTER(Expl2D), ctypes.c_void_p]),
     "bella_fbicgstab": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, _dp, _dp, ctypes.POINTER(SolveOpts),
                                        ctypes.POINTER(SolveStats), ctypes.c_void_p]),
     "bella_cnn_set_params": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_void_p]),

@@ -11,6 +11,9 @@
 //   k_ghost_x / _y      set_ghostnodes_p2 (periodic_plus_one, reflect)  boundary.py:296-369
 //   k_correction        grad_nodes + correction_nodes              :280-306, :496-521
 //   k_scatter_add       p2_full[i2] = x; p2_nodes += p2_full       :241-245, :275
+// and the explicit parts (bella_euler_forward2d, bella_expl_part2d):
+//   k_fw_div / k_fw_cells / k_fw_nodes   euler_forward_non_advective  :22-74
+//   k_ex_cells          euler_backward_non_advective_expl_part       :77-92
 // Array layout is the reference's NumPy C order over (x, y).
 #include <cstring>
 #include <string>
@@ -323,6 +326,96 @@ __global__ void k_add(long long n, double *a, const double *b) {
     if (e < n) a[e] += b[e];
 }
 
+// ---- explicit parts (second_projection.py:22-92) --------------------------------
+struct ExplDev {
+    double u0, v0, w0;       // background wind
+    double c1, cv, c2;       // coriolis strengths (ud.coriolis_strength)
+    double ak;               // 1 - is_ArakawaKonor
+};
+
+// divergence_nodes without the 1/dt (:39) and scale_wall_node_values(rhs, 2.0) (:40,
+// second_projection.py:433-474: rows 1 and -2 of a wall axis, the other axis [2:-2])
+__global__ void k_fw_div(ProjDev P, const double *rho, const double *rhou, const double *rhov, const double *rhoY,
+                         double *div) {
+    const int nix = P.icx - 1, niy = P.icy - 1;
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= (long long)nix * niy) return;
+    const int a = (int)(e / niy), b = (int)(e - (long long)a * niy);
+    auto qu = [&](int i, int j) { return rhou[cidx(P, i, j)] * (rhoY[cidx(P, i, j)] / rho[cidx(P, i, j)]); };
+    auto qv = [&](int i, int j) { return rhov[cidx(P, i, j)] * (rhoY[cidx(P, i, j)] / rho[cidx(P, i, j)]); };
+    const double d0 = (qu(a + 1, b) - qu(a, b)) / P.dx;
+    const double d1 = (qu(a + 1, b + 1) - qu(a, b + 1)) / P.dx;
+    const double e0 = (qv(a, b + 1) - qv(a, b)) / P.dy;
+    const double e1 = (qv(a + 1, b + 1) - qv(a + 1, b)) / P.dy;
+    double v = 0.5 * (d0 + d1) + 0.5 * (e0 + e1);
+    if (P.xbc == 1 && (a == 1 || a == nix - 2) && b >= 2 && b < niy - 2) v *= 2.0;
+    if (P.ybc == 1 && (b == 1 || b == niy - 2) && a >= 2 && a < nix - 2) v *= 2.0;
+    div[e] = v;
+}
+
+// momenta and rhoX of euler_forward_non_advective (:45-64), every cell, old p2
+__global__ void k_fw_cells(ProjDev P, ExplDev X, const double *p2, double *rho, double *rhou, double *rhov,
+                           double *rhow, const double *rhoY, double *rhoX, const double *S0c, const double *S0n) {
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= (long long)P.icx * P.icy) return;
+    const int i = (int)(e / P.icy), j = (int)(e - (long long)i * P.icy);
+    const double a00 = p2[nidx(P, i, j)], a01 = p2[nidx(P, i, j + 1)];
+    const double a10 = p2[nidx(P, i + 1, j)], a11 = p2[nidx(P, i + 1, j + 1)];
+    double Dpx = 0.0, Dpy = 0.0;
+    Dpx = Dpx + -1.0 * a00; Dpy = Dpy + -1.0 * a00;
+    Dpx = Dpx + -1.0 * a01; Dpy = Dpy + 1.0 * a01;
+    Dpx = Dpx + 1.0 * a10;  Dpy = Dpy + -1.0 * a10;
+    Dpx = Dpx + 1.0 * a11;  Dpy = Dpy + 1.0 * a11;
+    Dpx = Dpx * (0.5 / P.dx);
+    Dpy = Dpy * (0.5 / P.dy);
+    const double Gammainv = P.gamm / (P.gamm - 1.0);
+    const double r = rho[e], rY = rhoY[e], ru = rhou[e], rv = rhov[e], rw = rhow[e];
+    const double rhoYovG = Gammainv * rY;
+    const double dbuoy = rY * (rhoX[e] / r);
+    const double drhou = ru - X.u0 * r, drhov = rv - X.v0 * r, drhow = rw - X.w0 * r;
+    const double v = rv / r;
+    const double ch1 = X.c1, cv = X.cv, ch2 = X.c2;
+    rhou[e] = ru - P.dt * (rhoYovG * Dpx - ch2 * drhov + cv * drhow);
+    rhov[e] = rv - P.dt * (rhoYovG * Dpy + (P.g / P.Msq) * dbuoy * P.nonhydro - ch1 * drhow + ch2 * drhou) * X.ak;
+    rhoX[e] = (r * (r / rY - S0c[e])) - P.dt * (v * dSdy(P, S0n, j)) * r;
+}
+
+// p2[1:-1,1:-1] += compressibility * (-dt * dpidP * div) (:45-47, :66-69)
+__global__ void k_fw_nodes(ProjDev P, const double *rhoY, const double *div, double *p2) {
+    const int nix = P.icx - 1, niy = P.icy - 1;
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= (long long)nix * niy) return;
+    const int a = (int)(e / niy), b = (int)(e - (long long)a * niy);
+    const double ex = P.gamm - 2.0;
+    const double box = pow(rhoY[cidx(P, a, b)], ex) + pow(rhoY[cidx(P, a + 1, b)], ex) +
+                       pow(rhoY[cidx(P, a, b + 1)], ex) + pow(rhoY[cidx(P, a + 1, b + 1)], ex);
+    const double dpidP = ((P.gamm - 1.0) / P.Msq) * box / 4.0;
+    const double dp = 0.0 - P.dt * dpidP * div[e];
+    double &q = p2[nidx(P, a + 1, b + 1)];
+    q = q + P.compressibility * dp;
+}
+
+// euler_backward_non_advective_expl_part (:82-90), every cell
+__global__ void k_ex_cells(ProjDev P, ExplDev X, double *rho, double *rhou, double *rhov, double *rhow,
+                           const double *rhoY, const double *rhoX, const double *S0n) {
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= (long long)P.icx * P.icy) return;
+    const int j = (int)(e % P.icy);
+    const double r = rho[e];
+    const double dbuoy = rhoY[e] * (rhoX[e] / r);
+    double U = rhou[e], V = (P.nonhydro * rhov[e]) - P.dt * (P.g / P.Msq) * dbuoy, W = rhow[e];
+    U = U + (-1.0 * X.u0) * r;
+    V = V + (-1.0 * X.v0) * r;
+    W = W + (-1.0 * X.w0) * r;
+    const CorCoef c = cor_coef(P, rhoY[e] / r, dSdy(P, S0n, j));
+    const double U2 = c.denom * (c.uu * U + c.uv * V + c.uw * W);
+    const double V2 = c.denom * (c.vu * U + c.vv * V + c.vw * W);
+    const double W2 = c.denom * (c.wu * U + c.wv * V + c.ww * W);
+    rhou[e] = U2 + (1.0 * X.u0) * r;
+    rhov[e] = V2 + (1.0 * X.v0) * r;
+    rhow[e] = W2 + (1.0 * X.w0) * r;
+}
+
 }  // namespace bella
 
 using namespace bella;
@@ -425,4 +518,59 @@ extern "C" int bella_projection2d(bella_ws *ws, const bella_proj2d *a, const bel
     ws->launches += 9;
     if (cudaGetLastError() != cudaSuccess) return BELLA_ECUDA;
     return st;
+}
+
+static int expl_setup(const bella_expl2d *a, ProjDev &P, ExplDev &X) {
+    if (!a || a->inx < 3 || a->iny < 3 || !a->rho || !a->rhou || !a->rhov || !a->rhow || !a->rhoY || !a->rhoX ||
+        !a->S0n || !a->hydro_rhoY0 || !a->strat_inv || !(a->dt > 0.0))
+        return BELLA_EINVAL;
+    P.icx = a->inx + 3; P.icy = a->iny + 3;
+    P.ncx = a->inx + 4; P.ncy = a->iny + 4;
+    P.xbc = a->x_wall ? 1 : 0; P.ybc = a->y_wall ? 1 : 0;
+    P.dx = a->dx; P.dy = a->dy; P.dt = a->dt; P.Msq = a->Msq; P.g = a->g; P.gamm = a->gamm;
+    P.nonhydro = a->nonhydro; P.compressibility = a->compressibility;
+    P.wh1 = a->dt * a->coriolis[0]; P.wv = a->dt * a->coriolis[1]; P.wh2 = a->dt * a->coriolis[2];
+    P.is_compressible = a->is_compressible;
+    X.u0 = a->wind[0]; X.v0 = a->wind[1]; X.w0 = a->wind[2];
+    X.c1 = a->coriolis[0]; X.cv = a->coriolis[1]; X.c2 = a->coriolis[2];
+    X.ak = 1.0 - (double)a->is_ArakawaKonor;
+    return BELLA_OK;
+}
+
+extern "C" int bella_euler_forward2d(const bella_expl2d *a, void *stream) {
+    ProjDev P;
+    ExplDev X;
+    int rc = expl_setup(a, P, X);
+    if (rc != BELLA_OK) return rc;
+    if (!a->p2 || !a->rhs_out || !a->S0c) return BELLA_EINVAL;
+    cudaStream_t s = (cudaStream_t)stream;
+    const long long ncell = (long long)P.icx * P.icy, nisc = (long long)(P.icx - 1) * (P.icy - 1);
+    // divergence of the momenta with the wall ghosts zeroed (:39-42), into mpv.rhs
+    k_zero_ghost_momenta<<<grid1(P.icx), 256, 0, s>>>(P, a->rhou, a->rhov, a->rhow);
+    k_fw_div<<<grid1(nisc), 256, 0, s>>>(P, a->rho, a->rhou, a->rhov, a->rhoY, a->rhs_out);
+    // momenta and rhoX with the old p2 (:45-64), then p2 (:66-69)
+    k_fw_cells<<<grid1(ncell), 256, 0, s>>>(P, X, a->p2, a->rho, a->rhou, a->rhov, a->rhow, a->rhoY, a->rhoX,
+                                           a->S0c, a->S0n);
+    k_fw_nodes<<<grid1(nisc), 256, 0, s>>>(P, a->rhoY, a->rhs_out, a->p2);
+    // ghost nodes and boundary data (:71-72)
+    k_ghost_x<<<grid1(P.ncy), 256, 0, s>>>(P, a->p2);
+    k_ghost_y<<<grid1(P.ncx), 256, 0, s>>>(P, a->p2);
+    k_bd_x<<<grid1(P.icy), 256, 0, s>>>(P, a->rho, a->rhou, a->rhov, a->rhow, a->rhoY, a->rhoX);
+    k_bd_y<<<grid1(P.icx), 256, 0, s>>>(P, a->rho, a->rhou, a->rhov, a->rhow, a->rhoY, a->rhoX, a->hydro_rhoY0,
+                                       a->strat_inv);
+    return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
+}
+
+extern "C" int bella_expl_part2d(const bella_expl2d *a, void *stream) {
+    ProjDev P;
+    ExplDev X;
+    int rc = expl_setup(a, P, X);
+    if (rc != BELLA_OK) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const long long ncell = (long long)P.icx * P.icy;
+    k_ex_cells<<<grid1(ncell), 256, 0, s>>>(P, X, a->rho, a->rhou, a->rhov, a->rhow, a->rhoY, a->rhoX, a->S0n);
+    k_bd_x<<<grid1(P.icy), 256, 0, s>>>(P, a->rho, a->rhou, a->rhov, a->rhow, a->rhoY, a->rhoX);
+    k_bd_y<<<grid1(P.icx), 256, 0, s>>>(P, a->rho, a->rhou, a->rhov, a->rhow, a->rhoY, a->rhoX, a->hydro_rhoY0,
+                                       a->strat_inv);
+    return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
 }

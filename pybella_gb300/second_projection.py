@@ -8,6 +8,11 @@ Coriolis factors, Jacobi diagonal, divergence, the BiCGStab solve, ghost
 nodes, correction -- runs as kernels of libbella_gb300
 (``bella_projection2d``).  2D only; the reference's 3D branches cannot run.
 
+``euler_forward_non_advective`` (second_projection.py:22) and
+``euler_backward_non_advective_expl_part`` (:77) are the explicit parts of the
+step (bella_euler_forward2d, bella_expl_part2d), with the same signatures and
+in-place effects.
+
 Not reproduced: the side-effect attributes ``mpv.wplus``, ``mpv.wcenter``,
 ``mpv.nu_c`` and ``mpv.u/v/w`` that the reference leaves behind; nothing on
 the projection path reads them afterwards.
@@ -107,3 +112,84 @@ def euler_backward_non_advective_impl_part(Sol, mpv, elem, node, ud, th, t, dt, 
         logging.warning("projection solve status %d (%s), true relative residual %.3e",
                         rc, ws._lib.bella_status_string(rc).decode(), st.relres)
     return None
+
+
+def _expl_args(Sol, mpv, elem, node, ud, th, dt, keep, dev, with_p2):
+    def d(a, name):
+        t_ = torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(dev)
+        keep[name] = t_
+        return ctypes.c_void_p(t_.data_ptr())
+
+    a = _lib.Expl2D()
+    a.inx, a.iny = int(node.iicx), int(node.iicy)
+    a.x_wall, a.y_wall = int(_is_wall(ud.bdry_type[0])), int(_is_wall(ud.bdry_type[1]))
+    a.dx, a.dy, a.dt = float(node.dx), float(node.dy), float(dt)
+    a.Msq, a.g, a.gamm = float(ud.Msq), float(ud.gravity_strength[1]), float(th.gamm)
+    a.nonhydro, a.compressibility = float(ud.nonhydrostasy), float(ud.compressibility)
+    for k in range(3):
+        a.coriolis[k] = float(ud.coriolis_strength[k])
+    a.wind[0], a.wind[1], a.wind[2] = float(ud.u_wind_speed), float(ud.v_wind_speed), float(ud.w_wind_speed)
+    a.is_compressible = int(ud.is_compressible)
+    a.is_ArakawaKonor = int(getattr(ud, "is_ArakawaKonor", 0))
+    for f in _FIELDS:
+        setattr(a, f, d(getattr(Sol, f), f))
+    if with_p2:
+        a.p2 = d(mpv.p2_nodes, "p2")
+        a.S0c = d(mpv.HydroState.get_S0c(elem), "S0c")
+        rhs = torch.empty(tuple(node.isc[:2]), dtype=torch.float64, device=dev)
+        keep["rhs"] = rhs
+        a.rhs_out = ctypes.c_void_p(rhs.data_ptr())
+    a.S0n = d(mpv.HydroState_n.S0, "S0n")
+    a.hydro_rhoY0 = d(mpv.HydroState.rhoY0, "hydro_rhoY0")
+    a.strat_inv = d(np.array([1.0 / ud.stratification(y) for y in elem.y], dtype=np.float64), "strat_inv")
+    return a
+
+
+def euler_forward_non_advective(Sol, mpv, elem, node, dt, ud, th, writer=None, label=None, debug=False,
+                                device=None):
+    """Explicit (forward) projection of second_projection.py:22-74 on the GPU (2D).
+
+    Updates ``Sol`` (momenta, rhoX, ghost cells), ``mpv.p2_nodes`` and
+    ``mpv.rhs`` in place, as the reference does.
+    """
+    if elem.ndim != 2:
+        raise NotImplementedError("the device explicit projection is 2D")
+    if hasattr(ud, "LAMB_BDRY"):
+        raise NotImplementedError("the LAMB_BDRY variant is not on this path")
+    dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+    keep = {}
+    a = _expl_args(Sol, mpv, elem, node, ud, th, dt, keep, dev, True)
+    lib = _lib.load()
+    with torch.cuda.device(dev):
+        _lib.check(lib.bella_euler_forward2d(ctypes.byref(a), ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)),
+                   "bella_euler_forward2d")
+    for f in _FIELDS:
+        setattr(Sol, f, keep[f].cpu().numpy())
+    mpv.p2_nodes[...] = keep["p2"].cpu().numpy()
+    mpv.rhs[...] = keep["rhs"].cpu().numpy()
+
+
+def euler_backward_non_advective_expl_part(Sol, mpv, elem, dt, ud, th, device=None):
+    """Explicit part of the implicit step, second_projection.py:77-92, on the GPU (2D); updates ``Sol``."""
+    if elem.ndim != 2:
+        raise NotImplementedError("the device explicit projection is 2D")
+    dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+    keep = {}
+    # elem doubles as the node grid for the sizes this call needs (the reference passes elem, elem
+    # to multiply_inverse_coriolis); the node counts come from elem.sc
+    node = _NodeSizes(elem)
+    a = _expl_args(Sol, mpv, elem, node, ud, th, dt, keep, dev, False)
+    lib = _lib.load()
+    with torch.cuda.device(dev):
+        _lib.check(lib.bella_expl_part2d(ctypes.byref(a), ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)),
+                   "bella_expl_part2d")
+    for f in _FIELDS:
+        setattr(Sol, f, keep[f].cpu().numpy())
+
+
+class _NodeSizes:
+    """Node-grid sizes derived from the cell grid (elem.sc = inx - 1 + 4 per axis)."""
+
+    def __init__(self, elem):
+        self.iicx, self.iicy = int(elem.sc[0]) - 3, int(elem.sc[1]) - 3
+        self.dx, self.dy = float(elem.dx), float(elem.dy)

@@ -13,6 +13,10 @@ It imports the reference through ``refshim`` (numba, h5py, ... stubbed; SciPy
 * ``diag_kat.npz``    -- ``precon_diag_prepare`` (laplacian.py:1284-1356);
 * ``pieces_kat.npz``  -- ``divergence_nodes``, ``correction_nodes``,
   ``set_ghostnodes_p2`` and ``set_explicit_boundary_data`` on a random state;
+* ``explicit_kat.npz`` -- ``euler_forward_non_advective`` and
+  ``euler_backward_non_advective_expl_part`` (second_projection.py:22-92) on
+  perturbed rising-bubble states, with and without Coriolis / background wind /
+  compressibility;
 * ``rising_bubble_step0.npz`` -- inputs and outputs of the two non-trivial
   ``euler_backward_non_advective_impl_part`` calls of the first rising-bubble
   time step (160x80 cells, pseudo-incompressible, tol 1e-10): the full-step
@@ -151,6 +155,69 @@ def pieces_kat(out):
     np.savez_compressed(os.path.join(out, "pieces_kat.npz"), **rec)
 
 
+def explicit_kat(out):
+    """The explicit parts of the projection on perturbed 64x32 rising-bubble states."""
+    import dycore.physics.low_mach.second_projection as lm_sp
+    rec = {}
+    cases = [("a", dict()),
+             ("b", dict(coriolis=(0.3, 0.2, 0.1), wind=(0.5, 0.0, 0.2), compressibility=1.0))]
+    for tag, opt in cases:
+        rng = np.random.default_rng(11 if tag == "a" else 12)
+        ud, elem, node, Sol, th, mpv = _rb_setup_sized(64, 32)
+        if "coriolis" in opt:
+            ud.coriolis_strength = np.array(opt["coriolis"])
+            ud.u_wind_speed, ud.v_wind_speed, ud.w_wind_speed = opt["wind"]
+            ud.compressibility = opt["compressibility"]
+        for k in ("rhou", "rhov", "rhow", "rhoX"):
+            setattr(Sol, k, getattr(Sol, k) + 0.01 * rng.standard_normal(elem.sc[:2]))
+        Sol.rho = Sol.rho * (1.0 + 0.01 * rng.standard_normal(elem.sc[:2]))
+        Sol.rhoY = Sol.rhoY * (1.0 + 0.001 * rng.standard_normal(elem.sc[:2]))
+        mpv.p2_nodes[...] = 0.1 * rng.standard_normal(node.sc[:2])
+        dt = 0.005
+        rec[tag + "_scalars"] = np.array([ud.Msq, ud.gravity_strength[1], th.gamm, ud.nonhydrostasy,
+                                          ud.compressibility, ud.is_compressible, dt,
+                                          *ud.coriolis_strength, ud.u_wind_speed, ud.v_wind_speed,
+                                          ud.w_wind_speed, getattr(ud, "is_ArakawaKonor", 0)])
+        rec[tag + "_S0c"] = np.copy(mpv.HydroState.get_S0c(elem))
+        rec[tag + "_S0n"] = np.copy(mpv.HydroState_n.S0)
+        rec[tag + "_rhoY0"] = np.copy(mpv.HydroState.rhoY0)
+        rec[tag + "_strat_inv"] = np.array([1.0 / ud.stratification(y) for y in elem.y])
+        for k in FIELDS:
+            rec[tag + "_in_" + k] = np.copy(getattr(Sol, k))
+        rec[tag + "_p2_in"] = np.copy(mpv.p2_nodes)
+        # euler_forward_non_advective on a copy of the state
+        import copy
+        Sol_f, mpv_f = copy.deepcopy(Sol), copy.deepcopy(mpv)
+        lm_sp.euler_forward_non_advective(Sol_f, mpv_f, elem, node, dt, ud, th)
+        for k in FIELDS:
+            rec[tag + "_fw_" + k] = np.copy(getattr(Sol_f, k))
+        rec[tag + "_fw_p2"] = np.copy(mpv_f.p2_nodes)
+        rec[tag + "_fw_rhs"] = np.copy(mpv_f.rhs)
+        # euler_backward_non_advective_expl_part on another copy
+        Sol_e, mpv_e = copy.deepcopy(Sol), copy.deepcopy(mpv)
+        lm_sp.euler_backward_non_advective_expl_part(Sol_e, mpv_e, elem, dt, ud, th)
+        for k in FIELDS:
+            rec[tag + "_ex_" + k] = np.copy(getattr(Sol_e, k))
+    np.savez_compressed(os.path.join(out, "explicit_kat.npz"), **rec)
+
+
+def _rb_setup_sized(inx, iny):
+    import dycore.discretisation.grid as dis_grid
+    import dycore.utils.variable as var
+    import dycore.physics.low_mach.mpv as lm_var
+    import dycore.physics.gas_dynamics.thermodynamic as gd_thermodynamics
+    import inputs.rising_bubble as rb
+    ud = _ud_rising_bubble()
+    ud.inx, ud.iny = inx, iny
+    elem, node = dis_grid.grid_init(ud)
+    Sol = var.Vars(elem.sc, ud)
+    th = gd_thermodynamics.init(ud)
+    mpv = lm_var.MPV(elem, node, ud)
+    Sol = rb.sol_init(Sol, mpv, elem, node, th, ud)
+    ud.nonhydrostasy = 1.0
+    return ud, elem, node, Sol, th, mpv
+
+
 def rising_bubble_step0(out):
     import dycore.discretisation.time_update as dis_time_update
     import dycore.physics.low_mach.second_projection as lm_sp
@@ -201,13 +268,16 @@ def rising_bubble_step0(out):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    ref = args[0] if args else "/root/reference"
     refshim.install(ref)
     out = HERE
     lap2d_kat(out)
     diag_kat(out)
     pieces_kat(out)
-    rising_bubble_step0(out)
+    explicit_kat(out)
+    if "--explicit-only" not in sys.argv:
+        rising_bubble_step0(out)
     print("fixtures written to", out)
 
 

@@ -121,3 +121,39 @@ def test_stratified_rhs_is_consistent():
     x, info, it = bicgstab_legacy(w["op"], w["b"], 1e-8, 5000)
     assert info == 0
     assert true_relres(w["op"], x, w["b"]) <= 1e-8
+
+
+def _explicit_case(tag):
+    from oracle import nodal2d as n2
+    d = np.load(golden("explicit_kat.npz"))
+    sc = d[tag + "_scalars"]
+    Msq, g, gamm, nonhydro, compressibility, is_comp, dt = sc[:7]
+    cor, wind, arakawa = sc[7:10], sc[10:13], int(sc[13])
+    grid = n2.Grid2D(64, 32, -1.0, 1.0, 0.0, 1.0, (n2.PERIODIC, n2.WALL))
+    prm = n2.Params(Msq=Msq, g=g, gamm=gamm, coriolis=cor, nonhydro=nonhydro, is_compressible=int(is_comp),
+                    compressibility=compressibility)
+    Sol = {k: d["%s_in_%s" % (tag, k)].copy() for k in ("rho", "rhou", "rhov", "rhow", "rhoY", "rhoX")}
+    hc = {"rhoY0": d[tag + "_rhoY0"]}
+    return d, grid, prm, Sol, hc, float(dt), wind, arakawa
+
+
+@pytest.mark.parametrize("tag", ["a", "b"])
+def test_oracle_explicit_parts_match_reference(tag):
+    """euler_forward_non_advective and euler_backward_non_advective_expl_part
+    (second_projection.py:22-92) against the reference's outputs."""
+    from oracle import nodal2d as n2
+    d, grid, prm, Sol, hc, dt, wind, arakawa = _explicit_case(tag)
+    strat = lambda y: 1.0
+    p2 = d[tag + "_p2_in"].copy()
+    S = {k: v.copy() for k, v in Sol.items()}
+    rhs = n2.euler_forward_non_advective(S, p2, d[tag + "_S0c"], d[tag + "_S0n"], grid, prm, dt, hc, strat,
+                                         wind=wind, is_ArakawaKonor=arakawa)
+    # bit for bit (same expression order; the box sum uses the reference's fftconvolve)
+    for k in S:
+        np.testing.assert_array_equal(S[k], d["%s_fw_%s" % (tag, k)], err_msg=k)
+    np.testing.assert_array_equal(p2, d[tag + "_fw_p2"])
+    np.testing.assert_array_equal(rhs, d[tag + "_fw_rhs"])
+    S = {k: v.copy() for k, v in Sol.items()}
+    n2.euler_backward_non_advective_expl_part(S, d[tag + "_S0n"], grid, prm, dt, hc, strat, wind=wind)
+    for k in S:
+        np.testing.assert_array_equal(S[k], d["%s_ex_%s" % (tag, k)], err_msg=k)
