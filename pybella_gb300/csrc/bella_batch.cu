@@ -251,7 +251,7 @@ __device__ void stencil_tile(const BMember<T> &M, int lt, const MScal &c, int k,
     T *pnew = M.p[par], *vnew = M.v[par];
     const bool first = (k == 0);
     const T beta = Num<T>::from(c.beta), omega = Num<T>::from(c.omega), alpha = Num<T>::from(c.alpha);
-    const T half = Num<T>::from(0.5), zero = Num<T>::from(0.0);
+    const T zero = Num<T>::from(0.0);
     for (int e = threadIdx.x; e < (TYB + 2) * (TXB + 2); e += blockDim.x) {
         const int la = e / (TXB + 2), lb = e - la * (TXB + 2);
         int gj = j0 - 1 + la, gi = i0 - 1 + lb;
@@ -280,8 +280,9 @@ __device__ void stencil_tile(const BMember<T> &M, int lt, const MScal &c, int k,
             const size_t cc = (size_t)cj * (nx + 1) + ci;
             const T tl = su[la * (TXB + 2) + lb], tr = su[la * (TXB + 2) + lb + 1];
             const T bl = su[(la + 1) * (TXB + 2) + lb], br = su[(la + 1) * (TXB + 2) + lb + 1];
-            const T gx = half * ((tr - tl) + (br - bl));
-            const T gy = half * ((bl - tl) + (br - tr));
+            const T d1 = br - tl, d2 = tr - bl;     // diagonal differences (bella_op2d.cu)
+            const T gx = half_of(d1 + d2);
+            const T gy = half_of(d1 - d2);
             fx = op.axx[cc] * gx;
             fy = op.ayy[cc] * gy;
             if (M.cross) {
@@ -289,8 +290,8 @@ __device__ void stencil_tile(const BMember<T> &M, int lt, const MScal &c, int k,
                 fy += op.ayx[cc] * gx;
             }
         }
-        sfx[e] = fx;
-        sfy[e] = fy;
+        sfx[e] = fx + fy;   // P
+        sfy[e] = fx - fy;   // M
     }
     __syncthreads();
     AccT a0, a1, a2;
@@ -302,8 +303,7 @@ __device__ void stencil_tile(const BMember<T> &M, int lt, const MScal &c, int k,
             const size_t g = (size_t)gj * nx + gi;
             const T u = su[(la + 1) * (TXB + 2) + lb + 1];
             const int W = TXB + 1;
-            T s = ((sfx[la * W + lb + 1] + sfx[(la + 1) * W + lb + 1]) - (sfx[la * W + lb] + sfx[(la + 1) * W + lb])) +
-                  ((sfy[(la + 1) * W + lb] + sfy[(la + 1) * W + lb + 1]) - (sfy[la * W + lb] + sfy[la * W + lb + 1]));
+            T s = (sfy[la * W + lb + 1] - sfy[(la + 1) * W + lb]) + (sfx[(la + 1) * W + lb + 1] - sfx[la * W + lb]);
             if (M.has_hc) s += op.hc[g] * u;
             const T y = s * op.dinv[g];
             if (MODE == 1) {

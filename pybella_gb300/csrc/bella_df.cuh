@@ -68,6 +68,10 @@ __device__ __forceinline__ dfloat operator-(dfloat a, dfloat b) { return df_add(
 __device__ __forceinline__ dfloat operator*(dfloat a, dfloat b) { return df_mul(a, b); }
 __device__ __forceinline__ dfloat &operator+=(dfloat &a, dfloat b) { a = df_add(a, b); return a; }
 
+// x / 2, exact in every type (scaling by a power of two)
+template <typename T> __device__ __forceinline__ T half_of(T a) { return (T)0.5 * a; }
+template <> __device__ __forceinline__ dfloat half_of<dfloat>(dfloat a) { return dfloat(a.hi * 0.5f, a.lo * 0.5f); }
+
 // Inner-product accumulator: each product a*b of two double-floats is formed
 // to ~2^-48 relative (exact hi*hi via fmaf plus the cross terms) and summed
 // into a compensated FP32 pair; converted to FP64 once per thread.

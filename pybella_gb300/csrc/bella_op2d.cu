@@ -2,13 +2,15 @@
 // BiCGStab kernels built on it (sm_103a).
 //
 // The operator is the reference's lap2D_gather_new (laplacian.py:546-746)
-// rewritten in cell-flux form: every cell c computes
-//   Gx = 0.5*((TR-TL)+(BR-BL)),  Gy = 0.5*((BL-TL)+(BR-TR))
-//   Fx = Axx*Gx + Axy*Gy,        Fy = Ayy*Gy + Ayx*Gx
-// once, and each node sums the fluxes of its four cells:
-//   y = dinv * ( Fx[TR]+Fx[BR]-Fx[TL]-Fx[BL] + Fy[BL]+Fy[BR]-Fy[TL]-Fy[TR] + hc*u )
+// rewritten in cell-flux form: every cell c computes, from the diagonal
+// differences d1 = BR - TL and d2 = TR - BL,
+//   Gx = (d1 + d2)/2 = ((TR-TL)+(BR-BL))/2,  Gy = (d1 - d2)/2 = ((BL-TL)+(BR-TR))/2
+//   Fx = Axx*Gx + Axy*Gy,  Fy = Ayy*Gy + Ayx*Gx,  P = Fx + Fy,  M = Fx - Fy
+// once, and each node sums its four cells
+//   y = dinv * ( (M[TR] - M[BL]) + (P[BR] - P[TL]) + hc*u )
+//     = dinv * ( Fx[TR]+Fx[BR]-Fx[TL]-Fx[BL] + Fy[BL]+Fy[BR]-Fy[TL]-Fy[TR] + hc*u )
 // which is algebraically the reference's Dxx+Dyy+Dyx+Dxy+hcenter*p scaled by
-// diag_inv (laplacian.py:721-739).  Walls are folded into the cell planes
+// diag_inv (laplacian.py:721-739); 9 additions per node instead of 13.  Walls are folded into the cell planes
 // (zeroed outer cell column/row, laplacian.py:691-713); the periodic wrap
 // with the duplicated seam (laplacian.py:595-638) is done on the halo load.
 //
@@ -155,8 +157,9 @@ k_stencil2d(Op2D<T> op, StArgs<T> a, KState *ks, double *partials, unsigned *cou
                 const size_t c = (size_t)cj * (nx + 1) + ci;
                 const T tl = su[la][lb], tr = su[la][lb + 1];
                 const T bl = su[la + 1][lb], br = su[la + 1][lb + 1];
-                const T gx = (T)0.5 * ((tr - tl) + (br - bl));
-                const T gy = (T)0.5 * ((bl - tl) + (br - tr));
+                const T d1 = br - tl, d2 = tr - bl;
+                const T gx = half_of(d1 + d2);
+                const T gy = half_of(d1 - d2);
                 fx = op.axx[c] * gx;
                 fy = op.ayy[c] * gy;
                 if (CROSS) {
@@ -164,8 +167,8 @@ k_stencil2d(Op2D<T> op, StArgs<T> a, KState *ks, double *partials, unsigned *cou
                     fy += op.ayx[c] * gx;
                 }
             }
-            sfx[la][lb] = fx;
-            sfy[la][lb] = fy;
+            sfx[la][lb] = fx + fy;   // P
+            sfy[la][lb] = fx - fy;   // M
         }
         __syncthreads();
         // 3. node outputs
@@ -177,8 +180,9 @@ k_stencil2d(Op2D<T> op, StArgs<T> a, KState *ks, double *partials, unsigned *cou
             if (gj < ny && gi < nx) {
                 const size_t g = (size_t)gj * nx + gi;
                 const T u = su[la + 1][lb + 1];
-                T s = ((sfx[la][lb + 1] + sfx[la + 1][lb + 1]) - (sfx[la][lb] + sfx[la + 1][lb])) +
-                      ((sfy[la + 1][lb] + sfy[la + 1][lb + 1]) - (sfy[la][lb] + sfy[la][lb + 1]));
+                // cells around node (la+1, lb+1) of the halo tile: TL (la, lb), TR (la, lb+1),
+                // BL (la+1, lb), BR (la+1, lb+1); sfx holds P, sfy holds M
+                T s = (sfy[la][lb + 1] - sfy[la + 1][lb]) + (sfx[la + 1][lb + 1] - sfx[la][lb]);
                 if (HC) s += op.hc[g] * u;
                 T yv = s * op.dinv[g];
                 if (MODE == M_RESID) {
