@@ -114,3 +114,26 @@ def test_df64_recovers_from_a_diverging_recursion():
         assert rel <= 1e-10
     else:
         assert st["status"] in (1, 2, 4) and rel < 1e-6, st
+
+
+def test_3d_solutions_against_the_fp64_solve(capsys):
+    """129x65x129 to a 1e-10 relative residual: the double-float and the mixed
+    (FP32 inner iterations in FP64 refinement) solutions against the pure-FP64 GPU
+    solve of the same system."""
+    import torch
+    from pybella_gb300 import learned, workloads
+    w = workloads.stratified_3d(2, 129, 65, 129)
+    A = learned.operator_3d(w)
+    x64, s64 = A.solve(w["b"], tol=1e-10, maxiter=200000, precision="fp64", timeout_s=120)
+    assert s64["status"] == 0, s64
+    out = {}
+    for prec in ("df64", "mixed"):
+        x, st = A.solve(w["b"], tol=1e-10, maxiter=200000, precision=prec, timeout_s=120)
+        assert st["status"] == 0 and st["relres"] <= 1e-10, (prec, st)
+        err = float(torch.linalg.norm(x - x64) / torch.linalg.norm(x64))
+        out[prec] = (err, st["iterations"], st["fallback"])
+        # both are solutions to 1e-10 of a system whose condition number is ~1e5-1e6
+        assert err < 1e-4, (prec, err)
+    with capsys.disabled():
+        print("\n3D 129x65x129 rtol 1e-10, rel L2 vs FP64 (%d iterations): %s"
+              % (s64["iterations"], {k: "%.2e (%d it, fallback %d)" % v for k, v in out.items()}))

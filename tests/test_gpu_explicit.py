@@ -109,3 +109,43 @@ def test_explicit_parts_time(capsys):
         torch.cuda.synchronize()
         with capsys.disabled():
             print("\n%s at 640x320 cells: %.1f us per call" % (fn.__name__, e0.elapsed_time(e1) / 20 * 1e3))
+
+
+def _ref_objects(d, tag):
+    """Reference-shaped Sol / mpv / elem / node / ud / th objects for the drop-ins."""
+    from types import SimpleNamespace as NS
+    sc = d[tag + "_scalars"]
+    Msq, g, gamm, nonhydro, compressibility, is_comp, dt = sc[:7]
+    Sol = NS(**{f: d["%s_in_%s" % (tag, f)].copy() for f in FIELDS})
+    S0c = d[tag + "_S0c"]
+    mpv = NS(p2_nodes=d[tag + "_p2_in"].copy(), rhs=np.zeros((66, 34)),
+             HydroState=NS(get_S0c=lambda elem: S0c, rhoY0=d[tag + "_rhoY0"]),
+             HydroState_n=NS(S0=d[tag + "_S0n"]))
+    dx, dy = 2.0 / 63.0, 1.0 / 31.0
+    y = -2 * dy + 0.5 * dy + dy * np.arange(35)
+    elem = NS(ndim=2, sc=(67, 35), y=y, dx=dx, dy=dy)
+    node = NS(iicx=64, iicy=32, dx=dx, dy=dy, isc=(66, 34))
+    ud = NS(bdry_type=["periodic", "wall", "wall"], Msq=Msq, gravity_strength=[0.0, g, 0.0],
+            nonhydrostasy=nonhydro, compressibility=compressibility, is_compressible=int(is_comp),
+            coriolis_strength=sc[7:10], u_wind_speed=sc[10], v_wind_speed=sc[11], w_wind_speed=sc[12],
+            is_ArakawaKonor=int(sc[13]), stratification=lambda yy: 1.0)
+    th = NS(gamm=gamm)
+    return Sol, mpv, elem, node, ud, th, float(dt)
+
+
+@pytest.mark.parametrize("tag", ["a", "b"])
+def test_python_drop_ins_match_reference(tag):
+    """pybella_gb300.second_projection.euler_forward_non_advective and
+    euler_backward_non_advective_expl_part with the reference's argument objects."""
+    from pybella_gb300 import second_projection as sp
+    d = np.load(golden("explicit_kat.npz"))
+    Sol, mpv, elem, node, ud, th, dt = _ref_objects(d, tag)
+    sp.euler_forward_non_advective(Sol, mpv, elem, node, dt, ud, th)
+    for f in FIELDS:
+        _close(getattr(Sol, f), d["%s_fw_%s" % (tag, f)], f)
+    _close(mpv.p2_nodes, d[tag + "_fw_p2"], "p2")
+    _close(mpv.rhs, d[tag + "_fw_rhs"], "rhs")
+    Sol, mpv, elem, node, ud, th, dt = _ref_objects(d, tag)
+    sp.euler_backward_non_advective_expl_part(Sol, mpv, elem, dt, ud, th)
+    for f in FIELDS:
+        _close(getattr(Sol, f), d["%s_ex_%s" % (tag, f)], f)
