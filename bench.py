@@ -2,9 +2,13 @@
 
 One step = one projection solve of one seeded synthetic system: the
 reference-packed operands are turned into device flux planes
-(bella_op2d_set) and solved by BiCGStab on the GPU (``--precision fp64``,
-the default: the reference algorithm in FP64; ``mixed``: FP32 inner solves
-in FP64 refinement with FP64 fallback) to a true relative residual of 1e-8.
+(bella_op2d_set) and solved by BiCGStab on the GPU (``--precision df64``,
+the default: double-float arithmetic on the FP32 pipe, convergence judged on
+the FP64 true residual; ``fp64``: the reference algorithm in FP64; ``mixed``:
+FP32 inner solves in FP64 refinement with FP64 fallback) to a true relative
+residual of 1e-8.  ``--workload ensemble`` times the 48-member ensemble in one
+persistent launch per round; ``--workload learned3d`` trains the learned
+preconditioner and times it against plain BiCGStab on the 3D 27-point system.
 Seeds cycle over up to 64 pre-generated systems resident in HBM; the L2 is
 flushed (256 MB write) before every step.
 
