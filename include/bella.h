@@ -243,6 +243,11 @@ int       bella_cnn_set_mode(bella_cnn *net, int mode);
 /* identity path: every map (forward, gradients, training, solver) returns omega*in + CNN(in);
  * default 0 */
 int       bella_cnn_set_skip(bella_cnn *net, float omega);
+/* forward layers 0-4 on the tcgen05 tensor-core path (1) or mma.sync (0); tcgen05 is used
+ * when the padded z extent of the grid the net runs on is at most 204 */
+int       bella_cnn_set_tc(bella_cnn *net, int on);
+/* 1 if a tensor-core completion wait gave up since the last call (synchronises) */
+int       bella_cnn_tc_error(bella_cnn *net);
 /* FP32 parameters, layer by layer W[27][cin][cout] (tap = (dx+1)*9+(dy+1)*3+(dz+1)) then b[cout];
  * host or device pointer; set_params resets the Adam state */
 int       bella_cnn_set_params(bella_cnn *net, const float *params, void *stream);

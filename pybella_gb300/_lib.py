@@ -110,6 +110,8 @@ SIGNATURES = {
     "bella_cnn_block": (ctypes.c_int, [ctypes.c_void_p]),
     "bella_cnn_set_mode": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "bella_cnn_set_skip": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float]),
+    "bella_cnn_set_tc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "bella_cnn_tc_error": (ctypes.c_int, [ctypes.c_void_p]),
     "bella_cnn_train_step_op": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp,
                                                ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                                ctypes.c_float,

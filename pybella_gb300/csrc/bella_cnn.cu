@@ -184,6 +184,185 @@ k_conv3d(int nx, int ny, int nz, int xseg, const __nv_bfloat16 *__restrict__ in,
 template <int CIN, int COUT>
 constexpr size_t conv_smem() { return (size_t)27 * COUT * CIN * 2 + (size_t)CH_VOX * CIN * 2; }
 
+// ---------------------------------------------------------------------------
+// The same convolution on the sm_100-family tensor-core path: tcgen05.mma with
+// FP32 accumulators in tensor memory.  Rows of the GEMM are 128 consecutive
+// positions of the zero-padded (y, z) plane of one x-plane, f = (y+1)*PZ + (z+1)
+// with PZ = nz + 2: for tap (dx, dy, dz) the A operand is the same row set of
+// input plane x+dx shifted by dy*PZ + dz rows, so every tap reads a canonical
+// K-major operand straight from the staged planes (no im2col copy).  Staged
+// layout per input plane: [16-byte channel chunk][row][8 channels]; the
+// descriptor's LBO steps between the two chunks of a K=16 step, its SBO between
+// groups of 8 rows.  Rows on the padding ring are computed and discarded.
+// A work item is one x-plane and TC_ROWS padded rows (TC_MB accumulators of
+// 128 rows, 32 TMEM columns each).  One thread issues the MMAs and commits them
+// to an mbarrier; the wait is bounded and on time-out the CTA records an error,
+// frees its tensor memory and returns.
+constexpr int TC_MB = 4;                    // 128-row accumulators per work item
+constexpr int TC_ROWS = 128 * TC_MB;
+constexpr long long TC_SPIN_LIMIT = 1LL << 24;
+
+__device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;                 // sm_100-family descriptor version; no swizzle
+    return d;
+}
+
+template <int N>
+__device__ __forceinline__ uint32_t tc_idesc() {   // kind::f16: BF16 x BF16 -> FP32, K-major A and B, M = 128
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+
+template <int CIN, int COUT>
+__host__ __device__ constexpr size_t tc_smem_bytes(int pz) {
+    return (size_t)27 * (CIN / 8) * COUT * 16 + (size_t)3 * (CIN / 8) * (TC_ROWS + 2 * pz + 2) * 16 + 16;
+}
+
+template <int CIN, int COUT, bool RELU>
+__global__ void __launch_bounds__(256, 1)
+k_conv3d_tc(int nx, int ny, int nz, int xseg, const __nv_bfloat16 *__restrict__ in,
+            const __nv_bfloat16 *__restrict__ Wtc, const float *__restrict__ bias, __nv_bfloat16 *out, int *err) {
+    static_assert(COUT == 32, "tensor-memory epilogue reads 32 columns");
+    constexpr int NCH = CIN / 8;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int ok_flag;
+    const int PZ = nz + 2, PY = ny + 2;
+    const int L = TC_ROWS + 2 * PZ + 2;                   // staged rows per plane and chunk
+    unsigned char *sW = smem;                             // [27][NCH][COUT][16 B]
+    unsigned char *sA = smem + (size_t)27 * NCH * COUT * 16;   // [3][NCH][L][16 B]
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // weights (already in the tap-chunk-row order of the descriptors)
+    for (int e = tid; e < 27 * NCH * COUT; e += 256)
+        reinterpret_cast<uint4 *>(sW)[e] = reinterpret_cast<const uint4 *>(Wtc)[e];
+    const uint32_t mbar_a = (uint32_t)__cvta_generic_to_shared(&mbar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_a));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (warp == 0) {
+        const uint32_t slot = (uint32_t)__cvta_generic_to_shared(&tmem_slot);
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(32 * TC_MB));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_slot;
+    const uint32_t sW_a = (uint32_t)__cvta_generic_to_shared(sW), sA_a = (uint32_t)__cvta_generic_to_shared(sA);
+    const long long plane = (long long)PY * PZ;
+    const int nblk = (int)((plane + TC_ROWS - 1) / TC_ROWS);
+    const long long nitems = (long long)nx * nblk;
+    uint32_t phase = 0;
+    for (long long item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const int i = (int)(item / nblk), fb = (int)(item - (long long)i * nblk);
+        const long long f0 = (long long)fb * TC_ROWS - (PZ + 1);   // padded row of staged row 0
+        // ---- stage the three input planes (zero outside the grid and the sample's x segment)
+        for (int e = tid; e < 3 * NCH * L; e += 256) {
+            const int xp = e / (NCH * L), rem = e - xp * (NCH * L), ch = rem / L, rb = rem - ch * L;
+            const int gi = i - 1 + xp;
+            const long long f = f0 + rb;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (gi >= 0 && gi < nx && (gi / xseg) == (i / xseg) && f >= 0 && f < plane) {
+                const int y = (int)(f / PZ) - 1, z = (int)(f % PZ) - 1;
+                if (y >= 0 && y < ny && z >= 0 && z < nz)
+                    v = *reinterpret_cast<const uint4 *>(in + (((size_t)gi * ny + y) * nz + z) * CIN + ch * 8);
+            }
+            reinterpret_cast<uint4 *>(sA)[((size_t)xp * NCH + ch) * L + rb] = v;
+        }
+        asm volatile("fence.proxy.async.shared::cta;");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        // ---- one thread issues 27 taps x CIN/16 k-steps for each 128-row accumulator
+        if (tid == 0) {
+            const uint32_t idesc = tc_idesc<COUT>();
+            for (int mb = 0; mb < TC_MB; ++mb) {
+                int first = 1;
+                for (int tap = 0; tap < 27; ++tap) {
+                    const int dx = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dz = tap % 3 - 1;
+                    const int row0 = mb * 128 + (PZ + 1) + dy * PZ + dz;
+                    for (int ks = 0; ks < CIN / 16; ++ks) {
+                        const uint32_t a = sA_a + (uint32_t)((((dx + 1) * NCH + 2 * ks) * (long long)L + row0) * 16);
+                        const uint32_t b = sW_a + (uint32_t)(((tap * NCH + 2 * ks) * COUT) * 16);
+                        const uint64_t ad = tc_sdesc(a, (uint32_t)L * 16, 128), bd = tc_sdesc(b, COUT * 16, 128);
+                        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                                     ::"r"(tmem + (uint32_t)(mb * 32)), "l"(ad), "l"(bd), "r"(idesc), "r"(first ? 0 : 1));
+                        first = 0;
+                    }
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_a));
+            uint32_t done = 0;
+            for (long long it = 0; it < TC_SPIN_LIMIT && !done; ++it)
+                asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                             "selp.b32 %0, 1, 0, p;\n\t}" : "=r"(done) : "r"(mbar_a), "r"(phase));
+            ok_flag = done ? 1 : 0;
+        }
+        __syncthreads();
+        phase ^= 1;
+        if (!ok_flag) {
+            if (tid == 0) atomicExch(err, 1);
+            break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        // ---- epilogue: warp w reads rows 32*(w%4).. of accumulators 2*(w/4) and 2*(w/4)+1
+        for (int h = 0; h < 2; ++h) {
+            const int mb = (warp >> 2) * 2 + h;
+            uint32_t r[32];
+            const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(mb * 32);
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                         "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                         "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                           "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                           "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+                           "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+                           "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                         : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+            const long long f = (long long)fb * TC_ROWS + mb * 128 + (warp & 3) * 32 + lane;
+            if (f < plane) {
+                const int y = (int)(f / PZ) - 1, z = (int)(f % PZ) - 1;
+                if (y >= 0 && y < ny && z >= 0 && z < nz) {
+                    uint32_t w[16];
+#pragma unroll
+                    for (int c = 0; c < 16; ++c) {
+                        float v0 = __uint_as_float(r[2 * c]), v1 = __uint_as_float(r[2 * c + 1]);
+                        if (bias) { v0 += bias[2 * c]; v1 += bias[2 * c + 1]; }
+                        if (RELU) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
+                        const __nv_bfloat162 h2 = __floats2bfloat162_rn(v0, v1);
+                        w[c] = *reinterpret_cast<const uint32_t *>(&h2);
+                    }
+                    uint4 *o = reinterpret_cast<uint4 *>(out + (((size_t)i * ny + y) * nz + z) * COUT);
+                    o[0] = make_uint4(w[0], w[1], w[2], w[3]);
+                    o[1] = make_uint4(w[4], w[5], w[6], w[7]);
+                    o[2] = make_uint4(w[8], w[9], w[10], w[11]);
+                    o[3] = make_uint4(w[12], w[13], w[14], w[15]);
+                }
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();                     // accumulators read, staging buffer free
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(32 * TC_MB));
+}
+
+// kernel weights [27][COUTP][CINP] -> tensor-core operand order [27][CINP/8][COUTP][8]
+__global__ void k_wk_to_tc(const __nv_bfloat16 *wk, int cinp, int coutp, __nv_bfloat16 *wtc) {
+    const int total = 27 * cinp * coutp;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        const int tap = e / (cinp * coutp), r = e - tap * cinp * coutp, co = r / cinp, ci = r - co * cinp;
+        wtc[(((size_t)tap * (cinp / 8) + ci / 8) * coutp + co) * 8 + (ci % 8)] = wk[e];
+    }
+}
+
 // Node grid <-> net grid.  Samples are stacked along x: node (s, i, j, k) of a
 // [B][nx][ny][nz] array maps to net voxel ((s*cx + i/b)*cy + j/b)*cz + k/b and
 // sub-node channel ((i%b)*b + j%b)*b + k%b, with cx = ceil(nx/b) etc.
@@ -538,6 +717,9 @@ using namespace bella;
 struct bella_cnn {
     int device, block;
     int linear;               // 1: no ReLU and no biases (a linear map)
+    int use_tc;               // 1: layers 0-4 of the forward pass on tcgen05 (k_conv3d_tc)
+    __nv_bfloat16 *wtc[5];    // their weights in tensor-core operand order
+    int *tc_err;              // set when a tensor-core wait gave up
     float omega;              // identity path: output = omega * input + network
     int bias_free;            // 1: biases held at zero (positively homogeneous map)
     long long cap;            // net-grid voxel capacity
@@ -601,6 +783,8 @@ static void cnn_free(bella_cnn *net) {
     cudaFree(net->gact[0]); cudaFree(net->gact[1]);
     cudaFree(net->y8); cudaFree(net->t8); cudaFree(net->g8); cudaFree(net->inv_e2); cudaFree(net->loss);
     cudaFree(net->yf); cudaFree(net->qf); cudaFree(net->gf); cudaFree(net->flux); cudaFree(net->wcrop);
+    for (int l = 0; l < 5; ++l) cudaFree(net->wtc[l]);
+    cudaFree(net->tc_err);
 }
 
 template <typename K>
@@ -621,9 +805,41 @@ static bool map_ok(const bella_cnn *net, const BlockMap &m) {
     return m.nvox() <= net->cap && (m.B == 1 || m.cx % CT_X == 0);
 }
 
+static int tc_grid(long long nitems) {
+    int nsm = NSM;
+    return (int)(nitems < nsm ? nitems : nsm);
+}
+
+// layers 0-4 on tcgen05 when enabled and the staged planes fit in shared memory
+static bool tc_fits(const BlockMap &m) {
+    return tc_smem_bytes<32, 32>(m.cz + 2) <= 227 * 1024;
+}
+
 static void forward_layers(bella_cnn *net, const BlockMap &m, float out_scale, cudaStream_t s) {
     const int g = conv_grid(m);
     const int nx = m.B * m.cx, ny = m.cy, nz = m.cz, xs = m.cx;
+    if (net->use_tc && tc_fits(m)) {
+        const long long plane = (long long)(ny + 2) * (nz + 2);
+        const long long nitems = (long long)nx * ((plane + TC_ROWS - 1) / TC_ROWS);
+        const int gt = tc_grid(nitems), pz = nz + 2;
+        if (net->linear) {
+            k_conv3d_tc<16, 32, false><<<gt, 256, tc_smem_bytes<16, 32>(pz), s>>>(
+                nx, ny, nz, xs, net->act[0], net->wtc[0], nullptr, net->act[1], net->tc_err);
+            for (int l = 1; l <= 4; ++l)
+                k_conv3d_tc<32, 32, false><<<gt, 256, tc_smem_bytes<32, 32>(pz), s>>>(
+                    nx, ny, nz, xs, net->act[l], net->wtc[l], nullptr, net->act[l + 1], net->tc_err);
+        } else {
+            k_conv3d_tc<16, 32, true><<<gt, 256, tc_smem_bytes<16, 32>(pz), s>>>(
+                nx, ny, nz, xs, net->act[0], net->wtc[0], net->bias[0], net->act[1], net->tc_err);
+            for (int l = 1; l <= 4; ++l)
+                k_conv3d_tc<32, 32, true><<<gt, 256, tc_smem_bytes<32, 32>(pz), s>>>(
+                    nx, ny, nz, xs, net->act[l], net->wtc[l], net->bias[l], net->act[l + 1], net->tc_err);
+        }
+        k_conv3d<32, 8, false, true, false><<<g, CNN_THREADS, conv_smem<32, 8>(), s>>>(
+            nx, ny, nz, xs, net->act[5], net->wk[5], net->linear ? nullptr : net->bias[5], net->y8, out_scale, nullptr);
+        net->launches += 6;
+        return;
+    }
     if (net->linear) {
         k_conv3d<16, 32, false, false, false><<<g, CNN_THREADS, conv_smem<16, 32>(), s>>>(
             nx, ny, nz, xs, net->act[0], net->wk[0], nullptr, net->act[1], 1.f, nullptr);
@@ -695,6 +911,10 @@ static int cnn_sync_weights(bella_cnn *net, cudaStream_t s) {
                                           net->wk[l], net->wkT[l]);
         k_cast_bias<<<1, 32, 0, s>>>(b, net->cout[l], COUTP_L[l], net->bias[l]);
         net->launches += 2;
+        if (l < 5 && net->wtc[l]) {
+            k_wk_to_tc<<<64, 256, 0, s>>>(net->wk[l], CINP_L[l], COUTP_L[l], net->wtc[l]);
+            net->launches += 1;
+        }
     }
     return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
 }
@@ -744,6 +964,8 @@ int bella_cnn_create(bella_cnn **out, int device, int block, long long capacity)
     for (int k = 0; k < 2 && ok; ++k) ok = cudaMalloc(&net->gact[k], C * 32 * 2) == cudaSuccess;
     for (float **p : {&net->y8, &net->t8, &net->g8}) ok = ok && cudaMalloc(p, C * 8 * sizeof(float)) == cudaSuccess;
     ok = ok && cudaMalloc(&net->inv_e2, C * sizeof(float)) == cudaSuccess;
+    for (int l = 0; l < 5 && ok; ++l) ok = cudaMalloc(&net->wtc[l], 27ULL * CINP_L[l] * COUTP_L[l] * 2) == cudaSuccess;
+    ok = ok && cudaMalloc(&net->tc_err, sizeof(int)) == cudaSuccess && cudaMemset(net->tc_err, 0, sizeof(int)) == cudaSuccess;
     ok = ok && cudaMalloc(&net->loss, sizeof(double)) == cudaSuccess;
     for (float *p : {net->params, net->grads, net->adam_m, net->adam_v})
         ok = ok && cudaMemset(p, 0, net->nparams * sizeof(float)) == cudaSuccess;
@@ -758,7 +980,9 @@ int bella_cnn_create(bella_cnn **out, int device, int block, long long capacity)
          big_smem(k_wgrad<32, 32, 8, 1, float>, wgrad_smem<32, 1>()) &&
          big_smem(k_wgrad<32, 32, 32, 32, __nv_bfloat16>, wgrad_smem<32, 32>()) &&
          big_smem(k_wgrad<16, 8, 32, 32, __nv_bfloat16>, wgrad_smem<8, 32>()) &&
-         big_smem(k_wgrad<16, 1, 32, 32, __nv_bfloat16>, wgrad_smem<1, 32>());
+         big_smem(k_wgrad<16, 1, 32, 32, __nv_bfloat16>, wgrad_smem<1, 32>()) &&
+         big_smem(k_conv3d_tc<16, 32, false>, 227 * 1024) && big_smem(k_conv3d_tc<16, 32, true>, 227 * 1024) &&
+         big_smem(k_conv3d_tc<32, 32, false>, 227 * 1024) && big_smem(k_conv3d_tc<32, 32, true>, 227 * 1024);
     if (ok) ok = cnn_sync_weights(net, 0) == BELLA_OK && cudaDeviceSynchronize() == cudaSuccess;
     if (!ok) {
         g_cnn_err = "bella_cnn_create: allocation or attribute failed";
@@ -968,6 +1192,22 @@ int bella_cnn_set_skip(bella_cnn *net, float omega) {
     if (!net || !isfinite(omega)) return BELLA_EINVAL;
     net->omega = omega;
     return BELLA_OK;
+}
+
+// forward layers 0-4 on the tcgen05 tensor-core path (1) or on mma.sync (0)
+int bella_cnn_set_tc(bella_cnn *net, int on) {
+    if (!net) return BELLA_EINVAL;
+    net->use_tc = on ? 1 : 0;
+    return BELLA_OK;
+}
+
+// 1 if a tensor-core completion wait gave up since the last call (synchronises), then cleared
+int bella_cnn_tc_error(bella_cnn *net) {
+    if (!net) return BELLA_EINVAL;
+    int h = 0;
+    if (cudaMemcpy(&h, net->tc_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return BELLA_ECUDA;
+    if (h) cudaMemset(net->tc_err, 0, sizeof(int));
+    return h;
 }
 
 int bella_cnn_set_mode(bella_cnn *net, int mode) {

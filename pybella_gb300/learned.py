@@ -113,6 +113,14 @@ class CNN:
                                                   self._stream()), "bella_cnn_train_step")
         return loss.value
 
+    def set_tensor_cores(self, on):
+        """Forward layers 0-4 on tcgen05 (True) or mma.sync (False)."""
+        _lib.check(self._lib.bella_cnn_set_tc(self.handle, int(bool(on))), "bella_cnn_set_tc")
+
+    def tensor_core_error(self):
+        """True if a tensor-core completion wait gave up (synchronises)."""
+        return bool(_lib.check(self._lib.bella_cnn_tc_error(self.handle), "bella_cnn_tc_error"))
+
     @property
     def launches(self):
         return int(self._lib.bella_cnn_launches(self.handle))

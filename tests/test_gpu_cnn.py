@@ -167,3 +167,30 @@ class _nullctx:
 
     def __exit__(self, *a):
         self._w.__exit__(*a)
+
+
+@pytest.mark.parametrize("mode", ["relu", "linear"])
+@pytest.mark.parametrize("shape", [(16, 8, 32), (9, 10, 35), (66, 40, 130)])
+def test_tcgen05_forward_matches_mma_sync_and_oracle(mode, shape):
+    """Layers 0-4 on tcgen05 (tensor memory accumulators): same output as the
+    mma.sync kernels and the oracle, no completion wait given up."""
+    import torch
+    from pybella_gb300.learned import CNN
+    rng = np.random.default_rng(sum(shape))
+    params = _params(2, 9)
+    if mode == "linear":
+        for l in range(6):
+            params["b%d" % l] = np.zeros_like(params["b%d" % l])
+    r = rng.standard_normal(shape).astype(np.float32)
+    net = CNN(shape, block=2, mode=mode)
+    net.set_params(params)
+    x = torch.tensor(r.ravel(), device="cuda")
+    y_mma = net.forward(x, shape, scale=1.0).cpu().numpy()
+    net.set_tensor_cores(True)
+    y_tc = net.forward(x, shape, scale=1.0).cpu().numpy()
+    assert not net.tensor_core_error()
+    # same BF16 operands, FP32 accumulation in another order
+    assert _rel(y_tc, y_mma) < 1e-2, _rel(y_tc, y_mma)
+    if shape[0] * shape[1] * shape[2] < 40000:
+        ref, _ = ocnn.forward(r, params, 2, linear=(mode == "linear"))
+        assert _rel(y_tc.reshape(shape), ref) < 2e-2
