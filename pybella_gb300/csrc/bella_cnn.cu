@@ -194,13 +194,20 @@ constexpr size_t conv_smem() { return (size_t)27 * COUT * CIN * 2 + (size_t)CH_V
 // layout per input plane: [16-byte channel chunk][row][8 channels]; the
 // descriptor's LBO steps between the two chunks of a K=16 step, its SBO between
 // groups of 8 rows.  Rows on the padding ring are computed and discarded.
-// A work item is one x-plane and TC_ROWS padded rows (TC_MB accumulators of
-// 128 rows, 32 TMEM columns each).  One thread issues the MMAs and commits them
-// to an mbarrier; the wait is bounded and on time-out the CTA records an error,
-// frees its tensor memory and returns.
-constexpr int TC_MB = 4;                    // 128-row accumulators per work item
+// Work: a CTA takes runs of consecutive x-planes of one block of TC_ROWS padded
+// rows (TC_MB accumulators of 128 rows).  Consecutive planes share two of their
+// three input planes, so the staged planes live in a ring of five slots and
+// each output plane prefetches one new input plane two planes ahead (cp.async
+// groups) while the tensor cores work on the previous output plane.  The accumulators are double-buffered in tensor
+// memory, so the MMAs of plane k+1 run during the epilogue of plane k.  One
+// thread issues the MMAs and commits them to the mbarrier of their accumulator
+// set; its waits are bounded and on time-out the CTA records an error, waits
+// (bounded) for its other set, frees its tensor memory and returns.
+constexpr int TC_MB = 2;                    // 128-row accumulators per output plane
 constexpr int TC_ROWS = 128 * TC_MB;
+constexpr int TC_SLOTS = 5;                 // ring of staged input planes: k-1 .. k+3
 constexpr long long TC_SPIN_LIMIT = 1LL << 24;
+constexpr size_t TC_SMEM_MAX = 225 * 1024;   // dynamic part; the kernel's static shared variables come on top
 
 __device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
     uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
@@ -217,35 +224,44 @@ __device__ __forceinline__ uint32_t tc_idesc() {   // kind::f16: BF16 x BF16 -> 
 
 template <int CIN, int COUT>
 __host__ __device__ constexpr size_t tc_smem_bytes(int pz) {
-    return (size_t)27 * (CIN / 8) * COUT * 16 + (size_t)3 * (CIN / 8) * (TC_ROWS + 2 * pz + 2) * 16 + 16;
+    return (size_t)27 * (CIN / 8) * COUT * 16 + (size_t)TC_SLOTS * (CIN / 8) * (TC_ROWS + 2 * pz + 2) * 16;
+}
+
+__device__ __forceinline__ uint32_t tc_try_wait(uint32_t mbar, uint32_t parity) {
+    uint32_t done = 0;
+    for (long long it = 0; it < TC_SPIN_LIMIT && !done; ++it)
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.b32 %0, 1, 0, p;\n\t}" : "=r"(done) : "r"(mbar), "r"(parity));
+    return done;
 }
 
 template <int CIN, int COUT, bool RELU>
 __global__ void __launch_bounds__(256, 1)
-k_conv3d_tc(int nx, int ny, int nz, int xseg, const __nv_bfloat16 *__restrict__ in,
+k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *__restrict__ in,
             const __nv_bfloat16 *__restrict__ Wtc, const float *__restrict__ bias, __nv_bfloat16 *out, int *err) {
     static_assert(COUT == 32, "tensor-memory epilogue reads 32 columns");
     constexpr int NCH = CIN / 8;
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_slot;
     __shared__ int ok_flag;
     const int PZ = nz + 2, PY = ny + 2;
     const int L = TC_ROWS + 2 * PZ + 2;                   // staged rows per plane and chunk
     unsigned char *sW = smem;                             // [27][NCH][COUT][16 B]
-    unsigned char *sA = smem + (size_t)27 * NCH * COUT * 16;   // [3][NCH][L][16 B]
+    unsigned char *sA = smem + (size_t)27 * NCH * COUT * 16;   // [TC_SLOTS][NCH][L][16 B]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    // weights (already in the tap-chunk-row order of the descriptors)
     for (int e = tid; e < 27 * NCH * COUT; e += 256)
         reinterpret_cast<uint4 *>(sW)[e] = reinterpret_cast<const uint4 *>(Wtc)[e];
-    const uint32_t mbar_a = (uint32_t)__cvta_generic_to_shared(&mbar);
+    const uint32_t mbar_a0 = (uint32_t)__cvta_generic_to_shared(&mbar[0]);
+    const uint32_t mbar_a1 = (uint32_t)__cvta_generic_to_shared(&mbar[1]);
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_a));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_a0));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_a1));
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
     if (warp == 0) {
         const uint32_t slot = (uint32_t)__cvta_generic_to_shared(&tmem_slot);
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(32 * TC_MB));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(64 * TC_MB));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
@@ -253,105 +269,170 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, const __nv_bfloat16 *__restrict__ 
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_slot;
     const uint32_t sW_a = (uint32_t)__cvta_generic_to_shared(sW), sA_a = (uint32_t)__cvta_generic_to_shared(sA);
-    const long long plane = (long long)PY * PZ;
-    const int nblk = (int)((plane + TC_ROWS - 1) / TC_ROWS);
-    const long long nitems = (long long)nx * nblk;
-    uint32_t phase = 0;
-    for (long long item = blockIdx.x; item < nitems; item += gridDim.x) {
-        const int i = (int)(item / nblk), fb = (int)(item - (long long)i * nblk);
-        const long long f0 = (long long)fb * TC_ROWS - (PZ + 1);   // padded row of staged row 0
-        // ---- stage the three input planes (zero outside the grid and the sample's x segment)
-        for (int e = tid; e < 3 * NCH * L; e += 256) {
-            const int xp = e / (NCH * L), rem = e - xp * (NCH * L), ch = rem / L, rb = rem - ch * L;
-            const int gi = i - 1 + xp;
-            const long long f = f0 + rb;
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (gi >= 0 && gi < nx && (gi / xseg) == (i / xseg) && f >= 0 && f < plane) {
-                const int y = (int)(f / PZ) - 1, z = (int)(f % PZ) - 1;
-                if (y >= 0 && y < ny && z >= 0 && z < nz)
-                    v = *reinterpret_cast<const uint4 *>(in + (((size_t)gi * ny + y) * nz + z) * CIN + ch * 8);
+    const uint64_t a0 = tc_sdesc(sA_a, (uint32_t)L * 16, 128), b0 = tc_sdesc(sW_a, COUT * 16, 128);
+    const uint32_t idesc = tc_idesc<COUT>();
+    const int plane = PY * PZ;
+    const int nblk = (plane + TC_ROWS - 1) / TC_ROWS;
+    const int nseg = (nx + runlen - 1) / runlen;
+    const int nruns = nblk * nseg;
+    uint32_t phase[2] = {0u, 0u};
+    int committed[2] = {0, 0};              // commits not yet waited for, per accumulator set (thread 0)
+    bool failed = false;
+
+    for (int run = blockIdx.x; run < nruns && !failed; run += gridDim.x) {
+        const int fb = run / nseg, seg = run - fb * nseg;
+        const int ia = seg * runlen, ib = min(nx, ia + runlen);
+        const int f0 = fb * TC_ROWS - (PZ + 1);           // padded row of staged row 0
+        // stage input plane p into ring slot p % TC_SLOTS with 16-byte asynchronous copies
+        // (source size 0 fills the zero padding); every copy of a thread is in flight
+        // before the single wait in sync_staged()
+        auto stage = [&](int p) {
+            const uint32_t base = sA_a + (uint32_t)((size_t)(p % TC_SLOTS) * NCH * L * 16);
+            for (int rb = tid; rb < L; rb += 256) {
+                const int f = f0 + rb;
+                const __nv_bfloat16 *src = in;
+                uint32_t bytes = 0;
+                if (f >= 0 && f < plane) {
+                    const int yq = f / PZ;
+                    const int y = yq - 1, z = f - yq * PZ - 1;
+                    if (y >= 0 && y < ny && z >= 0 && z < nz) {
+                        src = in + (((size_t)p * ny + y) * nz + z) * CIN;
+                        bytes = 16;
+                    }
+                }
+#pragma unroll
+                for (int ch = 0; ch < NCH; ++ch)
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
+                                 ::"r"(base + (uint32_t)((ch * L + rb) * 16)), "l"(src + (bytes ? ch * 8 : 0)),
+                                   "r"(bytes));
             }
-            reinterpret_cast<uint4 *>(sA)[((size_t)xp * NCH + ch) * L + rb] = v;
-        }
+        };
+        // thread 0: every tap of output plane k into accumulator set `set`, then commit.
+        // Fully unrolled: per MMA only two 64-bit adds of precomputed offsets.
+        auto issue = [&](int k, int set) {
+            int first = 1;
+#pragma unroll
+            for (int mb = 0; mb < TC_MB; ++mb) {
+                const uint32_t dtm = tmem + (uint32_t)(set * 32 * TC_MB + mb * 32);
+                first = 1;
+#pragma unroll
+                for (int dxi = 0; dxi < 3; ++dxi) {
+                    const int gi = k + dxi - 1;
+                    if (gi < 0 || gi >= nx || (gi / xseg) != (k / xseg)) continue;   // zero padding along x
+                    const uint64_t abase = a0 + (uint64_t)((gi % TC_SLOTS) * NCH * L + mb * 128 + PZ + 1);
+#pragma unroll
+                    for (int dyi = 0; dyi < 3; ++dyi) {
+                        const int yoff = (dyi - 1) * PZ;
+#pragma unroll
+                        for (int dzi = 0; dzi < 3; ++dzi) {
+                            const int tap = dxi * 9 + dyi * 3 + dzi;
+#pragma unroll
+                            for (int ks = 0; ks < CIN / 16; ++ks) {
+                                const uint64_t ad = abase + (uint64_t)(2 * ks * L + yoff + (dzi - 1));
+                                const uint64_t bd = b0 + (uint64_t)((tap * NCH + 2 * ks) * COUT);
+                                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                                             ::"r"(dtm), "l"(ad), "l"(bd), "r"(idesc), "r"(first ? 0 : 1));
+                                first = 0;
+                            }
+                        }
+                    }
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                         ::"r"(set ? mbar_a1 : mbar_a0));
+            committed[set] += 1;
+        };
+        for (int p = ia - 1; p <= ia + 1; ++p)
+            if (p >= 0 && p < nx) stage(p);
+        asm volatile("cp.async.commit_group;");
+        if (ia + 1 < ib && ia + 2 < nx) stage(ia + 2);
+        asm volatile("cp.async.commit_group;");
+        asm volatile("cp.async.wait_group 1;");          // planes ia-1 .. ia+1 have landed
         asm volatile("fence.proxy.async.shared::cta;");
         asm volatile("tcgen05.fence::before_thread_sync;");
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;");
-        // ---- one thread issues 27 taps x CIN/16 k-steps for each 128-row accumulator
-        if (tid == 0) {
-            const uint32_t idesc = tc_idesc<COUT>();
-            for (int mb = 0; mb < TC_MB; ++mb) {
-                int first = 1;
-                for (int tap = 0; tap < 27; ++tap) {
-                    const int dx = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dz = tap % 3 - 1;
-                    const int row0 = mb * 128 + (PZ + 1) + dy * PZ + dz;
-                    for (int ks = 0; ks < CIN / 16; ++ks) {
-                        const uint32_t a = sA_a + (uint32_t)((((dx + 1) * NCH + 2 * ks) * (long long)L + row0) * 16);
-                        const uint32_t b = sW_a + (uint32_t)(((tap * NCH + 2 * ks) * COUT) * 16);
-                        const uint64_t ad = tc_sdesc(a, (uint32_t)L * 16, 128), bd = tc_sdesc(b, COUT * 16, 128);
-                        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                                     ::"r"(tmem + (uint32_t)(mb * 32)), "l"(ad), "l"(bd), "r"(idesc), "r"(first ? 0 : 1));
-                        first = 0;
-                    }
-                }
+        if (tid == 0) issue(ia, 0);
+        for (int k = ia; k < ib; ++k) {
+            const int set = (k - ia) & 1;
+            // prefetch plane k+3: its ring slot last held plane k-2, read only by plane
+            // k-1's MMAs, which were waited for before plane k-1's epilogue
+            if (k + 2 < ib && k + 3 < nx) stage(k + 3);
+            asm volatile("cp.async.commit_group;");
+            asm volatile("cp.async.wait_group 1;");      // plane k+2 (for plane k+1's MMAs) has landed
+            asm volatile("fence.proxy.async.shared::cta;");
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncthreads();
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            if (tid == 0) {
+                if (k + 1 < ib) issue(k + 1, set ^ 1);
+                const uint32_t done = tc_try_wait(set ? mbar_a1 : mbar_a0, phase[set]);
+                if (done) committed[set] -= 1;
+                ok_flag = done ? 1 : 0;
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_a));
-            uint32_t done = 0;
-            for (long long it = 0; it < TC_SPIN_LIMIT && !done; ++it)
-                asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                             "selp.b32 %0, 1, 0, p;\n\t}" : "=r"(done) : "r"(mbar_a), "r"(phase));
-            ok_flag = done ? 1 : 0;
-        }
-        __syncthreads();
-        phase ^= 1;
-        if (!ok_flag) {
-            if (tid == 0) atomicExch(err, 1);
-            break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        // ---- epilogue: warp w reads rows 32*(w%4).. of accumulators 2*(w/4) and 2*(w/4)+1
-        for (int h = 0; h < 2; ++h) {
-            const int mb = (warp >> 2) * 2 + h;
-            uint32_t r[32];
-            const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(mb * 32);
-            asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-                         "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                         "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                           "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-                           "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-                           "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-                           "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-                         : "r"(taddr));
-            asm volatile("tcgen05.wait::ld.sync.aligned;");
-            const long long f = (long long)fb * TC_ROWS + mb * 128 + (warp & 3) * 32 + lane;
-            if (f < plane) {
-                const int y = (int)(f / PZ) - 1, z = (int)(f % PZ) - 1;
-                if (y >= 0 && y < ny && z >= 0 && z < nz) {
-                    uint32_t w[16];
+            __syncthreads();
+            if (!ok_flag) {                  // the phase of this set stays at the unfinished commit
+                if (tid == 0) atomicExch(err, 1);
+                failed = true;
+                break;
+            }
+            phase[set] ^= 1u;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            // epilogue of plane k: warp w reads rows 32*(w%4).. of accumulator w/4 of the set
+            {
+                const int mb = warp >> 2;
+                uint32_t r[32];
+                const uint32_t taddr =
+                    tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(set * 32 * TC_MB + mb * 32);
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                             "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                             "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                               "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                               "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+                               "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+                               "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                             : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;");
+                const int f = fb * TC_ROWS + mb * 128 + (warp & 3) * 32 + lane;
+                if (f < plane) {
+                    const int yq = f / PZ;
+                    const int y = yq - 1, z = f - yq * PZ - 1;
+                    if (y >= 0 && y < ny && z >= 0 && z < nz) {
+                        uint32_t w[16];
 #pragma unroll
-                    for (int c = 0; c < 16; ++c) {
-                        float v0 = __uint_as_float(r[2 * c]), v1 = __uint_as_float(r[2 * c + 1]);
-                        if (bias) { v0 += bias[2 * c]; v1 += bias[2 * c + 1]; }
-                        if (RELU) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
-                        const __nv_bfloat162 h2 = __floats2bfloat162_rn(v0, v1);
-                        w[c] = *reinterpret_cast<const uint32_t *>(&h2);
+                        for (int c = 0; c < 16; ++c) {
+                            float v0 = __uint_as_float(r[2 * c]), v1 = __uint_as_float(r[2 * c + 1]);
+                            if (bias) { v0 += bias[2 * c]; v1 += bias[2 * c + 1]; }
+                            if (RELU) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
+                            const __nv_bfloat162 h2 = __floats2bfloat162_rn(v0, v1);
+                            w[c] = *reinterpret_cast<const uint32_t *>(&h2);
+                        }
+                        uint4 *o = reinterpret_cast<uint4 *>(out + (((size_t)k * ny + y) * nz + z) * COUT);
+                        o[0] = make_uint4(w[0], w[1], w[2], w[3]);
+                        o[1] = make_uint4(w[4], w[5], w[6], w[7]);
+                        o[2] = make_uint4(w[8], w[9], w[10], w[11]);
+                        o[3] = make_uint4(w[12], w[13], w[14], w[15]);
                     }
-                    uint4 *o = reinterpret_cast<uint4 *>(out + (((size_t)i * ny + y) * nz + z) * COUT);
-                    o[0] = make_uint4(w[0], w[1], w[2], w[3]);
-                    o[1] = make_uint4(w[4], w[5], w[6], w[7]);
-                    o[2] = make_uint4(w[8], w[9], w[10], w[11]);
-                    o[3] = make_uint4(w[12], w[13], w[14], w[15]);
                 }
             }
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncthreads();                 // accumulator set read; its next writer may start
         }
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();                     // accumulators read, staging buffer free
+    }
+    // after a time-out, commits that were issued but not waited for may still be in
+    // flight: wait for them (bounded) before freeing tensor memory
+    if (failed && tid == 0) {
+        for (int q = 0; q < 2; ++q)
+            for (int c = 0; c < committed[q]; ++c) {
+                tc_try_wait(q ? mbar_a1 : mbar_a0, phase[q]);
+                phase[q] ^= 1u;
+            }
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(32 * TC_MB));
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(64 * TC_MB));
 }
 
 // kernel weights [27][COUTP][CINP] -> tensor-core operand order [27][CINP/8][COUTP][8]
@@ -812,28 +893,34 @@ static int tc_grid(long long nitems) {
 
 // layers 0-4 on tcgen05 when enabled and the staged planes fit in shared memory
 static bool tc_fits(const BlockMap &m) {
-    return tc_smem_bytes<32, 32>(m.cz + 2) <= 227 * 1024;
+    return tc_smem_bytes<32, 32>(m.cz + 2) <= TC_SMEM_MAX;
 }
 
 static void forward_layers(bella_cnn *net, const BlockMap &m, float out_scale, cudaStream_t s) {
     const int g = conv_grid(m);
     const int nx = m.B * m.cx, ny = m.cy, nz = m.cz, xs = m.cx;
     if (net->use_tc && tc_fits(m)) {
+        // runs of consecutive x-planes: about one run per SM
         const long long plane = (long long)(ny + 2) * (nz + 2);
-        const long long nitems = (long long)nx * ((plane + TC_ROWS - 1) / TC_ROWS);
-        const int gt = tc_grid(nitems), pz = nz + 2;
+        const int nblk = (int)((plane + TC_ROWS - 1) / TC_ROWS);
+        int nseg = (int)((NSM + nblk / 2) / nblk);
+        if (nseg < 1) nseg = 1;
+        if (nseg > nx) nseg = nx;
+        const int runlen = (nx + nseg - 1) / nseg;
+        const long long nruns = (long long)nblk * ((nx + runlen - 1) / runlen);
+        const int gt = tc_grid(nruns), pz = nz + 2;
         if (net->linear) {
             k_conv3d_tc<16, 32, false><<<gt, 256, tc_smem_bytes<16, 32>(pz), s>>>(
-                nx, ny, nz, xs, net->act[0], net->wtc[0], nullptr, net->act[1], net->tc_err);
+                nx, ny, nz, xs, runlen, net->act[0], net->wtc[0], nullptr, net->act[1], net->tc_err);
             for (int l = 1; l <= 4; ++l)
                 k_conv3d_tc<32, 32, false><<<gt, 256, tc_smem_bytes<32, 32>(pz), s>>>(
-                    nx, ny, nz, xs, net->act[l], net->wtc[l], nullptr, net->act[l + 1], net->tc_err);
+                    nx, ny, nz, xs, runlen, net->act[l], net->wtc[l], nullptr, net->act[l + 1], net->tc_err);
         } else {
             k_conv3d_tc<16, 32, true><<<gt, 256, tc_smem_bytes<16, 32>(pz), s>>>(
-                nx, ny, nz, xs, net->act[0], net->wtc[0], net->bias[0], net->act[1], net->tc_err);
+                nx, ny, nz, xs, runlen, net->act[0], net->wtc[0], net->bias[0], net->act[1], net->tc_err);
             for (int l = 1; l <= 4; ++l)
                 k_conv3d_tc<32, 32, true><<<gt, 256, tc_smem_bytes<32, 32>(pz), s>>>(
-                    nx, ny, nz, xs, net->act[l], net->wtc[l], net->bias[l], net->act[l + 1], net->tc_err);
+                    nx, ny, nz, xs, runlen, net->act[l], net->wtc[l], net->bias[l], net->act[l + 1], net->tc_err);
         }
         k_conv3d<32, 8, false, true, false><<<g, CNN_THREADS, conv_smem<32, 8>(), s>>>(
             nx, ny, nz, xs, net->act[5], net->wk[5], net->linear ? nullptr : net->bias[5], net->y8, out_scale, nullptr);
@@ -950,6 +1037,7 @@ int bella_cnn_create(bella_cnn **out, int device, int block, long long capacity)
     const int b3 = block * block * block;
     for (int l = 0; l < 6; ++l) { net->cin[l] = l == 0 ? b3 : 32; net->cout[l] = l == 5 ? b3 : 32; }
     net->nparams = param_count_b(block);
+    net->use_tc = 1;                 // tcgen05 forward where the staged planes fit (mma.sync otherwise)
     const size_t C = (size_t)capacity;
     bool ok = true;
     for (float **p : {&net->params, &net->grads, &net->adam_m, &net->adam_v})
@@ -981,8 +1069,8 @@ int bella_cnn_create(bella_cnn **out, int device, int block, long long capacity)
          big_smem(k_wgrad<32, 32, 32, 32, __nv_bfloat16>, wgrad_smem<32, 32>()) &&
          big_smem(k_wgrad<16, 8, 32, 32, __nv_bfloat16>, wgrad_smem<8, 32>()) &&
          big_smem(k_wgrad<16, 1, 32, 32, __nv_bfloat16>, wgrad_smem<1, 32>()) &&
-         big_smem(k_conv3d_tc<16, 32, false>, 227 * 1024) && big_smem(k_conv3d_tc<16, 32, true>, 227 * 1024) &&
-         big_smem(k_conv3d_tc<32, 32, false>, 227 * 1024) && big_smem(k_conv3d_tc<32, 32, true>, 227 * 1024);
+         big_smem(k_conv3d_tc<16, 32, false>, TC_SMEM_MAX) && big_smem(k_conv3d_tc<16, 32, true>, TC_SMEM_MAX) &&
+         big_smem(k_conv3d_tc<32, 32, false>, TC_SMEM_MAX) && big_smem(k_conv3d_tc<32, 32, true>, TC_SMEM_MAX);
     if (ok) ok = cnn_sync_weights(net, 0) == BELLA_OK && cudaDeviceSynchronize() == cudaSuccess;
     if (!ok) {
         g_cnn_err = "bella_cnn_create: allocation or attribute failed";

@@ -185,6 +185,7 @@ def test_tcgen05_forward_matches_mma_sync_and_oracle(mode, shape):
     net = CNN(shape, block=2, mode=mode)
     net.set_params(params)
     x = torch.tensor(r.ravel(), device="cuda")
+    net.set_tensor_cores(False)
     y_mma = net.forward(x, shape, scale=1.0).cpu().numpy()
     net.set_tensor_cores(True)
     y_tc = net.forward(x, shape, scale=1.0).cpu().numpy()
