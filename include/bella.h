@@ -291,6 +291,31 @@ long long bella_cnn_launches(const bella_cnn *net);
 int       bella_fbicgstab(bella_ws *ws, bella_cnn *net, const double *b, double *x,
                           const bella_solve_opts *opts, bella_solve_stats *stats, void *stream);
 
+/* ---- background (spectral) solve of the 3D operator (no counterpart in the
+ *      reference, whose bicgstab call at second_projection.py:230 passes no M) --
+ * The exact inverse of the operator with every cell coefficient replaced by
+ * its mean over x and z per y-cell (the stratified background) and hcenter by
+ * its mean per y-node: Hartley (periodic axis) or DCT-I (wall axis) transforms
+ * in x and z as FP32 GEMMs, one FP64 tridiagonal solve along y per mode, with
+ * the pseudo-inverse on the singular modes.  The Coriolis cross terms are not
+ * part of the background.  y must be a wall axis.  op holds device FP64
+ * arrays as for bella_op3d_set; they are read during create only.
+ * apply: out = A_bg^+ (in / diag_inv) for a residual of the Jacobi-scaled
+ * system; device FP32 arrays of nx*ny*nz. */
+typedef struct bella_spectral3d bella_spectral3d;
+int       bella_spectral3d_create(bella_spectral3d **sp, const bella_op3d *op, int device, void *stream);
+int       bella_spectral3d_destroy(bella_spectral3d *sp);
+int       bella_spectral3d_apply(bella_spectral3d *sp, const float *in, float *out, void *stream);
+long long bella_spectral3d_launches(const bella_spectral3d *sp);
+/* Flexible BiCGStab as bella_fbicgstab with the preconditioner
+ *   sp only:   M(r) = A_bg^+ r
+ *   net only:  M(r) = net(r)                         (= bella_fbicgstab)
+ *   both:      M(r) = y + net(r - A y),  y = A_bg^+ r  (the network corrects the
+ *              background solve where the coefficients depart from it)
+ * sp must have been created for the operator set on ws. */
+int       bella_fbicgstab_pc(bella_ws *ws, bella_spectral3d *sp, bella_cnn *net, const double *b, double *x,
+                             const bella_solve_opts *opts, bella_solve_stats *stats, void *stream);
+
 /* ---- allocation-free variant (no counterpart in the reference) ----------
  * FP64 BiCGStab of bella_bicgstab (precision 0 only) on the reference-packed
  * 2D operands, for callers that cannot allocate device memory while they run

@@ -131,6 +131,13 @@ SIGNATURES = {
     "bella_expl_part2d": (ctypes.c_int, [ctypes.POINTER(Expl2D), ctypes.c_void_p]),
     "bella_fbicgstab": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, _dp, _dp, ctypes.POINTER(SolveOpts),
                                        ctypes.POINTER(SolveStats), ctypes.c_void_p]),
+    "bella_spectral3d_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Op3D), ctypes.c_int,
+                                               ctypes.c_void_p]),
+    "bella_spectral3d_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "bella_spectral3d_apply": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, ctypes.c_void_p]),
+    "bella_spectral3d_launches": (ctypes.c_longlong, [ctypes.c_void_p]),
+    "bella_fbicgstab_pc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _dp, _dp,
+                                          ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), ctypes.c_void_p]),
     "bella_cnn_set_params": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_void_p]),
     "bella_cnn_get_params": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_void_p]),
     "bella_cnn_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp,

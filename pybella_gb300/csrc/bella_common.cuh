@@ -54,6 +54,7 @@ struct KState {
     double scale;      // IR: inner system = outer residual / scale
     double dot_aux;    // result of the generic FP64 dot kernel
     double dot_aux2;
+    double pss;        // sum of squares of the learned correction's input (flexible solver)
     int    iter;       // iterations done in this (inner) solve
     int    maxiter;    // iteration limit of this (inner) solve
     int    done;       // 1 once converged / failed: later kernels return at once

@@ -1033,18 +1033,71 @@ k_flex_update(long long n, float *x, const float *ph, const float *sh, float *r,
     if (threadIdx.x == 0) finalize_update(ks, tot[0], tot[1]);
 }
 
-static int flex_iteration(bella_ws *ws, bella_cnn *net, cudaStream_t s) {
+// tmp = in - Ay (in place over Ay) and ||tmp||^2 -> ks->pss: the input of the
+// learned correction of the background solve
+__global__ void __launch_bounds__(VEC_BLOCK)
+k_flex_corr_in(long long n, const float *in, float *Ay, KState *ks, double *partials, unsigned *counter) {
+    if (ks->done) return;
+    double a[1] = {0.0};
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
+        const float d = in[g] - Ay[g];
+        Ay[g] = d;
+        a[0] += (double)d * (double)d;
+    }
+    double tot[1];
+    if (!grid_sum<1>(a, partials, counter, tot)) return;
+    if (threadIdx.x == 0) ks->pss = tot[0];
+}
+
+__global__ void __launch_bounds__(VEC_BLOCK)
+k_flex_add(long long n, float *out, const float *add, const KState *ks) {
+    if (ks->done) return;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x)
+        out[g] += add[g];
+}
+
+// the preconditioner of the flexible solver: the network, the background
+// solve, or the background solve corrected by the network
+struct Precond {
+    bella_cnn *net;
+    bella_spectral3d *sp;
+};
+
+static int precond_apply(bella_ws *ws, const Precond &pc, const float *in, float *out, double *in_sumsq,
+                         cudaStream_t s) {
+    const long long n = ws->n;
+    const int gv = ws->grid_vec;
+    if (!pc.sp) {
+        const int rc = cnn_apply_dev(pc.net, ws->nx, ws->ny, ws->nz, in, out, in_sumsq, s);
+        if (rc != BELLA_OK) return set_err(rc, "bella_fbicgstab: grid exceeds the network's capacity");
+        return BELLA_OK;
+    }
+    int rc = spectral_apply_dev(pc.sp, in, out, s);
+    if (rc != BELLA_OK) return cuda_check(cudaGetLastError(), "bella_fbicgstab_pc: background solve");
+    if (pc.net) {
+        float *tmp = spectral_work(pc.sp, 0), *corr = spectral_work(pc.sp, 1);
+        op_apply(ws, 1, out, tmp, s);
+        k_flex_corr_in<<<gv, VEC_BLOCK, 0, s>>>(n, in, tmp, ws->ks, ws->partials, ws->counter);
+        rc = cnn_apply_dev(pc.net, ws->nx, ws->ny, ws->nz, tmp, corr, &ws->ks->pss, s);
+        if (rc != BELLA_OK) return set_err(rc, "bella_fbicgstab_pc: grid exceeds the network's capacity");
+        k_flex_add<<<gv, VEC_BLOCK, 0, s>>>(n, out, corr, ws->ks);
+        ws->launches += 3;
+    }
+    return BELLA_OK;
+}
+
+static int flex_iteration(bella_ws *ws, const Precond &pc, cudaStream_t s) {
     const long long n = ws->n;
     const int gv = ws->grid_vec;
     double *scale = &ws->ks->dot_aux;   // device address of the running sum of squares
     k_flex_p<<<gv, VEC_BLOCK, 0, s>>>(n, ws->r32, ws->p32[0], ws->v32[0], ws->ks, ws->partials, ws->counter);
-    int rc = cnn_apply_dev(net, ws->nx, ws->ny, ws->nz, ws->p32[0], ws->ph32, scale, s);
-    if (rc != BELLA_OK) return set_err(rc, "bella_fbicgstab: grid exceeds the network's capacity");
+    int rc = precond_apply(ws, pc, ws->p32[0], ws->ph32, scale, s);
+    if (rc != BELLA_OK) return rc;
     op_apply(ws, 1, ws->ph32, ws->v32[0], s);
     k_flex_alpha<<<gv, VEC_BLOCK, 0, s>>>(n, ws->rh32, ws->v32[0], ws->ks, ws->partials, ws->counter);
     k_flex_s<<<gv, VEC_BLOCK, 0, s>>>(n, ws->r32, ws->v32[0], ws->s32, ws->ks, ws->partials, ws->counter);
-    rc = cnn_apply_dev(net, ws->nx, ws->ny, ws->nz, ws->s32, ws->sh32, scale, s);
-    if (rc != BELLA_OK) return set_err(rc, "bella_fbicgstab: grid exceeds the network's capacity");
+    rc = precond_apply(ws, pc, ws->s32, ws->sh32, scale, s);
+    if (rc != BELLA_OK) return rc;
     op_apply(ws, 1, ws->sh32, ws->t32, s);
     k_flex_omega<<<gv, VEC_BLOCK, 0, s>>>(n, ws->t32, ws->s32, ws->ks, ws->partials, ws->counter);
     k_flex_update<<<gv, VEC_BLOCK, 0, s>>>(n, ws->x32, ws->ph32, ws->sh32, ws->r32, ws->s32, ws->t32, ws->rh32,
@@ -1053,7 +1106,7 @@ static int flex_iteration(bella_ws *ws, bella_cnn *net, cudaStream_t s) {
     return cuda_check(cudaGetLastError(), "flexible BiCGStab iteration");
 }
 
-static int run_flex(bella_ws *ws, bella_cnn *net, const bella_solve_opts *o, cudaStream_t s,
+static int run_flex(bella_ws *ws, const Precond &pc, const bella_solve_opts *o, cudaStream_t s,
                     std::chrono::steady_clock::time_point t0, int *timed_out) {
     const int blk = o->check_every > 0 ? (o->check_every < 4 ? o->check_every : 4) : 4;
     *timed_out = 0;
@@ -1066,7 +1119,7 @@ static int run_flex(bella_ws *ws, bella_cnn *net, const bella_solve_opts *o, cud
             if (el > o->timeout_s) { *timed_out = 1; return BELLA_OK; }
         }
         for (int k = 0; k < blk; ++k) {
-            rc = flex_iteration(ws, net, s);
+            rc = flex_iteration(ws, pc, s);
             if (rc != BELLA_OK) return rc;
         }
     }
@@ -1074,9 +1127,8 @@ static int run_flex(bella_ws *ws, bella_cnn *net, const bella_solve_opts *o, cud
 
 }  // namespace bella
 
-extern "C" int bella_fbicgstab(bella_ws *ws, bella_cnn *net, const double *b, double *x,
-                               const bella_solve_opts *opts, bella_solve_stats *stats, void *stream) {
-    if (!ws || !net || !b || !x) return set_err(BELLA_EINVAL, "bella_fbicgstab: null argument");
+static int fbicgstab_impl(bella_ws *ws, const bella::Precond &pc, const double *b, double *x,
+                          const bella_solve_opts *opts, bella_solve_stats *stats, void *stream) {
     if (ws->ndim != 3) return set_err(ws->ndim == 0 ? BELLA_ENOOP : BELLA_EINVAL,
                                       "bella_fbicgstab: needs a 3D operator (bella_op3d_set)");
     bella_solve_opts o;
@@ -1131,7 +1183,7 @@ extern "C" int bella_fbicgstab(bella_ws *ws, bella_cnn *net, const double *b, do
             k_init32<<<gv, VEC_BLOCK, 0, s>>>(n, ws->r64, 1.0 / rnorm, ws->r32, ws->rh32, ws->x32, rel, cap, ws->ks,
                                               ws->partials, ws->counter);
             ws->launches++;
-            rc = run_flex(ws, net, &o, s, t0, &timed_out);
+            rc = run_flex(ws, pc, &o, s, t0, &timed_out);
             if (rc != BELLA_OK) return rc;
             const int it = ws->ks_host->iter;
             const int inner_status = ws->ks_host->status;
@@ -1185,6 +1237,20 @@ extern "C" int bella_fbicgstab(bella_ws *ws, bella_cnn *net, const double *b, do
     st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (stats) *stats = st;
     return st.status;
+}
+
+extern "C" int bella_fbicgstab(bella_ws *ws, bella_cnn *net, const double *b, double *x,
+                               const bella_solve_opts *opts, bella_solve_stats *stats, void *stream) {
+    if (!ws || !net || !b || !x) return set_err(BELLA_EINVAL, "bella_fbicgstab: null argument");
+    return fbicgstab_impl(ws, bella::Precond{net, nullptr}, b, x, opts, stats, stream);
+}
+
+extern "C" int bella_fbicgstab_pc(bella_ws *ws, bella_spectral3d *sp, bella_cnn *net, const double *b, double *x,
+                                  const bella_solve_opts *opts, bella_solve_stats *stats, void *stream) {
+    if (!ws || (!sp && !net) || !b || !x) return set_err(BELLA_EINVAL, "bella_fbicgstab_pc: null argument");
+    if (sp && (ws->ndim != 3 || bella::spectral_size(sp) != ws->n))
+        return set_err(BELLA_EINVAL, "bella_fbicgstab_pc: background solve made for another grid");
+    return fbicgstab_impl(ws, bella::Precond{net, sp}, b, x, opts, stats, stream);
 }
 
 // ============================================================================

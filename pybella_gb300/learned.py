@@ -134,6 +134,22 @@ class CNN:
             pass
 
 
+class LearnedPreconditioner:
+    """The background solve corrected by the network:
+    ``M(r) = y + net(r - A y)`` with ``y = A_bg^+ r`` (:class:`pybella_gb300.spectral.BackgroundSolve`).
+
+    The background solve inverts the horizontally averaged (stratified)
+    operator exactly; the network, trained on the residuals and errors the
+    background solve leaves (:func:`harvest_pairs` with ``background=True``),
+    corrects it where the cell coefficients depart from their horizontal means.
+    Pass as ``preconditioner=`` to :meth:`~pybella_gb300.linalg.NodalHelmholtz3D.solve`.
+    """
+
+    def __init__(self, background, network):
+        self.background = background
+        self.network = network
+
+
 # ---------------------------------------------------------------------------
 # training data and training
 # ---------------------------------------------------------------------------
@@ -190,9 +206,9 @@ class PairSet:
         return self
 
 
-def harvest_pairs(seeds, shape=(129, 65, 129), npairs=20000, crop=32, checkpoints=(2, 8, 32, 128, 512, 2048),
+def harvest_pairs(seeds, shape=(129, 65, 129), npairs=20000, crop=32, checkpoints=None,
                   random_fraction=0.25, powers=(0.0, 2.0, 4.0), solve_tol=1e-9, solve_maxiter=200000,
-                  gen_seed=0, log=None):
+                  gen_seed=0, log=None, background=False):
     """(residual, error) training windows on the device (a :class:`PairSet`).
 
     For every seed a :func:`~pybella_gb300.workloads.stratified_3d` problem of
@@ -203,7 +219,17 @@ def harvest_pairs(seeds, shape=(129, 65, 129), npairs=20000, crop=32, checkpoint
     the pairs are (A e, e) for seeded Gaussian fields e with power ~k^-p
     (``powers``), covering error components the solver's own iterates leave
     out.  A seed whose x* solve fails contributes only the latter.
+
+    ``background=True`` harvests for the correction stage of a
+    :class:`LearnedPreconditioner`: the iterates come from the
+    background-preconditioned solver itself (stopped after 0..4 iterations by
+    default) and every pair (r, e) becomes (r - A y, e - y) with y = A_bg^+ r,
+    the residual and error the background solve leaves.  ``checkpoints``
+    defaults to (2, 8, 32, 128, 512, 2048) plain iterations, or (0, 1, 2, 3, 4)
+    preconditioned ones with ``background``.
     """
+    if checkpoints is None:
+        checkpoints = (0, 1, 2, 3, 4) if background else (2, 8, 32, 128, 512, 2048)
     from . import workloads
     gen = torch.Generator(device="cpu")
     gen.manual_seed(int(gen_seed))
@@ -218,8 +244,21 @@ def harvest_pairs(seeds, shape=(129, 65, 129), npairs=20000, crop=32, checkpoint
             ps = PairSet(npairs, crop, (w["dx"], w["dy"], w["dz"]))
         A = operator_3d(w)
         h = wall_zeroed_cells(w)
+        if background:
+            from .spectral import BackgroundSolve
+            bg = BackgroundSolve(A)
+
+            def add(r, e, count):
+                y = bg.apply(r).to(torch.float64)
+                ps.add(r - A.matvec(y), e - y, h, w["diag_inv"], shape, count, gen)
+        else:
+            def add(r, e, count):
+                ps.add(r, e, h, w["diag_inv"], shape, count, gen)
         b = w["b"]
-        xs, st = A.solve(b, tol=solve_tol, maxiter=solve_maxiter, precision="df64")
+        if background:
+            xs, st = A.solve(b, tol=solve_tol, maxiter=solve_maxiter, preconditioner=bg)
+        else:
+            xs, st = A.solve(b, tol=solve_tol, maxiter=solve_maxiter, precision="df64")
         ok = st["status"] == 0
         if log:
             log("seed %d: x* %s in %d iterations (relres %.2e)" % (seed, "found" if ok else "NOT found",
@@ -228,10 +267,13 @@ def harvest_pairs(seeds, shape=(129, 65, 129), npairs=20000, crop=32, checkpoint
         for k in (checkpoints if ok else ()):
             if ps.n >= n_iter:
                 break
-            x, _ = A.solve(b, x0=x, tol=1e-300, maxiter=k - done, precision="df64")
-            done = k
+            if background:
+                x = torch.zeros_like(b) if k == 0 else A.solve(b, tol=1e-300, maxiter=k, preconditioner=bg)[0]
+            else:
+                x, _ = A.solve(b, x0=x, tol=1e-300, maxiter=k - done, precision="df64")
+                done = k
             r = b - A.matvec(x)
-            ps.add(r, xs - x, h, w["diag_inv"], shape, min(per_state, n_iter - ps.n), gen)
+            add(r, xs - x, min(per_state, n_iter - ps.n))
         if n_rand:
             g = torch.Generator(device="cuda")
             g.manual_seed(1000 + int(seed))
@@ -239,7 +281,9 @@ def harvest_pairs(seeds, shape=(129, 65, 129), npairs=20000, crop=32, checkpoint
                 if ps.n >= npairs:
                     break
                 e = workloads._power_field(shape, p, g, torch.device("cuda")).reshape(-1)
-                ps.add(A.matvec(e), e, h, w["diag_inv"], shape, min(per_rand, npairs - ps.n), gen)
+                add(A.matvec(e), e, min(per_rand, npairs - ps.n))
+        if background:
+            bg.close()
         del A
     return ps.trim()
 
@@ -279,16 +323,17 @@ def train(net, pairs, steps=3000, batch=32, lr=1e-3, lr_final=1e-5, seed=0, log=
 
 def train_preconditioner(shape=(129, 65, 129), seeds=(1, 2, 3, 5), npairs=6000, crop=48, steps=2000, batch=32,
                          block=2, mode="linear", skip=1.0, last_gain=0.01, random_fraction=0.25,
-                         powers=(0.0, 2.0, 4.0), lr=5e-4, seed=0, log=None):
+                         powers=(0.0, 2.0, 4.0), lr=5e-4, seed=0, log=None, background=False):
     """Harvest pairs, train from a seeded init on the GPU and return the flat FP32 parameters.
 
     The defaults are the configuration measured for the 3D stratified problem:
     a linear network on 2x2x2 node blocks with an identity path (training
     starts from the plain method), trained on the operator residual of each
-    window's core.
+    window's core.  ``background=True`` trains the correction stage of a
+    :class:`LearnedPreconditioner` (pairs left by the background solve).
     """
     pairs = harvest_pairs(list(seeds), shape=shape, npairs=npairs, crop=crop, random_fraction=random_fraction,
-                          powers=powers, gen_seed=seed, log=log)
+                          powers=powers, gen_seed=seed, log=log, background=background)
     net = CNN((crop, crop, crop), block=block, nsamples=batch, mode=mode, skip=skip)
     net.init(seed, last_gain=last_gain)
     losses = train(net, pairs, steps=steps, batch=batch, lr=lr, seed=seed, log=log, log_every=max(1, steps // 8))

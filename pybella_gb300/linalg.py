@@ -104,11 +104,14 @@ class _NodalOperator:
         finished by FP64 BiCGStab and ``stats['fallback'] == 1``.  ``'df64'``
         is double-float BiCGStab with FP64 reliable updates.
 
-        ``preconditioner`` (a :class:`pybella_gb300.learned.CNN`, 3D only)
-        selects flexible BiCGStab right-preconditioned by the network (FP32
-        inner iterations in FP64 refinement, ``precision`` ignored); a failed
-        learned solve is finished by the plain double-float method, reported
-        in ``stats['fallback']`` and by a warning.
+        ``preconditioner`` (3D only) selects flexible BiCGStab right-
+        preconditioned by a :class:`pybella_gb300.learned.CNN`, a
+        :class:`pybella_gb300.spectral.BackgroundSolve` or a
+        :class:`pybella_gb300.learned.LearnedPreconditioner` (background solve
+        corrected by the network): FP32 inner iterations in FP64 refinement,
+        ``precision`` ignored; a failed preconditioned solve is finished by the
+        plain double-float method, reported in ``stats['fallback']`` and by a
+        warning.
         """
         bd = _to_dev(b, self.dev)
         if bd.numel() != self.n:
@@ -137,13 +140,31 @@ class _NodalOperator:
                 _lib.check(self.ws._lib.bella_bicgstab(self.ws.handle, _ptr(bd), _ptr(x), ctypes.byref(o),
                                                        ctypes.byref(st), _stream(self.dev)), "bella_bicgstab")
             else:
-                _lib.check(self.ws._lib.bella_fbicgstab(self.ws.handle, preconditioner.handle, _ptr(bd), _ptr(x),
-                                                        ctypes.byref(o), ctypes.byref(st), _stream(self.dev)),
-                           "bella_fbicgstab")
+                sp, net = _precond_parts(preconditioner)
+                if sp is None:
+                    _lib.check(self.ws._lib.bella_fbicgstab(self.ws.handle, net.handle, _ptr(bd), _ptr(x),
+                                                            ctypes.byref(o), ctypes.byref(st), _stream(self.dev)),
+                               "bella_fbicgstab")
+                else:
+                    _lib.check(self.ws._lib.bella_fbicgstab_pc(self.ws.handle, sp.handle,
+                                                               net.handle if net is not None else None,
+                                                               _ptr(bd), _ptr(x), ctypes.byref(o), ctypes.byref(st),
+                                                               _stream(self.dev)), "bella_fbicgstab_pc")
                 if st.fallback:
-                    warnings.warn("learned-preconditioner solve failed; finished by plain BiCGStab "
+                    warnings.warn("preconditioned solve failed; finished by plain BiCGStab "
                                   "(status %d, relres %.3e)" % (st.status, st.relres), RuntimeWarning)
         return x, st.as_dict()
+
+
+def _precond_parts(pc):
+    """(background solve or None, network or None) of a ``preconditioner=`` argument."""
+    if hasattr(pc, "background") and hasattr(pc, "network"):
+        return pc.background, pc.network
+    if getattr(pc, "kind", None) == "background":
+        return pc, None
+    if not hasattr(pc, "handle"):
+        raise TypeError("preconditioner must be a CNN, a BackgroundSolve or a LearnedPreconditioner")
+    return None, pc
 
 
 class NodalHelmholtz2D(_NodalOperator):
@@ -264,13 +285,17 @@ def bicgstab(A, b, x0=None, tol=None, maxiter=None, M=None, callback=None, atol=
     ``callback(xk)``: the reference only counts calls (solver_counter,
     second_projection.py:11-20); it is invoked once per BiCGStab iteration
     after the solve, each time with the final iterate (per-iteration
-    iterates stay on the device).  ``M`` (preconditioner) is not supported on
-    this path unless it is a :class:`pybella_gb300.learned.CNN` (3D operators),
-    which selects the flexible solver.  ``stats`` (a dict) receives iterations, outer refinement
+    iterates stay on the device).  ``M`` (preconditioner, 3D operators) may be
+    a :class:`pybella_gb300.learned.CNN`, a
+    :class:`pybella_gb300.spectral.BackgroundSolve` or a
+    :class:`pybella_gb300.learned.LearnedPreconditioner`; it selects the
+    flexible solver.  ``stats`` (a dict) receives iterations, outer refinement
     steps, true relative residual, status and time.
     """
-    if M is not None and not hasattr(M, "train_step"):
-        raise NotImplementedError("bicgstab: M must be a pybella_gb300.learned.CNN (flexible BiCGStab)")
+    if M is not None and not (hasattr(M, "train_step") or getattr(M, "kind", None) == "background"
+                              or hasattr(M, "background")):
+        raise NotImplementedError("bicgstab: M must be a pybella_gb300 CNN, BackgroundSolve or "
+                                  "LearnedPreconditioner (flexible BiCGStab)")
     op = A.op if isinstance(A, LinearOperator) else A
     if not hasattr(op, "solve"):
         raise TypeError("bicgstab needs a pybella_gb300 device operator, got %r" % (A,))

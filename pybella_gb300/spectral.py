@@ -1,0 +1,74 @@
+"""Background solve of the 3D nodal operator (libbella_gb300 ``bella_spectral3d_*``).
+
+The exact inverse of the 27-point operator with every cell coefficient
+replaced by its mean over x and z per y-cell (the stratified background) and
+``hcenter`` by its mean per y-node: Hartley or DCT-I transforms along x and z
+(dense FP32 GEMMs on the device), an FP64 tridiagonal solve along y for every
+(kx, kz) mode, pseudo-inverse on the modes of the operator's null space.  As a
+right preconditioner of flexible BiCGStab it bounds the condition number by
+the spread of the cell coefficients about their horizontal means.  The
+reference solves without a preconditioner (second_projection.py:230 passes no
+``M`` to scipy's bicgstab); this is the slot it fills.
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+class BackgroundSolve:
+    """Background inverse of a :class:`pybella_gb300.linalg.NodalHelmholtz3D` (y must be a wall axis).
+
+    ``apply(r)`` maps a residual of the Jacobi-scaled system (FP32 CUDA tensor)
+    to ``A_bg^+ (r / diag_inv)``; pass the object as ``preconditioner=`` to
+    :meth:`~pybella_gb300.linalg.NodalHelmholtz3D.solve`, alone or inside a
+    :class:`pybella_gb300.learned.LearnedPreconditioner`.
+    """
+
+    kind = "background"
+
+    def __init__(self, op):
+        self.op = op
+        self.dev = op.dev
+        self.n = op.n
+        self._lib = op.ws._lib
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.dev):
+            _lib.check(self._lib.bella_spectral3d_create(ctypes.byref(h), ctypes.byref(op._op), self.dev.index,
+                                                         ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)),
+                       "bella_spectral3d_create")
+        self.handle = h
+
+    def _stream(self):
+        return ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
+
+    def apply(self, r, out=None):
+        x = r.detach().to(device=self.dev, dtype=torch.float32).contiguous().reshape(-1)
+        if x.numel() != self.n:
+            raise ValueError("vector has %d entries, operator has %d unknowns" % (x.numel(), self.n))
+        y = torch.empty_like(x) if out is None else out
+        with torch.cuda.device(self.dev):
+            _lib.check(self._lib.bella_spectral3d_apply(self.handle, _ptr(x), _ptr(y), self._stream()),
+                       "bella_spectral3d_apply")
+        return y
+
+    __call__ = apply
+
+    def launches(self):
+        return int(self._lib.bella_spectral3d_launches(self.handle))
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            self._lib.bella_spectral3d_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
