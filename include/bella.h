@@ -310,11 +310,25 @@ long long bella_spectral3d_launches(const bella_spectral3d *sp);
 /* Flexible BiCGStab as bella_fbicgstab with the preconditioner
  *   sp only:   M(r) = A_bg^+ r
  *   net only:  M(r) = net(r)                         (= bella_fbicgstab)
- *   both:      M(r) = y + net(r - A y),  y = A_bg^+ r  (the network corrects the
- *              background solve where the coefficients depart from it)
- * sp must have been created for the operator set on ws. */
-int       bella_fbicgstab_pc(bella_ws *ws, bella_spectral3d *sp, bella_cnn *net, const double *b, double *x,
-                             const bella_solve_opts *opts, bella_solve_stats *stats, void *stream);
+ *   both, each stage applied to the residual the previous stages leave
+ *   (the network corrects the background solve where the coefficients
+ *   depart from it):
+ *     compose 0: y = A_bg^+ r;  y += net(r - A y)
+ *     compose 1: y = net(r);    y += A_bg^+ (r - A y)
+ *     compose 2: y = A_bg^+ r;  y += net(r - A y);  y += A_bg^+ (r - A y)
+ * sp must have been created for the operator set on ws; compose is ignored
+ * unless both are given. */
+int       bella_fbicgstab_pc(bella_ws *ws, bella_spectral3d *sp, bella_cnn *net, int compose, const double *b,
+                             double *x, const bella_solve_opts *opts, bella_solve_stats *stats, void *stream);
+/* As bella_fbicgstab_pc with flexible GMRES (Saad's FGMRES, restart 1..30) as the
+ * inner solver: one cycle of at most restart iterations per refinement step, FP32
+ * Arnoldi vectors with FP64 inner products and Gram-Schmidt reorthogonalisation.
+ * FGMRES keeps every preconditioned vector, so it stays exact for a preconditioner
+ * that is not one fixed linear map (the BF16 network), where BiCGStab's
+ * recurrences lose their footing; one preconditioner application per iteration. */
+int       bella_fgmres_pc(bella_ws *ws, bella_spectral3d *sp, bella_cnn *net, int compose, int restart,
+                          const double *b, double *x, const bella_solve_opts *opts, bella_solve_stats *stats,
+                          void *stream);
 
 /* ---- allocation-free variant (no counterpart in the reference) ----------
  * FP64 BiCGStab of bella_bicgstab (precision 0 only) on the reference-packed

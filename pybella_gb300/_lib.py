@@ -136,8 +136,11 @@ SIGNATURES = {
     "bella_spectral3d_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "bella_spectral3d_apply": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, ctypes.c_void_p]),
     "bella_spectral3d_launches": (ctypes.c_longlong, [ctypes.c_void_p]),
-    "bella_fbicgstab_pc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _dp, _dp,
+    "bella_fbicgstab_pc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _dp, _dp,
                                           ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), ctypes.c_void_p]),
+    "bella_fgmres_pc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                       _dp, _dp, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats),
+                                       ctypes.c_void_p]),
     "bella_cnn_set_params": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_void_p]),
     "bella_cnn_get_params": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_void_p]),
     "bella_cnn_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp,

@@ -241,6 +241,12 @@ struct bella_ws {
     bella::KState *ks_host;   // pinned mirror
     int grid_stencil, grid_vec;
     long long launches;
+    // flexible GMRES: Arnoldi basis V [(m+1)][n], preconditioned basis Z [m][n],
+    // per-block partial dot products and small device results
+    float *fg_v, *fg_z;
+    double *fg_part, *fg_dev;
+    int fg_m;
+    long long fg_n;
     // scratch of the device projection (bella_projection2d)
     double *proj_buf;
     size_t proj_cap;

@@ -85,7 +85,8 @@ inline void op_iteration(bella_ws *ws, int prec, cudaStream_t s) {
 template <typename T> void launch_update(bella_ws *ws, cudaStream_t s);
 
 // background (spectral) solve (bella_spectral.cu): out = A_bg^+ (in / diag_inv);
-// two work arrays of n floats that are free between applications
+// two work arrays of n floats for a composed preconditioner (not used by the
+// background solve itself)
 int spectral_apply_dev(bella_spectral3d *sp, const float *in, float *out, cudaStream_t s);
 float *spectral_work(bella_spectral3d *sp, int which);
 long long spectral_size(const bella_spectral3d *sp);

@@ -411,6 +411,10 @@ int bella_ws_destroy(bella_ws *ws) {
     if (ws->prof) bella_ws_profile(ws, 0);
     free_op(ws);
     cudaFree(ws->proj_buf);
+    cudaFree(ws->fg_v);
+    cudaFree(ws->fg_z);
+    cudaFree(ws->fg_part);
+    cudaFree(ws->fg_dev);
     cudaFree(ws->vbase);
     cudaFree(ws->partials);
     cudaFree(ws->counter);
@@ -1057,33 +1061,61 @@ k_flex_add(long long n, float *out, const float *add, const KState *ks) {
 }
 
 // the preconditioner of the flexible solver: the network, the background
-// solve, or the background solve corrected by the network
+// solve, or the two composed (compose: 0 background then network on its
+// residual, 1 network then background on its residual, 2 background, network,
+// background)
 struct Precond {
     bella_cnn *net;
     bella_spectral3d *sp;
+    int compose;
 };
+
+// out += correction of the stage that maps the residual in - A out; c1/c2 scratch
+static int stage_net(bella_ws *ws, const Precond &pc, const float *in, float *out, cudaStream_t s) {
+    const long long n = ws->n;
+    const int gv = ws->grid_vec;
+    float *tmp = spectral_work(pc.sp, 0), *corr = spectral_work(pc.sp, 1);
+    op_apply(ws, 1, out, tmp, s);
+    k_flex_corr_in<<<gv, VEC_BLOCK, 0, s>>>(n, in, tmp, ws->ks, ws->partials, ws->counter);
+    const int rc = cnn_apply_dev(pc.net, ws->nx, ws->ny, ws->nz, tmp, corr, &ws->ks->pss, s);
+    if (rc != BELLA_OK) return set_err(rc, "bella_fbicgstab_pc: grid exceeds the network's capacity");
+    k_flex_add<<<gv, VEC_BLOCK, 0, s>>>(n, out, corr, ws->ks);
+    ws->launches += 3;
+    return BELLA_OK;
+}
+
+static int stage_background(bella_ws *ws, const Precond &pc, const float *in, float *out, cudaStream_t s) {
+    const long long n = ws->n;
+    const int gv = ws->grid_vec;
+    float *tmp = spectral_work(pc.sp, 0), *corr = spectral_work(pc.sp, 1);
+    op_apply(ws, 1, out, tmp, s);
+    k_flex_corr_in<<<gv, VEC_BLOCK, 0, s>>>(n, in, tmp, ws->ks, ws->partials, ws->counter);
+    int rc = spectral_apply_dev(pc.sp, tmp, corr, s);
+    if (rc != BELLA_OK) return cuda_check(cudaGetLastError(), "bella_fbicgstab_pc: background solve");
+    k_flex_add<<<gv, VEC_BLOCK, 0, s>>>(n, out, corr, ws->ks);
+    ws->launches += 3;
+    return BELLA_OK;
+}
 
 static int precond_apply(bella_ws *ws, const Precond &pc, const float *in, float *out, double *in_sumsq,
                          cudaStream_t s) {
-    const long long n = ws->n;
-    const int gv = ws->grid_vec;
     if (!pc.sp) {
         const int rc = cnn_apply_dev(pc.net, ws->nx, ws->ny, ws->nz, in, out, in_sumsq, s);
         if (rc != BELLA_OK) return set_err(rc, "bella_fbicgstab: grid exceeds the network's capacity");
         return BELLA_OK;
     }
-    int rc = spectral_apply_dev(pc.sp, in, out, s);
-    if (rc != BELLA_OK) return cuda_check(cudaGetLastError(), "bella_fbicgstab_pc: background solve");
-    if (pc.net) {
-        float *tmp = spectral_work(pc.sp, 0), *corr = spectral_work(pc.sp, 1);
-        op_apply(ws, 1, out, tmp, s);
-        k_flex_corr_in<<<gv, VEC_BLOCK, 0, s>>>(n, in, tmp, ws->ks, ws->partials, ws->counter);
-        rc = cnn_apply_dev(pc.net, ws->nx, ws->ny, ws->nz, tmp, corr, &ws->ks->pss, s);
+    int rc;
+    if (pc.net && pc.compose == 1) {
+        rc = cnn_apply_dev(pc.net, ws->nx, ws->ny, ws->nz, in, out, in_sumsq, s);
         if (rc != BELLA_OK) return set_err(rc, "bella_fbicgstab_pc: grid exceeds the network's capacity");
-        k_flex_add<<<gv, VEC_BLOCK, 0, s>>>(n, out, corr, ws->ks);
-        ws->launches += 3;
+        return stage_background(ws, pc, in, out, s);
     }
-    return BELLA_OK;
+    rc = spectral_apply_dev(pc.sp, in, out, s);
+    if (rc != BELLA_OK) return cuda_check(cudaGetLastError(), "bella_fbicgstab_pc: background solve");
+    if (!pc.net) return BELLA_OK;
+    rc = stage_net(ws, pc, in, out, s);
+    if (rc != BELLA_OK || pc.compose != 2) return rc;
+    return stage_background(ws, pc, in, out, s);
 }
 
 static int flex_iteration(bella_ws *ws, const Precond &pc, cudaStream_t s) {
@@ -1125,10 +1157,204 @@ static int run_flex(bella_ws *ws, const Precond &pc, const bella_solve_opts *o, 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Flexible GMRES (Saad's FGMRES): the inner solver for preconditioners that are
+// not one fixed linear map (the BF16 network).  One cycle of up to m
+// iterations per refinement step; Arnoldi vectors in FP32, every inner product
+// in FP64, classical Gram-Schmidt with one reorthogonalisation pass; the small
+// Hessenberg least-squares problem (Givens rotations) on the host.
+// ---------------------------------------------------------------------------
+constexpr int FG_MAXM = 30;
+constexpr int FG_MAXV = FG_MAXM + 1;
+
+// per-block partial sums of <V_i, w> (i < nv) and, with norm, of <w, w> (slot nv)
+__global__ void __launch_bounds__(VEC_BLOCK)
+k_fg_mdot(long long n, const float *V, long long ld, int nv, const float *w, int norm, double *part) {
+    double acc[FG_MAXV + 1];
+#pragma unroll
+    for (int i = 0; i <= FG_MAXV; ++i) acc[i] = 0.0;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
+        const double wg = w[g];
+#pragma unroll
+        for (int i = 0; i < FG_MAXV; ++i)
+            if (i < nv) acc[i] += (double)V[i * ld + g] * wg;
+        if (norm) acc[FG_MAXV] += wg * wg;
+    }
+    __shared__ double red[FG_MAXV + 1][VEC_BLOCK / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i <= FG_MAXV; ++i) {
+        if (i < nv || (i == FG_MAXV && norm)) {
+            const double v = warp_sum(acc[i]);
+            if (lane == 0) red[i][wid] = v;
+        }
+    }
+    __syncthreads();
+    const int q = threadIdx.x;
+    if (q < nv || (q == nv && norm)) {
+        const int src = q < nv ? q : FG_MAXV;
+        double sum = 0.0;
+        for (int k = 0; k < VEC_BLOCK / 32; ++k) sum += red[src][k];
+        part[(size_t)blockIdx.x * (FG_MAXV + 1) + q] = sum;
+    }
+}
+
+// out[q] = sum over blocks of part[b][q], q < nq, in block order (deterministic)
+__global__ void k_fg_reduce(int nblk, const double *part, int nq, double *out) {
+    const int q = threadIdx.x;
+    if (q >= nq) return;
+    double sum = 0.0;
+    for (int b = 0; b < nblk; ++b) sum += part[(size_t)b * (FG_MAXV + 1) + q];
+    out[q] = sum;
+}
+
+// w -= sum_i h[i] V_i, and with norm per-block partial sums of the new <w, w> (slot 0)
+__global__ void __launch_bounds__(VEC_BLOCK)
+k_fg_update(long long n, const float *V, long long ld, int nv, const double *h, float *w, int norm, double *part) {
+    __shared__ float hs[FG_MAXV];
+    if ((int)threadIdx.x < nv) hs[threadIdx.x] = (float)h[threadIdx.x];
+    __syncthreads();
+    double acc = 0.0;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
+        float wg = w[g];
+        for (int i = 0; i < nv; ++i) wg = fmaf(-hs[i], V[i * ld + g], wg);
+        w[g] = wg;
+        acc += (double)wg * (double)wg;
+    }
+    if (!norm) return;
+    __shared__ double red[VEC_BLOCK / 32];
+    const double v = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sum = 0.0;
+        for (int k = 0; k < VEC_BLOCK / 32; ++k) sum += red[k];
+        part[(size_t)blockIdx.x * (FG_MAXV + 1)] = sum;
+    }
+}
+
+// out = w / sqrt(*nrm2) (in place allowed); zero when the norm is not positive
+__global__ void k_fg_scale(long long n, const float *w, const double *nrm2, float *out) {
+    const double q = *nrm2;
+    const float inv = (q > 0.0 && isfinite(q)) ? (float)(1.0 / sqrt(q)) : 0.f;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x)
+        out[g] = w[g] * inv;
+}
+
+// x += sum_i y[i] Z_i
+__global__ void k_fg_combine(long long n, const float *Z, long long ld, int nz, const double *y, float *x) {
+    __shared__ float ys[FG_MAXM];
+    if ((int)threadIdx.x < nz) ys[threadIdx.x] = (float)y[threadIdx.x];
+    __syncthreads();
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
+        float xg = x[g];
+        for (int i = 0; i < nz; ++i) xg = fmaf(ys[i], Z[i * ld + g], xg);
+        x[g] = xg;
+    }
+}
+
+static int fg_ensure(bella_ws *ws, int m) {
+    const long long n = ws->n;
+    if (ws->fg_v && ws->fg_m >= m && ws->fg_n == n) return BELLA_OK;
+    cudaFree(ws->fg_v); cudaFree(ws->fg_z); cudaFree(ws->fg_part); cudaFree(ws->fg_dev);
+    ws->fg_v = ws->fg_z = nullptr;
+    ws->fg_part = ws->fg_dev = nullptr;
+    ws->fg_m = 0;
+    BELLA_CUDA(cudaMalloc(&ws->fg_v, (size_t)(m + 1) * n * sizeof(float)));
+    BELLA_CUDA(cudaMalloc(&ws->fg_z, (size_t)m * n * sizeof(float)));
+    BELLA_CUDA(cudaMalloc(&ws->fg_part, (size_t)NSM * 8 * (FG_MAXV + 1) * sizeof(double)));
+    BELLA_CUDA(cudaMalloc(&ws->fg_dev, 4 * (FG_MAXV + 1) * sizeof(double)));
+    const double one = 1.0;
+    BELLA_CUDA(cudaMemcpy(ws->fg_dev + 3 * (FG_MAXV + 1), &one, sizeof(double), cudaMemcpyHostToDevice));
+    ws->fg_m = m;
+    ws->fg_n = n;
+    return BELLA_OK;
+}
+
+// One FGMRES cycle on A x32 = r32 (x32 = 0 on entry, r32 = the scaled outer
+// residual set by k_init32, ||r32||^2 in ks->rr): stops when the Arnoldi
+// residual estimate falls to rel*||r32|| or after m iterations.  *iters gets
+// the iterations, *status BELLA_OK / BELLA_MAXITER / BELLA_NONFINITE.
+static int fgmres_cycle(bella_ws *ws, const Precond &pc, int m, double rel, cudaStream_t s, int *iters,
+                        int *status) {
+    const long long n = ws->n;
+    const int gv = ws->grid_vec;
+    double *h1 = ws->fg_dev, *h2 = ws->fg_dev + (FG_MAXV + 1), *nrm = ws->fg_dev + 2 * (FG_MAXV + 1);
+    double *unit = ws->fg_dev + 3 * (FG_MAXV + 1);   // 1.0: sum of squares of a basis vector
+    float *V = ws->fg_v, *Z = ws->fg_z;
+    int rc = sync_state(ws, s);
+    if (rc != BELLA_OK) return rc;
+    const double beta = sqrt(ws->ks_host->rr);
+    *iters = 0;
+    *status = BELLA_MAXITER;
+    if (!isfinite(beta)) { *status = BELLA_NONFINITE; return BELLA_OK; }
+    if (!(beta > 0.0)) { *status = BELLA_OK; return BELLA_OK; }
+    k_fg_scale<<<gv, VEC_BLOCK, 0, s>>>(n, ws->r32, &ws->ks->rr, V);
+    double H[FG_MAXV][FG_MAXM], cs[FG_MAXM], sn[FG_MAXM], gvec[FG_MAXV];
+    memset(H, 0, sizeof(H));
+    gvec[0] = beta;
+    double hhost[3 * (FG_MAXV + 1)];
+    int j = 0, k = 0;
+    for (j = 0; j < m; ++j) {
+        float *vj = V + (size_t)j * n, *zj = Z + (size_t)j * n, *w = V + (size_t)(j + 1) * n;
+        rc = precond_apply(ws, pc, vj, zj, unit, s);
+        if (rc != BELLA_OK) return rc;
+        op_apply(ws, 1, zj, w, s);
+        const int nv = j + 1;
+        k_fg_mdot<<<gv, VEC_BLOCK, 0, s>>>(n, V, n, nv, w, 0, ws->fg_part);
+        k_fg_reduce<<<1, 64, 0, s>>>(gv, ws->fg_part, nv, h1);
+        k_fg_update<<<gv, VEC_BLOCK, 0, s>>>(n, V, n, nv, h1, w, 0, ws->fg_part);
+        k_fg_mdot<<<gv, VEC_BLOCK, 0, s>>>(n, V, n, nv, w, 0, ws->fg_part);
+        k_fg_reduce<<<1, 64, 0, s>>>(gv, ws->fg_part, nv, h2);
+        k_fg_update<<<gv, VEC_BLOCK, 0, s>>>(n, V, n, nv, h2, w, 1, ws->fg_part);
+        k_fg_reduce<<<1, 64, 0, s>>>(gv, ws->fg_part, 1, nrm);
+        k_fg_scale<<<gv, VEC_BLOCK, 0, s>>>(n, w, nrm, w);
+        ws->launches += 10;
+        BELLA_CUDA(cudaMemcpyAsync(hhost, ws->fg_dev, sizeof(hhost), cudaMemcpyDeviceToHost, s));
+        BELLA_CUDA(cudaStreamSynchronize(s));
+        BELLA_CUDA(cudaGetLastError());
+        for (int i = 0; i <= j; ++i) H[i][j] = hhost[i] + hhost[(FG_MAXV + 1) + i];
+        H[j + 1][j] = sqrt(fmax(hhost[2 * (FG_MAXV + 1)], 0.0));
+        bool finite = isfinite(H[j + 1][j]);
+        for (int i = 0; i <= j; ++i) finite = finite && isfinite(H[i][j]);
+        if (!finite) { *status = BELLA_NONFINITE; *iters = j + 1; return BELLA_OK; }
+        for (int i = 0; i < j; ++i) {             // earlier rotations
+            const double t = cs[i] * H[i][j] + sn[i] * H[i + 1][j];
+            H[i + 1][j] = -sn[i] * H[i][j] + cs[i] * H[i + 1][j];
+            H[i][j] = t;
+        }
+        const double a = H[j][j], b = H[j + 1][j];
+        const double r = hypot(a, b);
+        cs[j] = r > 0.0 ? a / r : 1.0;
+        sn[j] = r > 0.0 ? b / r : 0.0;
+        H[j][j] = r;
+        H[j + 1][j] = 0.0;
+        gvec[j + 1] = -sn[j] * gvec[j];
+        gvec[j] = cs[j] * gvec[j];
+        k = j + 1;
+        if (fabs(gvec[j + 1]) <= rel * beta) { *status = BELLA_OK; break; }
+        if (b == 0.0) { *status = BELLA_OK; break; }   // invariant subspace: exact in it
+    }
+    // y = H^-1 g (upper triangular k x k), x32 = Z y
+    double y[FG_MAXM];
+    for (int i = k - 1; i >= 0; --i) {
+        double t = gvec[i];
+        for (int l = i + 1; l < k; ++l) t -= H[i][l] * y[l];
+        y[i] = H[i][i] != 0.0 ? t / H[i][i] : 0.0;
+    }
+    BELLA_CUDA(cudaMemcpyAsync(ws->fg_dev, y, k * sizeof(double), cudaMemcpyHostToDevice, s));
+    k_fg_combine<<<gv, VEC_BLOCK, 0, s>>>(n, Z, n, k, ws->fg_dev, ws->x32);
+    ws->launches += 1;
+    BELLA_CUDA(cudaStreamSynchronize(s));   // y lives on this stack frame until the copy is done
+    *iters = k;
+    return cuda_check(cudaGetLastError(), "flexible GMRES cycle");
+}
+
 }  // namespace bella
 
 static int fbicgstab_impl(bella_ws *ws, const bella::Precond &pc, const double *b, double *x,
-                          const bella_solve_opts *opts, bella_solve_stats *stats, void *stream) {
+                          const bella_solve_opts *opts, bella_solve_stats *stats, void *stream,
+                          int restart = 0) {
     if (ws->ndim != 3) return set_err(ws->ndim == 0 ? BELLA_ENOOP : BELLA_EINVAL,
                                       "bella_fbicgstab: needs a 3D operator (bella_op3d_set)");
     bella_solve_opts o;
@@ -1183,13 +1409,22 @@ static int fbicgstab_impl(bella_ws *ws, const bella::Precond &pc, const double *
             k_init32<<<gv, VEC_BLOCK, 0, s>>>(n, ws->r64, 1.0 / rnorm, ws->r32, ws->rh32, ws->x32, rel, cap, ws->ks,
                                               ws->partials, ws->counter);
             ws->launches++;
-            rc = run_flex(ws, pc, &o, s, t0, &timed_out);
-            if (rc != BELLA_OK) return rc;
-            const int it = ws->ks_host->iter;
-            const int inner_status = ws->ks_host->status;
-            st.detail = ws->ks_host->pad[0];
+            int it, inner_status;
+            if (restart > 0) {
+                rc = fgmres_cycle(ws, pc, restart < cap ? restart : cap, rel, s, &it, &inner_status);
+                if (rc != BELLA_OK) return rc;
+                if (o.timeout_s > 0.0 &&
+                    std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() > o.timeout_s)
+                    timed_out = 1;
+            } else {
+                rc = run_flex(ws, pc, &o, s, t0, &timed_out);
+                if (rc != BELLA_OK) return rc;
+                it = ws->ks_host->iter;
+                inner_status = ws->ks_host->status;
+                st.detail = ws->ks_host->pad[0];
+            }
             total += it;
-            st.matvecs += 2 * it;
+            st.matvecs += (restart > 0 ? 1 : 2) * it;
             st.outer = outer + 1;
             if (inner_status == BELLA_NONFINITE || it == 0) { failed = true; break; }
             BELLA_CUDA(cudaMemcpyAsync(ws->x64v, x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -1242,15 +1477,32 @@ static int fbicgstab_impl(bella_ws *ws, const bella::Precond &pc, const double *
 extern "C" int bella_fbicgstab(bella_ws *ws, bella_cnn *net, const double *b, double *x,
                                const bella_solve_opts *opts, bella_solve_stats *stats, void *stream) {
     if (!ws || !net || !b || !x) return set_err(BELLA_EINVAL, "bella_fbicgstab: null argument");
-    return fbicgstab_impl(ws, bella::Precond{net, nullptr}, b, x, opts, stats, stream);
+    return fbicgstab_impl(ws, bella::Precond{net, nullptr, 0}, b, x, opts, stats, stream);
 }
 
-extern "C" int bella_fbicgstab_pc(bella_ws *ws, bella_spectral3d *sp, bella_cnn *net, const double *b, double *x,
-                                  const bella_solve_opts *opts, bella_solve_stats *stats, void *stream) {
+extern "C" int bella_fbicgstab_pc(bella_ws *ws, bella_spectral3d *sp, bella_cnn *net, int compose, const double *b,
+                                  double *x, const bella_solve_opts *opts, bella_solve_stats *stats, void *stream) {
     if (!ws || (!sp && !net) || !b || !x) return set_err(BELLA_EINVAL, "bella_fbicgstab_pc: null argument");
+    if (compose < 0 || compose > 2) return set_err(BELLA_EINVAL, "bella_fbicgstab_pc: compose must be 0, 1 or 2");
     if (sp && (ws->ndim != 3 || bella::spectral_size(sp) != ws->n))
         return set_err(BELLA_EINVAL, "bella_fbicgstab_pc: background solve made for another grid");
-    return fbicgstab_impl(ws, bella::Precond{net, sp}, b, x, opts, stats, stream);
+    return fbicgstab_impl(ws, bella::Precond{net, sp, compose}, b, x, opts, stats, stream);
+}
+
+extern "C" int bella_fgmres_pc(bella_ws *ws, bella_spectral3d *sp, bella_cnn *net, int compose, int restart,
+                               const double *b, double *x, const bella_solve_opts *opts, bella_solve_stats *stats,
+                               void *stream) {
+    if (!ws || (!sp && !net) || !b || !x) return set_err(BELLA_EINVAL, "bella_fgmres_pc: null argument");
+    if (compose < 0 || compose > 2) return set_err(BELLA_EINVAL, "bella_fgmres_pc: compose must be 0, 1 or 2");
+    if (restart < 1 || restart > bella::FG_MAXM) return set_err(BELLA_EINVAL, "bella_fgmres_pc: restart must be 1..30");
+    if (ws->ndim != 3) return set_err(ws->ndim == 0 ? BELLA_ENOOP : BELLA_EINVAL,
+                                      "bella_fgmres_pc: needs a 3D operator (bella_op3d_set)");
+    if (sp && bella::spectral_size(sp) != ws->n)
+        return set_err(BELLA_EINVAL, "bella_fgmres_pc: background solve made for another grid");
+    BELLA_CUDA(cudaSetDevice(ws->device));
+    int rc = bella::fg_ensure(ws, restart);
+    if (rc != BELLA_OK) return rc;
+    return fbicgstab_impl(ws, bella::Precond{net, sp, compose}, b, x, opts, stats, stream, restart);
 }
 
 // ============================================================================

@@ -45,6 +45,7 @@ struct bella_spectral3d {
     double *hcm;           // y-node means of hcenter (ny)
     float *dscale;         // 1 / diag_inv
     float *w1, *w2;        // transform work arrays (n floats each)
+    float *c1, *c2;        // work arrays of a preconditioner composed with the network
     double *lc, *ld;       // Thomas scratch, [ny][Kx*Kz] each
     double idx2, idy2, idz2;
     long long launches;
@@ -289,7 +290,7 @@ int spectral_apply_dev(bella_spectral3d *sp, const float *in, float *out, cudaSt
     return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
 }
 
-float *spectral_work(bella_spectral3d *sp, int which) { return which ? sp->w2 : sp->w1; }
+float *spectral_work(bella_spectral3d *sp, int which) { return which ? sp->c2 : sp->c1; }
 long long spectral_size(const bella_spectral3d *sp) { return sp->n; }
 
 // eigenvalues of D^T D and the forward / inverse transform matrices of one axis
@@ -351,7 +352,7 @@ int bella_spectral3d_destroy(bella_spectral3d *sp) {
     if (!sp) return BELLA_OK;
     cudaSetDevice(sp->device);
     void *ptrs[] = {sp->txf, sp->txi, sp->tzfT, sp->tziT, sp->mux, sp->muz, sp->cx, sp->cy, sp->cz,
-                    sp->hcm, sp->dscale, sp->w1, sp->w2, sp->lc, sp->ld};
+                    sp->hcm, sp->dscale, sp->w1, sp->w2, sp->c1, sp->c2, sp->lc, sp->ld};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete sp;
@@ -402,6 +403,8 @@ int bella_spectral3d_create(bella_spectral3d **out, const bella_op3d *op, int de
               cudaMalloc(&sp->dscale, sp->n * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&sp->w1, sp->n * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&sp->w2, sp->n * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&sp->c1, sp->n * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&sp->c2, sp->n * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&sp->lc, (size_t)ny * nl * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&sp->ld, (size_t)ny * nl * sizeof(double)) == cudaSuccess;
     if (!ok) {

@@ -135,8 +135,12 @@ class CNN:
 
 
 class LearnedPreconditioner:
-    """The background solve corrected by the network:
-    ``M(r) = y + net(r - A y)`` with ``y = A_bg^+ r`` (:class:`pybella_gb300.spectral.BackgroundSolve`).
+    """The background solve corrected by the network, each stage applied to the
+    residual the previous ones leave (:class:`pybella_gb300.spectral.BackgroundSolve`):
+
+    * ``order="post"``: ``y = A_bg^+ r``, ``y += net(r - A y)``;
+    * ``order="pre"``: ``y = net(r)``, ``y += A_bg^+ (r - A y)``;
+    * ``order="sym"``: background, network, background.
 
     The background solve inverts the horizontally averaged (stratified)
     operator exactly; the network, trained on the residuals and errors the
@@ -145,9 +149,13 @@ class LearnedPreconditioner:
     Pass as ``preconditioner=`` to :meth:`~pybella_gb300.linalg.NodalHelmholtz3D.solve`.
     """
 
-    def __init__(self, background, network):
+    ORDERS = {"post": 0, "pre": 1, "sym": 2}
+
+    def __init__(self, background, network, order="post"):
         self.background = background
         self.network = network
+        self.order = order
+        self.compose = self.ORDERS[order]
 
 
 # ---------------------------------------------------------------------------

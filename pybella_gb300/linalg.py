@@ -94,7 +94,8 @@ class _NodalOperator:
 
     # -- solve -------------------------------------------------------------
     def solve(self, b, x0=None, tol=1e-8, atol=0.0, maxiter=6000, precision="fp64", inner_tol=1e-5,
-              project_null=True, check_every=16, timeout_s=0.0, out=None, preconditioner=None, max_outer=30):
+              project_null=True, check_every=16, timeout_s=0.0, out=None, preconditioner=None, max_outer=30,
+              method="bicgstab", restart=20):
         """Solve ``A x = b``; returns ``(x, stats)`` with ``x`` a CUDA float64 tensor.
 
         ``precision='fp64'`` (default) is BiCGStab in FP64 with scipy's
@@ -111,7 +112,10 @@ class _NodalOperator:
         corrected by the network): FP32 inner iterations in FP64 refinement,
         ``precision`` ignored; a failed preconditioned solve is finished by the
         plain double-float method, reported in ``stats['fallback']`` and by a
-        warning.
+        warning.  ``method='fgmres'`` runs the preconditioned inner solves as
+        flexible GMRES cycles of at most ``restart`` iterations (exact for a
+        preconditioner that varies between applications, such as the BF16
+        network) instead of flexible BiCGStab.
         """
         bd = _to_dev(b, self.dev)
         if bd.numel() != self.n:
@@ -141,13 +145,22 @@ class _NodalOperator:
                                                        ctypes.byref(st), _stream(self.dev)), "bella_bicgstab")
             else:
                 sp, net = _precond_parts(preconditioner)
-                if sp is None:
+                if method == "fgmres":
+                    _lib.check(self.ws._lib.bella_fgmres_pc(self.ws.handle, sp.handle if sp is not None else None,
+                                                            net.handle if net is not None else None,
+                                                            int(getattr(preconditioner, "compose", 0)), int(restart),
+                                                            _ptr(bd), _ptr(x), ctypes.byref(o), ctypes.byref(st),
+                                                            _stream(self.dev)), "bella_fgmres_pc")
+                elif method != "bicgstab":
+                    raise ValueError("method must be 'bicgstab' or 'fgmres'")
+                elif sp is None:
                     _lib.check(self.ws._lib.bella_fbicgstab(self.ws.handle, net.handle, _ptr(bd), _ptr(x),
                                                             ctypes.byref(o), ctypes.byref(st), _stream(self.dev)),
                                "bella_fbicgstab")
                 else:
                     _lib.check(self.ws._lib.bella_fbicgstab_pc(self.ws.handle, sp.handle,
                                                                net.handle if net is not None else None,
+                                                               int(getattr(preconditioner, "compose", 0)),
                                                                _ptr(bd), _ptr(x), ctypes.byref(o), ctypes.byref(st),
                                                                _stream(self.dev)), "bella_fbicgstab_pc")
                 if st.fallback:

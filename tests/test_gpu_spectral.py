@@ -162,3 +162,64 @@ def test_learned_preconditioner_runs_the_correction_and_scipy_signature():
     xs, info = linalg.bicgstab(linalg.LinearOperator(A.shape, A), w["b"], rtol=1e-8, maxiter=2000, M=bg,
                                stats=stats)
     assert info == 0 and stats["fallback"] == 0
+
+
+@pytest.mark.parametrize("order", ["post", "pre", "sym"])
+def test_fgmres_with_every_preconditioner_kind(order):
+    """Flexible GMRES with the background solve and the three compositions with a
+    network: every solve meets rtol 1e-8 on the FP64 true residual without
+    falling back."""
+    import torch
+    from pybella_gb300 import learned, workloads
+    from pybella_gb300.spectral import BackgroundSolve
+    shape = (41, 21, 41)
+    w = workloads.stratified_3d(5, *shape)
+    A = learned.operator_3d(w)
+    bg = BackgroundSolve(A)
+    net = learned.CNN(shape, block=2, mode="linear", skip=0.5)
+    net.init(1, last_gain=0.05)
+    pcs = [learned.LearnedPreconditioner(bg, net, order)]
+    if order == "post":
+        pcs.append(bg)
+    for pc in pcs:
+        with warnings.catch_warnings(record=True) as rec:
+            warnings.simplefilter("always")
+            x, st = A.solve(w["b"], tol=1e-8, maxiter=4000, preconditioner=pc, method="fgmres", restart=30)
+        assert st["status"] == 0 and st["fallback"] == 0 and not rec, (order, st)
+        r = w["b"] - A.matvec(x)
+        assert float(torch.linalg.norm(r) / torch.linalg.norm(w["b"])) <= 1e-8
+
+
+def test_trained_correction_of_the_background_solve(capsys):
+    """Train the network on the pairs the background solve leaves (from the
+    background-preconditioned solver's own iterates), then solve with and
+    without it: the learned solve meets the tolerance on the FP64 true residual,
+    never falls back silently, and what the network gains (or costs) against the
+    background solve alone is measured and printed."""
+    import torch
+    from pybella_gb300 import learned, workloads
+    from pybella_gb300.spectral import BackgroundSolve
+    params, losses = learned.train_preconditioner(shape=(65, 33, 65), seeds=(1, 2), npairs=512, crop=32,
+                                                  steps=200, batch=16, background=True, skip=0.7)
+    assert np.isfinite(losses[-1][1]) and losses[-1][1] < losses[0][1]
+    shape = (65, 33, 65)
+    w = workloads.stratified_3d(9, *shape)
+    A = learned.operator_3d(w)
+    bg = BackgroundSolve(A)
+    net = learned.CNN(shape, block=2, mode="linear", skip=0.7)
+    net.set_params(params)
+    xb, sb = A.solve(w["b"], tol=1e-8, maxiter=4000, preconditioner=bg)
+    with warnings.catch_warnings(record=True) as rec:
+        warnings.simplefilter("always")
+        xl, sl = A.solve(w["b"], tol=1e-8, maxiter=4000, preconditioner=learned.LearnedPreconditioner(bg, net),
+                         method="fgmres", restart=30)
+    for x, st in ((xb, sb), (xl, sl)):
+        assert st["status"] == 0, st
+        r = w["b"] - A.matvec(x)
+        assert float(torch.linalg.norm(r) / torch.linalg.norm(w["b"])) <= 1e-8
+    assert bool(sl["fallback"]) == any("preconditioned solve failed" in str(m.message) for m in rec)
+    with capsys.disabled():
+        print("\ntrained correction (%s): background alone %d iterations %.4f s; background + network %d "
+              "iterations %.4f s (fallback %d); training loss %.3f -> %.3f"
+              % ("x".join(map(str, shape)), sb["iterations"], sb["seconds"], sl["iterations"], sl["seconds"],
+                 sl["fallback"], losses[0][1], losses[-1][1]))
