@@ -1167,44 +1167,34 @@ static int run_flex(bella_ws *ws, const Precond &pc, const bella_solve_opts *o, 
 constexpr int FG_MAXM = 30;
 constexpr int FG_MAXV = FG_MAXM + 1;
 
-// per-block partial sums of <V_i, w> (i < nv) and, with norm, of <w, w> (slot nv)
+constexpr int FG_XBLK = NSM * 2;    // blocks per inner product
+
+// block (bx, i): partial sum of <V_i, w> over a grid-stride share -> part[i * gridDim.x + bx]
+// (one inner product per block keeps the registers low; w is re-read from L2)
 __global__ void __launch_bounds__(VEC_BLOCK)
-k_fg_mdot(long long n, const float *V, long long ld, int nv, const float *w, int norm, double *part) {
-    double acc[FG_MAXV + 1];
-#pragma unroll
-    for (int i = 0; i <= FG_MAXV; ++i) acc[i] = 0.0;
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
-        const double wg = w[g];
-#pragma unroll
-        for (int i = 0; i < FG_MAXV; ++i)
-            if (i < nv) acc[i] += (double)V[i * ld + g] * wg;
-        if (norm) acc[FG_MAXV] += wg * wg;
-    }
-    __shared__ double red[FG_MAXV + 1][VEC_BLOCK / 32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int i = 0; i <= FG_MAXV; ++i) {
-        if (i < nv || (i == FG_MAXV && norm)) {
-            const double v = warp_sum(acc[i]);
-            if (lane == 0) red[i][wid] = v;
-        }
-    }
+k_fg_mdot(long long n, const float *V, long long ld, const float *w, double *part) {
+    const int i = blockIdx.y;
+    const float *v = V + i * ld;
+    double acc = 0.0;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x)
+        acc += (double)v[g] * (double)w[g];
+    __shared__ double red[VEC_BLOCK / 32];
+    const double s = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
     __syncthreads();
-    const int q = threadIdx.x;
-    if (q < nv || (q == nv && norm)) {
-        const int src = q < nv ? q : FG_MAXV;
+    if (threadIdx.x == 0) {
         double sum = 0.0;
-        for (int k = 0; k < VEC_BLOCK / 32; ++k) sum += red[src][k];
-        part[(size_t)blockIdx.x * (FG_MAXV + 1) + q] = sum;
+        for (int k = 0; k < VEC_BLOCK / 32; ++k) sum += red[k];
+        part[(size_t)i * gridDim.x + blockIdx.x] = sum;
     }
 }
 
-// out[q] = sum over blocks of part[b][q], q < nq, in block order (deterministic)
+// out[q] = sum over blocks of part[q * nblk + b], q < nq, in block order (deterministic)
 __global__ void k_fg_reduce(int nblk, const double *part, int nq, double *out) {
     const int q = threadIdx.x;
     if (q >= nq) return;
     double sum = 0.0;
-    for (int b = 0; b < nblk; ++b) sum += part[(size_t)b * (FG_MAXV + 1) + q];
+    for (int b = 0; b < nblk; ++b) sum += part[(size_t)q * nblk + b];
     out[q] = sum;
 }
 
@@ -1229,7 +1219,7 @@ k_fg_update(long long n, const float *V, long long ld, int nv, const double *h, 
     if (threadIdx.x == 0) {
         double sum = 0.0;
         for (int k = 0; k < VEC_BLOCK / 32; ++k) sum += red[k];
-        part[(size_t)blockIdx.x * (FG_MAXV + 1)] = sum;
+        part[blockIdx.x] = sum;
     }
 }
 
@@ -1262,7 +1252,8 @@ static int fg_ensure(bella_ws *ws, int m) {
     ws->fg_m = 0;
     BELLA_CUDA(cudaMalloc(&ws->fg_v, (size_t)(m + 1) * n * sizeof(float)));
     BELLA_CUDA(cudaMalloc(&ws->fg_z, (size_t)m * n * sizeof(float)));
-    BELLA_CUDA(cudaMalloc(&ws->fg_part, (size_t)NSM * 8 * (FG_MAXV + 1) * sizeof(double)));
+    BELLA_CUDA(cudaMalloc(&ws->fg_part, (size_t)(FG_XBLK > NSM * 8 ? FG_XBLK : NSM * 8) * (FG_MAXV + 1) *
+                                        sizeof(double)));
     BELLA_CUDA(cudaMalloc(&ws->fg_dev, 4 * (FG_MAXV + 1) * sizeof(double)));
     const double one = 1.0;
     BELLA_CUDA(cudaMemcpy(ws->fg_dev + 3 * (FG_MAXV + 1), &one, sizeof(double), cudaMemcpyHostToDevice));
@@ -1301,11 +1292,11 @@ static int fgmres_cycle(bella_ws *ws, const Precond &pc, int m, double rel, cuda
         if (rc != BELLA_OK) return rc;
         op_apply(ws, 1, zj, w, s);
         const int nv = j + 1;
-        k_fg_mdot<<<gv, VEC_BLOCK, 0, s>>>(n, V, n, nv, w, 0, ws->fg_part);
-        k_fg_reduce<<<1, 64, 0, s>>>(gv, ws->fg_part, nv, h1);
+        k_fg_mdot<<<dim3(FG_XBLK, nv), VEC_BLOCK, 0, s>>>(n, V, n, w, ws->fg_part);
+        k_fg_reduce<<<1, 64, 0, s>>>(FG_XBLK, ws->fg_part, nv, h1);
         k_fg_update<<<gv, VEC_BLOCK, 0, s>>>(n, V, n, nv, h1, w, 0, ws->fg_part);
-        k_fg_mdot<<<gv, VEC_BLOCK, 0, s>>>(n, V, n, nv, w, 0, ws->fg_part);
-        k_fg_reduce<<<1, 64, 0, s>>>(gv, ws->fg_part, nv, h2);
+        k_fg_mdot<<<dim3(FG_XBLK, nv), VEC_BLOCK, 0, s>>>(n, V, n, w, ws->fg_part);
+        k_fg_reduce<<<1, 64, 0, s>>>(FG_XBLK, ws->fg_part, nv, h2);
         k_fg_update<<<gv, VEC_BLOCK, 0, s>>>(n, V, n, nv, h2, w, 1, ws->fg_part);
         k_fg_reduce<<<1, 64, 0, s>>>(gv, ws->fg_part, 1, nrm);
         k_fg_scale<<<gv, VEC_BLOCK, 0, s>>>(n, w, nrm, w);
