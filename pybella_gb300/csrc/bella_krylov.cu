@@ -1167,25 +1167,36 @@ static int run_flex(bella_ws *ws, const Precond &pc, const bella_solve_opts *o, 
 constexpr int FG_MAXM = 30;
 constexpr int FG_MAXV = FG_MAXM + 1;
 
-constexpr int FG_XBLK = NSM * 2;    // blocks per inner product
+constexpr int FG_XBLK = NSM * 2;    // blocks per group of inner products
+constexpr int FG_GROUP = 8;         // inner products per block
 
-// block (bx, i): partial sum of <V_i, w> over a grid-stride share -> part[i * gridDim.x + bx]
-// (one inner product per block keeps the registers low; w is re-read from L2)
+// block (bx, gy): partial sums of <V_i, w> for the FG_GROUP vectors i of group gy
+// over a grid-stride share -> part[i * gridDim.x + bx]; w is read once per group
 __global__ void __launch_bounds__(VEC_BLOCK)
-k_fg_mdot(long long n, const float *V, long long ld, const float *w, double *part) {
-    const int i = blockIdx.y;
-    const float *v = V + i * ld;
-    double acc = 0.0;
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x)
-        acc += (double)v[g] * (double)w[g];
-    __shared__ double red[VEC_BLOCK / 32];
-    const double s = warp_sum(acc);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+k_fg_mdot(long long n, const float *V, long long ld, int nv, const float *w, double *part) {
+    const int i0 = blockIdx.y * FG_GROUP;
+    const int cnt = nv - i0 < FG_GROUP ? nv - i0 : FG_GROUP;
+    double acc[FG_GROUP];
+#pragma unroll
+    for (int q = 0; q < FG_GROUP; ++q) acc[q] = 0.0;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
+        const double wg = w[g];
+#pragma unroll
+        for (int q = 0; q < FG_GROUP; ++q)
+            if (q < cnt) acc[q] += (double)V[(i0 + q) * ld + g] * wg;
+    }
+    __shared__ double red[FG_GROUP][VEC_BLOCK / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < FG_GROUP; ++q) {
+        const double v = warp_sum(acc[q]);
+        if (lane == 0) red[q][wid] = v;
+    }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if ((int)threadIdx.x < cnt) {
         double sum = 0.0;
-        for (int k = 0; k < VEC_BLOCK / 32; ++k) sum += red[k];
-        part[(size_t)i * gridDim.x + blockIdx.x] = sum;
+        for (int k = 0; k < VEC_BLOCK / 32; ++k) sum += red[threadIdx.x][k];
+        part[(size_t)(i0 + threadIdx.x) * gridDim.x + blockIdx.x] = sum;
     }
 }
 
@@ -1292,10 +1303,11 @@ static int fgmres_cycle(bella_ws *ws, const Precond &pc, int m, double rel, cuda
         if (rc != BELLA_OK) return rc;
         op_apply(ws, 1, zj, w, s);
         const int nv = j + 1;
-        k_fg_mdot<<<dim3(FG_XBLK, nv), VEC_BLOCK, 0, s>>>(n, V, n, w, ws->fg_part);
+        const unsigned ng = (unsigned)((nv + FG_GROUP - 1) / FG_GROUP);
+        k_fg_mdot<<<dim3(FG_XBLK, ng), VEC_BLOCK, 0, s>>>(n, V, n, nv, w, ws->fg_part);
         k_fg_reduce<<<1, 64, 0, s>>>(FG_XBLK, ws->fg_part, nv, h1);
         k_fg_update<<<gv, VEC_BLOCK, 0, s>>>(n, V, n, nv, h1, w, 0, ws->fg_part);
-        k_fg_mdot<<<dim3(FG_XBLK, nv), VEC_BLOCK, 0, s>>>(n, V, n, w, ws->fg_part);
+        k_fg_mdot<<<dim3(FG_XBLK, ng), VEC_BLOCK, 0, s>>>(n, V, n, nv, w, ws->fg_part);
         k_fg_reduce<<<1, 64, 0, s>>>(FG_XBLK, ws->fg_part, nv, h2);
         k_fg_update<<<gv, VEC_BLOCK, 0, s>>>(n, V, n, nv, h2, w, 1, ws->fg_part);
         k_fg_reduce<<<1, 64, 0, s>>>(gv, ws->fg_part, 1, nrm);

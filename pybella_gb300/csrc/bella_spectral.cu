@@ -46,8 +46,11 @@ struct bella_spectral3d {
     float *dscale;         // 1 / diag_inv
     float *w1, *w2;        // transform work arrays (n floats each)
     float *c1, *c2;        // work arrays of a preconditioner composed with the network
-    double *lc, *ld;       // Thomas scratch, [ny][Kx*Kz] each
+    float *la, *lc, *li;   // Thomas factors of every mode line, [ny][Kx*Kz] each
     double idx2, idy2, idz2;
+    int fft_x, fft_z;      // 1: this axis transforms by FFT (power-of-two length), 0: by GEMM
+    int Lx, Lz, px, pz;    // FFT lengths and their log2
+    float2 *twx, *twz;     // twiddles exp(-2 pi i t / L), t < L/2
     long long launches;
 };
 
@@ -152,6 +155,181 @@ static void sgemm(int M, int N, int K, const float *A, long long lda, const floa
     else k_sgemm<false><<<grid, SG_THREADS, 0, s>>>(M, N, K, A, lda, nullptr, B, ldb, C, ldc);
 }
 
+// ---- FFT path of the transforms (power-of-two lengths 16..1024) ---------------
+// Every line of the axis is transformed by a two-pass FFT, L = 16 * R2:
+//   X[k1 + 16 k2] = sum_n2 W_R2^(n2 k2) W_L^(n2 k1) sum_n1 W_16^(n1 k1) x[R2 n1 + n2]
+// pass A: one thread per (line, n2) does the 16-point DFT in registers and the
+// twiddle W_L^(n2 k1), writing through shared memory; pass B: one thread per
+// (line, k1) does the R2-point DFT in registers and writes the outputs.
+//   Hartley (periodic axis, N = n - 1 = L):  H_k = Re F_k - Im F_k of the FFT of
+//     p (p_0 = (r_0 + r_N)/2 on the duplicated seam); inverse: the same with 1/N,
+//     the seam copied out.
+//   DCT-I (wall axis, M = n - 1, L = 2M):  S_k = sum_{i=0..M} cos(pi k i / M) r_i
+//     = (Y_k + r_0 + (-1)^k r_M) / 2 with Y the FFT of the even extension
+//     (r_0 .. r_M, r_{M-1} .. r_1); forward divides by the DCT-I norms, the
+//     inverse is S itself.
+// Line l of the axis has its t-th value at l * lmul + t * ts (z lines: lmul =
+// row length, ts = 1; x lines: lmul = 1, ts = ny * Kz).  Threads run along t for
+// z lines and across lines for x lines, so global accesses are coalesced both
+// ways, and the shared-memory layout follows the same order.
+constexpr int FFT_R1 = 16;
+__constant__ float2 c_tw64[64];            // exp(-2 pi i t / 64)
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__host__ __device__ constexpr int bitrev_c(int i, int R) {
+    int r = 0;
+    for (int b = 1; b < R; b <<= 1) {
+        r = (r << 1) | (i & 1);
+        i >>= 1;
+    }
+    return r;
+}
+
+// one radix-2 stage (butterflies of span LEN) of an in-register FFT of R values,
+// then the next stage; every index is a compile-time constant
+template <int R, int LEN>
+struct RegStage {
+    static __device__ __forceinline__ void run(float2 (&v)[R]) {
+#pragma unroll
+        for (int i = 0; i < R; i += LEN) {
+#pragma unroll
+            for (int k = 0; k < LEN / 2; ++k) {
+                const float2 w = c_tw64[k * (64 / LEN)];
+                const float2 u = v[i + k], t = cmulf(w, v[i + k + LEN / 2]);
+                v[i + k] = make_float2(u.x + t.x, u.y + t.y);
+                v[i + k + LEN / 2] = make_float2(u.x - t.x, u.y - t.y);
+            }
+        }
+        RegStage<R, 2 * LEN>::run(v);
+    }
+};
+template <int R>
+struct RegStage<R, 2 * R> {
+    static __device__ __forceinline__ void run(float2 (&)[R]) {}
+};
+
+// forward DFT of R (power of two, <= 64) values in registers, natural order out
+template <int R>
+__device__ __forceinline__ void reg_fft(float2 (&v)[R]) {
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const int j = bitrev_c(i, R);
+        if (j > i) {
+            const float2 t = v[i];
+            v[i] = v[j];
+            v[j] = t;
+        }
+    }
+    RegStage<R, 2>::run(v);
+}
+template <>
+__device__ __forceinline__ void reg_fft<1>(float2 (&)[1]) {}
+
+template <int R2>
+struct FftShape {
+    static constexpr int L = FFT_R1 * R2;
+    static constexpr int LPC = (256 / R2) < 128 ? (256 / R2) : 128;   // lines per CTA
+    static constexpr int SMEM = LPC * FFT_R1 * (R2 + 1) > FFT_R1 * R2 * (LPC + 1) ? LPC * FFT_R1 * (R2 + 1)
+                                                                                  : FFT_R1 * R2 * (LPC + 1);
+};
+
+template <int KIND, bool FWD, int R2>   // KIND 0: Hartley, 1: DCT-I
+__global__ void __launch_bounds__(256)
+k_sp_fft(long long nlines, const float *__restrict__ in, long long in_lmul, long long in_ts,
+         const float *__restrict__ scale, float *__restrict__ out, long long out_lmul, long long out_ts,
+         const float2 *__restrict__ twL) {
+    constexpr int R1 = FFT_R1, L = FftShape<R2>::L, M = L / 2, LPC = FftShape<R2>::LPC;
+    __shared__ float2 S[FftShape<R2>::SMEM];
+    const long long l0 = (long long)blockIdx.x * LPC;
+    const int nl = (int)(nlines - l0 < LPC ? nlines - l0 : LPC);
+    const bool ic = in_ts == 1, oc = out_ts == 1;
+    // shared layout: [line][k1][n2] (padded rows) when threads run along a line,
+    // [k1][n2][line] (padded) when they run across lines
+    auto sidx = [&](int line, int k1, int n2) {
+        return ic ? (line * R1 + k1) * (R2 + 1) + n2 : (k1 * R2 + n2) * (LPC + 1) + line;
+    };
+    auto ld = [&](long long g) {
+        float v = in[g];
+        if (scale) v *= scale[g];
+        return v;
+    };
+    for (int q = threadIdx.x; q < nl * R2; q += blockDim.x) {
+        const int line = ic ? q / R2 : q % nl, n2 = ic ? q % R2 : q / nl;
+        const long long base = (l0 + line) * in_lmul;
+        float2 v[R1];
+#pragma unroll
+        for (int n1 = 0; n1 < R1; ++n1) {
+            const int j = R2 * n1 + n2;
+            float x;
+            if (KIND == 0)
+                x = (FWD && j == 0) ? 0.5f * (ld(base) + ld(base + (long long)L * in_ts)) : ld(base + (long long)j * in_ts);
+            else
+                x = ld(base + (long long)(j <= M ? j : L - j) * in_ts);
+            v[n1] = make_float2(x, 0.f);
+        }
+        reg_fft<R1>(v);
+#pragma unroll
+        for (int k1 = 0; k1 < R1; ++k1) S[sidx(line, k1, n2)] = cmulf(twL[n2 * k1], v[k1]);
+    }
+    __syncthreads();
+    const int nout = KIND == 0 ? L : M + 1;
+    for (int q = threadIdx.x; q < nl * R1; q += blockDim.x) {
+        const int line = ic ? q / R1 : q % nl, k1 = ic ? q % R1 : q / nl;
+        float2 u[R2];
+#pragma unroll
+        for (int n2 = 0; n2 < R2; ++n2) u[n2] = S[sidx(line, k1, n2)];
+        reg_fft<R2>(u);
+        const long long obase = (l0 + line) * out_lmul;
+        float e0 = 0.f, eM = 0.f;
+        if (KIND == 1) {
+            const long long base = (l0 + line) * in_lmul;
+            e0 = ld(base);
+            eM = ld(base + (long long)M * in_ts);
+        }
+#pragma unroll
+        for (int k2 = 0; k2 < R2; ++k2) {
+            const int k = k1 + R1 * k2;
+            if (k >= nout) continue;
+            float val;
+            if (KIND == 0) {
+                val = u[k2].x - u[k2].y;
+                if (!FWD) val *= 1.f / (float)L;
+            } else {
+                val = 0.5f * (u[k2].x + e0 + ((k & 1) ? -eM : eM));
+                if (FWD) val *= (k == 0 || k == M) ? 1.f / (float)M : 2.f / (float)M;
+            }
+            out[obase + (long long)k * out_ts] = val;
+            if (KIND == 0 && !FWD && k == 0) out[obase + (long long)L * out_ts] = val;   // seam copy
+        }
+    }
+    (void)oc;
+}
+
+template <int KIND, bool FWD>
+static void sp_fft(long long nlines, int L, const float *in, long long in_lmul, long long in_ts, const float *scale,
+                   float *out, long long out_lmul, long long out_ts, const float2 *tw, cudaStream_t s) {
+#define BELLA_FFT_CASE(R2)                                                                                      \
+    case FFT_R1 * R2: {                                                                                         \
+        const unsigned grid = (unsigned)((nlines + FftShape<R2>::LPC - 1) / FftShape<R2>::LPC);                 \
+        k_sp_fft<KIND, FWD, R2><<<grid, 256, 0, s>>>(nlines, in, in_lmul, in_ts, scale, out, out_lmul, out_ts, tw); \
+        break;                                                                                                  \
+    }
+    switch (L) {
+        BELLA_FFT_CASE(1)
+        BELLA_FFT_CASE(2)
+        BELLA_FFT_CASE(4)
+        BELLA_FFT_CASE(8)
+        BELLA_FFT_CASE(16)
+        BELLA_FFT_CASE(32)
+        BELLA_FFT_CASE(64)
+        default: break;
+    }
+#undef BELLA_FFT_CASE
+}
+
 // y-cell means of the three cell coefficients over the interior x and z cells
 // (cells 1..n-1: one period on a periodic axis, the cells between walls on a
 // wall axis) and y-node means of hcenter; one CTA per y index, fixed-order sums.
@@ -202,90 +380,190 @@ __global__ void k_sp_recip(long long n, const double *dinv, float *out) {
         out[g] = (float)(1.0 / dinv[g]);
 }
 
-// One FP64 Thomas solve along y per (kx, kz) mode, in place on W [Kx][ny][Kz].
-// Line operator: alpha M^T Cx M + beta D^T Cy D + gamma M^T Cz M + diag(hcm)
-// with alpha = -mux (4 - muz) / (16 dx^2), beta = -(4 - mux)(4 - muz) / (16 dy^2),
-// gamma = -(4 - mux) muz / (16 dz^2).  Without hcenter, three kinds of line are
-// singular: alpha = gamma = 0 (null vector: constants), beta = 0 (null vector
-// (-1)^j) and all zero (output 0).
+// Line operator of mode (kx, kz): alpha M^T Cx M + beta D^T Cy D + gamma M^T Cz M
+// + diag(hcm) with alpha = -mux (4 - muz) / (16 dx^2), beta = -(4 - mux)(4 - muz) /
+// (16 dy^2), gamma = -(4 - mux) muz / (16 dz^2).  Without hcenter three kinds of
+// line are singular: alpha = gamma = 0 (null vector: constants, cat 1), beta = 0
+// (null vector (-1)^j, cat 2) and all zero (cat 3, output 0).
+struct LineCoef {
+    double al, be, ga;
+    int cat;
+};
+
+__device__ __forceinline__ LineCoef line_coef(int kx, int kz, const double *mux, const double *muz, int hc_zero,
+                                              double idx2, double idy2, double idz2) {
+    const double mx = mux[kx], mz = muz[kz];
+    LineCoef c;
+    c.al = -0.0625 * mx * (4.0 - mz) * idx2;
+    c.be = -0.0625 * (4.0 - mx) * (4.0 - mz) * idy2;
+    c.ga = -0.0625 * (4.0 - mx) * mz * idz2;
+    c.cat = 0;
+    if (hc_zero) {
+        if (c.al == 0.0 && c.be == 0.0 && c.ga == 0.0) c.cat = 3;
+        else if (c.al == 0.0 && c.ga == 0.0) c.cat = 1;
+        else if (c.be == 0.0) c.cat = 2;
+    }
+    return c;
+}
+
+// Thomas factors of every mode line, once per operator, computed in FP64 and
+// stored in FP32: la[j] (sub-diagonal, 0 on the first solved row), lc[j] = c'_j,
+// li[j] = 1 / (b_j - a_j c'_{j-1}); a singular line pins x_0 = 0 and is factored
+// from row 1.  Layout [j][line].
 __global__ void __launch_bounds__(128)
-k_sp_lines(int Kx, int ny, int Kz, float *W, const double *mux, const double *muz, const double *cx,
-           const double *cy, const double *cz, const double *hcm, int hc_zero, double idx2, double idy2, double idz2,
-           double *lc, double *ld) {
+k_sp_factor(int Kx, int ny, int Kz, const double *mux, const double *muz, const double *cx, const double *cy,
+            const double *cz, const double *hcm, int hc_zero, double idx2, double idy2, double idz2, float *la,
+            float *lc, float *li) {
+    const long long nl = (long long)Kx * Kz;
+    const long long line = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (line >= nl) return;
+    const LineCoef L = line_coef((int)(line / Kz), (int)(line % Kz), mux, muz, hc_zero, idx2, idy2, idz2);
+    if (L.cat == 3) return;
+    auto off = [&](int j) { return L.al * cx[j] - L.be * cy[j] + L.ga * cz[j]; };   // between nodes j, j+1
+    auto diag = [&](int j) {
+        double d = hcm[j];
+        if (j > 0) d += L.al * cx[j - 1] + L.be * cy[j - 1] + L.ga * cz[j - 1];
+        if (j < ny - 1) d += L.al * cx[j] + L.be * cy[j] + L.ga * cz[j];
+        return d;
+    };
+    const int j0 = L.cat ? 1 : 0;
+    double cprev = 0.0;
+    for (int j = j0; j < ny; ++j) {
+        const double a = j > j0 ? off(j - 1) : 0.0;
+        const double c = j < ny - 1 ? off(j) : 0.0;
+        const double inv = 1.0 / (diag(j) - a * cprev);
+        cprev = c * inv;
+        la[(long long)j * nl + line] = (float)a;
+        lc[(long long)j * nl + line] = (float)cprev;
+        li[(long long)j * nl + line] = (float)inv;
+    }
+}
+
+// One Thomas solve along y per (kx, kz) mode with the precomputed factors, in
+// place on W [Kx][ny][Kz] (a mode's values are Kz apart; consecutive threads
+// take consecutive kz, so every access is coalesced across the warp).  The
+// sweeps run in FP32 with the factors computed in FP64 (GB300's FP64 pipe runs
+// at 1/64 of the FP32 rate and would bound this kernel); the null-component
+// sums of the few singular lines stay in FP64.
+__global__ void __launch_bounds__(128)
+k_sp_lines(int Kx, int ny, int Kz, float *__restrict__ W, const double *__restrict__ mux,
+           const double *__restrict__ muz, int hc_zero, double idx2, double idy2, double idz2,
+           const float *__restrict__ la, const float *__restrict__ lc, const float *__restrict__ li) {
     const long long nl = (long long)Kx * Kz;
     const long long line = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (line >= nl) return;
     const int kx = (int)(line / Kz), kz = (int)(line % Kz);
-    const double mx = mux[kx], mz = muz[kz];
-    const double al = -0.0625 * mx * (4.0 - mz) * idx2;
-    const double be = -0.0625 * (4.0 - mx) * (4.0 - mz) * idy2;
-    const double ga = -0.0625 * (4.0 - mx) * mz * idz2;
-    float *w = W + (long long)kx * ny * Kz + kz;
-    int cat = 0;
-    if (hc_zero) {
-        if (al == 0.0 && be == 0.0 && ga == 0.0) cat = 3;
-        else if (al == 0.0 && ga == 0.0) cat = 1;
-        else if (be == 0.0) cat = 2;
-    }
-    if (cat == 3) {
+    const LineCoef L = line_coef(kx, kz, mux, muz, hc_zero, idx2, idy2, idz2);
+    float *__restrict__ w = W + (long long)kx * ny * Kz + kz;
+    if (L.cat == 3) {
         for (int j = 0; j < ny; ++j) w[(long long)j * Kz] = 0.f;
         return;
     }
-    double proj = 0.0;
-    if (cat) {
-        for (int j = 0; j < ny; ++j) proj += (cat == 2 && (j & 1)) ? -(double)w[(long long)j * Kz] : (double)w[(long long)j * Kz];
-        proj /= ny;
+    float proj = 0.f;
+    if (L.cat) {                               // remove the right-hand side's null component
+        double ps = 0.0;
+        for (int j = 0; j < ny; ++j) ps += (L.cat == 2 && (j & 1)) ? -(double)w[(long long)j * Kz] : (double)w[(long long)j * Kz];
+        proj = (float)(ps / ny);
     }
-    auto off = [&](int j) { return al * cx[j] - be * cy[j] + ga * cz[j]; };   // between nodes j and j+1
-    auto diag = [&](int j) {
-        double d = hcm[j];
-        if (j > 0) d += al * cx[j - 1] + be * cy[j - 1] + ga * cz[j - 1];
-        if (j < ny - 1) d += al * cx[j] + be * cy[j] + ga * cz[j];
-        return d;
-    };
-    const int j0 = cat ? 1 : 0;
-    double cprev = 0.0, dprev = 0.0;
-    for (int j = j0; j < ny; ++j) {
-        double rhs = w[(long long)j * Kz];
-        if (cat) rhs -= (cat == 2 && (j & 1)) ? -proj : proj;
-        const double a = j > j0 ? off(j - 1) : 0.0;
-        const double c = j < ny - 1 ? off(j) : 0.0;
-        const double den = diag(j) - a * cprev;
-        cprev = c / den;
-        dprev = (rhs - a * dprev) / den;
-        lc[(long long)j * nl + line] = cprev;
-        ld[(long long)j * nl + line] = dprev;
+    // sweeps in batches of 8 rows: the 8 loads of a batch are issued before its
+    // dependent arithmetic, and its stores after it (the in-place rows would
+    // otherwise serialise every load behind the previous row's store)
+    constexpr int B = 8;
+    const int j0 = L.cat ? 1 : 0;
+    float d = 0.f;
+    for (int jb = j0; jb < ny; jb += B) {
+        float r[B], a[B], iv[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int j = jb + u;
+            if (j < ny) {
+                const long long q = (long long)j * nl + line;
+                r[u] = w[(long long)j * Kz];
+                a[u] = la[q];
+                iv[u] = li[q];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int j = jb + u;
+            if (j < ny) {
+                float rhs = r[u];
+                if (L.cat) rhs -= (L.cat == 2 && (j & 1)) ? -proj : proj;
+                d = fmaf(-a[u], d, rhs) * iv[u];
+                r[u] = d;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+            if (jb + u < ny) w[(long long)(jb + u) * Kz] = r[u];
     }
-    double x = 0.0, sum = 0.0;
-    for (int j = ny - 1; j >= j0; --j) {
-        x = ld[(long long)j * nl + line] - (j < ny - 1 ? lc[(long long)j * nl + line] * x : 0.0);
-        ld[(long long)j * nl + line] = x;
-        sum += (cat == 2 && (j & 1)) ? -x : x;
+    float x = 0.f;
+    double sum = 0.0;
+    for (int jt = ny - 1; jt >= j0; jt -= B) {
+        float r[B], c[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int j = jt - u;
+            if (j >= j0) {
+                r[u] = w[(long long)j * Kz];
+                c[u] = lc[(long long)j * nl + line];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int j = jt - u;
+            if (j >= j0) {
+                x = fmaf(-c[u], x, r[u]);
+                r[u] = x;
+                if (L.cat) sum += (L.cat == 2 && (j & 1)) ? -(double)x : (double)x;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+            if (jt - u >= j0) w[(long long)(jt - u) * Kz] = r[u];
     }
-    const double shift = cat ? sum / ny : 0.0;   // x_0 = 0 pinned; remove the null component
-    if (cat) w[0] = (float)(-shift);
-    for (int j = j0; j < ny; ++j) {
-        const double u = (cat == 2 && (j & 1)) ? -1.0 : 1.0;
-        w[(long long)j * Kz] = (float)(ld[(long long)j * nl + line] - shift * u);
-    }
+    if (!L.cat) return;
+    const float shift = (float)(sum / ny);     // x_0 = 0 pinned; remove the null component
+    w[0] = -shift;
+    for (int j = j0; j < ny; ++j) w[(long long)j * Kz] -= (L.cat == 2 && (j & 1)) ? -shift : shift;
 }
 
 // out = A_bg^+ (in / diag_inv): the background inverse applied to a residual of
 // the Jacobi-scaled system; FP32 in and out.
 int spectral_apply_dev(bella_spectral3d *sp, const float *in, float *out, cudaStream_t s) {
     const int nx = sp->nx, ny = sp->ny, nz = sp->nz, Kx = sp->Kx, Kz = sp->Kz;
-    // z forward: w1[(x,y)][kz] = sum_z in[(x,y)][z] / dinv * Fz[kz][z]
-    sgemm(nx * ny, Kz, nz, in, nz, sp->dscale, sp->tzfT, Kz, sp->w1, Kz, s);
-    // x forward: w2[kx][(y,kz)] = sum_x Fx[kx][x] w1[x][(y,kz)]
-    sgemm(Kx, ny * Kz, nx, sp->txf, nx, nullptr, sp->w1, (long long)ny * Kz, sp->w2, (long long)ny * Kz, s);
+    const long long rows = (long long)nx * ny, xl = (long long)ny * Kz;
+    // z forward: w1[(x,y)][kz] from in[(x,y)][z] / dinv
+    if (sp->fft_z) {
+        if (sp->zper) sp_fft<0, true>(rows, sp->Lz, in, nz, 1, sp->dscale, sp->w1, Kz, 1, sp->twz, s);
+        else sp_fft<1, true>(rows, sp->Lz, in, nz, 1, sp->dscale, sp->w1, Kz, 1, sp->twz, s);
+    } else {
+        sgemm(nx * ny, Kz, nz, in, nz, sp->dscale, sp->tzfT, Kz, sp->w1, Kz, s);
+    }
+    // x forward: w2[kx][(y,kz)] from w1[x][(y,kz)]
+    if (sp->fft_x) {
+        if (sp->xper) sp_fft<0, true>(xl, sp->Lx, sp->w1, 1, xl, nullptr, sp->w2, 1, xl, sp->twx, s);
+        else sp_fft<1, true>(xl, sp->Lx, sp->w1, 1, xl, nullptr, sp->w2, 1, xl, sp->twx, s);
+    } else {
+        sgemm(Kx, ny * Kz, nx, sp->txf, nx, nullptr, sp->w1, xl, sp->w2, xl, s);
+    }
     const long long nl = (long long)Kx * Kz;
-    k_sp_lines<<<(unsigned)((nl + 127) / 128), 128, 0, s>>>(Kx, ny, Kz, sp->w2, sp->mux, sp->muz, sp->cx, sp->cy,
-                                                            sp->cz, sp->hcm, sp->hc_zero, sp->idx2, sp->idy2,
-                                                            sp->idz2, sp->lc, sp->ld);
-    // x inverse: w1[x][(y,kz)] = sum_kx Ix[x][kx] w2[kx][(y,kz)]
-    sgemm(nx, ny * Kz, Kx, sp->txi, Kx, nullptr, sp->w2, (long long)ny * Kz, sp->w1, (long long)ny * Kz, s);
-    // z inverse: out[(x,y)][z] = sum_kz w1[(x,y)][kz] Iz[z][kz]
-    sgemm(nx * ny, nz, Kz, sp->w1, Kz, nullptr, sp->tziT, nz, out, nz, s);
+    k_sp_lines<<<(unsigned)((nl + 127) / 128), 128, 0, s>>>(Kx, ny, Kz, sp->w2, sp->mux, sp->muz, sp->hc_zero,
+                                                            sp->idx2, sp->idy2, sp->idz2, sp->la, sp->lc, sp->li);
+    // x inverse: w1[x][(y,kz)] from w2[kx][(y,kz)]
+    if (sp->fft_x) {
+        if (sp->xper) sp_fft<0, false>(xl, sp->Lx, sp->w2, 1, xl, nullptr, sp->w1, 1, xl, sp->twx, s);
+        else sp_fft<1, false>(xl, sp->Lx, sp->w2, 1, xl, nullptr, sp->w1, 1, xl, sp->twx, s);
+    } else {
+        sgemm(nx, ny * Kz, Kx, sp->txi, Kx, nullptr, sp->w2, xl, sp->w1, xl, s);
+    }
+    // z inverse: out[(x,y)][z] from w1[(x,y)][kz]
+    if (sp->fft_z) {
+        if (sp->zper) sp_fft<0, false>(rows, sp->Lz, sp->w1, Kz, 1, nullptr, out, nz, 1, sp->twz, s);
+        else sp_fft<1, false>(rows, sp->Lz, sp->w1, Kz, 1, nullptr, out, nz, 1, sp->twz, s);
+    } else {
+        sgemm(nx * ny, nz, Kz, sp->w1, Kz, nullptr, sp->tziT, nz, out, nz, s);
+    }
     sp->launches += 5;
     return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
 }
@@ -293,8 +571,9 @@ int spectral_apply_dev(bella_spectral3d *sp, const float *in, float *out, cudaSt
 float *spectral_work(bella_spectral3d *sp, int which) { return which ? sp->c2 : sp->c1; }
 long long spectral_size(const bella_spectral3d *sp) { return sp->n; }
 
-// eigenvalues of D^T D and the forward / inverse transform matrices of one axis
-static void axis_basis(int n, int periodic, std::vector<double> &mu, std::vector<float> &fwd,
+// eigenvalues of D^T D and (dense = 1, the GEMM path) the forward / inverse
+// transform matrices of one axis
+static void axis_basis(int n, int periodic, int dense, std::vector<double> &mu, std::vector<float> &fwd,
                        std::vector<float> &inv, int &K) {
     const double pi = 3.14159265358979323846;
     if (periodic) {
@@ -307,6 +586,7 @@ static void axis_basis(int n, int periodic, std::vector<double> &mu, std::vector
         }
         mu[0] = 0.0;
         if (N % 2 == 0) mu[N / 2] = 4.0;
+        if (!dense) return;
         fwd.assign((size_t)K * n, 0.f);
         inv.assign((size_t)n * K, 0.f);
         for (int k = 0; k < K; ++k)
@@ -328,6 +608,7 @@ static void axis_basis(int n, int periodic, std::vector<double> &mu, std::vector
         }
         mu[0] = 0.0;
         mu[K - 1] = 4.0;
+        if (!dense) return;
         fwd.assign((size_t)K * n, 0.f);
         inv.assign((size_t)n * K, 0.f);
         for (int k = 0; k < K; ++k) {
@@ -352,7 +633,8 @@ int bella_spectral3d_destroy(bella_spectral3d *sp) {
     if (!sp) return BELLA_OK;
     cudaSetDevice(sp->device);
     void *ptrs[] = {sp->txf, sp->txi, sp->tzfT, sp->tziT, sp->mux, sp->muz, sp->cx, sp->cy, sp->cz,
-                    sp->hcm, sp->dscale, sp->w1, sp->w2, sp->c1, sp->c2, sp->lc, sp->ld};
+                    sp->hcm, sp->dscale, sp->w1, sp->w2, sp->c1, sp->c2, sp->la, sp->lc, sp->li,
+                    sp->twx, sp->twz};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete sp;
@@ -378,22 +660,39 @@ int bella_spectral3d_create(bella_spectral3d **out, const bella_op3d *op, int de
     sp->idx2 = 1.0 / (op->dx * op->dx);
     sp->idy2 = 1.0 / (op->dy * op->dy);
     sp->idz2 = 1.0 / (op->dz * op->dz);
+    // FFT path per axis when the transform length is a power of two that fits a CTA
+    auto fft_len = [](int n, int periodic, int *L, int *p) {
+        const int len = periodic ? n - 1 : 2 * (n - 1);
+        if (len < FFT_R1 || len > 64 * FFT_R1 || (len & (len - 1))) return 0;
+        *L = len;
+        *p = 0;
+        while ((1 << *p) < len) ++*p;
+        return 1;
+    };
+    sp->fft_x = fft_len(op->nx, sp->xper, &sp->Lx, &sp->px);
+    sp->fft_z = fft_len(op->nz, sp->zper, &sp->Lz, &sp->pz);
     std::vector<double> mux, muz;
     std::vector<float> fx, ix, fz, iz;
-    axis_basis(op->nx, sp->xper, mux, fx, ix, sp->Kx);
-    axis_basis(op->nz, sp->zper, muz, fz, iz, sp->Kz);
+    axis_basis(op->nx, sp->xper, !sp->fft_x, mux, fx, ix, sp->Kx);
+    axis_basis(op->nz, sp->zper, !sp->fft_z, muz, fz, iz, sp->Kz);
     const int nx = op->nx, ny = op->ny, nz = op->nz, Kx = sp->Kx, Kz = sp->Kz;
-    std::vector<float> fzT((size_t)nz * Kz), izT((size_t)Kz * nz);
-    for (int k = 0; k < Kz; ++k)
-        for (int z = 0; z < nz; ++z) {
-            fzT[(size_t)z * Kz + k] = fz[(size_t)k * nz + z];
-            izT[(size_t)k * nz + z] = iz[(size_t)z * Kz + k];
-        }
+    std::vector<float> fzT, izT;
+    if (!sp->fft_z) {
+        fzT.resize((size_t)nz * Kz);
+        izT.resize((size_t)Kz * nz);
+        for (int k = 0; k < Kz; ++k)
+            for (int z = 0; z < nz; ++z) {
+                fzT[(size_t)z * Kz + k] = fz[(size_t)k * nz + z];
+                izT[(size_t)k * nz + z] = iz[(size_t)z * Kz + k];
+            }
+    }
     const long long nl = (long long)Kx * Kz;
-    bool ok = cudaMalloc(&sp->txf, fx.size() * sizeof(float)) == cudaSuccess &&
-              cudaMalloc(&sp->txi, ix.size() * sizeof(float)) == cudaSuccess &&
-              cudaMalloc(&sp->tzfT, fzT.size() * sizeof(float)) == cudaSuccess &&
-              cudaMalloc(&sp->tziT, izT.size() * sizeof(float)) == cudaSuccess &&
+    auto upload = [&](float **dst, const std::vector<float> &v) {
+        if (v.empty()) return true;
+        return cudaMalloc(dst, v.size() * sizeof(float)) == cudaSuccess &&
+               cudaMemcpyAsync(*dst, v.data(), v.size() * sizeof(float), cudaMemcpyHostToDevice, s) == cudaSuccess;
+    };
+    bool ok = upload(&sp->txf, fx) && upload(&sp->txi, ix) && upload(&sp->tzfT, fzT) && upload(&sp->tziT, izT) &&
               cudaMalloc(&sp->mux, Kx * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&sp->muz, Kz * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&sp->cx, ny * sizeof(double)) == cudaSuccess &&
@@ -405,16 +704,13 @@ int bella_spectral3d_create(bella_spectral3d **out, const bella_op3d *op, int de
               cudaMalloc(&sp->w2, sp->n * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&sp->c1, sp->n * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&sp->c2, sp->n * sizeof(float)) == cudaSuccess &&
-              cudaMalloc(&sp->lc, (size_t)ny * nl * sizeof(double)) == cudaSuccess &&
-              cudaMalloc(&sp->ld, (size_t)ny * nl * sizeof(double)) == cudaSuccess;
+              cudaMalloc(&sp->la, (size_t)ny * nl * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&sp->lc, (size_t)ny * nl * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&sp->li, (size_t)ny * nl * sizeof(float)) == cudaSuccess;
     if (!ok) {
         bella_spectral3d_destroy(sp);
         return BELLA_ECUDA;
     }
-    cudaMemcpyAsync(sp->txf, fx.data(), fx.size() * sizeof(float), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(sp->txi, ix.data(), ix.size() * sizeof(float), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(sp->tzfT, fzT.data(), fzT.size() * sizeof(float), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(sp->tziT, izT.data(), izT.size() * sizeof(float), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(sp->mux, mux.data(), Kx * sizeof(double), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(sp->muz, muz.data(), Kz * sizeof(double), cudaMemcpyHostToDevice, s);
     k_sp_means<<<ny, 256, 0, s>>>(nx, ny, nz, op->hplusx, op->hplusy, op->hplusz, op->hcenter, sp->cx, sp->cy,
@@ -429,7 +725,36 @@ int bella_spectral3d_create(bella_spectral3d **out, const bella_op3d *op, int de
     sp->hc_zero = 1;
     for (int j = 0; j < ny; ++j)
         if (hcm[j] != 0.0) sp->hc_zero = 0;
-    sp->launches = 2;
+    auto twiddles = [&](int L, float2 **dst) {
+        std::vector<float2> t(L);
+        const double pi = 3.14159265358979323846;
+        for (int k = 0; k < L; ++k)
+            t[k] = make_float2((float)cos(2.0 * pi * k / L), (float)-sin(2.0 * pi * k / L));
+        if (cudaMalloc(dst, t.size() * sizeof(float2)) != cudaSuccess) return false;
+        return cudaMemcpy(*dst, t.data(), t.size() * sizeof(float2), cudaMemcpyHostToDevice) == cudaSuccess;
+    };
+    {
+        float2 t64[64];
+        for (int k = 0; k < 64; ++k)
+            t64[k] = make_float2((float)cos(2.0 * 3.14159265358979323846 * k / 64),
+                                 (float)-sin(2.0 * 3.14159265358979323846 * k / 64));
+        if (cudaMemcpyToSymbol(c_tw64, t64, sizeof(t64)) != cudaSuccess) {
+            bella_spectral3d_destroy(sp);
+            return BELLA_ECUDA;
+        }
+    }
+    if ((sp->fft_x && !twiddles(sp->Lx, &sp->twx)) || (sp->fft_z && !twiddles(sp->Lz, &sp->twz))) {
+        bella_spectral3d_destroy(sp);
+        return BELLA_ECUDA;
+    }
+    k_sp_factor<<<(unsigned)((nl + 127) / 128), 128, 0, s>>>(Kx, ny, Kz, sp->mux, sp->muz, sp->cx, sp->cy, sp->cz,
+                                                             sp->hcm, sp->hc_zero, sp->idx2, sp->idy2, sp->idz2,
+                                                             sp->la, sp->lc, sp->li);
+    if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+        bella_spectral3d_destroy(sp);
+        return BELLA_ECUDA;
+    }
+    sp->launches = 3;
     *out = sp;
     return BELLA_OK;
 }
