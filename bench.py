@@ -1,24 +1,30 @@
-"""Benchmark: standalone 2D nodal Helmholtz solves (2049x1025, 9-point, rtol 1e-8).
+"""Benchmark: solves/s to a 1e-8 relative residual, learned preconditioner vs plain BiCGStab.
 
-One step = one projection solve of one seeded synthetic system: the
-reference-packed operands are turned into device flux planes
-(bella_op2d_set) and solved by BiCGStab on the GPU (``--precision df64``,
-the default: double-float arithmetic on the FP32 pipe, convergence judged on
-the FP64 true residual; ``fp64``: the reference algorithm in FP64; ``mixed``:
-FP32 inner solves in FP64 refinement with FP64 fallback) to a true relative
-residual of 1e-8.  ``--workload ensemble`` times the 48-member ensemble in one
-persistent launch per round; ``--workload learned3d`` trains the learned
-preconditioner and times it against plain BiCGStab on the 3D 27-point system.
-Seeds cycle over up to 64 pre-generated systems resident in HBM; the L2 is
-flushed (256 MB write) before every step.
+Default workload (``--workload learned3d``): the 3D 27-point nodal system at
+257x129x257 nodes (stratified background times a seeded log-normal(0.1) cell
+factor, divergence right-hand side).  The learned preconditioner -- the
+background (spectral) solve of the horizontally averaged operator corrected by
+a 6-layer BF16 network trained on the GPU with the library's own kernels --
+runs inside flexible GMRES with FP64 refinement; one step = the background
+solve's set-up from the step's coefficients + one solve, 256 MB L2 flush
+before every step.  The same JSON line carries the plain double-float
+BiCGStab arm (1 warm-up + 1 timed step: one plain solve takes tens of
+seconds), the background-solve-only arm, the end-to-end rate from host
+memory, the network's roofline and the CPU baseline.
 
-    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+``--workload solve2d``: the 2049x1025 standalone 9-point solve (plain
+double-float BiCGStab on the GPU, ``--precision df64`` default; ``fp64``:
+the reference algorithm in FP64; ``mixed``: FP32 inner solves in FP64
+refinement), 64 seeds resident in HBM.  ``--workload ensemble``: the
+48-member ensemble in one persistent launch per round.
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--workload ...]
 
 Prints one JSON line (rank 0).  Under torchrun (N > 1) each rank solves its
-own seeds (independent replicas, weak scaling) and the time is the max over
+own system (independent replicas, weak scaling) and the time is the max over
 ranks.  ``--impl reference`` times the reference algorithm on the host cores
-(the CPU restatement of the reference path: NumPy stencil + SciPy BiCGStab,
-FP64) on the same configuration.
+(the CPU restatement of the reference path: NumPy stencil + plain FP64
+BiCGStab) on the same configuration.
 """
 import argparse
 import json
@@ -54,7 +60,7 @@ def _args():
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--workload", default="solve2d", choices=["solve2d", "ensemble", "learned3d"])
+    ap.add_argument("--workload", default="learned3d", choices=["solve2d", "ensemble", "learned3d"])
     ap.add_argument("--nz", type=int, default=257)
     ap.add_argument("--train-steps", type=int, default=1000)
     ap.add_argument("--skip", type=float, default=0.7)
@@ -546,23 +552,26 @@ def cpu_sample_3d(op, seconds):
 def run_learned3d(args):
     import torch
     import warnings
-    from pybella_gb300 import learned, workloads, _lib
+    from pybella_gb300 import learned, workloads, _lib, replicas
     from pybella_gb300.linalg import NodalHelmholtz3D
     from pybella_gb300.spectral import BackgroundSolve
     world, rank, local = _dist()
-    if world > 1 and rank != 0:
-        return
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
     shape = (args.nx, args.ny, args.nz)
-    # training (not timed): pairs from the background-preconditioned solver's own
-    # iterates on seeds 1,2,3,5, Adam on the library's kernels
+    # training (not timed; every rank trains the same network from the same seeds):
+    # pairs from the background-preconditioned solver's own iterates on seeds
+    # 1, 2, 3, 5, Adam on the library's kernels
     t0 = time.perf_counter()
     params, losses = learned.train_preconditioner(shape=shape, background=True, skip=args.skip,
                                                   steps=args.train_steps, npairs=4000)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
-    w = workloads.stratified_3d(7, *shape)
+    w = workloads.stratified_3d(7 + 1000 * rank, *shape)          # each replica its own system
     ws = _lib.Workspace(local)
     A = learned.operator_3d(w, ws=ws)
     net = learned.CNN(shape, block=2, mode="linear", skip=args.skip)
@@ -585,16 +594,15 @@ def run_learned3d(args):
         bg.close()
         return st
 
-    res = {}
-    clocks = ClockSampler(local)
-    for name in ("background", "learned", "plain"):
-        # the plain solve takes tens of seconds: one warm-up and one timed step
-        nw, ns = (1, 1) if name == "plain" else (args.warmup, args.steps)
+    def timed(name, nw, ns, sample_clocks=False):
         for _ in range(nw):
             step(name)
-        if name == "learned":
+        clocks = ClockSampler(local) if sample_clocks else None
+        if clocks:
             clocks.start()
-            l0, n0, b0 = ws.launches, net.launches, bg_launches[0]
+        l0, n0, b0 = ws.launches, net.launches, bg_launches[0]
+        if dist is not None:
+            dist.barrier()
         tot, sts = 0.0, []
         for _ in range(ns):
             flush.fill_(1.0)
@@ -605,18 +613,29 @@ def run_learned3d(args):
             e1.record()
             torch.cuda.synchronize()
             tot += e0.elapsed_time(e1)
-        if name == "learned":
-            launches = (ws.launches - l0) + (net.launches - n0) + (bg_launches[0] - b0)
-            clk = clocks.stop()
-        res[name] = {"ms": tot / ns, "stats": sts}
-    L, B, P = res["learned"], res["background"], res["plain"]
+        if dist is not None:
+            dist.barrier()
+        launches = (ws.launches - l0) + (net.launches - n0) + (bg_launches[0] - b0)
+        clk = clocks.stop() if clocks else None
+        return {"ms": tot / ns, "stats": sts, "launches": launches, "clocks": clk}
+
+    # the headline: learned-preconditioned solves, every rank, max over ranks
+    L = timed("learned", args.warmup, args.steps, sample_clocks=True)
+    ms_max = replicas.max_over_ranks(L["ms"] * args.steps, device=dev)
+    value = replicas.aggregate_rate(args.steps, world, ms_max / 1000.0)
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    B = timed("background", args.warmup, args.steps)
+    P = timed("plain", 1, 1)                         # one plain solve takes tens of seconds
     # end to end through the public API: operator planes and b from pinned host
     # memory, device operator and background set-up, solve, x back to the host
     host = {k: w[k].detach().cpu().pin_memory() for k in ("hplusx", "hplusy", "hplusz", "diag_inv", "b")}
     h2d = sum(t.numel() * t.element_size() for t in host.values())
     e2e_ms = []
     ws_e2e = _lib.Workspace(local)
-    for i in range(args.warmup + args.steps):
+    for i in range(0 if args.no_e2e else args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         Ah = NodalHelmholtz3D(host["hplusx"], host["hplusy"], host["hplusz"], None, host["diag_inv"], *shape,
@@ -657,7 +676,7 @@ def run_learned3d(args):
     hbm, tpeak, pkind = _peaks()
     ach = cnn_flops / (cnn_ms / 1000.0) / 1e12
     cpu = None
-    if not args.no_cpu_baseline:
+    if world == 1 and not args.no_cpu_baseline:
         from oracle import cases
         wc = cases.stratified_3d(7, *shape)
         per_it, k = cpu_sample_3d(wc["op"], args.cpu_seconds)
@@ -670,41 +689,85 @@ def run_learned3d(args):
                        "outer": R["stats"][-1]["outer"], "relres": R["stats"][-1]["relres"],
                        "fallback": R["stats"][-1]["fallback"], "status": R["stats"][-1]["status"]}
     line = {
-        "metric": METRIC, "value": 1000.0 / L["ms"], "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": L["ms"], "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16 network + f32 inner / f64 refinement", "data": "synthetic",
         "config": {"workload": LEARNED3D % "x".join(map(str, shape)),
                    "network": "6 layers 3x3x3, 32 channels, 2x2x2-blocked grid, linear, identity path %.2f" % args.skip,
                    "train_steps": args.train_steps, "train_s": train_s, "final_loss": losses[-1][1],
+                   "parallelism": "replicas" if world > 1 else "single GPU",
                    "plain_steps": "1 warm-up + 1 timed (one plain solve takes tens of seconds)",
                    "l2": "256 MB L2 flush before every step; operator planes %.0f MB" % (A.n * 8 * 6 / 1e6)},
         "plain": stats(P), "background": stats(B), "learned": stats(L),
         "learned_over_plain": P["ms"] / L["ms"], "background_over_plain": P["ms"] / B["ms"],
         "network_gain_over_background": B["ms"] / L["ms"],
-        "e2e": {"value": 1000.0 / statistics.median(e2e_ms), "unit": "solves/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": A.n * 8},
-        "gpu_launches": launches,
+        "e2e": ({"value": 1000.0 / statistics.median(e2e_ms), "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                 "d2h_bytes_per_step": A.n * 8} if e2e_ms else None),
+        "gpu_launches": L["launches"],
         "roofline": {"bound": "tensor", "achieved": ach, "peak": tpeak, "unit": "TFLOP/s", "frac": ach / tpeak,
                      "traffic": None, "kernel": "k_conv3d_tc x5 + k_conv3d (one network application)",
                      "peak_source": pkind + " bf16 sustained", "flops_per_launch": cnn_flops,
                      "ms_per_application": cnn_ms, "applications_per_solve": napp,
                      "background_apply_ms": bg_ms},
-        "clocks": clk,
+        "clocks": L["clocks"],
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+# iterations of plain FP64 BiCGStab on the seed-7 257x129x257 system (the GPU
+# FP64/double-float solve of the same system, same algorithm and tolerance);
+# the CPU arm times iterations on the full grid and multiplies by this count
+PLAIN3D_ITERS = 40512
+
+
+def run_reference_3d(args):
+    """``--impl reference`` for the 3D workload: plain FP64 BiCGStab with the
+    NumPy restatement of lap3D on the host cores (bounded iteration samples)."""
+    world, rank, local = _dist()
+    if world > 1 and rank != 0:
+        return
+    from oracle import cases
+    shape = (args.nx, args.ny, args.nz)
+    wc = cases.stratified_3d(7, *shape)
+    iters = PLAIN3D_ITERS * (((args.nx - 1) / 256.0) ** 2 if shape != (257, 129, 257) else 1.0)
+    vals = []
+    t_all0 = time.perf_counter()
+    for s_ in range(args.warmup + args.steps):
+        per_it, k = cpu_sample_3d(wc["op"], max(2.0, args.cpu_seconds / 4))
+        if s_ >= args.warmup:
+            vals.append(1.0 / (per_it * iters))
+    value = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": LEARNED3D % "x".join(map(str, shape)), "arm": "plain BiCGStab on the host",
+                       "l2": "inputs resident on host"},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": 1, "kind": "port",
+                             "sample": "NumPy lap3D restatement + plain FP64 BiCGStab iterations on the full grid "
+                                       "(bounded samples of ~%.0f s), times %d iterations per solve (the count of "
+                                       "the same algorithm on this system)" % (max(2.0, args.cpu_seconds / 4),
+                                                                              iters)},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": time.perf_counter() - t_all0}
     print(json.dumps(line), flush=True)
 
 
 def main():
     args = _args()
+    if args.workload == "learned3d" and args.nx == NX and args.ny == NY:
+        args.nx, args.ny = 257, 129
     if args.impl == "reference":
-        run_reference(args)
+        if args.workload == "learned3d":
+            run_reference_3d(args)
+        else:
+            run_reference(args)
     elif args.workload == "ensemble":
         run_ensemble(args)
     elif args.workload == "learned3d":
-        if args.nx == NX and args.ny == NY:
-            args.nx, args.ny = 257, 129
         run_learned3d(args)
     else:
         run_gpu(args)
