@@ -966,13 +966,14 @@ k_flex_p(long long n, const float *r, float *p, const float *v, KState *ks, doub
     if (ks->done) return;
     const bool first = ks->iter == 0;
     const float beta = (float)ks->beta, omega = (float)ks->omega;
-    double a[1] = {0.0};
+    DF d0;
+    d0.zero();
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
         const float pg = first ? r[g] : fmaf(beta, fmaf(-omega, v[g], p[g]), r[g]);
         p[g] = pg;
-        a[0] += (double)pg * (double)pg;
+        d0.add_prod(pg, pg);
     }
-    double tot[1];
+    double a[1] = {d0.value()}, tot[1];
     if (!grid_sum<1>(a, partials, counter, tot)) return;
     if (threadIdx.x == 0) ks->dot_aux = tot[0];
 }
@@ -980,10 +981,11 @@ k_flex_p(long long n, const float *r, float *p, const float *v, KState *ks, doub
 __global__ void __launch_bounds__(VEC_BLOCK)
 k_flex_alpha(long long n, const float *rh, const float *v, KState *ks, double *partials, unsigned *counter) {
     if (ks->done) return;
-    double a[1] = {0.0};
+    DF d0;
+    d0.zero();
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x)
-        a[0] += (double)rh[g] * (double)v[g];
-    double tot[1];
+        d0.add_prod(rh[g], v[g]);
+    double a[1] = {d0.value()}, tot[1];
     if (!grid_sum<1>(a, partials, counter, tot)) return;
     if (threadIdx.x == 0) finalize_pdir(ks, tot[0]);
 }
@@ -993,13 +995,14 @@ __global__ void __launch_bounds__(VEC_BLOCK)
 k_flex_s(long long n, const float *r, const float *v, float *s, KState *ks, double *partials, unsigned *counter) {
     if (ks->done) return;
     const float alpha = (float)ks->alpha;
-    double a[1] = {0.0};
+    DF d0;
+    d0.zero();
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
         const float sg = fmaf(-alpha, v[g], r[g]);
         s[g] = sg;
-        a[0] += (double)sg * (double)sg;
+        d0.add_prod(sg, sg);
     }
-    double tot[1];
+    double a[1] = {d0.value()}, tot[1];
     if (!grid_sum<1>(a, partials, counter, tot)) return;
     if (threadIdx.x == 0) { ks->ss = tot[0]; ks->dot_aux = tot[0]; }
 }
@@ -1007,13 +1010,15 @@ k_flex_s(long long n, const float *r, const float *v, float *s, KState *ks, doub
 __global__ void __launch_bounds__(VEC_BLOCK)
 k_flex_omega(long long n, const float *t, const float *s, KState *ks, double *partials, unsigned *counter) {
     if (ks->done) return;
-    double a[2] = {0.0, 0.0};
+    DF d0, d1;
+    d0.zero();
+    d1.zero();
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
-        const double tg = t[g];
-        a[0] += tg * (double)s[g];
-        a[1] += tg * tg;
+        const float tg = t[g];
+        d0.add_prod(tg, s[g]);
+        d1.add_prod(tg, tg);
     }
-    double tot[2];
+    double a[2] = {d0.value(), d1.value()}, tot[2];
     if (!grid_sum<2>(a, partials, counter, tot)) return;
     if (threadIdx.x == 0) finalize_sdir(ks, tot[0], tot[1], ks->ss);
 }
@@ -1024,15 +1029,17 @@ k_flex_update(long long n, float *x, const float *ph, const float *sh, float *r,
               const float *rh, KState *ks, double *partials, unsigned *counter) {
     if (ks->done) return;
     const float alpha = (float)ks->alpha, omega = ks->early ? 0.f : (float)ks->omega;
-    double a[2] = {0.0, 0.0};
+    DF d0, d1;
+    d0.zero();
+    d1.zero();
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
         x[g] = fmaf(omega, sh[g], fmaf(alpha, ph[g], x[g]));
         const float rg = fmaf(-omega, t[g], s[g]);
         r[g] = rg;
-        a[0] += (double)rh[g] * (double)rg;
-        a[1] += (double)rg * (double)rg;
+        d0.add_prod(rh[g], rg);
+        d1.add_prod(rg, rg);
     }
-    double tot[2];
+    double a[2] = {d0.value(), d1.value()}, tot[2];
     if (!grid_sum<2>(a, partials, counter, tot)) return;
     if (threadIdx.x == 0) finalize_update(ks, tot[0], tot[1]);
 }
@@ -1042,13 +1049,14 @@ k_flex_update(long long n, float *x, const float *ph, const float *sh, float *r,
 __global__ void __launch_bounds__(VEC_BLOCK)
 k_flex_corr_in(long long n, const float *in, float *Ay, KState *ks, double *partials, unsigned *counter) {
     if (ks->done) return;
-    double a[1] = {0.0};
+    DF d0;
+    d0.zero();
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
         const float d = in[g] - Ay[g];
         Ay[g] = d;
-        a[0] += (double)d * (double)d;
+        d0.add_prod(d, d);
     }
-    double tot[1];
+    double a[1] = {d0.value()}, tot[1];
     if (!grid_sum<1>(a, partials, counter, tot)) return;
     if (threadIdx.x == 0) ks->pss = tot[0];
 }
@@ -1176,20 +1184,22 @@ __global__ void __launch_bounds__(VEC_BLOCK)
 k_fg_mdot(long long n, const float *V, long long ld, int nv, const float *w, double *part) {
     const int i0 = blockIdx.y * FG_GROUP;
     const int cnt = nv - i0 < FG_GROUP ? nv - i0 : FG_GROUP;
-    double acc[FG_GROUP];
+    // double-float accumulation on the FP32 pipe (GB300's FP64 pipe runs at 1/64
+    // of the FP32 rate and would bound this kernel)
+    DF acc[FG_GROUP];
 #pragma unroll
-    for (int q = 0; q < FG_GROUP; ++q) acc[q] = 0.0;
+    for (int q = 0; q < FG_GROUP; ++q) acc[q].zero();
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
-        const double wg = w[g];
+        const float wg = w[g];
 #pragma unroll
         for (int q = 0; q < FG_GROUP; ++q)
-            if (q < cnt) acc[q] += (double)V[(i0 + q) * ld + g] * wg;
+            if (q < cnt) acc[q].add_prod(V[(i0 + q) * ld + g], wg);
     }
     __shared__ double red[FG_GROUP][VEC_BLOCK / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < FG_GROUP; ++q) {
-        const double v = warp_sum(acc[q]);
+        const double v = warp_sum(acc[q].value());
         if (lane == 0) red[q][wid] = v;
     }
     __syncthreads();
@@ -1215,16 +1225,17 @@ k_fg_update(long long n, const float *V, long long ld, int nv, const double *h, 
     __shared__ float hs[FG_MAXV];
     if ((int)threadIdx.x < nv) hs[threadIdx.x] = (float)h[threadIdx.x];
     __syncthreads();
-    double acc = 0.0;
+    DF acc;
+    acc.zero();
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
         float wg = w[g];
         for (int i = 0; i < nv; ++i) wg = fmaf(-hs[i], V[i * ld + g], wg);
         w[g] = wg;
-        acc += (double)wg * (double)wg;
+        if (norm) acc.add_prod(wg, wg);
     }
     if (!norm) return;
     __shared__ double red[VEC_BLOCK / 32];
-    const double v = warp_sum(acc);
+    const double v = warp_sum(acc.value());
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
     __syncthreads();
     if (threadIdx.x == 0) {

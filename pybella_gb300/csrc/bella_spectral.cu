@@ -43,6 +43,7 @@ struct bella_spectral3d {
     double *mux, *muz;     // eigenvalues of D^T D per mode
     double *cx, *cy, *cz;  // y-cell means (ny - 1 interior cells)
     double *hcm;           // y-node means of hcenter (ny)
+    double *mpart;         // partial sums of the means (ny * SP_CHUNKS * 4)
     float *dscale;         // 1 / diag_inv
     float *w1, *w2;        // transform work arrays (n floats each)
     float *c1, *c2;        // work arrays of a preconditioner composed with the network
@@ -332,25 +333,30 @@ static void sp_fft(long long nlines, int L, const float *in, long long in_lmul, 
 
 // y-cell means of the three cell coefficients over the interior x and z cells
 // (cells 1..n-1: one period on a periodic axis, the cells between walls on a
-// wall axis) and y-node means of hcenter; one CTA per y index, fixed-order sums.
+// wall axis) and y-node means of hcenter.  Block (j, c) sums chunk c of y index
+// j into part[(j * SP_CHUNKS + c) * 4 + v]; k_sp_means_final adds the chunks in
+// order (deterministic).
+constexpr int SP_CHUNKS = 16;
+
 __global__ void __launch_bounds__(256)
 k_sp_means(int nx, int ny, int nz, const double *hx, const double *hy, const double *hz, const double *hc,
-           double *cx, double *cy, double *cz, double *hcm) {
-    const int j = blockIdx.x;                 // 0..ny-1
+           double *part) {
+    const int j = blockIdx.x, c = blockIdx.y;
     __shared__ double red[4][256];
     double a[4] = {0.0, 0.0, 0.0, 0.0};
     const long long cyz = (long long)(ny + 1) * (nz + 1);
+    const long long step = (long long)blockDim.x * SP_CHUNKS;
     if (j >= 1) {                             // y-cell j (between nodes j-1 and j)
-        for (long long q = threadIdx.x; q < (long long)(nx - 1) * (nz - 1); q += blockDim.x) {
+        for (long long q = (long long)c * blockDim.x + threadIdx.x; q < (long long)(nx - 1) * (nz - 1); q += step) {
             const long long i = 1 + q / (nz - 1), k = 1 + q % (nz - 1);
-            const long long c = i * cyz + (long long)j * (nz + 1) + k;
-            a[0] += hx[c];
-            a[1] += hy[c];
-            a[2] += hz[c];
+            const long long cc = i * cyz + (long long)j * (nz + 1) + k;
+            a[0] += hx[cc];
+            a[1] += hy[cc];
+            a[2] += hz[cc];
         }
     }
     if (hc) {
-        for (long long q = threadIdx.x; q < (long long)nx * nz; q += blockDim.x) {
+        for (long long q = (long long)c * blockDim.x + threadIdx.x; q < (long long)nx * nz; q += step) {
             const long long i = q / nz, k = q % nz;
             a[3] += hc[(i * ny + j) * nz + k];
         }
@@ -364,20 +370,28 @@ k_sp_means(int nx, int ny, int nz, const double *hx, const double *hy, const dou
             for (int v = 0; v < 4; ++v) red[v][threadIdx.x] += red[v][threadIdx.x + w];
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        if (j >= 1) {
-            const double inv = 1.0 / ((double)(nx - 1) * (nz - 1));
-            cx[j - 1] = red[0][0] * inv;
-            cy[j - 1] = red[1][0] * inv;
-            cz[j - 1] = red[2][0] * inv;
-        }
-        hcm[j] = hc ? red[3][0] / ((double)nx * nz) : 0.0;
+    if (threadIdx.x < 4) part[((long long)j * SP_CHUNKS + c) * 4 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void k_sp_means_final(int nx, int ny, int nz, int has_hc, const double *part, double *cx, double *cy,
+                                 double *cz, double *hcm) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= ny) return;
+    double a[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int c = 0; c < SP_CHUNKS; ++c)
+        for (int v = 0; v < 4; ++v) a[v] += part[((long long)j * SP_CHUNKS + c) * 4 + v];
+    if (j >= 1) {
+        const double inv = 1.0 / ((double)(nx - 1) * (nz - 1));
+        cx[j - 1] = a[0] * inv;
+        cy[j - 1] = a[1] * inv;
+        cz[j - 1] = a[2] * inv;
     }
+    hcm[j] = has_hc ? a[3] / ((double)nx * nz) : 0.0;
 }
 
 __global__ void k_sp_recip(long long n, const double *dinv, float *out) {
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x)
-        out[g] = (float)(1.0 / dinv[g]);
+        out[g] = 1.f / (float)dinv[g];
 }
 
 // Line operator of mode (kx, kz): alpha M^T Cx M + beta D^T Cy D + gamma M^T Cz M
@@ -633,7 +647,7 @@ int bella_spectral3d_destroy(bella_spectral3d *sp) {
     if (!sp) return BELLA_OK;
     cudaSetDevice(sp->device);
     void *ptrs[] = {sp->txf, sp->txi, sp->tzfT, sp->tziT, sp->mux, sp->muz, sp->cx, sp->cy, sp->cz,
-                    sp->hcm, sp->dscale, sp->w1, sp->w2, sp->c1, sp->c2, sp->la, sp->lc, sp->li,
+                    sp->hcm, sp->mpart, sp->dscale, sp->w1, sp->w2, sp->c1, sp->c2, sp->la, sp->lc, sp->li,
                     sp->twx, sp->twz};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -699,6 +713,7 @@ int bella_spectral3d_create(bella_spectral3d **out, const bella_op3d *op, int de
               cudaMalloc(&sp->cy, ny * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&sp->cz, ny * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&sp->hcm, ny * sizeof(double)) == cudaSuccess &&
+              cudaMalloc(&sp->mpart, (size_t)ny * SP_CHUNKS * 4 * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&sp->dscale, sp->n * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&sp->w1, sp->n * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&sp->w2, sp->n * sizeof(float)) == cudaSuccess &&
@@ -713,8 +728,10 @@ int bella_spectral3d_create(bella_spectral3d **out, const bella_op3d *op, int de
     }
     cudaMemcpyAsync(sp->mux, mux.data(), Kx * sizeof(double), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(sp->muz, muz.data(), Kz * sizeof(double), cudaMemcpyHostToDevice, s);
-    k_sp_means<<<ny, 256, 0, s>>>(nx, ny, nz, op->hplusx, op->hplusy, op->hplusz, op->hcenter, sp->cx, sp->cy,
-                                  sp->cz, sp->hcm);
+    k_sp_means<<<dim3(ny, SP_CHUNKS), 256, 0, s>>>(nx, ny, nz, op->hplusx, op->hplusy, op->hplusz, op->hcenter,
+                                                   sp->mpart);
+    k_sp_means_final<<<(ny + 127) / 128, 128, 0, s>>>(nx, ny, nz, op->hcenter ? 1 : 0, sp->mpart, sp->cx, sp->cy,
+                                                      sp->cz, sp->hcm);
     k_sp_recip<<<vec_grid(sp->n), VEC_BLOCK, 0, s>>>(sp->n, op->diag_inv, sp->dscale);
     std::vector<double> hcm(ny);
     cudaMemcpyAsync(hcm.data(), sp->hcm, ny * sizeof(double), cudaMemcpyDeviceToHost, s);
