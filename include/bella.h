@@ -320,7 +320,7 @@ long long bella_spectral3d_launches(const bella_spectral3d *sp);
  * unless both are given. */
 int       bella_fbicgstab_pc(bella_ws *ws, bella_spectral3d *sp, bella_cnn *net, int compose, const double *b,
                              double *x, const bella_solve_opts *opts, bella_solve_stats *stats, void *stream);
-/* As bella_fbicgstab_pc with flexible GMRES (Saad's FGMRES, restart 1..30) as the
+/* As bella_fbicgstab_pc with flexible GMRES (Saad's FGMRES, restart 1..64) as the
  * inner solver: one cycle of at most restart iterations per refinement step, FP32
  * Arnoldi vectors with FP64 inner products and Gram-Schmidt reorthogonalisation.
  * FGMRES keeps every preconditioned vector, so it stays exact for a preconditioner

@@ -1172,7 +1172,7 @@ static int run_flex(bella_ws *ws, const Precond &pc, const bella_solve_opts *o, 
 // in FP64, classical Gram-Schmidt with one reorthogonalisation pass; the small
 // Hessenberg least-squares problem (Givens rotations) on the host.
 // ---------------------------------------------------------------------------
-constexpr int FG_MAXM = 30;
+constexpr int FG_MAXM = 64;
 constexpr int FG_MAXV = FG_MAXM + 1;
 
 constexpr int FG_XBLK = NSM * 2;    // blocks per group of inner products
@@ -1316,10 +1316,10 @@ static int fgmres_cycle(bella_ws *ws, const Precond &pc, int m, double rel, cuda
         const int nv = j + 1;
         const unsigned ng = (unsigned)((nv + FG_GROUP - 1) / FG_GROUP);
         k_fg_mdot<<<dim3(FG_XBLK, ng), VEC_BLOCK, 0, s>>>(n, V, n, nv, w, ws->fg_part);
-        k_fg_reduce<<<1, 64, 0, s>>>(FG_XBLK, ws->fg_part, nv, h1);
+        k_fg_reduce<<<1, 128, 0, s>>>(FG_XBLK, ws->fg_part, nv, h1);
         k_fg_update<<<gv, VEC_BLOCK, 0, s>>>(n, V, n, nv, h1, w, 0, ws->fg_part);
         k_fg_mdot<<<dim3(FG_XBLK, ng), VEC_BLOCK, 0, s>>>(n, V, n, nv, w, ws->fg_part);
-        k_fg_reduce<<<1, 64, 0, s>>>(FG_XBLK, ws->fg_part, nv, h2);
+        k_fg_reduce<<<1, 128, 0, s>>>(FG_XBLK, ws->fg_part, nv, h2);
         k_fg_update<<<gv, VEC_BLOCK, 0, s>>>(n, V, n, nv, h2, w, 1, ws->fg_part);
         k_fg_reduce<<<1, 64, 0, s>>>(gv, ws->fg_part, 1, nrm);
         k_fg_scale<<<gv, VEC_BLOCK, 0, s>>>(n, w, nrm, w);
@@ -1508,7 +1508,7 @@ extern "C" int bella_fgmres_pc(bella_ws *ws, bella_spectral3d *sp, bella_cnn *ne
                                void *stream) {
     if (!ws || (!sp && !net) || !b || !x) return set_err(BELLA_EINVAL, "bella_fgmres_pc: null argument");
     if (compose < 0 || compose > 2) return set_err(BELLA_EINVAL, "bella_fgmres_pc: compose must be 0, 1 or 2");
-    if (restart < 1 || restart > bella::FG_MAXM) return set_err(BELLA_EINVAL, "bella_fgmres_pc: restart must be 1..30");
+    if (restart < 1 || restart > bella::FG_MAXM) return set_err(BELLA_EINVAL, "bella_fgmres_pc: restart must be 1..64");
     if (ws->ndim != 3) return set_err(ws->ndim == 0 ? BELLA_ENOOP : BELLA_EINVAL,
                                       "bella_fgmres_pc: needs a 3D operator (bella_op3d_set)");
     if (sp && bella::spectral_size(sp) != ws->n)
