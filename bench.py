@@ -63,7 +63,7 @@ def _args():
     ap.add_argument("--workload", default="learned3d", choices=["solve2d", "ensemble", "learned3d"])
     ap.add_argument("--nz", type=int, default=257)
     ap.add_argument("--train-steps", type=int, default=1000)
-    ap.add_argument("--skip", type=float, default=0.7)
+    ap.add_argument("--skip", type=float, default=0.9)
     return ap.parse_args()
 
 
