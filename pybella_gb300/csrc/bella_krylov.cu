@@ -1175,7 +1175,7 @@ static int run_flex(bella_ws *ws, const Precond &pc, const bella_solve_opts *o, 
 constexpr int FG_MAXM = 64;
 constexpr int FG_MAXV = FG_MAXM + 1;
 
-constexpr int FG_XBLK = NSM * 2;    // blocks per group of inner products
+constexpr int FG_XBLK = NSM * 8;    // blocks per group of inner products (enough warps to cover memory latency)
 constexpr int FG_GROUP = 8;         // inner products per block
 
 // block (bx, gy): partial sums of <V_i, w> for the FG_GROUP vectors i of group gy
