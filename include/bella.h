@@ -304,6 +304,14 @@ int       bella_fbicgstab(bella_ws *ws, bella_cnn *net, const double *b, double 
  * system; device FP32 arrays of nx*ny*nz. */
 typedef struct bella_spectral3d bella_spectral3d;
 int       bella_spectral3d_create(bella_spectral3d **sp, const bella_op3d *op, int device, void *stream);
+/* The same background solve for the 2D 9-point operator (the reference's
+ * lap2D_gather_new, laplacian.py:546-746): cxx*hplusx and cyy*hplusy averaged
+ * over x per y-cell, hcenter per node row; Hartley / DCT-I along x, tridiagonal
+ * along y; the Coriolis cross terms (cxy, cyx) are not part of the background.
+ * op as for bella_op2d_set (y must be a wall axis); the object is used with
+ * bella_spectral3d_apply / _destroy / bella_fbicgstab_pc / bella_fgmres_pc (no
+ * network in 2D). */
+int       bella_spectral2d_create(bella_spectral3d **sp, const bella_op2d *op, int device, void *stream);
 int       bella_spectral3d_destroy(bella_spectral3d *sp);
 int       bella_spectral3d_apply(bella_spectral3d *sp, const float *in, float *out, void *stream);
 long long bella_spectral3d_launches(const bella_spectral3d *sp);
@@ -316,8 +324,8 @@ long long bella_spectral3d_launches(const bella_spectral3d *sp);
  *     compose 0: y = A_bg^+ r;  y += net(r - A y)
  *     compose 1: y = net(r);    y += A_bg^+ (r - A y)
  *     compose 2: y = A_bg^+ r;  y += net(r - A y);  y += A_bg^+ (r - A y)
- * sp must have been created for the operator set on ws; compose is ignored
- * unless both are given. */
+ * sp must have been created for the operator set on ws (2D or 3D; the network
+ * needs a 3D operator); compose is ignored unless both are given. */
 int       bella_fbicgstab_pc(bella_ws *ws, bella_spectral3d *sp, bella_cnn *net, int compose, const double *b,
                              double *x, const bella_solve_opts *opts, bella_solve_stats *stats, void *stream);
 /* As bella_fbicgstab_pc with flexible GMRES (Saad's FGMRES, restart 1..64) as the

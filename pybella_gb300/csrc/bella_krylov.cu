@@ -1369,8 +1369,9 @@ static int fgmres_cycle(bella_ws *ws, const Precond &pc, int m, double rel, cuda
 static int fbicgstab_impl(bella_ws *ws, const bella::Precond &pc, const double *b, double *x,
                           const bella_solve_opts *opts, bella_solve_stats *stats, void *stream,
                           int restart = 0) {
-    if (ws->ndim != 3) return set_err(ws->ndim == 0 ? BELLA_ENOOP : BELLA_EINVAL,
-                                      "bella_fbicgstab: needs a 3D operator (bella_op3d_set)");
+    if (ws->ndim == 0) return set_err(BELLA_ENOOP, "bella_fbicgstab: no operator set");
+    if (pc.net && ws->ndim != 3)
+        return set_err(BELLA_EINVAL, "bella_fbicgstab: the network needs a 3D operator (bella_op3d_set)");
     bella_solve_opts o;
     if (opts) o = *opts; else bella_solve_opts_default(&o);
     if (!(o.tol >= 0.0) || o.maxiter < 0) return set_err(BELLA_EINVAL, "bella_fbicgstab: bad tol/maxiter");
@@ -1498,7 +1499,7 @@ extern "C" int bella_fbicgstab_pc(bella_ws *ws, bella_spectral3d *sp, bella_cnn 
                                   double *x, const bella_solve_opts *opts, bella_solve_stats *stats, void *stream) {
     if (!ws || (!sp && !net) || !b || !x) return set_err(BELLA_EINVAL, "bella_fbicgstab_pc: null argument");
     if (compose < 0 || compose > 2) return set_err(BELLA_EINVAL, "bella_fbicgstab_pc: compose must be 0, 1 or 2");
-    if (sp && (ws->ndim != 3 || bella::spectral_size(sp) != ws->n))
+    if (sp && bella::spectral_size(sp) != ws->n)
         return set_err(BELLA_EINVAL, "bella_fbicgstab_pc: background solve made for another grid");
     return fbicgstab_impl(ws, bella::Precond{net, sp, compose}, b, x, opts, stats, stream);
 }
@@ -1509,8 +1510,7 @@ extern "C" int bella_fgmres_pc(bella_ws *ws, bella_spectral3d *sp, bella_cnn *ne
     if (!ws || (!sp && !net) || !b || !x) return set_err(BELLA_EINVAL, "bella_fgmres_pc: null argument");
     if (compose < 0 || compose > 2) return set_err(BELLA_EINVAL, "bella_fgmres_pc: compose must be 0, 1 or 2");
     if (restart < 1 || restart > bella::FG_MAXM) return set_err(BELLA_EINVAL, "bella_fgmres_pc: restart must be 1..64");
-    if (ws->ndim != 3) return set_err(ws->ndim == 0 ? BELLA_ENOOP : BELLA_EINVAL,
-                                      "bella_fgmres_pc: needs a 3D operator (bella_op3d_set)");
+    if (ws->ndim == 0) return set_err(BELLA_ENOOP, "bella_fgmres_pc: no operator set");
     if (sp && bella::spectral_size(sp) != ws->n)
         return set_err(BELLA_EINVAL, "bella_fgmres_pc: background solve made for another grid");
     BELLA_CUDA(cudaSetDevice(ws->device));

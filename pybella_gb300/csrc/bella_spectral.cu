@@ -50,6 +50,7 @@ struct bella_spectral3d {
     float *la, *lc, *li;   // Thomas factors of every mode line, [ny][Kx*Kz] each
     double idx2, idy2, idz2;
     int fft_x, fft_z;      // 1: this axis transforms by FFT (power-of-two length), 0: by GEMM
+    int twod;              // the 2D 9-point operator: one transformed axis (x, in the z role), no x pass
     int Lx, Lz, px, pz;    // FFT lengths and their log2
     float2 *twx, *twz;     // twiddles exp(-2 pi i t / L), t < L/2
     long long launches;
@@ -156,10 +157,11 @@ static void sgemm(int M, int N, int K, const float *A, long long lda, const floa
     else k_sgemm<false><<<grid, SG_THREADS, 0, s>>>(M, N, K, A, lda, nullptr, B, ldb, C, ldc);
 }
 
-// ---- FFT path of the transforms (power-of-two lengths 16..1024) ---------------
-// Every line of the axis is transformed by a two-pass FFT, L = 16 * R2:
-//   X[k1 + 16 k2] = sum_n2 W_R2^(n2 k2) W_L^(n2 k1) sum_n1 W_16^(n1 k1) x[R2 n1 + n2]
-// pass A: one thread per (line, n2) does the 16-point DFT in registers and the
+// ---- FFT path of the transforms (power-of-two lengths 16..2048) ---------------
+// Every line of the axis is transformed by a two-pass FFT, L = R1 * R2 (R1 = 16,
+// or 32 for L = 2048):
+//   X[k1 + R1 k2] = sum_n2 W_R2^(n2 k2) W_L^(n2 k1) sum_n1 W_R1^(n1 k1) x[R2 n1 + n2]
+// pass A: one thread per (line, n2) does the R1-point DFT in registers and the
 // twiddle W_L^(n2 k1), writing through shared memory; pass B: one thread per
 // (line, k1) does the R2-point DFT in registers and writes the outputs.
 //   Hartley (periodic axis, N = n - 1 = L):  H_k = Re F_k - Im F_k of the FFT of
@@ -229,21 +231,25 @@ __device__ __forceinline__ void reg_fft(float2 (&v)[R]) {
 template <>
 __device__ __forceinline__ void reg_fft<1>(float2 (&)[1]) {}
 
-template <int R2>
+template <int R1, int R2>
 struct FftShape {
-    static constexpr int L = FFT_R1 * R2;
-    static constexpr int LPC = (256 / R2) < 128 ? (256 / R2) : 128;   // lines per CTA
-    static constexpr int SMEM = LPC * FFT_R1 * (R2 + 1) > FFT_R1 * R2 * (LPC + 1) ? LPC * FFT_R1 * (R2 + 1)
-                                                                                  : FFT_R1 * R2 * (LPC + 1);
+    static constexpr int L = R1 * R2;
+    // lines per CTA: pass A runs R2 threads per line; at most 6144 complex values
+    // of shared memory (48 KB of static shared memory with the padding)
+    static constexpr int LPC_A = (256 / R2) < 128 ? (256 / R2) : 128;
+    static constexpr int LPC_S = 6144 / (R1 * (R2 + 1));
+    static constexpr int LPC = LPC_A < LPC_S ? LPC_A : LPC_S;
+    static constexpr int SMEM = LPC * R1 * (R2 + 1) > R1 * R2 * (LPC + 1) ? LPC * R1 * (R2 + 1)
+                                                                          : R1 * R2 * (LPC + 1);
 };
 
-template <int KIND, bool FWD, int R2>   // KIND 0: Hartley, 1: DCT-I
+template <int KIND, bool FWD, int R1, int R2>   // KIND 0: Hartley, 1: DCT-I
 __global__ void __launch_bounds__(256)
 k_sp_fft(long long nlines, const float *__restrict__ in, long long in_lmul, long long in_ts,
          const float *__restrict__ scale, float *__restrict__ out, long long out_lmul, long long out_ts,
          const float2 *__restrict__ twL) {
-    constexpr int R1 = FFT_R1, L = FftShape<R2>::L, M = L / 2, LPC = FftShape<R2>::LPC;
-    __shared__ float2 S[FftShape<R2>::SMEM];
+    constexpr int L = FftShape<R1, R2>::L, M = L / 2, LPC = FftShape<R1, R2>::LPC;
+    __shared__ float2 S[FftShape<R1, R2>::SMEM];
     const long long l0 = (long long)blockIdx.x * LPC;
     const int nl = (int)(nlines - l0 < LPC ? nlines - l0 : LPC);
     const bool ic = in_ts == 1, oc = out_ts == 1;
@@ -312,20 +318,22 @@ k_sp_fft(long long nlines, const float *__restrict__ in, long long in_lmul, long
 template <int KIND, bool FWD>
 static void sp_fft(long long nlines, int L, const float *in, long long in_lmul, long long in_ts, const float *scale,
                    float *out, long long out_lmul, long long out_ts, const float2 *tw, cudaStream_t s) {
-#define BELLA_FFT_CASE(R2)                                                                                      \
-    case FFT_R1 * R2: {                                                                                         \
-        const unsigned grid = (unsigned)((nlines + FftShape<R2>::LPC - 1) / FftShape<R2>::LPC);                 \
-        k_sp_fft<KIND, FWD, R2><<<grid, 256, 0, s>>>(nlines, in, in_lmul, in_ts, scale, out, out_lmul, out_ts, tw); \
+#define BELLA_FFT_CASE(R1, R2)                                                                                  \
+    case R1 * R2: {                                                                                             \
+        const unsigned grid = (unsigned)((nlines + FftShape<R1, R2>::LPC - 1) / FftShape<R1, R2>::LPC);         \
+        k_sp_fft<KIND, FWD, R1, R2><<<grid, 256, 0, s>>>(nlines, in, in_lmul, in_ts, scale, out, out_lmul, out_ts, \
+                                                         tw);                                                   \
         break;                                                                                                  \
     }
     switch (L) {
-        BELLA_FFT_CASE(1)
-        BELLA_FFT_CASE(2)
-        BELLA_FFT_CASE(4)
-        BELLA_FFT_CASE(8)
-        BELLA_FFT_CASE(16)
-        BELLA_FFT_CASE(32)
-        BELLA_FFT_CASE(64)
+        BELLA_FFT_CASE(16, 1)
+        BELLA_FFT_CASE(16, 2)
+        BELLA_FFT_CASE(16, 4)
+        BELLA_FFT_CASE(16, 8)
+        BELLA_FFT_CASE(16, 16)
+        BELLA_FFT_CASE(16, 32)
+        BELLA_FFT_CASE(16, 64)
+        BELLA_FFT_CASE(32, 64)
         default: break;
     }
 #undef BELLA_FFT_CASE
@@ -387,6 +395,53 @@ __global__ void k_sp_means_final(int nx, int ny, int nz, int has_hc, const doubl
         cz[j - 1] = a[2] * inv;
     }
     hcm[j] = has_hc ? a[3] / ((double)nx * nz) : 0.0;
+}
+
+// 2D operator (cells (ny+1) x (nx+1), row stride nx+1; nodes ny x nx): per interior
+// y-cell row a = 1..ny-1, the mean over the interior columns 1..nx-1 of cxx*hplusx
+// and cyy*hplusy; per node row, the mean of hcenter.  Block (a, c) sums chunk c into
+// part[(a * SP_CHUNKS + c) * 4 + v] (v: 2 -> x coefficient, 1 -> y coefficient, 3 -> hcenter).
+__global__ void __launch_bounds__(256)
+k_sp2_means(int nx, int ny, const double *hx, const double *hy, const double *cxx, const double *cyy,
+            const double *hc, double *part) {
+    const int a = blockIdx.x, c = blockIdx.y;
+    __shared__ double red[4][256];
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int b = 1 + c * (int)blockDim.x + (int)threadIdx.x; b <= nx - 1 && a >= 1; b += (int)blockDim.x * SP_CHUNKS) {
+        const long long q = (long long)a * (nx + 1) + b;
+        v[1] += cyy[q] * hy[q];
+        v[2] += cxx[q] * hx[q];
+    }
+    if (hc && a < ny)
+        for (int i = c * (int)blockDim.x + (int)threadIdx.x; i < nx; i += (int)blockDim.x * SP_CHUNKS)
+            v[3] += hc[(long long)a * nx + i];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) red[q][threadIdx.x] = v[q];
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x < 4) part[((long long)a * SP_CHUNKS + c) * 4 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+// the 2D means in the 3D roles: cy = mean(cyy hplusy), cz = mean(cxx hplusx), cx = 0
+__global__ void k_sp2_means_final(int nx, int ny, int has_hc, const double *part, double *cx, double *cy,
+                                  double *cz, double *hcm) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= ny) return;
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int c = 0; c < SP_CHUNKS; ++c)
+        for (int q = 0; q < 4; ++q) v[q] += part[((long long)a * SP_CHUNKS + c) * 4 + q];
+    if (a >= 1) {
+        const double inv = 1.0 / (double)(nx - 1);
+        cx[a - 1] = 0.0;
+        cy[a - 1] = v[1] * inv;
+        cz[a - 1] = v[2] * inv;
+    }
+    hcm[a] = has_hc ? v[3] / (double)nx : 0.0;
 }
 
 __global__ void k_sp_recip(long long n, const double *dinv, float *out) {
@@ -547,6 +602,26 @@ k_sp_lines(int Kx, int ny, int Kz, float *__restrict__ W, const double *__restri
 int spectral_apply_dev(bella_spectral3d *sp, const float *in, float *out, cudaStream_t s) {
     const int nx = sp->nx, ny = sp->ny, nz = sp->nz, Kx = sp->Kx, Kz = sp->Kz;
     const long long rows = (long long)nx * ny, xl = (long long)ny * Kz;
+    if (sp->twod) {                                       // one transformed axis: rows of nz values
+        const long long nl = Kz;
+        if (sp->fft_z) {
+            if (sp->zper) sp_fft<0, true>(rows, sp->Lz, in, nz, 1, sp->dscale, sp->w2, Kz, 1, sp->twz, s);
+            else sp_fft<1, true>(rows, sp->Lz, in, nz, 1, sp->dscale, sp->w2, Kz, 1, sp->twz, s);
+        } else {
+            sgemm(ny, Kz, nz, in, nz, sp->dscale, sp->tzfT, Kz, sp->w2, Kz, s);
+        }
+        k_sp_lines<<<(unsigned)((nl + 127) / 128), 128, 0, s>>>(1, ny, Kz, sp->w2, sp->mux, sp->muz, sp->hc_zero,
+                                                                sp->idx2, sp->idy2, sp->idz2, sp->la, sp->lc,
+                                                                sp->li);
+        if (sp->fft_z) {
+            if (sp->zper) sp_fft<0, false>(rows, sp->Lz, sp->w2, Kz, 1, nullptr, out, nz, 1, sp->twz, s);
+            else sp_fft<1, false>(rows, sp->Lz, sp->w2, Kz, 1, nullptr, out, nz, 1, sp->twz, s);
+        } else {
+            sgemm(ny, nz, Kz, sp->w2, Kz, nullptr, sp->tziT, nz, out, nz, s);
+        }
+        sp->launches += 3;
+        return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
+    }
     // z forward: w1[(x,y)][kz] from in[(x,y)][z] / dinv
     if (sp->fft_z) {
         if (sp->zper) sp_fft<0, true>(rows, sp->Lz, in, nz, 1, sp->dscale, sp->w1, Kz, 1, sp->twz, s);
@@ -655,41 +730,50 @@ int bella_spectral3d_destroy(bella_spectral3d *sp) {
     return BELLA_OK;
 }
 
-int bella_spectral3d_create(bella_spectral3d **out, const bella_op3d *op, int device, void *stream) {
-    if (!out || !op) return BELLA_EINVAL;
-    *out = nullptr;
-    if (op->nx < 3 || op->ny < 3 || op->nz < 3 || !op->hplusx || !op->hplusy || !op->hplusz || !op->diag_inv)
-        return BELLA_EINVAL;
-    if (!op->y_wall) return BELLA_EINVAL;     // the line solves run along a walled y axis
-    if (!(op->dx > 0.0) || !(op->dy > 0.0) || !(op->dz > 0.0)) return BELLA_EINVAL;
-    if (cudaSetDevice(device) != cudaSuccess) return BELLA_ECUDA;
-    cudaStream_t s = (cudaStream_t)stream;
+}  // extern "C"
+
+// the parts of the set-up shared by the 3D and 2D operators: transform bases,
+// allocations, means (launch_means), 1/diag_inv, Thomas factors
+struct SpGeom {
+    int nx, ny, nz, xper, zper, twod;
+    double idx2, idy2, idz2;
+    const double *dinv;
+};
+
+template <typename F>
+static int sp_build(bella_spectral3d **out, const SpGeom &g, int device, cudaStream_t s, F launch_means) {
     bella_spectral3d *sp = new bella_spectral3d;
     memset(sp, 0, sizeof(*sp));
     sp->device = device;
-    sp->nx = op->nx; sp->ny = op->ny; sp->nz = op->nz;
-    sp->xper = op->x_wall ? 0 : 1;
-    sp->zper = op->z_wall ? 0 : 1;
-    sp->n = (long long)op->nx * op->ny * op->nz;
-    sp->idx2 = 1.0 / (op->dx * op->dx);
-    sp->idy2 = 1.0 / (op->dy * op->dy);
-    sp->idz2 = 1.0 / (op->dz * op->dz);
+    sp->nx = g.nx; sp->ny = g.ny; sp->nz = g.nz;
+    sp->xper = g.xper;
+    sp->zper = g.zper;
+    sp->twod = g.twod;
+    sp->n = (long long)g.nx * g.ny * g.nz;
+    sp->idx2 = g.idx2;
+    sp->idy2 = g.idy2;
+    sp->idz2 = g.idz2;
     // FFT path per axis when the transform length is a power of two that fits a CTA
     auto fft_len = [](int n, int periodic, int *L, int *p) {
         const int len = periodic ? n - 1 : 2 * (n - 1);
-        if (len < FFT_R1 || len > 64 * FFT_R1 || (len & (len - 1))) return 0;
+        if (len < FFT_R1 || len > 2048 || (len & (len - 1))) return 0;
         *L = len;
         *p = 0;
         while ((1 << *p) < len) ++*p;
         return 1;
     };
-    sp->fft_x = fft_len(op->nx, sp->xper, &sp->Lx, &sp->px);
-    sp->fft_z = fft_len(op->nz, sp->zper, &sp->Lz, &sp->pz);
+    sp->fft_x = g.twod ? 0 : fft_len(g.nx, sp->xper, &sp->Lx, &sp->px);
+    sp->fft_z = fft_len(g.nz, sp->zper, &sp->Lz, &sp->pz);
     std::vector<double> mux, muz;
     std::vector<float> fx, ix, fz, iz;
-    axis_basis(op->nx, sp->xper, !sp->fft_x, mux, fx, ix, sp->Kx);
-    axis_basis(op->nz, sp->zper, !sp->fft_z, muz, fz, iz, sp->Kz);
-    const int nx = op->nx, ny = op->ny, nz = op->nz, Kx = sp->Kx, Kz = sp->Kz;
+    if (g.twod) {                         // no x axis: one mode with eigenvalue 0
+        sp->Kx = 1;
+        mux.assign(1, 0.0);
+    } else {
+        axis_basis(g.nx, sp->xper, !sp->fft_x, mux, fx, ix, sp->Kx);
+    }
+    axis_basis(g.nz, sp->zper, !sp->fft_z, muz, fz, iz, sp->Kz);
+    const int ny = g.ny, nz = g.nz, Kx = sp->Kx, Kz = sp->Kz;
     std::vector<float> fzT, izT;
     if (!sp->fft_z) {
         fzT.resize((size_t)nz * Kz);
@@ -728,11 +812,8 @@ int bella_spectral3d_create(bella_spectral3d **out, const bella_op3d *op, int de
     }
     cudaMemcpyAsync(sp->mux, mux.data(), Kx * sizeof(double), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(sp->muz, muz.data(), Kz * sizeof(double), cudaMemcpyHostToDevice, s);
-    k_sp_means<<<dim3(ny, SP_CHUNKS), 256, 0, s>>>(nx, ny, nz, op->hplusx, op->hplusy, op->hplusz, op->hcenter,
-                                                   sp->mpart);
-    k_sp_means_final<<<(ny + 127) / 128, 128, 0, s>>>(nx, ny, nz, op->hcenter ? 1 : 0, sp->mpart, sp->cx, sp->cy,
-                                                      sp->cz, sp->hcm);
-    k_sp_recip<<<vec_grid(sp->n), VEC_BLOCK, 0, s>>>(sp->n, op->diag_inv, sp->dscale);
+    launch_means(sp);
+    k_sp_recip<<<vec_grid(sp->n), VEC_BLOCK, 0, s>>>(sp->n, g.dinv, sp->dscale);
     std::vector<double> hcm(ny);
     cudaMemcpyAsync(hcm.data(), sp->hcm, ny * sizeof(double), cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
@@ -774,6 +855,47 @@ int bella_spectral3d_create(bella_spectral3d **out, const bella_op3d *op, int de
     sp->launches = 3;
     *out = sp;
     return BELLA_OK;
+}
+
+extern "C" {
+
+int bella_spectral3d_create(bella_spectral3d **out, const bella_op3d *op, int device, void *stream) {
+    if (!out || !op) return BELLA_EINVAL;
+    *out = nullptr;
+    if (op->nx < 3 || op->ny < 3 || op->nz < 3 || !op->hplusx || !op->hplusy || !op->hplusz || !op->diag_inv)
+        return BELLA_EINVAL;
+    if (!op->y_wall) return BELLA_EINVAL;     // the line solves run along a walled y axis
+    if (!(op->dx > 0.0) || !(op->dy > 0.0) || !(op->dz > 0.0)) return BELLA_EINVAL;
+    if (cudaSetDevice(device) != cudaSuccess) return BELLA_ECUDA;
+    cudaStream_t s = (cudaStream_t)stream;
+    const SpGeom g{op->nx, op->ny, op->nz, op->x_wall ? 0 : 1, op->z_wall ? 0 : 1, 0,
+                   1.0 / (op->dx * op->dx), 1.0 / (op->dy * op->dy), 1.0 / (op->dz * op->dz), op->diag_inv};
+    return sp_build(out, g, device, s, [&](bella_spectral3d *sp) {
+        k_sp_means<<<dim3(op->ny, SP_CHUNKS), 256, 0, s>>>(op->nx, op->ny, op->nz, op->hplusx, op->hplusy, op->hplusz,
+                                                           op->hcenter, sp->mpart);
+        k_sp_means_final<<<(op->ny + 127) / 128, 128, 0, s>>>(op->nx, op->ny, op->nz, op->hcenter ? 1 : 0, sp->mpart,
+                                                              sp->cx, sp->cy, sp->cz, sp->hcm);
+    });
+}
+
+int bella_spectral2d_create(bella_spectral3d **out, const bella_op2d *op, int device, void *stream) {
+    if (!out || !op) return BELLA_EINVAL;
+    *out = nullptr;
+    if (op->nx < 3 || op->ny < 3 || !op->hplusx || !op->hplusy || !op->cxx || !op->cyy || !op->diag_inv)
+        return BELLA_EINVAL;
+    if (!op->y_wall) return BELLA_EINVAL;     // the line solves run along a walled y axis
+    if (!(op->dx > 0.0) || !(op->dy > 0.0)) return BELLA_EINVAL;
+    if (cudaSetDevice(device) != cudaSuccess) return BELLA_ECUDA;
+    cudaStream_t s = (cudaStream_t)stream;
+    // nodes [ny][nx] as the 3D layout [1][ny][nx]: x takes the role of z
+    const SpGeom g{1, op->ny, op->nx, 1, op->x_wall ? 0 : 1, 1, 0.0, 1.0 / (op->dy * op->dy),
+                   1.0 / (op->dx * op->dx), op->diag_inv};
+    return sp_build(out, g, device, s, [&](bella_spectral3d *sp) {
+        k_sp2_means<<<dim3(op->ny, SP_CHUNKS), 256, 0, s>>>(op->nx, op->ny, op->hplusx, op->hplusy, op->cxx, op->cyy,
+                                                            op->hcenter, sp->mpart);
+        k_sp2_means_final<<<(op->ny + 127) / 128, 128, 0, s>>>(op->nx, op->ny, op->hcenter ? 1 : 0, sp->mpart, sp->cx,
+                                                               sp->cy, sp->cz, sp->hcm);
+    });
 }
 
 int bella_spectral3d_apply(bella_spectral3d *sp, const float *in, float *out, void *stream) {

@@ -22,7 +22,9 @@ def _ptr(t):
 
 
 class BackgroundSolve:
-    """Background inverse of a :class:`pybella_gb300.linalg.NodalHelmholtz3D` (y must be a wall axis).
+    """Background inverse of a :class:`pybella_gb300.linalg.NodalHelmholtz3D` or
+    :class:`~pybella_gb300.linalg.NodalHelmholtz2D` (y must be a wall axis; in 2D the
+    transform runs along x and the Coriolis cross terms are left out).
 
     ``apply(r)`` maps a residual of the Jacobi-scaled system (FP32 CUDA tensor)
     to ``A_bg^+ (r / diag_inv)``; pass the object as ``preconditioner=`` to
@@ -38,10 +40,12 @@ class BackgroundSolve:
         self.n = op.n
         self._lib = op.ws._lib
         h = ctypes.c_void_p()
+        create = (self._lib.bella_spectral2d_create if isinstance(op._op, _lib.Op2D)
+                  else self._lib.bella_spectral3d_create)
         with torch.cuda.device(self.dev):
-            _lib.check(self._lib.bella_spectral3d_create(ctypes.byref(h), ctypes.byref(op._op), self.dev.index,
-                                                         ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)),
-                       "bella_spectral3d_create")
+            _lib.check(create(ctypes.byref(h), ctypes.byref(op._op), self.dev.index,
+                              ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)),
+                       "bella_spectral_create")
         self.handle = h
 
     def _stream(self):

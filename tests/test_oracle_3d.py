@@ -154,3 +154,45 @@ def test_background_inverse_preconditions_lognormal_coefficients():
     assert np.linalg.norm(b - A(x)) <= 1e-8 * np.linalg.norm(b) * 1.01
     _, info, it_plain = bicgstab_legacy(A, b, 1e-8, 5000)
     assert info == 0 and it_plain > 10 * it
+
+
+def test_background2d_inverse_is_exact_without_cross_terms_periodic_x():
+    """2D 9-point operator with horizontally uniform coefficients (sigma = 0) and no
+    Coriolis cross terms: A (A_bg^+ r) = r for r in the range of A."""
+    from oracle import cases, spectral2d
+    w = cases.stratified_2d(1, 33, 17, sigma=0.0)
+    op = dict(w["op"])
+    op["cor"] = (op["cor"][0], op["cor"][1], np.zeros_like(op["cor"][2]), np.zeros_like(op["cor"][3]))
+    B = spectral2d.BackgroundInverse2D(op)
+    X = np.random.default_rng(0).standard_normal((17, 33))
+    X[:, -1] = X[:, 0]                          # duplicated periodic seam
+    r = n2.lap2d_gather(X.reshape(-1), op)
+    assert np.linalg.norm(n2.lap2d_gather(B.apply(r), op) - r) <= 1e-12 * np.linalg.norm(r)
+
+
+def _uniform_op2d(rng, nx, ny, x_wall, with_hc):
+    prof_x, prof_y = rng.uniform(0.5, 2.0, ny + 1), rng.uniform(0.5, 2.0, ny + 1)
+    hx = np.broadcast_to(prof_x[:, None], (ny + 1, nx + 1)).reshape(-1).copy()
+    hy = np.broadcast_to(prof_y[:, None], (ny + 1, nx + 1)).reshape(-1).copy()
+    hc = (np.broadcast_to(-rng.uniform(0.1, 1.0, ny)[:, None], (ny, nx)).reshape(-1).copy() if with_hc
+          else np.zeros(nx * ny))
+    nc = (nx + 1) * (ny + 1)
+    return dict(hplusx=hx, hplusy=hy, hcenter=hc, cor=(np.ones(nc), np.full(nc, 0.7), np.zeros(nc), np.zeros(nc)),
+                diag_inv=-rng.uniform(0.5, 1.5, nx * ny), nx=nx, ny=ny, dx=0.3, dy=0.2, x_wall=x_wall,
+                y_wall=True)
+
+
+@pytest.mark.parametrize("x_wall,with_hc", [(True, False), (False, True)])
+def test_background2d_inverse_exact_walls_and_hcenter(x_wall, with_hc):
+    """Walls in x (DCT-I with trapezoid weights, exact without hcenter) and a
+    periodic x with a row-uniform hcenter (exact): A (A_bg^+ r) = r on the range."""
+    from oracle import spectral2d
+    rng = np.random.default_rng(4)
+    nx, ny = 19, 11
+    op = _uniform_op2d(rng, nx, ny, x_wall, with_hc)
+    B = spectral2d.BackgroundInverse2D(op)
+    X = rng.standard_normal((ny, nx))
+    if not x_wall:
+        X[:, -1] = X[:, 0]
+    r = n2.lap2d_gather(X.reshape(-1), op)
+    assert np.linalg.norm(n2.lap2d_gather(B.apply(r), op) - r) <= 1e-11 * np.linalg.norm(r)
