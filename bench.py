@@ -548,7 +548,8 @@ LEARNED3D = ("3D 27-point nodal solve %s nodes, stratified x log-normal(0.1) cel
              "preconditioner (background solve + trained network, flexible GMRES) vs plain double-float BiCGStab")
 
 
-def _peaks():
+def _peaks_tensor():
+    """(HBM GB/s, sustained BF16 TFLOP/s, source) from MEASURED_PEAKS.json."""
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             d = json.load(f)
@@ -705,7 +706,7 @@ def run_learned3d(args):
     nv = learned.net_voxels(shape, 2)
     cnn_flops = nv * 2 * 27 * (8 * 32 + 4 * 32 * 32 + 32 * 8)      # 8 sub-node channels in and out
     napp = L["stats"][-1]["iterations"]
-    hbm, tpeak, pkind = _peaks()
+    hbm, tpeak, pkind = _peaks_tensor()
     ach = cnn_flops / (cnn_ms / 1000.0) / 1e12
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
