@@ -1179,27 +1179,28 @@ constexpr int FG_XBLK = NSM * 8;    // blocks per group of inner products (enoug
 constexpr int FG_GROUP = 8;         // inner products per block
 
 // block (bx, gy): partial sums of <V_i, w> for the FG_GROUP vectors i of group gy
-// over a grid-stride share -> part[i * gridDim.x + bx]; w is read once per group
+// over a grid-stride share -> part[i * gridDim.x + bx]; w is read once per group.
+// With FG_XBLK x 256 threads each thread adds a few tens of products (FP32, on
+// the FP32 pipe); block and grid sums are FP64.
 __global__ void __launch_bounds__(VEC_BLOCK)
-k_fg_mdot(long long n, const float *V, long long ld, int nv, const float *w, double *part) {
+k_fg_mdot(long long n, const float *__restrict__ V, long long ld, int nv, const float *__restrict__ w,
+          double *__restrict__ part) {
     const int i0 = blockIdx.y * FG_GROUP;
     const int cnt = nv - i0 < FG_GROUP ? nv - i0 : FG_GROUP;
-    // double-float accumulation on the FP32 pipe (GB300's FP64 pipe runs at 1/64
-    // of the FP32 rate and would bound this kernel)
-    DF acc[FG_GROUP];
+    float acc[FG_GROUP];
 #pragma unroll
-    for (int q = 0; q < FG_GROUP; ++q) acc[q].zero();
+    for (int q = 0; q < FG_GROUP; ++q) acc[q] = 0.f;
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
         const float wg = w[g];
 #pragma unroll
         for (int q = 0; q < FG_GROUP; ++q)
-            if (q < cnt) acc[q].add_prod(V[(i0 + q) * ld + g], wg);
+            if (q < cnt) acc[q] = fmaf(V[(i0 + q) * ld + g], wg, acc[q]);
     }
     __shared__ double red[FG_GROUP][VEC_BLOCK / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < FG_GROUP; ++q) {
-        const double v = warp_sum(acc[q].value());
+        const double v = warp_sum((double)acc[q]);
         if (lane == 0) red[q][wid] = v;
     }
     __syncthreads();
@@ -1210,13 +1211,21 @@ k_fg_mdot(long long n, const float *V, long long ld, int nv, const float *w, dou
     }
 }
 
-// out[q] = sum over blocks of part[q * nblk + b], q < nq, in block order (deterministic)
-__global__ void k_fg_reduce(int nblk, const double *part, int nq, double *out) {
-    const int q = threadIdx.x;
+// out[q] = sum over blocks of part[q * nblk + b]: block q, fixed strided partial
+// sums and a fixed tree (deterministic)
+__global__ void __launch_bounds__(256) k_fg_reduce(int nblk, const double *part, int nq, double *out) {
+    const int q = blockIdx.x;
     if (q >= nq) return;
     double sum = 0.0;
-    for (int b = 0; b < nblk; ++b) sum += part[(size_t)q * nblk + b];
-    out[q] = sum;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) sum += part[(size_t)q * nblk + b];
+    __shared__ double red[256];
+    red[threadIdx.x] = sum;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[q] = red[0];
 }
 
 // w -= sum_i h[i] V_i, and with norm per-block partial sums of the new <w, w> (slot 0)
@@ -1316,12 +1325,12 @@ static int fgmres_cycle(bella_ws *ws, const Precond &pc, int m, double rel, cuda
         const int nv = j + 1;
         const unsigned ng = (unsigned)((nv + FG_GROUP - 1) / FG_GROUP);
         k_fg_mdot<<<dim3(FG_XBLK, ng), VEC_BLOCK, 0, s>>>(n, V, n, nv, w, ws->fg_part);
-        k_fg_reduce<<<1, 128, 0, s>>>(FG_XBLK, ws->fg_part, nv, h1);
+        k_fg_reduce<<<nv, 256, 0, s>>>(FG_XBLK, ws->fg_part, nv, h1);
         k_fg_update<<<gv, VEC_BLOCK, 0, s>>>(n, V, n, nv, h1, w, 0, ws->fg_part);
         k_fg_mdot<<<dim3(FG_XBLK, ng), VEC_BLOCK, 0, s>>>(n, V, n, nv, w, ws->fg_part);
-        k_fg_reduce<<<1, 128, 0, s>>>(FG_XBLK, ws->fg_part, nv, h2);
+        k_fg_reduce<<<nv, 256, 0, s>>>(FG_XBLK, ws->fg_part, nv, h2);
         k_fg_update<<<gv, VEC_BLOCK, 0, s>>>(n, V, n, nv, h2, w, 1, ws->fg_part);
-        k_fg_reduce<<<1, 64, 0, s>>>(gv, ws->fg_part, 1, nrm);
+        k_fg_reduce<<<1, 256, 0, s>>>(gv, ws->fg_part, 1, nrm);
         k_fg_scale<<<gv, VEC_BLOCK, 0, s>>>(n, w, nrm, w);
         ws->launches += 10;
         BELLA_CUDA(cudaMemcpyAsync(hhost, ws->fg_dev, sizeof(hhost), cudaMemcpyDeviceToHost, s));
