@@ -51,7 +51,7 @@ struct bella_spectral3d {
     double idx2, idy2, idz2;
     int fft_x, fft_z;      // 1: this axis transforms by FFT (power-of-two length), 0: by GEMM
     int twod;              // the 2D 9-point operator: one transformed axis (x, in the z role), no x pass
-    int Lx, Lz, px, pz;    // FFT lengths and their log2
+    int Lx, Lz;            // FFT lengths
     float2 *twx, *twz;     // twiddles exp(-2 pi i t / L), t < L/2
     long long launches;
 };
@@ -754,16 +754,14 @@ static int sp_build(bella_spectral3d **out, const SpGeom &g, int device, cudaStr
     sp->idy2 = g.idy2;
     sp->idz2 = g.idz2;
     // FFT path per axis when the transform length is a power of two that fits a CTA
-    auto fft_len = [](int n, int periodic, int *L, int *p) {
+    auto fft_len = [](int n, int periodic, int *L) {
         const int len = periodic ? n - 1 : 2 * (n - 1);
         if (len < FFT_R1 || len > 2048 || (len & (len - 1))) return 0;
         *L = len;
-        *p = 0;
-        while ((1 << *p) < len) ++*p;
         return 1;
     };
-    sp->fft_x = g.twod ? 0 : fft_len(g.nx, sp->xper, &sp->Lx, &sp->px);
-    sp->fft_z = fft_len(g.nz, sp->zper, &sp->Lz, &sp->pz);
+    sp->fft_x = g.twod ? 0 : fft_len(g.nx, sp->xper, &sp->Lx);
+    sp->fft_z = fft_len(g.nz, sp->zper, &sp->Lz);
     std::vector<double> mux, muz;
     std::vector<float> fx, ix, fz, iz;
     if (g.twod) {                         // no x axis: one mode with eigenvalue 0
