@@ -224,7 +224,7 @@ __device__ __forceinline__ uint32_t tc_idesc() {   // kind::f16: BF16 x BF16 -> 
 
 template <int CIN, int COUT>
 __host__ __device__ constexpr size_t tc_smem_bytes(int pz) {
-    return (size_t)27 * (CIN / 8) * COUT * 16 + (size_t)TC_SLOTS * (CIN / 8) * (TC_ROWS + 2 * pz + 2) * 16;
+    return (size_t)9 * (CIN / 8) * 3 * COUT * 16 + (size_t)TC_SLOTS * (CIN / 8) * (TC_ROWS + 2 * pz + 2) * 16;
 }
 
 __device__ __forceinline__ uint32_t tc_try_wait(uint32_t mbar, uint32_t parity) {
@@ -235,22 +235,35 @@ __device__ __forceinline__ uint32_t tc_try_wait(uint32_t mbar, uint32_t parity) 
     return done;
 }
 
+// Input plane p feeds output planes p+1, p, p-1 through the weights of taps dx = 0, 1, 2:
+// with the three taps side by side in B (N = 96) one MMA per (dy, dz, K-step) serves
+// all three output planes.  Their accumulators live in a ring of TC_RING planes of 32
+// tensor-memory columns per row block, in descending plane order (plane q at column
+// 32 * (TC_RING - 1 - q % TC_RING)), so the three are adjacent unless the ring wraps
+// between them (then two MMAs, N = 32 and 64).  Every slot is zeroed after its
+// epilogue and every MMA accumulates.  Output planes outside the run or in another
+// sample's x-segment are left out of an MMA's column range.
+constexpr int TC_RING = 8;                   // accumulator planes per row block (8 x 32 = 256 columns)
+constexpr int TC_TMEM_COLS = TC_MB * TC_RING * 32;
+
 template <int CIN, int COUT, bool RELU>
 __global__ void __launch_bounds__(256, 1)
 k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *__restrict__ in,
             const __nv_bfloat16 *__restrict__ Wtc, const float *__restrict__ bias, __nv_bfloat16 *out, int *err) {
     static_assert(COUT == 32, "tensor-memory epilogue reads 32 columns");
+    static_assert(TC_TMEM_COLS == 512, "the accumulator ring fills the tensor memory");
     constexpr int NCH = CIN / 8;
+    constexpr int NB = 3 * COUT;                          // B rows: the three dx taps
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_slot;
     __shared__ int ok_flag;
     const int PZ = nz + 2, PY = ny + 2;
     const int L = TC_ROWS + 2 * PZ + 2;                   // staged rows per plane and chunk
-    unsigned char *sW = smem;                             // [27][NCH][COUT][16 B]
-    unsigned char *sA = smem + (size_t)27 * NCH * COUT * 16;   // [TC_SLOTS][NCH][L][16 B]
+    unsigned char *sW = smem;                             // [9][NCH][3*COUT][16 B]
+    unsigned char *sA = smem + (size_t)9 * NCH * NB * 16; // [TC_SLOTS][NCH][L][16 B]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    for (int e = tid; e < 27 * NCH * COUT; e += 256)
+    for (int e = tid; e < 9 * NCH * NB; e += 256)
         reinterpret_cast<uint4 *>(sW)[e] = reinterpret_cast<const uint4 *>(Wtc)[e];
     const uint32_t mbar_a0 = (uint32_t)__cvta_generic_to_shared(&mbar[0]);
     const uint32_t mbar_a1 = (uint32_t)__cvta_generic_to_shared(&mbar[1]);
@@ -261,22 +274,35 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
     }
     if (warp == 0) {
         const uint32_t slot = (uint32_t)__cvta_generic_to_shared(&tmem_slot);
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(64 * TC_MB));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(TC_TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_slot;
+    // warp w owns lanes 32*(w%4).. of row block w/4: zero its whole accumulator ring
+    const uint32_t tlane = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)((warp >> 2) * TC_RING * 32);
+    auto zero_cols = [&](uint32_t taddr) {
+        const uint32_t z = 0u;
+        asm volatile("tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+                     "{%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,"
+                     "%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr), "r"(z));
+    };
+    for (int q = 0; q < TC_RING; ++q) zero_cols(tlane + (uint32_t)(q * 32));
+    asm volatile("tcgen05.wait::st.sync.aligned;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t sW_a = (uint32_t)__cvta_generic_to_shared(sW), sA_a = (uint32_t)__cvta_generic_to_shared(sA);
-    const uint64_t a0 = tc_sdesc(sA_a, (uint32_t)L * 16, 128), b0 = tc_sdesc(sW_a, COUT * 16, 128);
-    const uint32_t idesc = tc_idesc<COUT>();
+    const uint64_t a0 = tc_sdesc(sA_a, (uint32_t)L * 16, 128), b0 = tc_sdesc(sW_a, NB * 16, 128);
+    const uint32_t idesc32 = tc_idesc<32>(), idesc64 = tc_idesc<64>(), idesc96 = tc_idesc<96>();
     const int plane = PY * PZ;
     const int nblk = (plane + TC_ROWS - 1) / TC_ROWS;
     const int nseg = (nx + runlen - 1) / runlen;
     const int nruns = nblk * nseg;
     uint32_t phase[2] = {0u, 0u};
-    int committed[2] = {0, 0};              // commits not yet waited for, per accumulator set (thread 0)
+    int committed[2] = {0, 0};              // commits not yet waited for, per mbarrier (thread 0)
     bool failed = false;
 
     for (int run = blockIdx.x; run < nruns && !failed; run += gridDim.x) {
@@ -284,9 +310,9 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
         const int ia = seg * runlen, ib = min(nx, ia + runlen);
         const int f0 = fb * TC_ROWS - (PZ + 1);           // padded row of staged row 0
         // stage input plane p into ring slot p % TC_SLOTS with 16-byte asynchronous copies
-        // (source size 0 fills the zero padding); every copy of a thread is in flight
-        // before the single wait in sync_staged()
+        // (source size 0 fills the zero padding); a run reads planes ia-1 .. ib
         auto stage = [&](int p) {
+            if (p < 0 || p >= nx || p < ia - 1 || p > ib) return;
             const uint32_t base = sA_a + (uint32_t)((size_t)(p % TC_SLOTS) * NCH * L * 16);
             for (int rb = tid; rb < L; rb += 256) {
                 const int f = f0 + rb;
@@ -307,84 +333,95 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
                                    "r"(bytes));
             }
         };
-        // thread 0: every tap of output plane k into accumulator set `set`, then commit.
-        // Fully unrolled: per MMA only two 64-bit adds of precomputed offsets.
-        auto issue = [&](int k, int set) {
-            int first = 1;
+        // thread 0: the MMAs of input plane p into output planes qlo..qhi (descending
+        // columns from qhi), then one commit to mbarrier p & 1 (also when p has no MMAs)
+        auto mma_range = [&](int p, int qhi, int qlo) {
+            const int n = qhi - qlo + 1;                      // 1..3 output planes
+            const uint32_t col = (uint32_t)(32 * (TC_RING - 1 - qhi % TC_RING));
+            const int d0 = p + 1 - qhi;                       // dx tap of plane qhi
+            const uint32_t idesc = n == 3 ? idesc96 : (n == 2 ? idesc64 : idesc32);
+            const uint64_t abase = a0 + (uint64_t)((p % TC_SLOTS) * NCH * L + PZ + 1);
 #pragma unroll
             for (int mb = 0; mb < TC_MB; ++mb) {
-                const uint32_t dtm = tmem + (uint32_t)(set * 32 * TC_MB + mb * 32);
-                first = 1;
+                const uint32_t dtm = tmem + (uint32_t)(mb * TC_RING * 32) + col;
 #pragma unroll
-                for (int dxi = 0; dxi < 3; ++dxi) {
-                    const int gi = k + dxi - 1;
-                    if (gi < 0 || gi >= nx || (gi / xseg) != (k / xseg)) continue;   // zero padding along x
-                    const uint64_t abase = a0 + (uint64_t)((gi % TC_SLOTS) * NCH * L + mb * 128 + PZ + 1);
+                for (int dyi = 0; dyi < 3; ++dyi) {
 #pragma unroll
-                    for (int dyi = 0; dyi < 3; ++dyi) {
-                        const int yoff = (dyi - 1) * PZ;
+                    for (int dzi = 0; dzi < 3; ++dzi) {
+                        const int t9 = dyi * 3 + dzi;
 #pragma unroll
-                        for (int dzi = 0; dzi < 3; ++dzi) {
-                            const int tap = dxi * 9 + dyi * 3 + dzi;
-#pragma unroll
-                            for (int ks = 0; ks < CIN / 16; ++ks) {
-                                const uint64_t ad = abase + (uint64_t)(2 * ks * L + yoff + (dzi - 1));
-                                const uint64_t bd = b0 + (uint64_t)((tap * NCH + 2 * ks) * COUT);
-                                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                                             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                                             ::"r"(dtm), "l"(ad), "l"(bd), "r"(idesc), "r"(first ? 0 : 1));
-                                first = 0;
-                            }
+                        for (int ks = 0; ks < CIN / 16; ++ks) {
+                            const uint64_t ad = abase + (uint64_t)(mb * 128 + 2 * ks * L + (dyi - 1) * PZ + (dzi - 1));
+                            const uint64_t bd = b0 + (uint64_t)((t9 * NCH + 2 * ks) * NB + 32 * d0);
+                            asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                                         ::"r"(dtm), "l"(ad), "l"(bd), "r"(idesc), "r"(1));
                         }
                     }
                 }
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                         ::"r"(set ? mbar_a1 : mbar_a0));
-            committed[set] += 1;
         };
-        for (int p = ia - 1; p <= ia + 1; ++p)
-            if (p >= 0 && p < nx) stage(p);
-        asm volatile("cp.async.commit_group;");
-        if (ia + 1 < ib && ia + 2 < nx) stage(ia + 2);
-        asm volatile("cp.async.commit_group;");
-        asm volatile("cp.async.wait_group 1;");          // planes ia-1 .. ia+1 have landed
+        auto issue = [&](int p) {
+            if (p >= 0 && p < nx) {
+                const int s0 = (p / xseg) * xseg;             // this sample's x-segment
+                const int qlo = max(max(p - 1, ia), s0), qhi = min(min(p + 1, ib - 1), s0 + xseg - 1);
+                if (qlo <= qhi) {
+                    const int cut = (qhi / TC_RING) * TC_RING;    // ring boundary below qhi
+                    if (qlo >= cut) {
+                        mma_range(p, qhi, qlo);
+                    } else {
+                        mma_range(p, qhi, cut);
+                        mma_range(p, cut - 1, qlo);
+                    }
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                         ::"r"((p & 1) ? mbar_a1 : mbar_a0));
+            committed[p & 1] += 1;
+        };
+        // Pipeline over input planes p = ia-1 .. ib: plane p+1's MMAs are issued before
+        // plane p's are waited for; output plane p-1 is complete once plane p's MMAs are
+        // (MMAs of one thread complete in order), and its epilogue then runs while plane
+        // p+1's MMAs are on the tensor cores.  Input plane p's ring slot is free after
+        // its own MMAs: plane p+5 is staged into it.  One cp.async group per plane.
+        for (int p = ia - 1; p <= ia + 3; ++p) {
+            stage(p);
+            asm volatile("cp.async.commit_group;");
+        }
+        asm volatile("cp.async.wait_group 4;");          // plane ia-1 has landed
         asm volatile("fence.proxy.async.shared::cta;");
         asm volatile("tcgen05.fence::before_thread_sync;");
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;");
-        if (tid == 0) issue(ia, 0);
-        for (int k = ia; k < ib; ++k) {
-            const int set = (k - ia) & 1;
-            // prefetch plane k+3: its ring slot last held plane k-2, read only by plane
-            // k-1's MMAs, which were waited for before plane k-1's epilogue
-            if (k + 2 < ib && k + 3 < nx) stage(k + 3);
-            asm volatile("cp.async.commit_group;");
-            asm volatile("cp.async.wait_group 1;");      // plane k+2 (for plane k+1's MMAs) has landed
+        if (tid == 0) issue(ia - 1);
+        for (int p = ia - 1; p <= ib; ++p) {
+            asm volatile("cp.async.wait_group 3;");      // plane p+1 has landed
             asm volatile("fence.proxy.async.shared::cta;");
             asm volatile("tcgen05.fence::before_thread_sync;");
-            __syncthreads();
+            __syncthreads();                             // also: the last epilogue's zeroing is done
             asm volatile("tcgen05.fence::after_thread_sync;");
             if (tid == 0) {
-                if (k + 1 < ib) issue(k + 1, set ^ 1);
-                const uint32_t done = tc_try_wait(set ? mbar_a1 : mbar_a0, phase[set]);
-                if (done) committed[set] -= 1;
+                if (p + 1 <= ib) issue(p + 1);
+                const int b = p & 1;
+                const uint32_t done = tc_try_wait(b ? mbar_a1 : mbar_a0, phase[b]);
+                if (done) committed[b] -= 1;
                 ok_flag = done ? 1 : 0;
             }
             __syncthreads();
-            if (!ok_flag) {                  // the phase of this set stays at the unfinished commit
+            if (!ok_flag) {                  // the phase of this barrier stays at the unfinished commit
                 if (tid == 0) atomicExch(err, 1);
                 failed = true;
                 break;
             }
-            phase[set] ^= 1u;
+            phase[p & 1] ^= 1u;
             asm volatile("tcgen05.fence::after_thread_sync;");
-            // epilogue of plane k: warp w reads rows 32*(w%4).. of accumulator w/4 of the set
-            {
+            stage(p + 5);                    // ring slot of plane p: read only by plane p's MMAs
+            asm volatile("cp.async.commit_group;");
+            const int q = p - 1;             // output plane complete after input plane p
+            if (q >= ia && q < ib) {
                 const int mb = warp >> 2;
+                const uint32_t taddr = tlane + (uint32_t)(32 * (TC_RING - 1 - q % TC_RING));
                 uint32_t r[32];
-                const uint32_t taddr =
-                    tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(set * 32 * TC_MB + mb * 32);
                 asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
                              "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
                              "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -395,6 +432,7 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
                                "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
                              : "r"(taddr));
                 asm volatile("tcgen05.wait::ld.sync.aligned;");
+                zero_cols(taddr);            // the slot's next plane accumulates from zero
                 const int f = fb * TC_ROWS + mb * 128 + (warp & 3) * 32 + lane;
                 if (f < plane) {
                     const int yq = f / PZ;
@@ -409,38 +447,44 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
                             const __nv_bfloat162 h2 = __floats2bfloat162_rn(v0, v1);
                             w[c] = *reinterpret_cast<const uint32_t *>(&h2);
                         }
-                        uint4 *o = reinterpret_cast<uint4 *>(out + (((size_t)k * ny + y) * nz + z) * COUT);
+                        uint4 *o = reinterpret_cast<uint4 *>(out + (((size_t)q * ny + y) * nz + z) * COUT);
                         o[0] = make_uint4(w[0], w[1], w[2], w[3]);
                         o[1] = make_uint4(w[4], w[5], w[6], w[7]);
                         o[2] = make_uint4(w[8], w[9], w[10], w[11]);
                         o[3] = make_uint4(w[12], w[13], w[14], w[15]);
                     }
                 }
+                asm volatile("tcgen05.wait::st.sync.aligned;");
             }
             asm volatile("tcgen05.fence::before_thread_sync;");
-            __syncthreads();                 // accumulator set read; its next writer may start
         }
+        asm volatile("cp.async.wait_group 0;");          // no copy of this run outlives it
+        __syncthreads();
     }
     // after a time-out, commits that were issued but not waited for may still be in
     // flight: wait for them (bounded) before freeing tensor memory
     if (failed && tid == 0) {
-        for (int q = 0; q < 2; ++q)
-            for (int c = 0; c < committed[q]; ++c) {
-                tc_try_wait(q ? mbar_a1 : mbar_a0, phase[q]);
-                phase[q] ^= 1u;
+        for (int b = 0; b < 2; ++b)
+            for (int c = 0; c < committed[b]; ++c) {
+                tc_try_wait(b ? mbar_a1 : mbar_a0, phase[b]);
+                phase[b] ^= 1u;
             }
     }
+    asm volatile("cp.async.wait_group 0;");
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(64 * TC_MB));
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS));
 }
 
-// kernel weights [27][COUTP][CINP] -> tensor-core operand order [27][CINP/8][COUTP][8]
+// kernel weights [27][COUTP][CINP] (tap = (dx+1)*9 + (dy+1)*3 + (dz+1)) -> tensor-core
+// operand order [dy,dz][CINP/8][dx][COUTP][8]: for each (dy, dz) and 8-channel chunk,
+// the three dx taps' output channels are 3*COUTP consecutive B rows
 __global__ void k_wk_to_tc(const __nv_bfloat16 *wk, int cinp, int coutp, __nv_bfloat16 *wtc) {
     const int total = 27 * cinp * coutp;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
         const int tap = e / (cinp * coutp), r = e - tap * cinp * coutp, co = r / cinp, ci = r - co * cinp;
-        wtc[(((size_t)tap * (cinp / 8) + ci / 8) * coutp + co) * 8 + (ci % 8)] = wk[e];
+        const int dx = tap / 9, t9 = tap - dx * 9;
+        wtc[((((size_t)t9 * (cinp / 8) + ci / 8) * 3 + dx) * coutp + co) * 8 + (ci % 8)] = wk[e];
     }
 }
 
