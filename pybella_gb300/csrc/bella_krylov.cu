@@ -1426,7 +1426,7 @@ static int fbicgstab_impl(bella_ws *ws, const bella::Precond &pc, const double *
             const double need = 0.5 * target / rnorm;
             if (need > rel) rel = need;
             // each inner solve is capped so that a stagnating learned iteration is
-            // judged (and, without progress, replaced by the plain method) early
+            // checked (and, without progress, replaced by the plain method) early
             int cap = o.maxiter / (o.max_outer > 0 ? o.max_outer : 1);
             if (cap < 100) cap = 100;
             if (cap > o.maxiter - total) cap = o.maxiter - total;

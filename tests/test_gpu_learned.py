@@ -1,6 +1,6 @@
 """The learned preconditioner end to end on the GPU: pairs harvested from the
 solver's own iterations, training by the library's forward/backward/Adam kernels
-from a seeded init, and the flexible solve judged by the FP64 true residual
+from a seeded init, and the flexible solve checked by the FP64 true residual
 against plain BiCGStab on the same inputs and tolerance."""
 import warnings
 
@@ -10,7 +10,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_trained_network_lowers_its_training_loss_and_solves_are_judged_by_true_residual(capsys):
+def test_trained_network_lowers_its_training_loss_and_solves_are_checked_by_true_residual(capsys):
     import torch
     from pybella_gb300 import learned, workloads
     pairs = learned.harvest_pairs([1], shape=(97, 49, 97), npairs=256, crop=40, random_fraction=0.25)
@@ -30,7 +30,7 @@ def test_trained_network_lowers_its_training_loss_and_solves_are_judged_by_true_
     with warnings.catch_warnings(record=True) as rec:
         warnings.simplefilter("always")
         xl, sl = A.solve(w["b"], tol=1e-8, maxiter=20000, preconditioner=net)
-    # the plain method is the judge: the returned x meets the tolerance on the FP64
+    # the plain method decides: the returned x meets the tolerance on the FP64
     # true residual, and a fallback to it is never silent
     for x, st in ((xp, sp), (xl, sl)):
         assert st["status"] == 0, st

@@ -1,5 +1,5 @@
 """Background (spectral) solve of the 3D operator on the GPU against the oracle's
-FP64 restatement (oracle/spectral3d.py), and the solves it preconditions, judged
+FP64 restatement (oracle/spectral3d.py), and the solves it preconditions, checked
 by the FP64 true residual and compared with the plain FP64 solve."""
 import warnings
 
