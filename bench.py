@@ -738,7 +738,7 @@ def run_learned3d(args):
                  "d2h_bytes_per_step": A.n * 8} if e2e_ms else None),
         "gpu_launches": L["launches"],
         "roofline": {"bound": "tensor", "achieved": ach, "peak": tpeak, "unit": "TFLOP/s", "frac": ach / tpeak,
-                     "traffic": None, "kernel": "k_conv3d_tc x5 + k_conv3d (one network application)",
+                     "traffic": None, "kernel": "k_conv3d_tc x6 (one network application)",
                      "peak_source": pkind + " bf16 sustained", "flops_per_launch": cnn_flops,
                      "ms_per_application": cnn_ms, "applications_per_solve": napp,
                      "background_apply_ms": bg_ms},

@@ -243,7 +243,7 @@ int       bella_cnn_set_mode(bella_cnn *net, int mode);
 /* identity path: every map (forward, gradients, training, solver) returns omega*in + CNN(in);
  * default 0 */
 int       bella_cnn_set_skip(bella_cnn *net, float omega);
-/* forward layers 0-4 on the tcgen05 tensor-core path (1, the default) or mma.sync (0); tcgen05
+/* all six forward layers on the tcgen05 tensor-core path (1, the default) or mma.sync (0); tcgen05
  * is used when the z extent of the grid the net runs on is at most 142 (staged planes fit in
  * shared memory), mma.sync otherwise */
 int       bella_cnn_set_tc(bella_cnn *net, int on);

@@ -222,6 +222,10 @@ __device__ __forceinline__ uint32_t tc_idesc() {   // kind::f16: BF16 x BF16 -> 
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
 }
 
+__device__ __forceinline__ uint32_t tc_idesc_n(int n) {   // as tc_idesc<N> with N at run time
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+
 template <int CIN, int COUT>
 __host__ __device__ constexpr size_t tc_smem_bytes(int pz) {
     return (size_t)9 * (CIN / 8) * 3 * COUT * 16 + (size_t)TC_SLOTS * (CIN / 8) * (TC_ROWS + 2 * pz + 2) * 16;
@@ -243,15 +247,18 @@ __device__ __forceinline__ uint32_t tc_try_wait(uint32_t mbar, uint32_t parity) 
 // between them (then two MMAs, N = 32 and 64).  Every slot is zeroed after its
 // epilogue and every MMA accumulates.  Output planes outside the run or in another
 // sample's x-segment are left out of an MMA's column range.
-constexpr int TC_RING = 8;                   // accumulator planes per row block (8 x 32 = 256 columns)
-constexpr int TC_TMEM_COLS = TC_MB * TC_RING * 32;
+constexpr int TC_RING = 8;                   // accumulator planes per row block
 
-template <int CIN, int COUT, bool RELU>
+// COUT = 32: hidden layers, BF16 output with bias and optional ReLU.  COUT = 16 with
+// OUTF32: the output layer (8 channels padded to 16), FP32 output (acc + bias) *
+// out_scale of its first 8 channels.
+template <int CIN, int COUT, bool RELU, bool OUTF32>
 __global__ void __launch_bounds__(256, 1)
 k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *__restrict__ in,
-            const __nv_bfloat16 *__restrict__ Wtc, const float *__restrict__ bias, __nv_bfloat16 *out, int *err) {
-    static_assert(COUT == 32, "tensor-memory epilogue reads 32 columns");
-    static_assert(TC_TMEM_COLS == 512, "the accumulator ring fills the tensor memory");
+            const __nv_bfloat16 *__restrict__ Wtc, const float *__restrict__ bias, void *out, float out_scale,
+            int *err) {
+    static_assert(COUT == 32 || (COUT == 16 && OUTF32), "hidden layers: 32 channels; output layer: 16 (8 used)");
+    constexpr int TMEM_COLS = TC_MB * TC_RING * COUT;     // 512 or 256: a power of two
     constexpr int NCH = CIN / 8;
     constexpr int NB = 3 * COUT;                          // B rows: the three dx taps
     extern __shared__ __align__(128) unsigned char smem[];
@@ -274,7 +281,7 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
     }
     if (warp == 0) {
         const uint32_t slot = (uint32_t)__cvta_generic_to_shared(&tmem_slot);
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(TC_TMEM_COLS));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
@@ -282,21 +289,25 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_slot;
     // warp w owns lanes 32*(w%4).. of row block w/4: zero its whole accumulator ring
-    const uint32_t tlane = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)((warp >> 2) * TC_RING * 32);
+    const uint32_t tlane = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)((warp >> 2) * TC_RING * COUT);
     auto zero_cols = [&](uint32_t taddr) {
         const uint32_t z = 0u;
-        asm volatile("tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
-                     "{%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,"
-                     "%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr), "r"(z));
+        if (COUT == 32)
+            asm volatile("tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+                         "{%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,"
+                         "%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr), "r"(z));
+        else
+            asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+                         "{%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr), "r"(z));
     };
-    for (int q = 0; q < TC_RING; ++q) zero_cols(tlane + (uint32_t)(q * 32));
+    for (int q = 0; q < TC_RING; ++q) zero_cols(tlane + (uint32_t)(q * COUT));
     asm volatile("tcgen05.wait::st.sync.aligned;");
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t sW_a = (uint32_t)__cvta_generic_to_shared(sW), sA_a = (uint32_t)__cvta_generic_to_shared(sA);
     const uint64_t a0 = tc_sdesc(sA_a, (uint32_t)L * 16, 128), b0 = tc_sdesc(sW_a, NB * 16, 128);
-    const uint32_t idesc32 = tc_idesc<32>(), idesc64 = tc_idesc<64>(), idesc96 = tc_idesc<96>();
+
     const int plane = PY * PZ;
     const int nblk = (plane + TC_ROWS - 1) / TC_ROWS;
     const int nseg = (nx + runlen - 1) / runlen;
@@ -337,13 +348,13 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
         // columns from qhi), then one commit to mbarrier p & 1 (also when p has no MMAs)
         auto mma_range = [&](int p, int qhi, int qlo) {
             const int n = qhi - qlo + 1;                      // 1..3 output planes
-            const uint32_t col = (uint32_t)(32 * (TC_RING - 1 - qhi % TC_RING));
+            const uint32_t col = (uint32_t)(COUT * (TC_RING - 1 - qhi % TC_RING));
             const int d0 = p + 1 - qhi;                       // dx tap of plane qhi
-            const uint32_t idesc = n == 3 ? idesc96 : (n == 2 ? idesc64 : idesc32);
+            const uint32_t idesc = tc_idesc_n(n * COUT);
             const uint64_t abase = a0 + (uint64_t)((p % TC_SLOTS) * NCH * L + PZ + 1);
 #pragma unroll
             for (int mb = 0; mb < TC_MB; ++mb) {
-                const uint32_t dtm = tmem + (uint32_t)(mb * TC_RING * 32) + col;
+                const uint32_t dtm = tmem + (uint32_t)(mb * TC_RING * COUT) + col;
 #pragma unroll
                 for (int dyi = 0; dyi < 3; ++dyi) {
 #pragma unroll
@@ -352,7 +363,7 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
 #pragma unroll
                         for (int ks = 0; ks < CIN / 16; ++ks) {
                             const uint64_t ad = abase + (uint64_t)(mb * 128 + 2 * ks * L + (dyi - 1) * PZ + (dzi - 1));
-                            const uint64_t bd = b0 + (uint64_t)((t9 * NCH + 2 * ks) * NB + 32 * d0);
+                            const uint64_t bd = b0 + (uint64_t)((t9 * NCH + 2 * ks) * NB + COUT * d0);
                             asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
                                          "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
                                          ::"r"(dtm), "l"(ad), "l"(bd), "r"(idesc), "r"(1));
@@ -420,17 +431,26 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
             const int q = p - 1;             // output plane complete after input plane p
             if (q >= ia && q < ib) {
                 const int mb = warp >> 2;
-                const uint32_t taddr = tlane + (uint32_t)(32 * (TC_RING - 1 - q % TC_RING));
+                const uint32_t taddr = tlane + (uint32_t)(COUT * (TC_RING - 1 - q % TC_RING));
                 uint32_t r[32];
-                asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-                             "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                             "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                               "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-                               "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-                               "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-                               "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-                             : "r"(taddr));
+                if (COUT == 32)
+                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+                                   "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+                                   "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+                                   "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+                                   "=r"(r[31])
+                                 : "r"(taddr));
+                else
+                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+                                   "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                                 : "r"(taddr));
                 asm volatile("tcgen05.wait::ld.sync.aligned;");
                 zero_cols(taddr);            // the slot's next plane accumulates from zero
                 const int f = fb * TC_ROWS + mb * 128 + (warp & 3) * 32 + lane;
@@ -438,20 +458,31 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
                     const int yq = f / PZ;
                     const int y = yq - 1, z = f - yq * PZ - 1;
                     if (y >= 0 && y < ny && z >= 0 && z < nz) {
-                        uint32_t w[16];
+                        const size_t g = ((size_t)q * ny + y) * nz + z;
+                        if (OUTF32) {                // the output layer's 8 real channels
+                            float v[8];
 #pragma unroll
-                        for (int c = 0; c < 16; ++c) {
-                            float v0 = __uint_as_float(r[2 * c]), v1 = __uint_as_float(r[2 * c + 1]);
-                            if (bias) { v0 += bias[2 * c]; v1 += bias[2 * c + 1]; }
-                            if (RELU) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
-                            const __nv_bfloat162 h2 = __floats2bfloat162_rn(v0, v1);
-                            w[c] = *reinterpret_cast<const uint32_t *>(&h2);
+                            for (int c = 0; c < 8; ++c)
+                                v[c] = (__uint_as_float(r[c]) + (bias ? bias[c] : 0.f)) * out_scale;
+                            float4 *o = reinterpret_cast<float4 *>(reinterpret_cast<float *>(out) + g * 8);
+                            o[0] = make_float4(v[0], v[1], v[2], v[3]);
+                            o[1] = make_float4(v[4], v[5], v[6], v[7]);
+                        } else {
+                            uint32_t w[16];
+#pragma unroll
+                            for (int c = 0; c < 16; ++c) {
+                                float v0 = __uint_as_float(r[2 * c]), v1 = __uint_as_float(r[2 * c + 1]);
+                                if (bias) { v0 += bias[2 * c]; v1 += bias[2 * c + 1]; }
+                                if (RELU) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
+                                const __nv_bfloat162 h2 = __floats2bfloat162_rn(v0, v1);
+                                w[c] = *reinterpret_cast<const uint32_t *>(&h2);
+                            }
+                            uint4 *o = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(out) + g * COUT);
+                            o[0] = make_uint4(w[0], w[1], w[2], w[3]);
+                            o[1] = make_uint4(w[4], w[5], w[6], w[7]);
+                            o[2] = make_uint4(w[8], w[9], w[10], w[11]);
+                            o[3] = make_uint4(w[12], w[13], w[14], w[15]);
                         }
-                        uint4 *o = reinterpret_cast<uint4 *>(out + (((size_t)q * ny + y) * nz + z) * COUT);
-                        o[0] = make_uint4(w[0], w[1], w[2], w[3]);
-                        o[1] = make_uint4(w[4], w[5], w[6], w[7]);
-                        o[2] = make_uint4(w[8], w[9], w[10], w[11]);
-                        o[3] = make_uint4(w[12], w[13], w[14], w[15]);
                     }
                 }
                 asm volatile("tcgen05.wait::st.sync.aligned;");
@@ -473,18 +504,20 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
     asm volatile("cp.async.wait_group 0;");
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS));
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
 }
 
 // kernel weights [27][COUTP][CINP] (tap = (dx+1)*9 + (dy+1)*3 + (dz+1)) -> tensor-core
-// operand order [dy,dz][CINP/8][dx][COUTP][8]: for each (dy, dz) and 8-channel chunk,
-// the three dx taps' output channels are 3*COUTP consecutive B rows
-__global__ void k_wk_to_tc(const __nv_bfloat16 *wk, int cinp, int coutp, __nv_bfloat16 *wtc) {
-    const int total = 27 * cinp * coutp;
+// operand order [dy,dz][CINP/8][dx][COUTD][8] (COUTD >= COUTP; rows past COUTP are
+// zero): for each (dy, dz) and 8-channel chunk, the three dx taps' output channels
+// are 3*COUTD consecutive B rows
+__global__ void k_wk_to_tc(const __nv_bfloat16 *wk, int cinp, int coutp, int coutd, __nv_bfloat16 *wtc) {
+    const int total = 27 * cinp * coutd;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-        const int tap = e / (cinp * coutp), r = e - tap * cinp * coutp, co = r / cinp, ci = r - co * cinp;
+        const int tap = e / (cinp * coutd), r = e - tap * cinp * coutd, co = r / cinp, ci = r - co * cinp;
         const int dx = tap / 9, t9 = tap - dx * 9;
-        wtc[((((size_t)t9 * (cinp / 8) + ci / 8) * 3 + dx) * coutp + co) * 8 + (ci % 8)] = wk[e];
+        const __nv_bfloat16 v = co < coutp ? wk[((size_t)tap * coutp + co) * cinp + ci] : __float2bfloat16(0.f);
+        wtc[((((size_t)t9 * (cinp / 8) + ci / 8) * 3 + dx) * coutd + co) * 8 + (ci % 8)] = v;
     }
 }
 
@@ -842,8 +875,8 @@ using namespace bella;
 struct bella_cnn {
     int device, block;
     int linear;               // 1: no ReLU and no biases (a linear map)
-    int use_tc;               // 1: layers 0-4 of the forward pass on tcgen05 (k_conv3d_tc)
-    __nv_bfloat16 *wtc[5];    // their weights in tensor-core operand order
+    int use_tc;               // 1: the forward pass on tcgen05 (k_conv3d_tc)
+    __nv_bfloat16 *wtc[6];    // its weights in tensor-core operand order (layer 5: 16 output rows)
     int *tc_err;              // set when a tensor-core wait gave up
     float omega;              // identity path: output = omega * input + network
     int bias_free;            // 1: biases held at zero (positively homogeneous map)
@@ -868,6 +901,7 @@ struct bella_cnn {
 static const int CINP_L[6] = {16, 32, 32, 32, 32, 32};
 static const int COUTP_L[6] = {32, 32, 32, 32, 32, 8};
 static const int COUTPT_L[6] = {32, 32, 32, 32, 32, 16};
+static const int COUTTC_L[6] = {32, 32, 32, 32, 32, 16};   // tensor-core B rows per dx tap
 
 static long long param_count_b(int block) {
     const int b3 = block * block * block;
@@ -908,7 +942,7 @@ static void cnn_free(bella_cnn *net) {
     cudaFree(net->gact[0]); cudaFree(net->gact[1]);
     cudaFree(net->y8); cudaFree(net->t8); cudaFree(net->g8); cudaFree(net->inv_e2); cudaFree(net->loss);
     cudaFree(net->yf); cudaFree(net->qf); cudaFree(net->gf); cudaFree(net->flux); cudaFree(net->wcrop);
-    for (int l = 0; l < 5; ++l) cudaFree(net->wtc[l]);
+    for (int l = 0; l < 6; ++l) cudaFree(net->wtc[l]);
     cudaFree(net->tc_err);
 }
 
@@ -935,7 +969,7 @@ static int tc_grid(long long nitems) {
     return (int)(nitems < nsm ? nitems : nsm);
 }
 
-// layers 0-4 on tcgen05 when enabled and the staged planes fit in shared memory
+// the forward pass on tcgen05 when enabled and the staged planes fit in shared memory
 static bool tc_fits(const BlockMap &m) {
     return tc_smem_bytes<32, 32>(m.cz + 2) <= TC_SMEM_MAX;
 }
@@ -953,21 +987,23 @@ static void forward_layers(bella_cnn *net, const BlockMap &m, float out_scale, c
         const int runlen = (nx + nseg - 1) / nseg;
         const long long nruns = (long long)nblk * ((nx + runlen - 1) / runlen);
         const int gt = tc_grid(nruns), pz = nz + 2;
+        const float *b5 = net->linear ? nullptr : net->bias[5];
         if (net->linear) {
-            k_conv3d_tc<16, 32, false><<<gt, 256, tc_smem_bytes<16, 32>(pz), s>>>(
-                nx, ny, nz, xs, runlen, net->act[0], net->wtc[0], nullptr, net->act[1], net->tc_err);
+            k_conv3d_tc<16, 32, false, false><<<gt, 256, tc_smem_bytes<16, 32>(pz), s>>>(
+                nx, ny, nz, xs, runlen, net->act[0], net->wtc[0], nullptr, net->act[1], 1.f, net->tc_err);
             for (int l = 1; l <= 4; ++l)
-                k_conv3d_tc<32, 32, false><<<gt, 256, tc_smem_bytes<32, 32>(pz), s>>>(
-                    nx, ny, nz, xs, runlen, net->act[l], net->wtc[l], nullptr, net->act[l + 1], net->tc_err);
+                k_conv3d_tc<32, 32, false, false><<<gt, 256, tc_smem_bytes<32, 32>(pz), s>>>(
+                    nx, ny, nz, xs, runlen, net->act[l], net->wtc[l], nullptr, net->act[l + 1], 1.f, net->tc_err);
         } else {
-            k_conv3d_tc<16, 32, true><<<gt, 256, tc_smem_bytes<16, 32>(pz), s>>>(
-                nx, ny, nz, xs, runlen, net->act[0], net->wtc[0], net->bias[0], net->act[1], net->tc_err);
+            k_conv3d_tc<16, 32, true, false><<<gt, 256, tc_smem_bytes<16, 32>(pz), s>>>(
+                nx, ny, nz, xs, runlen, net->act[0], net->wtc[0], net->bias[0], net->act[1], 1.f, net->tc_err);
             for (int l = 1; l <= 4; ++l)
-                k_conv3d_tc<32, 32, true><<<gt, 256, tc_smem_bytes<32, 32>(pz), s>>>(
-                    nx, ny, nz, xs, runlen, net->act[l], net->wtc[l], net->bias[l], net->act[l + 1], net->tc_err);
+                k_conv3d_tc<32, 32, true, false><<<gt, 256, tc_smem_bytes<32, 32>(pz), s>>>(
+                    nx, ny, nz, xs, runlen, net->act[l], net->wtc[l], net->bias[l], net->act[l + 1], 1.f,
+                    net->tc_err);
         }
-        k_conv3d<32, 8, false, true, false><<<g, CNN_THREADS, conv_smem<32, 8>(), s>>>(
-            nx, ny, nz, xs, net->act[5], net->wk[5], net->linear ? nullptr : net->bias[5], net->y8, out_scale, nullptr);
+        k_conv3d_tc<32, 16, false, true><<<gt, 256, tc_smem_bytes<32, 16>(pz), s>>>(
+            nx, ny, nz, xs, runlen, net->act[5], net->wtc[5], b5, net->y8, out_scale, net->tc_err);
         net->launches += 6;
         return;
     }
@@ -1042,8 +1078,8 @@ static int cnn_sync_weights(bella_cnn *net, cudaStream_t s) {
                                           net->wk[l], net->wkT[l]);
         k_cast_bias<<<1, 32, 0, s>>>(b, net->cout[l], COUTP_L[l], net->bias[l]);
         net->launches += 2;
-        if (l < 5 && net->wtc[l]) {
-            k_wk_to_tc<<<64, 256, 0, s>>>(net->wk[l], CINP_L[l], COUTP_L[l], net->wtc[l]);
+        if (net->wtc[l]) {
+            k_wk_to_tc<<<64, 256, 0, s>>>(net->wk[l], CINP_L[l], COUTP_L[l], COUTTC_L[l], net->wtc[l]);
             net->launches += 1;
         }
     }
@@ -1096,7 +1132,7 @@ int bella_cnn_create(bella_cnn **out, int device, int block, long long capacity)
     for (int k = 0; k < 2 && ok; ++k) ok = cudaMalloc(&net->gact[k], C * 32 * 2) == cudaSuccess;
     for (float **p : {&net->y8, &net->t8, &net->g8}) ok = ok && cudaMalloc(p, C * 8 * sizeof(float)) == cudaSuccess;
     ok = ok && cudaMalloc(&net->inv_e2, C * sizeof(float)) == cudaSuccess;
-    for (int l = 0; l < 5 && ok; ++l) ok = cudaMalloc(&net->wtc[l], 27ULL * CINP_L[l] * COUTP_L[l] * 2) == cudaSuccess;
+    for (int l = 0; l < 6 && ok; ++l) ok = cudaMalloc(&net->wtc[l], 27ULL * CINP_L[l] * COUTTC_L[l] * 2) == cudaSuccess;
     ok = ok && cudaMalloc(&net->tc_err, sizeof(int)) == cudaSuccess && cudaMemset(net->tc_err, 0, sizeof(int)) == cudaSuccess;
     ok = ok && cudaMalloc(&net->loss, sizeof(double)) == cudaSuccess;
     for (float *p : {net->params, net->grads, net->adam_m, net->adam_v})
@@ -1113,8 +1149,10 @@ int bella_cnn_create(bella_cnn **out, int device, int block, long long capacity)
          big_smem(k_wgrad<32, 32, 32, 32, __nv_bfloat16>, wgrad_smem<32, 32>()) &&
          big_smem(k_wgrad<16, 8, 32, 32, __nv_bfloat16>, wgrad_smem<8, 32>()) &&
          big_smem(k_wgrad<16, 1, 32, 32, __nv_bfloat16>, wgrad_smem<1, 32>()) &&
-         big_smem(k_conv3d_tc<16, 32, false>, TC_SMEM_MAX) && big_smem(k_conv3d_tc<16, 32, true>, TC_SMEM_MAX) &&
-         big_smem(k_conv3d_tc<32, 32, false>, TC_SMEM_MAX) && big_smem(k_conv3d_tc<32, 32, true>, TC_SMEM_MAX);
+         big_smem(k_conv3d_tc<16, 32, false, false>, TC_SMEM_MAX) &&
+         big_smem(k_conv3d_tc<16, 32, true, false>, TC_SMEM_MAX) &&
+         big_smem(k_conv3d_tc<32, 32, false, false>, TC_SMEM_MAX) &&
+         big_smem(k_conv3d_tc<32, 32, true, false>, TC_SMEM_MAX) && big_smem(k_conv3d_tc<32, 16, false, true>, TC_SMEM_MAX);
     if (ok) ok = cnn_sync_weights(net, 0) == BELLA_OK && cudaDeviceSynchronize() == cudaSuccess;
     if (!ok) {
         g_cnn_err = "bella_cnn_create: allocation or attribute failed";
@@ -1326,7 +1364,7 @@ int bella_cnn_set_skip(bella_cnn *net, float omega) {
     return BELLA_OK;
 }
 
-// forward layers 0-4 on the tcgen05 tensor-core path (1) or on mma.sync (0)
+// the forward layers on the tcgen05 tensor-core path (1) or on mma.sync (0)
 int bella_cnn_set_tc(bella_cnn *net, int on) {
     if (!net) return BELLA_EINVAL;
     net->use_tc = on ? 1 : 0;

@@ -114,7 +114,7 @@ class CNN:
         return loss.value
 
     def set_tensor_cores(self, on):
-        """Forward layers 0-4 on tcgen05 (True) or mma.sync (False)."""
+        """Forward layers on tcgen05 (True) or mma.sync (False)."""
         _lib.check(self._lib.bella_cnn_set_tc(self.handle, int(bool(on))), "bella_cnn_set_tc")
 
     def tensor_core_error(self):

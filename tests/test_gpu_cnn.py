@@ -170,19 +170,20 @@ class _nullctx:
 
 
 @pytest.mark.parametrize("mode", ["relu", "linear"])
-@pytest.mark.parametrize("shape", [(16, 8, 32), (9, 10, 35), (66, 40, 130)])
-def test_tcgen05_forward_matches_mma_sync_and_oracle(mode, shape):
-    """Layers 0-4 on tcgen05 (tensor memory accumulators): same output as the
-    mma.sync kernels and the oracle, no completion wait given up."""
+@pytest.mark.parametrize("block,shape", [(2, (16, 8, 32)), (2, (9, 10, 35)), (2, (66, 40, 130)), (1, (9, 7, 21))])
+def test_tcgen05_forward_matches_mma_sync_and_oracle(mode, block, shape):
+    """All six forward layers on tcgen05 (tensor memory accumulators; the output
+    layer's 8 or 1 channels padded to 16): same output as the mma.sync kernels
+    and the oracle, no completion wait given up."""
     import torch
     from pybella_gb300.learned import CNN
     rng = np.random.default_rng(sum(shape))
-    params = _params(2, 9)
+    params = _params(block, 9)
     if mode == "linear":
         for l in range(6):
             params["b%d" % l] = np.zeros_like(params["b%d" % l])
     r = rng.standard_normal(shape).astype(np.float32)
-    net = CNN(shape, block=2, mode=mode)
+    net = CNN(shape, block=block, mode=mode)
     net.set_params(params)
     x = torch.tensor(r.ravel(), device="cuda")
     net.set_tensor_cores(False)
@@ -193,5 +194,5 @@ def test_tcgen05_forward_matches_mma_sync_and_oracle(mode, shape):
     # same BF16 operands, FP32 accumulation in another order
     assert _rel(y_tc, y_mma) < 1e-2, _rel(y_tc, y_mma)
     if shape[0] * shape[1] * shape[2] < 40000:
-        ref, _ = ocnn.forward(r, params, 2, linear=(mode == "linear"))
+        ref, _ = ocnn.forward(r, params, block, linear=(mode == "linear"))
         assert _rel(y_tc.reshape(shape), ref) < 2e-2
