@@ -1,21 +1,24 @@
 """FP64 NumPy restatement of the reference's 3D 27-point nodal operator (oracle; tests only).
 
-PARITY UNPINNED: the reference's 3D projection cannot run as shipped
-(second_projection.py:183-203 uses ``diag_inv`` and ``p2`` before assignment,
-and ``lap3D`` reshapes a C-ordered (x,y,z) vector as (z,y,x),
-laplacian.py:901 vs second_projection.py:224), so no reference output exists
-to pin against.  This restatement follows the arithmetic of ``lap3D``
-(laplacian.py:898-1026) term by term -- edge differences summed over the four
-edges of a cell, weighted by the cell's ``hplus``, summed over the four cells
-on each side of a node, the 1/16 factor, the Coriolis cross terms with
-``corrf`` and ``hcenter * p`` scaled by ``diag_inv`` -- and defines the glue
-the reference lacks with the conventions of the reference's working 2D path
-(laplacian.py:546-746): the unknowns are all inner nodes, a periodic axis
-wraps with the duplicated seam (wrap distance n-1), a wall zeroes the
-``hplus`` of the outer cell planes (as lap3D does for non-periodic axes,
-laplacian.py:933-965).  Vector order is C order over (x, y, z), z fastest
-(second_projection.py:224).  Pinned only by self-consistency tests: a
-z-invariant field reproduces the 2D 9-point operator, null modes, symmetry.
+Pinned against the reference itself: ``lap3D`` (laplacian.py:898-1026) is a
+pure function of its operands, so tests/golden/make_golden.py calls it on
+random operands (periodic/wall mixes, Coriolis cross terms) and
+tests/test_oracle_golden.py checks that ``lap3d`` below reproduces its inner
+nodes bit for bit, and ``precon_diag_3d`` its 3D ``precon_diag_prepare``.
+What cannot be pinned is the 3D projection glue, which cannot run as shipped
+(second_projection.py:183-203 uses ``diag_inv`` and ``p2`` before
+assignment); this module defines it with the conventions of the reference's
+working 2D path (laplacian.py:546-746): the unknowns are the inner nodes, a
+periodic axis wraps with the duplicated seam (wrap distance n-1), a wall
+zeroes the ``hplus`` of the outer cell planes (laplacian.py:933-965).  Two
+properties of ``lap3D`` the glue leaves behind: it takes the vector with a
+one-node halo and returns zeros on that shell, and along a periodic axis it
+overwrites inner node 0 with inner node n-1 before differencing
+(laplacian.py:927-960), so it equals ``lap3d`` on vectors whose duplicated
+seam values agree.  ``lap3D`` reshapes its vector as (z, y, x) but indexes
+its coefficients (x, y, z), consistent only for nx == nz (laplacian.py:901);
+vector order here is C order over (x, y, z), z fastest
+(second_projection.py:224).
 """
 import numpy as np
 

@@ -29,3 +29,28 @@ def rb_background(d):
     hn["S0"] = d["hydro_n_S0"].copy()
     hc["rhoY0"] = d["hydro_c_rhoY0"].copy()
     return grid, prm, hn, hc, sf
+
+
+def lap3d_case(d, tag, seam_copy=True):
+    """Operands of one ``lap3d_kat`` case for the oracle: inner nodes of the
+    halo-carrying reference vector, after lap3D's periodic seam overwrite
+    (inner node 0 <- inner node n-1, laplacian.py:927-960) when ``seam_copy``."""
+    g = lambda k: d["%s_%s" % (tag, k)]
+    m = g("meta")
+    nx, ny, nz = (int(v) for v in m[:3])
+    per = [bool(v) for v in m[3:6]]
+    dx, dy, dz, corrf = (float(v) for v in m[6:10])
+    p = g("p").copy()
+    if seam_copy:
+        for axis in range(3):
+            if per[axis]:
+                src = [slice(None)] * 3
+                dst = [slice(None)] * 3
+                src[axis], dst[axis] = -2, 1
+                p[tuple(dst)] = p[tuple(src)]
+    inner = (slice(1, -1),) * 3
+    from oracle import nodal3d as n3
+    op = n3.pack_27pt(g("hx"), g("hy"), g("hz"), g("hc"), g("dinv")[inner], nx, ny, nz, dx, dy, dz,
+                      walls=[not v for v in per], corrf=corrf)
+    y = g("y").reshape(nx + 2, ny + 2, nz + 2)
+    return op, p[inner].reshape(-1), y

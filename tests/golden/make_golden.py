@@ -3,13 +3,17 @@
 Run in a container where the reference is checked out (it is not needed at
 test time; the fixtures are committed):
 
-    python tests/golden/make_golden.py /path/to/pyBELLA
+    python tests/golden/make_golden.py /path/to/pyBELLA [--3d-only]
 
 It imports the reference through ``refshim`` (numba, h5py, ... stubbed; SciPy
 ``tol=`` keyword restored) and records:
 
 * ``lap2d_kat.npz``   -- ``lap2D_gather_new`` (laplacian.py:546-746) on random
   operands for three grids / boundary combinations, incl. Coriolis cross terms;
+* ``lap3d_kat.npz``   -- ``lap3D`` (laplacian.py:898-1026) called directly on
+  random operands: four grids (nx == nz) and boundary combinations, Coriolis
+  cross terms, the periodic seam overwrite;
+* ``diag3d_kat.npz``  -- the 3D branch of ``precon_diag_prepare``;
 * ``diag_kat.npz``    -- ``precon_diag_prepare`` (laplacian.py:1284-1356);
 * ``pieces_kat.npz``  -- ``divergence_nodes``, ``correction_nodes``,
   ``set_ghostnodes_p2`` and ``set_explicit_boundary_data`` on a random state;
@@ -85,6 +89,65 @@ def diag_kat(out):
     d = lm_lp.precon_diag_prepare(mpv, elem, node, ud, None)
     np.savez_compressed(os.path.join(out, "diag_kat.npz"), wplus=wplus, wcenter=wcenter, diag_inv=d,
                         meta=np.array([0.1, 0.07]))
+
+
+def lap3d_kat(out):
+    """``lap3D`` (laplacian.py:898-1026) called directly on random operands.
+
+    The reference's 3D projection glue cannot run (second_projection.py:183-203),
+    but ``lap3D`` itself is a pure function of its operands.  Its vector is
+    reshaped as (z, y, x) = (nz+2, ny+2, nx+2) while its coefficients are indexed
+    (x, y, z), which is consistent only for nx == nz: every case has nx == nz.
+    The vector carries the one-node halo; a periodic axis overwrites the halo and
+    the first inner node with copies (laplacian.py:927-960), so cases a-c give p
+    with the duplicated seam already equal (inner node 0 == inner node n-1) and
+    case d gives an unequal seam to record the overwrite.  lap3D zeroes the
+    hplus planes of wall axes in place: it gets copies.
+    """
+    import dycore.physics.low_mach.laplacian as lm_lp
+    rng = np.random.default_rng(4242)
+    cases = [("a", (7, 5, 7), (True, False, True), 0.3, True),
+             ("b", (6, 6, 6), (False, False, False), 0.0, True),
+             ("c", (5, 7, 5), (True, True, True), -0.2, True),
+             ("d", (6, 4, 6), (True, False, True), 0.25, False)]
+    rec = {}
+    for tag, (nx, ny, nz), per, corrf, seam in cases:
+        shp = (nx + 1, ny + 1, nz + 1)
+        hx, hy, hz = (rng.uniform(0.5, 2.0, shp) for _ in range(3))
+        hc = rng.uniform(-1.0, 0.0, (nx, ny, nz))
+        dinv = rng.uniform(-2.0, -0.5, (nx + 2, ny + 2, nz + 2))    # on the vector's nodes, halo included
+        p = rng.standard_normal((nx + 2, ny + 2, nz + 2))
+        if seam:
+            for axis in range(3):
+                if per[axis]:
+                    src = [slice(None)] * 3
+                    dst = [slice(None)] * 3
+                    src[axis], dst[axis] = -2, 1
+                    p[tuple(dst)] = p[tuple(src)]
+        dx, dy, dz = 0.11, 0.07, 0.09
+        y = lm_lp.lap3D(p.reshape(-1).copy(), hx.copy(), hy.copy(), hz.copy(), hc, 1.0 / dx ** 2,
+                        1.0 / dy ** 2, 1.0 / dz ** 2, np.array(per), dinv, corrf, 1.0 / dx, 1.0 / dz)
+        for k, v in dict(hx=hx, hy=hy, hz=hz, hc=hc, dinv=dinv, p=p, y=np.asarray(y),
+                         meta=np.array([nx, ny, nz, *[int(v) for v in per], dx, dy, dz, corrf])).items():
+            rec["%s_%s" % (tag, k)] = v
+    np.savez_compressed(os.path.join(out, "lap3d_kat.npz"), **rec)
+
+
+def diag3d_kat(out):
+    """3D branch of ``precon_diag_prepare`` (laplacian.py:1284-1356)."""
+    import dycore.physics.low_mach.laplacian as lm_lp
+    import dycore.utils.options as opts
+    rng = np.random.default_rng(98)
+    nx, ny, nz = 9, 6, 8
+    wplus = rng.uniform(0.5, 2.0, (3, nx + 1, ny + 1, nz + 1))
+    wcenter = rng.uniform(-1.0, 0.0, (nx, ny, nz))
+    mpv = types.SimpleNamespace(wplus=wplus, wcenter=wcenter)
+    node = types.SimpleNamespace(dx=0.1, dy=0.07, dz=0.13, igs=[2, 2, 2])
+    elem = types.SimpleNamespace(ndim=3)
+    ud = types.SimpleNamespace(bdry_type=[opts.BdryType.PERIODIC, opts.BdryType.WALL, opts.BdryType.PERIODIC])
+    d = lm_lp.precon_diag_prepare(mpv, elem, node, ud, None)
+    np.savez_compressed(os.path.join(out, "diag3d_kat.npz"), wplus=wplus, wcenter=wcenter, diag_inv=d,
+                        meta=np.array([0.1, 0.07, 0.13]))
 
 
 def _rb_setup():
@@ -272,6 +335,11 @@ def main():
     ref = args[0] if args else "/root/reference"
     refshim.install(ref)
     out = HERE
+    lap3d_kat(out)
+    diag3d_kat(out)
+    if "--3d-only" in sys.argv:
+        print("fixtures written to", out)
+        return
     lap2d_kat(out)
     diag_kat(out)
     pieces_kat(out)

@@ -1,7 +1,9 @@
-"""GPU parity of the 3D 27-point operator and solves against the 3D oracle.
+"""GPU parity of the 3D 27-point operator and solves.
 
-The reference's 3D glue cannot run, so these comparisons are against the
-oracle's restatement of lap3D (parity unpinned, see oracle/nodal3d.py).
+The operator is compared with the reference's own ``lap3D`` outputs on random
+operands (tests/golden/lap3d_kat.npz) and with the oracle's restatement of it,
+which reproduces those outputs bit for bit; the reference's 3D projection glue
+cannot run, so solves are compared with the oracle's scipy-semantics BiCGStab.
 """
 import numpy as np
 import pytest
@@ -43,6 +45,21 @@ def test_apply3d_f64_f32_vs_oracle(shape, walls, corrf, hc):
     A = _dev_op(op)
     p = rng.standard_normal(A.n)
     ref = n3.lap3d(p, op)
+    assert _rel(A.matvec(p), ref) < 1e-13
+    y32 = A.matvec_f32(torch.tensor(p, dtype=torch.float32, device="cuda")).double().cpu().numpy()
+    assert _rel(y32, ref) < 5e-6
+
+
+@pytest.mark.parametrize("tag", ["a", "b", "c", "d"])
+def test_apply3d_vs_reference_lap3d_kat(tag):
+    """The device operator on the operands the reference's lap3D was called with
+    (tests/golden/lap3d_kat.npz): FP64 within 1e-13 of the reference's output,
+    FP32 within its rounding."""
+    import torch
+    from conftest import golden, lap3d_case
+    op, p, y = lap3d_case(np.load(golden("lap3d_kat.npz")), tag)
+    ref = y[1:-1, 1:-1, 1:-1].reshape(-1)
+    A = _dev_op(op)
     assert _rel(A.matvec(p), ref) < 1e-13
     y32 = A.matvec_f32(torch.tensor(p, dtype=torch.float32, device="cuda")).double().cpu().numpy()
     assert _rel(y32, ref) < 5e-6

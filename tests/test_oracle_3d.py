@@ -1,7 +1,8 @@
-"""Self-consistency of the 3D 27-point oracle (the reference's 3D path cannot run).
+"""Self-consistency of the 3D 27-point oracle and of the background inverses.
 
-Parity of the 3D operator is unpinned: these tests pin it to the reference's
-working 2D operator and to structural properties instead.
+The operator itself is pinned against the reference's ``lap3D`` outputs in
+tests/test_oracle_golden.py; these tests add its relation to the 2D operator
+and structural properties (null modes, symmetry).
 """
 import numpy as np
 import pytest

@@ -7,8 +7,8 @@ arithmetic in the same operation order, so most comparisons are exact.
 import numpy as np
 import pytest
 
-from conftest import golden
-from oracle import cases, nodal2d as n2
+from conftest import golden, lap3d_case
+from oracle import cases, nodal2d as n2, nodal3d as n3
 from oracle.krylov import bicgstab_legacy, true_relres
 
 FIELDS = ["rho", "rhou", "rhov", "rhow", "rhoY", "rhoX"]
@@ -31,6 +31,40 @@ def test_precon_diag_matches_reference_kat():
     dx, dy = d["meta"]
     out = n2.precon_diag_prepare(d["wplus"], d["wcenter"], dx, dy)
     np.testing.assert_array_equal(out, d["diag_inv"])
+
+
+@pytest.mark.parametrize("tag", ["a", "b", "c", "d"])
+def test_lap3d_matches_reference_kat(tag):
+    """The reference's lap3D on random operands (periodic/wall mixes, Coriolis
+    cross terms): the oracle reproduces the inner nodes bit for bit and the
+    reference's outer node shell is zero."""
+    d = np.load(golden("lap3d_kat.npz"))
+    op, p, y = lap3d_case(d, tag)
+    np.testing.assert_array_equal(n3.lap3d(p, op).reshape(y[1:-1, 1:-1, 1:-1].shape), y[1:-1, 1:-1, 1:-1])
+    shell = y.copy()
+    shell[1:-1, 1:-1, 1:-1] = 0.0
+    assert not shell.any()
+
+
+def test_lap3d_reference_overwrites_the_periodic_seam():
+    """Case d has unequal seam values: lap3D replaces inner node 0 by inner node
+    n-1 along each periodic axis before differencing, so its output is the
+    operator applied to the seam-copied vector, not to the vector given."""
+    d = np.load(golden("lap3d_kat.npz"))
+    op, p_raw, y = lap3d_case(d, "d", seam_copy=False)
+    _, p_seam, _ = lap3d_case(d, "d")
+    inner = y[1:-1, 1:-1, 1:-1].reshape(-1)
+    assert not np.array_equal(p_raw, p_seam)
+    np.testing.assert_array_equal(n3.lap3d(p_seam, op), inner)
+    assert not np.allclose(n3.lap3d(p_raw, op), inner)
+
+
+def test_precon_diag_3d_matches_reference_kat():
+    d = np.load(golden("diag3d_kat.npz"))
+    dx, dy, dz = d["meta"]
+    w = d["wplus"]
+    out = n3.precon_diag_3d(w[0], w[1], w[2], d["wcenter"], dx, dy, dz)
+    np.testing.assert_allclose(out, d["diag_inv"], rtol=1e-14, atol=0)
 
 
 def _small_rb_state():
