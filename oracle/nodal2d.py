@@ -261,16 +261,22 @@ def operator_coefficients_nodes(Sol, S0n, grid, prm, dt):
 
 
 def scale_wall_node_values(a, grid, factor=0.5):
-    """``scale_wall_node_values`` (second_projection.py:433-474) on a node.isc array."""
+    """``scale_wall_node_values`` (second_projection.py:433-474) on a node.isc array (2D or 3D).
+
+    The index starts as ``[igs:-igs]`` on every axis; each wall axis in turn is
+    set to row -2, then row 1, and scaled there -- and is left at row 1, so a
+    later wall axis scales only the entries on row 1 of the earlier ones (with
+    walls in x and y, the y-wall rows are scaled at x row 1 alone).
+    """
     ig = grid.igs
-    for dim in range(2):
+    nd = a.ndim
+    idx = [slice(ig[d], -ig[d]) for d in range(nd)]
+    for dim in range(nd):
         if grid.bdry[dim] in (WALL, RAYLEIGH):
             for direction in (-1, 1):
-                w = (ig[dim] - 1) * direction
+                idx[dim] = (ig[dim] - 1) * direction
                 if direction == -1:
-                    w -= 1
-                idx = [slice(ig[0], -ig[0]), slice(ig[1], -ig[1])]
-                idx[dim] = w
+                    idx[dim] -= 1
                 a[tuple(idx)] *= factor
 
 

@@ -16,6 +16,29 @@ enum { M_APPLY = 0, M_RESID = 1, M_PDIR = 2, M_SDIR = 3 };
 // side (||b|| ~ 4e-5 at 2049x1025) near convergence for no numerical reason.
 
 // after v = A p:  alpha = rho / <r^, v>
+// scale_wall_node_values (second_projection.py:433-474): the factor that entry c of
+// a node.isc array of extents n (nd axes, two ghost layers) receives.  The reference
+// walks the wall axes in order, scales row n-2 then row 1 of each, and leaves that
+// axis's index at row 1, so a later wall axis scales only the entries on row 1 of
+// every earlier wall axis; the other axes run over [2, n-3].
+__device__ __forceinline__ double wall_scale(int nd, const int *c, const int *n, const int *wall, double f) {
+    double s = 1.0;
+    for (int d = 0; d < nd; ++d) {
+        if (!wall[d]) continue;
+        for (int t = 0; t < 2; ++t) {
+            const int row = t == 0 ? n[d] - 2 : 1;
+            bool hit = true;
+            for (int e = 0; e < nd; ++e) {
+                if (e == d) hit = hit && c[e] == row;
+                else if (e < d && wall[e]) hit = hit && c[e] == 1;
+                else hit = hit && c[e] >= 2 && c[e] <= n[e] - 3;
+            }
+            if (hit) s *= f;
+        }
+    }
+    return s;
+}
+
 __device__ __forceinline__ void finalize_pdir(KState *ks, double rv) {
     if (!isfinite(rv)) { ks->status = BELLA_NONFINITE; ks->done = 1; return; }
     if (rv == 0.0) { ks->status = BELLA_BREAKDOWN; ks->pad[0] = 3; ks->done = 1; return; }

@@ -185,9 +185,11 @@ __global__ void k_coeff_nodes(ProjDev P, const double *rhoYC, const double *wplu
     const double s = pow(rhoYC[cidx(P, a, b)], cexp) + pow(rhoYC[cidx(P, a + 1, b)], cexp) +
                      pow(rhoYC[cidx(P, a, b + 1)], cexp) + pow(rhoYC[cidx(P, a + 1, b + 1)], cexp);
     double wc = ccenter * s / 4.0;
-    // scale_wall_node_values(wcenter, 0.5) on the node rows next to a wall (second_projection.py:433-474)
-    if (P.ybc == 1 && (b == 1 || b == niy - 2) && a >= 2 && a <= nix - 3) wc *= 0.5;
-    if (P.xbc == 1 && (a == 1 || a == nix - 2) && b >= 2 && b <= niy - 3) wc *= 0.5;
+    // scale_wall_node_values(wcenter, 0.5) on the node rows next to a wall (second_projection.py:356)
+    {
+        const int c[2] = {a, b}, n[2] = {nix, niy}, wall[2] = {P.xbc, P.ybc};
+        wc *= wall_scale(2, c, n, wall, 0.5);
+    }
     if (P.is_compressible != 1) wc *= P.compressibility;          // :147-153
     const double S = wplus0[cidx(P, a, b)] + wplus0[cidx(P, a + 1, b)] + wplus0[cidx(P, a, b + 1)] +
                      wplus0[cidx(P, a + 1, b + 1)];
@@ -334,7 +336,7 @@ struct ExplDev {
 };
 
 // divergence_nodes without the 1/dt (:39) and scale_wall_node_values(rhs, 2.0) (:40,
-// second_projection.py:433-474: rows 1 and -2 of a wall axis, the other axis [2:-2])
+// second_projection.py:433-474, wall_scale)
 __global__ void k_fw_div(ProjDev P, const double *rho, const double *rhou, const double *rhov, const double *rhoY,
                          double *div) {
     const int nix = P.icx - 1, niy = P.icy - 1;
@@ -348,8 +350,10 @@ __global__ void k_fw_div(ProjDev P, const double *rho, const double *rhou, const
     const double e0 = (qv(a, b + 1) - qv(a, b)) / P.dy;
     const double e1 = (qv(a + 1, b + 1) - qv(a + 1, b)) / P.dy;
     double v = 0.5 * (d0 + d1) + 0.5 * (e0 + e1);
-    if (P.xbc == 1 && (a == 1 || a == nix - 2) && b >= 2 && b < niy - 2) v *= 2.0;
-    if (P.ybc == 1 && (b == 1 || b == niy - 2) && a >= 2 && a < nix - 2) v *= 2.0;
+    {
+        const int c[2] = {a, b}, n[2] = {nix, niy}, wall[2] = {P.xbc, P.ybc};
+        v *= wall_scale(2, c, n, wall, 2.0);
+    }
     div[e] = v;
 }
 

@@ -14,6 +14,8 @@ It imports the reference through ``refshim`` (numba, h5py, ... stubbed; SciPy
   random operands: four grids (nx == nz) and boundary combinations, Coriolis
   cross terms, the periodic seam overwrite;
 * ``diag3d_kat.npz``  -- the 3D branch of ``precon_diag_prepare``;
+* ``wall_kat.npz``    -- ``scale_wall_node_values`` for wall/periodic mixes in
+  2D and 3D (its index carries over between wall axes);
 * ``diag_kat.npz``    -- ``precon_diag_prepare`` (laplacian.py:1284-1356);
 * ``pieces_kat.npz``  -- ``divergence_nodes``, ``correction_nodes``,
   ``set_ghostnodes_p2`` and ``set_explicit_boundary_data`` on a random state;
@@ -148,6 +150,29 @@ def diag3d_kat(out):
     d = lm_lp.precon_diag_prepare(mpv, elem, node, ud, None)
     np.savez_compressed(os.path.join(out, "diag3d_kat.npz"), wplus=wplus, wcenter=wcenter, diag_inv=d,
                         meta=np.array([0.1, 0.07, 0.13]))
+
+
+def wall_kat(out):
+    """``scale_wall_node_values`` (second_projection.py:433-474) on random node.isc
+    arrays for every wall/periodic mix in 2D and several in 3D."""
+    import dycore.physics.low_mach.second_projection as lm_sp
+    import dycore.utils.options as opts
+    W, P = opts.BdryType.WALL, opts.BdryType.PERIODIC
+    rng = np.random.default_rng(5)
+    rec = {}
+    cases = [("ww", (W, W), (9, 7)), ("pw", (P, W), (9, 7)), ("wp", (W, P), (8, 9)),
+             ("pwp", (P, W, P), (8, 7, 9)), ("www", (W, W, W), (8, 7, 9)), ("wwp", (W, W, P), (7, 8, 6)),
+             ("pww", (P, W, W), (7, 8, 6))]
+    for tag, bt, shp in cases:
+        a = rng.uniform(0.5, 1.5, shp)
+        rec[tag + "_in"] = a.copy()
+        node = types.SimpleNamespace(ndim=len(shp), igs=[2] * len(shp))
+        for f, name in ((0.5, "half"), (2.0, "two")):
+            b = a.copy()
+            lm_sp.scale_wall_node_values(b, node, types.SimpleNamespace(bdry_type=list(bt)), f)
+            rec["%s_%s" % (tag, name)] = b
+        rec[tag + "_walls"] = np.array([int(v == W) for v in bt])
+    np.savez_compressed(os.path.join(out, "wall_kat.npz"), **rec)
 
 
 def _rb_setup():
@@ -337,6 +362,7 @@ def main():
     out = HERE
     lap3d_kat(out)
     diag3d_kat(out)
+    wall_kat(out)
     if "--3d-only" in sys.argv:
         print("fixtures written to", out)
         return

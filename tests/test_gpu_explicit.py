@@ -77,6 +77,34 @@ def test_expl_part_matches_reference(tag):
         _close(keep[f].cpu().numpy(), d["%s_ex_%s" % (tag, f)], f)
 
 
+def test_euler_forward_two_walls_vs_oracle():
+    """Walls in x and y: the divergence's wall rows are doubled by
+    scale_wall_node_values, whose index carries over from the x wall to the y
+    wall (pinned in tests/test_oracle_golden.py); device against the oracle."""
+    import torch
+    from pybella_gb300 import _lib
+    from oracle import nodal2d as n2
+    d = np.load(golden("explicit_kat.npz"))
+    keep = {}
+    a = _args(d, "a", keep)
+    a.x_wall = 1
+    lib = _lib.load()
+    assert lib.bella_euler_forward2d(ctypes.byref(a), None) == 0
+    torch.cuda.synchronize()
+    sc = d["a_scalars"]
+    grid = n2.Grid2D(64, 32, -1.0, 1.0, 0.0, 1.0, (n2.WALL, n2.WALL))
+    prm = n2.Params(Msq=sc[0], g=sc[1], gamm=sc[2], coriolis=sc[7:10], nonhydro=sc[3],
+                    is_compressible=int(sc[5]), compressibility=sc[4])
+    Sol = {f: d["a_in_" + f].copy() for f in FIELDS}
+    p2 = d["a_p2_in"].copy()
+    div = n2.euler_forward_non_advective(Sol, p2, d["a_S0c"], d["a_S0n"], grid, prm, float(sc[6]),
+                                         dict(rhoY0=d["a_rhoY0"]), lambda y: 1.0)
+    _close(keep["rhs"].cpu().numpy(), div, "rhs")
+    for f in FIELDS:
+        _close(keep[f].cpu().numpy(), Sol[f], f)
+    _close(keep["p2"].cpu().numpy(), p2, "p2")
+
+
 def test_explicit_parts_time(capsys):
     """Device time of both explicit parts at 640x320 cells (the largest ensemble grid)."""
     import torch

@@ -67,6 +67,21 @@ def test_precon_diag_3d_matches_reference_kat():
     np.testing.assert_allclose(out, d["diag_inv"], rtol=1e-14, atol=0)
 
 
+@pytest.mark.parametrize("tag", ["ww", "pw", "wp", "pwp", "www", "wwp", "pww"])
+def test_scale_wall_node_values_matches_reference_kat(tag):
+    """Wall/periodic mixes in 2D and 3D, factors 0.5 and 2: with two wall axes the
+    reference's index carries over, and the oracle reproduces that."""
+    import types
+    d = np.load(golden("wall_kat.npz"))
+    a = d[tag + "_in"]
+    grid = types.SimpleNamespace(igs=[2] * a.ndim,
+                                 bdry=[n2.WALL if w else n2.PERIODIC for w in d[tag + "_walls"]])
+    for f, name in ((0.5, "half"), (2.0, "two")):
+        b = a.copy()
+        n2.scale_wall_node_values(b, grid, f)
+        np.testing.assert_array_equal(b, d["%s_%s" % (tag, name)])
+
+
 def _small_rb_state():
     d = np.load(golden("pieces_kat.npz"))
     inx, iny, dt = d["meta"]
