@@ -54,3 +54,23 @@ def lap3d_case(d, tag, seam_copy=True):
                       walls=[not v for v in per], corrf=corrf)
     y = g("y").reshape(nx + 2, ny + 2, nz + 2)
     return op, p[inner].reshape(-1), y
+
+
+def proj3d_case(d, tag):
+    """Grid, parameters and backgrounds of one ``proj3d_kat`` case for the oracle:
+    ``(grid, prm, dt, S0n, hydro_c, strat_fn)``.  The state is the reference's
+    rising-bubble domain extended to z in [-1, 1] (stratification 1)."""
+    import numpy as np
+    from oracle import nodal2d as n2, proj3d as o3
+    m = d[tag + "_meta"]
+    inx, iny, inz = (int(v) for v in m[:3])
+    walls = [bool(v) for v in m[3:6]]
+    dx, dy, dz, dt, Msq, g, gamm, nonhydro, comp, is_comp = (float(v) for v in m[6:16])
+    grid = o3.Grid3D(inx, iny, inz, -1.0, 1.0, 0.0, 1.0, -1.0, 1.0,
+                     bdry=[n2.WALL if w else n2.PERIODIC for w in walls])
+    assert np.allclose((grid.dx, grid.dy, grid.dz), (dx, dy, dz), rtol=1e-15, atol=0)
+    prm = n2.Params(Msq=Msq, g=g, gamm=gamm, coriolis=m[16:19], nonhydro=nonhydro, is_compressible=int(is_comp),
+                    compressibility=comp)
+    sinv = d[tag + "_strat_inv"]
+    assert np.all(sinv == 1.0)
+    return grid, prm, dt, d[tag + "_S0n"], dict(rhoY0=d[tag + "_rhoY0"]), (lambda y: 1.0)

@@ -16,6 +16,8 @@ It imports the reference through ``refshim`` (numba, h5py, ... stubbed; SciPy
 * ``diag3d_kat.npz``  -- the 3D branch of ``precon_diag_prepare``;
 * ``wall_kat.npz``    -- ``scale_wall_node_values`` for wall/periodic mixes in
   2D and 3D (its index carries over between wall axes);
+* ``proj3d_kat.npz``  -- the projection pieces in 3D (boundary data,
+  coefficients, divergence, ghost nodes, correction) on two small states;
 * ``diag_kat.npz``    -- ``precon_diag_prepare`` (laplacian.py:1284-1356);
 * ``pieces_kat.npz``  -- ``divergence_nodes``, ``correction_nodes``,
   ``set_ghostnodes_p2`` and ``set_explicit_boundary_data`` on a random state;
@@ -173,6 +175,79 @@ def wall_kat(out):
             rec["%s_%s" % (tag, name)] = b
         rec[tag + "_walls"] = np.array([int(v == W) for v in bt])
     np.savez_compressed(os.path.join(out, "wall_kat.npz"), **rec)
+
+
+def proj3d_kat(out):
+    """The reference's projection pieces on small 3D states (they are
+    dimension-generic; only the step's glue is broken in 3D).
+
+    Case a: periodic x / wall y / periodic z, no Coriolis, pseudo-incompressible.
+    Case b: wall x / wall y / periodic z, Coriolis, compressible ghost cells.
+    The state is the rising bubble's hydrostatic background in 3D with seeded
+    perturbations; each piece runs on a copy of the state left by the previous
+    one, as in the projection step."""
+    import copy
+    import dycore.discretisation.grid as dis_grid
+    import dycore.utils.variable as var
+    import dycore.physics.low_mach.mpv as lm_var
+    import dycore.physics.gas_dynamics.thermodynamic as gd_thermodynamics
+    import dycore.physics.low_mach.second_projection as lm_sp
+    import dycore.physics.hydrostatics as hydrostatic
+    import dycore.utils.boundary as bdry
+    import dycore.utils.options as opts
+    W, P = opts.BdryType.WALL, opts.BdryType.PERIODIC
+    rec = {}
+    cases = [("a", (P, W, P), (0.0, 0.0, 0.0), 0, 0.01, 71),
+             ("b", (W, W, P), (3.0, 2.0, 1.0), 1, 0.05, 72)]
+    for tag, bt, cor, is_comp, dt, seed in cases:
+        rng = np.random.default_rng(seed)
+        ud = _ud_rising_bubble()
+        ud.inx, ud.iny, ud.inz = 9, 7, 8
+        ud.zmin, ud.zmax = -1.0, 1.0
+        ud.bdry_type = np.array(list(bt))
+        ud.coriolis_strength = np.array(cor)
+        ud.is_compressible = is_comp
+        elem, node = dis_grid.grid_init(ud)
+        ud.nonhydrostasy = 1.0
+        Sol = var.Vars(elem.sc, ud)
+        th = gd_thermodynamics.init(ud)
+        mpv = lm_var.MPV(elem, node, ud)
+        hydrostatic.state(mpv, elem, node, th, ud)
+        rhoY = np.broadcast_to(mpv.HydroState.rhoY0.reshape(1, -1, 1), elem.sc)
+        yy = np.broadcast_to(elem.y.reshape(1, -1, 1), elem.sc)
+        Sol.rhoY[...] = rhoY * (1.0 + 0.001 * rng.standard_normal(elem.sc))
+        Sol.rho[...] = rhoY / ud.stratification(yy) * (1.0 + 0.01 * rng.standard_normal(elem.sc))
+        for k in ("rhou", "rhov", "rhow", "rhoX"):
+            getattr(Sol, k)[...] = 0.01 * rng.standard_normal(elem.sc)
+        for k in FIELDS:
+            rec["%s_in_%s" % (tag, k)] = np.copy(getattr(Sol, k))
+        bdry.set_explicit_boundary_data(Sol, elem, ud, th, mpv)
+        for k in FIELDS:
+            rec["%s_bd_%s" % (tag, k)] = np.copy(getattr(Sol, k))
+        S = copy.deepcopy(Sol)
+        lm_sp.operator_coefficients_nodes(elem, node, S, mpv, ud, th, dt)
+        rec[tag + "_wplus"] = np.copy(mpv.wplus)
+        rec[tag + "_wcenter"] = np.copy(mpv.wcenter)
+        rhs = lm_sp.divergence_nodes(np.zeros(node.sc), elem, node, S, ud)
+        rec[tag + "_div"] = np.copy(rhs)
+        for k in ("rhou", "rhov", "rhow"):
+            rec["%s_dv_%s" % (tag, k)] = np.copy(getattr(S, k))
+        p = rng.standard_normal(node.sc)
+        rec[tag + "_p"] = np.copy(p)
+        q = np.copy(p)
+        bdry.set_ghostnodes_p2(q, node, ud)
+        rec[tag + "_gn"] = q
+        S = copy.deepcopy(Sol)
+        lm_sp.correction_nodes(S, elem, node, mpv, q, dt, ud, th, 1)
+        for k in FIELDS:
+            rec["%s_cr_%s" % (tag, k)] = np.copy(getattr(S, k))
+        rec[tag + "_S0n"] = np.copy(mpv.HydroState_n.S0)
+        rec[tag + "_rhoY0"] = np.copy(mpv.HydroState.rhoY0)
+        rec[tag + "_strat_inv"] = np.array([1.0 / ud.stratification(y) for y in elem.y])
+        rec[tag + "_meta"] = np.array([ud.inx, ud.iny, ud.inz, int(bt[0] == W), int(bt[1] == W), int(bt[2] == W),
+                                       node.dx, node.dy, node.dz, dt, ud.Msq, ud.gravity_strength[1], th.gamm,
+                                       ud.nonhydrostasy, ud.compressibility, is_comp, *cor])
+    np.savez_compressed(os.path.join(out, "proj3d_kat.npz"), **rec)
 
 
 def _rb_setup():
@@ -363,6 +438,7 @@ def main():
     lap3d_kat(out)
     diag3d_kat(out)
     wall_kat(out)
+    proj3d_kat(out)
     if "--3d-only" in sys.argv:
         print("fixtures written to", out)
         return
