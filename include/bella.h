@@ -179,6 +179,39 @@ typedef struct bella_proj2d {
 int bella_projection2d(bella_ws *ws, const bella_proj2d *args, const bella_solve_opts *opts,
                        bella_solve_stats *stats, void *stream);
 
+/* ---- the whole 3D projection on the device -------------------------------
+ * euler_backward_non_advective_impl_part (second_projection.py:97-277) in 3D.
+ * The reference's pieces run in 3D (boundary.py:7-369; second_projection.py:
+ * 280-356, 496-575, 604-646, with divergence_nodes' 3D sign on the x term, :563),
+ * its step does not (:183-203 use diag_inv and p2 unassigned); this entry point
+ * assembles it with the glue of the 2D branch: unknowns the inner nodes
+ * (inx*iny*inz, C order over x, y, z, :224), the 27-point operator of lap3D
+ * (laplacian.py:898-1026) on the cells around them with corrf = dt *
+ * coriolis[0], the 3D precon_diag_prepare, rhs = divergence / dt * diag_inv.
+ * Arrays: the reference's NumPy C order over (x, y, z), ghosts included: cells
+ * (inx+3)(iny+3)(inz+3), p2 on nodes (inx+4)(iny+4)(inz+4), rhs_out (mpv.rhs)
+ * on node.isc (inx+2)(iny+2)(inz+2).  Gravity along y.  precond 0: the solve of
+ * opts->precision (bella_bicgstab); 1: flexible BiCGStab preconditioned by the
+ * background solve (bella_spectral3d, y must be a wall), set up per call. */
+typedef struct bella_proj3d {
+    int inx, iny, inz;            /* grid nodes per direction (ud.inx, ud.iny, ud.inz) */
+    int x_wall, y_wall, z_wall;   /* 0: periodic, 1: wall                              */
+    double dx, dy, dz, dt;
+    double Msq, g, gamm, nonhydro, compressibility;
+    double coriolis[3];           /* ud.coriolis_strength                             */
+    int is_compressible;
+    int precond;
+    double *rho, *rhou, *rhov, *rhow, *rhoY, *rhoX;          /* Sol                    */
+    double *rho0, *rhou0, *rhov0, *rhow0, *rhoY0, *rhoX0;    /* Sol0 or all NULL       */
+    double *p2;                   /* mpv.p2_nodes                                     */
+    const double *hydro_rhoY0;    /* mpv.HydroState.rhoY0 (iny+3 cell planes)          */
+    const double *S0n;            /* mpv.HydroState_n.S0 (iny+4 node planes)           */
+    const double *strat_inv;      /* 1/ud.stratification(elem.y) (iny+3)               */
+    double *rhs_out;              /* mpv.rhs (inx+2)(iny+2)(inz+2) or NULL             */
+} bella_proj3d;
+int bella_projection3d(bella_ws *ws, const bella_proj3d *args, const bella_solve_opts *opts,
+                       bella_solve_stats *stats, void *stream);
+
 /* ---- explicit parts of the projection (2D), in place on device arrays ------
  * Arrays as in bella_proj2d (reference NumPy C order over (x, y), ghosts
  * included).  S0c: mpv.HydroState.get_S0c(elem) on cells; S0n, hydro_rhoY0,

@@ -75,6 +75,40 @@ def rising_bubble(inx=161, iny=81, delth=2.0, x0=0.0, y0=0.2, r0=0.2, tol=1e-10)
     return grid, prm, Sol, p2, hn, hc, strat_fn
 
 
+def bubble_3d(inx=65, iny=33, inz=65, seed=0, delth=2.0, y0=0.2, r0=0.2, wind=0.05, tol=1e-10,
+              bdry=(n2.PERIODIC, n2.WALL, n2.PERIODIC), coriolis=(0.0, 0.0, 0.0), compressible=False):
+    """A 3D projection input: the rising bubble's background and warm bubble
+    (rising_bubble.py:42-98, centred at x = z = 0) on x, z in [-1, 1], y in
+    [0, 1], with seeded smooth momenta (k^-3 spectrum, amplitude ``wind``
+    times rho) so that the divergence is not zero.
+
+    Returns ``(grid, prm, Sol, p2_nodes, hydro_n, hydro_c, strat_fn)``.
+    """
+    from oracle import proj3d as o3
+    rng = np.random.default_rng(seed)
+    grid = o3.Grid3D(inx, iny, inz, -1.0, 1.0, 0.0, 1.0, -1.0, 1.0, bdry)
+    Msq, g, _ = _derived(grav=10.0, t_ref=1000.0)
+    prm = n2.Params(Msq=Msq, g=g, gamm=GAMM, coriolis=coriolis, nonhydro=1.0,
+                    is_compressible=1 if compressible else 0, compressibility=1.0 if compressible else 0.0,
+                    tol=tol, max_iterations=100000)
+    g2 = n2.Grid2D(inx, iny, -1.0, 1.0, 0.0, 1.0)
+    hn, hc = hydro_state(g2, prm)
+    strat_fn = lambda y: 1.0                                # user_data.py:181-183
+    ex = -1.0 - 2 * grid.dx + 0.5 * grid.dx + grid.dx * np.arange(grid.elem_sc[0])
+    ez = -1.0 - 2 * grid.dz + 0.5 * grid.dz + grid.dz * np.arange(grid.elem_sc[2])
+    X, Yg, Z = np.meshgrid(ex, grid.elem_y, ez, indexing="ij")
+    r = np.sqrt(X ** 2 + (Yg - y0) ** 2 + Z ** 2) / r0
+    pert = (delth / 300.0) * (np.cos(0.5 * np.pi * r) ** 2)
+    pert[np.where(r > 1.0)] = 0.0
+    rhoY = np.broadcast_to(hc["rhoY0"][None, :, None], grid.elem_sc).copy()
+    rho = rhoY / (strat_fn(Yg) + pert)
+    mom = [wind * rho * _kminus3_field(grid.elem_sc, rng) for _ in range(3)]
+    Sol = dict(rho=rho, rhou=mom[0], rhov=mom[1], rhow=mom[2], rhoY=rhoY, rhoX=np.zeros(grid.elem_sc))
+    p2 = np.zeros(grid.node_sc)
+    o3.set_explicit_boundary_data(Sol, grid, prm, hc, strat_fn)
+    return grid, prm, Sol, p2, hn, hc, strat_fn
+
+
 # --------------------------------------------------------------------------
 # standalone solves on a stratified background
 # --------------------------------------------------------------------------

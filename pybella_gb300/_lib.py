@@ -52,6 +52,19 @@ class Proj2D(ctypes.Structure):
                             "p2", "hydro_rhoY0", "S0n", "strat_inv", "rhs_out")]
 
 
+class Proj3D(ctypes.Structure):
+    """``bella_proj3d``: device arrays of one 3D projection (reference layout)."""
+    _fields_ = [("inx", ctypes.c_int), ("iny", ctypes.c_int), ("inz", ctypes.c_int),
+                ("x_wall", ctypes.c_int), ("y_wall", ctypes.c_int), ("z_wall", ctypes.c_int),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double), ("dt", ctypes.c_double),
+                ("Msq", ctypes.c_double), ("g", ctypes.c_double), ("gamm", ctypes.c_double),
+                ("nonhydro", ctypes.c_double), ("compressibility", ctypes.c_double),
+                ("coriolis", ctypes.c_double * 3), ("is_compressible", ctypes.c_int), ("precond", ctypes.c_int)] + \
+        [(k, _dp) for k in ("rho", "rhou", "rhov", "rhow", "rhoY", "rhoX",
+                            "rho0", "rhou0", "rhov0", "rhow0", "rhoY0", "rhoX0",
+                            "p2", "hydro_rhoY0", "S0n", "strat_inv", "rhs_out")]
+
+
 class Expl2D(ctypes.Structure):
     _fields_ = [("inx", ctypes.c_int), ("iny", ctypes.c_int), ("x_wall", ctypes.c_int), ("y_wall", ctypes.c_int),
                 ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dt", ctypes.c_double),
@@ -102,6 +115,8 @@ SIGNATURES = {
     "bella_bicgstab": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, ctypes.POINTER(SolveOpts),
                                       ctypes.POINTER(SolveStats), ctypes.c_void_p]),
     "bella_projection2d": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Proj2D), ctypes.POINTER(SolveOpts),
+                                          ctypes.POINTER(SolveStats), ctypes.c_void_p]),
+    "bella_projection3d": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Proj3D), ctypes.POINTER(SolveOpts),
                                           ctypes.POINTER(SolveStats), ctypes.c_void_p]),
     "bella_cnn_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int,
                                         ctypes.c_longlong]),

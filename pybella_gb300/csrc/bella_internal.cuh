@@ -16,6 +16,28 @@ enum { M_APPLY = 0, M_RESID = 1, M_PDIR = 2, M_SDIR = 3 };
 // side (||b|| ~ 4e-5 at 2049x1025) near convergence for no numerical reason.
 
 // after v = A p:  alpha = rho / <r^, v>
+// nu and the implicit Coriolis / buoyancy factors on cells (second_projection.py:609-633)
+struct CorCoef { double uu, uv, uw, vu, vv, vw, wu, wv, ww, denom; };
+
+// P: the projection parameters of either dimension (dt, g, Msq, nonhydro, wh1, wv, wh2)
+template <class PD>
+__device__ __forceinline__ CorCoef cor_coef(const PD &P, double Y, double strat) {
+    const double nonhydro = P.nonhydro, wh1 = P.wh1, wv = P.wv, wh2 = P.wh2;
+    const double nu = -P.dt * P.dt * (P.g / P.Msq) * strat * Y;
+    CorCoef c;
+    c.denom = 1.0 / (wh1 * wh1 + wh2 * wh2 + (nu + nonhydro) * (wv * wv + 1.0));
+    c.uu = (wh1 * wh1 + nu + nonhydro);
+    c.uv = nonhydro * (wh1 * wv + wh2);
+    c.uw = (wh1 * wh2 - (nu + nonhydro) * wv);
+    c.vu = (wh1 * wv - wh2);
+    c.vv = nonhydro * (1.0 + wv * wv);
+    c.vw = (wh2 * wv + wh1);
+    c.wu = (wh1 * wh2 + (nu + nonhydro) * wv);
+    c.wv = nonhydro * (wh2 * wv - wh1);
+    c.ww = (nu + nonhydro + wh2 * wh2);
+    return c;
+}
+
 // scale_wall_node_values (second_projection.py:433-474): the factor that entry c of
 // a node.isc array of extents n (nd axes, two ghost layers) receives.  The reference
 // walks the wall axes in order, scales row n-2 then row 1 of each, and leaves that

@@ -120,26 +120,6 @@ __global__ void k_bd_y(ProjDev P, double *rho, double *rhou, double *rhov, doubl
     }
 }
 
-// nu and the implicit Coriolis / buoyancy factors on cells (second_projection.py:609-633)
-struct CorCoef { double uu, uv, uw, vu, vv, vw, wu, wv, ww, denom; };
-
-__device__ __forceinline__ CorCoef cor_coef(const ProjDev &P, double Y, double strat) {
-    const double nonhydro = P.nonhydro, wh1 = P.wh1, wv = P.wv, wh2 = P.wh2;
-    const double nu = -P.dt * P.dt * (P.g / P.Msq) * strat * Y;
-    CorCoef c;
-    c.denom = 1.0 / (wh1 * wh1 + wh2 * wh2 + (nu + nonhydro) * (wv * wv + 1.0));
-    c.uu = (wh1 * wh1 + nu + nonhydro);
-    c.uv = nonhydro * (wh1 * wv + wh2);
-    c.uw = (wh1 * wh2 - (nu + nonhydro) * wv);
-    c.vu = (wh1 * wv - wh2);
-    c.vv = nonhydro * (1.0 + wv * wv);
-    c.vw = (wh2 * wv + wh1);
-    c.wu = (wh1 * wh2 + (nu + nonhydro) * wv);
-    c.wv = nonhydro * (wh2 * wv - wh1);
-    c.ww = (nu + nonhydro + wh2 * wh2);
-    return c;
-}
-
 // dS/dy on cell row j from the node background S0 (variable.py:162-177)
 __device__ __forceinline__ double dSdy(const ProjDev &P, const double *S0n, int j) {
     return (S0n[j + 1] - S0n[j]) / P.dy;

@@ -6,7 +6,9 @@
 divergence right-hand side.  The whole step -- boundary data, coefficients,
 Coriolis factors, Jacobi diagonal, divergence, the BiCGStab solve, ghost
 nodes, correction -- runs as kernels of libbella_gb300
-(``bella_projection2d``).  2D only; the reference's 3D branches cannot run.
+(``bella_projection2d``, ``bella_projection3d``).  The reference's 3D step
+cannot run (second_projection.py:183-203); its 3D pieces can, and the 3D
+device step assembles them with the glue of the 2D branch.
 
 ``euler_forward_non_advective`` (second_projection.py:22) and
 ``euler_backward_non_advective_expl_part`` (:77) are the explicit parts of the
@@ -46,18 +48,25 @@ def _workspace(dev):
 
 def euler_backward_non_advective_impl_part(Sol, mpv, elem, node, ud, th, t, dt, alpha_diff, Sol0=None,
                                            writer=None, label=None, debug=False, precision="df64",
-                                           stats=None, device=None):
+                                           stats=None, device=None, preconditioner="none"):
     """Implicit nodal pressure projection of one (half) time step on the GPU.
 
-    Mirrors second_projection.py:97-277.  ``precision`` selects the Krylov
-    arithmetic ('df64' double-float by default, 'fp64', 'mixed'); the stop
-    test is the reference's ``tol=ud.tol`` on the FP64 true residual.
+    Mirrors second_projection.py:97-277 in 2D (``bella_projection2d``) and in 3D
+    (``bella_projection3d``: the reference's 3D pieces with the glue of its 2D
+    branch, whose own 3D branch cannot run).  ``precision`` selects the Krylov
+    arithmetic ('df64' double-float by default, 'fp64', 'mixed'); the stop test
+    is the reference's ``tol=ud.tol`` on the FP64 true residual.  3D only:
+    ``preconditioner='background'`` solves with the background solve as the
+    preconditioner of flexible BiCGStab (y must be a wall).
     """
     global total_iter, total_calls
-    if elem.ndim != 2:
-        raise NotImplementedError("the device projection is 2D (the reference's 3D branches cannot run)")
+    if elem.ndim not in (2, 3):
+        raise NotImplementedError("the device projection is 2D or 3D")
     if hasattr(ud, "LAMB_BDRY"):
         raise NotImplementedError("the LAMB_BDRY variant is not on this path")
+    if preconditioner not in ("none", "background") or (preconditioner != "none" and elem.ndim != 3):
+        raise ValueError("preconditioner must be 'none', or 'background' in 3D")
+    three = elem.ndim == 3
     dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
     keep = {}
 
@@ -66,10 +75,13 @@ def euler_backward_non_advective_impl_part(Sol, mpv, elem, node, ud, th, t, dt, 
         keep[name] = t_
         return ctypes.c_void_p(t_.data_ptr())
 
-    args = _lib.Proj2D()
+    args = _lib.Proj3D() if three else _lib.Proj2D()
     args.inx, args.iny = int(node.iicx), int(node.iicy)
     args.x_wall, args.y_wall = int(_is_wall(ud.bdry_type[0])), int(_is_wall(ud.bdry_type[1]))
     args.dx, args.dy, args.dt = float(node.dx), float(node.dy), float(dt)
+    if three:
+        args.inz, args.z_wall, args.dz = int(node.iicz), int(_is_wall(ud.bdry_type[2])), float(node.dz)
+        args.precond = 1 if preconditioner == "background" else 0
     args.Msq, args.g, args.gamm = float(ud.Msq), float(ud.gravity_strength[1]), float(th.gamm)
     args.nonhydro, args.compressibility = float(ud.nonhydrostasy), float(ud.compressibility)
     for k in range(3):
@@ -83,7 +95,7 @@ def euler_backward_non_advective_impl_part(Sol, mpv, elem, node, ud, th, t, dt, 
     args.S0n = d(mpv.HydroState_n.S0, "S0n")
     strat = np.array([1.0 / ud.stratification(y) for y in elem.y], dtype=np.float64)
     args.strat_inv = d(strat, "strat_inv")
-    rhs = torch.empty(tuple(node.isc[:2]), dtype=torch.float64, device=dev)
+    rhs = torch.empty(tuple(node.isc[:elem.ndim]), dtype=torch.float64, device=dev)
     args.rhs_out = ctypes.c_void_p(rhs.data_ptr())
     ws = _workspace(dev)
     o = _lib.SolveOpts()
@@ -93,9 +105,10 @@ def euler_backward_non_advective_impl_part(Sol, mpv, elem, node, ud, th, t, dt, 
     o.precision = {"fp64": 0, "mixed": 1, "df64": 2}[precision]
     st = _lib.SolveStats()
     with torch.cuda.device(dev):
-        rc = ws._lib.bella_projection2d(ws.handle, ctypes.byref(args), ctypes.byref(o), ctypes.byref(st),
-                                        ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
-    _lib.check(rc, "bella_projection2d")
+        fn = ws._lib.bella_projection3d if three else ws._lib.bella_projection2d
+        rc = fn(ws.handle, ctypes.byref(args), ctypes.byref(o), ctypes.byref(st),
+                ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
+    _lib.check(rc, "bella_projection%dd" % elem.ndim)
     for f in _FIELDS:
         getattr(Sol, f)[...] = keep[f].cpu().numpy()
         if Sol0 is not None:
