@@ -167,7 +167,9 @@ typedef struct bella_proj2d {
     double Msq, g, gamm, nonhydro, compressibility;
     double coriolis[3];           /* ud.coriolis_strength                             */
     int is_compressible;
-    int pad_;
+    int precond;                  /* 0: the solve of opts->precision; 1: flexible
+                                     BiCGStab preconditioned by the background solve
+                                     (bella_spectral2d_create, y a wall), set up per call */
     double *rho, *rhou, *rhov, *rhow, *rhoY, *rhoX;          /* Sol                    */
     double *rho0, *rhou0, *rhov0, *rhow0, *rhoY0, *rhoX0;    /* Sol0 or all NULL       */
     double *p2;                   /* mpv.p2_nodes                                     */

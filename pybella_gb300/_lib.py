@@ -46,7 +46,7 @@ class Proj2D(ctypes.Structure):
                 ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dt", ctypes.c_double),
                 ("Msq", ctypes.c_double), ("g", ctypes.c_double), ("gamm", ctypes.c_double),
                 ("nonhydro", ctypes.c_double), ("compressibility", ctypes.c_double),
-                ("coriolis", ctypes.c_double * 3), ("is_compressible", ctypes.c_int), ("pad_", ctypes.c_int)] + \
+                ("coriolis", ctypes.c_double * 3), ("is_compressible", ctypes.c_int), ("precond", ctypes.c_int)] + \
         [(k, _dp) for k in ("rho", "rhou", "rhov", "rhow", "rhoY", "rhoX",
                             "rho0", "rhou0", "rhov0", "rhow0", "rhoY0", "rhoX0",
                             "p2", "hydro_rhoY0", "S0n", "strat_inv", "rhs_out")]

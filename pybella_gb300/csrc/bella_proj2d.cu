@@ -218,7 +218,8 @@ __global__ void k_divergence(ProjDev P, const double *rho, const double *rhou, c
     const double e0 = (qv(a, b + 1) - qv(a, b)) / P.dy;
     const double e1 = (qv(a + 1, b + 1) - qv(a + 1, b)) / P.dy;
     const double Vy = 0.5 * (e0 + e1);
-    const double rhs = (Ux + Vy) / P.dt;
+    double rhs = (Ux + Vy) / P.dt;
+    if (P.is_compressible == 0) rhs = P.compressibility * rhs + (1.0 - P.compressibility) * rhs;   // :149-150
     rhs_isc[e] = rhs;
     if (a >= 1 && a <= nix - 2 && b >= 1 && b <= niy - 2) {
         const int inx = nix - 2;
@@ -412,6 +413,7 @@ extern "C" int bella_projection2d(bella_ws *ws, const bella_proj2d *a, const bel
     if (a->inx < 3 || a->iny < 3 || !a->rho || !a->rhou || !a->rhov || !a->rhow || !a->rhoY || !a->rhoX ||
         !a->p2 || !a->hydro_rhoY0 || !a->S0n || !a->strat_inv)
         return BELLA_EINVAL;
+    if (a->precond != 0 && (a->precond != 1 || !a->y_wall)) return BELLA_EINVAL;
     cudaStream_t s = (cudaStream_t)stream;
     ProjDev P;
     P.icx = a->inx + 3; P.icy = a->iny + 3;
@@ -485,7 +487,16 @@ extern "C" int bella_projection2d(bella_ws *ws, const bella_proj2d *a, const bel
     bella_solve_opts o;
     if (opts) o = *opts; else bella_solve_opts_default(&o);
     o.x0_zero = 1;
-    const int st = bella_bicgstab(ws, bvec, xvec, &o, stats, stream);
+    int st;
+    if (a->precond == 1) {
+        bella_spectral3d *sp = nullptr;
+        rc = bella_spectral2d_create(&sp, &op, ws->device, stream);
+        if (rc != BELLA_OK) return rc;
+        st = bella_fbicgstab_pc(ws, sp, nullptr, 0, bvec, xvec, &o, stats, stream);
+        bella_spectral3d_destroy(sp);
+    } else {
+        st = bella_bicgstab(ws, bvec, xvec, &o, stats, stream);
+    }
     if (st < 0) return st;
     // 6. p2_full, ghost nodes, correction with updt_chi = 1, p2 += p2_full, ghosts (:241-277)
     k_scatter<<<grid1(nnode), 256, 0, s>>>(P, xvec, pfull);

@@ -55,7 +55,7 @@ def euler_backward_non_advective_impl_part(Sol, mpv, elem, node, ud, th, t, dt, 
     (``bella_projection3d``: the reference's 3D pieces with the glue of its 2D
     branch, whose own 3D branch cannot run).  ``precision`` selects the Krylov
     arithmetic ('df64' double-float by default, 'fp64', 'mixed'); the stop test
-    is the reference's ``tol=ud.tol`` on the FP64 true residual.  3D only:
+    is the reference's ``tol=ud.tol`` on the FP64 true residual.
     ``preconditioner='background'`` solves with the background solve as the
     preconditioner of flexible BiCGStab (y must be a wall).
     """
@@ -64,8 +64,8 @@ def euler_backward_non_advective_impl_part(Sol, mpv, elem, node, ud, th, t, dt, 
         raise NotImplementedError("the device projection is 2D or 3D")
     if hasattr(ud, "LAMB_BDRY"):
         raise NotImplementedError("the LAMB_BDRY variant is not on this path")
-    if preconditioner not in ("none", "background") or (preconditioner != "none" and elem.ndim != 3):
-        raise ValueError("preconditioner must be 'none', or 'background' in 3D")
+    if preconditioner not in ("none", "background"):
+        raise ValueError("preconditioner must be 'none' or 'background'")
     three = elem.ndim == 3
     dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
     keep = {}
@@ -79,9 +79,9 @@ def euler_backward_non_advective_impl_part(Sol, mpv, elem, node, ud, th, t, dt, 
     args.inx, args.iny = int(node.iicx), int(node.iicy)
     args.x_wall, args.y_wall = int(_is_wall(ud.bdry_type[0])), int(_is_wall(ud.bdry_type[1]))
     args.dx, args.dy, args.dt = float(node.dx), float(node.dy), float(dt)
+    args.precond = 1 if preconditioner == "background" else 0
     if three:
         args.inz, args.z_wall, args.dz = int(node.iicz), int(_is_wall(ud.bdry_type[2])), float(node.dz)
-        args.precond = 1 if preconditioner == "background" else 0
     args.Msq, args.g, args.gamm = float(ud.Msq), float(ud.gravity_strength[1]), float(th.gamm)
     args.nonhydro, args.compressibility = float(ud.nonhydrostasy), float(ud.compressibility)
     for k in range(3):

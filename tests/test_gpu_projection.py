@@ -55,8 +55,8 @@ def _converged(d, tag):
 
 
 @pytest.mark.parametrize("tag", ["full", "half"])
-@pytest.mark.parametrize("precision", ["fp64", "df64"])
-def test_device_projection_matches_reference(tag, precision):
+@pytest.mark.parametrize("precision,preconditioner", [("fp64", "none"), ("df64", "none"), ("fp64", "background")])
+def test_device_projection_matches_reference(tag, precision, preconditioner):
     """Right-hand side to rounding; pressure and momentum as close to the converged
     answer as the reference's own tol=1e-10 result is (or within 1e-8 of it).
 
@@ -70,7 +70,8 @@ def test_device_projection_matches_reference(tag, precision):
     Sol, Sol0, mpv, elem, node, ud, th = _objects(d, tag)
     st = {}
     euler_backward_non_advective_impl_part(Sol, mpv, elem, node, ud, th, 0.0, float(d[tag + "_dt"]), 1.0,
-                                           Sol0=Sol0, precision=precision, stats=st)
+                                           Sol0=Sol0, precision=precision, stats=st,
+                                           preconditioner=preconditioner)
     assert st["status"] == 0 and st["relres"] <= ud.tol, st
     np.testing.assert_allclose(mpv.rhs, d[tag + "_rhs"], rtol=1e-12, atol=1e-12 * np.abs(d[tag + "_rhs"]).max())
     Sc, pc = _converged(d, tag)
