@@ -74,3 +74,15 @@ def proj3d_case(d, tag):
     sinv = d[tag + "_strat_inv"]
     assert np.all(sinv == 1.0)
     return grid, prm, dt, d[tag + "_S0n"], dict(rhoY0=d[tag + "_rhoY0"]), (lambda y: 1.0)
+
+
+def step2d_case(d, tag):
+    """Grid, parameters and backgrounds of one ``step2d_kat`` case (33x17 nodes)."""
+    from oracle import nodal2d as n2
+    m = d[tag + "_meta"]
+    inx, iny, xw = int(m[0]), int(m[1]), bool(m[2])
+    dt, Msq, g, gamm, is_comp, comp = (float(v) for v in m[3:9])
+    grid = n2.Grid2D(inx, iny, -1.0, 1.0, 0.0, 1.0, (n2.WALL if xw else n2.PERIODIC, n2.WALL))
+    prm = n2.Params(Msq=Msq, g=g, gamm=gamm, coriolis=m[9:12], nonhydro=1.0, is_compressible=int(is_comp),
+                    compressibility=comp, tol=1e-10, max_iterations=6000)
+    return grid, prm, dt, dict(S0=d[tag + "_S0n"]), dict(rhoY0=d[tag + "_rhoY0"]), (lambda y: 1.0)

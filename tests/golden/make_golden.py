@@ -18,6 +18,8 @@ It imports the reference through ``refshim`` (numba, h5py, ... stubbed; SciPy
   2D and 3D (its index carries over between wall axes);
 * ``proj3d_kat.npz``  -- the projection pieces in 3D (boundary data,
   coefficients, divergence, ghost nodes, correction) on two small states;
+* ``step2d_kat.npz``  -- the whole 2D step on 33x17 states with walls in x and
+  y, and with Coriolis in the compressible regime;
 * ``diag_kat.npz``    -- ``precon_diag_prepare`` (laplacian.py:1284-1356);
 * ``pieces_kat.npz``  -- ``divergence_nodes``, ``correction_nodes``,
   ``set_ghostnodes_p2`` and ``set_explicit_boundary_data`` on a random state;
@@ -381,6 +383,49 @@ def _rb_setup_sized(inx, iny):
     return ud, elem, node, Sol, th, mpv
 
 
+def step2d_kat(out):
+    """The reference's whole 2D projection step (impl_part) on two small states
+    the rising-bubble fixture does not cover, both in the compressible regime
+    (hcenter != 0): walls in x and y; and periodic x with Coriolis (cross
+    terms).  33x17 nodes, seeded momenta, tol 1e-10.  (With walls in x the
+    pseudo-incompressible step does not converge in the reference: its wall
+    padding keeps rhou symmetric and negates rhov, boundary.py:161-166, so the
+    divergence is not in the range of the singular operator.)"""
+    import dycore.physics.low_mach.second_projection as lm_sp
+    import dycore.utils.options as opts
+    rec = {}
+    cases = [("ww", opts.BdryType.WALL, (0.0, 0.0, 0.0), 1, 1.0, 21),
+             ("cor", opts.BdryType.PERIODIC, (3.0, 2.0, 1.0), 1, 1.0, 22)]
+    for tag, xb, cor, is_comp, comp, seed in cases:
+        rng = np.random.default_rng(seed)
+        ud, elem, node, Sol, th, mpv = _rb_setup_sized(33, 17)
+        ud.bdry_type[0] = xb
+        ud.coriolis_strength = np.array(cor)
+        ud.is_compressible, ud.compressibility = is_comp, comp
+        for k in ("rhou", "rhov", "rhow"):
+            setattr(Sol, k, getattr(Sol, k) + 0.05 * Sol.rho * rng.standard_normal(elem.sc[:2]))
+        mpv.p2_nodes[...] = 0.01 * rng.standard_normal(node.sc[:2])
+        import dycore.utils.boundary as bdry
+        bdry.set_explicit_boundary_data(Sol, elem, ud, th, mpv)
+        dt = 0.01
+        for k in FIELDS:
+            rec["%s_in_%s" % (tag, k)] = np.copy(getattr(Sol, k))
+        rec[tag + "_p2_in"] = np.copy(mpv.p2_nodes)
+        n0 = lm_sp.total_iter
+        lm_sp.euler_backward_non_advective_impl_part(Sol, mpv, elem, node, ud, th, 0.0, dt, 1.0)
+        rec[tag + "_niter"] = np.array(lm_sp.total_iter - n0)
+        for k in FIELDS:
+            rec["%s_out_%s" % (tag, k)] = np.copy(getattr(Sol, k))
+        rec[tag + "_p2_out"] = np.copy(mpv.p2_nodes)
+        rec[tag + "_rhs"] = np.copy(mpv.rhs)
+        rec[tag + "_S0n"] = np.copy(mpv.HydroState_n.S0)
+        rec[tag + "_rhoY0"] = np.copy(mpv.HydroState.rhoY0)
+        rec[tag + "_meta"] = np.array([33, 17, int(xb == opts.BdryType.WALL), dt, ud.Msq, ud.gravity_strength[1],
+                                       th.gamm, is_comp, comp, *cor])
+        print("step2d %s: %d iterations" % (tag, int(rec[tag + "_niter"])), flush=True)
+    np.savez_compressed(os.path.join(out, "step2d_kat.npz"), **rec)
+
+
 def rising_bubble_step0(out):
     import dycore.discretisation.time_update as dis_time_update
     import dycore.physics.low_mach.second_projection as lm_sp
@@ -439,6 +484,7 @@ def main():
     diag3d_kat(out)
     wall_kat(out)
     proj3d_kat(out)
+    step2d_kat(out)
     if "--3d-only" in sys.argv:
         print("fixtures written to", out)
         return

@@ -7,7 +7,7 @@ arithmetic in the same operation order, so most comparisons are exact.
 import numpy as np
 import pytest
 
-from conftest import golden, lap3d_case
+from conftest import golden, lap3d_case, step2d_case
 from oracle import cases, nodal2d as n2, nodal3d as n3
 from oracle.krylov import bicgstab_legacy, true_relres
 
@@ -165,6 +165,24 @@ def test_impl_part_matches_reference_rising_bubble(tag):
     for k in FIELDS:
         np.testing.assert_array_equal(Sol[k], d["%s_out_%s" % (tag, k)], err_msg=k)
     assert true_relres(out["op"], out["x"], out["rhs_inner"]) <= prm.tol
+
+
+@pytest.mark.parametrize("tag", ["ww", "cor"])
+def test_impl_part_matches_reference_walls_and_coriolis(tag):
+    """The whole 2D step with walls in x and y (the wall-scaling index carry-over,
+    x-wall ghost cells and nodes) and with Coriolis cross terms in the
+    compressible regime: the oracle reproduces the reference bit for bit,
+    iteration count included."""
+    d = np.load(golden("step2d_kat.npz"))
+    grid, prm, dt, hn, hc, sf = step2d_case(d, tag)
+    Sol = {k: d["%s_in_%s" % (tag, k)].copy() for k in FIELDS}
+    p2 = d[tag + "_p2_in"].copy()
+    out = n2.impl_part(Sol, p2, hn["S0"], hc, sf, grid, prm, dt)
+    assert out["niter"] == int(d[tag + "_niter"])
+    np.testing.assert_array_equal(out["rhs"], d[tag + "_rhs"])
+    np.testing.assert_array_equal(p2, d[tag + "_p2_out"])
+    for k in FIELDS:
+        np.testing.assert_array_equal(Sol[k], d["%s_out_%s" % (tag, k)], err_msg=k)
 
 
 def test_oracle_operator_left_null_vector():
