@@ -20,6 +20,8 @@ It imports the reference through ``refshim`` (numba, h5py, ... stubbed; SciPy
   coefficients, divergence, ghost nodes, correction) on two small states;
 * ``step2d_kat.npz``  -- the whole 2D step on 33x17 states with walls in x and
   y, and with Coriolis in the compressible regime;
+* ``advect_kat.npz``  -- the 2D advection (face mass fluxes, Strang-split
+  ``advect`` for odd and even steps, ``advect_rk``) on a perturbed 64x32 state;
 * ``diag_kat.npz``    -- ``precon_diag_prepare`` (laplacian.py:1284-1356);
 * ``pieces_kat.npz``  -- ``divergence_nodes``, ``correction_nodes``,
   ``set_ghostnodes_p2`` and ``set_explicit_boundary_data`` on a random state;
@@ -426,6 +428,46 @@ def step2d_kat(out):
     np.savez_compressed(os.path.join(out, "step2d_kat.npz"), **rec)
 
 
+def advect_kat(out):
+    """The reference's 2D advection on a perturbed 64x32 rising-bubble state:
+    the face mass fluxes (recompute_advective_fluxes), the Strang-split
+    ``advect`` for an odd and an even step, and the first-order ``advect_rk``,
+    each from the same state and freshly computed fluxes."""
+    import copy
+    import dycore.utils.variable as var
+    import dycore.physics.gas_dynamics.explicit as gd_explicit
+    import dycore.physics.gas_dynamics.numerical_flux as gd_flux
+    rng = np.random.default_rng(31)
+    ud, elem, node, Sol, th, mpv = _rb_setup_sized(64, 32)
+    for k in ("rhou", "rhov", "rhow"):
+        setattr(Sol, k, getattr(Sol, k) + 0.1 * Sol.rho * rng.standard_normal(elem.sc[:2]))
+    Sol.rhoX = Sol.rhoX + 0.01 * Sol.rho * rng.standard_normal(elem.sc[:2])
+    import dycore.utils.boundary as bdry
+    bdry.set_explicit_boundary_data(Sol, elem, ud, th, mpv)
+    rec = {("in_" + k): np.copy(getattr(Sol, k)) for k in FIELDS}
+    dt = 0.01
+    for tag, call in (("odd", lambda S, f: gd_explicit.advect(S, f, dt, elem, 1, ud, th, mpv, node, "x")),
+                      ("even", lambda S, f: gd_explicit.advect(S, f, dt, elem, 0, ud, th, mpv, node, "x")),
+                      ("rk", lambda S, f: gd_explicit.advect_rk(S, f, 0.5 * dt, elem, 0, ud, th, mpv, node, "x"))):
+        S = copy.deepcopy(Sol)
+        flux = np.empty((3), dtype=object)
+        flux[0] = var.States(elem.sfx, ud)
+        flux[1] = var.States(elem.sfy, ud)
+        gd_flux.recompute_advective_fluxes(flux, S)
+        if tag == "odd":
+            rec["flux0_rhoY"] = np.copy(flux[0].rhoY)
+            rec["flux1_rhoY"] = np.copy(flux[1].rhoY)
+        call(S, flux)
+        for k in FIELDS:
+            rec["%s_%s" % (tag, k)] = np.copy(getattr(S, k))
+        if tag == "rk":
+            rec["rk_pwchi"] = np.copy(S.pwchi)
+    rec["meta"] = np.array([64, 32, dt, ud.Msq, ud.gravity_strength[1], th.gamm])
+    rec["S0n"] = np.copy(mpv.HydroState_n.S0)
+    rec["rhoY0"] = np.copy(mpv.HydroState.rhoY0)
+    np.savez_compressed(os.path.join(out, "advect_kat.npz"), **rec)
+
+
 def rising_bubble_step0(out):
     import dycore.discretisation.time_update as dis_time_update
     import dycore.physics.low_mach.second_projection as lm_sp
@@ -485,6 +527,7 @@ def main():
     wall_kat(out)
     proj3d_kat(out)
     step2d_kat(out)
+    advect_kat(out)
     if "--3d-only" in sys.argv:
         print("fixtures written to", out)
         return
