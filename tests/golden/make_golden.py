@@ -22,6 +22,8 @@ It imports the reference through ``refshim`` (numba, h5py, ... stubbed; SciPy
   y, and with Coriolis in the compressible regime;
 * ``advect_kat.npz``  -- the 2D advection (face mass fluxes, Strang-split
   ``advect`` for odd and even steps, ``advect_rk``) on a perturbed 64x32 state;
+* ``step_kat.npz``    -- the whole time step (``time_update.do``) of the 64x32
+  rising bubble, after one and after two steps;
 * ``diag_kat.npz``    -- ``precon_diag_prepare`` (laplacian.py:1284-1356);
 * ``pieces_kat.npz``  -- ``divergence_nodes``, ``correction_nodes``,
   ``set_ghostnodes_p2`` and ``set_explicit_boundary_data`` on a random state;
@@ -468,6 +470,38 @@ def advect_kat(out):
     np.savez_compressed(os.path.join(out, "advect_kat.npz"), **rec)
 
 
+def step_kat(out):
+    """The reference's whole time step (time_update.do, time_update.py:129-708) on
+    the 64x32 rising bubble: the state after one and after two steps (fixed
+    dt = 21.69 / t_ref for the first two steps, 'CFLfixed')."""
+    import dycore.discretisation.time_update as dis_time_update
+    import dycore.utils.variable as var
+    from data_assimilation import blending as da_blending
+    rec = {}
+    for nsteps in (1, 2):
+        ud, elem, node, Sol, th, mpv = _rb_setup_sized(64, 32)
+        if nsteps == 1:
+            for k in FIELDS:
+                rec["in_" + k] = np.copy(getattr(Sol, k))
+            rec["p2_in"] = np.copy(mpv.p2_nodes)
+            rec["S0n"] = np.copy(mpv.HydroState_n.S0)
+            rec["rhoY0"] = np.copy(mpv.HydroState.rhoY0)
+            rec["S0c"] = np.copy(mpv.HydroState.get_S0c(elem))
+        ud.stepmax = nsteps
+        flux = np.empty((3), dtype=object)
+        flux[0] = var.States(elem.sfx, ud)
+        flux[1] = var.States(elem.sfy, ud)
+        ret = dis_time_update.do(Sol, flux, mpv, 0.0, ud.tout[0], ud, elem, node, [0, 0], th,
+                                 da_blending.Blend(ud), None, False)
+        S, m = ret[0], ret[2]
+        for k in FIELDS:
+            rec["s%d_%s" % (nsteps, k)] = np.copy(getattr(S, k))
+        rec["s%d_p2" % nsteps] = np.copy(m.p2_nodes)
+        print("step_kat: %d step(s) done" % nsteps, flush=True)
+    rec["meta"] = np.array([64, 32, 21.69 / ud.t_ref, ud.Msq, ud.gravity_strength[1], th.gamm])
+    np.savez_compressed(os.path.join(out, "step_kat.npz"), **rec)
+
+
 def rising_bubble_step0(out):
     import dycore.discretisation.time_update as dis_time_update
     import dycore.physics.low_mach.second_projection as lm_sp
@@ -528,6 +562,7 @@ def main():
     proj3d_kat(out)
     step2d_kat(out)
     advect_kat(out)
+    step_kat(out)
     if "--3d-only" in sys.argv:
         print("fixtures written to", out)
         return

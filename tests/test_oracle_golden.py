@@ -208,6 +208,25 @@ def test_advection_matches_reference_kat(tag):
         np.testing.assert_array_equal(Sol[k], d["%s_%s" % (tag, k)], err_msg=k)
 
 
+def test_time_step_matches_reference_kat():
+    """Two whole time steps of the 64x32 rising bubble (advection, explicit and
+    implicit projection halves, Strang sweeps for an even and an odd step):
+    the oracle's step reproduces the reference's time_update.do bit for bit."""
+    from oracle import advection2d as adv, step2d
+    d = np.load(golden("step_kat.npz"))
+    grid, prm, Sol_rb, p2_rb, hn, hc, sf = cases.rising_bubble(inx=64, iny=32)
+    hn, hc = dict(hn, S0=d["S0n"]), dict(hc, rhoY0=d["rhoY0"])   # the reference's background arrays
+    Sol = {k: d["in_" + k].copy() for k in FIELDS}
+    p2 = d["p2_in"].copy()
+    flux = adv.new_flux(grid)
+    dt = float(d["meta"][2])
+    for step in (0, 1):
+        Sol = step2d.time_step(Sol, p2, flux, step, dt, grid, prm, hn, hc, d["S0c"], sf)
+        for k in FIELDS:
+            np.testing.assert_array_equal(Sol[k], d["s%d_%s" % (step + 1, k)], err_msg="step %d %s" % (step, k))
+        np.testing.assert_array_equal(p2, d["s%d_p2" % (step + 1)])
+
+
 def test_oracle_operator_left_null_vector():
     """Seam-consistent vectors: the trapezoid weights annihilate the range.
 
