@@ -237,6 +237,31 @@ int bella_euler_forward2d(const bella_expl2d *args, void *stream);
 /* euler_backward_non_advective_expl_part (second_projection.py:77-92) */
 int bella_expl_part2d(const bella_expl2d *args, void *stream);
 
+/* ---- 2D advection (the reference's explicit.py, recovery.py, numerical_flux.py) --
+ * Device arrays in the reference's NumPy C order: cells (inx+3)(iny+3) over (x, y);
+ * fx[q]: x-face arrays (iny+3)(inx+4) (elem.sfx: row y, face x), fy[q]: y-face
+ * arrays (inx+3)(iny+4), q = rho, rhou, rhov, rhow, rhoY (the face mass flux),
+ * rhoX.  Face arrays are zeroed by the caller once: their outer faces are never
+ * written.  Gravity along y (g = ud.gravity_strength[1]); hydro_rhoY0 and strat_inv
+ * as in bella_proj2d.  The limiter is the reference's only one (NONE).  */
+typedef struct bella_adv2d {
+    int inx, iny;                 /* grid nodes per direction                          */
+    int x_wall, y_wall;           /* 0: periodic, 1: wall                              */
+    double dx, dy, g, gamm;
+    int is_compressible;
+    int pad_;
+    double *rho, *rhou, *rhov, *rhow, *rhoY, *rhoX;          /* Sol                    */
+    double *fx[6], *fy[6];        /* flux[0], flux[1] of the reference                */
+    const double *hydro_rhoY0, *strat_inv;
+    double *pwchi;                /* advect_rk's Sol.pwchi (cells) or NULL              */
+} bella_adv2d;
+/* recompute_advective_fluxes (numerical_flux.py:5-46): fx rhoY, fy rhoY on the inner faces */
+int bella_advective_fluxes2d(const bella_adv2d *args, void *stream);
+/* advect (explicit.py:5-74): Strang-split sweeps over dt, odd = step % 2 */
+int bella_advect2d(const bella_adv2d *args, double dt, int odd, void *stream);
+/* advect_rk (explicit.py:160-257): first-order update over dt from the start state's fluxes */
+int bella_advect_rk2d(const bella_adv2d *args, double dt, void *stream);
+
 /* ---- ensemble: the solves of many 2D members in one persistent launch ----
  * Each member is the reference's call (second_projection.py:205-230) on its own
  * workspace (bella_op2d_set): FP64 BiCGStab, scipy 1.7 control flow, x0 = 0.

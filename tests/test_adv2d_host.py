@@ -22,7 +22,7 @@ def host_lib(tmp_path_factory):
     if cxx is None:
         pytest.skip("no g++")
     out = str(tmp_path_factory.mktemp("adv2d") / "libadv2d_host.so")
-    subprocess.run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-o", out,
+    subprocess.run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-shared", "-fPIC", "-o", out,
                     os.path.join(ROOT, "tests", "adv2d_host.cpp")], check=True)
     return ctypes.CDLL(out)
 
