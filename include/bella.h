@@ -261,6 +261,8 @@ int bella_advective_fluxes2d(const bella_adv2d *args, void *stream);
 int bella_advect2d(const bella_adv2d *args, double dt, int odd, void *stream);
 /* advect_rk (explicit.py:160-257): first-order update over dt from the start state's fluxes */
 int bella_advect_rk2d(const bella_adv2d *args, double dt, void *stream);
+/* set_explicit_boundary_data (boundary.py:7-216) of the cell state: along x, then y */
+int bella_boundary2d(const bella_adv2d *args, void *stream);
 
 /* ---- ensemble: the solves of many 2D members in one persistent launch ----
  * Each member is the reference's call (second_projection.py:205-230) on its own

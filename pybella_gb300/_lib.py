@@ -130,6 +130,7 @@ SIGNATURES = {
     "bella_advective_fluxes2d": (ctypes.c_int, [ctypes.POINTER(Adv2D), ctypes.c_void_p]),
     "bella_advect2d": (ctypes.c_int, [ctypes.POINTER(Adv2D), ctypes.c_double, ctypes.c_int, ctypes.c_void_p]),
     "bella_advect_rk2d": (ctypes.c_int, [ctypes.POINTER(Adv2D), ctypes.c_double, ctypes.c_void_p]),
+    "bella_boundary2d": (ctypes.c_int, [ctypes.POINTER(Adv2D), ctypes.c_void_p]),
     "bella_cnn_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int,
                                         ctypes.c_longlong]),
     "bella_cnn_destroy": (ctypes.c_int, [ctypes.c_void_p]),

@@ -132,3 +132,12 @@ extern "C" int bella_advect_rk2d(const bella_adv2d *a, double dt, void *stream) 
     adv_rk(ex, ex.G, dt);
     return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
 }
+
+// set_explicit_boundary_data (boundary.py:7-216) of the whole state: x, then y
+extern "C" int bella_boundary2d(const bella_adv2d *a, void *stream) {
+    DevEx ex;
+    if (!adv_setup(a, ex, stream)) return BELLA_EINVAL;
+    ex.bd(0);
+    ex.bd(1);
+    return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
+}

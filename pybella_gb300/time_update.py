@@ -1,0 +1,147 @@
+"""Device-resident 2D time step: the reference's ``time_update.do``
+(time_update.py:129-489) for the pseudo-incompressible case without blending,
+data assimilation or Rayleigh damping, with every array on the GPU between
+steps.
+
+One step, as the reference orders it: boundary data; ``Sol0`` = the state;
+face mass fluxes and first-order advection over dt/2 (``bella_advective_fluxes2d``,
+``bella_advect_rk2d``); the explicit and implicit projection halves with
+``Sol0``'s coefficients (``bella_expl_part2d``, ``bella_projection2d``); face mass
+fluxes of that half-step state; the state reset to ``Sol0`` (``p2`` kept); the
+forward explicit projection (``bella_euler_forward2d``), Strang-split advection
+over dt (``bella_advect2d``) and both projection halves again.  The host only
+launches; the state stays in HBM until :meth:`DeviceStep2D.download`.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .second_projection import _is_wall
+
+_FIELDS = ("rho", "rhou", "rhov", "rhow", "rhoY", "rhoX")
+
+
+class DeviceStep2D:
+    """The state of a 2D run on one GPU and its time step.
+
+    Built from the reference's objects (``Sol``, ``mpv``, ``elem``, ``node``,
+    ``ud``, ``th``); :meth:`step` advances by ``dt`` (``step`` is the step index,
+    whose parity picks the Strang order), :meth:`download` writes the state
+    back into ``Sol`` and ``mpv.p2_nodes``.
+    """
+
+    def __init__(self, Sol, mpv, elem, node, ud, th, device=None):
+        if elem.ndim != 2:
+            raise NotImplementedError("the device time step is 2D")
+        if int(ud.is_compressible) != 0:
+            raise NotImplementedError("the pseudo-incompressible step only")
+        self.dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        d = lambda a: torch.tensor(np.ascontiguousarray(a, dtype=np.float64), device=self.dev)
+        self.f = {k: d(getattr(Sol, k)) for k in _FIELDS}
+        self.f0 = {k: torch.empty_like(v) for k, v in self.f.items()}
+        self.p2 = d(mpv.p2_nodes)
+        icx, icy = self.f["rho"].shape
+        self.fx = [torch.zeros((icy, icx + 1), dtype=torch.float64, device=self.dev) for _ in _FIELDS]
+        self.fy = [torch.zeros((icx, icy + 1), dtype=torch.float64, device=self.dev) for _ in _FIELDS]
+        self.pwchi = torch.zeros((icx, icy), dtype=torch.float64, device=self.dev)
+        self.rhs = torch.empty((icx - 1, icy - 1), dtype=torch.float64, device=self.dev)
+        self.S0c = d(mpv.HydroState.get_S0c(elem))
+        self.S0n = d(mpv.HydroState_n.S0)
+        self.rhoY0 = d(mpv.HydroState.rhoY0)
+        self.strat_inv = d(np.array([1.0 / ud.stratification(y) for y in elem.y], dtype=np.float64))
+        self.ws = _lib.Workspace(self.dev.index)
+        self.lib = self.ws._lib
+        p = lambda t: ctypes.c_void_p(t.data_ptr())
+        inx, iny = int(node.iicx), int(node.iicy)
+        xw, yw = int(_is_wall(ud.bdry_type[0])), int(_is_wall(ud.bdry_type[1]))
+        g, gamm = float(ud.gravity_strength[1]), float(th.gamm)
+        # advection
+        a = _lib.Adv2D()
+        a.inx, a.iny, a.x_wall, a.y_wall = inx, iny, xw, yw
+        a.dx, a.dy, a.g, a.gamm, a.is_compressible = float(node.dx), float(node.dy), g, gamm, 0
+        for k in _FIELDS:
+            setattr(a, k, p(self.f[k]))
+        for q in range(6):
+            a.fx[q], a.fy[q] = p(self.fx[q]), p(self.fy[q])
+        a.hydro_rhoY0, a.strat_inv, a.pwchi = p(self.rhoY0), p(self.strat_inv), p(self.pwchi)
+        self.adv = a
+        # explicit projection parts
+        e = _lib.Expl2D()
+        e.inx, e.iny, e.x_wall, e.y_wall = inx, iny, xw, yw
+        e.dx, e.dy = float(node.dx), float(node.dy)
+        e.Msq, e.g, e.gamm = float(ud.Msq), g, gamm
+        e.nonhydro, e.compressibility = float(ud.nonhydrostasy), float(ud.compressibility)
+        for k in range(3):
+            e.coriolis[k] = float(ud.coriolis_strength[k])
+        e.wind[0], e.wind[1], e.wind[2] = float(ud.u_wind_speed), float(ud.v_wind_speed), float(ud.w_wind_speed)
+        e.is_compressible, e.is_ArakawaKonor = 0, int(getattr(ud, "is_ArakawaKonor", 0))
+        for k in _FIELDS:
+            setattr(e, k, p(self.f[k]))
+        e.p2, e.rhs_out = p(self.p2), p(self.rhs)
+        e.S0c, e.S0n, e.hydro_rhoY0, e.strat_inv = p(self.S0c), p(self.S0n), p(self.rhoY0), p(self.strat_inv)
+        self.expl = e
+        # implicit projection (coefficients from Sol0 in the half step)
+        r = _lib.Proj2D()
+        r.inx, r.iny, r.x_wall, r.y_wall = inx, iny, xw, yw
+        r.dx, r.dy = float(node.dx), float(node.dy)
+        r.Msq, r.g, r.gamm = float(ud.Msq), g, gamm
+        r.nonhydro, r.compressibility = float(ud.nonhydrostasy), float(ud.compressibility)
+        for k in range(3):
+            r.coriolis[k] = float(ud.coriolis_strength[k])
+        r.is_compressible = 0
+        for k in _FIELDS:
+            setattr(r, k, p(self.f[k]))
+        r.p2, r.rhs_out = p(self.p2), p(self.rhs)
+        r.hydro_rhoY0, r.S0n, r.strat_inv = p(self.rhoY0), p(self.S0n), p(self.strat_inv)
+        self.proj = r
+        self.opts = _lib.SolveOpts()
+        self.lib.bella_solve_opts_default(ctypes.byref(self.opts))
+        self.opts.tol, self.opts.maxiter = float(ud.tol), int(ud.max_iterations)
+        self.stats = []
+
+    def _stream(self):
+        return ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
+
+    def _project(self, dt, with_sol0):
+        r = self.proj
+        r.dt = float(dt)
+        for k in _FIELDS:
+            setattr(r, k + "0", ctypes.c_void_p(self.f0[k].data_ptr()) if with_sol0 else ctypes.c_void_p(0))
+        st = _lib.SolveStats()
+        rc = self.lib.bella_projection2d(self.ws.handle, ctypes.byref(r), ctypes.byref(self.opts), ctypes.byref(st),
+                                         self._stream())
+        _lib.check(rc, "bella_projection2d")
+        self.stats.append(st.as_dict())
+
+    def _expl_part(self, dt):
+        self.expl.dt = float(dt)
+        _lib.check(self.lib.bella_expl_part2d(ctypes.byref(self.expl), self._stream()), "bella_expl_part2d")
+
+    def step(self, step, dt, precision="fp64"):
+        """One time step of length ``dt`` (time_update.py:129-489)."""
+        self.opts.precision = {"fp64": 0, "mixed": 1, "df64": 2}[precision]
+        lib, s, h = self.lib, self._stream(), 0.5 * dt
+        with torch.cuda.device(self.dev):
+            _lib.check(lib.bella_boundary2d(ctypes.byref(self.adv), s), "bella_boundary2d")   # :130
+            for k in _FIELDS:                                                  # Sol0 (:205)
+                self.f0[k].copy_(self.f[k])
+            _lib.check(lib.bella_advective_fluxes2d(ctypes.byref(self.adv), s), "bella_advective_fluxes2d")
+            _lib.check(lib.bella_advect_rk2d(ctypes.byref(self.adv), h, s), "bella_advect_rk2d")    # :224
+            self._expl_part(h)                                                 # :247
+            self._project(h, True)                                             # :251
+            _lib.check(lib.bella_advective_fluxes2d(ctypes.byref(self.adv), s), "bella_advective_fluxes2d")
+            for k in _FIELDS:                                                  # Sol = Sol0 (:376)
+                self.f[k].copy_(self.f0[k])
+            self.expl.dt = float(h)                                            # :419
+            _lib.check(lib.bella_euler_forward2d(ctypes.byref(self.expl), s), "bella_euler_forward2d")
+            _lib.check(lib.bella_advect2d(ctypes.byref(self.adv), dt, int(step) % 2, s), "bella_advect2d")  # :434
+            self._expl_part(h)                                                 # :455
+            self._project(h, False)                                            # :462
+
+    def download(self, Sol, mpv):
+        torch.cuda.synchronize(self.dev)
+        for k in _FIELDS:
+            setattr(Sol, k, self.f[k].cpu().numpy())
+        mpv.p2_nodes[...] = self.p2.cpu().numpy()
