@@ -8,12 +8,18 @@ with the coefficients of the step's start (``Sol0``), fluxes from that
 half-step state, then from the start state again the forward explicit part,
 Strang-split advection over dt and both projection halves.  Pinned bit for bit
 against the reference's ``do`` after one and two steps of the 64x32 rising
-bubble (tests/golden/step_kat.npz).
+bubble (tests/golden/step_kat.npz); ``dynamic_timestep`` and ``run`` add the
+CFL time step and the loop, pinned over a run to tout (two steps with the fixed
+dt of 'CFLfixed', a third whose CFL step is cut to reach tout).
 """
 import copy
 
+import numpy as np
+
 from oracle import advection2d as adv
 from oracle import nodal2d as n2
+
+MACHINE_EPSILON = np.finfo(float).eps
 
 
 def time_step(Sol, p2, flux, step, dt, grid, prm, hydro_n, hydro_c, S0c, strat_fn):
@@ -34,3 +40,51 @@ def time_step(Sol, p2, flux, step, dt, grid, prm, hydro_n, hydro_c, S0c, strat_f
     n2.euler_backward_non_advective_expl_part(Sol, S0n, grid, prm, 0.5 * dt, hydro_c, strat_fn)   # :455
     n2.impl_part(Sol, p2, S0n, hydro_c, strat_fn, grid, prm, 0.5 * dt)           # :462-473
     return Sol
+
+
+def dynamic_timestep(Sol, time, time_output, grid, prm, step, CFL=0.5, dtfixed0=100.0, dtfixed=100.0,
+                     acoustic_timestep=0):
+    """``dynamic_timestep`` (cfl.py:5-74) in 2D (elem.dz = 1, grid.py:110, 171);
+    returns ``dt`` (and, in the advective branch, ``cfl``, ``cfl_ac`` as the reference does)."""
+    Minv = 1.0 / np.sqrt(prm.Msq)
+    p = Sol["rhoY"] ** prm.gamm
+    c = np.sqrt(prm.gamm * p / Sol["rho"]) * Minv
+    u = np.abs(Sol["rhou"] / Sol["rho"])
+    v = np.abs(Sol["rhov"] / Sol["rho"])
+    w = np.abs(Sol["rhow"] / Sol["rho"])
+    eps = MACHINE_EPSILON
+    u_max, v_max, w_max = max(u.max(), eps), max(v.max(), eps), max(w.max(), eps)
+    upc_max, vpc_max, wpc_max = max((u + c).max(), eps), max((v + c).max(), eps), max((w + c).max(), eps)
+    dx, dy, dz = grid.dx, grid.dy, 1.0
+    if acoustic_timestep == 1:
+        dt_cfl = min(min(CFL * dx / upc_max, CFL * dy / vpc_max), CFL * dz / wpc_max)
+        dt = min(dt_cfl, dtfixed0 + min(step, 1.) * (dtfixed - dtfixed0))
+        if dt > (time_output - time):
+            dt = (time_output - time) + eps
+        return dt
+    dt_cfl = min(min(CFL * dx / u_max, CFL * dy / v_max), CFL * dz / w_max)
+    dt = min(dt_cfl, dtfixed0 + min(step, 1.) * (dtfixed - dtfixed0))
+    dt *= min(float(step + 1), 1.0)
+    if dt > (time_output - time):
+        dt = (time_output - time)
+    cfl = CFL * dt / dt_cfl
+    cfl_ac = max(dt * upc_max / dx, dt * vpc_max / dy, dt * wpc_max / dz)
+    return dt, cfl, cfl_ac
+
+
+def run(Sol, p2, t, tout, nsteps, grid, prm, hydro_n, hydro_c, S0c, strat_fn, t_ref, cfl_fixed=True):
+    """The loop of ``do`` (time_update.py:129-140, 486-489): the CFL time step
+    ('CFLfixed': 21.69 / t_ref for the first two steps), then :func:`time_step`,
+    until ``tout`` or ``nsteps`` steps.  Returns ``(Sol, t, dts)``."""
+    flux = adv.new_flux(grid)
+    step, dts = 0, []
+    while t < tout and step < nsteps:
+        n2.set_explicit_boundary_data(Sol, grid, prm, hydro_c, strat_fn)
+        dt, _, _ = dynamic_timestep(Sol, t, tout, grid, prm, step)
+        if cfl_fixed and step < 2:
+            dt = 21.69 / t_ref
+        Sol = time_step(Sol, p2, flux, step, dt, grid, prm, hydro_n, hydro_c, S0c, strat_fn)
+        dts.append(dt)
+        t += dt
+        step += 1
+    return Sol, t, dts

@@ -472,13 +472,14 @@ def advect_kat(out):
 
 def step_kat(out):
     """The reference's whole time step (time_update.do, time_update.py:129-708) on
-    the 64x32 rising bubble: the state after one and after two steps (fixed
-    dt = 21.69 / t_ref for the first two steps, 'CFLfixed')."""
+    the 64x32 rising bubble: the state after one and two steps (fixed dt =
+    21.69 / t_ref, 'CFLfixed') and after a run with stepmax 4, which reaches
+    tout[0] = 0.1 after three steps (the CFL step of the third is cut to tout)."""
     import dycore.discretisation.time_update as dis_time_update
     import dycore.utils.variable as var
     from data_assimilation import blending as da_blending
     rec = {}
-    for nsteps in (1, 2):
+    for nsteps in (1, 2, 4):
         ud, elem, node, Sol, th, mpv = _rb_setup_sized(64, 32)
         if nsteps == 1:
             for k in FIELDS:
@@ -498,7 +499,8 @@ def step_kat(out):
             rec["s%d_%s" % (nsteps, k)] = np.copy(getattr(S, k))
         rec["s%d_p2" % nsteps] = np.copy(m.p2_nodes)
         print("step_kat: %d step(s) done" % nsteps, flush=True)
-    rec["meta"] = np.array([64, 32, 21.69 / ud.t_ref, ud.Msq, ud.gravity_strength[1], th.gamm])
+    rec["meta"] = np.array([64, 32, 21.69 / ud.t_ref, ud.Msq, ud.gravity_strength[1], th.gamm, ud.t_ref,
+                            ud.tout[0]])
     np.savez_compressed(os.path.join(out, "step_kat.npz"), **rec)
 
 

@@ -227,6 +227,24 @@ def test_time_step_matches_reference_kat():
         np.testing.assert_array_equal(p2, d["s%d_p2" % (step + 1)])
 
 
+def test_run_to_tout_matches_reference_kat():
+    """The loop of time_update.do with the CFL time step: a run with stepmax 4
+    reaches tout = 0.1 after three steps (21.69 ms twice, then the CFL step cut
+    to tout); the oracle's run reproduces the reference's state bit for bit."""
+    from oracle import step2d
+    d = np.load(golden("step_kat.npz"))
+    grid, prm, _, _, hn, hc, sf = cases.rising_bubble(inx=64, iny=32)
+    hn, hc = dict(hn, S0=d["S0n"]), dict(hc, rhoY0=d["rhoY0"])
+    Sol = {k: d["in_" + k].copy() for k in FIELDS}
+    p2 = d["p2_in"].copy()
+    Sol, t, dts = step2d.run(Sol, p2, 0.0, float(d["meta"][7]), 4, grid, prm, hn, hc, d["S0c"], sf,
+                             float(d["meta"][6]))
+    assert len(dts) == 3 and t == pytest.approx(float(d["meta"][7]), rel=1e-15)
+    for k in FIELDS:
+        np.testing.assert_array_equal(Sol[k], d["s4_" + k], err_msg=k)
+    np.testing.assert_array_equal(p2, d["s4_p2"])
+
+
 def test_oracle_operator_left_null_vector():
     """Seam-consistent vectors: the trapezoid weights annihilate the range.
 
