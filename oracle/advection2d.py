@@ -83,10 +83,11 @@ def _primitives(U):
 
 
 def _recovery(Sol, flux, lmbda, split):
-    """``recovery.do`` (recovery.py:6-141) with limiter NONE: interface states."""
+    """``recovery.do`` (recovery.py:6-141) with limiter NONE: interface states
+    along the last axis (2D or 3D)."""
     P = _primitives(Sol)
-    L, R = (slice(None), slice(0, -1)), (slice(None), slice(1, None))
-    inner = (slice(1, -1), slice(1, -1))
+    L, R = (Ellipsis, slice(0, -1)), (Ellipsis, slice(1, None))
+    inner = (slice(1, -1),) * Sol["rho"].ndim
     u = np.zeros_like(Sol["rhoY"])
     fr = flux["rhoY"][inner]
     u[inner] = 0.5 * (fr[L] + fr[R]) / Sol["rhoY"][inner]
@@ -131,7 +132,7 @@ def _recovery(Sol, flux, lmbda, split):
 
 def _hll(flux, Lefts, Rights):
     """``hll_solver`` (numerical_flux.py:48-99): upwind by the sign of the face mass flux."""
-    L, R, mid = (slice(None), slice(0, -1)), (slice(None), slice(1, None)), (slice(None), slice(1, -1))
+    L, R, mid = (Ellipsis, slice(0, -1)), (Ellipsis, slice(1, None)), (Ellipsis, slice(1, -1))
     PL, PR = _primitives(Lefts), _primitives(Rights)
     upwind = 0.5 * (1.0 + np.sign(flux["rhoY"]))
     upl = upwind[R]
@@ -146,7 +147,7 @@ def _hll(flux, Lefts, Rights):
 
 
 def _update(Sol, flux, lmbda):
-    L, R = (slice(None), slice(0, -1)), (slice(None), slice(1, None))
+    L, R = (Ellipsis, slice(0, -1)), (Ellipsis, slice(1, None))
     for k in ("rho", "rhou", "rhov", "rhow", "rhoX", "rhoY"):
         Sol[k] = Sol[k] + lmbda * (flux[k][L] - flux[k][R])
 

@@ -22,8 +22,9 @@ It imports the reference through ``refshim`` (numba, h5py, ... stubbed; SciPy
   y, and with Coriolis in the compressible regime;
 * ``advect_kat.npz``  -- the 2D advection (face mass fluxes, Strang-split
   ``advect`` for odd and even steps, ``advect_rk``) on a perturbed 64x32 state;
+* ``advect3d_kat.npz`` -- the 3D advection on small 3D states, two boundary mixes;
 * ``step_kat.npz``    -- the whole time step (``time_update.do``) of the 64x32
-  rising bubble, after one and after two steps;
+  rising bubble, after one and two steps and a run to tout;
 * ``diag_kat.npz``    -- ``precon_diag_prepare`` (laplacian.py:1284-1356);
 * ``pieces_kat.npz``  -- ``divergence_nodes``, ``correction_nodes``,
   ``set_ghostnodes_p2`` and ``set_explicit_boundary_data`` on a random state;
@@ -470,6 +471,68 @@ def advect_kat(out):
     np.savez_compressed(os.path.join(out, "advect_kat.npz"), **rec)
 
 
+def advect3d_kat(out):
+    """The reference's 3D advection (dimension-generic in the reference): face
+    mass fluxes, Strang-split ``advect`` for an odd and an even step and
+    ``advect_rk``, on the 3D hydrostatic state with seeded perturbations, for
+    periodic/wall/periodic and wall/wall/periodic boundaries."""
+    import copy
+    import dycore.discretisation.grid as dis_grid
+    import dycore.utils.variable as var
+    import dycore.physics.low_mach.mpv as lm_var
+    import dycore.physics.gas_dynamics.thermodynamic as gd_thermodynamics
+    import dycore.physics.hydrostatics as hydrostatic
+    import dycore.physics.gas_dynamics.explicit as gd_explicit
+    import dycore.physics.gas_dynamics.numerical_flux as gd_flux
+    import dycore.utils.boundary as bdry
+    import dycore.utils.options as opts
+    W, P = opts.BdryType.WALL, opts.BdryType.PERIODIC
+    rec = {}
+    for case, bt, seed in (("pwp", (P, W, P), 41), ("wwp", (W, W, P), 42)):
+        rng = np.random.default_rng(seed)
+        ud = _ud_rising_bubble()
+        ud.inx, ud.iny, ud.inz = 9, 7, 8
+        ud.zmin, ud.zmax = -1.0, 1.0
+        ud.bdry_type = np.array(list(bt))
+        elem, node = dis_grid.grid_init(ud)
+        ud.nonhydrostasy = 1.0
+        Sol = var.Vars(elem.sc, ud)
+        th = gd_thermodynamics.init(ud)
+        mpv = lm_var.MPV(elem, node, ud)
+        hydrostatic.state(mpv, elem, node, th, ud)
+        rhoY = np.broadcast_to(mpv.HydroState.rhoY0.reshape(1, -1, 1), elem.sc)
+        Sol.rhoY[...] = rhoY
+        Sol.rho[...] = rhoY * (1.0 + 0.01 * rng.standard_normal(elem.sc))
+        for k in ("rhou", "rhov", "rhow", "rhoX"):
+            getattr(Sol, k)[...] = 0.1 * Sol.rho * rng.standard_normal(elem.sc)
+        bdry.set_explicit_boundary_data(Sol, elem, ud, th, mpv)
+        for k in FIELDS:
+            rec["%s_in_%s" % (case, k)] = np.copy(getattr(Sol, k))
+        dt = 0.01
+        for tag, call in (("odd", lambda S, f: gd_explicit.advect(S, f, dt, elem, 1, ud, th, mpv, node, "x")),
+                          ("even", lambda S, f: gd_explicit.advect(S, f, dt, elem, 0, ud, th, mpv, node, "x")),
+                          ("rk", lambda S, f: gd_explicit.advect_rk(S, f, 0.5 * dt, elem, 0, ud, th, mpv, node,
+                                                                    "x"))):
+            S = copy.deepcopy(Sol)
+            flux = np.empty((3), dtype=object)
+            flux[0] = var.States(elem.sfx, ud)
+            flux[1] = var.States(elem.sfy, ud)
+            flux[2] = var.States(elem.sfz, ud)
+            gd_flux.recompute_advective_fluxes(flux, S)
+            if tag == "odd":
+                for q in range(3):
+                    rec["%s_flux%d_rhoY" % (case, q)] = np.copy(flux[q].rhoY)
+            call(S, flux)
+            for k in FIELDS:
+                rec["%s_%s_%s" % (case, tag, k)] = np.copy(getattr(S, k))
+            if tag == "rk":
+                rec[case + "_rk_pwchi"] = np.copy(S.pwchi)
+        rec[case + "_rhoY0"] = np.copy(mpv.HydroState.rhoY0)
+        rec[case + "_meta"] = np.array([9, 7, 8, int(bt[0] == W), int(bt[1] == W), int(bt[2] == W), dt,
+                                        ud.Msq, ud.gravity_strength[1], th.gamm])
+    np.savez_compressed(os.path.join(out, "advect3d_kat.npz"), **rec)
+
+
 def step_kat(out):
     """The reference's whole time step (time_update.do, time_update.py:129-708) on
     the 64x32 rising bubble: the state after one and two steps (fixed dt =
@@ -564,6 +627,7 @@ def main():
     proj3d_kat(out)
     step2d_kat(out)
     advect_kat(out)
+    advect3d_kat(out)
     step_kat(out)
     if "--3d-only" in sys.argv:
         print("fixtures written to", out)
