@@ -237,7 +237,7 @@ int bella_euler_forward2d(const bella_expl2d *args, void *stream);
 /* euler_backward_non_advective_expl_part (second_projection.py:77-92) */
 int bella_expl_part2d(const bella_expl2d *args, void *stream);
 
-/* ---- 2D advection (the reference's explicit.py, recovery.py, numerical_flux.py) --
+/* ---- advection (the reference's explicit.py, recovery.py, numerical_flux.py) --
  * Device arrays in the reference's NumPy C order: cells (inx+3)(iny+3) over (x, y);
  * fx[q]: x-face arrays (iny+3)(inx+4) (elem.sfx: row y, face x), fy[q]: y-face
  * arrays (inx+3)(iny+4), q = rho, rhou, rhov, rhow, rhoY (the face mass flux),
@@ -263,6 +263,26 @@ int bella_advect2d(const bella_adv2d *args, double dt, int odd, void *stream);
 int bella_advect_rk2d(const bella_adv2d *args, double dt, void *stream);
 /* set_explicit_boundary_data (boundary.py:7-216) of the cell state: along x, then y */
 int bella_boundary2d(const bella_adv2d *args, void *stream);
+
+/* The same in 3D: cells (inx+3)(iny+3)(inz+3) over (x, y, z); face arrays as the
+ * reference's elem.sfx = (iny+3)(inz+3)(inx+4), sfy = (inz+3)(inx+3)(iny+4),
+ * sfz = (inx+3)(iny+3)(inz+4); pwchi (cells) after the z sweep's flip, i.e. in
+ * the (x, y, z) order of the state. */
+typedef struct bella_adv3d {
+    int inx, iny, inz;
+    int x_wall, y_wall, z_wall;
+    double dx, dy, dz, g, gamm;
+    int is_compressible;
+    int pad_;
+    double *rho, *rhou, *rhov, *rhow, *rhoY, *rhoX;
+    double *fx[6], *fy[6], *fz[6];
+    const double *hydro_rhoY0, *strat_inv;
+    double *pwchi;
+} bella_adv3d;
+int bella_advective_fluxes3d(const bella_adv3d *args, void *stream);
+int bella_advect3d(const bella_adv3d *args, double dt, int odd, void *stream);
+int bella_advect_rk3d(const bella_adv3d *args, double dt, void *stream);
+int bella_boundary3d(const bella_adv3d *args, void *stream);
 
 /* ---- ensemble: the solves of many 2D members in one persistent launch ----
  * Each member is the reference's call (second_projection.py:205-230) on its own

@@ -74,6 +74,18 @@ class Adv2D(ctypes.Structure):
         [("fx", _dp * 6), ("fy", _dp * 6), ("hydro_rhoY0", _dp), ("strat_inv", _dp), ("pwchi", _dp)]
 
 
+class Adv3D(ctypes.Structure):
+    """``bella_adv3d``: device arrays of the 3D advection (reference layout)."""
+    _fields_ = [("inx", ctypes.c_int), ("iny", ctypes.c_int), ("inz", ctypes.c_int),
+                ("x_wall", ctypes.c_int), ("y_wall", ctypes.c_int), ("z_wall", ctypes.c_int),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
+                ("g", ctypes.c_double), ("gamm", ctypes.c_double),
+                ("is_compressible", ctypes.c_int), ("pad_", ctypes.c_int)] + \
+        [(k, _dp) for k in ("rho", "rhou", "rhov", "rhow", "rhoY", "rhoX")] + \
+        [("fx", _dp * 6), ("fy", _dp * 6), ("fz", _dp * 6), ("hydro_rhoY0", _dp), ("strat_inv", _dp),
+         ("pwchi", _dp)]
+
+
 class Expl2D(ctypes.Structure):
     _fields_ = [("inx", ctypes.c_int), ("iny", ctypes.c_int), ("x_wall", ctypes.c_int), ("y_wall", ctypes.c_int),
                 ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dt", ctypes.c_double),
@@ -131,6 +143,10 @@ SIGNATURES = {
     "bella_advect2d": (ctypes.c_int, [ctypes.POINTER(Adv2D), ctypes.c_double, ctypes.c_int, ctypes.c_void_p]),
     "bella_advect_rk2d": (ctypes.c_int, [ctypes.POINTER(Adv2D), ctypes.c_double, ctypes.c_void_p]),
     "bella_boundary2d": (ctypes.c_int, [ctypes.POINTER(Adv2D), ctypes.c_void_p]),
+    "bella_advective_fluxes3d": (ctypes.c_int, [ctypes.POINTER(Adv3D), ctypes.c_void_p]),
+    "bella_advect3d": (ctypes.c_int, [ctypes.POINTER(Adv3D), ctypes.c_double, ctypes.c_int, ctypes.c_void_p]),
+    "bella_advect_rk3d": (ctypes.c_int, [ctypes.POINTER(Adv3D), ctypes.c_double, ctypes.c_void_p]),
+    "bella_boundary3d": (ctypes.c_int, [ctypes.POINTER(Adv3D), ctypes.c_void_p]),
     "bella_cnn_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int,
                                         ctypes.c_longlong]),
     "bella_cnn_destroy": (ctypes.c_int, [ctypes.c_void_p]),

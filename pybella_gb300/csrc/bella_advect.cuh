@@ -1,15 +1,18 @@
-// bella_adv2d.cuh -- arithmetic of the 2D advection (explicit.py, recovery.py,
-// numerical_flux.py of the reference), one face, cell or boundary line at a time.
+// bella_advect.cuh -- arithmetic of the reference's advection (explicit.py,
+// recovery.py, numerical_flux.py) in 2D and 3D, one face, cell or boundary line
+// at a time.
 //
-// Every function is __host__ __device__: the kernels of bella_adv2d.cu call them
-// one thread per item, and the host build of the same header (tests/adv2d_host.cpp)
+// Every function is __host__ __device__: the kernels of bella_advect.cu call them
+// one thread per item, and the host build of the same header (tests/advect_host.cpp)
 // checks them against the oracle on the CPU.  Arithmetic follows the reference
 // operation by operation (FP64), so that the sweeps reproduce it to rounding.
 //
-// Layout: cell arrays C order over (x, y), icx x icy with two ghost layers.  A
-// sweep along axis s works on lines of the other axis: sweep 0 (x) runs along x
-// at fixed y row l, sweep 1 (y) along y at fixed x column l.  Face arrays of
-// sweep s are (n_other, n_s + 1), face f between cells f-1 and f of a line.
+// Layout: cell arrays C order over (x, y) or (x, y, z), ic[] cells per axis with
+// two ghost layers.  A sweep along axis s works on lines along s; the line index
+// runs over the other axes in the order the reference's flips leave them (the
+// cyclic successors of s: sweep x over (y, z), y over (z, x), z over (x, y)), so
+// the face arrays of sweep s are the reference's elem.sfx / sfy / sfz: (lines,
+// n_s + 1), face f between cells f-1 and f of a line.
 #pragma once
 #include <math.h>
 
@@ -22,9 +25,10 @@
 namespace bella {
 
 struct AdvGeom {
-    int icx, icy;              // cells incl. ghosts
-    int bc[2];                 // 0 periodic, 1 wall
-    double dx, dy;
+    int nd;                    // 2 or 3
+    int ic[3];                 // cells incl. ghosts per axis (ic[2] = 1 in 2D)
+    int bc[3];                 // 0 periodic, 1 wall
+    double d[3];               // dx, dy, dz
     double g, gamm;            // gravity along y (ud.gravity_strength[1]), th.gamm
     int is_compressible;
 };
@@ -37,14 +41,43 @@ struct AdvFaces {              // face arrays of one sweep: rho, rhou, rhov, rho
     double *f[6];
 };
 
-BELLA_HD int adv_ns(const AdvGeom &G, int s) { return s == 0 ? G.icx : G.icy; }
-BELLA_HD int adv_nl(const AdvGeom &G, int s) { return s == 0 ? G.icy : G.icx; }
-// cell (line l, position c) of sweep s -> flat (x, y) index
+BELLA_HD int adv_ns(const AdvGeom &G, int s) { return G.ic[s]; }
+// the other axes of sweep s, outer first
+BELLA_HD int adv_a1(const AdvGeom &G, int s) { return (s + 1) % G.nd; }
+BELLA_HD int adv_a2(const AdvGeom &G, int s) { return (s + 2) % G.nd; }
+BELLA_HD int adv_nl(const AdvGeom &G, int s) {
+    return G.nd == 2 ? G.ic[adv_a1(G, s)] : G.ic[adv_a1(G, s)] * G.ic[adv_a2(G, s)];
+}
+BELLA_HD void adv_coords(const AdvGeom &G, int s, int l, int c, int *x) {
+    x[2] = 0;
+    x[s] = c;
+    if (G.nd == 2) {
+        x[adv_a1(G, s)] = l;
+    } else {
+        const int n2 = G.ic[adv_a2(G, s)];
+        x[adv_a1(G, s)] = l / n2;
+        x[adv_a2(G, s)] = l - (l / n2) * n2;
+    }
+}
+BELLA_HD long long adv_flat(const AdvGeom &G, const int *x) {
+    return G.nd == 2 ? (long long)x[0] * G.ic[1] + x[1] : ((long long)x[0] * G.ic[1] + x[1]) * G.ic[2] + x[2];
+}
+// cell (line l, position c) of sweep s -> flat index of the state arrays
 BELLA_HD long long adv_cell(const AdvGeom &G, int s, int l, int c) {
-    return s == 0 ? (long long)c * G.icy + l : (long long)l * G.icy + c;
+    int x[3];
+    adv_coords(G, s, l, c, x);
+    return adv_flat(G, x);
 }
 BELLA_HD long long adv_face(const AdvGeom &G, int s, int l, int f) {
     return (long long)l * (adv_ns(G, s) + 1) + f;
+}
+// every coordinate of the line off the outer ghost layer (the reference's inner_idx)
+BELLA_HD bool adv_inner_line(const AdvGeom &G, int s, int l) {
+    int x[3];
+    adv_coords(G, s, l, 1, x);
+    for (int a = 0; a < G.nd; ++a)
+        if (a != s && (x[a] < 1 || x[a] > G.ic[a] - 2)) return false;
+    return true;
 }
 
 // set_explicit_boundary_data along axis s for line l of the other axis
@@ -54,7 +87,7 @@ BELLA_HD long long adv_face(const AdvGeom &G, int s, int l, int f) {
 BELLA_HD void adv_bd_line(const AdvGeom &G, int s, int l, const AdvFields &F, const double *hydro_rhoY0,
                           const double *strat_inv) {
     const int n = adv_ns(G, s);
-    if (s == 0 || G.g == 0.0) {
+    if (s != 1 || G.g == 0.0) {
         for (int q = 0; q < 6; ++q) {
             double *a = F.f[q];
             if (G.bc[s] == 0) {
@@ -88,7 +121,7 @@ BELLA_HD void adv_bd_line(const AdvGeom &G, int s, int l, const AdvFields &F, co
             const double Y_last = rhoY[L] / rho[L];
             const double rhoYv_image = -rhov[S_] * rhoY[S_] / rho[S_];
             const double S = strat_inv[cur_idx];
-            const double dpi = direction * (Gamma * G.g) * 0.5 * G.dy * (1.0 / Y_last + S);
+            const double dpi = direction * (Gamma * G.g) * 0.5 * G.d[1] * (1.0 / Y_last + S);
             const double rY = (G.is_compressible == 1) ? pow(pow(rhoY[L], gm1) + dpi, gm1inv) : hydro_rhoY0[cur_idx];
             const double r = rY * S;
             const double v = rhoYv_image / rY;
@@ -131,10 +164,10 @@ BELLA_HD void adv_prims(const AdvGeom &G, int s, int l, int c, const AdvFields &
 
 BELLA_HD void adv_cell_state(const AdvGeom &G, int s, int l, int c, const AdvFields &F, const double *mflux,
                              AdvCell &A) {
-    const int ns = adv_ns(G, s), nl = adv_nl(G, s);
+    const int ns = adv_ns(G, s);
     adv_prims(G, s, l, c, F, A.p);
     A.U = 0.0;
-    if (l >= 1 && l <= nl - 2 && c >= 1 && c <= ns - 2)
+    if (c >= 1 && c <= ns - 2 && adv_inner_line(G, s, l))
         A.U = 0.5 * (mflux[adv_face(G, s, l, c)] + mflux[adv_face(G, s, l, c + 1)]) / F.f[4][adv_cell(G, s, l, c)];
     if (c < ns - 1) {
         double r[5];
@@ -188,7 +221,7 @@ BELLA_HD void adv_face_flux(const AdvGeom &G, int s, int l, int f, const AdvFiel
     double SL[5], SR[5];
     adv_slopes(ns, f - 1, a0, a1, SL);
     adv_slopes(ns, f, a1, a2, SR);
-    // face mass density between cells f-1 and f (recovery.py:117-119), vel = u (x) or v (y)
+    // face mass density between cells f-1 and f (recovery.py:117-119), vel = u, v or w of the sweep
     const long long eL = adv_cell(G, s, l, f - 1), eR = adv_cell(G, s, l, f);
     const double rYL = F.f[4][eL], rYR = F.f[4][eR];
     const double vL = a1.p[s], vR = a2.p[s];
@@ -214,33 +247,34 @@ BELLA_HD void adv_update_cell(const AdvGeom &G, int s, int l, int c, const AdvFi
     for (int q = 0; q < 6; ++q) F.f[q][e] = F.f[q][e] + lmbda * (fl.f[q][a] - fl.f[q][b]);
 }
 
-// face mass fluxes (recompute_advective_fluxes, numerical_flux.py:5-46, 2D): x faces
-// (row j, face f) = weighted 2x3 box of rhoY u, y faces (column i, face f) = 3x2 box
-// of rhoY v, both / 4, on the inner faces
-BELLA_HD double adv_mass_x(const AdvGeom &G, const AdvFields &F, int j, int f) {
+// face mass flux of inner face f of line l of sweep s (recompute_advective_fluxes,
+// numerical_flux.py:5-46): rhoY times the sweep's velocity on the two cells of the
+// face, weighted across it by (0.5, 1, 0.5) over -1..+1 in 2D (sum of weights 4)
+// and by [[1,2,1],[2,4,2],[1,2,1]] over the two other axes in 3D (sum 32).
+// Inner faces: f in 1..n_s-1 on lines off the outer ghost layer.
+BELLA_HD double adv_mass(const AdvGeom &G, int s, int l, int f, const AdvFields &F) {
+    int x0[3];
+    adv_coords(G, s, l, f - 1, x0);
+    const int a1 = adv_a1(G, s), a2 = adv_a2(G, s);
+    const double *mom = F.f[1 + s];
+    const double w1[3] = {0.5, 1.0, 0.5};
+    const double K2[3][3] = {{1, 2, 1}, {2, 4, 2}, {1, 2, 1}};
     double sum = 0.0;
-    for (int p = 0; p < 2; ++p) {
-        const int i = f - 1 + p;
-        for (int q = 0; q < 3; ++q) {
-            const long long e = (long long)i * G.icy + (j - 1 + q);
-            const double w = q == 1 ? 1.0 : 0.5;
-            sum += w * (F.f[4][e] * F.f[1][e] / F.f[0][e]);
-        }
-    }
-    return sum / 4.0;
-}
-
-BELLA_HD double adv_mass_y(const AdvGeom &G, const AdvFields &F, int i, int f) {
-    double sum = 0.0;
-    for (int p = 0; p < 3; ++p) {
-        const int ii = i - 1 + p;
-        const double w = p == 1 ? 1.0 : 0.5;
-        for (int q = 0; q < 2; ++q) {
-            const long long e = (long long)ii * G.icy + (f - 1 + q);
-            sum += w * (F.f[4][e] * F.f[2][e] / F.f[0][e]);
-        }
-    }
-    return sum / 4.0;
+    for (int p = 0; p < 2; ++p)
+        for (int q = 0; q < 3; ++q)
+            for (int r = 0; r < (G.nd == 3 ? 3 : 1); ++r) {
+                int x[3] = {x0[0], x0[1], x0[2]};
+                x[s] += p;
+                x[a1] += q - 1;
+                double w = w1[q];
+                if (G.nd == 3) {
+                    x[a2] += r - 1;
+                    w = K2[q][r];
+                }
+                const long long e = adv_flat(G, x);
+                sum += w * (F.f[4][e] * mom[e] / F.f[0][e]);
+            }
+    return sum / (G.nd == 3 ? 32.0 : 4.0);
 }
 
 }  // namespace bella
@@ -265,34 +299,27 @@ void adv_sweep(Ex &ex, int s, double lmbda) {          // explicit_step_and_flux
 template <class Ex>
 void adv_strang(Ex &ex, const AdvGeom &G, double dt, int odd) {
     const double h = 0.5 * dt;
-    const double lx = h / G.dx, ly = h / G.dy;
+    const int nd = G.nd;
     if (odd) {
-        adv_sweep(ex, 0, lx);
-        adv_sweep(ex, 1, ly);
-        adv_sweep(ex, 1, ly);
-        adv_sweep(ex, 0, lx);
+        for (int s = 0; s < nd; ++s) adv_sweep(ex, s, h / G.d[s]);
+        for (int s = nd - 1; s >= 0; --s) adv_sweep(ex, s, h / G.d[s]);
     } else {
-        adv_sweep(ex, 1, ly);
-        adv_sweep(ex, 0, lx);
-        adv_sweep(ex, 0, lx);
-        adv_sweep(ex, 1, ly);
+        for (int s = nd - 1; s >= 0; --s) adv_sweep(ex, s, h / G.d[s]);
+        for (int s = 0; s < nd; ++s) adv_sweep(ex, s, h / G.d[s]);
     }
-    ex.bd(0);
-    ex.bd(1);
+    for (int s = 0; s < nd; ++s) ex.bd(s);
 }
 
 template <class Ex>
 void adv_rk(Ex &ex, const AdvGeom &G, double dt) {
-    for (int s = 0; s < 2; ++s) {                       // fluxes from the start state (lmbda 0 in recovery)
+    for (int s = 0; s < G.nd; ++s) {                    // fluxes from the start state (lmbda 0 in recovery)
         ex.bd(s);
         ex.faces(s, 0.0);
         ex.bd(s);
     }
-    ex.update(0, dt / G.dx);
-    ex.update(1, dt / G.dy);
-    ex.pwchi(dt / G.dy);
-    ex.bd(0);
-    ex.bd(1);
+    for (int s = 0; s < G.nd; ++s) ex.update(s, dt / G.d[s]);
+    ex.pwchi(dt / G.d[1]);
+    for (int s = 0; s < G.nd; ++s) ex.bd(s);
 }
 
 }  // namespace bella
