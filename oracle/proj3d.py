@@ -296,3 +296,62 @@ def impl_part(Sol, p2_nodes, S0n, hydro_c, strat_fn, grid, prm, dt, Sol0=None, s
     set_explicit_boundary_data(Sol, grid, prm, hydro_c, strat_fn)           # :277
     return dict(rhs=mpv_rhs, b=b, diag_inv=diag_inv, op=op, x=x, info=info, niter=niter,
                 wplus=wplus, wcenter=wcenter, nu_c=nu)
+
+
+# --------------------------------------------------------------------------
+# explicit parts of the projection (second_projection.py:22-92), 3D
+# --------------------------------------------------------------------------
+def mod_bg_wind(Sol, wind, fac):
+    """``Vars.mod_bg_wind`` (variable.py:109-116)."""
+    u0, v0, w0 = wind
+    Sol["rhou"] = Sol["rhou"] + fac * u0 * Sol["rho"]
+    Sol["rhov"] = Sol["rhov"] + fac * v0 * Sol["rho"]
+    Sol["rhow"] = Sol["rhow"] + fac * w0 * Sol["rho"]
+
+
+def euler_backward_non_advective_expl_part(Sol, S0n, grid, prm, dt, hydro_c, strat_fn, wind=(0.0, 0.0, 0.0)):
+    """``euler_backward_non_advective_expl_part`` (second_projection.py:77-92) in 3D;
+    updates ``Sol``.  Dimension-generic in the reference; pinned by proj3d_kat.npz."""
+    dbuoy = Sol["rhoY"] * (Sol["rhoX"] / Sol["rho"])                        # :82
+    Sol["rhov"] = (prm.nonhydro * Sol["rhov"]) - dt * (prm.g / prm.Msq) * dbuoy  # :83
+    mod_bg_wind(Sol, wind, -1.0)                                             # :86
+    U, V, W = multiply_inverse_coriolis(Sol["rhou"], Sol["rhov"], Sol["rhow"], Sol, S0n, grid, prm, dt)  # :88
+    Sol["rhou"], Sol["rhov"], Sol["rhow"] = U, V, W
+    mod_bg_wind(Sol, wind, +1.0)                                             # :90
+    set_explicit_boundary_data(Sol, grid, prm, hydro_c, strat_fn)            # :92
+
+
+def euler_forward_non_advective(Sol, p2, S0c, S0n, grid, prm, dt, hydro_c, strat_fn, wind=(0.0, 0.0, 0.0),
+                                is_ArakawaKonor=0):
+    """``euler_forward_non_advective`` (second_projection.py:22-74) in 3D with the
+    2D branch's glue: the divergence on node.isc (the reference's 3D call writes
+    divergence_nodes' node.sc result into the node.isc ``mpv.rhs`` and cannot
+    run), wall rows doubled there, ``dp2n[node.i1] -= dt * dpidP * div``.
+    Updates ``Sol`` and ``p2`` in place; returns the divergence (``mpv.rhs``)."""
+    corr_h1, corr_v, corr_h2 = prm.coriolis
+    u0, v0, w0 = wind
+    p2n = np.copy(p2)
+    dp2n = np.zeros_like(p2n)
+    dSdy = get_dSdy(S0n, grid)
+    div = divergence_nodes(Sol, grid)[1:-1, 1:-1, 1:-1]                       # :39
+    scale_wall_node_values(div, grid, 2.0)                                   # :40
+    rhoY = Sol["rhoY"] ** (prm.gamm - 2.0)                                   # :45-47
+    kern = np.ones((2, 2, 2))
+    dpidP = (prm.gm1 / prm.Msq) * fftconvolve(rhoY, kern, mode="valid") / kern.sum()
+    rhoYovG = prm.Gammainv * Sol["rhoY"]                                     # :49
+    dbuoy = Sol["rhoY"] * (Sol["rhoX"] / Sol["rho"])
+    dpdx, dpdy, dpdz = grad_nodes(p2n, grid.dx, grid.dy, grid.dz)            # :51
+    drhou = Sol["rhou"] - u0 * Sol["rho"]                                    # :53-56
+    drhov = Sol["rhov"] - v0 * Sol["rho"]
+    drhow = Sol["rhow"] - w0 * Sol["rho"]
+    v = Sol["rhov"] / Sol["rho"]
+    Sol["rhou"] = Sol["rhou"] - dt * (rhoYovG * dpdx - corr_h2 * drhov + corr_v * drhow)          # :58
+    Sol["rhov"] = Sol["rhov"] - dt * (rhoYovG * dpdy + (prm.g / prm.Msq) * dbuoy * prm.nonhydro
+                                      - corr_h1 * drhow + corr_h2 * drhou) * (1 - is_ArakawaKonor)  # :60
+    Sol["rhow"] = Sol["rhow"] - dt * (rhoYovG * dpdz - corr_v * drhou + corr_h1 * drhov) * True     # :62
+    Sol["rhoX"] = (Sol["rho"] * (Sol["rho"] / Sol["rhoY"] - S0c)) - dt * (v * dSdy) * Sol["rho"]  # :64
+    dp2n[1:-1, 1:-1, 1:-1] -= dt * dpidP * div                               # :66
+    p2 += prm.compressibility * dp2n                                         # :68-69
+    set_ghostnodes_p2(p2, grid)                                              # :71
+    set_explicit_boundary_data(Sol, grid, prm, hydro_c, strat_fn)            # :72
+    return div

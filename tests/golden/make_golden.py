@@ -17,7 +17,8 @@ It imports the reference through ``refshim`` (numba, h5py, ... stubbed; SciPy
 * ``wall_kat.npz``    -- ``scale_wall_node_values`` for wall/periodic mixes in
   2D and 3D (its index carries over between wall axes);
 * ``proj3d_kat.npz``  -- the projection pieces in 3D (boundary data,
-  coefficients, divergence, ghost nodes, correction) on two small states;
+  coefficients, divergence, ghost nodes, correction, the explicit part) on two
+  small states;
 * ``step2d_kat.npz``  -- the whole 2D step on 33x17 states with walls in x and
   y, and with Coriolis in the compressible regime;
 * ``advect_kat.npz``  -- the 2D advection (face mass fluxes, Strang-split
@@ -248,6 +249,14 @@ def proj3d_kat(out):
         lm_sp.correction_nodes(S, elem, node, mpv, q, dt, ud, th, 1)
         for k in FIELDS:
             rec["%s_cr_%s" % (tag, k)] = np.copy(getattr(S, k))
+        # euler_backward_non_advective_expl_part (dimension-generic), case b with background wind
+        if tag == "b":
+            ud.u_wind_speed, ud.v_wind_speed, ud.w_wind_speed = 0.5, 0.0, 0.2
+        S = copy.deepcopy(Sol)
+        lm_sp.euler_backward_non_advective_expl_part(S, mpv, elem, dt, ud, th)
+        for k in FIELDS:
+            rec["%s_xp_%s" % (tag, k)] = np.copy(getattr(S, k))
+        rec[tag + "_wind"] = np.array([ud.u_wind_speed, ud.v_wind_speed, ud.w_wind_speed])
         rec[tag + "_S0n"] = np.copy(mpv.HydroState_n.S0)
         rec[tag + "_rhoY0"] = np.copy(mpv.HydroState.rhoY0)
         rec[tag + "_strat_inv"] = np.array([1.0 / ud.stratification(y) for y in elem.y])

@@ -85,8 +85,9 @@ def test_scale_wall_node_values_matches_reference_kat(tag):
 @pytest.mark.parametrize("tag", ["a", "b"])
 def test_projection_pieces_3d_match_reference_kat(tag):
     """The 3D projection pieces (boundary data, coefficients, divergence with its
-    x-sign, ghost nodes, correction with Coriolis) reproduce the reference's
-    outputs bit for bit on periodic/wall and wall/wall states."""
+    x-sign, ghost nodes, correction with Coriolis, the explicit part with
+    background wind) reproduce the reference's outputs bit for bit on
+    periodic/wall and wall/wall states."""
     from conftest import proj3d_case
     from oracle import proj3d as o3
     d = np.load(golden("proj3d_kat.npz"))
@@ -109,6 +110,10 @@ def test_projection_pieces_3d_match_reference_kat(tag):
     o3.correction_nodes(S, q, S0n, grid, prm, dt, 1)
     for k in FIELDS:
         np.testing.assert_array_equal(S[k], d["%s_cr_%s" % (tag, k)], err_msg="correction " + k)
+    S = {k: v.copy() for k, v in Sol.items()}
+    o3.euler_backward_non_advective_expl_part(S, S0n, grid, prm, dt, hc, sf, wind=d[tag + "_wind"])
+    for k in FIELDS:
+        np.testing.assert_array_equal(S[k], d["%s_xp_%s" % (tag, k)], err_msg="explicit part " + k)
 
 
 def _small_rb_state():
