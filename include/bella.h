@@ -284,6 +284,29 @@ int bella_advect3d(const bella_adv3d *args, double dt, int odd, void *stream);
 int bella_advect_rk3d(const bella_adv3d *args, double dt, void *stream);
 int bella_boundary3d(const bella_adv3d *args, void *stream);
 
+/* ---- explicit parts of the projection (3D), in place on device arrays ------
+ * Arrays as in bella_proj3d; S0c: mpv.HydroState.get_S0c(elem) on cells (S0 along
+ * y repeated over x and z); scratch: (inx+2)(iny+2)(inz+2) doubles for the forward
+ * part's pressure increment; rhs_out (mpv.rhs, node.isc) or NULL. */
+typedef struct bella_expl3d {
+    int inx, iny, inz;
+    int x_wall, y_wall, z_wall;
+    double dx, dy, dz, dt;
+    double Msq, g, gamm, nonhydro, compressibility;
+    double coriolis[3];           /* ud.coriolis_strength                              */
+    double wind[3];               /* ud.u_wind_speed, v_wind_speed, w_wind_speed       */
+    int is_compressible, is_ArakawaKonor;
+    double *rho, *rhou, *rhov, *rhow, *rhoY, *rhoX;
+    double *p2, *rhs_out, *scratch;
+    const double *S0c, *S0n, *hydro_rhoY0, *strat_inv;
+} bella_expl3d;
+/* euler_forward_non_advective (second_projection.py:22-74) in 3D, with the glue of the
+ * 2D branch (the reference's 3D call cannot run: it writes divergence_nodes' node.sc
+ * result into the node.isc mpv.rhs): divergence on node.isc, wall rows doubled */
+int bella_euler_forward3d(const bella_expl3d *args, void *stream);
+/* euler_backward_non_advective_expl_part (second_projection.py:77-92) in 3D */
+int bella_expl_part3d(const bella_expl3d *args, void *stream);
+
 /* ---- ensemble: the solves of many 2D members in one persistent launch ----
  * Each member is the reference's call (second_projection.py:205-230) on its own
  * workspace (bella_op2d_set): FP64 BiCGStab, scipy 1.7 control flow, x0 = 0.

@@ -86,6 +86,19 @@ class Adv3D(ctypes.Structure):
          ("pwchi", _dp)]
 
 
+class Expl3D(ctypes.Structure):
+    """``bella_expl3d``: device arrays of the 3D explicit projection parts."""
+    _fields_ = [("inx", ctypes.c_int), ("iny", ctypes.c_int), ("inz", ctypes.c_int),
+                ("x_wall", ctypes.c_int), ("y_wall", ctypes.c_int), ("z_wall", ctypes.c_int),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double), ("dt", ctypes.c_double),
+                ("Msq", ctypes.c_double), ("g", ctypes.c_double), ("gamm", ctypes.c_double),
+                ("nonhydro", ctypes.c_double), ("compressibility", ctypes.c_double),
+                ("coriolis", ctypes.c_double * 3), ("wind", ctypes.c_double * 3),
+                ("is_compressible", ctypes.c_int), ("is_ArakawaKonor", ctypes.c_int)] + \
+        [(k, _dp) for k in ("rho", "rhou", "rhov", "rhow", "rhoY", "rhoX", "p2", "rhs_out", "scratch",
+                            "S0c", "S0n", "hydro_rhoY0", "strat_inv")]
+
+
 class Expl2D(ctypes.Structure):
     _fields_ = [("inx", ctypes.c_int), ("iny", ctypes.c_int), ("x_wall", ctypes.c_int), ("y_wall", ctypes.c_int),
                 ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dt", ctypes.c_double),
@@ -147,6 +160,8 @@ SIGNATURES = {
     "bella_advect3d": (ctypes.c_int, [ctypes.POINTER(Adv3D), ctypes.c_double, ctypes.c_int, ctypes.c_void_p]),
     "bella_advect_rk3d": (ctypes.c_int, [ctypes.POINTER(Adv3D), ctypes.c_double, ctypes.c_void_p]),
     "bella_boundary3d": (ctypes.c_int, [ctypes.POINTER(Adv3D), ctypes.c_void_p]),
+    "bella_euler_forward3d": (ctypes.c_int, [ctypes.POINTER(Expl3D), ctypes.c_void_p]),
+    "bella_expl_part3d": (ctypes.c_int, [ctypes.POINTER(Expl3D), ctypes.c_void_p]),
     "bella_cnn_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int,
                                         ctypes.c_longlong]),
     "bella_cnn_destroy": (ctypes.c_int, [ctypes.c_void_p]),
