@@ -210,6 +210,8 @@ typedef struct bella_proj3d {
     const double *S0n;            /* mpv.HydroState_n.S0 (iny+4 node planes)           */
     const double *strat_inv;      /* 1/ud.stratification(elem.y) (iny+3)               */
     double *rhs_out;              /* mpv.rhs (inx+2)(iny+2)(inz+2) or NULL             */
+    int div_sign_2d;              /* 0: divergence_nodes' 3D sign on its x term (:563);
+                                     1: the 2D branch's sign (the 3D time step needs it) */
 } bella_proj3d;
 int bella_projection3d(bella_ws *ws, const bella_proj3d *args, const bella_solve_opts *opts,
                        bella_solve_stats *stats, void *stream);
@@ -299,6 +301,7 @@ typedef struct bella_expl3d {
     double *rho, *rhou, *rhov, *rhow, *rhoY, *rhoX;
     double *p2, *rhs_out, *scratch;
     const double *S0c, *S0n, *hydro_rhoY0, *strat_inv;
+    int div_sign_2d;              /* as in bella_proj3d */
 } bella_expl3d;
 /* euler_forward_non_advective (second_projection.py:22-74) in 3D, with the glue of the
  * 2D branch (the reference's 3D call cannot run: it writes divergence_nodes' node.sc

@@ -76,11 +76,14 @@ def operator_coefficients_nodes(Sol, S0n, grid, prm, dt):
     return wplus, wcenter, nu
 
 
-def divergence_nodes(Sol, grid):
+def divergence_nodes(Sol, grid, x_sign=-1.0):
     """3D ``divergence_nodes`` (second_projection.py:525-575) on a node.sc array.
 
     Zeroes the momenta in the two ghost rows of a y wall in place (:542-551).
-    The x term carries the reference's 3D sign, ``Ux = -0.5 * (...)`` (:563).
+    The x term carries the reference's 3D sign, ``Ux = -0.5 * (...)`` (:563),
+    unless ``x_sign = +1``: the sign of the 2D branch, with which the 3D time step
+    stays bounded (with the reference's sign it blows up within a few steps,
+    tests/test_oracle_3d.py).
     """
     if grid.wall(1):
         for k in ("rhou", "rhov", "rhow"):
@@ -91,7 +94,7 @@ def divergence_nodes(Sol, grid):
     Ux = 0.5 * (Ux[:, :-1, ...] + Ux[:, 1:, ...])
     Vy = np.diff(Sol["rhov"] * Y, axis=1) / grid.dy
     Vy = 0.5 * (Vy[:-1, ...] + Vy[1:, ...])
-    Ux = -0.5 * (Ux[..., :-1] + Ux[..., 1:])
+    Ux = (0.5 * x_sign) * (Ux[..., :-1] + Ux[..., 1:])
     Vy = 0.5 * (Vy[..., :-1] + Vy[..., 1:])
     Wz = np.diff(Sol["rhow"] * Y, axis=2) / grid.dz
     Wz = 0.5 * (Wz[:-1, ...] + Wz[1:, ...])
@@ -254,7 +257,7 @@ def _gravity_ghosts(Sol, grid, prm, hydro_c, strat_fn):
         offset += 1
 
 
-def impl_part(Sol, p2_nodes, S0n, hydro_c, strat_fn, grid, prm, dt, Sol0=None, solver=None):
+def impl_part(Sol, p2_nodes, S0n, hydro_c, strat_fn, grid, prm, dt, Sol0=None, solver=None, x_sign=-1.0):
     """The 3D projection step from the pinned pieces, with the glue of the 2D branch.
 
     Same order as second_projection.py:113-277.  ``Sol`` (dict of cell arrays)
@@ -270,7 +273,7 @@ def impl_part(Sol, p2_nodes, S0n, hydro_c, strat_fn, grid, prm, dt, Sol0=None, s
     set_ghostnodes_p2(p2_nodes, grid)                                       # :130
     correction_nodes(Sol, p2_nodes, S0n, grid, prm, dt, 0)                  # :131
     set_explicit_boundary_data(Sol, grid, prm, hydro_c, strat_fn)           # :132
-    rhs = divergence_nodes(Sol, grid)[1:-1, 1:-1, 1:-1]                     # :134, on node.isc
+    rhs = divergence_nodes(Sol, grid, x_sign)[1:-1, 1:-1, 1:-1]             # :134, on node.isc
     rhs = rhs / dt                                                          # :139
     i1 = (slice(1, -1),) * 3
     if prm.is_compressible == 1:
@@ -322,7 +325,7 @@ def euler_backward_non_advective_expl_part(Sol, S0n, grid, prm, dt, hydro_c, str
 
 
 def euler_forward_non_advective(Sol, p2, S0c, S0n, grid, prm, dt, hydro_c, strat_fn, wind=(0.0, 0.0, 0.0),
-                                is_ArakawaKonor=0):
+                                is_ArakawaKonor=0, x_sign=-1.0):
     """``euler_forward_non_advective`` (second_projection.py:22-74) in 3D with the
     2D branch's glue: the divergence on node.isc (the reference's 3D call writes
     divergence_nodes' node.sc result into the node.isc ``mpv.rhs`` and cannot
@@ -333,7 +336,7 @@ def euler_forward_non_advective(Sol, p2, S0c, S0n, grid, prm, dt, hydro_c, strat
     p2n = np.copy(p2)
     dp2n = np.zeros_like(p2n)
     dSdy = get_dSdy(S0n, grid)
-    div = divergence_nodes(Sol, grid)[1:-1, 1:-1, 1:-1]                       # :39
+    div = divergence_nodes(Sol, grid, x_sign)[1:-1, 1:-1, 1:-1]               # :39
     scale_wall_node_values(div, grid, 2.0)                                   # :40
     rhoY = Sol["rhoY"] ** (prm.gamm - 2.0)                                   # :45-47
     kern = np.ones((2, 2, 2))

@@ -62,7 +62,8 @@ class Proj3D(ctypes.Structure):
                 ("coriolis", ctypes.c_double * 3), ("is_compressible", ctypes.c_int), ("precond", ctypes.c_int)] + \
         [(k, _dp) for k in ("rho", "rhou", "rhov", "rhow", "rhoY", "rhoX",
                             "rho0", "rhou0", "rhov0", "rhow0", "rhoY0", "rhoX0",
-                            "p2", "hydro_rhoY0", "S0n", "strat_inv", "rhs_out")]
+                            "p2", "hydro_rhoY0", "S0n", "strat_inv", "rhs_out")] + \
+        [("div_sign_2d", ctypes.c_int)]
 
 
 class Adv2D(ctypes.Structure):
@@ -96,7 +97,8 @@ class Expl3D(ctypes.Structure):
                 ("coriolis", ctypes.c_double * 3), ("wind", ctypes.c_double * 3),
                 ("is_compressible", ctypes.c_int), ("is_ArakawaKonor", ctypes.c_int)] + \
         [(k, _dp) for k in ("rho", "rhou", "rhov", "rhow", "rhoY", "rhoX", "p2", "rhs_out", "scratch",
-                            "S0c", "S0n", "hydro_rhoY0", "strat_inv")]
+                            "S0c", "S0n", "hydro_rhoY0", "strat_inv")] + \
+        [("div_sign_2d", ctypes.c_int)]
 
 
 class Expl2D(ctypes.Structure):

@@ -101,6 +101,7 @@ bool e3_setup(const bella_expl3d *a, Expl3Geom &G, Expl3Fields &F, AdvGeom &A, A
         G.wind[q] = a->wind[q];
     }
     G.is_ArakawaKonor = a->is_ArakawaKonor;
+    G.xsign = a->div_sign_2d ? 1.0 : -1.0;
     double *f[6] = {a->rho, a->rhou, a->rhov, a->rhow, a->rhoY, a->rhoX};
     for (int q = 0; q < 6; ++q) F.f[q] = AF.f[q] = f[q];
     A.nd = 3;

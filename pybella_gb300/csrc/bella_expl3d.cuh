@@ -23,6 +23,7 @@ struct Expl3Geom {
     double Msq, g, gamm, nonhydro, compressibility;
     double cor[3];                   // ud.coriolis_strength
     double wind[3];                  // ud.u_wind_speed, v_wind_speed, w_wind_speed
+    double xsign;                    // divergence x term: -1 as divergence_nodes' 3D branch, +1 as its 2D branch
     int is_ArakawaKonor;
 };
 
@@ -113,7 +114,7 @@ BELLA_HD double e3_forward_node(const Expl3Geom &G, int a, int b, int c, const E
         const double f1 = (q(rhow, a + 1, b + t, c + 1) - q(rhow, a + 1, b + t, c)) / G.dz;
         wz[t] = 0.5 * (f0 + f1);
     }
-    const double Ux = -0.5 * (ux[0] + ux[1]);
+    const double Ux = (0.5 * G.xsign) * (ux[0] + ux[1]);
     const double Vy = 0.5 * (vy[0] + vy[1]);
     const double Wz = 0.5 * (wz[0] + wz[1]);
     double div = (Ux + Vy + Wz);

@@ -31,6 +31,7 @@ struct Proj3Dev {
     int ncx, ncy, ncz;     // nodes incl. ghosts (inx+4, iny+4, inz+4)
     int bc[3];             // 0 periodic, 1 wall
     double dx, dy, dz, dt, Msq, g, gamm, nonhydro, compressibility, wh1, wv, wh2;
+    double xsign;          // divergence x term: -1 as divergence_nodes' 3D branch, +1 as its 2D branch
     int is_compressible;
 };
 
@@ -200,7 +201,8 @@ __global__ void k3_zero_ghost(Proj3Dev P, double *rhou, double *rhov, double *rh
 }
 
 // divergence_nodes, 3D branch (second_projection.py:556-570) on node.isc, with the
-// reference's sign on the x term (Ux = -0.5 * (...), :563); /dt (:139), the
+// reference's sign on the x term (Ux = -0.5 * (...), :563) or the 2D branch's
+// (P.xsign); /dt (:139), the
 // regime mix (:149-150), b = (rhs * diag_inv)[inner] in C order (:170, :224)
 __global__ void k3_divergence(Proj3Dev P, const double *rho, const double *rhou, const double *rhov,
                               const double *rhow, const double *rhoY, const double *dinv_isc, double *rhs_isc,
@@ -227,7 +229,7 @@ __global__ void k3_divergence(Proj3Dev P, const double *rho, const double *rhou,
         const double f1 = (qw(a + 1, b + t, c + 1) - qw(a + 1, b + t, c)) / P.dz;
         wz[t] = 0.5 * (f0 + f1);
     }
-    const double Ux = -0.5 * (ux[0] + ux[1]);
+    const double Ux = (0.5 * P.xsign) * (ux[0] + ux[1]);
     const double Vy = 0.5 * (vy[0] + vy[1]);
     const double Wz = 0.5 * (wz[0] + wz[1]);
     double rhs = (Ux + Vy + Wz) / P.dt;
@@ -364,6 +366,7 @@ extern "C" int bella_projection3d(bella_ws *ws, const bella_proj3d *a, const bel
     P.nonhydro = a->nonhydro; P.compressibility = a->compressibility;
     P.wh1 = a->dt * a->coriolis[0]; P.wv = a->dt * a->coriolis[1]; P.wh2 = a->dt * a->coriolis[2];
     P.is_compressible = a->is_compressible;
+    P.xsign = a->div_sign_2d ? 1.0 : -1.0;
     const long long ncell = (long long)P.icx * P.icy * P.icz, nnode = (long long)P.ncx * P.ncy * P.ncz;
     const long long nisc = (long long)(P.icx - 1) * (P.icy - 1) * (P.icz - 1);
     const long long nin = (long long)a->inx * a->iny * a->inz;

@@ -48,7 +48,7 @@ def _workspace(dev):
 
 def euler_backward_non_advective_impl_part(Sol, mpv, elem, node, ud, th, t, dt, alpha_diff, Sol0=None,
                                            writer=None, label=None, debug=False, precision="df64",
-                                           stats=None, device=None, preconditioner="none"):
+                                           stats=None, device=None, preconditioner="none", div_sign_2d=False):
     """Implicit nodal pressure projection of one (half) time step on the GPU.
 
     Mirrors second_projection.py:97-277 in 2D (``bella_projection2d``) and in 3D
@@ -57,7 +57,9 @@ def euler_backward_non_advective_impl_part(Sol, mpv, elem, node, ud, th, t, dt, 
     arithmetic ('df64' double-float by default, 'fp64', 'mixed'); the stop test
     is the reference's ``tol=ud.tol`` on the FP64 true residual.
     ``preconditioner='background'`` solves with the background solve as the
-    preconditioner of flexible BiCGStab (y must be a wall).
+    preconditioner of flexible BiCGStab (y must be a wall).  3D: ``div_sign_2d``
+    gives the divergence's x term the 2D branch's sign instead of the 3D
+    branch's (second_projection.py:563), which a 3D time step needs to stay bounded.
     """
     global total_iter, total_calls
     if elem.ndim not in (2, 3):
@@ -82,6 +84,7 @@ def euler_backward_non_advective_impl_part(Sol, mpv, elem, node, ud, th, t, dt, 
     args.precond = 1 if preconditioner == "background" else 0
     if three:
         args.inz, args.z_wall, args.dz = int(node.iicz), int(_is_wall(ud.bdry_type[2])), float(node.dz)
+        args.div_sign_2d = int(bool(div_sign_2d))
     args.Msq, args.g, args.gamm = float(ud.Msq), float(ud.gravity_strength[1]), float(th.gamm)
     args.nonhydro, args.compressibility = float(ud.nonhydrostasy), float(ud.compressibility)
     for k in range(3):

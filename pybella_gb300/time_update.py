@@ -145,3 +145,137 @@ class DeviceStep2D:
         for k in _FIELDS:
             setattr(Sol, k, self.f[k].cpu().numpy())
         mpv.p2_nodes[...] = self.p2.cpu().numpy()
+
+
+class DeviceStep3D:
+    """The 3D time step with the state resident on the GPU (the reference's
+    ``time_update.do`` in 3D, which the reference itself cannot run: its 3D
+    projection step and forward explicit part break on unassigned names and
+    array shapes).  The same stages as :class:`DeviceStep2D` on the 3D entry
+    points (``bella_advect3d``, ``bella_advect_rk3d``, ``bella_expl_part3d``,
+    ``bella_euler_forward3d``, ``bella_projection3d``), with the divergence's x
+    term in the 2D branch's sign: with the reference's 3D sign the step blows up
+    within a few steps.  ``preconditioner='background'`` solves the projections
+    with the background solve (y a wall).
+    """
+
+    def __init__(self, Sol, mpv, elem, node, ud, th, device=None, preconditioner="none"):
+        if elem.ndim != 3:
+            raise NotImplementedError("DeviceStep3D is the 3D step")
+        if int(ud.is_compressible) != 0:
+            raise NotImplementedError("the pseudo-incompressible step only")
+        self.dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        d = lambda a: torch.tensor(np.ascontiguousarray(a, dtype=np.float64), device=self.dev)
+        self.f = {k: d(getattr(Sol, k)) for k in _FIELDS}
+        self.f0 = {k: torch.empty_like(v) for k, v in self.f.items()}
+        self.p2 = d(mpv.p2_nodes)
+        icx, icy, icz = self.f["rho"].shape
+        z = lambda *shape: torch.zeros(shape, dtype=torch.float64, device=self.dev)
+        self.fx = [z(icy, icz, icx + 1) for _ in _FIELDS]
+        self.fy = [z(icz, icx, icy + 1) for _ in _FIELDS]
+        self.fz = [z(icx, icy, icz + 1) for _ in _FIELDS]
+        self.pwchi = z(icx, icy, icz)
+        self.rhs = z(icx - 1, icy - 1, icz - 1)
+        self.scratch = z(icx - 1, icy - 1, icz - 1)
+        self.S0c = d(mpv.HydroState.get_S0c(elem))
+        self.S0n = d(mpv.HydroState_n.S0)
+        self.rhoY0 = d(mpv.HydroState.rhoY0)
+        self.strat_inv = d(np.array([1.0 / ud.stratification(y) for y in elem.y], dtype=np.float64))
+        self.ws = _lib.Workspace(self.dev.index)
+        self.lib = self.ws._lib
+        p = lambda t: ctypes.c_void_p(t.data_ptr())
+        inx, iny, inz = int(node.iicx), int(node.iicy), int(node.iicz)
+        walls = [int(_is_wall(ud.bdry_type[k])) for k in range(3)]
+        dx, dy, dz = float(node.dx), float(node.dy), float(node.dz)
+        g, gamm = float(ud.gravity_strength[1]), float(th.gamm)
+        a = _lib.Adv3D()
+        a.inx, a.iny, a.inz = inx, iny, inz
+        a.x_wall, a.y_wall, a.z_wall = walls
+        a.dx, a.dy, a.dz, a.g, a.gamm, a.is_compressible = dx, dy, dz, g, gamm, 0
+        for k in _FIELDS:
+            setattr(a, k, p(self.f[k]))
+        for q in range(6):
+            a.fx[q], a.fy[q], a.fz[q] = p(self.fx[q]), p(self.fy[q]), p(self.fz[q])
+        a.hydro_rhoY0, a.strat_inv, a.pwchi = p(self.rhoY0), p(self.strat_inv), p(self.pwchi)
+        self.adv = a
+        e = _lib.Expl3D()
+        e.inx, e.iny, e.inz = inx, iny, inz
+        e.x_wall, e.y_wall, e.z_wall = walls
+        e.dx, e.dy, e.dz = dx, dy, dz
+        e.Msq, e.g, e.gamm = float(ud.Msq), g, gamm
+        e.nonhydro, e.compressibility = float(ud.nonhydrostasy), float(ud.compressibility)
+        for k in range(3):
+            e.coriolis[k] = float(ud.coriolis_strength[k])
+        e.wind[0], e.wind[1], e.wind[2] = float(ud.u_wind_speed), float(ud.v_wind_speed), float(ud.w_wind_speed)
+        e.is_compressible, e.is_ArakawaKonor = 0, int(getattr(ud, "is_ArakawaKonor", 0))
+        for k in _FIELDS:
+            setattr(e, k, p(self.f[k]))
+        e.p2, e.rhs_out, e.scratch = p(self.p2), p(self.rhs), p(self.scratch)
+        e.S0c, e.S0n, e.hydro_rhoY0, e.strat_inv = p(self.S0c), p(self.S0n), p(self.rhoY0), p(self.strat_inv)
+        e.div_sign_2d = 1
+        self.expl = e
+        r = _lib.Proj3D()
+        r.inx, r.iny, r.inz = inx, iny, inz
+        r.x_wall, r.y_wall, r.z_wall = walls
+        r.dx, r.dy, r.dz = dx, dy, dz
+        r.Msq, r.g, r.gamm = float(ud.Msq), g, gamm
+        r.nonhydro, r.compressibility = float(ud.nonhydrostasy), float(ud.compressibility)
+        for k in range(3):
+            r.coriolis[k] = float(ud.coriolis_strength[k])
+        r.is_compressible = 0
+        r.precond = 1 if preconditioner == "background" else 0
+        r.div_sign_2d = 1
+        for k in _FIELDS:
+            setattr(r, k, p(self.f[k]))
+        r.p2, r.rhs_out = p(self.p2), p(self.rhs)
+        r.hydro_rhoY0, r.S0n, r.strat_inv = p(self.rhoY0), p(self.S0n), p(self.strat_inv)
+        self.proj = r
+        self.opts = _lib.SolveOpts()
+        self.lib.bella_solve_opts_default(ctypes.byref(self.opts))
+        self.opts.tol, self.opts.maxiter = float(ud.tol), int(ud.max_iterations)
+        self.stats = []
+
+    def _stream(self):
+        return ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
+
+    def _project(self, dt, with_sol0):
+        r = self.proj
+        r.dt = float(dt)
+        for k in _FIELDS:
+            setattr(r, k + "0", ctypes.c_void_p(self.f0[k].data_ptr()) if with_sol0 else ctypes.c_void_p(0))
+        st = _lib.SolveStats()
+        rc = self.lib.bella_projection3d(self.ws.handle, ctypes.byref(r), ctypes.byref(self.opts), ctypes.byref(st),
+                                         self._stream())
+        _lib.check(rc, "bella_projection3d")
+        self.stats.append(st.as_dict())
+
+    def _expl_part(self, dt):
+        self.expl.dt = float(dt)
+        _lib.check(self.lib.bella_expl_part3d(ctypes.byref(self.expl), self._stream()), "bella_expl_part3d")
+
+    def step(self, step, dt, precision="fp64"):
+        """One time step of length ``dt``."""
+        self.opts.precision = {"fp64": 0, "mixed": 1, "df64": 2}[precision]
+        lib, s, h = self.lib, self._stream(), 0.5 * dt
+        with torch.cuda.device(self.dev):
+            _lib.check(lib.bella_boundary3d(ctypes.byref(self.adv), s), "bella_boundary3d")
+            for k in _FIELDS:
+                self.f0[k].copy_(self.f[k])
+            _lib.check(lib.bella_advective_fluxes3d(ctypes.byref(self.adv), s), "bella_advective_fluxes3d")
+            _lib.check(lib.bella_advect_rk3d(ctypes.byref(self.adv), h, s), "bella_advect_rk3d")
+            self._expl_part(h)
+            self._project(h, True)
+            _lib.check(lib.bella_advective_fluxes3d(ctypes.byref(self.adv), s), "bella_advective_fluxes3d")
+            for k in _FIELDS:
+                self.f[k].copy_(self.f0[k])
+            self.expl.dt = float(h)
+            _lib.check(lib.bella_euler_forward3d(ctypes.byref(self.expl), s), "bella_euler_forward3d")
+            _lib.check(lib.bella_advect3d(ctypes.byref(self.adv), dt, int(step) % 2, s), "bella_advect3d")
+            self._expl_part(h)
+            self._project(h, False)
+
+    def download(self, Sol, mpv):
+        torch.cuda.synchronize(self.dev)
+        for k in _FIELDS:
+            setattr(Sol, k, self.f[k].cpu().numpy())
+        mpv.p2_nodes[...] = self.p2.cpu().numpy()

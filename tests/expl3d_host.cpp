@@ -9,13 +9,14 @@ using namespace bella;
 
 namespace {
 
-// ints: icx, icy, icz, walls[3], is_compressible, is_ArakawaKonor
+// ints: icx, icy, icz, walls[3], is_compressible, is_ArakawaKonor, div_sign_2d
 // doubles: dx, dy, dz, dt, Msq, g, gamm, nonhydro, compressibility, cor[3], wind[3]
 void setup(const int *gi, const double *gd, double **fields, Expl3Geom &G, Expl3Fields &F, AdvGeom &A,
            AdvFields &AF) {
     G.icx = gi[0]; G.icy = gi[1]; G.icz = gi[2];
     for (int q = 0; q < 3; ++q) G.bc[q] = gi[3 + q];
     G.is_ArakawaKonor = gi[7];
+    G.xsign = gi[8] ? 1.0 : -1.0;
     G.dx = gd[0]; G.dy = gd[1]; G.dz = gd[2]; G.dt = gd[3];
     G.Msq = gd[4]; G.g = gd[5]; G.gamm = gd[6]; G.nonhydro = gd[7]; G.compressibility = gd[8];
     for (int q = 0; q < 3; ++q) {

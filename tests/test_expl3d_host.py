@@ -31,8 +31,9 @@ def _ptr(a):
     return ctypes.c_void_p(a.ctypes.data)
 
 
-def _geom(grid, prm, dt, wind, ak=0):
-    gi = np.array([*grid.elem_sc, *[int(grid.wall(d)) for d in range(3)], prm.is_compressible, ak], dtype=np.int32)
+def _geom(grid, prm, dt, wind, ak=0, sign_2d=0):
+    gi = np.array([*grid.elem_sc, *[int(grid.wall(d)) for d in range(3)], prm.is_compressible, ak, sign_2d],
+                  dtype=np.int32)
     gd = np.array([grid.dx, grid.dy, grid.dz, dt, prm.Msq, prm.g, prm.gamm, prm.nonhydro, prm.compressibility,
                    *prm.coriolis, *wind])
     return gi, gd
@@ -57,11 +58,12 @@ def test_expl_part3d_host_vs_reference(host_lib, tag):
                                    err_msg=k)
 
 
+@pytest.mark.parametrize("sign_2d", [0, 1])
 @pytest.mark.parametrize("walls,cor,wind", [
     ((False, True, False), (0.0, 0.0, 0.0), (0.0, 0.0, 0.0)),
     ((True, True, False), (3.0, 2.0, 1.0), (0.5, 0.0, 0.2)),
 ])
-def test_euler_forward3d_host_vs_oracle(host_lib, walls, cor, wind):
+def test_euler_forward3d_host_vs_oracle(host_lib, walls, cor, wind, sign_2d):
     """Momenta, rhoX, the divergence (mpv.rhs) bit for bit; p2 (compressible, so the
     increment counts) to rounding: the oracle's 2x2x2 mean of rhoY^(gamma-2) is an
     FFT convolution."""
@@ -73,12 +75,13 @@ def test_euler_forward3d_host_vs_oracle(host_lib, walls, cor, wind):
     dt = 0.02
     So = {k: v.copy() for k, v in Sol.items()}
     po = p2.copy()
-    div = o3.euler_forward_non_advective(So, po, S0c, hn["S0"], grid, prm, dt, hc, sf, wind=wind)
+    div = o3.euler_forward_non_advective(So, po, S0c, hn["S0"], grid, prm, dt, hc, sf, wind=wind,
+                                         x_sign=1.0 if sign_2d else -1.0)
     F = [np.ascontiguousarray(Sol[k]).copy() for k in FIELDS]
     ph = np.ascontiguousarray(p2).copy()
     rhs = np.zeros(grid.node_isc)
     dp = np.zeros(grid.node_isc)
-    gi, gd = _geom(grid, prm, dt, wind)
+    gi, gd = _geom(grid, prm, dt, wind, sign_2d=sign_2d)
     sinv = np.ones(grid.elem_sc[1])
     host_lib.e3_host_forward(_ptr(gi), _ptr(gd), (ctypes.c_void_p * 6)(*[a.ctypes.data for a in F]), _ptr(ph),
                              _ptr(rhs), _ptr(dp), _ptr(S0c), _ptr(np.ascontiguousarray(hn["S0"])),

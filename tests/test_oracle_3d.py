@@ -197,3 +197,33 @@ def test_background2d_inverse_exact_walls_and_hcenter(x_wall, with_hc):
         X[:, -1] = X[:, 0]
     r = n2.lap2d_gather(X.reshape(-1), op)
     assert np.linalg.norm(n2.lap2d_gather(B.apply(r), op) - r) <= 1e-11 * np.linalg.norm(r)
+
+
+def test_3d_step_needs_the_2d_divergence_sign():
+    """The reference's 3D divergence_nodes flips the sign of its x term
+    (second_projection.py:563).  Four 3D time steps of the warm bubble (17x9x17,
+    dt 21.69 ms): with the reference's sign the divergence of the projected
+    momenta grows every step and the state turns non-finite; with the 2D
+    branch's sign it stays small and the bubble rises smoothly."""
+    from oracle import advection3d as a3, cases, step3d
+    results = {}
+    for x_sign in (-1.0, 1.0):
+        grid, prm, Sol, p2, hn, hc, sf = cases.bubble_3d(17, 9, 17, seed=3, tol=1e-12, wind=0.0)
+        S0c = np.broadcast_to(hc["S0"][None, :, None], grid.elem_sc).copy()
+        flux = a3.new_flux(grid)
+        divs = []
+        with np.errstate(all="ignore"):
+            for step in range(4):
+                Sol = step3d.time_step(Sol, p2, flux, step, 0.02169, grid, prm, hn, hc, S0c, sf, x_sign=x_sign)
+                check = {k: v.copy() for k, v in Sol.items()}
+                divs.append(np.abs(o3_div(check, grid)).max())
+        results[x_sign] = (divs, Sol)
+    bad, good = results[-1.0], results[1.0]
+    assert not np.all(np.isfinite(bad[1]["rhov"])) or bad[0][-1] > 10.0 * bad[0][0], bad[0]
+    assert np.all(np.isfinite(good[1]["rhov"])) and good[0][-1] < 1e-2 * good[0][0], good[0]
+
+
+def o3_div(Sol, grid):
+    """The nodal divergence with the 2D branch's sign, away from the walls."""
+    from oracle import proj3d as o3
+    return o3.divergence_nodes(Sol, grid, x_sign=1.0)[3:-3, 3:-3, 3:-3]
