@@ -121,7 +121,7 @@ def _kminus3_field(shape, rng, power=3.0):
     amp = np.zeros_like(K)
     nz = K > 0
     amp[nz] = K[nz] ** (-0.5 * power)
-    f = np.fft.irfftn(F * amp, s=shape)
+    f = np.fft.irfftn(F * amp, s=shape, axes=tuple(range(len(shape))))
     f -= f.mean()
     return f / f.std()
 
