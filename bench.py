@@ -60,7 +60,7 @@ def _args():
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--workload", default="learned3d", choices=["solve2d", "ensemble", "learned3d"])
+    ap.add_argument("--workload", default="learned3d", choices=["solve2d", "ensemble", "learned3d", "step3d"])
     ap.add_argument("--nz", type=int, default=257)
     ap.add_argument("--train-steps", type=int, default=1000)
     ap.add_argument("--skip", type=float, default=0.9)
@@ -789,11 +789,66 @@ def run_reference_3d(args):
     print(json.dumps(line), flush=True)
 
 
+def run_step3d(args):
+    """``--workload step3d``: whole 3D time steps of the warm bubble (advection,
+    explicit and implicit projection halves, background-preconditioned solves to
+    1e-10) with the state resident on the GPU; value = steps/s.  Replicas under
+    torchrun.  The reference cannot run a 3D step, so there is no CPU arm."""
+    import torch
+    from types import SimpleNamespace as NS
+    from pybella_gb300 import workloads
+    from pybella_gb300.time_update import DeviceStep3D
+    world, rank, local = _dist()
+    torch.cuda.set_device(local)
+    nx, ny, nz = args.nx, args.ny, args.nz
+    st = workloads.bubble_3d_state(nx, ny, nz, seed=11 + rank)
+    run = DeviceStep3D(st["Sol"], st["mpv"], st["elem"], st["node"], st["ud"], st["th"], device=local,
+                       preconditioner="background")
+    dt = 0.02169
+    for k in range(args.warmup):
+        run.step(k, dt)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for k in range(args.steps):
+        run.step(args.warmup + k, dt)
+    e1.record()
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    if rank == 0:
+        its = [s_["iterations"] for s_ in run.stats[-2 * args.steps:]]
+        print(json.dumps({"metric": "3D time steps/s (warm bubble, projections to 1e-10)", "value": world * 1000.0 / ms,
+                          "unit": "steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "f64 state, f32/f64 solves", "data": "synthetic",
+                          "config": {"workload": "3D time step %dx%dx%d nodes, rising-bubble background, "
+                                                 "background-preconditioned projections" % (nx, ny, nz),
+                                     "parallelism": "replicas" if world > 1 else "single GPU",
+                                     "l2": "state of %.1f GB resident, larger than L2" % (
+                                         6 * 8 * (nx + 2) * (ny + 2) * (nz + 2) / 1e9)},
+                          "solve_iterations": its, "clocks": clocks, "cpu_baseline": None,
+                          "gpu_launches": None}), flush=True)
+
+
 def main():
     args = _args()
-    if args.workload == "learned3d" and args.nx == NX and args.ny == NY:
+    if args.workload in ("learned3d", "step3d") and args.nx == NX and args.ny == NY:
         args.nx, args.ny = 257, 129
     if args.impl == "reference":
+        if args.workload == "step3d":
+            if _dist()[1] == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference's 3D time step cannot run "
+                                  "(second_projection.py:183-203 use diag_inv and p2 unassigned)"}))
+            return
         if args.workload == "learned3d":
             run_reference_3d(args)
         else:
@@ -802,6 +857,8 @@ def main():
         run_ensemble(args)
     elif args.workload == "learned3d":
         run_learned3d(args)
+    elif args.workload == "step3d":
+        run_step3d(args)
     else:
         run_gpu(args)
 

@@ -269,3 +269,50 @@ def rising_bubble_ensemble(seed, per_grid=16, grids=ENSEMBLE_GRIDS, device="cuda
             x0 = rng.normal(0.0, 200.0 / H_REF)
             members.append(rising_bubble_member(cells, amp, x0, device=device))
     return members
+
+
+def bubble_3d_state(nx, ny, nz, seed=0, delth=2.0, y0=0.2, r0=0.2, grav=10.0, t_ref=1000.0):
+    """The state of a 3D warm-bubble run in the reference's objects (host NumPy
+    arrays): the rising bubble's set-up (inputs/rising_bubble.py:42-98) on x, z in
+    [-1, 1] (periodic), y in [0, 1] (walls), nx x ny x nz nodes, the bubble centred
+    at x = z = 0 (its amplitude shifted by ``seed`` * 1e-3 K so that replicas differ),
+    the isentropic hydrostatic background of hydrostatics.state (hydrostatics.py:
+    79-117), fluid at rest.  Returns a dict with ``Sol``, ``mpv``, ``elem``,
+    ``node``, ``ud``, ``th`` for :class:`pybella_gb300.time_update.DeviceStep3D`."""
+    from types import SimpleNamespace as NS
+    ig = 2
+    u_ref = H_REF / t_ref
+    Msq = u_ref * u_ref / (R_GAS * T_REF)
+    g = grav * H_REF / (R_GAS * T_REF)
+    Gamma, gm1inv = (GAMM - 1.0) / GAMM, 1.0 / (GAMM - 1.0)
+    dx, dy, dz = 2.0 / (nx - 1.0), 1.0 / (ny - 1.0), 2.0 / (nz - 1.0)
+    sc = (nx - 1 + 2 * ig, ny - 1 + 2 * ig, nz - 1 + 2 * ig)
+    ex = -1.0 - ig * dx + 0.5 * dx + dx * np.arange(sc[0])
+    ey = 0.0 - ig * dy + 0.5 * dy + dy * np.arange(sc[1])
+    ez = -1.0 - ig * dz + 0.5 * dz + dz * np.arange(sc[2])
+    ny_ = 0.0 - ig * dy + dy * np.arange(ny + 2 * ig)
+    Hex = 1.0 / (Gamma * g)
+
+    def column(y):
+        pi_p, pi_m, pi = np.exp(-(y + 0.5 * dy) / Hex), np.exp(-(y - 0.5 * dy) / Hex), np.exp(-y / Hex)
+        Y = -Gamma * g * dy / (pi_p - pi_m)
+        return pi ** gm1inv, Y                           # rhoY0 and Y0 (hydrostatics.py:92-112)
+    rhoY0_c, _ = column(ey)
+    _, Y0_n = column(ny_)
+    X, Yg, Z = np.meshgrid(ex, ey, ez, indexing="ij")
+    r = np.sqrt(X ** 2 + (Yg - y0) ** 2 + Z ** 2) / r0
+    pert = ((delth + 1e-3 * seed) / 300.0) * np.cos(0.5 * np.pi * r) ** 2
+    pert[r > 1.0] = 0.0
+    rhoY = np.broadcast_to(rhoY0_c[None, :, None], sc).copy()
+    rho = rhoY / (1.0 + pert)
+    z = np.zeros(sc)
+    Sol = NS(rho=rho, rhou=z.copy(), rhov=z.copy(), rhow=z.copy(), rhoY=rhoY, rhoX=z.copy())
+    S0c = np.broadcast_to((1.0 / column(ey)[1])[None, :, None], sc).copy()
+    mpv = NS(p2_nodes=np.zeros((nx + 2 * ig, ny + 2 * ig, nz + 2 * ig)),
+             HydroState=NS(rhoY0=rhoY0_c, get_S0c=lambda elem: S0c), HydroState_n=NS(S0=1.0 / Y0_n))
+    elem = NS(ndim=3, y=ey)
+    node = NS(iicx=nx, iicy=ny, iicz=nz, dx=dx, dy=dy, dz=dz)
+    ud = NS(bdry_type=["wrap", "symmetric", "wrap"], gravity_strength=[0.0, g, 0.0], Msq=Msq, nonhydrostasy=1.0,
+            compressibility=0.0, is_compressible=0, coriolis_strength=np.zeros(3), u_wind_speed=0.0,
+            v_wind_speed=0.0, w_wind_speed=0.0, stratification=lambda y: 1.0, tol=1e-10, max_iterations=1000)
+    return dict(Sol=Sol, mpv=mpv, elem=elem, node=node, ud=ud, th=NS(gamm=GAMM))
