@@ -125,8 +125,10 @@ __device__ __forceinline__ double dSdy3(const Proj3Dev &P, const double *S0n, in
 
 // wplus = Gammainv * rhoY * Y of the coefficient state on every cell, and the
 // cells around the inner nodes packed (inx+1)(iny+1)(inz+1) for the operator
-// (the same plane serves hplusx, hplusy, hplusz)
-__global__ void k3_coeff_cells(Proj3Dev P, const double *rhoC, const double *rhoYC, double *wplus0, double *hpk) {
+// (the same plane serves hplusx, hplusy, hplusz); rhoY^(2-gamma) per cell for
+// wcenter, so that each node sums eight values instead of taking eight pows
+__global__ void k3_coeff_cells(Proj3Dev P, const double *rhoC, const double *rhoYC, double *wplus0, double *hpk,
+                               double *pwc) {
     const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (e >= (long long)P.icx * P.icy * P.icz) return;
     const int i = (int)(e / ((long long)P.icy * P.icz));
@@ -136,6 +138,7 @@ __global__ void k3_coeff_cells(Proj3Dev P, const double *rhoC, const double *rho
     const double Y = rhoYC[e] / rhoC[e];
     const double w = Gammainv * rhoYC[e] * Y;
     wplus0[e] = w;
+    pwc[e] = pow(rhoYC[e], 2.0 - P.gamm);
     if (i >= 1 && i <= P.icx - 2 && j >= 1 && j <= P.icy - 2 && k >= 1 && k <= P.icz - 2)
         hpk[((long long)(i - 1) * (P.icy - 2) + (j - 1)) * (P.icz - 2) + (k - 1)] = w;
 }
@@ -144,7 +147,7 @@ __global__ void k3_coeff_cells(Proj3Dev P, const double *rhoC, const double *rho
 // times compressibility in the pseudo-incompressible regime; the 3D Jacobi
 // diagonal (laplacian.py:1334-1356: coefficient 0.0625, the x-y cross terms
 // kept as the reference has them); inner nodes packed -> hc, dinv
-__global__ void k3_coeff_nodes(Proj3Dev P, const double *rhoYC, const double *wplus0, double *dinv_isc, double *hc,
+__global__ void k3_coeff_nodes(Proj3Dev P, const double *pwc, const double *wplus0, double *dinv_isc, double *hc,
                                double *dinv) {
     const int nix = P.icx - 1, niy = P.icy - 1, niz = P.icz - 1;
     const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -152,13 +155,13 @@ __global__ void k3_coeff_nodes(Proj3Dev P, const double *rhoYC, const double *wp
     const int a = (int)(e / ((long long)niy * niz));
     const int r = (int)(e - (long long)a * niy * niz);
     const int b = r / niz, c = r - b * niz;
-    const double gm1inv = 1.0 / (P.gamm - 1.0), cexp = 2.0 - P.gamm;
+    const double gm1inv = 1.0 / (P.gamm - 1.0);
     const double ccenter = -P.Msq * gm1inv / (P.dt * P.dt);
     double s = 0.0, S = 0.0;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const long long cc = c3(P, a + (q >> 2), b + ((q >> 1) & 1), c + (q & 1));
-        s += pow(rhoYC[cc], cexp);
+        s += pwc[cc];
         S += wplus0[cc];
     }
     double wc = ccenter * s / 8.0;
@@ -200,20 +203,25 @@ __global__ void k3_zero_ghost(Proj3Dev P, double *rhou, double *rhov, double *rh
     }
 }
 
+// Y = rhoY / rho per cell for the divergence (eight cells share it per node)
+__global__ void k3_cell_y(Proj3Dev P, const double *rho, const double *rhoY, double *Yc) {
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e < (long long)P.icx * P.icy * P.icz) Yc[e] = rhoY[e] / rho[e];
+}
+
 // divergence_nodes, 3D branch (second_projection.py:556-570) on node.isc, with the
 // reference's sign on the x term (Ux = -0.5 * (...), :563) or the 2D branch's
 // (P.xsign); /dt (:139), the
 // regime mix (:149-150), b = (rhs * diag_inv)[inner] in C order (:170, :224)
-__global__ void k3_divergence(Proj3Dev P, const double *rho, const double *rhou, const double *rhov,
-                              const double *rhow, const double *rhoY, const double *dinv_isc, double *rhs_isc,
-                              double *bvec) {
+__global__ void k3_divergence(Proj3Dev P, const double *Yc, const double *rhou, const double *rhov,
+                              const double *rhow, const double *dinv_isc, double *rhs_isc, double *bvec) {
     const int nix = P.icx - 1, niy = P.icy - 1, niz = P.icz - 1;
     const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (e >= (long long)nix * niy * niz) return;
     const int a = (int)(e / ((long long)niy * niz));
     const int r = (int)(e - (long long)a * niy * niz);
     const int b = r / niz, c = r - b * niz;
-    auto Y = [&](int i, int j, int k) { const long long q = c3(P, i, j, k); return rhoY[q] / rho[q]; };
+    auto Y = [&](int i, int j, int k) { return Yc[c3(P, i, j, k)]; };
     auto qu = [&](int i, int j, int k) { return rhou[c3(P, i, j, k)] * Y(i, j, k); };
     auto qv = [&](int i, int j, int k) { return rhov[c3(P, i, j, k)] * Y(i, j, k); };
     auto qw = [&](int i, int j, int k) { return rhow[c3(P, i, j, k)] * Y(i, j, k); };
@@ -371,8 +379,9 @@ extern "C" int bella_projection3d(bella_ws *ws, const bella_proj3d *a, const bel
     const long long nisc = (long long)(P.icx - 1) * (P.icy - 1) * (P.icz - 1);
     const long long nin = (long long)a->inx * a->iny * a->inz;
     const long long npk = (long long)(a->inx + 1) * (a->iny + 1) * (a->inz + 1);
-    // scratch: wplus0, dinv_isc, rhs_isc, packed cells, hc, dinv, b, x, pfull
-    const size_t need = (size_t)(ncell + 2 * nisc + npk + 4 * nin + nnode);
+    // scratch: wplus0, dinv_isc, rhs_isc, packed cells, hc, dinv, b, x, pfull, a cell field
+    // (rhoY^(2-gamma) for the coefficients, then Y for the divergence)
+    const size_t need = (size_t)(2 * ncell + 2 * nisc + npk + 4 * nin + nnode);
     if (ws->proj_cap < need) {
         cudaFree(ws->proj_buf);
         ws->proj_buf = nullptr;
@@ -389,7 +398,8 @@ extern "C" int bella_projection3d(bella_ws *ws, const bella_proj3d *a, const bel
     double *dinv = q; q += nin;
     double *bvec = q; q += nin;
     double *xvec = q; q += nin;
-    double *pfull = q;
+    double *pfull = q; q += nnode;
+    double *cellf = q;
 
     const bool has0 = a->rho0 != nullptr;
     double *const F[6] = {a->rho, a->rhou, a->rhov, a->rhow, a->rhoY, a->rhoX};
@@ -404,13 +414,13 @@ extern "C" int bella_projection3d(bella_ws *ws, const bella_proj3d *a, const bel
                                               a->S0n, 0.0);
     bd3(P, F, a->hydro_rhoY0, a->strat_inv, s, L);
     // 3. coefficients from the coefficient state and the diagonal
-    k3_coeff_cells<<<grid3(ncell), 256, 0, s>>>(P, C[0], C[4], wplus0, hpk);
-    k3_coeff_nodes<<<grid3(nisc), 256, 0, s>>>(P, C[4], wplus0, dinv_isc, hc, dinv);
+    k3_coeff_cells<<<grid3(ncell), 256, 0, s>>>(P, C[0], C[4], wplus0, hpk, cellf);
+    k3_coeff_nodes<<<grid3(nisc), 256, 0, s>>>(P, cellf, wplus0, dinv_isc, hc, dinv);
     // 4. divergence right-hand side (:134-170, :224)
     k3_zero_ghost<<<grid3((long long)P.icx * P.icz), 256, 0, s>>>(P, a->rhou, a->rhov, a->rhow);
-    k3_divergence<<<grid3(nisc), 256, 0, s>>>(P, a->rho, a->rhou, a->rhov, a->rhow, a->rhoY, dinv_isc, rhs_isc,
-                                             bvec);
-    L += 5;
+    k3_cell_y<<<grid3(ncell), 256, 0, s>>>(P, a->rho, a->rhoY, cellf);
+    k3_divergence<<<grid3(nisc), 256, 0, s>>>(P, cellf, a->rhou, a->rhov, a->rhow, dinv_isc, rhs_isc, bvec);
+    L += 6;
     if (a->rhs_out) cudaMemcpyAsync(a->rhs_out, rhs_isc, nisc * sizeof(double), cudaMemcpyDeviceToDevice, s);
     ws->launches += L;
     if (cudaGetLastError() != cudaSuccess) return BELLA_ECUDA;
