@@ -310,6 +310,12 @@ int bella_euler_forward3d(const bella_expl3d *args, void *stream);
 /* euler_backward_non_advective_expl_part (second_projection.py:77-92) in 3D */
 int bella_expl_part3d(const bella_expl3d *args, void *stream);
 
+/* ---- CFL time step (cfl.py:5-74): the maxima over the device state ----------
+ * out[6] (host) = max |u|, |v|, |w|, |u|+c, |v|+c, |w|+c over all n cells, with
+ * c = sqrt(gamm rhoY^gamm / rho) / sqrt(Msq); synchronises the stream. */
+int bella_cfl_maxima(const double *rho, const double *rhou, const double *rhov, const double *rhow,
+                     const double *rhoY, long long n, double gamm, double Msq, double *out, void *stream);
+
 /* ---- ensemble: the solves of many 2D members in one persistent launch ----
  * Each member is the reference's call (second_projection.py:205-230) on its own
  * workspace (bella_op2d_set): FP64 BiCGStab, scipy 1.7 control flow, x0 = 0.

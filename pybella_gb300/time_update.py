@@ -21,9 +21,62 @@ from . import _lib
 from .second_projection import _is_wall
 
 _FIELDS = ("rho", "rhou", "rhov", "rhow", "rhoY", "rhoX")
+_EPS = np.finfo(float).eps
 
 
-class DeviceStep2D:
+def dynamic_timestep(maxima, time, time_output, dxyz, step, CFL=0.5, dtfixed0=100.0, dtfixed=100.0,
+                     acoustic_timestep=0):
+    """The time step of cfl.py:5-74 from the state's maxima (``bella_cfl_maxima``:
+    |u|, |v|, |w|, |u|+c, |v|+c, |w|+c); ``dxyz`` = (dx, dy, dz) with dz = 1 in 2D
+    (grid.py:110, 171).  Returns dt."""
+    u_max, v_max, w_max, upc_max, vpc_max, wpc_max = (max(m, _EPS) for m in maxima)
+    dx, dy, dz = dxyz
+    if acoustic_timestep == 1:
+        dt_cfl = min(min(CFL * dx / upc_max, CFL * dy / vpc_max), CFL * dz / wpc_max)
+        dt = min(dt_cfl, dtfixed0 + min(step, 1.) * (dtfixed - dtfixed0))
+        if dt > (time_output - time):
+            dt = (time_output - time) + _EPS
+        return dt
+    dt_cfl = min(min(CFL * dx / u_max, CFL * dy / v_max), CFL * dz / w_max)
+    dt = min(dt_cfl, dtfixed0 + min(step, 1.) * (dtfixed - dtfixed0))
+    dt *= min(float(step + 1), 1.0)
+    if dt > (time_output - time):
+        dt = (time_output - time)
+    return dt
+
+
+class _Loop:
+    """The loop of ``do`` (time_update.py:129-140, 686-706) over a device step."""
+
+    def cfl_maxima(self):
+        out = (ctypes.c_double * 6)()
+        f = self.f
+        with torch.cuda.device(self.dev):
+            _lib.check(self.lib.bella_cfl_maxima(*[ctypes.c_void_p(f[k].data_ptr()) for k in
+                                                   ("rho", "rhou", "rhov", "rhow", "rhoY")],
+                                                 f["rho"].numel(), self.gamm, self.Msq, out, self._stream()),
+                       "bella_cfl_maxima")
+        return list(out)
+
+    def run(self, t, tout, nsteps, t_ref=None, CFL=0.5, dtfixed0=100.0, dtfixed=100.0, acoustic_timestep=0,
+            precision="fp64"):
+        """Steps until ``tout`` or ``nsteps`` steps, dt from the CFL condition of the
+        state at each step's start ('CFLfixed': 21.69 / ``t_ref`` for the first two
+        steps when ``t_ref`` is given).  Returns ``(t, dts)``."""
+        step, dts = 0, []
+        while t < tout and step < nsteps:
+            dt = dynamic_timestep(self.cfl_maxima(), t, tout, self.dxyz, step, CFL, dtfixed0, dtfixed,
+                                  acoustic_timestep)
+            if t_ref is not None and step < 2:
+                dt = 21.69 / t_ref
+            self.step(step, dt, precision)
+            dts.append(dt)
+            t += dt
+            step += 1
+        return t, dts
+
+
+class DeviceStep2D(_Loop):
     """The state of a 2D run on one GPU and its time step.
 
     Built from the reference's objects (``Sol``, ``mpv``, ``elem``, ``node``,
@@ -100,6 +153,7 @@ class DeviceStep2D:
         self.lib.bella_solve_opts_default(ctypes.byref(self.opts))
         self.opts.tol, self.opts.maxiter = float(ud.tol), int(ud.max_iterations)
         self.stats = []
+        self.gamm, self.Msq, self.dxyz = gamm, float(ud.Msq), (float(node.dx), float(node.dy), 1.0)
 
     def _stream(self):
         return ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
@@ -147,7 +201,7 @@ class DeviceStep2D:
         mpv.p2_nodes[...] = self.p2.cpu().numpy()
 
 
-class DeviceStep3D:
+class DeviceStep3D(_Loop):
     """The 3D time step with the state resident on the GPU (the reference's
     ``time_update.do`` in 3D, which the reference itself cannot run: its 3D
     projection step and forward explicit part break on unassigned names and
@@ -234,6 +288,7 @@ class DeviceStep3D:
         self.lib.bella_solve_opts_default(ctypes.byref(self.opts))
         self.opts.tol, self.opts.maxiter = float(ud.tol), int(ud.max_iterations)
         self.stats = []
+        self.gamm, self.Msq, self.dxyz = gamm, float(ud.Msq), (dx, dy, dz)
 
     def _stream(self):
         return ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)

@@ -57,3 +57,33 @@ def test_device_time_step_matches_reference():
             assert my_err <= max(1e-8, 3.0 * ref_err), (step, name, my_err, ref_err)
         for k in ("rho", "rhoY"):
             assert _rel(getattr(Sol, k), d[tag + k]) < 1e-10, (step, k)
+
+
+def test_device_run_to_tout_matches_reference():
+    """DeviceStep2D.run: dt from the CFL maxima of the device state
+    (bella_cfl_maxima) and the loop of time_update.do, to tout = 0.1 (two fixed
+    steps, a third cut to tout), against the reference's run (step_kat.npz)."""
+    from oracle import cases
+    from pybella_gb300.time_update import DeviceStep2D
+    d = np.load(golden("step_kat.npz"))
+    grid, prm, _, _, hn, hc, sf = cases.rising_bubble(inx=64, iny=32)
+    hn, hc = dict(hn, S0=d["S0n"]), dict(hc, rhoY0=d["rhoY0"])
+    S0c = d["S0c"]
+    Sol = NS(**{k: d["in_" + k].copy() for k in FIELDS})
+    mpv = NS(p2_nodes=d["p2_in"].copy(), HydroState=NS(rhoY0=hc["rhoY0"], get_S0c=lambda elem: S0c),
+             HydroState_n=NS(S0=hn["S0"]))
+    ud = NS(bdry_type=["wrap", "symmetric", "symmetric"], gravity_strength=[0.0, prm.g, 0.0], Msq=prm.Msq,
+            nonhydrostasy=1.0, compressibility=0.0, is_compressible=0, coriolis_strength=np.zeros(3),
+            u_wind_speed=0.0, v_wind_speed=0.0, w_wind_speed=0.0, stratification=sf, tol=1e-10,
+            max_iterations=6000)
+    run = DeviceStep2D(Sol, mpv, NS(ndim=2, y=grid.elem_y), NS(iicx=grid.inx, iicy=grid.iny, dx=grid.dx, dy=grid.dy),
+                       ud, NS(gamm=prm.gamm))
+    t, dts = run.run(0.0, float(d["meta"][7]), 4, t_ref=float(d["meta"][6]))
+    run.download(Sol, mpv)
+    assert len(dts) == 3 and abs(t - float(d["meta"][7])) < 1e-12
+    for st in run.stats:
+        assert st["status"] == 0 and st["relres"] <= 1e-10, st
+    for k in ("rho", "rhoY"):
+        assert _rel(getattr(Sol, k), d["s4_" + k]) < 1e-10, k
+    for k in ("rhou", "rhov", "rhoX"):
+        assert _rel(getattr(Sol, k), d["s4_" + k]) < 1e-6, (k, _rel(getattr(Sol, k), d["s4_" + k]))

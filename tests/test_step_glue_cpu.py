@@ -180,6 +180,15 @@ class _Stand:
         from oracle import nodal2d as n2
         return self._project(p, st, n2.impl_part, {})
 
+    def bella_cfl_maxima(self, rho, rhou, rhov, rhow, rhoY, n, gamm, Msq, out, s):
+        a = {k: _arr(v, (n,)) for k, v in (("rho", rho), ("rhou", rhou), ("rhov", rhov), ("rhow", rhow),
+                                            ("rhoY", rhoY))}
+        c = np.sqrt(gamm * a["rhoY"] ** gamm / a["rho"]) * (1.0 / np.sqrt(Msq))
+        u, v, w = (np.abs(a[k] / a["rho"]) for k in ("rhou", "rhov", "rhow"))
+        for k, m in enumerate((u.max(), v.max(), w.max(), (u + c).max(), (v + c).max(), (w + c).max())):
+            out[k] = m
+        return 0
+
     # 3D
     def bella_boundary3d(self, p, s):
         from oracle import proj3d as o3
@@ -290,3 +299,50 @@ def test_device_step3d_orchestration_vs_oracle(host_torch, monkeypatch, tmp_path
         Sc = step3d.time_step(Sc, pc, flux, step, 0.02169, grid, prm, hn, hc, S0c, sf, solver=solver)
         for k in FIELDS:
             assert _rel(getattr(S, k), Sc[k]) < 1e-10, (step, k)
+
+
+def test_device_step2d_run_to_tout_vs_reference(host_torch, monkeypatch, tmp_path):
+    """DeviceStep2D.run: the CFL time step from the device state's maxima and the
+    loop of time_update.do, to tout = 0.1 (two fixed steps, a third cut to tout),
+    against the reference's run (step_kat.npz)."""
+    from oracle import cases
+    from pybella_gb300.time_update import DeviceStep2D
+    d = np.load(golden("step_kat.npz"))
+    grid, prm, _, _, hn, hc, sf = cases.rising_bubble(inx=64, iny=32)
+    hn, hc = dict(hn, S0=d["S0n"]), dict(hc, rhoY0=d["rhoY0"])
+    _install(monkeypatch, tmp_path, NS(grid=grid, prm=prm, hn=hn, hc=hc, sf=sf))
+    S0c = d["S0c"]
+    Sol = NS(**{k: d["in_" + k].copy() for k in FIELDS})
+    mpv = NS(p2_nodes=d["p2_in"].copy(), HydroState=NS(rhoY0=hc["rhoY0"], get_S0c=lambda elem: S0c),
+             HydroState_n=NS(S0=hn["S0"]))
+    ud = NS(bdry_type=["wrap", "symmetric", "symmetric"], gravity_strength=[0.0, prm.g, 0.0], Msq=prm.Msq,
+            nonhydrostasy=1.0, compressibility=0.0, is_compressible=0, coriolis_strength=np.zeros(3),
+            u_wind_speed=0.0, v_wind_speed=0.0, w_wind_speed=0.0, stratification=sf, tol=1e-10,
+            max_iterations=6000)
+    run = DeviceStep2D(Sol, mpv, NS(ndim=2, y=grid.elem_y), NS(iicx=grid.inx, iicy=grid.iny, dx=grid.dx, dy=grid.dy),
+                       ud, NS(gamm=prm.gamm))
+    t, dts = run.run(0.0, float(d["meta"][7]), 4, t_ref=float(d["meta"][6]))
+    run.download(Sol, mpv)
+    assert len(dts) == 3 and t == pytest.approx(float(d["meta"][7]), rel=1e-15)
+    for k in FIELDS:
+        assert _rel(getattr(Sol, k), d["s4_" + k]) < 1e-10, k
+    assert _rel(mpv.p2_nodes, d["s4_p2"]) < 1e-10
+
+
+def test_dynamic_timestep_matches_oracle():
+    """The host arithmetic of the CFL time step (pybella_gb300.time_update) from the
+    state's maxima equals the oracle's cfl.py restatement, both branches."""
+    from oracle import cases, step2d
+    from pybella_gb300.time_update import dynamic_timestep
+    grid, prm, Sol, p2, hn, hc, sf = cases.rising_bubble(inx=64, iny=32)
+    rng = np.random.default_rng(2)
+    Sol = dict(Sol, rhou=0.3 * Sol["rho"] * rng.standard_normal(Sol["rho"].shape),
+               rhov=0.2 * Sol["rho"] * rng.standard_normal(Sol["rho"].shape))
+    c = np.sqrt(prm.gamm * Sol["rhoY"] ** prm.gamm / Sol["rho"]) * (1.0 / np.sqrt(prm.Msq))
+    u, v, w = (np.abs(Sol[k] / Sol["rho"]) for k in ("rhou", "rhov", "rhow"))
+    maxima = [u.max(), v.max(), w.max(), (u + c).max(), (v + c).max(), (w + c).max()]
+    for step, t, tout in ((0, 0.0, 1.0), (3, 0.0, 1.0), (3, 0.99, 1.0)):
+        ref, _, _ = step2d.dynamic_timestep(Sol, t, tout, grid, prm, step, dtfixed=0.01)
+        assert dynamic_timestep(maxima, t, tout, (grid.dx, grid.dy, 1.0), step, dtfixed=0.01) == ref
+        ref_ac = step2d.dynamic_timestep(Sol, t, tout, grid, prm, step, acoustic_timestep=1)
+        assert dynamic_timestep(maxima, t, tout, (grid.dx, grid.dy, 1.0), step, acoustic_timestep=1) == ref_ac
