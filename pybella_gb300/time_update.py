@@ -1,7 +1,7 @@
-"""Device-resident 2D time step: the reference's ``time_update.do``
+"""Device-resident time steps, 2D and 3D: the reference's ``time_update.do``
 (time_update.py:129-489) for the pseudo-incompressible case without blending,
 data assimilation or Rayleigh damping, with every array on the GPU between
-steps.
+steps, and its loop with the CFL time step (cfl.py:5-74).
 
 One step, as the reference orders it: boundary data; ``Sol0`` = the state;
 face mass fluxes and first-order advection over dt/2 (``bella_advective_fluxes2d``,
@@ -48,6 +48,11 @@ def dynamic_timestep(maxima, time, time_output, dxyz, step, CFL=0.5, dtfixed0=10
 class _Loop:
     """The loop of ``do`` (time_update.py:129-140, 686-706) over a device step."""
 
+    def boundary(self):
+        fn = self.lib.bella_boundary3d if isinstance(self.adv, _lib.Adv3D) else self.lib.bella_boundary2d
+        with torch.cuda.device(self.dev):
+            _lib.check(fn(ctypes.byref(self.adv), self._stream()), "set_explicit_boundary_data")
+
     def cfl_maxima(self):
         out = (ctypes.c_double * 6)()
         f = self.f
@@ -65,6 +70,7 @@ class _Loop:
         steps when ``t_ref`` is given).  Returns ``(t, dts)``."""
         step, dts = 0, []
         while t < tout and step < nsteps:
+            self.boundary()                                 # :130, before the time step of :135
             dt = dynamic_timestep(self.cfl_maxima(), t, tout, self.dxyz, step, CFL, dtfixed0, dtfixed,
                                   acoustic_timestep)
             if t_ref is not None and step < 2:
