@@ -60,7 +60,8 @@ def _args():
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--workload", default="learned3d", choices=["solve2d", "ensemble", "learned3d", "step3d"])
+    ap.add_argument("--workload", default="learned3d",
+                    choices=["solve2d", "ensemble", "learned3d", "step3d", "step2d"])
     ap.add_argument("--nz", type=int, default=257)
     ap.add_argument("--train-steps", type=int, default=1000)
     ap.add_argument("--skip", type=float, default=0.9)
@@ -789,6 +790,71 @@ def run_reference_3d(args):
     print(json.dumps(line), flush=True)
 
 
+def _cpu_step2d_sample(seconds):
+    """Steps/s of the oracle's 2D time step (NumPy restatement of time_update.do,
+    pinned to the reference) on the 160x80-cell rising bubble, one host thread."""
+    from oracle import advection2d as adv, cases, step2d
+    grid, prm, Sol, p2, hn, hc, sf = cases.rising_bubble()
+    S0c = np.broadcast_to(hc["S0"][None, :], grid.elem_sc).copy()
+    flux = adv.new_flux(grid)
+    t0, k = time.perf_counter(), 0
+    while k < 1 or time.perf_counter() - t0 < seconds:
+        Sol = step2d.time_step(Sol, p2, flux, k, 0.02169, grid, prm, hn, hc, S0c, sf)
+        k += 1
+    return k / (time.perf_counter() - t0), k
+
+
+def run_step2d(args):
+    """``--workload step2d``: whole 2D time steps of the rising bubble (160x80
+    cells, tol 1e-10, fixed dt = 21.69 s as the reference's 'CFLfixed' first steps)
+    with the state resident on the GPU (DeviceStep2D: advection, explicit and
+    implicit projection halves, double-float solves); value = steps/s.  The CPU
+    baseline is the oracle's step (the reference's algorithm restated in NumPy)."""
+    import torch
+    from pybella_gb300 import workloads
+    from pybella_gb300.time_update import DeviceStep2D
+    world, rank, local = _dist()
+    torch.cuda.set_device(local)
+    st = workloads.bubble_2d_state()
+    run = DeviceStep2D(st["Sol"], st["mpv"], st["elem"], st["node"], st["ud"], st["th"], device=local)
+    dt = 21.69 / st["ud"].t_ref
+    for k in range(args.warmup):
+        run.step(k, dt, precision=args.precision)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for k in range(args.steps):
+        run.step(args.warmup + k, dt, precision=args.precision)
+    e1.record()
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    if rank == 0:
+        cpu = None
+        if world == 1 and not args.no_cpu_baseline:
+            v, k = _cpu_step2d_sample(args.cpu_seconds)
+            cpu = {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
+                   "sample": "%d steps of the oracle's time step on the same state" % k}
+        its = [s_["iterations"] for s_ in run.stats[-2 * args.steps:]]
+        print(json.dumps({"metric": "2D time steps/s (rising bubble 160x80, projections to 1e-10)",
+                          "value": world * 1000.0 / ms, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+                          "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f64 state, %s solves" % args.precision, "data": "synthetic",
+                          "config": {"workload": "2D time step, rising bubble 160x80 cells", "parallelism":
+                                     "replicas" if world > 1 else "single GPU",
+                                     "l2": "state of 1 MB, L2-resident (a launch-bound workload)"},
+                          "solve_iterations": its, "clocks": clocks, "cpu_baseline": cpu,
+                          "gpu_launches": None}), flush=True)
+
+
 def run_step3d(args):
     """``--workload step3d``: whole 3D time steps of the warm bubble (advection,
     explicit and implicit projection halves, background-preconditioned solves to
@@ -844,6 +910,18 @@ def main():
     if args.workload in ("learned3d", "step3d") and args.nx == NX and args.ny == NY:
         args.nx, args.ny = 257, 129
     if args.impl == "reference":
+        if args.workload == "step2d":
+            if _dist()[1] == 0:
+                v, k = _cpu_step2d_sample(args.cpu_seconds)
+                print(json.dumps({"impl": "reference", "metric": "2D time steps/s (rising bubble 160x80, "
+                                  "projections to 1e-10)", "value": v, "unit": "steps/s", "n_gpus": 1,
+                                  "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                                  "config": {"workload": "2D time step, rising bubble 160x80 cells"},
+                                  "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
+                                                   "sample": "%d steps of the oracle's time step" % k},
+                                  "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0,
+                                          "d2h_bytes_per_step": 0}}))
+            return
         if args.workload == "step3d":
             if _dist()[1] == 0:
                 print(json.dumps({"impl": "reference", "unavailable": "the reference's 3D time step cannot run "
@@ -859,6 +937,8 @@ def main():
         run_learned3d(args)
     elif args.workload == "step3d":
         run_step3d(args)
+    elif args.workload == "step2d":
+        run_step2d(args)
     else:
         run_gpu(args)
 

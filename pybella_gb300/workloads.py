@@ -316,3 +316,49 @@ def bubble_3d_state(nx, ny, nz, seed=0, delth=2.0, y0=0.2, r0=0.2, grav=10.0, t_
             compressibility=0.0, is_compressible=0, coriolis_strength=np.zeros(3), u_wind_speed=0.0,
             v_wind_speed=0.0, w_wind_speed=0.0, stratification=lambda y: 1.0, tol=1e-10, max_iterations=1000)
     return dict(Sol=Sol, mpv=mpv, elem=elem, node=node, ud=ud, th=NS(gamm=GAMM))
+
+
+def bubble_2d_state(inx=161, iny=81, delth=2.0, y0=0.2, r0=0.2, grav=10.0, t_ref=1000.0):
+    """The rising bubble's initial state (inputs/rising_bubble.py:42-98) in the
+    reference's objects (host NumPy arrays): inx x iny nodes on x in [-1, 1]
+    (periodic), y in [0, 1] (walls), isentropic hydrostatic background
+    (hydrostatics.py:79-117), the warm bubble at (0, y0), fluid at rest, the
+    reference's boundary data applied by the first step.  Returns a dict with
+    ``Sol``, ``mpv``, ``elem``, ``node``, ``ud``, ``th`` for
+    :class:`pybella_gb300.time_update.DeviceStep2D`."""
+    from types import SimpleNamespace as NS
+    ig = 2
+    u_ref = H_REF / t_ref
+    Msq = u_ref * u_ref / (R_GAS * T_REF)
+    g = grav * H_REF / (R_GAS * T_REF)
+    Gamma, gm1inv = (GAMM - 1.0) / GAMM, 1.0 / (GAMM - 1.0)
+    dx, dy = 2.0 / (inx - 1.0), 1.0 / (iny - 1.0)
+    sc = (inx - 1 + 2 * ig, iny - 1 + 2 * ig)
+    ex = -1.0 - ig * dx + 0.5 * dx + dx * np.arange(sc[0])
+    ey = 0.0 - ig * dy + 0.5 * dy + dy * np.arange(sc[1])
+    ny_ = 0.0 - ig * dy + dy * np.arange(iny + 2 * ig)
+    Hex = 1.0 / (Gamma * g)
+
+    def column(y):
+        pi_p, pi_m, pi = np.exp(-(y + 0.5 * dy) / Hex), np.exp(-(y - 0.5 * dy) / Hex), np.exp(-y / Hex)
+        return pi ** gm1inv, -Gamma * g * dy / (pi_p - pi_m)
+    rhoY0_c, Y0_c = column(ey)
+    _, Y0_n = column(ny_)
+    X, Yg = np.meshgrid(ex, ey, indexing="ij")
+    r = np.sqrt(X ** 2 + (Yg - y0) ** 2) / r0
+    pert = (delth / 300.0) * np.cos(0.5 * np.pi * r) ** 2
+    pert[r > 1.0] = 0.0
+    rhoY = np.broadcast_to(rhoY0_c[None, :], sc).copy()
+    rho = rhoY / (1.0 + pert)
+    z = np.zeros(sc)
+    Sol = NS(rho=rho, rhou=z.copy(), rhov=z.copy(), rhow=z.copy(), rhoY=rhoY, rhoX=z.copy())
+    S0c = np.broadcast_to((1.0 / Y0_c)[None, :], sc).copy()
+    mpv = NS(p2_nodes=np.zeros((inx + 2 * ig, iny + 2 * ig)),
+             HydroState=NS(rhoY0=rhoY0_c, get_S0c=lambda elem: S0c), HydroState_n=NS(S0=1.0 / Y0_n))
+    elem = NS(ndim=2, y=ey)
+    node = NS(iicx=inx, iicy=iny, dx=dx, dy=dy)
+    ud = NS(bdry_type=["wrap", "symmetric", "symmetric"], gravity_strength=[0.0, g, 0.0], Msq=Msq,
+            nonhydrostasy=1.0, compressibility=0.0, is_compressible=0, coriolis_strength=np.zeros(3),
+            u_wind_speed=0.0, v_wind_speed=0.0, w_wind_speed=0.0, stratification=lambda y: 1.0, tol=1e-10,
+            max_iterations=6000, t_ref=t_ref)
+    return dict(Sol=Sol, mpv=mpv, elem=elem, node=node, ud=ud, th=NS(gamm=GAMM))

@@ -36,3 +36,19 @@ def test_step3d_workload_inputs_and_reference_arm(monkeypatch, capsys):
     bench.main()
     line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     assert line["impl"] == "reference" and "cannot run" in line["unavailable"]
+
+
+def test_step2d_workload_inputs_and_cpu_sample(monkeypatch):
+    """The step2d workload's state (generated by the library) equals the oracle's
+    rising bubble; its CPU sample runs the oracle's step."""
+    import numpy as np
+    import bench
+    from oracle import cases
+    from pybella_gb300 import workloads
+    st = workloads.bubble_2d_state()
+    grid, prm, Sol, p2, hn, hc, sf = cases.rising_bubble()
+    inner = (slice(2, -2), slice(2, -2))
+    np.testing.assert_array_equal(st["Sol"].rho[inner], Sol["rho"][inner])
+    np.testing.assert_array_equal(st["mpv"].HydroState_n.S0, hn["S0"])
+    v, k = bench._cpu_step2d_sample(0.0)
+    assert k == 1 and v > 0
