@@ -12,6 +12,17 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built libbella_gb300.so")
 
 
+# Tests of the advection and of whole time steps build on the projection and solver
+# entry points the other files test: they run after those (in this order), so that a
+# failure in a building block is reported by that block's own test first.
+_COMPOSED = ("test_gpu_advection.py", "test_gpu_projection_walls.py", "test_gpu_step.py", "test_gpu_step3d.py")
+
+
+def pytest_collection_modifyitems(config, items):
+    rank = {name: k + 1 for k, name in enumerate(_COMPOSED)}
+    items.sort(key=lambda it: rank.get(os.path.basename(str(it.fspath)), 0))
+
+
 def golden(name):
     return os.path.join(ROOT, "tests", "golden", name)
 
