@@ -312,9 +312,13 @@ int bella_expl_part3d(const bella_expl3d *args, void *stream);
 
 /* ---- CFL time step (cfl.py:5-74): the maxima over the device state ----------
  * out[6] (host) = max |u|, |v|, |w|, |u|+c, |v|+c, |w|+c over all n cells, with
- * c = sqrt(gamm rhoY^gamm / rho) / sqrt(Msq); synchronises the stream. */
+ * c = sqrt(gamm rhoY^gamm / rho) / sqrt(Msq), as numpy's .max() over the whole
+ * arrays in cfl.py:25-45: a NaN in any cell makes that maximum NaN.  scratch: 48
+ * bytes (6 x 8) of device memory owned by the caller, reused across calls (the
+ * entry point allocates nothing).  Synchronises the stream. */
 int bella_cfl_maxima(const double *rho, const double *rhou, const double *rhov, const double *rhow,
-                     const double *rhoY, long long n, double gamm, double Msq, double *out, void *stream);
+                     const double *rhoY, long long n, double gamm, double Msq, void *scratch, double *out,
+                     void *stream);
 
 /* ---- ensemble: the solves of many 2D members in one persistent launch ----
  * Each member is the reference's call (second_projection.py:205-230) on its own

@@ -72,12 +72,16 @@ def dynamic_timestep(Sol, time, time_output, grid, prm, step, CFL=0.5, dtfixed0=
     return dt, cfl, cfl_ac
 
 
-def run(Sol, p2, t, tout, nsteps, grid, prm, hydro_n, hydro_c, S0c, strat_fn, t_ref, cfl_fixed=True):
-    """The loop of ``do`` (time_update.py:129-140, 486-489): the CFL time step
-    ('CFLfixed': 21.69 / t_ref for the first two steps), then :func:`time_step`,
-    until ``tout`` or ``nsteps`` steps.  Returns ``(Sol, t, dts)``."""
-    flux = adv.new_flux(grid)
-    step, dts = 0, []
+def run(Sol, p2, t, tout, nsteps, grid, prm, hydro_n, hydro_c, S0c, strat_fn, t_ref, cfl_fixed=True, step=0,
+        flux=None):
+    """The loop of ``do`` (time_update.py:129-140, 686-708): the CFL time step
+    ('CFLfixed': 21.69 / t_ref while the global step index is below 2), then
+    :func:`time_step`, until ``tout`` or until the global step index reaches
+    ``nsteps`` (the reference's ``stepmax``).  ``step`` is the global index the
+    run starts from (``do`` receives it in ``steps`` and returns it), so calls for
+    consecutive output times continue one run.  Returns ``(Sol, t, dts, step)``."""
+    flux = adv.new_flux(grid) if flux is None else flux
+    dts = []
     while t < tout and step < nsteps:
         n2.set_explicit_boundary_data(Sol, grid, prm, hydro_c, strat_fn)
         dt, _, _ = dynamic_timestep(Sol, t, tout, grid, prm, step)
@@ -87,4 +91,22 @@ def run(Sol, p2, t, tout, nsteps, grid, prm, hydro_n, hydro_c, S0c, strat_fn, t_
         dts.append(dt)
         t += dt
         step += 1
-    return Sol, t, dts
+    return Sol, t, dts, step
+
+
+def run_outputs(Sol, p2, touts, stepmax, grid, prm, hydro_n, hydro_c, S0c, strat_fn, t_ref, t=0.0,
+                on_output=None):
+    """The output loop of the reference's driver for one member (__main__.py:198-393):
+    one :func:`run` per output time, the step index carried across them, and
+    ``t`` set to the output time rounded to three decimals after each
+    (__main__.py:266, 388).  ``on_output(tout, Sol, p2, step)`` is called at
+    every output time.  Returns ``(Sol, t, step)``."""
+    flux = adv.new_flux(grid)
+    step = 0
+    for tout in touts:
+        Sol, t, _, step = run(Sol, p2, t, tout, stepmax, grid, prm, hydro_n, hydro_c, S0c, strat_fn, t_ref,
+                              step=step, flux=flux)
+        t = float(np.around(tout, 3))
+        if on_output is not None:
+            on_output(t, Sol, p2, step)
+    return Sol, t, step

@@ -164,7 +164,8 @@ SIGNATURES = {
     "bella_boundary3d": (ctypes.c_int, [ctypes.POINTER(Adv3D), ctypes.c_void_p]),
     "bella_euler_forward3d": (ctypes.c_int, [ctypes.POINTER(Expl3D), ctypes.c_void_p]),
     "bella_cfl_maxima": (ctypes.c_int, [ctypes.c_void_p] * 5 + [ctypes.c_longlong, ctypes.c_double, ctypes.c_double,
-                                                                  ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
+                                                                  ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                                                  ctypes.c_void_p]),
     "bella_expl_part3d": (ctypes.c_int, [ctypes.POINTER(Expl3D), ctypes.c_void_p]),
     "bella_cnn_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int,
                                         ctypes.c_longlong]),

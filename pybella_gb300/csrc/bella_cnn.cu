@@ -954,7 +954,7 @@ static bool big_smem(K kernel, size_t bytes) {
 static int conv_grid(const BlockMap &m) {
     const long long tiles = (long long)m.B * ((m.cx + CT_X - 1) / CT_X) * ((m.cy + CT_Y - 1) / CT_Y) *
                             ((m.cz + CT_Z - 1) / CT_Z);
-    const long long cap = (long long)NSM * 2;
+    const long long cap = (long long)num_sms() * 2;
     return (int)(tiles < cap ? tiles : cap);
 }
 
@@ -965,7 +965,7 @@ static bool map_ok(const bella_cnn *net, const BlockMap &m) {
 }
 
 static int tc_grid(long long nitems) {
-    int nsm = NSM;
+    int nsm = num_sms();
     return (int)(nitems < nsm ? nitems : nsm);
 }
 
@@ -981,7 +981,7 @@ static void forward_layers(bella_cnn *net, const BlockMap &m, float out_scale, c
         // runs of consecutive x-planes: about one run per SM
         const long long plane = (long long)(ny + 2) * (nz + 2);
         const int nblk = (int)((plane + TC_ROWS - 1) / TC_ROWS);
-        int nseg = (int)((NSM + nblk / 2) / nblk);
+        int nseg = (int)((num_sms() + nblk / 2) / nblk);
         if (nseg < 1) nseg = 1;
         if (nseg > nx) nseg = nx;
         const int runlen = (nx + nseg - 1) / nseg;
@@ -1032,7 +1032,7 @@ static void backward_layers(bella_cnn *net, const BlockMap &m, cudaStream_t s) {
     const int g = conv_grid(m);
     const int nx = m.B * m.cx, ny = m.cy, nz = m.cz, xs = m.cx;
     const long long n = m.nvox();
-    const int gw = g < NSM ? g : NSM;
+    const int gw = g < num_sms() ? g : num_sms();
     cudaMemsetAsync(net->grads, 0, net->nparams * sizeof(float), s);
     float *dW[6], *db[6];
     for (int l = 0; l < 6; ++l) {

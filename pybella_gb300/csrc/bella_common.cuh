@@ -30,10 +30,11 @@ constexpr int GRID_PER_SM = BELLA_GRID_PER_SM;
 constexpr int BX = 64;          // threads in x
 constexpr int BY = 4;           // threads in y  -> 256 threads, 4 rows each
 constexpr int NTHREADS = BX * BY;
-constexpr int NSM = 152;        // GB300 SMs (grid sizes are multiples of this)
+constexpr int MAX_SMS = 256;    // bound on the SM count: reduction partials are sized for MAX_SMS * 8 CTAs
+int num_sms();                  // SM count of the current device (152 on GB300), queried once per device
 constexpr int VEC_BLOCK = 256;  // block size of the streaming vector kernels
 constexpr int NQ = 8;           // reduction quantities per kernel (max)
-constexpr int MAXGRID = NSM * 8;  // largest grid of any reduction kernel (partials capacity)
+constexpr int MAXGRID = MAX_SMS * 8;  // largest grid of any reduction kernel (partials capacity)
 constexpr int MAXNULL = 8;      // null-space modes handled by the projection
 
 // --------------------------------------------------------------------------

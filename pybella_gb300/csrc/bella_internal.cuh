@@ -104,6 +104,10 @@ void prof_begin(bella_ws *ws, int kind, cudaStream_t s);
 void prof_end(bella_ws *ws, int kind, cudaStream_t s);
 void prof_harvest(bella_ws *ws);
 
+// ---- error reporting (host): the message bella_last_error() returns -------------
+int set_err(int code, const char *what);
+int cuda_check(cudaError_t e, const char *where);   // BELLA_OK or BELLA_ECUDA with the CUDA message
+
 // ---- launchers (host) --------------------------------------------------------
 int  stencil_grid(int nx, int ny);
 int  vec_grid(long long n);

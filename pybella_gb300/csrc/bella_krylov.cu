@@ -5,6 +5,7 @@
 //   p2, _ = scipy.sparse.linalg.bicgstab(lap, rhs_inner, tol=ud.tol,
 //                                        maxiter=ud.max_iterations, callback=counter)
 // (second_projection.py:230), with scipy 1.7 legacy `tol` semantics.
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -18,12 +19,12 @@ namespace bella {
 
 static thread_local std::string g_err;
 
-static int set_err(int code, const char *what) {
+int set_err(int code, const char *what) {
     g_err = what;
     return code;
 }
 
-static int cuda_check(cudaError_t e, const char *where) {
+int cuda_check(cudaError_t e, const char *where) {
     if (e == cudaSuccess) return BELLA_OK;
     g_err = std::string(where) + ": " + cudaGetErrorString(e);
     return BELLA_ECUDA;
@@ -35,9 +36,22 @@ static int cuda_check(cudaError_t e, const char *where) {
         if (_rc != BELLA_OK) return _rc;                             \
     } while (0)
 
+int num_sms() {
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) dev = 0;
+    std::atomic<int> *c = dev < 64 ? &cache[dev] : nullptr;
+    int n = c ? c->load(std::memory_order_relaxed) : 0;
+    if (n > 0) return n;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) n = 1;
+    if (n > MAX_SMS) n = MAX_SMS;
+    if (c) c->store(n, std::memory_order_relaxed);
+    return n;
+}
+
 int vec_grid(long long n) {
     long long g = (n + VEC_BLOCK - 1) / VEC_BLOCK;
-    const long long cap = (long long)NSM * 8;
+    const long long cap = (long long)num_sms() * 8;
     if (g > cap) g = cap;
     if (g < 1) g = 1;
     return (int)g;
@@ -385,7 +399,7 @@ int bella_ws_create(bella_ws **out, int device) {
     if (rc == BELLA_OK) rc = cuda_check(cudaMalloc(&ws->counter, 64), "cudaMalloc(counter)");
     if (rc == BELLA_OK) rc = cuda_check(cudaMemset(ws->counter, 0, 64), "cudaMemset(counter)");
     if (rc == BELLA_OK)
-        rc = cuda_check(cudaMalloc(&ws->partials, sizeof(double) * NQ * NSM * 8), "cudaMalloc(partials)");
+        rc = cuda_check(cudaMalloc(&ws->partials, sizeof(double) * NQ * MAXGRID), "cudaMalloc(partials)");
     if (rc == BELLA_OK) rc = cuda_check(cudaMemset(ws->ks, 0, sizeof(KState)), "cudaMemset(ks)");
     if (rc != BELLA_OK) {
         bella_ws_destroy(ws);
@@ -1175,7 +1189,8 @@ static int run_flex(bella_ws *ws, const Precond &pc, const bella_solve_opts *o, 
 constexpr int FG_MAXM = 64;
 constexpr int FG_MAXV = FG_MAXM + 1;
 
-constexpr int FG_XBLK = NSM * 8;    // blocks per group of inner products (enough warps to cover memory latency)
+// blocks per group of inner products: 8 per SM (enough warps to cover memory latency)
+static int fg_xblk() { return num_sms() * 8; }
 constexpr int FG_GROUP = 8;         // inner products per block
 
 // block (bx, gy): partial sums of <V_i, w> for the FG_GROUP vectors i of group gy
@@ -1283,7 +1298,7 @@ static int fg_ensure(bella_ws *ws, int m) {
     ws->fg_m = 0;
     BELLA_CUDA(cudaMalloc(&ws->fg_v, (size_t)(m + 1) * n * sizeof(float)));
     BELLA_CUDA(cudaMalloc(&ws->fg_z, (size_t)m * n * sizeof(float)));
-    BELLA_CUDA(cudaMalloc(&ws->fg_part, (size_t)(FG_XBLK > NSM * 8 ? FG_XBLK : NSM * 8) * (FG_MAXV + 1) *
+    BELLA_CUDA(cudaMalloc(&ws->fg_part, (size_t)MAXGRID * (FG_MAXV + 1) *
                                         sizeof(double)));
     BELLA_CUDA(cudaMalloc(&ws->fg_dev, 4 * (FG_MAXV + 1) * sizeof(double)));
     const double one = 1.0;
@@ -1312,6 +1327,7 @@ static int fgmres_cycle(bella_ws *ws, const Precond &pc, int m, double rel, cuda
     if (!isfinite(beta)) { *status = BELLA_NONFINITE; return BELLA_OK; }
     if (!(beta > 0.0)) { *status = BELLA_OK; return BELLA_OK; }
     k_fg_scale<<<gv, VEC_BLOCK, 0, s>>>(n, ws->r32, &ws->ks->rr, V);
+    const int xb = fg_xblk();
     double H[FG_MAXV][FG_MAXM], cs[FG_MAXM], sn[FG_MAXM], gvec[FG_MAXV];
     memset(H, 0, sizeof(H));
     gvec[0] = beta;
@@ -1324,11 +1340,11 @@ static int fgmres_cycle(bella_ws *ws, const Precond &pc, int m, double rel, cuda
         op_apply(ws, 1, zj, w, s);
         const int nv = j + 1;
         const unsigned ng = (unsigned)((nv + FG_GROUP - 1) / FG_GROUP);
-        k_fg_mdot<<<dim3(FG_XBLK, ng), VEC_BLOCK, 0, s>>>(n, V, n, nv, w, ws->fg_part);
-        k_fg_reduce<<<nv, 256, 0, s>>>(FG_XBLK, ws->fg_part, nv, h1);
+        k_fg_mdot<<<dim3(xb, ng), VEC_BLOCK, 0, s>>>(n, V, n, nv, w, ws->fg_part);
+        k_fg_reduce<<<nv, 256, 0, s>>>(xb, ws->fg_part, nv, h1);
         k_fg_update<<<gv, VEC_BLOCK, 0, s>>>(n, V, n, nv, h1, w, 0, ws->fg_part);
-        k_fg_mdot<<<dim3(FG_XBLK, ng), VEC_BLOCK, 0, s>>>(n, V, n, nv, w, ws->fg_part);
-        k_fg_reduce<<<nv, 256, 0, s>>>(FG_XBLK, ws->fg_part, nv, h2);
+        k_fg_mdot<<<dim3(xb, ng), VEC_BLOCK, 0, s>>>(n, V, n, nv, w, ws->fg_part);
+        k_fg_reduce<<<nv, 256, 0, s>>>(xb, ws->fg_part, nv, h2);
         k_fg_update<<<gv, VEC_BLOCK, 0, s>>>(n, V, n, nv, h2, w, 1, ws->fg_part);
         k_fg_reduce<<<1, 256, 0, s>>>(gv, ws->fg_part, 1, nrm);
         k_fg_scale<<<gv, VEC_BLOCK, 0, s>>>(n, w, nrm, w);
@@ -1546,7 +1562,7 @@ namespace bella {
 
 constexpr long long NOALLOC_MAX_NODES = 65536;                   // nx*ny
 constexpr long long NOALLOC_MAX_CELLS = 2 * NOALLOC_MAX_NODES;   // (nx+1)*(ny+1)
-constexpr long long NOALLOC_PARTIALS = (long long)NQ * NSM * 8;
+constexpr long long NOALLOC_PARTIALS = (long long)NQ * MAXGRID;
 // doubles: 4 FP64 cell planes + 4 FP32 cell planes (as 2 doubles' worth),
 // dinv/hc/z (FP64) + dinv/hc (FP32, one double's worth), 9 FP64 vectors,
 // partials, counter word and the Krylov state
@@ -1592,7 +1608,12 @@ extern "C" int bella_bicgstab2d_noalloc(const bella_op2d *op, const double *b, d
         return set_err(BELLA_EINVAL, "bella_bicgstab2d_noalloc: hplusx, hplusy, cxx, cyy, diag_inv are required");
     if (!(op->dx > 0.0) || !(op->dy > 0.0)) return set_err(BELLA_EINVAL, "bella_bicgstab2d_noalloc: dx, dy must be > 0");
     bella_solve_opts o;
-    if (opts) o = *opts; else bella_solve_opts_default(&o);
+    if (opts) {
+        o = *opts;
+    } else {   // the shared defaults, with the one precision this entry point has
+        bella_solve_opts_default(&o);
+        o.precision = 0;
+    }
     if (!(o.tol >= 0.0) || o.maxiter < 0) return set_err(BELLA_EINVAL, "bella_bicgstab2d_noalloc: bad tol/maxiter");
     if (o.precision != 0)
         return set_err(BELLA_EINVAL, "bella_bicgstab2d_noalloc: only precision 0 (FP64 BiCGStab) is available");

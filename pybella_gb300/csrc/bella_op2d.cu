@@ -253,7 +253,7 @@ Op2D<float> make_op<float>(bella_ws *ws) {
 
 int stencil_grid(int nx, int ny) {
     const int tiles = ((nx + TX - 1) / TX) * ((ny + TY - 1) / TY);
-    const int cap = NSM * (GRID_PER_SM < 8 ? GRID_PER_SM : 8);   // partials hold NSM*8 CTAs
+    const int cap = num_sms() * (GRID_PER_SM < 8 ? GRID_PER_SM : 8);   // partials hold MAXGRID CTAs
     return tiles < cap ? tiles : cap;
 }
 
@@ -278,7 +278,7 @@ static void launch_mode(bella_ws *ws, const StArgs<T> &a, cudaStream_t s) {
 int op2d_pack(bella_ws *ws, const bella_op2d *op, cudaStream_t s) {
     const size_t ncell = (size_t)(op->nx + 1) * (op->ny + 1);
     int g = (int)((ncell + 255) / 256);
-    if (g > NSM * 8) g = NSM * 8;
+    if (g > num_sms() * 8) g = num_sms() * 8;
     k_pack2d_cells<<<g, 256, 0, s>>>(*op, ws->a64, ws->a32, ws->adf, ws->cross);
     k_pack2d_nodes<<<g, 256, 0, s>>>(*op, ws->dinv64, ws->dinv32, ws->hc64, ws->hc32, ws->z64, ws->dinvdf,
                                      ws->hcdf);

@@ -252,7 +252,7 @@ static Op3D<dfloat> op3_of(bella_ws *ws, dfloat *) { return make_op3<dfloat>(ws,
 
 int stencil3d_grid(int nx, int ny, int nz) {
     const long long tiles = (long long)((nx + T3X - 1) / T3X) * ((ny + T3Y - 1) / T3Y) * ((nz + T3Z - 1) / T3Z);
-    const long long cap = (long long)NSM * 4;
+    const long long cap = (long long)num_sms() * 4;
     return (int)(tiles < cap ? tiles : cap);
 }
 
@@ -287,7 +287,7 @@ static void launch3(bella_ws *ws, const StArgs3<T> &a, cudaStream_t s) {
 int op3d_pack(bella_ws *ws, const bella_op3d *op, cudaStream_t s) {
     const long long ncell = (long long)(op->nx + 1) * (op->ny + 1) * (op->nz + 1);
     int g = (int)((ncell + 255) / 256);
-    if (g > NSM * 8) g = NSM * 8;
+    if (g > num_sms() * 8) g = num_sms() * 8;
     k_pack3d_cells<<<g, 256, 0, s>>>(*op, ws->a64, ws->a32, ws->adf);
     k_pack3d_nodes<<<g, 256, 0, s>>>(*op, ws->dinv64, ws->dinv32, ws->dinvdf, ws->hc64, ws->hc32, ws->hcdf,
                                      ws->z64);

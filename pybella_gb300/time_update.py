@@ -28,7 +28,10 @@ def dynamic_timestep(maxima, time, time_output, dxyz, step, CFL=0.5, dtfixed0=10
                      acoustic_timestep=0):
     """The time step of cfl.py:5-74 from the state's maxima (``bella_cfl_maxima``:
     |u|, |v|, |w|, |u|+c, |v|+c, |w|+c); ``dxyz`` = (dx, dy, dz) with dz = 1 in 2D
-    (grid.py:110, 171).  Returns dt."""
+    (grid.py:110, 171).  Returns dt; NaN when a maximum is NaN (a state that is
+    not finite), as the reference's numpy arithmetic gives it (cfl.py:25-45)."""
+    if any(m != m for m in maxima):
+        return float("nan")
     u_max, v_max, w_max, upc_max, vpc_max, wpc_max = (max(m, _EPS) for m in maxima)
     dx, dy, dz = dxyz
     if acoustic_timestep == 1:
@@ -56,30 +59,56 @@ class _Loop:
     def cfl_maxima(self):
         out = (ctypes.c_double * 6)()
         f = self.f
+        if getattr(self, "_cfl_scratch", None) is None:       # 6 words, allocated once per run
+            self._cfl_scratch = torch.zeros(6, dtype=torch.int64, device=self.dev)
         with torch.cuda.device(self.dev):
             _lib.check(self.lib.bella_cfl_maxima(*[ctypes.c_void_p(f[k].data_ptr()) for k in
                                                    ("rho", "rhou", "rhov", "rhow", "rhoY")],
-                                                 f["rho"].numel(), self.gamm, self.Msq, out, self._stream()),
+                                                 f["rho"].numel(), self.gamm, self.Msq,
+                                                 ctypes.c_void_p(self._cfl_scratch.data_ptr()), out,
+                                                 self._stream()),
                        "bella_cfl_maxima")
         return list(out)
 
     def run(self, t, tout, nsteps, t_ref=None, CFL=0.5, dtfixed0=100.0, dtfixed=100.0, acoustic_timestep=0,
-            precision="fp64"):
-        """Steps until ``tout`` or ``nsteps`` steps, dt from the CFL condition of the
-        state at each step's start ('CFLfixed': 21.69 / ``t_ref`` for the first two
-        steps when ``t_ref`` is given).  Returns ``(t, dts)``."""
-        step, dts = 0, []
+            precision="fp64", step=0):
+        """Steps until ``tout`` or until the global step index reaches ``nsteps``
+        (the reference's ``stepmax``), dt from the CFL condition of the state at each
+        step's start ('CFLfixed': 21.69 / ``t_ref`` while the step index is below 2,
+        when ``t_ref`` is given).  ``step`` is the global index to start from: ``do``
+        takes it in ``steps`` and returns it (time_update.py:129-135, 706-708), so
+        consecutive calls for successive output times continue one run (the Strang
+        order, the fixed first steps and the dt ramp follow the global index).
+        Returns ``(t, dts, step)``."""
+        dts = []
         while t < tout and step < nsteps:
             self.boundary()                                 # :130, before the time step of :135
             dt = dynamic_timestep(self.cfl_maxima(), t, tout, self.dxyz, step, CFL, dtfixed0, dtfixed,
                                   acoustic_timestep)
+            if not np.isfinite(dt):
+                raise FloatingPointError("non-finite time step at step %d: the state is not finite" % step)
             if t_ref is not None and step < 2:
                 dt = 21.69 / t_ref
             self.step(step, dt, precision)
             dts.append(dt)
             t += dt
             step += 1
-        return t, dts
+        return t, dts, step
+
+    def run_outputs(self, touts, stepmax, t=0.0, t_ref=None, precision="fp64", on_output=None, **cfl):
+        """The output loop of the reference's driver for one member
+        (__main__.py:198-393): :meth:`run` once per output time with the step index
+        carried across them, and ``t`` set to the output time rounded to three
+        decimals after each (__main__.py:266, 388).  ``on_output(t, step)`` is called
+        at every output time (the state is still on the device).  Returns
+        ``(t, step)``."""
+        step = 0
+        for tout in touts:
+            t, _, step = self.run(t, float(tout), stepmax, t_ref=t_ref, precision=precision, step=step, **cfl)
+            t = float(np.around(tout, 3))
+            if on_output is not None:
+                on_output(t, step)
+        return t, step
 
 
 class DeviceStep2D(_Loop):

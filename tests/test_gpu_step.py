@@ -78,7 +78,7 @@ def test_device_run_to_tout_matches_reference():
             max_iterations=6000)
     run = DeviceStep2D(Sol, mpv, NS(ndim=2, y=grid.elem_y), NS(iicx=grid.inx, iicy=grid.iny, dx=grid.dx, dy=grid.dy),
                        ud, NS(gamm=prm.gamm))
-    t, dts = run.run(0.0, float(d["meta"][7]), 4, t_ref=float(d["meta"][6]))
+    t, dts, nstep = run.run(0.0, float(d["meta"][7]), 4, t_ref=float(d["meta"][6]))
     run.download(Sol, mpv)
     assert len(dts) == 3 and abs(t - float(d["meta"][7])) < 1e-12
     for st in run.stats:

@@ -242,7 +242,7 @@ def test_run_to_tout_matches_reference_kat():
     hn, hc = dict(hn, S0=d["S0n"]), dict(hc, rhoY0=d["rhoY0"])
     Sol = {k: d["in_" + k].copy() for k in FIELDS}
     p2 = d["p2_in"].copy()
-    Sol, t, dts = step2d.run(Sol, p2, 0.0, float(d["meta"][7]), 4, grid, prm, hn, hc, d["S0c"], sf,
+    Sol, t, dts, _ = step2d.run(Sol, p2, 0.0, float(d["meta"][7]), 4, grid, prm, hn, hc, d["S0c"], sf,
                              float(d["meta"][6]))
     assert len(dts) == 3 and t == pytest.approx(float(d["meta"][7]), rel=1e-15)
     for k in FIELDS:

@@ -180,7 +180,7 @@ class _Stand:
         from oracle import nodal2d as n2
         return self._project(p, st, n2.impl_part, {})
 
-    def bella_cfl_maxima(self, rho, rhou, rhov, rhow, rhoY, n, gamm, Msq, out, s):
+    def bella_cfl_maxima(self, rho, rhou, rhov, rhow, rhoY, n, gamm, Msq, scratch, out, s):
         a = {k: _arr(v, (n,)) for k, v in (("rho", rho), ("rhou", rhou), ("rhov", rhov), ("rhow", rhow),
                                             ("rhoY", rhoY))}
         c = np.sqrt(gamm * a["rhoY"] ** gamm / a["rho"]) * (1.0 / np.sqrt(Msq))
@@ -321,7 +321,7 @@ def test_device_step2d_run_to_tout_vs_reference(host_torch, monkeypatch, tmp_pat
             max_iterations=6000)
     run = DeviceStep2D(Sol, mpv, NS(ndim=2, y=grid.elem_y), NS(iicx=grid.inx, iicy=grid.iny, dx=grid.dx, dy=grid.dy),
                        ud, NS(gamm=prm.gamm))
-    t, dts = run.run(0.0, float(d["meta"][7]), 4, t_ref=float(d["meta"][6]))
+    t, dts, nstep = run.run(0.0, float(d["meta"][7]), 4, t_ref=float(d["meta"][6]))
     run.download(Sol, mpv)
     assert len(dts) == 3 and t == pytest.approx(float(d["meta"][7]), rel=1e-15)
     for k in FIELDS:
@@ -346,3 +346,80 @@ def test_dynamic_timestep_matches_oracle():
         assert dynamic_timestep(maxima, t, tout, (grid.dx, grid.dy, 1.0), step, dtfixed=0.01) == ref
         ref_ac = step2d.dynamic_timestep(Sol, t, tout, grid, prm, step, acoustic_timestep=1)
         assert dynamic_timestep(maxima, t, tout, (grid.dx, grid.dy, 1.0), step, acoustic_timestep=1) == ref_ac
+
+
+def test_device_step2d_run_outputs_carries_the_step(host_torch, monkeypatch, tmp_path):
+    """Two output times (0.1, then 0.11) through DeviceStep2D.run_outputs continue one
+    run: the step index carries over, so the second window neither repeats the fixed
+    first steps ('CFLfixed') nor restarts the Strang order, and t is reset to the
+    rounded output time between them -- as the oracle's restatement of the
+    reference's output loop (__main__.py:198-393) does."""
+    from oracle import cases, step2d
+    from pybella_gb300.time_update import DeviceStep2D
+    d = np.load(golden("step_kat.npz"))
+    grid, prm, _, _, hn, hc, sf = cases.rising_bubble(inx=64, iny=32)
+    hn, hc = dict(hn, S0=d["S0n"]), dict(hc, rhoY0=d["rhoY0"])
+    _install(monkeypatch, tmp_path, NS(grid=grid, prm=prm, hn=hn, hc=hc, sf=sf))
+    S0c = d["S0c"]
+    Sol = NS(**{k: d["in_" + k].copy() for k in FIELDS})
+    mpv = NS(p2_nodes=d["p2_in"].copy(), HydroState=NS(rhoY0=hc["rhoY0"], get_S0c=lambda elem: S0c),
+             HydroState_n=NS(S0=hn["S0"]))
+    ud = NS(bdry_type=["wrap", "symmetric", "symmetric"], gravity_strength=[0.0, prm.g, 0.0], Msq=prm.Msq,
+            nonhydrostasy=1.0, compressibility=0.0, is_compressible=0, coriolis_strength=np.zeros(3),
+            u_wind_speed=0.0, v_wind_speed=0.0, w_wind_speed=0.0, stratification=sf, tol=1e-10,
+            max_iterations=6000)
+    run = DeviceStep2D(Sol, mpv, NS(ndim=2, y=grid.elem_y), NS(iicx=grid.inx, iicy=grid.iny, dx=grid.dx, dy=grid.dy),
+                       ud, NS(gamm=prm.gamm))
+    touts = [0.1, 0.11]
+    seen = []
+    t, step = run.run_outputs(touts, 10000, t_ref=1000.0, on_output=lambda t, s: seen.append((t, s)))
+    run.download(Sol, mpv)
+    rec = []
+    Sc = {k: d["in_" + k].copy() for k in FIELDS}
+    pc = d["p2_in"].copy()
+    Sc, tc, stepc = step2d.run_outputs(Sc, pc, touts, 10000, grid, prm, hn, hc, S0c, sf, 1000.0,
+                                       on_output=lambda t, S, p, s: rec.append((t, s)))
+    assert seen == rec and step == stepc and t == tc == 0.11
+    assert seen[0][1] == 3 and seen[1][1] > 3
+    for k in FIELDS:
+        assert _rel(getattr(Sol, k), Sc[k]) < 1e-10, k
+    assert _rel(mpv.p2_nodes, pc) < 1e-10
+
+
+def test_dynamic_timestep_propagates_nan():
+    """A NaN maximum (a state that is no longer finite) gives a NaN time step, as
+    numpy's .max() does in the reference (cfl.py:25-45), instead of a finite dt
+    from the other maxima."""
+    from pybella_gb300.time_update import dynamic_timestep
+    ok = [0.1, 0.2, 0.0, 1.1, 1.2, 1.0]
+    assert np.isfinite(dynamic_timestep(ok, 0.0, 1.0, (0.01, 0.01, 1.0), 3))
+    for k in range(6):
+        bad = list(ok)
+        bad[k] = float("nan")
+        assert np.isnan(dynamic_timestep(bad, 0.0, 1.0, (0.01, 0.01, 1.0), 3))
+        assert np.isnan(dynamic_timestep(bad, 0.0, 1.0, (0.01, 0.01, 1.0), 3, acoustic_timestep=1))
+
+
+def test_device_run_stops_on_a_non_finite_state(host_torch, monkeypatch, tmp_path):
+    """DeviceStep2D.run raises on a NaN in the state before it takes a step."""
+    from oracle import cases
+    from pybella_gb300.time_update import DeviceStep2D
+    d = np.load(golden("step_kat.npz"))
+    grid, prm, _, _, hn, hc, sf = cases.rising_bubble(inx=64, iny=32)
+    hn, hc = dict(hn, S0=d["S0n"]), dict(hc, rhoY0=d["rhoY0"])
+    _install(monkeypatch, tmp_path, NS(grid=grid, prm=prm, hn=hn, hc=hc, sf=sf))
+    S0c = d["S0c"]
+    rhou = d["in_rhou"].copy()
+    rhou[10, 10] = np.nan
+    Sol = NS(**{k: d["in_" + k].copy() for k in FIELDS})
+    Sol.rhou = rhou
+    mpv = NS(p2_nodes=d["p2_in"].copy(), HydroState=NS(rhoY0=hc["rhoY0"], get_S0c=lambda elem: S0c),
+             HydroState_n=NS(S0=hn["S0"]))
+    ud = NS(bdry_type=["wrap", "symmetric", "symmetric"], gravity_strength=[0.0, prm.g, 0.0], Msq=prm.Msq,
+            nonhydrostasy=1.0, compressibility=0.0, is_compressible=0, coriolis_strength=np.zeros(3),
+            u_wind_speed=0.0, v_wind_speed=0.0, w_wind_speed=0.0, stratification=sf, tol=1e-10,
+            max_iterations=6000)
+    run = DeviceStep2D(Sol, mpv, NS(ndim=2, y=grid.elem_y), NS(iicx=grid.inx, iicy=grid.iny, dx=grid.dx, dy=grid.dy),
+                       ud, NS(gamm=prm.gamm))
+    with pytest.raises(FloatingPointError):
+        run.run(0.0, 0.1, 10, t_ref=1000.0, step=2)
