@@ -65,6 +65,8 @@ def _args():
     ap.add_argument("--nz", type=int, default=257)
     ap.add_argument("--train-steps", type=int, default=1000)
     ap.add_argument("--skip", type=float, default=0.9)
+    ap.add_argument("--no-subresults", action="store_true",
+                    help="learned3d: skip the 2D solve and ensemble measurements carried in the same line")
     return ap.parse_args()
 
 
@@ -236,7 +238,19 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
 
-    nseeds = max(1, min(args.seeds, args.steps + args.warmup))
+    line = solve2d_line(args, dev, local, rank, world, dist, args.steps, args.warmup, max(1, args.seeds), args.steps,
+                        want_cpu=rank == 0 and world == 1 and not args.no_cpu_baseline)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def solve2d_line(args, dev, local, rank, world, dist, steps, warmup, nseeds, e2e_steps, want_cpu):
+    """The 2049x1025 standalone solve measured over ``steps`` solves of ``nseeds``
+    resident systems; returns the JSON line (dict)."""
+    import torch
+    from pybella_gb300 import linalg, workloads, _lib
     from pybella_gb300 import replicas
     systems = [workloads.stratified_2d(seed=sd, nx=NX, ny=NY, device=dev) for sd in replicas.seeds_for_rank(rank, nseeds)]
     ws = _lib.Workspace(local)
@@ -252,7 +266,7 @@ def run_gpu(args):
         stats.append(st)
 
     warm = []
-    for i in range(args.warmup):
+    for i in range(warmup):
         step(i, warm)
     # one FP64 solve of the first system: iteration count of the scipy-path algorithm
     w0 = systems[0]
@@ -272,8 +286,8 @@ def run_gpu(args):
     t0 = time.perf_counter()
     ev0.record()
     stats = []
-    for i in range(args.steps):
-        step(args.warmup + i, stats)
+    for i in range(steps):
+        step(warmup + i, stats)
     ev1.record()
     torch.cuda.synchronize()
     if dist is not None:
@@ -285,17 +299,17 @@ def run_gpu(args):
     kt = {k: ws.kernel_time(k) for k in range(4)}
     ws.profile(False)
     ms = replicas.max_over_ranks(ms, device=dev)
-    total_solves = args.steps * world
-    value = replicas.aggregate_rate(args.steps, world, ms / 1000.0)
+    total_solves = steps * world
+    value = replicas.aggregate_rate(steps, world, ms / 1000.0)
 
     # ---- end to end through the drop-in API with host buffers ----
-    host = [] if args.no_e2e else [_to_np(systems[i % nseeds]) for i in range(min(nseeds, 4))]
+    host = [] if args.no_e2e or e2e_steps == 0 else [_to_np(systems[i % nseeds]) for i in range(min(nseeds, 4))]
     e2e_stats = []
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
     te0 = time.perf_counter()
-    for i in range(args.steps if host else 0):
+    for i in range(e2e_steps if host else 0):
         h = host[i % len(host)]
         A = linalg.NodalHelmholtz2D(h["hplusx"], h["hplusy"], h["hcenter"], h["cor"], h["diag_inv"],
                                     NX, NY, h["dx"], h["dy"], h["x_wall"], h["y_wall"], ws=ws)
@@ -308,7 +322,7 @@ def run_gpu(args):
         t = torch.tensor([te], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         te = float(t.item())
-    e2e_value = total_solves / te if host else None
+    e2e_value = e2e_steps * world / te if host else None
     nnode = NX * NY
     ncell = (NX + 1) * (NY + 1)
     h2d = 8 * (4 * ncell + 2 * nnode) + 8 * nnode   # hplusx, hplusy, cxx, cyy, diag_inv, hcenter, b
@@ -341,21 +355,21 @@ def run_gpu(args):
         bg.close()
         bg_stats.append(st)
 
-    for i in range(args.warmup):
+    for i in range(warmup):
         bg_step(i)
     bg_stats.clear()
     torch.cuda.synchronize()
     eb0, eb1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     eb0.record()
-    for i in range(args.steps):
-        bg_step(args.warmup + i)
+    for i in range(steps):
+        bg_step(warmup + i)
     eb1.record()
     torch.cuda.synchronize()
-    bg_ms = eb0.elapsed_time(eb1) / args.steps
+    bg_ms = eb0.elapsed_time(eb1) / steps
 
     line = {
-        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": steps,
+        "warmup": warmup, "ms_per_step": ms / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": {"fp64": "f64", "mixed": "f32+f64", "df64": "f32x2 (double-float)"}[args.precision],
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "rtol": TOL, "precision": args.precision,
@@ -384,17 +398,14 @@ def run_gpu(args):
         "kernel_ms_per_launch": {names[k]: (kt[k][0] / kt[k][1] if kt[k][1] else None) for k in kt},
         "wall_s": wall,
     }
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if want_cpu:
         w_np = _to_np(systems[0])
         v, per_iter, n_it, dt = cpu_sample(w_np, st64["iterations"], args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": 1, "kind": "port",
                                 "sample": "%d FP64 BiCGStab iterations (NumPy lap2D_gather_new restatement + scipy) "
                                           "on seed 0 in %.1f s; solves/s = 1/(%.3f s/iter x %d iterations of the "
                                           "FP64 solve)" % (n_it, dt, per_iter, st64["iterations"])}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    if dist is not None:
-        dist.destroy_process_group()
+    return line
 
 
 # --------------------------------------------------------------------------
@@ -426,6 +437,18 @@ def run_ensemble(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
+    line = ensemble_line(args, dev, local, rank, world, dist, args.steps, args.warmup, args.steps,
+                         want_cpu=rank == 0 and world == 1 and not args.no_cpu_baseline)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def ensemble_line(args, dev, local, rank, world, dist, steps, warmup, e2e_steps, want_cpu):
+    """One round of the 48 members' solves per step in one persistent launch; returns the JSON line (dict)."""
+    import torch
+    from pybella_gb300 import ensemble, workloads
     members = workloads.rising_bubble_ensemble(seed=17 + rank, device=dev)
     ops = [workloads.operator_2d(w) for w in members]
     bs = [w["b"] for w in members]
@@ -433,7 +456,7 @@ def run_ensemble(args):
     prec = "fp64" if args.precision == "fp64" else "df64"
     choice, tune_ms = ensemble.autotune(ops, bs, probe_iters=20, precision=prec)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    for i in range(args.warmup):
+    for i in range(warmup):
         ensemble.solve_ensemble(ops, bs, tol=1e-10, maxiter=20000, out=xs, precision=prec)
     clocks = ClockSampler(local)
     clocks.start()
@@ -444,7 +467,7 @@ def run_ensemble(args):
     stats = None
     torch.cuda.synchronize()
     ev0.record()
-    for i in range(args.steps):
+    for i in range(steps):
         flush.fill_(float(i))
         k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         k0.record()
@@ -462,7 +485,7 @@ def run_ensemble(args):
         t = torch.tensor([ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    value = args.steps * world * len(ops) / (ms / 1000.0)
+    value = steps * world * len(ops) / (ms / 1000.0)
     # end to end: host operands -> device, one round, solutions back to the host
     def _np(v):
         if isinstance(v, torch.Tensor):
@@ -473,7 +496,7 @@ def run_ensemble(args):
     host = [{k: _np(v) for k, v in w.items()} for w in members]
     te0 = time.perf_counter()
     h2d = d2h = 0
-    for i in range(args.steps):
+    for i in range(e2e_steps):
         ops_e = [workloads.operator_2d(h, ws=op.ws) for h, op in zip(host, ops)]
         xs_e, _ = ensemble.solve_ensemble(ops_e, [h["b"] for h in host], tol=1e-10, maxiter=20000, precision=prec)
         out = [x.cpu().numpy() for x in xs_e]
@@ -498,8 +521,8 @@ def run_ensemble(args):
     alg = sum(200.0 * op.n * st["iterations"] for op, st in zip(ops, stats))
     achieved = alg / (statistics.median(step_ms) / 1000.0) / 1e9
     line = {
-        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": steps,
+        "warmup": warmup, "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32x2 (double-float) + f64 refinement",
         "data": "synthetic",
         "config": {"workload": ENS_WORKLOAD, "members": len(ops), "unknowns": int(sum(op.n for op in ops)),
@@ -507,9 +530,9 @@ def run_ensemble(args):
                    "rtol": 1e-10, "launch_config": ensemble.configs()[choice], "autotune_ms": tune_ms,
                    "l2": "flushed (256 MB write) before every round",
                    "parallelism": "replicas" if world > 1 else "single"},
-        "e2e": {"value": args.steps * world * len(ops) / te, "unit": "solves/s", "h2d_bytes_per_step": h2d,
+        "e2e": {"value": e2e_steps * world * len(ops) / te if e2e_steps else None, "unit": "solves/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "path": "pybella_gb300.ensemble.solve_ensemble on NumPy operands"},
-        "gpu_launches": args.steps,
+        "gpu_launches": steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "kernel": "k_batch_bicgstab (whole round, one launch)",
                      "peak_source": peak_kind, "alg_bytes_per_launch": alg},
@@ -520,7 +543,7 @@ def run_ensemble(args):
         "sequential_single_solves": {"solves_per_s": len(ops) / seq_s, "round_s": seq_s,
                                      "path": "NodalHelmholtz2D.solve per member, precision %s" % prec},
     }
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if want_cpu:
         per_grid = {}
         est = 0.0
         for w, op, st in zip(host, ops, stats):
@@ -536,10 +559,7 @@ def run_ensemble(args):
                                 "sample": "40 FP64 BiCGStab iterations per grid size (NumPy lap2D_gather_new "
                                           "restatement + scipy); a round = sum over members of s/iteration x the "
                                           "member's iterations"}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    if dist is not None:
-        dist.destroy_process_group()
+    return line
 
 
 # --------------------------------------------------------------------------
@@ -560,27 +580,80 @@ def _peaks_tensor():
 
 
 def cpu_sample_3d(op, seconds):
-    """Seconds per plain BiCGStab iteration of the FP64 NumPy restatement (oracle)
-    on the full 3D grid: two lap3D applications and the vector updates."""
-    from oracle import nodal3d as n3
-    n = op["nx"] * op["ny"] * op["nz"]
-    rng = np.random.default_rng(0)
-    r = rng.standard_normal(n)
-    p = r.copy()
+    """Seconds per plain FP64 BiCGStab iteration of the oracle's C restatement
+    (lap3D + scipy's BiCGStab loop, OpenMP over all host threads) on the full 3D
+    grid: bounded runs of a few iterations until ``seconds`` have passed.
+    Returns ``(seconds per iteration, iterations timed, threads)``."""
+    from oracle import cbuild
+    b = np.random.default_rng(0).standard_normal(op["nx"] * op["ny"] * op["nz"])
+    cbuild.bicgstab3d(op, b, 1e-30, 1)                       # first touch, thread start-up
     t0 = time.perf_counter()
     k = 0
-    while True:
-        v = n3.lap3d(p, op)
-        a = float(r @ r) / float(r @ v)
-        s_ = r - a * v
-        t = n3.lap3d(s_, op)
-        w = float(t @ s_) / max(float(t @ t), 1e-300)
-        r = s_ - w * t
-        p = r + 0.5 * (p - w * v)
-        k += 1
-        if time.perf_counter() - t0 >= seconds:
-            break
-    return (time.perf_counter() - t0) / k, k
+    while k < 3 or time.perf_counter() - t0 < seconds:
+        _, _, it, _ = cbuild.bicgstab3d(op, b, 1e-30, 5)
+        k += it
+    return (time.perf_counter() - t0) / k, k, cbuild.threads()
+
+
+def plain_iterations_fit(seed, shape, grids=((33, 17, 33), (65, 33, 65), (129, 65, 129))):
+    """Iterations of plain FP64 BiCGStab to rtol 1e-8 on ``shape``, from full solves
+    of the same construction (same seed) on smaller grids with the C restatement,
+    fitted as log(iterations) = a + alpha log(nx - 1) and evaluated at ``shape``
+    (plain BiCGStab on this operator needs about h^-alpha iterations; its slow
+    modes are the smooth and hourglass-modulated ones).  Returns
+    ``(estimate, {grid: iterations}, alpha, seconds)``."""
+    from oracle import cases, cbuild
+    t0 = time.perf_counter()
+    pts = {}
+    for g in grids:
+        w = cases.stratified_3d(seed, *g)
+        _, info, it, _ = cbuild.bicgstab3d(w["op"], w["b"], TOL, 400000)
+        pts["x".join(map(str, g))] = it
+    xs = np.log(np.array([g[0] - 1.0 for g in grids]))
+    ys = np.log(np.array(list(pts.values()), dtype=np.float64))
+    alpha, a = np.polyfit(xs, ys, 1)
+    est = float(np.exp(a + alpha * np.log(shape[0] - 1.0)))
+    return est, pts, float(alpha), time.perf_counter() - t0
+
+
+def fp64_oracle_errors(A, b, xs, shape):
+    """Relative L2 error of each solution in ``xs`` against a tightly converged FP64
+    solution of the same system (true FP64 residual <= 1e-13: background-
+    preconditioned solve with FP64 refinement), computed outside the timed region.
+    The pressure is determined up to the operator's null modes (constants and
+    hourglass modes), so it is compared through its cell gradients -- the 4-edge
+    differences that the momentum correction uses (rhou, rhov, rhow) -- and,
+    with its mean removed, directly."""
+    import torch
+    from pybella_gb300.spectral import BackgroundSolve
+    bg = BackgroundSolve(A)
+    xs_ref, st = A.solve(b, tol=1e-13, maxiter=5000, preconditioner=bg, method="bicgstab", max_outer=60)
+    bg.close()
+
+    def grads(x):
+        p = x.reshape(shape)
+        gx = p[1:] - p[:-1]
+        gy = p[:, 1:] - p[:, :-1]
+        gz = p[:, :, 1:] - p[:, :, :-1]
+        return (gx[:, 1:, 1:] + gx[:, :-1, 1:] + gx[:, 1:, :-1] + gx[:, :-1, :-1],
+                gy[1:, :, 1:] + gy[:-1, :, 1:] + gy[1:, :, :-1] + gy[:-1, :, :-1],
+                gz[1:, 1:] + gz[:-1, 1:] + gz[1:, :-1] + gz[:-1, :-1])
+    rel = lambda a_, b_: float(torch.linalg.norm(a_ - b_) / torch.linalg.norm(b_))
+    gref = grads(xs_ref)
+    out = {"reference_solution": {"relres": st["relres"], "iterations": st["iterations"], "status": st["status"],
+                                  "what": "FP64 true residual <= 1e-13, background-preconditioned, FP64 refinement"}}
+    for name, x in xs.items():
+        g = grads(x)
+        out[name] = {"p_mean_removed": rel(x - x.mean(), xs_ref - xs_ref.mean()),
+                     "grad_x_rhou": rel(g[0], gref[0]), "grad_y_rhov": rel(g[1], gref[1]),
+                     "grad_z_rhow": rel(g[2], gref[2])}
+    return out
+
+
+def learned3d_config(shape):
+    """The ``config`` of the 3D solve workload: identical in both arms."""
+    return {"workload": LEARNED3D % "x".join(map(str, shape)), "nodes": list(shape), "rtol": TOL,
+            "system_seed": 7}
 
 
 def run_learned3d(args):
@@ -614,16 +687,17 @@ def run_learned3d(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     kw_learned = dict(method="fgmres", restart=30)
     bg_launches = [0]
+    xs = {k: torch.zeros(A.n, dtype=torch.float64, device=dev) for k in ("plain", "background", "learned")}
 
     def step(name):
         if name == "plain":
-            return A.solve(b, tol=TOL, maxiter=200000, precision="df64")[1]
+            return A.solve(b, tol=TOL, maxiter=200000, precision="df64", out=xs[name])[1]
         bg = BackgroundSolve(A)                      # set up from this step's coefficients
         pc = bg if name == "background" else learned.LearnedPreconditioner(bg, net, "post")
         kw = dict(method="bicgstab") if name == "background" else kw_learned
         with warnings.catch_warnings():
             warnings.simplefilter("ignore", RuntimeWarning)
-            st = A.solve(b, tol=TOL, maxiter=20000, preconditioner=pc, **kw)[1]
+            st = A.solve(b, tol=TOL, maxiter=20000, preconditioner=pc, out=xs[name], **kw)[1]
         bg_launches[0] += bg.launches()
         bg.close()
         return st
@@ -713,25 +787,29 @@ def run_learned3d(args):
     if world == 1 and not args.no_cpu_baseline:
         from oracle import cases
         wc = cases.stratified_3d(7, *shape)
-        per_it, k = cpu_sample_3d(wc["op"], args.cpu_seconds)
-        cpu = {"value": 1.0 / (per_it * P["stats"][-1]["iterations"]), "unit": "solves/s", "cores": 1,
+        per_it, k, nthr = cpu_sample_3d(wc["op"], args.cpu_seconds)
+        cpu = {"value": 1.0 / (per_it * P["stats"][-1]["iterations"]), "unit": "solves/s", "cores": nthr,
                "kind": "port",
-               "sample": "%d iterations of plain FP64 BiCGStab with the NumPy lap3D restatement on the full "
-                         "grid (%.2f s each), times the %d iterations of the GPU plain solve"
-                         % (k, per_it, P["stats"][-1]["iterations"])}
+               "sample": "%d iterations of plain FP64 BiCGStab (the oracle's C restatement of lap3D and scipy's "
+                         "loop, OpenMP on %d host threads) on the full grid, %.1f ms each, times the %d iterations "
+                         "the same algorithm took on the GPU in this run" % (k, nthr, per_it * 1e3,
+                                                                            P["stats"][-1]["iterations"])}
     stats = lambda R: {"solves_per_s": 1000.0 / R["ms"], "ms": R["ms"], "iterations": R["stats"][-1]["iterations"],
                        "outer": R["stats"][-1]["outer"], "relres": R["stats"][-1]["relres"],
                        "fallback": R["stats"][-1]["fallback"], "status": R["stats"][-1]["status"]}
+    oracle_err = fp64_oracle_errors(A, b, xs, shape)
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16 network + f32 inner / f64 refinement", "data": "synthetic",
-        "config": {"workload": LEARNED3D % "x".join(map(str, shape)),
-                   "network": "6 layers 3x3x3, 32 channels, 2x2x2-blocked grid, linear, identity path %.2f" % args.skip,
-                   "train_steps": args.train_steps, "train_s": train_s, "final_loss": losses[-1][1],
-                   "parallelism": "replicas" if world > 1 else "single GPU",
-                   "plain_steps": "1 warm-up + 1 timed (one plain solve takes tens of seconds)",
-                   "l2": "256 MB L2 flush before every step; operator planes %.0f MB" % (A.n * 8 * 6 / 1e6)},
+        "config": learned3d_config(shape),
+        "setup": {"network": "6 layers 3x3x3, 32 channels, 2x2x2-blocked grid, linear, identity path %.2f"
+                             % args.skip,
+                  "train_steps": args.train_steps, "train_s": train_s, "final_loss": losses[-1][1],
+                  "parallelism": "replicas" if world > 1 else "single GPU",
+                  "plain_steps": "1 warm-up + 1 timed (one plain solve takes tens of seconds)",
+                  "l2": "256 MB L2 flush before every step; operator planes %.0f MB" % (A.n * 8 * 6 / 1e6)},
+        "fp64_oracle_err": oracle_err,
         "plain": stats(P), "background": stats(B), "learned": stats(L),
         "learned_over_plain": P["ms"] / L["ms"], "background_over_plain": P["ms"] / B["ms"],
         "network_gain_over_background": B["ms"] / L["ms"],
@@ -747,44 +825,53 @@ def run_learned3d(args):
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if world == 1 and not args.no_subresults:
+        # the other measured configurations, in the same run: the 2049x1025 standalone
+        # solve over its 64 seeds, and one ensemble round of 48 members per step
+        del A, net, xs, bg
+        torch.cuda.empty_cache()
+        line["solve2d"] = solve2d_line(args, dev, local, 0, 1, None, 64, 2, 64, 4, want_cpu=False)
+        line["ensemble"] = ensemble_line(args, dev, local, 0, 1, None, 5, 2, 2, want_cpu=False)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
 
 
-# iterations of plain FP64 BiCGStab on the seed-7 257x129x257 system (the GPU
-# FP64/double-float solve of the same system, same algorithm and tolerance);
-# the CPU arm times iterations on the full grid and multiplies by this count
-PLAIN3D_ITERS = 40512
-
-
 def run_reference_3d(args):
-    """``--impl reference`` for the 3D workload: plain FP64 BiCGStab with the
-    NumPy restatement of lap3D on the host cores (bounded iteration samples)."""
+    """``--impl reference`` for the 3D workload: plain FP64 BiCGStab -- the
+    reference's solve, scipy's bicgstab on lap3D -- as the oracle's C restatement
+    on all the host cores.  A full solve takes tens of thousands of iterations
+    (tens of minutes on the host), so each step times a bounded sample of
+    iterations on the full grid and the iterations per solve come from full
+    solves on smaller grids of the same construction, fitted over the grid size
+    (stated in the line as an extrapolation)."""
     world, rank, local = _dist()
     if world > 1 and rank != 0:
         return
     from oracle import cases
     shape = (args.nx, args.ny, args.nz)
-    wc = cases.stratified_3d(7, *shape)
-    iters = PLAIN3D_ITERS * (((args.nx - 1) / 256.0) ** 2 if shape != (257, 129, 257) else 1.0)
-    vals = []
     t_all0 = time.perf_counter()
+    iters, pts, alpha, fit_s = plain_iterations_fit(7, shape)
+    wc = cases.stratified_3d(7, *shape)
+    vals, per = [], []
     for s_ in range(args.warmup + args.steps):
-        per_it, k = cpu_sample_3d(wc["op"], max(2.0, args.cpu_seconds / 4))
+        per_it, k, nthr = cpu_sample_3d(wc["op"], max(1.0, args.cpu_seconds / 8))
         if s_ >= args.warmup:
             vals.append(1.0 / (per_it * iters))
+            per.append(per_it)
     value = float(np.mean(vals))
+    sample = ("plain FP64 BiCGStab (the oracle's C restatement of lap3D and scipy's loop) on %d host threads: "
+              "%.1f ms per iteration on the full grid (bounded samples), times %.0f iterations per solve "
+              "extrapolated from full solves of the same system construction on smaller grids %s (fit "
+              "iterations ~ (nx-1)^%.2f)" % (nthr, 1e3 * float(np.mean(per)), iters, pts, alpha))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": LEARNED3D % "x".join(map(str, shape)), "arm": "plain BiCGStab on the host",
-                       "l2": "inputs resident on host"},
-            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": 1, "kind": "port",
-                             "sample": "NumPy lap3D restatement + plain FP64 BiCGStab iterations on the full grid "
-                                       "(bounded samples of ~%.0f s), times %d iterations per solve (the count of "
-                                       "the same algorithm on this system)" % (max(2.0, args.cpu_seconds / 4),
-                                                                              iters)},
+            "config": learned3d_config(shape),
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": nthr, "kind": "port", "sample": sample},
+            "extrapolated": {"iterations_per_solve": iters, "fit_points": pts, "alpha": alpha, "fit_s": fit_s,
+                             "what": "solves/s = 1 / (measured s per iteration x fitted iterations per solve); "
+                                     "no full solve runs in this line"},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": time.perf_counter() - t_all0}
     print(json.dumps(line), flush=True)

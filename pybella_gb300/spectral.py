@@ -1,14 +1,18 @@
-"""Background solve of the 3D nodal operator (libbella_gb300 ``bella_spectral3d_*``).
+"""Background solve of the nodal operators (libbella_gb300 ``bella_spectral3d_*`` /
+``bella_spectral2d_create``).
 
-The exact inverse of the 27-point operator with every cell coefficient
-replaced by its mean over x and z per y-cell (the stratified background) and
-``hcenter`` by its mean per y-node: Hartley or DCT-I transforms along x and z
-(dense FP32 GEMMs on the device), an FP64 tridiagonal solve along y for every
-(kx, kz) mode, pseudo-inverse on the modes of the operator's null space.  As a
-right preconditioner of flexible BiCGStab it bounds the condition number by
-the spread of the cell coefficients about their horizontal means.  The
-reference solves without a preconditioner (second_projection.py:230 passes no
-``M`` to scipy's bicgstab); this is the slot it fills.
+The exact inverse of the 27-point (3D) or 9-point (2D) operator with every
+cell coefficient replaced by its mean over the horizontal axes per y-cell (the
+stratified background) and ``hcenter`` by its mean per y-node: Hartley
+(periodic axis) or DCT-I (wall axis) transforms along x and z, a tridiagonal
+solve along y for every horizontal mode, pseudo-inverse on the modes of the
+operator's null space.  The transforms are two-pass register FFTs for
+power-of-two lengths (dense FP32 GEMMs otherwise); the line solves sweep in FP32
+with Thomas factors computed once per operator in FP64.  As a right
+preconditioner it bounds the condition number by the spread of the cell
+coefficients about their horizontal means.  The reference solves without a
+preconditioner (second_projection.py:230 passes no ``M`` to scipy's bicgstab);
+this is the slot it fills.
 """
 import ctypes
 

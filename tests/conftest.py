@@ -15,7 +15,8 @@ def pytest_configure(config):
 # Tests of the advection and of whole time steps build on the projection and solver
 # entry points the other files test: they run after those (in this order), so that a
 # failure in a building block is reported by that block's own test first.
-_COMPOSED = ("test_gpu_advection.py", "test_gpu_projection_walls.py", "test_gpu_step.py", "test_gpu_step3d.py")
+_COMPOSED = ("test_gpu_advection.py", "test_gpu_projection_walls.py", "test_gpu_step.py", "test_gpu_step3d.py",
+             "test_gpu_fullrun.py")
 
 
 def pytest_collection_modifyitems(config, items):

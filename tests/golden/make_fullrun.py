@@ -3,6 +3,8 @@
 needed at test time).
 
     python tests/golden/make_fullrun.py /path/to/pyBELLA [--stop TOUT]
+    python tests/golden/make_fullrun.py --oracle
+
 
 The case is the reference's ``inputs/rising_bubble.py`` (160x80 cells, CFL 0.5,
 'CFLfixed', output times 0.1 ... 1.0 every 0.01 in units of t_ref = 1000 s),
@@ -18,6 +20,15 @@ Python: about 45 s per solve, a few hours for the whole run.  The state is
 written after every tenth output time (``fullrun_kat.npz``: theta = rhoY / rho
 at t = 0.1, 0.2, ..., all fields and p2 at the last output time reached, the
 step count and t), so an interrupted run still leaves a usable fixture.
+
+``--oracle`` runs the same case through the oracle's restatement of the step and
+its output loop (``oracle/step2d.py``: ``run_outputs``, pinned to the reference's
+``do``) in a few minutes and writes ``fullrun_oracle_kat.npz`` with the same
+keys, from the same initial state (the reference's, when ``fullrun_kat.npz``
+exists).  scipy's BiCGStab takes its inner products from BLAS, whose summation
+order depends on the thread count, so the two runs agree to rounding, not bit
+for bit, unless both use the same count; the committed oracle fixture was made
+with OPENBLAS_NUM_THREADS=1, the reference's with the host's default (8).
 """
 import os
 import sys
@@ -32,7 +43,41 @@ import refshim  # noqa: E402
 FIELDS = ["rho", "rhou", "rhov", "rhow", "rhoY", "rhoX"]
 
 
+def oracle_main():
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from oracle import cases, step2d
+    grid, prm, Sol, p2, hn, hc, sf = cases.rising_bubble()
+    S0c = np.broadcast_to(hc["S0"][None, :], grid.elem_sc).copy()
+    ref = os.path.join(HERE, "fullrun_kat.npz")
+    if os.path.exists(ref):                        # the reference's initial state and backgrounds
+        d = np.load(ref)
+        Sol = {k: d["in_" + k].copy() for k in FIELDS}
+        p2 = d["p2_in"].copy()
+        hn, hc, S0c = dict(hn, S0=d["S0n"]), dict(hc, rhoY0=d["rhoY0"]), d["S0c"]
+    rec = {"in_" + k: np.copy(Sol[k]) for k in FIELDS}
+    rec.update(p2_in=np.copy(p2), S0n=np.copy(hn["S0"]), rhoY0=np.copy(hc["rhoY0"]), S0c=np.copy(S0c),
+               meta=np.array([grid.inx, grid.iny, prm.Msq, prm.g, prm.gamm, 1000.0, prm.tol, 0.5]))
+    touts = np.arange(0.0, 1.01, 0.01)[10:]                      # inputs/rising_bubble.py:25
+    thetas, ts = [], []
+    t0 = time.time()
+
+    def on_output(t, S, p, step):
+        if int(round(t * 100)) % 10 == 0:
+            thetas.append(S["rhoY"] / S["rho"])
+            ts.append(t)
+            print("tout %.3f  step %d  %.0f s" % (t, step, time.time() - t0), flush=True)
+    Sol, t, step = step2d.run_outputs(Sol, p2, touts, 10000, grid, prm, hn, hc, S0c, sf, 1000.0,
+                                      on_output=on_output)
+    rec["theta"], rec["theta_t"] = np.array(thetas), np.array(ts)
+    for k in FIELDS:
+        rec["out_" + k] = np.copy(Sol[k])
+    rec.update(out_p2=np.copy(p2), out_t=np.array(t), out_step=np.array(step))
+    np.savez_compressed(os.path.join(HERE, "fullrun_oracle_kat.npz"), **rec)
+
+
 def main():
+    if "--oracle" in sys.argv:
+        return oracle_main()
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     if not args:
         raise SystemExit("usage: make_fullrun.py REFERENCE_ROOT [--stop TOUT]")

@@ -627,7 +627,9 @@ def rising_bubble_step0(out):
 
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    ref = args[0] if args else "/root/reference"
+    if not args:
+        raise SystemExit("usage: make_golden.py REFERENCE_ROOT [--3d-only | --explicit-only]")
+    ref = args[0]
     refshim.install(ref)
     out = HERE
     lap3d_kat(out)

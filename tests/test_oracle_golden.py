@@ -347,3 +347,32 @@ def test_oracle_explicit_parts_match_reference(tag):
     n2.euler_backward_non_advective_expl_part(S, d[tag + "_S0n"], grid, prm, dt, hc, strat, wind=wind)
     for k in S:
         np.testing.assert_array_equal(S[k], d["%s_ex_%s" % (tag, k)], err_msg=k)
+
+
+def test_oracle_output_loop_matches_reference_full_run():
+    """The oracle's output loop (``step2d.run_outputs``: __main__.py:198-393 around
+    time_update.do) against the reference's own rising-bubble run
+    (``fullrun_kat.npz``, 160x80 cells): theta at t = 0.1 (3 steps, one output
+    time) and t = 0.2 (13 steps over eleven output times, so the step index and
+    t carry across calls).  Equal to rounding: scipy's inner products come from
+    BLAS, whose summation order follows the host's thread count."""
+    from oracle import cases, step2d
+    d = np.load(golden("fullrun_kat.npz"))
+    grid, prm, _, _, hn, hc, sf = cases.rising_bubble()
+    hn, hc = dict(hn, S0=d["S0n"]), dict(hc, rhoY0=d["rhoY0"])
+    Sol = {k: d["in_" + k].copy() for k in FIELDS}
+    p2 = d["p2_in"].copy()
+    want = {round(float(t), 3): th for t, th in zip(d["theta_t"], d["theta"]) if t <= 0.2 + 1e-9}
+    touts = np.arange(0.0, 1.01, 0.01)[10:21]
+    got = {}
+
+    def on_output(t, S, p, step):
+        if round(t, 3) in want:
+            got[round(t, 3)] = (S["rhoY"] / S["rho"], step)
+    step2d.run_outputs(Sol, p2, touts[:1 if len(want) == 1 else 11], 10000, grid, prm, hn, hc, d["S0c"], sf, 1000.0,
+                       on_output=on_output)
+    assert set(got) == set(want)
+    for t, th in want.items():
+        mine, step = got[t]
+        assert np.abs(mine - th).max() <= 1e-13, (t, np.abs(mine - th).max())
+    assert got[0.1][1] == 3
