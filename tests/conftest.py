@@ -21,6 +21,7 @@ _COMPOSED = ("test_gpu_advection.py", "test_gpu_projection_walls.py", "test_gpu_
 
 def pytest_collection_modifyitems(config, items):
     rank = {name: k + 1 for k, name in enumerate(_COMPOSED)}
+    rank["test_zz_no_alloc.py"] = len(_COMPOSED) + 1      # the allocation-free entry point's test runs last
     items.sort(key=lambda it: rank.get(os.path.basename(str(it.fspath)), 0))
 
 

@@ -97,3 +97,24 @@ def test_noalloc_rejects_oversized_grid():
                                       ctypes.c_void_p(0))
     assert rc == _lib.BELLA_EINVAL
     assert b"too large" in lib.bella_last_error()
+
+
+def test_noalloc_null_opts_takes_the_defaults():
+    """opts == NULL: the shared defaults (tol 1e-8, 6000 iterations) in this entry
+    point's one precision, FP64; the result meets the default tolerance."""
+    import torch
+    from pybella_gb300 import _lib
+    lib = _lib.load()
+    op, b, _ = _system()
+    keep = [_dev(op["hplusx"]), _dev(op["hplusy"]), _dev(op["cor"][0]), _dev(op["cor"][1]), _dev(op["diag_inv"])]
+    o2 = _lib.Op2D(op["nx"], op["ny"], int(op["x_wall"]), int(op["y_wall"]), op["dx"], op["dy"],
+                   _ptr(keep[0]), _ptr(keep[1]), _ptr(None), _ptr(keep[2]), _ptr(keep[3]), _ptr(None),
+                   _ptr(None), _ptr(keep[4]))
+    bd = _dev(b)
+    x = torch.zeros_like(bd)
+    st = _lib.SolveStats()
+    rc = lib.bella_bicgstab2d_noalloc(ctypes.byref(o2), _ptr(bd), _ptr(x), None, ctypes.byref(st),
+                                      ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0, (rc, lib.bella_last_error())
+    torch.cuda.synchronize()
+    assert st.status == 0 and true_relres(op, x.cpu().numpy(), b) <= 1e-8
