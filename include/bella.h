@@ -47,7 +47,14 @@ typedef struct bella_ws bella_ws;   /* opaque workspace */
  * x_wall / y_wall: 1 zeroes the hplus of the outer cell column / row
  * (the reference's wall handling, laplacian.py:691-713); periodic wrap with
  * the duplicated seam (wrap distance n-1, laplacian.py:595-638) is always on.
+ * y_wall = BELLA_Y_MIRROR (x_wall = 0) is the operator of the reference's
+ * LAMB_BDRY branch (lap2D_numba_test, laplacian.py:511-512, 531-543, 749-868):
+ * the same operands, x periodic, y padded by mirroring (node -1 <- node 1,
+ * node ny <- node ny-2), no cell zeroed.  Only bella_apply_* and bella_bicgstab
+ * take it (no null-space projection); the ensemble, background solve and
+ * allocation-free entry points reject it.
  */
+#define BELLA_Y_MIRROR 2
 typedef struct bella_op2d {
     int nx, ny;
     int x_wall, y_wall;

@@ -168,6 +168,59 @@ def lap2d_gather(p, op):
     return lap.reshape(-1)
 
 
+def lap2d_lamb(p, op):
+    """The ``LAMB_BDRY`` branch of ``stencil_9pt_numba_test``: ``lap2D_numba_test``
+    (laplacian.py:531-543) with its padding ``periodic`` (:858-868) and the
+    ``kernel_9pt`` stencil (:749-856).
+
+    The inner nodes are padded by one node: x wraps with the duplicated seam
+    (column 0 <- column n-2, column n+1 <- column 1), then y mirrors (row 0 <- row
+    2, last <- third last); no cell coefficient is zeroed at a boundary.  With the
+    operands packed as :func:`pack_9pt` packs them (the reference's factory passes
+    the same arrays transposed), node (j, i) reads the cells (j, i), (j, i+1) below
+    it and (j+1, i), (j+1, i+1) above it, and y grows towards "top".  Same
+    operation order as ``kernel_9pt``.
+    """
+    nx, ny = op["nx"], op["ny"]
+    a = np.zeros((ny + 2, nx + 2))
+    a[1:-1, 1:-1] = np.asarray(p, dtype=np.float64).reshape(ny, nx)
+    a[:, 0] = a[:, -3]
+    a[:, -1] = a[:, 2]
+    a[0, :] = a[2, :]
+    a[-1, :] = a[-3, :]
+    c = slice(1, -1)
+    topleft, topmid, topright = a[2:, :-2], a[2:, c], a[2:, 2:]
+    midleft, midmid, midright = a[c, :-2], a[c, c], a[c, 2:]
+    botleft, botmid, botright = a[:-2, :-2], a[:-2, c], a[:-2, 2:]
+
+    def cells(flat):
+        q = np.asarray(flat, dtype=np.float64).reshape(ny + 1, nx + 1)
+        return q[1:, :-1], q[1:, 1:], q[:-1, :-1], q[:-1, 1:]         # tl, tr, bl, br
+    hpx_tl, hpx_tr, hpx_bl, hpx_br = cells(op["hplusx"])
+    hpy_tl, hpy_tr, hpy_bl, hpy_br = cells(op["hplusy"])
+    cxx, cyy, cxy, cyx = op["cor"]
+    cxx_tl, cxx_tr, cxx_bl, cxx_br = cells(cxx)
+    cyy_tl, cyy_tr, cyy_bl, cyy_br = cells(cyy)
+    cxy_tl, cxy_tr, cxy_bl, cxy_br = cells(cxy)
+    cyx_tl, cyx_tr, cyx_bl, cyx_br = cells(cyx)
+    oodx, oody = 1.0 / op["dx"], 1.0 / op["dy"]
+    Dx_tl = 0.5 * (topmid - topleft + midmid - midleft) * hpx_tl
+    Dx_tr = 0.5 * (topright - topmid + midright - midmid) * hpx_tr
+    Dx_bl = 0.5 * (botmid - botleft + midmid - midleft) * hpx_bl
+    Dx_br = 0.5 * (botright - botmid + midright - midmid) * hpx_br
+    Dy_tl = 0.5 * (topmid - midmid + topleft - midleft) * hpy_tl
+    Dy_tr = 0.5 * (topright - midright + topmid - midmid) * hpy_tr
+    Dy_bl = 0.5 * (midmid - botmid + midleft - botleft) * hpy_bl
+    Dy_br = 0.5 * (midright - botright + midmid - botmid) * hpy_br
+    Dxx = 0.5 * (cxx_tr * Dx_tr - cxx_tl * Dx_tl + cxx_br * Dx_br - cxx_bl * Dx_bl) * oodx * oodx
+    Dyy = 0.5 * (cyy_tr * Dy_tr - cyy_br * Dy_br + cyy_tl * Dy_tl - cyy_bl * Dy_bl) * oody * oody
+    Dyx = 0.5 * (cxy_br * Dy_br - cxy_bl * Dy_bl + cxy_tr * Dy_tr - cxy_tl * Dy_tl) * oody * oodx
+    Dxy = 0.5 * (cyx_tr * Dx_tr - cyx_br * Dx_br + cyx_tl * Dx_tl - cyx_bl * Dx_bl) * oodx * oody
+    hc = np.asarray(op["hcenter"], dtype=np.float64).reshape(ny, nx)
+    dinv = np.asarray(op["diag_inv"], dtype=np.float64).reshape(ny, nx)
+    return (((Dxx + Dyy + Dyx + Dxy) + hc * midmid) * dinv).reshape(-1)
+
+
 def precon_diag_prepare(wplus, wcenter, dx, dy, dz=None):
     """Approximate Jacobi diagonal, ``precon_diag_prepare`` (laplacian.py:1284-1356).
 

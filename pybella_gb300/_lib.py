@@ -17,6 +17,7 @@ BELLA_TIMEOUT = 4
 BELLA_EINVAL = -1
 BELLA_ECUDA = -2
 BELLA_ENOOP = -3
+BELLA_Y_MIRROR = 2      # bella_op2d.y_wall: the mirrored y boundary of the LAMB_BDRY stencil
 
 _dp = ctypes.c_void_p
 

@@ -670,6 +670,7 @@ static int check_members(bella_ws *const *ws, int nmem, const double *const *b, 
     for (int m = 0; m < nmem; ++m) {
         if (!ws[m] || !b[m] || !x[m]) return BELLA_EINVAL;
         if (ws[m]->ndim != 2) return BELLA_ENOOP;
+        if (ws[m]->ymirror) return BELLA_EINVAL;     // the batched stencil wraps y (no LAMB_BDRY mirror)
         if (ws[m]->device != ws[0]->device) return BELLA_EINVAL;
     }
     return BELLA_OK;

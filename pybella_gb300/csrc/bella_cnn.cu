@@ -195,19 +195,33 @@ constexpr size_t conv_smem() { return (size_t)27 * COUT * CIN * 2 + (size_t)CH_V
 // descriptor's LBO steps between the two chunks of a K=16 step, its SBO between
 // groups of 8 rows.  Rows on the padding ring are computed and discarded.
 // Work: a CTA takes runs of consecutive x-planes of one block of TC_ROWS padded
-// rows (TC_MB accumulators of 128 rows).  Consecutive planes share two of their
-// three input planes, so the staged planes live in a ring of five slots and
-// each output plane prefetches one new input plane two planes ahead (cp.async
-// groups) while the tensor cores work on the previous output plane.  The accumulators are double-buffered in tensor
-// memory, so the MMAs of plane k+1 run during the epilogue of plane k.  One
-// thread issues the MMAs and commits them to the mbarrier of their accumulator
-// set; its waits are bounded and on time-out the CTA records an error, waits
-// (bounded) for its other set, frees its tensor memory and returns.
+// rows (TC_MB accumulators of 128 rows); input plane p feeds output planes p+1,
+// p, p-1 (taps dx = -1, 0, 1), so consecutive planes share their inputs.
+//
+// The CTA is warp-specialised and its roles meet only on mbarriers, so the
+// tensor cores never wait for a block-wide barrier:
+//   * producer warps stage input planes into a ring of TC_SLOTS shared-memory
+//     slots with 16-byte asynchronous copies (source size 0 fills the padding),
+//     each waiting for its slot to be released by the MMAs that read it last;
+//   * one thread of the MMA warp issues each input plane's MMAs once the plane
+//     has landed and the accumulators it starts are free, then commits them to
+//     the plane's slot (freeing it) and to the output plane they complete;
+//   * epilogue warps (one per 32 tensor-memory lanes of each row block) take each
+//     completed output plane out of tensor memory, zero its columns, write it,
+//     and release the accumulators to the MMA thread.
+// Every wait is bounded (TC_SPIN_LIMIT polls): on time-out the CTA records an
+// error, every role leaves its loop, the MMA thread waits (bounded) for its
+// issued MMAs, and tensor memory is freed.
 constexpr int TC_MB = 2;                    // 128-row accumulators per output plane
 constexpr int TC_ROWS = 128 * TC_MB;
-constexpr int TC_SLOTS = 5;                 // ring of staged input planes: k-1 .. k+3
+constexpr int TC_SLOTS = 5;                 // ring of staged input planes
 constexpr long long TC_SPIN_LIMIT = 1LL << 24;
 constexpr size_t TC_SMEM_MAX = 225 * 1024;   // dynamic part; the kernel's static shared variables come on top
+constexpr int TC_EPI_WARPS = 4 * TC_MB;      // warps 0 .. 7: epilogue, row block w / 4, lanes 32 * (w % 4)
+constexpr int TC_PROD_WARPS = 2;             // warps 8, 9: producers
+constexpr int TC_MMA_WARP = TC_EPI_WARPS + TC_PROD_WARPS;   // warp 10: tensor memory and the MMAs
+constexpr int TC_THREADS = 32 * (TC_MMA_WARP + 1);
+constexpr int TC_LAG = 2;                    // copy groups a producer thread keeps in flight
 
 __device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
     uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
@@ -231,29 +245,64 @@ __host__ __device__ constexpr size_t tc_smem_bytes(int pz) {
     return (size_t)9 * (CIN / 8) * 3 * COUT * 16 + (size_t)TC_SLOTS * (CIN / 8) * (TC_ROWS + 2 * pz + 2) * 16;
 }
 
-__device__ __forceinline__ uint32_t tc_try_wait(uint32_t mbar, uint32_t parity) {
-    uint32_t done = 0;
-    for (long long it = 0; it < TC_SPIN_LIMIT && !done; ++it)
+// bounded wait for the completion of the mbarrier phase of the given parity;
+// gives up early when another role has set *abort
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity, volatile int *abort) {
+    for (long long it = 0; it < TC_SPIN_LIMIT; ++it) {
+        uint32_t done;
         asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
                      "selp.b32 %0, 1, 0, p;\n\t}" : "=r"(done) : "r"(mbar), "r"(parity));
-    return done;
+        if (done) return true;
+        if ((it & 255) == 255 && *abort) return false;
+    }
+    return false;
+}
+
+// the same wait for a whole warp: lane 0 polls, every lane gets the result
+__device__ __forceinline__ bool tc_wait_warp(uint32_t mbar, uint32_t parity, volatile int *abort) {
+    int ok = 0;
+    if ((threadIdx.x & 31) == 0) ok = tc_wait(mbar, parity, abort) ? 1 : 0;
+    return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
+
+__device__ __forceinline__ void tc_arrive(uint32_t mbar) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
+}
+
+// The run decomposition shared by all roles: run r covers padded-row block fb and
+// output x-planes [ia, ib); it reads input planes ia-1 .. ib.
+struct TcRun {
+    int fb, ia, ib;
+};
+__device__ __forceinline__ TcRun tc_run(int run, int nseg, int runlen, int nx) {
+    TcRun r;
+    r.fb = run / nseg;
+    const int seg = run - r.fb * nseg;
+    r.ia = seg * runlen;
+    r.ib = min(nx, r.ia + runlen);
+    return r;
 }
 
 // Input plane p feeds output planes p+1, p, p-1 through the weights of taps dx = 0, 1, 2:
 // with the three taps side by side in B (N = 96) one MMA per (dy, dz, K-step) serves
-// all three output planes.  Their accumulators live in a ring of TC_RING planes of 32
-// tensor-memory columns per row block, in descending plane order (plane q at column
-// 32 * (TC_RING - 1 - q % TC_RING)), so the three are adjacent unless the ring wraps
-// between them (then two MMAs, N = 32 and 64).  Every slot is zeroed after its
-// epilogue and every MMA accumulates.  Output planes outside the run or in another
-// sample's x-segment are left out of an MMA's column range.
+// all three output planes.  Output planes are numbered o = 0, 1, ... in the order the
+// CTA produces them; their accumulators live in a ring of TC_RING planes of COUT
+// tensor-memory columns per row block, in descending order (o at column
+// COUT * (TC_RING - 1 - o % TC_RING)), so the three are adjacent unless the ring wraps
+// between them (then two MMAs).  Every slot is zeroed by its epilogue and every MMA
+// accumulates.  Output planes outside the run or in another sample's x-segment are
+// left out of an MMA's column range.
 constexpr int TC_RING = 8;                   // accumulator planes per row block
 
 // COUT = 32: hidden layers, BF16 output with bias and optional ReLU.  COUT = 16 with
 // OUTF32: the output layer (8 channels padded to 16), FP32 output (acc + bias) *
 // out_scale of its first 8 channels.
 template <int CIN, int COUT, bool RELU, bool OUTF32>
-__global__ void __launch_bounds__(256, 1)
+__global__ void __launch_bounds__(TC_THREADS, 1)
 k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *__restrict__ in,
             const __nv_bfloat16 *__restrict__ Wtc, const float *__restrict__ bias, void *out, float out_scale,
             int *err) {
@@ -262,34 +311,42 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
     constexpr int NCH = CIN / 8;
     constexpr int NB = 3 * COUT;                          // B rows: the three dx taps
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ __align__(8) uint64_t bar_full[TC_SLOTS], bar_empty[TC_SLOTS], bar_acc[TC_RING], bar_free[TC_RING];
+    __shared__ __align__(8) uint64_t bar_done;
     __shared__ uint32_t tmem_slot;
-    __shared__ int ok_flag;
+    __shared__ int abort_flag;
+    volatile int *abort = &abort_flag;
     const int PZ = nz + 2, PY = ny + 2;
     const int L = TC_ROWS + 2 * PZ + 2;                   // staged rows per plane and chunk
     unsigned char *sW = smem;                             // [9][NCH][3*COUT][16 B]
     unsigned char *sA = smem + (size_t)9 * NCH * NB * 16; // [TC_SLOTS][NCH][L][16 B]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    for (int e = tid; e < 9 * NCH * NB; e += 256)
+    for (int e = tid; e < 9 * NCH * NB; e += TC_THREADS)
         reinterpret_cast<uint4 *>(sW)[e] = reinterpret_cast<const uint4 *>(Wtc)[e];
-    const uint32_t mbar_a0 = (uint32_t)__cvta_generic_to_shared(&mbar[0]);
-    const uint32_t mbar_a1 = (uint32_t)__cvta_generic_to_shared(&mbar[1]);
+    asm volatile("fence.proxy.async.shared::cta;");     // the weights are read by the tensor cores
+    auto sa = [](const void *p) { return (uint32_t)__cvta_generic_to_shared(p); };
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_a0));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_a1));
+        for (int k = 0; k < TC_SLOTS; ++k) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sa(&bar_full[k])), "r"(32 * TC_PROD_WARPS));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sa(&bar_empty[k])));
+        }
+        for (int k = 0; k < TC_RING; ++k) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sa(&bar_acc[k])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sa(&bar_free[k])), "r"(TC_EPI_WARPS));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sa(&bar_done)));
         asm volatile("fence.mbarrier_init.release.cluster;");
+        abort_flag = 0;
     }
-    if (warp == 0) {
-        const uint32_t slot = (uint32_t)__cvta_generic_to_shared(&tmem_slot);
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(TMEM_COLS));
+    if (warp == TC_MMA_WARP) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sa(&tmem_slot)),
+                     "r"(TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_slot;
-    // warp w owns lanes 32*(w%4).. of row block w/4: zero its whole accumulator ring
-    const uint32_t tlane = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)((warp >> 2) * TC_RING * COUT);
     auto zero_cols = [&](uint32_t taddr) {
         const uint32_t z = 0u;
         if (COUT == 32)
@@ -300,138 +357,167 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
             asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
                          "{%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr), "r"(z));
     };
-    for (int q = 0; q < TC_RING; ++q) zero_cols(tlane + (uint32_t)(q * COUT));
-    asm volatile("tcgen05.wait::st.sync.aligned;");
+    // epilogue warp w owns lanes 32*(w%4) of row block w/4: zero its accumulator ring
+    const uint32_t tlane = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)((warp >> 2) * TC_RING * COUT);
+    if (warp < TC_EPI_WARPS) {
+        for (int q = 0; q < TC_RING; ++q) zero_cols(tlane + (uint32_t)(q * COUT));
+        asm volatile("tcgen05.wait::st.sync.aligned;");
+    }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
-    const uint32_t sW_a = (uint32_t)__cvta_generic_to_shared(sW), sA_a = (uint32_t)__cvta_generic_to_shared(sA);
-    const uint64_t a0 = tc_sdesc(sA_a, (uint32_t)L * 16, 128), b0 = tc_sdesc(sW_a, NB * 16, 128);
 
     const int plane = PY * PZ;
     const int nblk = (plane + TC_ROWS - 1) / TC_ROWS;
     const int nseg = (nx + runlen - 1) / runlen;
     const int nruns = nblk * nseg;
-    uint32_t phase[2] = {0u, 0u};
-    int committed[2] = {0, 0};              // commits not yet waited for, per mbarrier (thread 0)
-    bool failed = false;
+    const uint32_t sW_a = sa(sW), sA_a = sa(sA);
 
-    for (int run = blockIdx.x; run < nruns && !failed; run += gridDim.x) {
-        const int fb = run / nseg, seg = run - fb * nseg;
-        const int ia = seg * runlen, ib = min(nx, ia + runlen);
-        const int f0 = fb * TC_ROWS - (PZ + 1);           // padded row of staged row 0
-        // stage input plane p into ring slot p % TC_SLOTS with 16-byte asynchronous copies
-        // (source size 0 fills the zero padding); a run reads planes ia-1 .. ib
-        auto stage = [&](int p) {
-            if (p < 0 || p >= nx || p < ia - 1 || p > ib) return;
-            const uint32_t base = sA_a + (uint32_t)((size_t)(p % TC_SLOTS) * NCH * L * 16);
-            for (int rb = tid; rb < L; rb += 256) {
-                const int f = f0 + rb;
-                const __nv_bfloat16 *src = in;
-                uint32_t bytes = 0;
-                if (f >= 0 && f < plane) {
-                    const int yq = f / PZ;
-                    const int y = yq - 1, z = f - yq * PZ - 1;
-                    if (y >= 0 && y < ny && z >= 0 && z < nz) {
-                        src = in + (((size_t)p * ny + y) * nz + z) * CIN;
-                        bytes = 16;
+    if (warp >= TC_EPI_WARPS && warp < TC_MMA_WARP) {
+        // ---------------- producers: input planes into the slot ring ----------------
+        const int ptid = tid - 32 * TC_EPI_WARPS;
+        long long i = 0;                                  // input planes staged so far (this CTA)
+        bool ok = true;
+        for (int run = blockIdx.x; run < nruns && ok; run += gridDim.x) {
+            const TcRun R = tc_run(run, nseg, runlen, nx);
+            const int f0 = R.fb * TC_ROWS - (PZ + 1);     // padded row of staged row 0
+            for (int p = R.ia - 1; p <= R.ib && ok; ++p, ++i) {
+                const int slot = (int)(i % TC_SLOTS);
+                if (i >= TC_SLOTS &&
+                    !tc_wait_warp(sa(&bar_empty[slot]), (uint32_t)((i / TC_SLOTS - 1) & 1), abort)) {
+                    ok = false;
+                    break;
+                }
+                if (p >= 0 && p < nx) {
+                    const uint32_t base = sA_a + (uint32_t)((size_t)slot * NCH * L * 16);
+                    for (int rb = ptid; rb < L; rb += 32 * TC_PROD_WARPS) {
+                        const int f = f0 + rb;
+                        const __nv_bfloat16 *src = in;
+                        uint32_t bytes = 0;
+                        if (f >= 0 && f < plane) {
+                            const int yq = f / PZ;
+                            const int y = yq - 1, z = f - yq * PZ - 1;
+                            if (y >= 0 && y < ny && z >= 0 && z < nz) {
+                                src = in + (((size_t)p * ny + y) * nz + z) * CIN;
+                                bytes = 16;
+                            }
+                        }
+#pragma unroll
+                        for (int ch = 0; ch < NCH; ++ch)
+                            asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
+                                         ::"r"(base + (uint32_t)((ch * L + rb) * 16)), "l"(src + (bytes ? ch * 8 : 0)),
+                                           "r"(bytes));
                     }
                 }
-#pragma unroll
-                for (int ch = 0; ch < NCH; ++ch)
-                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
-                                 ::"r"(base + (uint32_t)((ch * L + rb) * 16)), "l"(src + (bytes ? ch * 8 : 0)),
-                                   "r"(bytes));
+                asm volatile("cp.async.commit_group;");
+                if (i >= TC_LAG) {                        // plane i - TC_LAG has landed
+                    asm volatile("cp.async.wait_group %0;" ::"n"(TC_LAG));
+                    asm volatile("fence.proxy.async.shared::cta;");
+                    tc_arrive(sa(&bar_full[(i - TC_LAG) % TC_SLOTS]));
+                }
             }
-        };
-        // thread 0: the MMAs of input plane p into output planes qlo..qhi (descending
-        // columns from qhi), then one commit to mbarrier p & 1 (also when p has no MMAs)
-        auto mma_range = [&](int p, int qhi, int qlo) {
-            const int n = qhi - qlo + 1;                      // 1..3 output planes
-            const uint32_t col = (uint32_t)(COUT * (TC_RING - 1 - qhi % TC_RING));
-            const int d0 = p + 1 - qhi;                       // dx tap of plane qhi
-            const uint32_t idesc = tc_idesc_n(n * COUT);
-            const uint64_t abase = a0 + (uint64_t)((p % TC_SLOTS) * NCH * L + PZ + 1);
+        }
+        asm volatile("cp.async.wait_group 0;");
+        asm volatile("fence.proxy.async.shared::cta;");
+        if (ok)
+            for (long long j = (i > TC_LAG ? i - TC_LAG : 0); j < i; ++j) tc_arrive(sa(&bar_full[j % TC_SLOTS]));
+        else if (ptid == 0) {
+            atomicExch(err, 1);
+            *abort = 1;
+        }
+    } else if (warp == TC_MMA_WARP) {
+        // ---------------- one thread issues the MMAs ----------------
+        if (lane == 0) {
+            const uint64_t a0 = tc_sdesc(sA_a, (uint32_t)L * 16, 128), b0 = tc_sdesc(sW_a, NB * 16, 128);
+            long long i = 0, obase = 0, acq = 0;
+            bool ok = true;
+            // the MMAs of input plane p (ring slot `slot`) into output planes ohi .. olo,
+            // descending columns from ohi; plane ohi uses the dx tap d0
+            auto mma_range = [&](int slot, long long ohi, long long olo, int d0) {
+                const int n = (int)(ohi - olo + 1);       // 1..3 output planes
+                const uint32_t col = (uint32_t)(COUT * (TC_RING - 1 - (int)(ohi % TC_RING)));
+                const uint32_t idesc = tc_idesc_n(n * COUT);
+                const uint64_t abase = a0 + (uint64_t)(slot * NCH * L + PZ + 1);
 #pragma unroll
-            for (int mb = 0; mb < TC_MB; ++mb) {
-                const uint32_t dtm = tmem + (uint32_t)(mb * TC_RING * COUT) + col;
+                for (int mb = 0; mb < TC_MB; ++mb) {
+                    const uint32_t dtm = tmem + (uint32_t)(mb * TC_RING * COUT) + col;
 #pragma unroll
-                for (int dyi = 0; dyi < 3; ++dyi) {
+                    for (int dyi = 0; dyi < 3; ++dyi) {
 #pragma unroll
-                    for (int dzi = 0; dzi < 3; ++dzi) {
-                        const int t9 = dyi * 3 + dzi;
+                        for (int dzi = 0; dzi < 3; ++dzi) {
+                            const int t9 = dyi * 3 + dzi;
 #pragma unroll
-                        for (int ks = 0; ks < CIN / 16; ++ks) {
-                            const uint64_t ad = abase + (uint64_t)(mb * 128 + 2 * ks * L + (dyi - 1) * PZ + (dzi - 1));
-                            const uint64_t bd = b0 + (uint64_t)((t9 * NCH + 2 * ks) * NB + COUT * d0);
-                            asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                                         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                                         ::"r"(dtm), "l"(ad), "l"(bd), "r"(idesc), "r"(1));
+                            for (int ks = 0; ks < CIN / 16; ++ks) {
+                                const uint64_t ad =
+                                    abase + (uint64_t)(mb * 128 + 2 * ks * L + (dyi - 1) * PZ + (dzi - 1));
+                                const uint64_t bd = b0 + (uint64_t)((t9 * NCH + 2 * ks) * NB + COUT * d0);
+                                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                                             ::"r"(dtm), "l"(ad), "l"(bd), "r"(idesc), "r"(1));
+                            }
                         }
                     }
                 }
-            }
-        };
-        auto issue = [&](int p) {
-            if (p >= 0 && p < nx) {
-                const int s0 = (p / xseg) * xseg;             // this sample's x-segment
-                const int qlo = max(max(p - 1, ia), s0), qhi = min(min(p + 1, ib - 1), s0 + xseg - 1);
-                if (qlo <= qhi) {
-                    const int cut = (qhi / TC_RING) * TC_RING;    // ring boundary below qhi
-                    if (qlo >= cut) {
-                        mma_range(p, qhi, qlo);
-                    } else {
-                        mma_range(p, qhi, cut);
-                        mma_range(p, cut - 1, qlo);
+            };
+            for (int run = blockIdx.x; run < nruns && ok; run += gridDim.x) {
+                const TcRun R = tc_run(run, nseg, runlen, nx);
+                for (int p = R.ia - 1; p <= R.ib; ++p, ++i) {
+                    const int slot = (int)(i % TC_SLOTS);
+                    if (!tc_wait(sa(&bar_full[slot]), (uint32_t)((i / TC_SLOTS) & 1), abort)) {
+                        ok = false;
+                        break;
                     }
+                    asm volatile("fence.proxy.async.shared::cta;");
+                    if (p >= 0 && p < nx) {
+                        const int s0 = (p / xseg) * xseg;     // this sample's x-segment
+                        const int qlo = max(max(p - 1, R.ia), s0), qhi = min(min(p + 1, R.ib - 1), s0 + xseg - 1);
+                        if (qlo <= qhi) {
+                            const long long olo = obase + (qlo - R.ia), ohi = obase + (qhi - R.ia);
+                            for (; acq <= ohi && ok; ++acq)   // accumulators of ohi free again?
+                                if (acq >= TC_RING &&
+                                    !tc_wait(sa(&bar_free[acq % TC_RING]), (uint32_t)((acq / TC_RING - 1) & 1), abort))
+                                    ok = false;
+                            if (!ok) break;
+                            asm volatile("tcgen05.fence::after_thread_sync;");
+                            const int d0 = p + 1 - qhi;           // dx tap of plane qhi
+                            const long long cut = (ohi / TC_RING) * TC_RING;   // ring boundary below ohi
+                            if (olo >= cut) {
+                                mma_range(slot, ohi, olo, d0);
+                            } else {
+                                mma_range(slot, ohi, cut, d0);
+                                mma_range(slot, cut - 1, olo, d0 + (int)(ohi - cut) + 1);
+                            }
+                        }
+                    }
+                    tc_commit(sa(&bar_empty[slot]));          // the slot is free once these MMAs are done
+                    const int q = p - 1;                      // output plane complete after input plane p
+                    if (q >= R.ia && q < R.ib) tc_commit(sa(&bar_acc[(obase + q - R.ia) % TC_RING]));
                 }
+                obase += R.ib - R.ia;
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                         ::"r"((p & 1) ? mbar_a1 : mbar_a0));
-            committed[p & 1] += 1;
-        };
-        // Pipeline over input planes p = ia-1 .. ib: plane p+1's MMAs are issued before
-        // plane p's are waited for; output plane p-1 is complete once plane p's MMAs are
-        // (MMAs of one thread complete in order), and its epilogue then runs while plane
-        // p+1's MMAs are on the tensor cores.  Input plane p's ring slot is free after
-        // its own MMAs: plane p+5 is staged into it.  One cp.async group per plane.
-        for (int p = ia - 1; p <= ia + 3; ++p) {
-            stage(p);
-            asm volatile("cp.async.commit_group;");
+            if (!ok) {
+                atomicExch(err, 1);
+                *abort = 1;
+            }
+            tc_commit(sa(&bar_done));                         // every MMA issued above has completed
+            int never = 0;                                    // (this wait does not give up on an abort)
+            if (!tc_wait(sa(&bar_done), 0u, &never)) atomicExch(err, 1);
         }
-        asm volatile("cp.async.wait_group 4;");          // plane ia-1 has landed
-        asm volatile("fence.proxy.async.shared::cta;");
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        if (tid == 0) issue(ia - 1);
-        for (int p = ia - 1; p <= ib; ++p) {
-            asm volatile("cp.async.wait_group 3;");      // plane p+1 has landed
-            asm volatile("fence.proxy.async.shared::cta;");
-            asm volatile("tcgen05.fence::before_thread_sync;");
-            __syncthreads();                             // also: the last epilogue's zeroing is done
-            asm volatile("tcgen05.fence::after_thread_sync;");
-            if (tid == 0) {
-                if (p + 1 <= ib) issue(p + 1);
-                const int b = p & 1;
-                const uint32_t done = tc_try_wait(b ? mbar_a1 : mbar_a0, phase[b]);
-                if (done) committed[b] -= 1;
-                ok_flag = done ? 1 : 0;
-            }
-            __syncthreads();
-            if (!ok_flag) {                  // the phase of this barrier stays at the unfinished commit
-                if (tid == 0) atomicExch(err, 1);
-                failed = true;
-                break;
-            }
-            phase[p & 1] ^= 1u;
-            asm volatile("tcgen05.fence::after_thread_sync;");
-            stage(p + 5);                    // ring slot of plane p: read only by plane p's MMAs
-            asm volatile("cp.async.commit_group;");
-            const int q = p - 1;             // output plane complete after input plane p
-            if (q >= ia && q < ib) {
-                const int mb = warp >> 2;
-                const uint32_t taddr = tlane + (uint32_t)(COUT * (TC_RING - 1 - q % TC_RING));
+        __syncwarp();
+    } else {
+        // ---------------- epilogue warps ----------------
+        const int mb = warp >> 2;
+        long long o = 0;
+        bool ok = true;
+        for (int run = blockIdx.x; run < nruns && ok; run += gridDim.x) {
+            const TcRun R = tc_run(run, nseg, runlen, nx);
+            for (int q = R.ia; q < R.ib; ++q, ++o) {
+                if (!tc_wait_warp(sa(&bar_acc[o % TC_RING]), (uint32_t)((o / TC_RING) & 1), abort)) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t taddr = tlane + (uint32_t)(COUT * (TC_RING - 1 - (int)(o % TC_RING)));
                 uint32_t r[32];
                 if (COUT == 32)
                     asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
@@ -452,21 +538,21 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
                                    "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
                                  : "r"(taddr));
                 asm volatile("tcgen05.wait::ld.sync.aligned;");
-                zero_cols(taddr);            // the slot's next plane accumulates from zero
-                const int f = fb * TC_ROWS + mb * 128 + (warp & 3) * 32 + lane;
+                zero_cols(taddr);                           // the slot's next plane accumulates from zero
+                const int f = R.fb * TC_ROWS + mb * 128 + (warp & 3) * 32 + lane;
                 if (f < plane) {
                     const int yq = f / PZ;
                     const int y = yq - 1, z = f - yq * PZ - 1;
                     if (y >= 0 && y < ny && z >= 0 && z < nz) {
                         const size_t g = ((size_t)q * ny + y) * nz + z;
-                        if (OUTF32) {                // the output layer's 8 real channels
+                        if (OUTF32) {                        // the output layer's 8 real channels
                             float v[8];
 #pragma unroll
                             for (int c = 0; c < 8; ++c)
                                 v[c] = (__uint_as_float(r[c]) + (bias ? bias[c] : 0.f)) * out_scale;
-                            float4 *o = reinterpret_cast<float4 *>(reinterpret_cast<float *>(out) + g * 8);
-                            o[0] = make_float4(v[0], v[1], v[2], v[3]);
-                            o[1] = make_float4(v[4], v[5], v[6], v[7]);
+                            float4 *ov = reinterpret_cast<float4 *>(reinterpret_cast<float *>(out) + g * 8);
+                            ov[0] = make_float4(v[0], v[1], v[2], v[3]);
+                            ov[1] = make_float4(v[4], v[5], v[6], v[7]);
                         } else {
                             uint32_t w[16];
 #pragma unroll
@@ -477,34 +563,30 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
                                 const __nv_bfloat162 h2 = __floats2bfloat162_rn(v0, v1);
                                 w[c] = *reinterpret_cast<const uint32_t *>(&h2);
                             }
-                            uint4 *o = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(out) + g * COUT);
-                            o[0] = make_uint4(w[0], w[1], w[2], w[3]);
-                            o[1] = make_uint4(w[4], w[5], w[6], w[7]);
-                            o[2] = make_uint4(w[8], w[9], w[10], w[11]);
-                            o[3] = make_uint4(w[12], w[13], w[14], w[15]);
+                            uint4 *ov = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(out) + g * COUT);
+                            ov[0] = make_uint4(w[0], w[1], w[2], w[3]);
+                            ov[1] = make_uint4(w[4], w[5], w[6], w[7]);
+                            ov[2] = make_uint4(w[8], w[9], w[10], w[11]);
+                            ov[3] = make_uint4(w[12], w[13], w[14], w[15]);
                         }
                     }
                 }
                 asm volatile("tcgen05.wait::st.sync.aligned;");
+                asm volatile("tcgen05.fence::before_thread_sync;");
+                __syncwarp();
+                if (lane == 0) tc_arrive(sa(&bar_free[o % TC_RING]));
             }
-            asm volatile("tcgen05.fence::before_thread_sync;");
         }
-        asm volatile("cp.async.wait_group 0;");          // no copy of this run outlives it
-        __syncthreads();
+        if (!ok && lane == 0) {
+            atomicExch(err, 1);
+            *abort = 1;
+        }
     }
-    // after a time-out, commits that were issued but not waited for may still be in
-    // flight: wait for them (bounded) before freeing tensor memory
-    if (failed && tid == 0) {
-        for (int b = 0; b < 2; ++b)
-            for (int c = 0; c < committed[b]; ++c) {
-                tc_try_wait(b ? mbar_a1 : mbar_a0, phase[b]);
-                phase[b] ^= 1u;
-            }
-    }
-    asm volatile("cp.async.wait_group 0;");
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (warp == TC_MMA_WARP)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
 }
 
 // kernel weights [27][COUTP][CINP] (tap = (dx+1)*9 + (dy+1)*3 + (dz+1)) -> tensor-core
@@ -989,20 +1071,20 @@ static void forward_layers(bella_cnn *net, const BlockMap &m, float out_scale, c
         const int gt = tc_grid(nruns), pz = nz + 2;
         const float *b5 = net->linear ? nullptr : net->bias[5];
         if (net->linear) {
-            k_conv3d_tc<16, 32, false, false><<<gt, 256, tc_smem_bytes<16, 32>(pz), s>>>(
+            k_conv3d_tc<16, 32, false, false><<<gt, TC_THREADS, tc_smem_bytes<16, 32>(pz), s>>>(
                 nx, ny, nz, xs, runlen, net->act[0], net->wtc[0], nullptr, net->act[1], 1.f, net->tc_err);
             for (int l = 1; l <= 4; ++l)
-                k_conv3d_tc<32, 32, false, false><<<gt, 256, tc_smem_bytes<32, 32>(pz), s>>>(
+                k_conv3d_tc<32, 32, false, false><<<gt, TC_THREADS, tc_smem_bytes<32, 32>(pz), s>>>(
                     nx, ny, nz, xs, runlen, net->act[l], net->wtc[l], nullptr, net->act[l + 1], 1.f, net->tc_err);
         } else {
-            k_conv3d_tc<16, 32, true, false><<<gt, 256, tc_smem_bytes<16, 32>(pz), s>>>(
+            k_conv3d_tc<16, 32, true, false><<<gt, TC_THREADS, tc_smem_bytes<16, 32>(pz), s>>>(
                 nx, ny, nz, xs, runlen, net->act[0], net->wtc[0], net->bias[0], net->act[1], 1.f, net->tc_err);
             for (int l = 1; l <= 4; ++l)
-                k_conv3d_tc<32, 32, true, false><<<gt, 256, tc_smem_bytes<32, 32>(pz), s>>>(
+                k_conv3d_tc<32, 32, true, false><<<gt, TC_THREADS, tc_smem_bytes<32, 32>(pz), s>>>(
                     nx, ny, nz, xs, runlen, net->act[l], net->wtc[l], net->bias[l], net->act[l + 1], 1.f,
                     net->tc_err);
         }
-        k_conv3d_tc<32, 16, false, true><<<gt, 256, tc_smem_bytes<32, 16>(pz), s>>>(
+        k_conv3d_tc<32, 16, false, true><<<gt, TC_THREADS, tc_smem_bytes<32, 16>(pz), s>>>(
             nx, ny, nz, xs, runlen, net->act[5], net->wtc[5], b5, net->y8, out_scale, net->tc_err);
         net->launches += 6;
         return;

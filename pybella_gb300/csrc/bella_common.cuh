@@ -206,6 +206,7 @@ __device__ __forceinline__ bool grid_sum(double (&v)[Q], double *partials, unsig
 template <typename T>
 struct Op2D {
     int nx, ny;
+    int ymirror;              // y boundary of the LAMB_BDRY stencil: node -1 <- node 1, node ny <- node ny-2
     const T *axx, *ayy, *axy, *ayx;
     const T *dinv, *hc;
 };
@@ -222,6 +223,7 @@ struct bella_ws {
     int nx, ny, nz;
     long long n;              // unknowns
     int cross, has_hc, singular;
+    int ymirror;              // 2D operator with the mirrored y boundary (bella_op2d.y_wall == BELLA_Y_MIRROR)
     double *a64;              // 4 cell planes
     float  *a32;
     double *dinv64, *hc64, *z64;

@@ -524,6 +524,10 @@ int bella_op2d_set(bella_ws *ws, const bella_op2d *op, void *stream) {
     if (!op->hplusx || !op->hplusy || !op->cxx || !op->cyy || !op->diag_inv)
         return set_err(BELLA_EINVAL, "bella_op2d_set: hplusx, hplusy, cxx, cyy, diag_inv are required");
     if (!(op->dx > 0.0) || !(op->dy > 0.0)) return set_err(BELLA_EINVAL, "bella_op2d_set: dx, dy must be > 0");
+    if (op->x_wall < 0 || op->x_wall > 1 || op->y_wall < 0 || op->y_wall > BELLA_Y_MIRROR)
+        return set_err(BELLA_EINVAL, "bella_op2d_set: x_wall must be 0 or 1, y_wall 0, 1 or BELLA_Y_MIRROR");
+    if (op->y_wall == BELLA_Y_MIRROR && op->x_wall)
+        return set_err(BELLA_EINVAL, "bella_op2d_set: the mirrored y boundary (LAMB_BDRY) has a periodic x axis");
     BELLA_CUDA(cudaSetDevice(ws->device));
     cudaStream_t s = (cudaStream_t)stream;
     const long long n = (long long)op->nx * op->ny;
@@ -550,12 +554,14 @@ int bella_op2d_set(bella_ws *ws, const bella_op2d *op, void *stream) {
     ws->n = n;
     ws->cross = (op->cxy != nullptr || op->cyx != nullptr) ? 1 : 0;
     ws->has_hc = op->hcenter != nullptr ? 1 : 0;
-    ws->singular = (!ws->has_hc && !ws->cross) ? 1 : 0;
+    ws->ymirror = op->y_wall == BELLA_Y_MIRROR ? 1 : 0;
+    // the null space projection is that of the wrapped/walled operator: not applied with the mirror
+    ws->singular = (!ws->has_hc && !ws->cross && !ws->ymirror) ? 1 : 0;
     ws->grid_stencil = stencil_grid(op->nx, op->ny);
     ws->grid_vec = vec_grid(n);
     rc = op2d_pack(ws, op, s);
     if (rc != BELLA_OK) return cuda_check(cudaGetLastError(), "op2d_pack");
-    rc = setup_null_space(ws, s, op->x_wall ? 0 : 1, op->y_wall ? 0 : 1, 0);
+    rc = setup_null_space(ws, s, op->x_wall ? 0 : 1, op->y_wall == 0 ? 1 : 0, 0);
     if (rc != BELLA_OK) return rc;
     return BELLA_OK;
 }
@@ -591,6 +597,7 @@ int bella_op3d_set(bella_ws *ws, const bella_op3d *op, void *stream) {
     ws->n = n;
     ws->cross = op->corrf != 0.0 ? 1 : 0;
     ws->has_hc = op->hcenter != nullptr ? 1 : 0;
+    ws->ymirror = 0;
     ws->singular = (!ws->has_hc && !ws->cross) ? 1 : 0;
     ws->grid_stencil = stencil3d_grid(op->nx, op->ny, op->nz);
     ws->grid_vec = vec_grid(n);
@@ -1606,6 +1613,8 @@ extern "C" int bella_bicgstab2d_noalloc(const bella_op2d *op, const double *b, d
                                      "(at most 65536 nodes and 131072 cells); use bella_bicgstab");
     if (!op->hplusx || !op->hplusy || !op->cxx || !op->cyy || !op->diag_inv)
         return set_err(BELLA_EINVAL, "bella_bicgstab2d_noalloc: hplusx, hplusy, cxx, cyy, diag_inv are required");
+    if (op->x_wall < 0 || op->x_wall > 1 || op->y_wall < 0 || op->y_wall > 1)
+        return set_err(BELLA_EINVAL, "bella_bicgstab2d_noalloc: x_wall, y_wall must be 0 or 1");
     if (!(op->dx > 0.0) || !(op->dy > 0.0)) return set_err(BELLA_EINVAL, "bella_bicgstab2d_noalloc: dx, dy must be > 0");
     bella_solve_opts o;
     if (opts) {

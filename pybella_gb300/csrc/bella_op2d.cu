@@ -13,6 +13,9 @@
 // diag_inv (laplacian.py:721-739); 9 additions per node instead of 13.  Walls are folded into the cell planes
 // (zeroed outer cell column/row, laplacian.py:691-713); the periodic wrap
 // with the duplicated seam (laplacian.py:595-638) is done on the halo load.
+// The LAMB_BDRY variant (lap2D_numba_test with its padding and the kernel_9pt
+// stencil, laplacian.py:531-543, 749-868) is the same operator on the same cell
+// planes with a mirrored y boundary on the halo load and no cell zeroed.
 //
 // A CTA owns a 64x16 node tile: it stages the tile plus a one-node halo of
 // the stencil input u in shared memory (computing u on the fly from the
@@ -46,7 +49,7 @@ __global__ void k_pack2d_cells(bella_op2d op, double *a64, float *a32, dfloat *a
         double hx = op.hplusx[c], hy = op.hplusy[c];
         // wall handling: the outer cell column/row never couples (laplacian.py:691-713)
         if (op.x_wall && (ci == 0 || ci == nx)) { hx = 0.0; hy = 0.0; }
-        if (op.y_wall && (cj == 0 || cj == ny)) { hx = 0.0; hy = 0.0; }
+        if (op.y_wall == 1 && (cj == 0 || cj == ny)) { hx = 0.0; hy = 0.0; }   // not for the mirror (2)
         const double axx = 0.5 * oodx * oodx * op.cxx[c] * hx;
         const double ayy = 0.5 * oody * oody * op.cyy[c] * hy;
         const double axy = cross ? 0.5 * oodx * oody * (op.cxy ? op.cxy[c] : 0.0) * hy : 0.0;
@@ -78,7 +81,7 @@ __global__ void k_pack2d_nodes(bella_op2d op, double *dinv64, float *dinv32, dou
         if (dinvdf) { dinvdf[g] = dfloat(d); hcdf[g] = dfloat(h); }
         double w = 1.0;
         if (!op.x_wall && (i == 0 || i == nx - 1)) w *= 0.5;
-        if (!op.y_wall && (j == 0 || j == ny - 1)) w *= 0.5;
+        if (op.y_wall == 0 && (j == 0 || j == ny - 1)) w *= 0.5;
         z64[g] = w / d;
     }
 }
@@ -127,7 +130,8 @@ k_stencil2d(Op2D<T> op, StArgs<T> a, KState *ks, double *partials, unsigned *cou
         for (int e = tid; e < (TY + 2) * (TX + 2); e += NTHREADS) {
             const int la = e / (TX + 2), lb = e - la * (TX + 2);
             int gj = j0 - 1 + la, gi = i0 - 1 + lb;
-            if (gj < 0) gj += ny - 1; else if (gj == ny) gj = 1;
+            if (gj < 0) gj = op.ymirror ? 1 : gj + ny - 1;          // mirror (LAMB_BDRY) or wrap
+            else if (gj == ny) gj = op.ymirror ? ny - 2 : 1;
             if (gi < 0) gi += nx - 1; else if (gi == nx) gi = 1;
             T u = 0;
             if (gj < ny && gi < nx) {
@@ -225,7 +229,7 @@ template <>
 Op2D<double> make_op<double>(bella_ws *ws) {
     const size_t nc = (size_t)(ws->nx + 1) * (ws->ny + 1);
     Op2D<double> o;
-    o.nx = ws->nx; o.ny = ws->ny;
+    o.nx = ws->nx; o.ny = ws->ny; o.ymirror = ws->ymirror;
     o.axx = ws->a64; o.ayy = ws->a64 + nc; o.axy = ws->a64 + 2 * nc; o.ayx = ws->a64 + 3 * nc;
     o.dinv = ws->dinv64; o.hc = ws->hc64;
     return o;
@@ -235,7 +239,7 @@ template <>
 Op2D<dfloat> make_op<dfloat>(bella_ws *ws) {
     const size_t nc = (size_t)(ws->nx + 1) * (ws->ny + 1);
     Op2D<dfloat> o;
-    o.nx = ws->nx; o.ny = ws->ny;
+    o.nx = ws->nx; o.ny = ws->ny; o.ymirror = ws->ymirror;
     o.axx = ws->adf; o.ayy = ws->adf + nc; o.axy = ws->adf + 2 * nc; o.ayx = ws->adf + 3 * nc;
     o.dinv = ws->dinvdf; o.hc = ws->hcdf;
     return o;
@@ -245,7 +249,7 @@ template <>
 Op2D<float> make_op<float>(bella_ws *ws) {
     const size_t nc = (size_t)(ws->nx + 1) * (ws->ny + 1);
     Op2D<float> o;
-    o.nx = ws->nx; o.ny = ws->ny;
+    o.nx = ws->nx; o.ny = ws->ny; o.ymirror = ws->ymirror;
     o.axx = ws->a32; o.ayy = ws->a32 + nc; o.axy = ws->a32 + 2 * nc; o.ayx = ws->a32 + 3 * nc;
     o.dinv = ws->dinv32; o.hc = ws->hc32;
     return o;

@@ -881,7 +881,7 @@ int bella_spectral2d_create(bella_spectral3d **out, const bella_op2d *op, int de
     *out = nullptr;
     if (op->nx < 3 || op->ny < 3 || !op->hplusx || !op->hplusy || !op->cxx || !op->cyy || !op->diag_inv)
         return BELLA_EINVAL;
-    if (!op->y_wall) return BELLA_EINVAL;     // the line solves run along a walled y axis
+    if (op->y_wall != 1) return BELLA_EINVAL;   // the line solves run along a walled y axis (no mirror)
     if (!(op->dx > 0.0) || !(op->dy > 0.0)) return BELLA_EINVAL;
     if (cudaSetDevice(device) != cudaSuccess) return BELLA_ECUDA;
     cudaStream_t s = (cudaStream_t)stream;

@@ -188,10 +188,13 @@ class NodalHelmholtz2D(_NodalOperator):
     ``(ny+1)*(nx+1)`` cells, ``hcenter`` and ``diag_inv`` on ``ny*nx`` nodes,
     all flattened y-major.  NumPy or torch inputs are accepted; they are copied
     once to the GPU and packed into flux planes (FP64, FP32, double-float).
+    ``y_mirror=True`` gives the operator of the reference's ``LAMB_BDRY``
+    branch (laplacian.py:531-543, 749-868): x periodic, y padded by mirroring,
+    no cell zeroed.
     """
 
     def __init__(self, hplusx, hplusy, hcenter, coriolis, diag_inv, nx, ny, dx, dy,
-                 x_wall, y_wall, device=None, ws=None):
+                 x_wall, y_wall, device=None, ws=None, y_mirror=False):
         self.dev = _device(device) if ws is None else torch.device("cuda", ws.device)
         self.nx, self.ny = int(nx), int(ny)
         self.n = self.nx * self.ny
@@ -212,9 +215,12 @@ class NodalHelmholtz2D(_NodalOperator):
                            (self._cyy, nc, "cyy"), (self._dinv, self.n, "diag_inv")):
             if t.numel() != m:
                 raise ValueError("%s has %d entries, expected %d" % (name, t.numel(), m))
-        self.singular = self._hc is None and self._cxy is None
+        if y_mirror and x_wall:
+            raise ValueError("the mirrored y boundary (LAMB_BDRY) goes with a periodic x axis")
+        self.singular = self._hc is None and self._cxy is None and not y_mirror
         self.ws = _lib.Workspace(d.index) if ws is None else ws
-        self._op = _lib.Op2D(self.nx, self.ny, int(bool(x_wall)), int(bool(y_wall)), float(dx), float(dy),
+        yb = _lib.BELLA_Y_MIRROR if y_mirror else int(bool(y_wall))
+        self._op = _lib.Op2D(self.nx, self.ny, int(bool(x_wall)), yb, float(dx), float(dy),
                              _ptr(self._hx), _ptr(self._hy), _ptr(self._hc), _ptr(self._cxx),
                              _ptr(self._cyy), _ptr(self._cxy), _ptr(self._cyx), _ptr(self._dinv))
         with torch.cuda.device(d):

@@ -27,6 +27,12 @@ It imports the reference through ``refshim`` (numba, h5py, ... stubbed; SciPy
 * ``step_kat.npz``    -- the whole time step (``time_update.do``) of the 64x32
   rising bubble, after one and two steps and a run to tout;
 * ``diag_kat.npz``    -- ``precon_diag_prepare`` (laplacian.py:1284-1356);
+* ``stencil_kat.npz`` -- the operator factory ``stencil_9pt_numba_test``
+  (laplacian.py:496-528) called with the reference's own grid and MPV objects
+  on random operands, and its closure applied to a random vector: the
+  ``lap2D_gather_new`` branch (periodic x, wall y; with and without Coriolis
+  cross terms) and the ``LAMB_BDRY`` branch (``lap2D_numba_test`` with the
+  ``kernel_9pt`` stencil, laplacian.py:531-543, 749-868);
 * ``pieces_kat.npz``  -- ``divergence_nodes``, ``correction_nodes``,
   ``set_ghostnodes_p2`` and ``set_explicit_boundary_data`` on a random state;
 * ``explicit_kat.npz`` -- ``euler_forward_non_advective`` and
@@ -625,13 +631,52 @@ def rising_bubble_step0(out):
     np.savez_compressed(os.path.join(out, "rising_bubble_step0.npz"), **rec)
 
 
+def stencil_kat(out):
+    import dycore.discretisation.grid as dis_grid
+    import dycore.physics.low_mach.laplacian as lm_lp
+    import dycore.physics.low_mach.mpv as lm_var
+    rec = {}
+    rng = np.random.default_rng(23)
+    for tag, lamb, cor, comp in (("std", False, False, False), ("std_cor", False, True, True),
+                                 ("lamb", True, True, True), ("lamb_plain", True, False, False)):
+        ud = _ud_rising_bubble()
+        ud.inx, ud.iny = 33, 17
+        elem, node = dis_grid.grid_init(ud)
+        mpv = lm_var.MPV(elem, node, ud)
+        if lamb:
+            ud.LAMB_BDRY = False              # the reference tests hasattr (test_lamb_wave.py:87)
+        mpv.wplus[...] = 0.5 + rng.random(mpv.wplus.shape)
+        mpv.wcenter[...] = -(0.5 + rng.random(mpv.wcenter.shape)) if comp else 0.0
+        csh = (elem.sc[1], elem.sc[0])        # transposed cell arrays (second_projection.py:651)
+        coriolis = (1.0 + 0.1 * rng.random(csh), 0.8 + 0.1 * rng.random(csh),
+                    0.1 * rng.standard_normal(csh) if cor else np.zeros(csh),
+                    0.1 * rng.standard_normal(csh) if cor else np.zeros(csh))
+        diag_inv = -(0.5 + rng.random(node.isc[:2]))     # 2D, as precon_diag_prepare returns it
+        f = lm_lp.stencil_9pt_numba_test(mpv, node, coriolis, diag_inv, ud)
+        p = rng.standard_normal(node.iicx * node.iicy)
+        y = f(p.copy())
+        rec[tag + "_wplus"] = np.copy(mpv.wplus)
+        rec[tag + "_wcenter"] = np.copy(mpv.wcenter)
+        for k in range(4):
+            rec[tag + "_cor%d" % k] = np.copy(coriolis[k])
+        rec[tag + "_diag_inv"] = np.copy(diag_inv)
+        rec[tag + "_p"] = p
+        rec[tag + "_y"] = np.copy(y)
+        rec[tag + "_meta"] = np.array([node.iicx, node.iicy, node.dx, node.dy, int(lamb)])
+        print("stencil_kat: %s done" % tag, flush=True)
+    np.savez_compressed(os.path.join(out, "stencil_kat.npz"), **rec)
+
+
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     if not args:
-        raise SystemExit("usage: make_golden.py REFERENCE_ROOT [--3d-only | --explicit-only]")
+        raise SystemExit("usage: make_golden.py REFERENCE_ROOT [--3d-only | --explicit-only | --stencil-only]")
     ref = args[0]
     refshim.install(ref)
     out = HERE
+    if "--stencil-only" in sys.argv:
+        stencil_kat(out)
+        return
     lap3d_kat(out)
     diag3d_kat(out)
     wall_kat(out)
@@ -647,6 +692,7 @@ def main():
     diag_kat(out)
     pieces_kat(out)
     explicit_kat(out)
+    stencil_kat(out)
     if "--explicit-only" not in sys.argv:
         rising_bubble_step0(out)
     print("fixtures written to", out)

@@ -5,7 +5,13 @@ It makes the reference's hot path importable with the packages present here:
 
 * ``numba`` is absent: ``jit``/``njit`` become identity decorators (the
   decorated functions then run as plain Python, which is slower but
-  numerically the same FP64 arithmetic).
+  numerically the same FP64 arithmetic).  ``numba.stencil`` becomes a loop
+  that applies the kernel at every point whose neighbourhood lies inside the
+  first array, with the kernel's relative indices resolved against each array
+  argument, and leaves the border at 0 (numba's default ``cval``); the
+  neighbourhood is one point each way, that of the one stencil on the
+  projection path (``kernel_9pt``, laplacian.py:749-856, used when
+  ``ud.LAMB_BDRY`` is set).
 * ``h5py``, ``dill``, ``yaml``, ``termcolor``, ``dask`` and ``matplotlib``
   are absent: they are replaced by empty modules (only imported, never
   used on the projection path).
@@ -30,6 +36,30 @@ def _identity_decorator(*args, **kwargs):
     return lambda f: f
 
 
+class _Relative:
+    """An array seen from one point of a stencil: a[di, dj] reads a[i + di, j + dj]."""
+
+    def __init__(self, a, i, j):
+        self.a, self.i, self.j = a, i, j
+
+    def __getitem__(self, idx):
+        di, dj = idx
+        return self.a[self.i + di, self.j + dj]
+
+
+def _stencil(func=None, **kwargs):
+    def wrap(kernel):
+        def run(*args):
+            a0 = args[0]
+            out = np.zeros(a0.shape, dtype=np.float64)
+            for i in range(1, a0.shape[0] - 1):
+                for j in range(1, a0.shape[1] - 1):
+                    out[i, j] = kernel(*[_Relative(a, i, j) if isinstance(a, np.ndarray) else a for a in args])
+            return out
+        return run
+    return wrap(func) if callable(func) else wrap
+
+
 def _stub_getattr(attr):
     if attr.startswith("__"):
         raise AttributeError(attr)
@@ -40,7 +70,7 @@ def _install_stub_modules():
     nb = types.ModuleType("numba")
     nb.jit = _identity_decorator
     nb.njit = _identity_decorator
-    nb.stencil = _identity_decorator
+    nb.stencil = _stencil
     nb.prange = range
     sys.modules.setdefault("numba", nb)
     for name in ["h5py", "dill", "yaml", "termcolor", "dask", "dask.distributed",

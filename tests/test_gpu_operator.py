@@ -89,3 +89,48 @@ def test_seam_consistency_preserved():
     x[:, -1] = x[:, 0]
     y = A.matvec(x.reshape(-1)).reshape(x.shape)
     np.testing.assert_allclose(y[:, 0], y[:, -1], rtol=4e-16 * 8, atol=0)
+
+
+def _factory_case(tag):
+    from types import SimpleNamespace as NS
+    d = np.load(golden("stencil_kat.npz"))
+    m = d[tag + "_meta"]
+    mpv = NS(wplus=d[tag + "_wplus"], wcenter=d[tag + "_wcenter"])
+    node = NS(dx=float(m[2]), dy=float(m[3]), iicx=int(m[0]), iicy=int(m[1]), i1=(slice(1, -1), slice(1, -1)))
+    ud = NS(bdry_type=["wrap", "symmetric", "symmetric"])
+    if m[4]:
+        ud.LAMB_BDRY = False              # the reference tests hasattr only
+    return d, mpv, node, ud, tuple(d[tag + "_cor%d" % k] for k in range(4)), d[tag + "_diag_inv"]
+
+
+@pytest.mark.parametrize("tag", ["std", "std_cor", "lamb", "lamb_plain"])
+def test_stencil_factory_drop_in_vs_reference(tag):
+    """pybella_gb300.laplacian.stencil_9pt_numba_test with the reference's arguments
+    (MPV wplus/wcenter, node, Coriolis 4-tuple, diag_inv, ud) against the closure the
+    reference's factory returned on the same operands (stencil_kat.npz): both
+    branches, lap2D_gather_new and LAMB_BDRY's lap2D_numba_test."""
+    from pybella_gb300 import laplacian
+    d, mpv, node, ud, cor, dinv = _factory_case(tag)
+    A = laplacian.stencil_9pt_numba_test(mpv, node, cor, dinv, ud)
+    y = A.matvec(d[tag + "_p"])
+    assert _rel(y, d[tag + "_y"]) < 1e-13
+
+
+def test_lamb_operator_solve_vs_scipy():
+    """A BiCGStab solve with the LAMB_BDRY operator (compressible: hcenter != 0)
+    against scipy's bicgstab on the oracle's restatement, tol 1e-10."""
+    from types import SimpleNamespace as NS
+    from oracle import nodal2d as n2
+    from oracle.krylov import bicgstab_legacy
+    from pybella_gb300 import laplacian, linalg
+    d, mpv, node, ud, cor, dinv = _factory_case("lamb")
+    g = NS(inx=node.iicx, iny=node.iicy, dx=node.dx, dy=node.dy, x_wall=False, y_wall=True)
+    op = n2.pack_9pt(mpv.wplus, mpv.wcenter, cor, dinv, g)
+    b = n2.lap2d_lamb(np.random.default_rng(3).standard_normal(node.iicx * node.iicy), op)
+    x_ref, info_ref, _ = bicgstab_legacy(lambda v: n2.lap2d_lamb(v, op), b, 1e-10, 5000)
+    A = laplacian.stencil_9pt_numba_test(mpv, node, cor, dinv, ud)
+    x, info = linalg.bicgstab(linalg.LinearOperator(A.shape, A), b, tol=1e-10, maxiter=5000)
+    assert info == 0 and info_ref == 0
+    r = b - n2.lap2d_lamb(x, op)
+    assert np.linalg.norm(r) / np.linalg.norm(b) <= 1e-10
+    assert _rel(x, x_ref) < 1e-7

@@ -376,3 +376,20 @@ def test_oracle_output_loop_matches_reference_full_run():
         mine, step = got[t]
         assert np.abs(mine - th).max() <= 1e-13, (t, np.abs(mine - th).max())
     assert got[0.1][1] == 3
+
+
+@pytest.mark.parametrize("tag", ["std", "std_cor", "lamb", "lamb_plain"])
+def test_oracle_stencil_factory_matches_reference(tag):
+    """Both closures of the reference's stencil_9pt_numba_test (laplacian.py:496-543):
+    lap2D_gather_new and, with ud.LAMB_BDRY, lap2D_numba_test with the kernel_9pt
+    stencil (mirrored y padding), on the reference's own grid/MPV objects
+    (stencil_kat.npz): the oracle's packing and operators reproduce them bit for bit."""
+    from types import SimpleNamespace as NS
+    from oracle import nodal2d as n2
+    d = np.load(golden("stencil_kat.npz"))
+    m = d[tag + "_meta"]
+    g = NS(inx=int(m[0]), iny=int(m[1]), dx=float(m[2]), dy=float(m[3]), x_wall=False, y_wall=True)
+    op = n2.pack_9pt(d[tag + "_wplus"], d[tag + "_wcenter"], tuple(d[tag + "_cor%d" % k] for k in range(4)),
+                     d[tag + "_diag_inv"], g)
+    y = n2.lap2d_lamb(d[tag + "_p"], op) if m[4] else n2.lap2d_gather(d[tag + "_p"], op)
+    np.testing.assert_array_equal(y, d[tag + "_y"])
