@@ -61,7 +61,7 @@ def _args():
     ap.add_argument("--ny", type=int, default=NY)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--workload", default="learned3d",
-                    choices=["solve2d", "ensemble", "learned3d", "step3d", "step2d"])
+                    choices=["solve2d", "ensemble", "learned3d", "step3d", "step2d", "ensemble_steps"])
     ap.add_argument("--nz", type=int, default=257)
     ap.add_argument("--train-steps", type=int, default=1000)
     ap.add_argument("--skip", type=float, default=0.9)
@@ -941,6 +941,97 @@ def run_step2d(args):
                           "gpu_launches": None}), flush=True)
 
 
+ENS_STEPS_WORKLOAD = ("ensemble time steps: 48 rising-bubble members (16 each at 160x80, 320x160, 640x320 cells, "
+                      "amplitude N(2 K, 0.2 K), centre N(0, 200 m)), each step's two projections of all members "
+                      "solved in one persistent launch (rtol 1e-10)")
+
+
+def ensemble_steps_line(args, local, rank, world, nsteps, warmup, want_cpu):
+    """``nsteps`` time steps of the 48-member ensemble with the state resident on the
+    GPU (EnsembleStep2D); returns the JSON line (dict)."""
+    import torch
+    from pybella_gb300 import workloads
+    from pybella_gb300.time_update import DeviceStep2D, EnsembleStep2D
+    states = workloads.bubble_ensemble_states(seed=17 + rank)
+    members = [DeviceStep2D(st["Sol"], st["mpv"], st["elem"], st["node"], st["ud"], st["th"], device=local)
+               for st in states]
+    prec = "fp64" if args.precision == "fp64" else "df64"
+    E = EnsembleStep2D(members, precision=prec)
+    step = 0
+    for _ in range(warmup):
+        E.step(step, E.time_steps(step, t_ref=1000.0))
+        step += 1
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record()
+    nstat0 = len(E.stats)
+    for _ in range(nsteps):
+        E.step(step, E.time_steps(step, t_ref=1000.0))
+        step += 1
+    e1.record()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    nmem = len(members)
+    stats = E.stats[nstat0:]
+    iters = np.array([[st["iterations"] for st in rnd] for rnd in stats], dtype=np.float64)
+    status = sorted(set(st["status"] for rnd in stats for st in rnd))
+    sizes = np.array([int(m.adv.inx) * int(m.adv.iny) for m in members], dtype=np.float64)
+    # algorithmic bytes of the batched solves: 25 words per node and iteration (two
+    # 5-word matvecs and the 15-word vector chain), 8 bytes each (FP64 or FP32 pair)
+    alg = float((iters * sizes[None, :]).sum() * 25 * 8)
+    peak, peak_kind = _peaks()
+    line = {
+        "metric": "ensemble time steps: projection solves/s (48 uneven members, batched)",
+        "value": 2.0 * nmem * nsteps / (ms / 1000.0), "unit": "solves/s", "n_gpus": world, "steps": nsteps,
+        "warmup": warmup, "ms_per_step": ms / nsteps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 state, %s solves" % prec, "data": "synthetic",
+        "config": {"workload": ENS_STEPS_WORKLOAD, "members": nmem, "unknowns": int(sizes.sum()),
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "state of %.0f MB resident (larger than L2 across the ensemble)" % (
+                       sum(6 * 8 * (int(m.adv.inx) + 3) * (int(m.adv.iny) + 3) for m in members) / 1e6)},
+        "member_steps_per_s": nmem * nsteps / (ms / 1000.0),
+        "solver": {"iterations_mean_per_grid": {
+            "%dx%d" % (int(m.adv.inx) - 1, int(m.adv.iny) - 1): float(iters[:, k].mean())
+            for k, m in enumerate(members) if k % 16 == 0},
+            "status": status, "solves": int(iters.size)},
+        "roofline": {"bound": "hbm", "achieved": alg / (ms / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": alg / (ms / 1000.0) / 1e9 / peak, "traffic": None,
+                     "kernel": "whole ensemble step (k_batch_bicgstab dominates)", "peak_source": peak_kind,
+                     "what": "algorithmic bytes of the batched solves / step time (the step's other kernels "
+                             "count as time, not bytes)"},
+        "clocks": clk, "wall_s": wall, "gpu_launches": None,
+    }
+    if want_cpu:
+        v, k = _cpu_step2d_sample(args.cpu_seconds)
+        it_small = float(iters[:, :16].mean())
+        work = float((iters.mean(axis=0) * sizes).sum()) / (it_small * sizes[0])
+        line["cpu_baseline"] = {"value": 2.0 * v / work, "unit": "solves/s", "cores": 1, "kind": "port",
+                                "sample": "%d steps of the oracle's time step on the 160x80 member (%.2f steps/s), "
+                                          "scaled to the whole ensemble by nodes x solver iterations (%.1f x one "
+                                          "160x80 member): extrapolated" % (k, v, work)}
+    return line
+
+
+def run_ensemble_steps(args):
+    import torch
+    world, rank, local = _dist()
+    torch.cuda.set_device(local)
+    line = ensemble_steps_line(args, local, rank, world, args.steps, args.warmup,
+                               want_cpu=rank == 0 and world == 1 and not args.no_cpu_baseline)
+    if world > 1:
+        t = torch.tensor([line["ms_per_step"]], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        line["ms_per_step"] = float(t.item())
+        line["value"] = world * 2.0 * line["config"]["members"] / (line["ms_per_step"] / 1000.0)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_step3d(args):
     """``--workload step3d``: whole 3D time steps of the warm bubble (advection,
     explicit and implicit projection halves, background-preconditioned solves to
@@ -1008,6 +1099,27 @@ def main():
                                   "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0,
                                           "d2h_bytes_per_step": 0}}))
             return
+        if args.workload == "ensemble_steps":
+            if _dist()[1] == 0:
+                v, k = _cpu_step2d_sample(args.cpu_seconds)
+                # work of one ensemble step in 160x80 member-steps: nodes x solver iterations,
+                # the iterations growing with the grid's linear size (231 / 460 / 950 measured)
+                from pybella_gb300.workloads import ENSEMBLE_GRIDS
+                work = 16.0 * sum((cx * cy) / (160.0 * 80.0) * (cx / 160.0) for cx, cy in ENSEMBLE_GRIDS)
+                ref = 96.0 * v / work
+                print(json.dumps({"impl": "reference", "metric": "ensemble time steps: projection solves/s "
+                                  "(48 uneven members, batched)", "value": ref, "unit": "solves/s",
+                                  "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                                  "config": {"workload": ENS_STEPS_WORKLOAD},
+                                  "cpu_baseline": {"value": ref, "unit": "solves/s", "cores": 1,
+                                                   "kind": "port",
+                                                   "sample": "%d steps of the oracle's time step on a 160x80 member, "
+                                                             "members run one after another (__main__.py:223-254); "
+                                                             "one ensemble step is %.0f such steps (nodes x "
+                                                             "iterations): extrapolated" % (k, work)},
+                                  "e2e": {"value": ref, "unit": "solves/s",
+                                          "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+            return
         if args.workload == "step3d":
             if _dist()[1] == 0:
                 print(json.dumps({"impl": "reference", "unavailable": "the reference's 3D time step cannot run "
@@ -1025,6 +1137,8 @@ def main():
         run_step3d(args)
     elif args.workload == "step2d":
         run_step2d(args)
+    elif args.workload == "ensemble_steps":
+        run_ensemble_steps(args)
     else:
         run_gpu(args)
 

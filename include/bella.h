@@ -187,6 +187,16 @@ typedef struct bella_proj2d {
 } bella_proj2d;
 int bella_projection2d(bella_ws *ws, const bella_proj2d *args, const bella_solve_opts *opts,
                        bella_solve_stats *stats, void *stream);
+/* The projections of an ensemble's members at one stage of their time steps
+ * (time_update.py:251, 462 for each member, __main__.py:223-254 runs them one
+ * after another): every member's preparation, then all members' solves in one
+ * persistent launch (bella_bicgstab_batched: opts->precision 0 FP64, otherwise
+ * double-float with FP64 refinement; config < 0 takes the autotuned launch
+ * configuration), then every member's correction.  Each member has its own
+ * workspace (ws[m] distinct); precond must be 0.  stats[nmembers]. */
+int bella_projection2d_batched(bella_ws *const *ws, const bella_proj2d *const *args, int nmembers,
+                               const bella_solve_opts *opts, int config, bella_solve_stats *stats,
+                               void *stream);
 
 /* ---- the whole 3D projection on the device -------------------------------
  * euler_backward_non_advective_impl_part (second_projection.py:97-277) in 3D.

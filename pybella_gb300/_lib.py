@@ -153,6 +153,9 @@ SIGNATURES = {
                                       ctypes.POINTER(SolveStats), ctypes.c_void_p]),
     "bella_projection2d": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Proj2D), ctypes.POINTER(SolveOpts),
                                           ctypes.POINTER(SolveStats), ctypes.c_void_p]),
+    "bella_projection2d_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                                  ctypes.POINTER(SolveOpts), ctypes.c_int, ctypes.c_void_p,
+                                                  ctypes.c_void_p]),
     "bella_projection3d": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Proj3D), ctypes.POINTER(SolveOpts),
                                           ctypes.POINTER(SolveStats), ctypes.c_void_p]),
     "bella_advective_fluxes2d": (ctypes.c_int, [ctypes.POINTER(Adv2D), ctypes.c_void_p]),

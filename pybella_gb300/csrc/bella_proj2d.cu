@@ -18,6 +18,8 @@
 #include <cstring>
 #include <string>
 
+#include <vector>
+
 #include "bella_internal.cuh"
 
 namespace bella {
@@ -407,15 +409,29 @@ using namespace bella;
 
 static int grid1(long long n) { return (int)((n + 255) / 256); }
 
-extern "C" int bella_projection2d(bella_ws *ws, const bella_proj2d *a, const bella_solve_opts *opts,
-                                  bella_solve_stats *stats, void *stream) {
+// One projection between its preparation and its correction: the geometry and
+// the scratch it keeps in the workspace (ws->proj_buf), and the operator it set.
+struct Proj2DState {
+    ProjDev P;
+    long long ncell, nnode, nisc, nin;
+    double *wplus0, *dinv_isc, *rhs_isc, *hx, *hy, *cxx, *cyy, *cxy, *cyx, *hc, *dinv, *bvec, *xvec, *pfull;
+    bella_op2d op;
+};
+
+static int proj2d_check(const bella_ws *ws, const bella_proj2d *a) {
     if (!ws || !a) return BELLA_EINVAL;
     if (a->inx < 3 || a->iny < 3 || !a->rho || !a->rhou || !a->rhov || !a->rhow || !a->rhoY || !a->rhoX ||
         !a->p2 || !a->hydro_rhoY0 || !a->S0n || !a->strat_inv)
         return BELLA_EINVAL;
     if (a->precond != 0 && (a->precond != 1 || !a->y_wall)) return BELLA_EINVAL;
-    cudaStream_t s = (cudaStream_t)stream;
-    ProjDev P;
+    return BELLA_OK;
+}
+
+// Steps 1-5 of the projection up to the solve: boundary data of the coefficient
+// state, ghost nodes and correction with the old p2, coefficients and diagonal,
+// divergence right-hand side, the operator set in ws (second_projection.py:113-205).
+static int proj2d_prepare(bella_ws *ws, const bella_proj2d *a, Proj2DState &S, cudaStream_t s) {
+    ProjDev &P = S.P;
     P.icx = a->inx + 3; P.icy = a->iny + 3;
     P.ncx = a->inx + 4; P.ncy = a->iny + 4;
     P.xbc = a->x_wall ? 1 : 0; P.ybc = a->y_wall ? 1 : 0;
@@ -426,29 +442,31 @@ extern "C" int bella_projection2d(bella_ws *ws, const bella_proj2d *a, const bel
     const long long ncell = (long long)P.icx * P.icy, nnode = (long long)P.ncx * P.ncy;
     const long long nisc = (long long)(P.icx - 1) * (P.icy - 1);
     const long long nin = (long long)a->inx * a->iny, npk = (long long)(a->inx + 1) * (a->iny + 1);
+    S.ncell = ncell; S.nnode = nnode; S.nisc = nisc; S.nin = nin;
     // scratch: wplus0, dinv_isc, rhs_isc, packed hx, hy, cxx, cyy, cxy, cyx, hc, dinv, b, x, pfull
     const size_t need = (size_t)(ncell + 2 * nisc + 6 * npk + 4 * nin + nnode);
     if (ws->proj_cap < need) {
         cudaFree(ws->proj_buf);
         ws->proj_buf = nullptr;
+        ws->proj_cap = 0;
         if (cudaMalloc(&ws->proj_buf, need * sizeof(double)) != cudaSuccess) return BELLA_ECUDA;
         ws->proj_cap = need;
     }
     double *q = ws->proj_buf;
-    double *wplus0 = q; q += ncell;
-    double *dinv_isc = q; q += nisc;
-    double *rhs_isc = q; q += nisc;
-    double *hx = q; q += npk;
-    double *hy = q; q += npk;
-    double *cxx = q; q += npk;
-    double *cyy = q; q += npk;
-    double *cxy = q; q += npk;
-    double *cyx = q; q += npk;
-    double *hc = q; q += nin;
-    double *dinv = q; q += nin;
-    double *bvec = q; q += nin;
-    double *xvec = q; q += nin;
-    double *pfull = q;
+    S.wplus0 = q; q += ncell;
+    S.dinv_isc = q; q += nisc;
+    S.rhs_isc = q; q += nisc;
+    S.hx = q; q += npk;
+    S.hy = q; q += npk;
+    S.cxx = q; q += npk;
+    S.cyy = q; q += npk;
+    S.cxy = q; q += npk;
+    S.cyx = q; q += npk;
+    S.hc = q; q += nin;
+    S.dinv = q; q += nin;
+    S.bvec = q; q += nin;
+    S.xvec = q; q += nin;
+    S.pfull = q;
 
     const bool has0 = a->rho0 != nullptr;
     // 1. coefficient state: set_explicit_boundary_data(Sol0 or Sol)   (:113-118)
@@ -465,24 +483,52 @@ extern "C" int bella_projection2d(bella_ws *ws, const bella_proj2d *a, const bel
     k_bd_y<<<grid1(P.icx), 256, 0, s>>>(P, a->rho, a->rhou, a->rhov, a->rhow, a->rhoY, a->rhoX, a->hydro_rhoY0,
                                        a->strat_inv);
     // 3. coefficients (wplus from the coefficient state, Coriolis factors from Sol) and diagonal
-    k_coeff_cells<<<grid1(ncell), 256, 0, s>>>(P, C[0], C[4], a->rho, a->rhoY, a->S0n, wplus0, hx, hy, cxx, cyy,
-                                              cxy, cyx);
-    k_coeff_nodes<<<grid1(nisc), 256, 0, s>>>(P, C[4], wplus0, dinv_isc, hc, dinv);
+    k_coeff_cells<<<grid1(ncell), 256, 0, s>>>(P, C[0], C[4], a->rho, a->rhoY, a->S0n, S.wplus0, S.hx, S.hy, S.cxx,
+                                              S.cyy, S.cxy, S.cyx);
+    k_coeff_nodes<<<grid1(nisc), 256, 0, s>>>(P, C[4], S.wplus0, S.dinv_isc, S.hc, S.dinv);
     // 4. divergence right-hand side (:134-170, :214)
     k_zero_ghost_momenta<<<grid1(P.icx), 256, 0, s>>>(P, a->rhou, a->rhov, a->rhow);
-    k_divergence<<<grid1(nisc), 256, 0, s>>>(P, a->rho, a->rhou, a->rhov, a->rhoY, dinv_isc, rhs_isc, bvec);
+    k_divergence<<<grid1(nisc), 256, 0, s>>>(P, a->rho, a->rhou, a->rhov, a->rhoY, S.dinv_isc, S.rhs_isc, S.bvec);
     ws->launches += 11;
-    if (a->rhs_out) cudaMemcpyAsync(a->rhs_out, rhs_isc, nisc * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    if (a->rhs_out) cudaMemcpyAsync(a->rhs_out, S.rhs_isc, nisc * sizeof(double), cudaMemcpyDeviceToDevice, s);
     if (cudaGetLastError() != cudaSuccess) return BELLA_ECUDA;
-    // 5. operator and solve (:175, :205, :230); cross planes only when Coriolis is on
+    // 5. operator (:175, :205); cross planes only when Coriolis is on
     const bool cross = (a->coriolis[0] != 0.0 || a->coriolis[1] != 0.0 || a->coriolis[2] != 0.0);
     const bool hc_on = !(a->is_compressible == 0 && a->compressibility == 0.0);
-    bella_op2d op;
+    bella_op2d &op = S.op;
     op.nx = a->inx; op.ny = a->iny; op.x_wall = a->x_wall; op.y_wall = a->y_wall; op.dx = a->dx; op.dy = a->dy;
-    op.hplusx = hx; op.hplusy = hy; op.hcenter = hc_on ? hc : nullptr;
-    op.cxx = cxx; op.cyy = cyy; op.cxy = cross ? cxy : nullptr; op.cyx = cross ? cyx : nullptr;
-    op.diag_inv = dinv;
-    int rc = bella_op2d_set(ws, &op, stream);
+    op.hplusx = S.hx; op.hplusy = S.hy; op.hcenter = hc_on ? S.hc : nullptr;
+    op.cxx = S.cxx; op.cyy = S.cyy; op.cxy = cross ? S.cxy : nullptr; op.cyx = cross ? S.cyx : nullptr;
+    op.diag_inv = S.dinv;
+    return bella_op2d_set(ws, &op, s);
+}
+
+// Step 6 after the solve: p2_full, ghost nodes, correction with updt_chi = 1,
+// p2 += p2_full, ghosts, boundary data (:241-277).
+static int proj2d_finish(bella_ws *ws, const bella_proj2d *a, const Proj2DState &S, cudaStream_t s) {
+    const ProjDev &P = S.P;
+    k_scatter<<<grid1(S.nnode), 256, 0, s>>>(P, S.xvec, S.pfull);
+    k_ghost_x<<<grid1(P.ncy), 256, 0, s>>>(P, S.pfull);
+    k_ghost_y<<<grid1(P.ncx), 256, 0, s>>>(P, S.pfull);
+    k_correction<<<grid1(S.ncell), 256, 0, s>>>(P, S.pfull, a->rho, a->rhou, a->rhov, a->rhow, a->rhoY, a->rhoX,
+                                               a->S0n, 1.0);
+    k_add<<<grid1(S.nnode), 256, 0, s>>>(S.nnode, a->p2, S.pfull);
+    k_ghost_x<<<grid1(P.ncy), 256, 0, s>>>(P, a->p2);
+    k_ghost_y<<<grid1(P.ncx), 256, 0, s>>>(P, a->p2);
+    k_bd_x<<<grid1(P.icy), 256, 0, s>>>(P, a->rho, a->rhou, a->rhov, a->rhow, a->rhoY, a->rhoX);
+    k_bd_y<<<grid1(P.icx), 256, 0, s>>>(P, a->rho, a->rhou, a->rhov, a->rhow, a->rhoY, a->rhoX, a->hydro_rhoY0,
+                                       a->strat_inv);
+    ws->launches += 9;
+    return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
+}
+
+extern "C" int bella_projection2d(bella_ws *ws, const bella_proj2d *a, const bella_solve_opts *opts,
+                                  bella_solve_stats *stats, void *stream) {
+    int rc = proj2d_check(ws, a);
+    if (rc != BELLA_OK) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    Proj2DState S;
+    rc = proj2d_prepare(ws, a, S, s);
     if (rc != BELLA_OK) return rc;
     bella_solve_opts o;
     if (opts) o = *opts; else bella_solve_opts_default(&o);
@@ -490,28 +536,45 @@ extern "C" int bella_projection2d(bella_ws *ws, const bella_proj2d *a, const bel
     int st;
     if (a->precond == 1) {
         bella_spectral3d *sp = nullptr;
-        rc = bella_spectral2d_create(&sp, &op, ws->device, stream);
+        rc = bella_spectral2d_create(&sp, &S.op, ws->device, stream);
         if (rc != BELLA_OK) return rc;
-        st = bella_fbicgstab_pc(ws, sp, nullptr, 0, bvec, xvec, &o, stats, stream);
+        st = bella_fbicgstab_pc(ws, sp, nullptr, 0, S.bvec, S.xvec, &o, stats, stream);
         bella_spectral3d_destroy(sp);
     } else {
-        st = bella_bicgstab(ws, bvec, xvec, &o, stats, stream);
+        st = bella_bicgstab(ws, S.bvec, S.xvec, &o, stats, stream);
     }
     if (st < 0) return st;
-    // 6. p2_full, ghost nodes, correction with updt_chi = 1, p2 += p2_full, ghosts (:241-277)
-    k_scatter<<<grid1(nnode), 256, 0, s>>>(P, xvec, pfull);
-    k_ghost_x<<<grid1(P.ncy), 256, 0, s>>>(P, pfull);
-    k_ghost_y<<<grid1(P.ncx), 256, 0, s>>>(P, pfull);
-    k_correction<<<grid1(ncell), 256, 0, s>>>(P, pfull, a->rho, a->rhou, a->rhov, a->rhow, a->rhoY, a->rhoX,
-                                             a->S0n, 1.0);
-    k_add<<<grid1(nnode), 256, 0, s>>>(nnode, a->p2, pfull);
-    k_ghost_x<<<grid1(P.ncy), 256, 0, s>>>(P, a->p2);
-    k_ghost_y<<<grid1(P.ncx), 256, 0, s>>>(P, a->p2);
-    k_bd_x<<<grid1(P.icy), 256, 0, s>>>(P, a->rho, a->rhou, a->rhov, a->rhow, a->rhoY, a->rhoX);
-    k_bd_y<<<grid1(P.icx), 256, 0, s>>>(P, a->rho, a->rhou, a->rhov, a->rhow, a->rhoY, a->rhoX, a->hydro_rhoY0,
-                                       a->strat_inv);
-    ws->launches += 9;
-    if (cudaGetLastError() != cudaSuccess) return BELLA_ECUDA;
+    rc = proj2d_finish(ws, a, S, s);
+    return rc != BELLA_OK ? rc : st;
+}
+
+extern "C" int bella_projection2d_batched(bella_ws *const *ws, const bella_proj2d *const *args, int nmembers,
+                                          const bella_solve_opts *opts, int config, bella_solve_stats *stats,
+                                          void *stream) {
+    if (!ws || !args || nmembers < 1) return BELLA_EINVAL;
+    for (int m = 0; m < nmembers; ++m) {
+        const int rc = proj2d_check(ws[m], args[m]);
+        if (rc != BELLA_OK) return rc;
+        if (args[m]->precond != 0) return BELLA_EINVAL;      // the batched solve is plain BiCGStab
+        for (int k = 0; k < m; ++k)
+            if (ws[k] == ws[m]) return BELLA_EINVAL;          // every member keeps its own workspace
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<Proj2DState> S(nmembers);
+    std::vector<const double *> b(nmembers);
+    std::vector<double *> x(nmembers);
+    for (int m = 0; m < nmembers; ++m) {
+        const int rc = proj2d_prepare(ws[m], args[m], S[m], s);
+        if (rc != BELLA_OK) return rc;
+        b[m] = S[m].bvec;
+        x[m] = S[m].xvec;
+    }
+    const int st = bella_bicgstab_batched(ws, nmembers, b.data(), x.data(), opts, config, stats, stream);
+    if (st < 0) return st;
+    for (int m = 0; m < nmembers; ++m) {
+        const int rc = proj2d_finish(ws[m], args[m], S[m], s);
+        if (rc != BELLA_OK) return rc;
+    }
     return st;
 }
 

@@ -194,10 +194,7 @@ class DeviceStep2D(_Loop):
         return ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
 
     def _project(self, dt, with_sol0):
-        r = self.proj
-        r.dt = float(dt)
-        for k in _FIELDS:
-            setattr(r, k + "0", ctypes.c_void_p(self.f0[k].data_ptr()) if with_sol0 else ctypes.c_void_p(0))
+        r = self._proj_args(dt, with_sol0)
         st = _lib.SolveStats()
         rc = self.lib.bella_projection2d(self.ws.handle, ctypes.byref(r), ctypes.byref(self.opts), ctypes.byref(st),
                                          self._stream())
@@ -208,9 +205,9 @@ class DeviceStep2D(_Loop):
         self.expl.dt = float(dt)
         _lib.check(self.lib.bella_expl_part2d(ctypes.byref(self.expl), self._stream()), "bella_expl_part2d")
 
-    def step(self, step, dt, precision="fp64"):
-        """One time step of length ``dt`` (time_update.py:129-489)."""
-        self.opts.precision = {"fp64": 0, "mixed": 1, "df64": 2}[precision]
+    def _half_step(self, dt):
+        """The step up to its first projection: boundary data, Sol0, face mass fluxes,
+        advection over dt/2, explicit projection half (time_update.py:130-247)."""
         lib, s, h = self.lib, self._stream(), 0.5 * dt
         with torch.cuda.device(self.dev):
             _lib.check(lib.bella_boundary2d(ctypes.byref(self.adv), s), "bella_boundary2d")   # :130
@@ -219,7 +216,13 @@ class DeviceStep2D(_Loop):
             _lib.check(lib.bella_advective_fluxes2d(ctypes.byref(self.adv), s), "bella_advective_fluxes2d")
             _lib.check(lib.bella_advect_rk2d(ctypes.byref(self.adv), h, s), "bella_advect_rk2d")    # :224
             self._expl_part(h)                                                 # :247
-            self._project(h, True)                                             # :251
+
+    def _full_step(self, step, dt):
+        """Between the two projections: fluxes of the half-step state, Sol reset to
+        Sol0, forward explicit part, Strang-split advection over dt, explicit
+        projection half (time_update.py:337-455)."""
+        lib, s, h = self.lib, self._stream(), 0.5 * dt
+        with torch.cuda.device(self.dev):
             _lib.check(lib.bella_advective_fluxes2d(ctypes.byref(self.adv), s), "bella_advective_fluxes2d")
             for k in _FIELDS:                                                  # Sol = Sol0 (:376)
                 self.f[k].copy_(self.f0[k])
@@ -227,13 +230,106 @@ class DeviceStep2D(_Loop):
             _lib.check(lib.bella_euler_forward2d(ctypes.byref(self.expl), s), "bella_euler_forward2d")
             _lib.check(lib.bella_advect2d(ctypes.byref(self.adv), dt, int(step) % 2, s), "bella_advect2d")  # :434
             self._expl_part(h)                                                 # :455
-            self._project(h, False)                                            # :462
+
+    def _proj_args(self, dt, with_sol0):
+        """The projection's argument block for a projection over ``dt`` (with Sol0's
+        coefficients in the half step)."""
+        r = self.proj
+        r.dt = float(dt)
+        for k in _FIELDS:
+            setattr(r, k + "0", ctypes.c_void_p(self.f0[k].data_ptr()) if with_sol0 else ctypes.c_void_p(0))
+        return r
+
+    def step(self, step, dt, precision="fp64"):
+        """One time step of length ``dt`` (time_update.py:129-489)."""
+        self.opts.precision = {"fp64": 0, "mixed": 1, "df64": 2}[precision]
+        with torch.cuda.device(self.dev):
+            self._half_step(dt)
+            self._project(0.5 * dt, True)                                      # :251
+            self._full_step(step, dt)
+            self._project(0.5 * dt, False)                                     # :462
 
     def download(self, Sol, mpv):
         torch.cuda.synchronize(self.dev)
         for k in _FIELDS:
             setattr(Sol, k, self.f[k].cpu().numpy())
         mpv.p2_nodes[...] = self.p2.cpu().numpy()
+
+
+class EnsembleStep2D:
+    """Time steps of an ensemble of 2D members on one GPU, the members' elliptic
+    solves batched.
+
+    The reference runs an ensemble's members one after another through
+    ``time_update.do`` (__main__.py:223-254).  Here every member is a
+    :class:`DeviceStep2D` (its own state and workspace, any grid size); each
+    stage of the step runs for all members in turn, and at each of the step's
+    two projections (time_update.py:251, 462) all members' solves run in one
+    persistent launch (``bella_projection2d_batched``), so a step of the whole
+    ensemble is two solver launches whatever the number of members.  Every
+    member takes its own time step (its CFL condition; 'CFLfixed' while the step
+    index is below 2).
+    """
+
+    def __init__(self, members, precision="df64", config=-1):
+        if not members:
+            raise ValueError("an ensemble needs members")
+        self.members = list(members)
+        self.dev = self.members[0].dev
+        if any(m.dev != self.dev for m in self.members):
+            raise ValueError("all members must live on one GPU")
+        self.lib = self.members[0].lib
+        self.config = int(config)
+        self.opts = _lib.SolveOpts()
+        self.lib.bella_solve_opts_default(ctypes.byref(self.opts))
+        self.opts.tol = float(self.members[0].opts.tol)
+        self.opts.maxiter = int(self.members[0].opts.maxiter)
+        self.opts.precision = {"fp64": 0, "df64": 2}[precision]
+        n = len(self.members)
+        self._ws = (ctypes.c_void_p * n)(*[m.ws.handle.value for m in self.members])
+        self.stats = []
+
+    def _stream(self):
+        return ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
+
+    def _project_all(self, dts, with_sol0):
+        n = len(self.members)
+        args = [m._proj_args(0.5 * dt, with_sol0) for m, dt in zip(self.members, dts)]
+        ptrs = (ctypes.c_void_p * n)(*[ctypes.addressof(a) for a in args])
+        st = (_lib.SolveStats * n)()
+        rc = self.lib.bella_projection2d_batched(self._ws, ptrs, n, ctypes.byref(self.opts), self.config, st,
+                                                 self._stream())
+        _lib.check(rc, "bella_projection2d_batched")
+        self.stats.append([s_.as_dict() for s_ in st])
+
+    def step(self, step, dts):
+        """One time step of every member, member m by ``dts[m]``."""
+        with torch.cuda.device(self.dev):
+            for m, dt in zip(self.members, dts):
+                m._half_step(dt)
+            self._project_all(dts, True)
+            for m, dt in zip(self.members, dts):
+                m._full_step(step, dt)
+            self._project_all(dts, False)
+
+    def time_steps(self, step, t_ref=None, CFL=0.5):
+        """Each member's dt from the CFL condition of its state (cfl.py:5-74), no
+        output time in reach; 'CFLfixed' (21.69 / t_ref) while ``step`` < 2."""
+        dts = []
+        for m in self.members:
+            m.boundary()
+            dt = dynamic_timestep(m.cfl_maxima(), 0.0, float("inf"), m.dxyz, step, CFL)
+            if not np.isfinite(dt):
+                raise FloatingPointError("non-finite time step in a member at step %d" % step)
+            dts.append(21.69 / t_ref if (t_ref is not None and step < 2) else dt)
+        return dts
+
+    def run(self, nsteps, t_ref=None, step=0):
+        """``nsteps`` steps of every member; returns the final step index."""
+        for _ in range(nsteps):
+            self.step(step, self.time_steps(step, t_ref))
+            step += 1
+        return step
 
 
 class DeviceStep3D(_Loop):

@@ -318,11 +318,11 @@ def bubble_3d_state(nx, ny, nz, seed=0, delth=2.0, y0=0.2, r0=0.2, grav=10.0, t_
     return dict(Sol=Sol, mpv=mpv, elem=elem, node=node, ud=ud, th=NS(gamm=GAMM))
 
 
-def bubble_2d_state(inx=161, iny=81, delth=2.0, y0=0.2, r0=0.2, grav=10.0, t_ref=1000.0):
+def bubble_2d_state(inx=161, iny=81, delth=2.0, y0=0.2, r0=0.2, grav=10.0, t_ref=1000.0, x0=0.0):
     """The rising bubble's initial state (inputs/rising_bubble.py:42-98) in the
     reference's objects (host NumPy arrays): inx x iny nodes on x in [-1, 1]
     (periodic), y in [0, 1] (walls), isentropic hydrostatic background
-    (hydrostatics.py:79-117), the warm bubble at (0, y0), fluid at rest, the
+    (hydrostatics.py:79-117), the warm bubble at (x0, y0), fluid at rest, the
     reference's boundary data applied by the first step.  Returns a dict with
     ``Sol``, ``mpv``, ``elem``, ``node``, ``ud``, ``th`` for
     :class:`pybella_gb300.time_update.DeviceStep2D`."""
@@ -345,7 +345,7 @@ def bubble_2d_state(inx=161, iny=81, delth=2.0, y0=0.2, r0=0.2, grav=10.0, t_ref
     rhoY0_c, Y0_c = column(ey)
     _, Y0_n = column(ny_)
     X, Yg = np.meshgrid(ex, ey, indexing="ij")
-    r = np.sqrt(X ** 2 + (Yg - y0) ** 2) / r0
+    r = np.sqrt((X - x0) ** 2 + (Yg - y0) ** 2) / r0
     pert = (delth / 300.0) * np.cos(0.5 * np.pi * r) ** 2
     pert[r > 1.0] = 0.0
     rhoY = np.broadcast_to(rhoY0_c[None, :], sc).copy()
@@ -362,3 +362,17 @@ def bubble_2d_state(inx=161, iny=81, delth=2.0, y0=0.2, r0=0.2, grav=10.0, t_ref
             u_wind_speed=0.0, v_wind_speed=0.0, w_wind_speed=0.0, stratification=lambda y: 1.0, tol=1e-10,
             max_iterations=6000, t_ref=t_ref)
     return dict(Sol=Sol, mpv=mpv, elem=elem, node=node, ud=ud, th=NS(gamm=GAMM))
+
+
+def bubble_ensemble_states(seed, per_grid=16, grids=ENSEMBLE_GRIDS):
+    """The 48-member rising-bubble ensemble as time-step states: ``per_grid``
+    members on each of ``grids`` (cells), bubble amplitude ~ N(2 K, 0.2 K) and
+    x-centre ~ N(0, 200 m) (units of h_ref = 10 km), seeded; each entry is a
+    :func:`bubble_2d_state` dict."""
+    rng = np.random.default_rng(int(seed))
+    out = []
+    for (cx, cy) in grids:
+        for _ in range(per_grid):
+            out.append(bubble_2d_state(inx=cx + 1, iny=cy + 1, delth=float(rng.normal(2.0, 0.2)),
+                                       x0=float(rng.normal(0.0, 200.0 / H_REF))))
+    return out

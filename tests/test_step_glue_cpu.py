@@ -180,6 +180,13 @@ class _Stand:
         from oracle import nodal2d as n2
         return self._project(p, st, n2.impl_part, {})
 
+    def bella_projection2d_batched(self, W, P, n, o, cfg, st, s):
+        from oracle import nodal2d as n2
+        from pybella_gb300 import _lib
+        for m in range(n):
+            self._project(ctypes.byref(_lib.Proj2D.from_address(P[m])), ctypes.byref(st[m]), n2.impl_part, {})
+        return 0
+
     def bella_cfl_maxima(self, rho, rhou, rhov, rhow, rhoY, n, gamm, Msq, scratch, out, s):
         a = {k: _arr(v, (n,)) for k, v in (("rho", rho), ("rhou", rhou), ("rhov", rhov), ("rhow", rhow),
                                             ("rhoY", rhoY))}
@@ -237,7 +244,7 @@ def _install(monkeypatch, tmp_path, ctx):
 
     class _Workspace:
         def __init__(self, device=0):
-            self._lib, self.handle = stand, None
+            self._lib, self.handle = stand, ctypes.c_void_p(0)
     monkeypatch.setattr(_lib, "Workspace", _Workspace)
 
 
@@ -423,3 +430,45 @@ def test_device_run_stops_on_a_non_finite_state(host_torch, monkeypatch, tmp_pat
                        ud, NS(gamm=prm.gamm))
     with pytest.raises(FloatingPointError):
         run.run(0.0, 0.1, 10, t_ref=1000.0, step=2)
+
+
+def test_ensemble_step2d_orchestration(host_torch, monkeypatch, tmp_path):
+    """EnsembleStep2D: each member's stages in the order of DeviceStep2D.step and
+    both projections through the batched entry point (stood in for by the oracle's
+    impl_part per member): two members of the 64x32 bubble (different amplitudes)
+    after two steps equal the same members stepped one by one."""
+    from oracle import cases
+    from pybella_gb300.time_update import DeviceStep2D, EnsembleStep2D
+    d = np.load(golden("step_kat.npz"))
+    grid, prm, _, _, hn, hc, sf = cases.rising_bubble(inx=64, iny=32)
+    hn, hc = dict(hn, S0=d["S0n"]), dict(hc, rhoY0=d["rhoY0"])
+    _install(monkeypatch, tmp_path, NS(grid=grid, prm=prm, hn=hn, hc=hc, sf=sf))
+    S0c = d["S0c"]
+    ud = NS(bdry_type=["wrap", "symmetric", "symmetric"], gravity_strength=[0.0, prm.g, 0.0], Msq=prm.Msq,
+            nonhydrostasy=1.0, compressibility=0.0, is_compressible=0, coriolis_strength=np.zeros(3),
+            u_wind_speed=0.0, v_wind_speed=0.0, w_wind_speed=0.0, stratification=sf, tol=1e-10,
+            max_iterations=6000)
+
+    def member(scale):
+        Sol = NS(**{k: d["in_" + k].copy() for k in FIELDS})
+        Sol.rho = Sol.rhoY / (1.0 + scale * (Sol.rhoY / d["in_rho"] - 1.0))
+        mpv = NS(p2_nodes=d["p2_in"].copy(), HydroState=NS(rhoY0=hc["rhoY0"], get_S0c=lambda elem: S0c),
+                 HydroState_n=NS(S0=hn["S0"]))
+        run = DeviceStep2D(Sol, mpv, NS(ndim=2, y=grid.elem_y),
+                           NS(iicx=grid.inx, iicy=grid.iny, dx=grid.dx, dy=grid.dy), ud, NS(gamm=prm.gamm))
+        return run, Sol, mpv
+    ens = [member(1.0), member(1.2)]
+    alone = [member(1.0), member(1.2)]
+    E = EnsembleStep2D([m[0] for m in ens], precision="fp64")
+    dts = [0.02169, 0.02169]
+    for step in (0, 1):
+        E.step(step, dts)
+        for (run, _, _), dt in zip(alone, dts):
+            run.step(step, dt)
+    assert len(E.stats) == 4 and all(len(x) == 2 for x in E.stats)
+    for (re, Se, me), (ra, Sa, ma) in zip(ens, alone):
+        re.download(Se, me)
+        ra.download(Sa, ma)
+        for k in FIELDS:
+            np.testing.assert_array_equal(getattr(Se, k), getattr(Sa, k), err_msg=k)
+        np.testing.assert_array_equal(me.p2_nodes, ma.p2_nodes)
