@@ -2,7 +2,7 @@
 (fixture generation only; the fixture is committed, the reference is not
 needed at test time).
 
-    python tests/golden/make_fullrun.py /path/to/pyBELLA [--stop TOUT]
+    python tests/golden/make_fullrun.py /path/to/pyBELLA [--stop TOUT] [--resume]
     python tests/golden/make_fullrun.py --oracle
 
 
@@ -20,6 +20,10 @@ Python: about 45 s per solve, a few hours for the whole run.  The state is
 written after every tenth output time (``fullrun_kat.npz``: theta = rhoY / rho
 at t = 0.1, 0.2, ..., all fields and p2 at the last output time reached, the
 step count and t), so an interrupted run still leaves a usable fixture.
+``--resume`` continues such a run from the last state written: a time step of
+the reference depends on nothing but ``Sol``, ``mpv.p2_nodes``, ``t`` and the
+step count (everything else it reads is the static background or is recomputed
+at the step's start), so the continuation is the same run.
 
 ``--oracle`` runs the same case through the oracle's restatement of the step and
 its output loop (``oracle/step2d.py``: ``run_outputs``, pinned to the reference's
@@ -80,7 +84,7 @@ def main():
         return oracle_main()
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     if not args:
-        raise SystemExit("usage: make_fullrun.py REFERENCE_ROOT [--stop TOUT]")
+        raise SystemExit("usage: make_fullrun.py REFERENCE_ROOT [--stop TOUT] [--resume]")
     stop = None
     if "--stop" in sys.argv:
         stop = float(sys.argv[sys.argv.index("--stop") + 1])
@@ -107,7 +111,20 @@ def main():
     steps = [0, 0]
     t, t0 = 0.0, time.time()
     thetas, touts_rec = [], []
+    if "--resume" in sys.argv and os.path.exists(out):
+        d = np.load(out)
+        for k in FIELDS:                      # the run started from this very state
+            assert np.array_equal(d["in_" + k], rec["in_" + k]), k
+        for k in FIELDS:
+            getattr(Sol, k)[...] = d["out_" + k]
+        mpv.p2_nodes[...] = d["out_p2"]
+        t = float(d["out_t"])
+        steps = [int(d["out_step"]), int(d["out_step"])]
+        thetas, touts_rec = list(d["theta"]), [float(v) for v in d["theta_t"]]
+        print("resumed at t = %.3f, step %d" % (t, steps[1]), flush=True)
     for n, tout in enumerate(ud.tout):
+        if float(np.around(tout, 3)) <= t:
+            continue
         steps[0] = steps[1]                                         # __main__.py:229-230
         ret = dis_time_update.do(Sol, flux, mpv, t, tout, ud, elem, node, steps, th, bld, None, False)
         Sol, flux, mpv, steps = ret[0], ret[1], ret[2], list(ret[3])
