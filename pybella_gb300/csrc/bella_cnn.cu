@@ -194,18 +194,22 @@ constexpr size_t conv_smem() { return (size_t)27 * COUT * CIN * 2 + (size_t)CH_V
 // layout per input plane: [16-byte channel chunk][row][8 channels]; the
 // descriptor's LBO steps between the two chunks of a K=16 step, its SBO between
 // groups of 8 rows.  Rows on the padding ring are computed and discarded.
-// Work: a CTA takes runs of consecutive x-planes of one block of TC_ROWS padded
-// rows (TC_MB accumulators of 128 rows); input plane p feeds output planes p+1,
-// p, p-1 (taps dx = -1, 0, 1), so consecutive planes share their inputs.
+// Work: the (block of TC_ROWS padded rows, x-plane) items are shared evenly among
+// the CTAs (one per SM); a CTA's share is one or two runs of consecutive x-planes
+// of one block (TC_MB accumulators of 128 rows); input plane p feeds output
+// planes p+1, p, p-1 (taps dx = -1, 0, 1), so consecutive planes share inputs.
 //
 // The CTA is warp-specialised and its roles meet only on mbarriers, so the
 // tensor cores never wait for a block-wide barrier:
 //   * producer warps stage input planes into a ring of TC_SLOTS shared-memory
 //     slots with 16-byte asynchronous copies (source size 0 fills the padding),
 //     each waiting for its slot to be released by the MMAs that read it last;
+//     the copies' own completion arrives on the slot's mbarrier (the producers
+//     never wait for their data);
 //   * one thread of the MMA warp issues each input plane's MMAs once the plane
-//     has landed and the accumulators it starts are free, then commits them to
-//     the plane's slot (freeing it) and to the output plane they complete;
+//     has landed and the accumulators it starts are free, then commits them once,
+//     to the input plane's entry of a ring of TC_DRING completion barriers, which
+//     both frees the plane's slot and marks the output plane it completes;
 //   * epilogue warps (one per 32 tensor-memory lanes of each row block) take each
 //     completed output plane out of tensor memory, zero its columns, write it,
 //     and release the accumulators to the MMA thread.
@@ -215,13 +219,15 @@ constexpr size_t conv_smem() { return (size_t)27 * COUT * CIN * 2 + (size_t)CH_V
 constexpr int TC_MB = 2;                    // 128-row accumulators per output plane
 constexpr int TC_ROWS = 128 * TC_MB;
 constexpr int TC_SLOTS = 5;                 // ring of staged input planes
+constexpr int TC_DRING = 32;                // completion barriers of input planes: longer than any
+                                            // waiter lags (input slots 5, accumulator ring 8 outputs
+                                            // of up to 3 inputs each), so no phase parity aliases
 constexpr long long TC_SPIN_LIMIT = 1LL << 24;
 constexpr size_t TC_SMEM_MAX = 225 * 1024;   // dynamic part; the kernel's static shared variables come on top
 constexpr int TC_EPI_WARPS = 4 * TC_MB;      // warps 0 .. 7: epilogue, row block w / 4, lanes 32 * (w % 4)
 constexpr int TC_PROD_WARPS = 2;             // warps 8, 9: producers
 constexpr int TC_MMA_WARP = TC_EPI_WARPS + TC_PROD_WARPS;   // warp 10: tensor memory and the MMAs
 constexpr int TC_THREADS = 32 * (TC_MMA_WARP + 1);
-constexpr int TC_LAG = 2;                    // copy groups a producer thread keeps in flight
 
 __device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
     uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
@@ -273,18 +279,20 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
 }
 
-// The run decomposition shared by all roles: run r covers padded-row block fb and
-// output x-planes [ia, ib); it reads input planes ia-1 .. ib.
+// The work decomposition shared by all roles: the (row block, x-plane) items
+// fb * nx + x, nblk * nx of them, are cut into one contiguous share of `work`
+// items per CTA; a share is one or more runs, each covering row block fb and
+// output x-planes [ia, ib) and reading input planes ia-1 .. ib.
 struct TcRun {
     int fb, ia, ib;
 };
-__device__ __forceinline__ TcRun tc_run(int run, int nseg, int runlen, int nx) {
-    TcRun r;
-    r.fb = run / nseg;
-    const int seg = run - r.fb * nseg;
-    r.ia = seg * runlen;
-    r.ib = min(nx, r.ia + runlen);
-    return r;
+__device__ __forceinline__ bool tc_next(long long &idx, long long hi, int nx, TcRun &r) {
+    if (idx >= hi) return false;
+    r.fb = (int)(idx / nx);
+    r.ia = (int)(idx - (long long)r.fb * nx);
+    r.ib = (int)min((long long)nx, (long long)r.ia + (hi - idx));
+    idx += r.ib - r.ia;
+    return true;
 }
 
 // Input plane p feeds output planes p+1, p, p-1 through the weights of taps dx = 0, 1, 2:
@@ -303,15 +311,15 @@ constexpr int TC_RING = 8;                   // accumulator planes per row block
 // out_scale of its first 8 channels.
 template <int CIN, int COUT, bool RELU, bool OUTF32>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *__restrict__ in,
+k_conv3d_tc(int nx, int ny, int nz, int xseg, long long work, const __nv_bfloat16 *__restrict__ in,
             const __nv_bfloat16 *__restrict__ Wtc, const float *__restrict__ bias, void *out, float out_scale,
-            int *err) {
+            int *err, const __nv_bfloat16 *__restrict__ mask) {
     static_assert(COUT == 32 || (COUT == 16 && OUTF32), "hidden layers: 32 channels; output layer: 16 (8 used)");
     constexpr int TMEM_COLS = TC_MB * TC_RING * COUT;     // 512 or 256: a power of two
     constexpr int NCH = CIN / 8;
     constexpr int NB = 3 * COUT;                          // B rows: the three dx taps
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t bar_full[TC_SLOTS], bar_empty[TC_SLOTS], bar_acc[TC_RING], bar_free[TC_RING];
+    __shared__ __align__(8) uint64_t bar_full[TC_SLOTS], bar_mma[TC_DRING], bar_free[TC_RING];
     __shared__ __align__(8) uint64_t bar_done;
     __shared__ uint32_t tmem_slot;
     __shared__ int abort_flag;
@@ -321,19 +329,19 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
     unsigned char *sW = smem;                             // [9][NCH][3*COUT][16 B]
     unsigned char *sA = smem + (size_t)9 * NCH * NB * 16; // [TC_SLOTS][NCH][L][16 B]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    for (int e = tid; e < 9 * NCH * NB; e += TC_THREADS)
-        reinterpret_cast<uint4 *>(sW)[e] = reinterpret_cast<const uint4 *>(Wtc)[e];
-    asm volatile("fence.proxy.async.shared::cta;");     // the weights are read by the tensor cores
     auto sa = [](const void *p) { return (uint32_t)__cvta_generic_to_shared(p); };
+    for (int e = tid; e < 9 * NCH * NB; e += TC_THREADS)      // the weights, all copies in flight at once
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa(sW) + 16u * e),
+                     "l"(reinterpret_cast<const uint4 *>(Wtc) + e));
+    asm volatile("cp.async.commit_group;");
+    asm volatile("cp.async.wait_group 0;");
+    asm volatile("fence.proxy.async.shared::cta;");     // the weights are read by the tensor cores
     if (tid == 0) {
-        for (int k = 0; k < TC_SLOTS; ++k) {
+        for (int k = 0; k < TC_SLOTS; ++k)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sa(&bar_full[k])), "r"(32 * TC_PROD_WARPS));
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sa(&bar_empty[k])));
-        }
-        for (int k = 0; k < TC_RING; ++k) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sa(&bar_acc[k])));
+        for (int k = 0; k < TC_DRING; ++k) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sa(&bar_mma[k])));
+        for (int k = 0; k < TC_RING; ++k)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sa(&bar_free[k])), "r"(TC_EPI_WARPS));
-        }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sa(&bar_done)));
         asm volatile("fence.mbarrier_init.release.cluster;");
         abort_flag = 0;
@@ -369,8 +377,8 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
 
     const int plane = PY * PZ;
     const int nblk = (plane + TC_ROWS - 1) / TC_ROWS;
-    const int nseg = (nx + runlen - 1) / runlen;
-    const int nruns = nblk * nseg;
+    const long long share_lo = (long long)blockIdx.x * work;
+    const long long share_hi = min(share_lo + work, (long long)nblk * nx);
     const uint32_t sW_a = sa(sW), sA_a = sa(sA);
 
     if (warp >= TC_EPI_WARPS && warp < TC_MMA_WARP) {
@@ -378,13 +386,15 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
         const int ptid = tid - 32 * TC_EPI_WARPS;
         long long i = 0;                                  // input planes staged so far (this CTA)
         bool ok = true;
-        for (int run = blockIdx.x; run < nruns && ok; run += gridDim.x) {
-            const TcRun R = tc_run(run, nseg, runlen, nx);
+        long long idx = share_lo;
+        TcRun R;
+        while (ok && tc_next(idx, share_hi, nx, R)) {
             const int f0 = R.fb * TC_ROWS - (PZ + 1);     // padded row of staged row 0
             for (int p = R.ia - 1; p <= R.ib && ok; ++p, ++i) {
                 const int slot = (int)(i % TC_SLOTS);
-                if (i >= TC_SLOTS &&
-                    !tc_wait_warp(sa(&bar_empty[slot]), (uint32_t)((i / TC_SLOTS - 1) & 1), abort)) {
+                const long long prev = i - TC_SLOTS;      // the slot's previous plane: its MMAs done?
+                if (prev >= 0 &&
+                    !tc_wait_warp(sa(&bar_mma[prev % TC_DRING]), (uint32_t)((prev / TC_DRING) & 1), abort)) {
                     ok = false;
                     break;
                 }
@@ -409,19 +419,12 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
                                            "r"(bytes));
                     }
                 }
-                asm volatile("cp.async.commit_group;");
-                if (i >= TC_LAG) {                        // plane i - TC_LAG has landed
-                    asm volatile("cp.async.wait_group %0;" ::"n"(TC_LAG));
-                    asm volatile("fence.proxy.async.shared::cta;");
-                    tc_arrive(sa(&bar_full[(i - TC_LAG) % TC_SLOTS]));
-                }
+                // arrives on the slot's barrier once this thread's copies so far have landed
+                asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(sa(&bar_full[slot])));
             }
         }
-        asm volatile("cp.async.wait_group 0;");
-        asm volatile("fence.proxy.async.shared::cta;");
-        if (ok)
-            for (long long j = (i > TC_LAG ? i - TC_LAG : 0); j < i; ++j) tc_arrive(sa(&bar_full[j % TC_SLOTS]));
-        else if (ptid == 0) {
+        asm volatile("cp.async.wait_all;");
+        if (!ok && ptid == 0) {
             atomicExch(err, 1);
             *abort = 1;
         }
@@ -459,8 +462,9 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
                     }
                 }
             };
-            for (int run = blockIdx.x; run < nruns && ok; run += gridDim.x) {
-                const TcRun R = tc_run(run, nseg, runlen, nx);
+            long long idx = share_lo;
+            TcRun R;
+            while (ok && tc_next(idx, share_hi, nx, R)) {
                 for (int p = R.ia - 1; p <= R.ib; ++p, ++i) {
                     const int slot = (int)(i % TC_SLOTS);
                     if (!tc_wait(sa(&bar_full[slot]), (uint32_t)((i / TC_SLOTS) & 1), abort)) {
@@ -489,9 +493,8 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
                             }
                         }
                     }
-                    tc_commit(sa(&bar_empty[slot]));          // the slot is free once these MMAs are done
-                    const int q = p - 1;                      // output plane complete after input plane p
-                    if (q >= R.ia && q < R.ib) tc_commit(sa(&bar_acc[(obase + q - R.ia) % TC_RING]));
+                    // one commit: the slot is free and output plane p-1 complete once these MMAs are done
+                    tc_commit(sa(&bar_mma[i % TC_DRING]));
                 }
                 obase += R.ib - R.ia;
             }
@@ -507,12 +510,14 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
     } else {
         // ---------------- epilogue warps ----------------
         const int mb = warp >> 2;
-        long long o = 0;
+        long long o = 0, ibase = 0;                       // output planes done; input index of the run's first
         bool ok = true;
-        for (int run = blockIdx.x; run < nruns && ok; run += gridDim.x) {
-            const TcRun R = tc_run(run, nseg, runlen, nx);
+        long long idx = share_lo;
+        TcRun R;
+        while (ok && tc_next(idx, share_hi, nx, R)) {
             for (int q = R.ia; q < R.ib; ++q, ++o) {
-                if (!tc_wait_warp(sa(&bar_acc[o % TC_RING]), (uint32_t)((o / TC_RING) & 1), abort)) {
+                const long long j = ibase + (q - R.ia + 2);  // input plane q+1 completes output plane q
+                if (!tc_wait_warp(sa(&bar_mma[j % TC_DRING]), (uint32_t)((j / TC_DRING) & 1), abort)) {
                     ok = false;
                     break;
                 }
@@ -554,12 +559,25 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
                             ov[0] = make_float4(v[0], v[1], v[2], v[3]);
                             ov[1] = make_float4(v[4], v[5], v[6], v[7]);
                         } else {
-                            uint32_t w[16];
+                            uint32_t w[16], mk[16];
+                            if (mask) {                  // ReLU derivative of the input-gradient pass
+                                const uint4 *mv = reinterpret_cast<const uint4 *>(mask + g * COUT);
+#pragma unroll
+                                for (int c4 = 0; c4 < 4; ++c4) {
+                                    const uint4 t = mv[c4];
+                                    mk[4 * c4] = t.x; mk[4 * c4 + 1] = t.y; mk[4 * c4 + 2] = t.z; mk[4 * c4 + 3] = t.w;
+                                }
+                            }
 #pragma unroll
                             for (int c = 0; c < 16; ++c) {
                                 float v0 = __uint_as_float(r[2 * c]), v1 = __uint_as_float(r[2 * c + 1]);
                                 if (bias) { v0 += bias[2 * c]; v1 += bias[2 * c + 1]; }
                                 if (RELU) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); }
+                                if (mask) {
+                                    const __nv_bfloat162 m2 = *reinterpret_cast<const __nv_bfloat162 *>(&mk[c]);
+                                    if (!(__bfloat162float(m2.x) > 0.f)) v0 = 0.f;
+                                    if (!(__bfloat162float(m2.y) > 0.f)) v1 = 0.f;
+                                }
                                 const __nv_bfloat162 h2 = __floats2bfloat162_rn(v0, v1);
                                 w[c] = *reinterpret_cast<const uint32_t *>(&h2);
                             }
@@ -576,6 +594,7 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
                 __syncwarp();
                 if (lane == 0) tc_arrive(sa(&bar_free[o % TC_RING]));
             }
+            ibase += R.ib - R.ia + 2;                     // the run read input planes ia-1 .. ib
         }
         if (!ok && lane == 0) {
             atomicExch(err, 1);
@@ -593,12 +612,14 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, int runlen, const __nv_bfloat16 *_
 // operand order [dy,dz][CINP/8][dx][COUTD][8] (COUTD >= COUTP; rows past COUTP are
 // zero): for each (dy, dz) and 8-channel chunk, the three dx taps' output channels
 // are 3*COUTD consecutive B rows
-__global__ void k_wk_to_tc(const __nv_bfloat16 *wk, int cinp, int coutp, int coutd, __nv_bfloat16 *wtc) {
+// flip: read the mirrored tap (-dx, -dy, -dz), i.e. 26 - tap (the input-gradient pass)
+__global__ void k_wk_to_tc(const __nv_bfloat16 *wk, int cinp, int coutp, int coutd, __nv_bfloat16 *wtc, int flip) {
     const int total = 27 * cinp * coutd;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
         const int tap = e / (cinp * coutd), r = e - tap * cinp * coutd, co = r / cinp, ci = r - co * cinp;
         const int dx = tap / 9, t9 = tap - dx * 9;
-        const __nv_bfloat16 v = co < coutp ? wk[((size_t)tap * coutp + co) * cinp + ci] : __float2bfloat16(0.f);
+        const int src = flip ? 26 - tap : tap;
+        const __nv_bfloat16 v = co < coutp ? wk[((size_t)src * coutp + co) * cinp + ci] : __float2bfloat16(0.f);
         wtc[((((size_t)t9 * (cinp / 8) + ci / 8) * 3 + dx) * coutd + co) * 8 + (ci % 8)] = v;
     }
 }
@@ -959,6 +980,7 @@ struct bella_cnn {
     int linear;               // 1: no ReLU and no biases (a linear map)
     int use_tc;               // 1: the forward pass on tcgen05 (k_conv3d_tc)
     __nv_bfloat16 *wtc[6];    // its weights in tensor-core operand order (layer 5: 16 output rows)
+    __nv_bfloat16 *wtcT[6];   // layers 1-5: the input-gradient pass's weights in that order
     int *tc_err;              // set when a tensor-core wait gave up
     float omega;              // identity path: output = omega * input + network
     int bias_free;            // 1: biases held at zero (positively homogeneous map)
@@ -1024,7 +1046,7 @@ static void cnn_free(bella_cnn *net) {
     cudaFree(net->gact[0]); cudaFree(net->gact[1]);
     cudaFree(net->y8); cudaFree(net->t8); cudaFree(net->g8); cudaFree(net->inv_e2); cudaFree(net->loss);
     cudaFree(net->yf); cudaFree(net->qf); cudaFree(net->gf); cudaFree(net->flux); cudaFree(net->wcrop);
-    for (int l = 0; l < 6; ++l) cudaFree(net->wtc[l]);
+    for (int l = 0; l < 6; ++l) { cudaFree(net->wtc[l]); cudaFree(net->wtcT[l]); }
     cudaFree(net->tc_err);
 }
 
@@ -1060,32 +1082,28 @@ static void forward_layers(bella_cnn *net, const BlockMap &m, float out_scale, c
     const int g = conv_grid(m);
     const int nx = m.B * m.cx, ny = m.cy, nz = m.cz, xs = m.cx;
     if (net->use_tc && tc_fits(m)) {
-        // runs of consecutive x-planes: about one run per SM
+        // the (row block, x-plane) items shared evenly, one CTA per SM
         const long long plane = (long long)(ny + 2) * (nz + 2);
-        const int nblk = (int)((plane + TC_ROWS - 1) / TC_ROWS);
-        int nseg = (int)((num_sms() + nblk / 2) / nblk);
-        if (nseg < 1) nseg = 1;
-        if (nseg > nx) nseg = nx;
-        const int runlen = (nx + nseg - 1) / nseg;
-        const long long nruns = (long long)nblk * ((nx + runlen - 1) / runlen);
-        const int gt = tc_grid(nruns), pz = nz + 2;
+        const long long items = ((plane + TC_ROWS - 1) / TC_ROWS) * (long long)nx;
+        const int gt = tc_grid(items), pz = nz + 2;
+        const long long work = (items + gt - 1) / gt;
         const float *b5 = net->linear ? nullptr : net->bias[5];
         if (net->linear) {
             k_conv3d_tc<16, 32, false, false><<<gt, TC_THREADS, tc_smem_bytes<16, 32>(pz), s>>>(
-                nx, ny, nz, xs, runlen, net->act[0], net->wtc[0], nullptr, net->act[1], 1.f, net->tc_err);
+                nx, ny, nz, xs, work, net->act[0], net->wtc[0], nullptr, net->act[1], 1.f, net->tc_err, nullptr);
             for (int l = 1; l <= 4; ++l)
                 k_conv3d_tc<32, 32, false, false><<<gt, TC_THREADS, tc_smem_bytes<32, 32>(pz), s>>>(
-                    nx, ny, nz, xs, runlen, net->act[l], net->wtc[l], nullptr, net->act[l + 1], 1.f, net->tc_err);
+                    nx, ny, nz, xs, work, net->act[l], net->wtc[l], nullptr, net->act[l + 1], 1.f, net->tc_err, nullptr);
         } else {
             k_conv3d_tc<16, 32, true, false><<<gt, TC_THREADS, tc_smem_bytes<16, 32>(pz), s>>>(
-                nx, ny, nz, xs, runlen, net->act[0], net->wtc[0], net->bias[0], net->act[1], 1.f, net->tc_err);
+                nx, ny, nz, xs, work, net->act[0], net->wtc[0], net->bias[0], net->act[1], 1.f, net->tc_err, nullptr);
             for (int l = 1; l <= 4; ++l)
                 k_conv3d_tc<32, 32, true, false><<<gt, TC_THREADS, tc_smem_bytes<32, 32>(pz), s>>>(
-                    nx, ny, nz, xs, runlen, net->act[l], net->wtc[l], net->bias[l], net->act[l + 1], 1.f,
-                    net->tc_err);
+                    nx, ny, nz, xs, work, net->act[l], net->wtc[l], net->bias[l], net->act[l + 1], 1.f,
+                    net->tc_err, nullptr);
         }
         k_conv3d_tc<32, 16, false, true><<<gt, TC_THREADS, tc_smem_bytes<32, 16>(pz), s>>>(
-            nx, ny, nz, xs, runlen, net->act[5], net->wtc[5], b5, net->y8, out_scale, net->tc_err);
+            nx, ny, nz, xs, work, net->act[5], net->wtc[5], b5, net->y8, out_scale, net->tc_err, nullptr);
         net->launches += 6;
         return;
     }
@@ -1127,16 +1145,34 @@ static void backward_layers(bella_cnn *net, const BlockMap &m, cudaStream_t s) {
     else
         k_wgrad<32, 32, 8, 1, float><<<gw, 256, wgrad_smem<32, 1>(), s>>>(nx, ny, nz, xs, net->act[5], net->g8, dW[5], db[5]);
     k_g8_to_bf16<<<vec_grid(n), 256, 0, s>>>(n, net->g8, net->gact[1]);
-    // input gradient of layer 5, masked by ReLU'(layer-4 output)
+    // input gradients (masked by ReLU' of the layer's input when the network has ReLUs):
+    // on tcgen05 -- the forward kernel with the mirrored, transposed weights -- where
+    // the staged planes fit, else on mma.sync
     const bool relu = !net->linear;
-    k_conv3d<16, 32, false, false, true><<<g, CNN_THREADS, conv_smem<16, 32>(), s>>>(
-        nx, ny, nz, xs, net->gact[1], net->wkT[5], nullptr, net->gact[0], 1.f, relu ? net->act[5] : nullptr);
+    const bool tc = net->use_tc && tc_fits(m);
+    const long long plane = (long long)(ny + 2) * (nz + 2);
+    const long long items = ((plane + TC_ROWS - 1) / TC_ROWS) * (long long)nx;
+    const int gt = tc_grid(items), pz = nz + 2;
+    const long long work = (items + gt - 1) / gt;
+    if (tc)
+        k_conv3d_tc<16, 32, false, false><<<gt, TC_THREADS, tc_smem_bytes<16, 32>(pz), s>>>(
+            nx, ny, nz, xs, work, net->gact[1], net->wtcT[5], nullptr, net->gact[0], 1.f, net->tc_err,
+            relu ? net->act[5] : nullptr);
+    else
+        k_conv3d<16, 32, false, false, true><<<g, CNN_THREADS, conv_smem<16, 32>(), s>>>(
+            nx, ny, nz, xs, net->gact[1], net->wkT[5], nullptr, net->gact[0], 1.f, relu ? net->act[5] : nullptr);
     int cur = 0;
     for (int l = 4; l >= 1; --l) {
         k_wgrad<32, 32, 32, 32, __nv_bfloat16><<<gw, 256, wgrad_smem<32, 32>(), s>>>(
             nx, ny, nz, xs, net->act[l], net->gact[cur], dW[l], db[l]);
-        k_conv3d<32, 32, false, false, true><<<g, CNN_THREADS, conv_smem<32, 32>(), s>>>(
-            nx, ny, nz, xs, net->gact[cur], net->wkT[l], nullptr, net->gact[cur ^ 1], 1.f, relu ? net->act[l] : nullptr);
+        if (tc)
+            k_conv3d_tc<32, 32, false, false><<<gt, TC_THREADS, tc_smem_bytes<32, 32>(pz), s>>>(
+                nx, ny, nz, xs, work, net->gact[cur], net->wtcT[l], nullptr, net->gact[cur ^ 1], 1.f, net->tc_err,
+                relu ? net->act[l] : nullptr);
+        else
+            k_conv3d<32, 32, false, false, true><<<g, CNN_THREADS, conv_smem<32, 32>(), s>>>(
+                nx, ny, nz, xs, net->gact[cur], net->wkT[l], nullptr, net->gact[cur ^ 1], 1.f,
+                relu ? net->act[l] : nullptr);
         cur ^= 1;
     }
     if (net->block == 2)
@@ -1161,7 +1197,11 @@ static int cnn_sync_weights(bella_cnn *net, cudaStream_t s) {
         k_cast_bias<<<1, 32, 0, s>>>(b, net->cout[l], COUTP_L[l], net->bias[l]);
         net->launches += 2;
         if (net->wtc[l]) {
-            k_wk_to_tc<<<64, 256, 0, s>>>(net->wk[l], CINP_L[l], COUTP_L[l], COUTTC_L[l], net->wtc[l]);
+            k_wk_to_tc<<<64, 256, 0, s>>>(net->wk[l], CINP_L[l], COUTP_L[l], COUTTC_L[l], net->wtc[l], 0);
+            net->launches += 1;
+        }
+        if (l >= 1 && net->wtcT[l]) {   // the input-gradient pass of layer l: mirrored taps, (ci, co) swapped
+            k_wk_to_tc<<<64, 256, 0, s>>>(net->wkT[l], COUTPT_L[l], CINP_L[l], CINP_L[l], net->wtcT[l], 1);
             net->launches += 1;
         }
     }
@@ -1215,6 +1255,7 @@ int bella_cnn_create(bella_cnn **out, int device, int block, long long capacity)
     for (float **p : {&net->y8, &net->t8, &net->g8}) ok = ok && cudaMalloc(p, C * 8 * sizeof(float)) == cudaSuccess;
     ok = ok && cudaMalloc(&net->inv_e2, C * sizeof(float)) == cudaSuccess;
     for (int l = 0; l < 6 && ok; ++l) ok = cudaMalloc(&net->wtc[l], 27ULL * CINP_L[l] * COUTTC_L[l] * 2) == cudaSuccess;
+    for (int l = 1; l < 6 && ok; ++l) ok = cudaMalloc(&net->wtcT[l], 27ULL * COUTPT_L[l] * CINP_L[l] * 2) == cudaSuccess;
     ok = ok && cudaMalloc(&net->tc_err, sizeof(int)) == cudaSuccess && cudaMemset(net->tc_err, 0, sizeof(int)) == cudaSuccess;
     ok = ok && cudaMalloc(&net->loss, sizeof(double)) == cudaSuccess;
     for (float *p : {net->params, net->grads, net->adam_m, net->adam_v})
