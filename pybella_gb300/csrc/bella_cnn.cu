@@ -698,8 +698,10 @@ __global__ void k_pack_f32(BlockMap m, const float *in, float scale, float *out)
 
 // net-grid f32 [nvox][8] -> node values (times RMS from sumsq when given), plus
 // omega * skip (the identity path of the preconditioner) when skip is given
+// seam: the network's reach in nodes; along an axis flagged in pmask (bit 0 x, 1 y,
+// 2 z) the output is 0 within that distance of the duplicated periodic seam
 __global__ void k_unpack(BlockMap m, const float *y8, float *out, const double *sumsq, const float *skip = nullptr,
-                         float omega = 0.f) {
+                         float omega = 0.f, int pmask = 0, int seam = 0) {
     const long long n = (long long)m.B * m.nx * m.ny * m.nz;
     const float mul = sumsq ? 1.f / rms_scale(sumsq, n) : 1.f;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
@@ -712,6 +714,12 @@ __global__ void k_unpack(BlockMap m, const float *y8, float *out, const double *
         const int q = ((i % m.b) * m.b + j % m.b) * m.b + k % m.b;
         float o = y8[v * 8 + q] * mul;
         if (skip) o = fmaf(omega, skip[e], o);
+        if (pmask) {
+            const bool near = ((pmask & 1) && min(i, m.nx - 1 - i) < seam) ||
+                              ((pmask & 2) && min(j, m.ny - 1 - j) < seam) ||
+                              ((pmask & 4) && min(k, m.nz - 1 - k) < seam);
+            if (near) o = 0.f;
+        }
         out[e] = o;
     }
 }
@@ -1215,12 +1223,14 @@ namespace bella {
 // synchronisation); used by the flexible solver.  BELLA_EINVAL if the grid
 // exceeds the network's capacity.
 int cnn_apply_dev(bella_cnn *net, int nx, int ny, int nz, const float *in, float *out, const double *sumsq,
-                  cudaStream_t s) {
+                  cudaStream_t s, const int *per) {
     const BlockMap m = make_map(1, nx, ny, nz, net->block);
     if (!map_ok(net, m)) return BELLA_EINVAL;
     k_pack_in<<<vec_grid(m.nvox()), 256, 0, s>>>(m, in, 1.f, net->act[0], sumsq);
     forward_layers(net, m, 1.f, s);
-    k_unpack<<<vec_grid((long long)nx * ny * nz), 256, 0, s>>>(m, net->y8, out, sumsq, in, net->omega);
+    const int pmask = per ? (per[0] ? 1 : 0) | (per[1] ? 2 : 0) | (per[2] ? 4 : 0) : 0;
+    const int seam = 7 * net->block - 1;      // six 3x3x3 layers on b-node blocks: 6b + (b - 1) nodes
+    k_unpack<<<vec_grid((long long)nx * ny * nz), 256, 0, s>>>(m, net->y8, out, sumsq, in, net->omega, pmask, seam);
     net->launches += 2;
     return BELLA_OK;
 }

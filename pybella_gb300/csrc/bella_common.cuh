@@ -224,6 +224,7 @@ struct bella_ws {
     long long n;              // unknowns
     int cross, has_hc, singular;
     int ymirror;              // 2D operator with the mirrored y boundary (bella_op2d.y_wall == BELLA_Y_MIRROR)
+    int per[3];               // periodic axes of the operator (x, y, z; the duplicated seam)
     double *a64;              // 4 cell planes
     float  *a32;
     double *dinv64, *hc64, *z64;

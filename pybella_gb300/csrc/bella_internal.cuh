@@ -141,7 +141,10 @@ float *spectral_work(bella_spectral3d *sp, int which);
 long long spectral_size(const bella_spectral3d *sp);
 
 // learned preconditioner (bella_cnn.cu)
+// per (optional): the periodic axes of the grid; the correction is left out within
+// the network's reach of a periodic seam, where its zero padding stands in for
+// the wrapped neighbours
 int cnn_apply_dev(bella_cnn *net, int nx, int ny, int nz, const float *in, float *out, const double *sumsq,
-                  cudaStream_t s);
+                  cudaStream_t s, const int *per = nullptr);
 
 }  // namespace bella

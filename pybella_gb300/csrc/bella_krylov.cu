@@ -557,6 +557,7 @@ int bella_op2d_set(bella_ws *ws, const bella_op2d *op, void *stream) {
     ws->ymirror = op->y_wall == BELLA_Y_MIRROR ? 1 : 0;
     // the null space projection is that of the wrapped/walled operator: not applied with the mirror
     ws->singular = (!ws->has_hc && !ws->cross && !ws->ymirror) ? 1 : 0;
+    ws->per[0] = op->x_wall ? 0 : 1; ws->per[1] = op->y_wall ? 0 : 1; ws->per[2] = 0;
     ws->grid_stencil = stencil_grid(op->nx, op->ny);
     ws->grid_vec = vec_grid(n);
     rc = op2d_pack(ws, op, s);
@@ -599,6 +600,7 @@ int bella_op3d_set(bella_ws *ws, const bella_op3d *op, void *stream) {
     ws->has_hc = op->hcenter != nullptr ? 1 : 0;
     ws->ymirror = 0;
     ws->singular = (!ws->has_hc && !ws->cross) ? 1 : 0;
+    ws->per[0] = op->x_wall ? 0 : 1; ws->per[1] = op->y_wall ? 0 : 1; ws->per[2] = op->z_wall ? 0 : 1;
     ws->grid_stencil = stencil3d_grid(op->nx, op->ny, op->nz);
     ws->grid_vec = vec_grid(n);
     rc = op3d_pack(ws, op, s);
@@ -1106,7 +1108,7 @@ static int stage_net(bella_ws *ws, const Precond &pc, const float *in, float *ou
     float *tmp = spectral_work(pc.sp, 0), *corr = spectral_work(pc.sp, 1);
     op_apply(ws, 1, out, tmp, s);
     k_flex_corr_in<<<gv, VEC_BLOCK, 0, s>>>(n, in, tmp, ws->ks, ws->partials, ws->counter);
-    const int rc = cnn_apply_dev(pc.net, ws->nx, ws->ny, ws->nz, tmp, corr, &ws->ks->pss, s);
+    const int rc = cnn_apply_dev(pc.net, ws->nx, ws->ny, ws->nz, tmp, corr, &ws->ks->pss, s, ws->per);
     if (rc != BELLA_OK) return set_err(rc, "bella_fbicgstab_pc: grid exceeds the network's capacity");
     k_flex_add<<<gv, VEC_BLOCK, 0, s>>>(n, out, corr, ws->ks);
     ws->launches += 3;
@@ -1129,13 +1131,13 @@ static int stage_background(bella_ws *ws, const Precond &pc, const float *in, fl
 static int precond_apply(bella_ws *ws, const Precond &pc, const float *in, float *out, double *in_sumsq,
                          cudaStream_t s) {
     if (!pc.sp) {
-        const int rc = cnn_apply_dev(pc.net, ws->nx, ws->ny, ws->nz, in, out, in_sumsq, s);
+        const int rc = cnn_apply_dev(pc.net, ws->nx, ws->ny, ws->nz, in, out, in_sumsq, s, ws->per);
         if (rc != BELLA_OK) return set_err(rc, "bella_fbicgstab: grid exceeds the network's capacity");
         return BELLA_OK;
     }
     int rc;
     if (pc.net && pc.compose == 1) {
-        rc = cnn_apply_dev(pc.net, ws->nx, ws->ny, ws->nz, in, out, in_sumsq, s);
+        rc = cnn_apply_dev(pc.net, ws->nx, ws->ny, ws->nz, in, out, in_sumsq, s, ws->per);
         if (rc != BELLA_OK) return set_err(rc, "bella_fbicgstab_pc: grid exceeds the network's capacity");
         return stage_background(ws, pc, in, out, s);
     }
