@@ -1131,7 +1131,8 @@ static int stage_background(bella_ws *ws, const Precond &pc, const float *in, fl
 static int precond_apply(bella_ws *ws, const Precond &pc, const float *in, float *out, double *in_sumsq,
                          cudaStream_t s) {
     if (!pc.sp) {
-        const int rc = cnn_apply_dev(pc.net, ws->nx, ws->ny, ws->nz, in, out, in_sumsq, s, ws->per);
+        // the network alone: no seam band left out (there is no other stage to cover it)
+        const int rc = cnn_apply_dev(pc.net, ws->nx, ws->ny, ws->nz, in, out, in_sumsq, s);
         if (rc != BELLA_OK) return set_err(rc, "bella_fbicgstab: grid exceeds the network's capacity");
         return BELLA_OK;
     }

@@ -195,8 +195,10 @@ def test_trained_correction_of_the_background_solve(capsys):
     """Train the network on the pairs the background solve leaves (from the
     background-preconditioned solver's own iterates), then solve with and
     without it: the learned solve meets the tolerance on the FP64 true residual,
-    never falls back silently, and what the network gains (or costs) against the
-    background solve alone is measured and printed."""
+    never falls back silently, and takes no more flexible-GMRES iterations than
+    the same method with the background solve alone; iterations and times of
+    both (and of background BiCGStab) are printed -- in time the network's
+    application costs more than the iterations it saves."""
     import torch
     from pybella_gb300 import learned, workloads
     from pybella_gb300.spectral import BackgroundSolve
@@ -210,20 +212,22 @@ def test_trained_correction_of_the_background_solve(capsys):
     net = learned.CNN(shape, block=2, mode="linear", skip=0.7)
     net.set_params(params)
     xb, sb = A.solve(w["b"], tol=1e-8, maxiter=4000, preconditioner=bg)
+    xf, sf = A.solve(w["b"], tol=1e-8, maxiter=4000, preconditioner=bg, method="fgmres", restart=30)
     with warnings.catch_warnings(record=True) as rec:
         warnings.simplefilter("always")
         xl, sl = A.solve(w["b"], tol=1e-8, maxiter=4000, preconditioner=learned.LearnedPreconditioner(bg, net),
                          method="fgmres", restart=30)
-    for x, st in ((xb, sb), (xl, sl)):
+    for x, st in ((xb, sb), (xf, sf), (xl, sl)):
         assert st["status"] == 0, st
         r = w["b"] - A.matvec(x)
         assert float(torch.linalg.norm(r) / torch.linalg.norm(w["b"])) <= 1e-8
     assert bool(sl["fallback"]) == any("preconditioned solve failed" in str(m.message) for m in rec)
+    assert sl["fallback"] == 0 and sl["iterations"] <= sf["iterations"], (sl, sf)
     with capsys.disabled():
-        print("\ntrained correction (%s): background alone %d iterations %.4f s; background + network %d "
-              "iterations %.4f s (fallback %d); training loss %.3f -> %.3f"
-              % ("x".join(map(str, shape)), sb["iterations"], sb["seconds"], sl["iterations"], sl["seconds"],
-                 sl["fallback"], losses[0][1], losses[-1][1]))
+        print("\ntrained correction (%s): background alone: BiCGStab %d iterations %.4f s, FGMRES %d iterations "
+              "%.4f s; background + network (FGMRES) %d iterations %.4f s (fallback %d); training loss %.3f -> %.3f"
+              % ("x".join(map(str, shape)), sb["iterations"], sb["seconds"], sf["iterations"], sf["seconds"],
+                 sl["iterations"], sl["seconds"], sl["fallback"], losses[0][1], losses[-1][1]))
 
 
 # ---------------------------------------------------------------------------
