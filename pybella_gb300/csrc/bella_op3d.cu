@@ -17,19 +17,28 @@
 // conventions of the reference's 2D operator (the 3D glue of the reference,
 // second_projection.py:183-203, cannot run).
 //
-// A CTA of 256 threads (32 along z, 8 along y) owns a 4x8x32 node tile:
-// it stages the stencil input u with a one-node halo (6x10x34) in dynamic
-// shared memory (u is formed on the fly from the Krylov vectors), computes the
-// 5x9x33 cell fluxes into shared memory and writes 4 nodes per thread.
+// The stencil streams along x.  A CTA of 256 threads owns a y-z tile of
+// 8 x 32 nodes (thread (ty, tz) = (tid / 32, tid % 32) owns node
+// (j0 + ty, k0 + tz)) and marches through a run of node planes [xs, xe).
+// Step i of a run stores u plane i+2 with its one-node y-z halo (10 x 34;
+// u is formed on the fly from the Krylov vectors), computes the 9 x 33 cell
+// fluxes of cell plane i+1 and finishes node plane i-1.  Four u planes and
+// three flux planes rotate in shared memory, so the three phases of a step
+// touch disjoint buffers and one barrier per step suffices.  Every global
+// load is issued two steps before its use (register sets A and B serve
+// alternate steps), which keeps enough bytes in flight per SM to cover the
+// DRAM latency.  The runs are even shares of the (tile, plane) sequence over
+// the grid (one resident wave), so a CTA's run may span two tiles.
 #include "bella_internal.cuh"
 
 namespace bella {
 
-constexpr int T3X = 4, T3Y = 8, T3Z = 32;
-constexpr int H3X = T3X + 2, H3Y = T3Y + 2, H3Z = T3Z + 2;
-constexpr int C3X = T3X + 1, C3Y = T3Y + 1, C3Z = T3Z + 1;
-constexpr int NU3 = H3X * H3Y * H3Z;      // 2040 halo values
-constexpr int NC3 = C3X * C3Y * C3Z;      // 1485 cells
+constexpr int S3Y = 8, S3Z = 32;
+constexpr int SUY = S3Y + 2, SUZ = S3Z + 2, SUN = SUY * SUZ;    // u plane with its halo: 10 x 34
+constexpr int SCY = S3Y + 1, SCZ = S3Z + 1, SCN = SCY * SCZ;    // cell plane: 9 x 33
+constexpr int SU_EXTRA = SUN - 256;                             // 84 halo nodes beyond one per thread
+constexpr int SC_EXTRA = SCN - 256;                             // 41 edge cells beyond one per thread
+constexpr int SU_BUF = 4, SF_BUF = 3;                           // rotating u and flux planes
 
 template <typename T>
 struct Op3D {
@@ -47,7 +56,20 @@ struct StArgs3 {
 };
 
 template <typename T>
-size_t smem3d_bytes() { return sizeof(T) * (NU3 + 3 * NC3); }
+size_t smem3d_bytes() { return sizeof(T) * (SU_BUF * SUN + SF_BUF * 3 * SCN); }
+
+// number of input vectors u is formed from: x (APPLY, RESID), r p v (PDIR), r v (SDIR)
+template <int MODE> struct In3 { static constexpr int n = MODE == M_PDIR ? 3 : MODE == M_SDIR ? 2 : 1; };
+
+// one thread's loads for one step: the inputs of u at its own and its extra
+// halo node, the coefficients of its own and its extra cell, and its node's
+// diag_inv, hcenter and rhat (PDIR) or b (RESID)
+template <typename T, int MODE, bool CROSS>
+struct Pref3 {
+    T ui[In3<MODE>::n][2];
+    T cf[CROSS ? 5 : 3][2];
+    T dinv, hc, aux;
+};
 
 // ---- operator packing -------------------------------------------------------
 __global__ void k_pack3d_cells(bella_op3d op, double *a64, float *a32, dfloat *adf) {
@@ -105,11 +127,10 @@ template <typename T, int MODE, bool CROSS, bool HC>
 __global__ void __launch_bounds__(256)
 k_stencil3d(Op3D<T> op, StArgs3<T> a, KState *ks, double *partials, unsigned *counter) {
     using AccT = typename Acc<T>::type;
+    constexpr int NI = In3<MODE>::n, NCF = CROSS ? 5 : 3;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *su = reinterpret_cast<T *>(smem_raw);          // [H3X][H3Y][H3Z]
-    T *sfx = su + NU3;                                // [C3X][C3Y][C3Z]
-    T *sfy = sfx + NC3;
-    T *sfz = sfy + NC3;
+    T *su = reinterpret_cast<T *>(smem_raw);          // [SU_BUF][SUY][SUZ]
+    T *sf = su + SU_BUF * SUN;                        // [SF_BUF][Fx, Fy, Fz][SCY][SCZ]
 
     int par = 0;
     bool first = false;
@@ -123,9 +144,9 @@ k_stencil3d(Op3D<T> op, StArgs3<T> a, KState *ks, double *partials, unsigned *co
         omega = (T)ks->omega;
     }
     const int nx = op.nx, ny = op.ny, nz = op.nz;
-    const int tx = (nx + T3X - 1) / T3X, ty = (ny + T3Y - 1) / T3Y, tz = (nz + T3Z - 1) / T3Z;
-    const long long ntiles = (long long)tx * ty * tz;
-    const int tid = threadIdx.x;
+    const int tyn = (ny + S3Y - 1) / S3Y, tzn = (nz + S3Z - 1) / S3Z;
+    const long long work = (long long)tyn * tzn * nx;          // (y-z tile, node plane) pairs
+    const int tid = threadIdx.x, ty = tid >> 5, tz = tid & 31;
     const T *pin = par ? a.p1 : a.p0;
     T *pout = par ? a.p0 : a.p1;
     const T *vold = par ? a.v1 : a.v0;
@@ -134,98 +155,180 @@ k_stencil3d(Op3D<T> op, StArgs3<T> a, KState *ks, double *partials, unsigned *co
     T *yout = (MODE == M_PDIR) ? vnew : a.y;
     const long long nyz = (long long)ny * nz;
     const long long cyz = (long long)(ny + 1) * (nz + 1);
+    const T *src[3] = {MODE == M_PDIR || MODE == M_SDIR ? a.r : a.x, MODE == M_PDIR ? pin : vin, vin};
+    const T *coef[5] = {op.ax, op.ay, op.az, op.cxz, op.czx};
 
     AccT acc0, acc1, acc2;
     acc0.zero(); acc1.zero(); acc2.zero();
 
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int tzi = (int)(tile % tz);
-        const long long rest = tile / tz;
-        const int tyi = (int)(rest % ty), txi = (int)(rest / ty);
-        const int i0 = txi * T3X, j0 = tyi * T3Y, k0 = tzi * T3Z;
-        // 1. u on the tile + halo
-        for (int e = tid; e < NU3; e += 256) {
-            const int la = e / (H3Y * H3Z), rem = e - la * (H3Y * H3Z), lb = rem / H3Z, ld = rem - lb * H3Z;
-            const int gi = wrap3(i0 - 1 + la, nx), gj = wrap3(j0 - 1 + lb, ny), gk = wrap3(k0 - 1 + ld, nz);
-            T u = 0;
-            if (gi < nx && gj < ny && gk < nz) {
-                const long long g = gi * nyz + (long long)gj * nz + gk;
-                if (MODE == M_APPLY || MODE == M_RESID) {
-                    u = a.x[g];
-                } else if (MODE == M_PDIR) {
-                    const T rg = a.r[g];
-                    u = first ? rg : rg + beta * (pin[g] - omega * vin[g]);
-                    const bool owner = la >= 1 && la <= T3X && lb >= 1 && lb <= T3Y && ld >= 1 && ld <= T3Z &&
-                                       i0 - 1 + la < nx && j0 - 1 + lb < ny && k0 - 1 + ld < nz;
-                    if (owner) pout[g] = u;
-                } else {
-                    u = a.r[g] - alpha * vin[g];
-                }
+    Pref3<T, MODE, CROSS> A, B;
+    long long lo = work * blockIdx.x / gridDim.x;
+    const long long hi = work * (blockIdx.x + 1) / gridDim.x;
+    while (lo < hi) {
+        const long long tile = lo / nx;
+        const int xs = (int)(lo - tile * nx);
+        const int xe = (int)(hi - lo < nx - xs ? xs + (hi - lo) : nx);
+        lo += xe - xs;
+        const int j0 = (int)(tile / tzn) * S3Y, k0 = (int)(tile % tzn) * S3Z;
+
+        // this thread's halo nodes (own + one extra for tid < 84): shared-memory
+        // slot and y-z offset (-1: outside the domain, u = 0 there)
+        int uslot[2] = {(ty + 1) * SUZ + tz + 1, -1};
+        long long uoff[2] = {-1, -1};
+        {
+            int lb[2] = {ty + 1, 0}, ld[2] = {tz + 1, 0};
+            if (tid < SU_EXTRA) {
+                const int e = tid;
+                if (e < SUZ)                { lb[1] = 0;                   ld[1] = e; }
+                else if (e < 2 * SUZ)       { lb[1] = SUY - 1;             ld[1] = e - SUZ; }
+                else if (e < 2 * SUZ + S3Y) { lb[1] = e - 2 * SUZ + 1;     ld[1] = 0; }
+                else                        { lb[1] = e - 2 * SUZ - S3Y + 1; ld[1] = SUZ - 1; }
+                uslot[1] = lb[1] * SUZ + ld[1];
             }
-            su[e] = u;
-        }
-        __syncthreads();
-        // 2. cell fluxes
-        for (int e = tid; e < NC3; e += 256) {
-            const int la = e / (C3Y * C3Z), rem = e - la * (C3Y * C3Z), lb = rem / C3Z, ld = rem - lb * C3Z;
-            const int ci = i0 + la, cj = j0 + lb, ck = k0 + ld;
-            T fx = 0, fy = 0, fz = 0;
-            if (ci <= nx && cj <= ny && ck <= nz) {
-                const long long c = ci * cyz + (long long)cj * (nz + 1) + ck;
-                const int b0 = (la * H3Y + lb) * H3Z + ld;
-                const T c000 = su[b0], c001 = su[b0 + 1];
-                const T c010 = su[b0 + H3Z], c011 = su[b0 + H3Z + 1];
-                const T c100 = su[b0 + H3Y * H3Z], c101 = su[b0 + H3Y * H3Z + 1];
-                const T c110 = su[b0 + H3Y * H3Z + H3Z], c111 = su[b0 + H3Y * H3Z + H3Z + 1];
-                const T gx = ((c100 + c110) + (c101 + c111)) - ((c000 + c010) + (c001 + c011));
-                const T gy = ((c010 + c110) + (c011 + c111)) - ((c000 + c100) + (c001 + c101));
-                const T gz = ((c001 + c101) + (c011 + c111)) - ((c000 + c100) + (c010 + c110));
-                fx = op.ax[c] * gx;
-                fy = op.ay[c] * gy;
-                fz = op.az[c] * gz;
-                if (CROSS) {
-                    fx += op.cxz[c] * gz;
-                    fz = fz - op.czx[c] * gx;
-                }
-            }
-            sfx[e] = fx;
-            sfy[e] = fy;
-            sfz[e] = fz;
-        }
-        __syncthreads();
-        // 3. nodes: thread (ld, lb) computes x-planes la = 0..T3X-1
-        const int ld = tid & 31, lb = tid >> 5;
 #pragma unroll
-        for (int la = 0; la < T3X; ++la) {
-            const int gi = i0 + la, gj = j0 + lb, gk = k0 + ld;
-            if (gi < nx && gj < ny && gk < nz) {
-                const long long g = gi * nyz + (long long)gj * nz + gk;
-                const int c0 = (la * C3Y + lb) * C3Z + ld;                 // cell (la, lb, ld)
-                const int dx_ = C3Y * C3Z, dy_ = C3Z;
-                const T xs = ((sfx[c0 + dx_] + sfx[c0 + dx_ + dy_]) + (sfx[c0 + dx_ + 1] + sfx[c0 + dx_ + dy_ + 1])) -
-                             ((sfx[c0] + sfx[c0 + dy_]) + (sfx[c0 + 1] + sfx[c0 + dy_ + 1]));
-                const T ys = ((sfy[c0 + dy_] + sfy[c0 + dx_ + dy_]) + (sfy[c0 + dy_ + 1] + sfy[c0 + dx_ + dy_ + 1])) -
-                             ((sfy[c0] + sfy[c0 + dx_]) + (sfy[c0 + 1] + sfy[c0 + dx_ + 1]));
-                const T zs = ((sfz[c0 + 1] + sfz[c0 + dx_ + 1]) + (sfz[c0 + dy_ + 1] + sfz[c0 + dx_ + dy_ + 1])) -
-                             ((sfz[c0] + sfz[c0 + dx_]) + (sfz[c0 + dy_] + sfz[c0 + dx_ + dy_]));
-                const T u = su[((la + 1) * H3Y + lb + 1) * H3Z + ld + 1];
-                T s = (xs + ys) + zs;
-                if (HC) s += op.hc[g] * u;
-                T yv = s * op.dinv[g];
+            for (int w = 0; w < 2; ++w) {
+                const int gj = wrap3(j0 - 1 + lb[w], ny), gk = wrap3(k0 - 1 + ld[w], nz);
+                if (uslot[w] >= 0 && gj < ny && gk < nz) uoff[w] = (long long)gj * nz + gk;
+            }
+        }
+        // this thread's cells (own + one extra for tid < 41): slot and y-z offset
+        int cslot[2] = {ty * SCZ + tz, -1};
+        long long coff[2] = {-1, -1};
+        {
+            int cb[2] = {ty, 0}, cd[2] = {tz, 0};
+            if (tid < SC_EXTRA) {
+                if (tid < SCZ) { cb[1] = SCY - 1; cd[1] = tid; }
+                else           { cb[1] = tid - SCZ; cd[1] = SCZ - 1; }
+                cslot[1] = cb[1] * SCZ + cd[1];
+            }
+#pragma unroll
+            for (int w = 0; w < 2; ++w) {
+                const int cj = j0 + cb[w], ck = k0 + cd[w];
+                if (cslot[w] >= 0 && cj <= ny && ck <= nz) coff[w] = (long long)cj * (nz + 1) + ck;
+            }
+        }
+        const bool nvalid = (j0 + ty < ny) && (k0 + tz < nz);
+        const long long noff = (long long)(j0 + ty) * nz + (k0 + tz);
+
+        // loads of u plane p, cell plane c, node plane n into a register set
+        auto load_u = [&](Pref3<T, MODE, CROSS> &S, int p) {
+            if (p > xe) return;
+            const long long base = (long long)wrap3(p, nx) * nyz;
+#pragma unroll
+            for (int w = 0; w < 2; ++w) {
+                if (uoff[w] < 0) continue;
+                S.ui[0][w] = src[0][base + uoff[w]];
+                if (NI > 1 && !(MODE == M_PDIR && first)) {
+#pragma unroll
+                    for (int q = 1; q < NI; ++q) S.ui[q][w] = src[q][base + uoff[w]];
+                }
+            }
+        };
+        auto load_cf = [&](Pref3<T, MODE, CROSS> &S, int c) {
+            if (c < xs || c > xe) return;
+            const long long base = (long long)c * cyz;
+#pragma unroll
+            for (int w = 0; w < 2; ++w) {
+                if (coff[w] < 0) continue;
+#pragma unroll
+                for (int q = 0; q < NCF; ++q) S.cf[q][w] = coef[q][base + coff[w]];
+            }
+        };
+        auto load_nd = [&](Pref3<T, MODE, CROSS> &S, int n) {
+            if (n < xs || n >= xe || !nvalid) return;
+            const long long g = (long long)n * nyz + noff;
+            S.dinv = op.dinv[g];
+            if (HC) S.hc = op.hc[g];
+            if (MODE == M_RESID) S.aux = a.b[g];
+            if (MODE == M_PDIR) S.aux = a.rh[g];
+        };
+        // step i: u plane i+2 -> shared memory, cell plane i+1, node plane i-1
+        auto step = [&](Pref3<T, MODE, CROSS> &S, int i) {
+            const int p = i + 2;
+            if (p >= xs - 1 && p <= xe) {
+                T *ub = su + ((p + 4) & 3) * SUN;
+#pragma unroll
+                for (int w = 0; w < 2; ++w) {
+                    if (uslot[w] < 0) continue;
+                    T u = 0;
+                    if (uoff[w] >= 0) {
+                        if (MODE == M_APPLY || MODE == M_RESID) u = S.ui[0][w];
+                        else if (MODE == M_PDIR) u = first ? S.ui[0][w] : S.ui[0][w] + beta * (S.ui[1][w] - omega * S.ui[2][w]);
+                        else u = S.ui[0][w] - alpha * S.ui[NI - 1][w];
+                    }
+                    ub[uslot[w]] = u;
+                    if (MODE == M_PDIR && w == 0 && nvalid && p >= xs && p < xe) pout[(long long)p * nyz + noff] = u;
+                }
+            }
+            load_u(S, i + 4);
+            const int c = i + 1;
+            if (c >= xs && c <= xe) {
+                const T *u0 = su + ((c + 3) & 3) * SUN, *u1 = su + ((c + 4) & 3) * SUN;   // planes c-1, c
+                T *fb = sf + (c % SF_BUF) * (3 * SCN);
+#pragma unroll
+                for (int w = 0; w < 2; ++w) {
+                    if (cslot[w] < 0) continue;
+                    T fx = 0, fy = 0, fz = 0;
+                    if (coff[w] >= 0) {
+                        const int cb = cslot[w] / SCZ, cd = cslot[w] - cb * SCZ;
+                        const int b0 = cb * SUZ + cd;
+                        const T c000 = u0[b0], c001 = u0[b0 + 1], c010 = u0[b0 + SUZ], c011 = u0[b0 + SUZ + 1];
+                        const T c100 = u1[b0], c101 = u1[b0 + 1], c110 = u1[b0 + SUZ], c111 = u1[b0 + SUZ + 1];
+                        const T gx = ((c100 + c110) + (c101 + c111)) - ((c000 + c010) + (c001 + c011));
+                        const T gy = ((c010 + c110) + (c011 + c111)) - ((c000 + c100) + (c001 + c101));
+                        const T gz = ((c001 + c101) + (c011 + c111)) - ((c000 + c100) + (c010 + c110));
+                        fx = S.cf[0][w] * gx;
+                        fy = S.cf[1][w] * gy;
+                        fz = S.cf[2][w] * gz;
+                        if (CROSS) {
+                            fx += S.cf[3][w] * gz;
+                            fz = fz - S.cf[NCF - 1][w] * gx;
+                        }
+                    }
+                    fb[cslot[w]] = fx;
+                    fb[SCN + cslot[w]] = fy;
+                    fb[2 * SCN + cslot[w]] = fz;
+                }
+            }
+            load_cf(S, i + 3);
+            const int n = i - 1;
+            if (n >= xs && n < xe && nvalid) {
+                const T *fl = sf + (n % SF_BUF) * (3 * SCN), *fu = sf + ((n + 1) % SF_BUF) * (3 * SCN);
+                const T *flx = fl, *fly = fl + SCN, *flz = fl + 2 * SCN;
+                const T *fux = fu, *fuy = fu + SCN, *fuz = fu + 2 * SCN;
+                const int c0 = ty * SCZ + tz, dy_ = SCZ;
+                const T xs_ = ((fux[c0] + fux[c0 + dy_]) + (fux[c0 + 1] + fux[c0 + dy_ + 1])) -
+                              ((flx[c0] + flx[c0 + dy_]) + (flx[c0 + 1] + flx[c0 + dy_ + 1]));
+                const T ys_ = ((fly[c0 + dy_] + fuy[c0 + dy_]) + (fly[c0 + dy_ + 1] + fuy[c0 + dy_ + 1])) -
+                              ((fly[c0] + fuy[c0]) + (fly[c0 + 1] + fuy[c0 + 1]));
+                const T zs_ = ((flz[c0 + 1] + fuz[c0 + 1]) + (flz[c0 + dy_ + 1] + fuz[c0 + dy_ + 1])) -
+                              ((flz[c0] + fuz[c0]) + (flz[c0 + dy_] + fuz[c0 + dy_]));
+                const T u = su[((n + 4) & 3) * SUN + (ty + 1) * SUZ + tz + 1];
+                T s = (xs_ + ys_) + zs_;
+                if (HC) s += S.hc * u;
+                T yv = s * S.dinv;
                 if (MODE == M_RESID) {
-                    yv = a.b[g] - yv;
+                    yv = S.aux - yv;
                     acc0.add_prod(yv, yv);
                 } else if (MODE == M_PDIR) {
-                    acc0.add_prod(a.rh[g], yv);
+                    acc0.add_prod(S.aux, yv);
                 } else if (MODE == M_SDIR) {
                     acc0.add_prod(yv, u);
                     acc1.add_prod(yv, yv);
                     acc2.add_prod(u, u);
                 }
-                yout[g] = yv;
+                yout[(long long)n * nyz + noff] = yv;
             }
+            load_nd(S, i + 1);
+            __syncthreads();
+        };
+
+        load_u(A, xs - 1);
+        load_u(B, xs);
+        for (int i = xs - 3; i <= xe; i += 2) {
+            step(A, i);
+            if (i + 1 <= xe) step(B, i + 1);
         }
-        __syncthreads();
     }
     if (MODE == M_APPLY) return;
     double v[3] = {acc0.value(), acc1.value(), acc2.value()};
@@ -250,23 +353,35 @@ static Op3D<double> op3_of(bella_ws *ws, double *) { return make_op3<double>(ws,
 static Op3D<float> op3_of(bella_ws *ws, float *) { return make_op3<float>(ws, ws->a32, ws->dinv32, ws->hc32); }
 static Op3D<dfloat> op3_of(bella_ws *ws, dfloat *) { return make_op3<dfloat>(ws, ws->adf, ws->dinvdf, ws->hcdf); }
 
+// number of (y-z tile, node plane) pairs the stencil's runs share out
+static long long stencil3d_work(int nx, int ny, int nz) {
+    return (long long)((ny + S3Y - 1) / S3Y) * ((nz + S3Z - 1) / S3Z) * nx;
+}
+
+// an upper bound of the grid (the per-kernel grid is one resident wave, at
+// most num_sms * 8 CTAs: the reduction partials hold MAXGRID)
 int stencil3d_grid(int nx, int ny, int nz) {
-    const long long tiles = (long long)((nx + T3X - 1) / T3X) * ((ny + T3Y - 1) / T3Y) * ((nz + T3Z - 1) / T3Z);
-    const long long cap = (long long)num_sms() * 4;
-    return (int)(tiles < cap ? tiles : cap);
+    const long long work = stencil3d_work(nx, ny, nz), cap = (long long)num_sms() * 8;
+    return (int)(work < cap ? work : cap);
 }
 
 template <typename T, int MODE, bool CROSS, bool HC>
 static void launch3_one(bella_ws *ws, const StArgs3<T> &a, cudaStream_t s) {
-    static bool attr_set[64] = {false};
+    static int per_sm[64] = {0};            // resident CTAs per SM, queried once per device
     const size_t sm = smem3d_bytes<T>();
     const int dev = ws->device & 63;
-    if (!attr_set[dev]) {   // > 48 KB of dynamic shared memory needs the opt-in (set per device)
+    if (!per_sm[dev]) {
         cudaFuncSetAttribute(k_stencil3d<T, MODE, CROSS, HC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        attr_set[dev] = true;
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_stencil3d<T, MODE, CROSS, HC>, 256, sm) !=
+                cudaSuccess || occ < 1)
+            occ = 1;
+        per_sm[dev] = occ < 8 ? occ : 8;
     }
-    k_stencil3d<T, MODE, CROSS, HC><<<ws->grid_stencil, 256, sm, s>>>(op3_of(ws, (T *)nullptr), a, ws->ks,
-                                                                        ws->partials, ws->counter);
+    const long long work = stencil3d_work(ws->nx, ws->ny, ws->nz), wave = (long long)num_sms() * per_sm[dev];
+    const int grid = (int)(work < wave ? work : wave);
+    k_stencil3d<T, MODE, CROSS, HC><<<grid, 256, sm, s>>>(op3_of(ws, (T *)nullptr), a, ws->ks, ws->partials,
+                                                         ws->counter);
 }
 
 template <typename T, int MODE>
