@@ -37,6 +37,9 @@ def _random_op(rng, nx, ny, nz, walls, corrf=0.0, hc=False):
     ((9, 7, 11), (False, True, True), 0.0, False),
     ((13, 10, 40), (False, True, False), 0.4, True),
     ((37, 20, 70), (True, True, True), 0.0, True),
+    # more (y-z tile, x plane) pairs than one resident wave of CTAs: a CTA's run
+    # of planes crosses from one tile into the next
+    ((61, 41, 100), (False, True, True), 0.3, True),
 ])
 def test_apply3d_f64_f32_vs_oracle(shape, walls, corrf, hc):
     import torch
