@@ -44,6 +44,11 @@ NX, NY = 2049, 1025
 TOL = 1e-8
 MAXIT = 30000
 METRIC = "solves/s to 1e-8 residual: learned-precond vs plain BiCGStab, 1 GB300"
+# DRAM bytes read + written by one launch of a roofline kernel, from one ncu capture
+# each (the summaries in profiles/ give the commands); per launch, like `achieved`
+STENCIL3D_TRAFFIC = 211.3e6     # k_stencil3d<float, APPLY>, 257x129x257 nodes
+STENCIL2D_TRAFFIC = 134.4e6     # k_stencil2d<dfloat, PDIR>, 2049x1025 nodes
+CONV_TRAFFIC = 108.9e6          # k_conv3d_tc<32, 32>, one hidden layer at 257x129x257 nodes (2x2x2 blocked)
 WORKLOAD = "2D nodal Helmholtz 9-point solve, 2049x1025 nodes, pseudo-incompressible, rtol 1e-8, 64 seeds"
 
 
@@ -344,15 +349,18 @@ def solve2d_line(args, dev, local, rank, world, dist, steps, warmup, nseeds, e2e
     # ---- the same systems with the background-solve preconditioner (set up per step) ----
     from pybella_gb300.spectral import BackgroundSolve
     bg_stats = []
+    bg_holder = []
 
     def bg_step(i):
         w = systems[i % nseeds]
         flush.fill_(float(i))
         A = linalg.NodalHelmholtz2D(w["hplusx"], w["hplusy"], w["hcenter"], w["cor"], w["diag_inv"],
                                     NX, NY, w["dx"], w["dy"], w["x_wall"], w["y_wall"], ws=ws)
-        bg = BackgroundSolve(A)
+        # the background solve re-derived from this step's coefficients (made once, updated in place)
+        if not bg_holder:
+            bg_holder.append(BackgroundSolve(A))
+        bg = bg_holder[0].update(A)
         x, st = A.solve(w["b"], tol=TOL, maxiter=MAXIT, preconditioner=bg, out=xbuf)
-        bg.close()
         bg_stats.append(st)
 
     for i in range(warmup):
@@ -379,7 +387,10 @@ def solve2d_line(args, dev, local, rank, world, dist, steps, warmup, nseeds, e2e
                 "d2h_bytes_per_step": d2h, "path": "pybella_gb300.linalg.bicgstab on NumPy operands"},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "frac": (achieved / peak) if achieved else None,
+                     "traffic": STENCIL2D_TRAFFIC if args.precision == "df64" else None,
+                     "traffic_source": "ncu dram bytes read + written of one launch "
+                                       "(profiles/stencil2d_df64_pdir_2049x1025_ncu.md)",
                      "kernel": "k_stencil2d<%s, PDIR>" % {"fp64": "double", "mixed": "float", "df64": "dfloat"}[args.precision],
                      "peak_source": peak_kind,
                      "alg_bytes_per_launch": alg_bytes},
@@ -689,17 +700,19 @@ def run_learned3d(args):
     xs = {k: torch.zeros(A.n, dtype=torch.float64, device=dev)
           for k in ("plain", "background", "background_fgmres", "learned")}
 
+    bg_keep = BackgroundSolve(A)                     # made once; every step re-derives it in place
+
     def step(name):
         if name == "plain":
             return A.solve(b, tol=TOL, maxiter=200000, precision="df64", out=xs[name])[1]
-        bg = BackgroundSolve(A)                      # set up from this step's coefficients
+        l0 = bg_keep.launches()
+        bg = bg_keep.update(A)                       # from this step's coefficients
         pc = bg if name.startswith("background") else learned.LearnedPreconditioner(bg, net, "post")
         kw = dict(method="bicgstab") if name == "background" else kw_learned
         with warnings.catch_warnings():
             warnings.simplefilter("ignore", RuntimeWarning)
             st = A.solve(b, tol=TOL, maxiter=20000, preconditioner=pc, out=xs[name], **kw)[1]
-        bg_launches[0] += bg.launches()
-        bg.close()
+        bg_launches[0] += bg.launches() - l0
         return st
 
     def timed(name, nw, ns, sample_clocks=False):
@@ -779,6 +792,12 @@ def run_learned3d(args):
 
     cnn_ms = ev_ms(lambda: net.forward(r32, shape, scale=1.0, out=y32))
     bg_ms = ev_ms(lambda: bg.apply(r32, out=y32))
+    # the FGMRES iteration's FP32 matvec (k_stencil3d<float, APPLY>), back to back:
+    # its 204 MB working set is larger than L2.  Algorithmic bytes: x, y, diag_inv
+    # per node, the three axis coefficients per cell, 4 bytes each.
+    st_ms = ev_ms(lambda: A.matvec_f32(r32), k=20)
+    ncell = (shape[0] + 1) * (shape[1] + 1) * (shape[2] + 1)
+    st_bytes = A.n * 3 * 4 + ncell * 3 * 4
     nv = learned.net_voxels(shape, 2)
     cnn_flops = nv * 2 * 27 * (8 * 32 + 4 * 32 * 32 + 32 * 8)      # 8 sub-node channels in and out
     napp = L["stats"][-1]["iterations"]
@@ -793,8 +812,10 @@ def run_learned3d(args):
                "kind": "port",
                "sample": "%d iterations of plain FP64 BiCGStab (the oracle's C restatement of lap3D and scipy's "
                          "loop, OpenMP on %d host threads) on the full grid, %.1f ms each, times the %d iterations "
-                         "the same algorithm took on the GPU in this run" % (k, nthr, per_it * 1e3,
-                                                                            P["stats"][-1]["iterations"])}
+                         "the GPU's plain BiCGStab (scipy's control flow in double-float arithmetic) took on this "
+                         "system in this run: extrapolated; the count of this ill-conditioned iteration depends on "
+                         "rounding (the reference arm fits FP64 solves on smaller grids instead)"
+                         % (k, nthr, per_it * 1e3, P["stats"][-1]["iterations"])}
     stats = lambda R: {"solves_per_s": 1000.0 / R["ms"], "ms": R["ms"], "iterations": R["stats"][-1]["iterations"],
                        "outer": R["stats"][-1]["outer"], "relres": R["stats"][-1]["relres"],
                        "fallback": R["stats"][-1]["fallback"], "status": R["stats"][-1]["status"]}
@@ -822,10 +843,20 @@ def run_learned3d(args):
                  "d2h_bytes_per_step": A.n * 8} if e2e_ms else None),
         "gpu_launches": L["launches"],
         "roofline": {"bound": "tensor", "achieved": ach, "peak": tpeak, "unit": "TFLOP/s", "frac": ach / tpeak,
-                     "traffic": None, "kernel": "k_conv3d_tc x6 (one network application)",
+                     "traffic": CONV_TRAFFIC,
+                     "traffic_source": "ncu dram bytes read + written of one hidden-layer launch (one of the "
+                                       "six; profiles/conv3d_tc_ws_bf16_257x129x257_ncu.md)",
+                     "kernel": "k_conv3d_tc x6 (one network application)",
                      "peak_source": pkind + " bf16 sustained", "flops_per_launch": cnn_flops,
                      "ms_per_application": cnn_ms, "applications_per_solve": napp,
                      "background_apply_ms": bg_ms},
+        "stencil_roofline": {"bound": "hbm", "kernel": "k_stencil3d<float, APPLY> (the FP32 matvec of each "
+                                                      "FGMRES iteration)",
+                             "achieved": st_bytes / (st_ms / 1000.0) / 1e9, "peak": hbm, "unit": "GB/s",
+                             "frac": st_bytes / (st_ms / 1000.0) / 1e9 / hbm, "us_per_launch": st_ms * 1000.0,
+                             "alg_bytes_per_launch": st_bytes, "traffic": STENCIL3D_TRAFFIC,
+                             "traffic_source": "ncu dram bytes read + written of one launch at this size "
+                                               "(profiles/stencil3d_f32_apply_257x129x257_ncu.md)"},
         "clocks": L["clocks"],
     }
     if cpu:

@@ -91,7 +91,8 @@ typedef struct bella_solve_opts {
     double atol;             /* absolute floor (0 = none)                    */
     int    maxiter;          /* inner BiCGStab iteration limit (total)       */
     int    precision;        /* 0: FP64 BiCGStab;  1: FP32 inner solves in FP64
-                                iterative refinement, FP64 fallback;
+                                iterative refinement, double-float fallback
+                                accepted on the FP64 true residual only;
                                 2: double-float BiCGStab (FP32-pair vectors
                                 and arithmetic, ~48-bit, on the FP32 pipe)   */
     int    x0_zero;          /* 1: start from x = 0 (x is output only)       */
@@ -447,6 +448,13 @@ int       bella_spectral3d_create(bella_spectral3d **sp, const bella_op3d *op, i
  * bella_spectral3d_apply / _destroy / bella_fbicgstab_pc / bella_fgmres_pc (no
  * network in 2D). */
 int       bella_spectral2d_create(bella_spectral3d **sp, const bella_op2d *op, int device, void *stream);
+/* Re-derive an existing background solve from new coefficients of an operator of
+ * the same shape and boundary kinds (a new time step): means, 1/diag_inv and the
+ * tridiagonal factors are recomputed in place, nothing is allocated, and the
+ * call waits for the device only when op has an hcenter term.  BELLA_EINVAL when
+ * the shape, a boundary kind or the dimension (2D/3D) differs from create's. */
+int       bella_spectral3d_update(bella_spectral3d *sp, const bella_op3d *op, void *stream);
+int       bella_spectral2d_update(bella_spectral3d *sp, const bella_op2d *op, void *stream);
 int       bella_spectral3d_destroy(bella_spectral3d *sp);
 int       bella_spectral3d_apply(bella_spectral3d *sp, const float *in, float *out, void *stream);
 long long bella_spectral3d_launches(const bella_spectral3d *sp);

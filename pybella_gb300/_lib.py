@@ -203,6 +203,8 @@ SIGNATURES = {
                                                ctypes.c_void_p]),
     "bella_spectral2d_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Op2D), ctypes.c_int,
                                                ctypes.c_void_p]),
+    "bella_spectral3d_update": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Op3D), ctypes.c_void_p]),
+    "bella_spectral2d_update": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Op2D), ctypes.c_void_p]),
     "bella_spectral3d_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "bella_spectral3d_apply": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, ctypes.c_void_p]),
     "bella_spectral3d_launches": (ctypes.c_longlong, [ctypes.c_void_p]),

@@ -254,6 +254,9 @@ struct bella_ws {
     // scratch of the device projection (bella_projection2d)
     double *proj_buf;
     size_t proj_cap;
+    // the background solve of the device projections, kept between calls and
+    // re-derived in place from each call's coefficients
+    bella_spectral3d *sp_cache;
     // optional per-kernel timing with CUDA events (bella_ws_profile)
     int prof;
     struct Prof {

@@ -423,6 +423,7 @@ int bella_ws_destroy(bella_ws *ws) {
     if (!ws) return BELLA_OK;
     cudaSetDevice(ws->device);
     if (ws->prof) bella_ws_profile(ws, 0);
+    bella_spectral3d_destroy(ws->sp_cache);
     free_op(ws);
     cudaFree(ws->proj_buf);
     cudaFree(ws->fg_v);
@@ -574,10 +575,12 @@ int bella_op3d_set(bella_ws *ws, const bella_op3d *op, void *stream) {
         return set_err(BELLA_EINVAL, "bella_op3d_set: hplusx, hplusy, hplusz, diag_inv are required");
     if (!(op->dx > 0.0) || !(op->dy > 0.0) || !(op->dz > 0.0))
         return set_err(BELLA_EINVAL, "bella_op3d_set: dx, dy, dz must be > 0");
+    const size_t ncell = (size_t)(op->nx + 1) * (op->ny + 1) * (op->nz + 1);
+    if (ncell >= (size_t)1 << 31)   // the stencil indexes nodes and cells with 32-bit offsets
+        return set_err(BELLA_EINVAL, "bella_op3d_set: (nx+1)(ny+1)(nz+1) must be below 2^31");
     BELLA_CUDA(cudaSetDevice(ws->device));
     cudaStream_t s = (cudaStream_t)stream;
     const long long n = (long long)op->nx * op->ny * op->nz;
-    const size_t ncell = (size_t)(op->nx + 1) * (op->ny + 1) * (op->nz + 1);
     if (ws->ndim != 3 || ws->nx != op->nx || ws->ny != op->ny || ws->nz != op->nz) {
         free_op(ws);
         BELLA_CUDA(cudaMalloc(&ws->a64, 5 * ncell * sizeof(double)));
@@ -857,6 +860,7 @@ int bella_bicgstab(bella_ws *ws, const double *b, double *x, const bella_solve_o
     const long long n = ws->n;
     const int gv = ws->grid_vec;
     int rc, timed_out = 0;
+    double rn_known = -1.0;                           // >= 0: ||b - A x|| of the returned x, measured
 
     if (o.precision == 0) {
         rc = solve_fp64(ws, b, x, o, o.x0_zero ? 0 : 1, o.maxiter, &st, s, t0);
@@ -886,11 +890,16 @@ int bella_bicgstab(bella_ws *ws, const double *b, double *x, const bella_solve_o
             NullSpace ns = ws->ns;
             if (!o.project_null) ns.nm = 0;
             const bool proj = ns.nm > 0;
-            op_resid(ws, 0, x, b, ws->r64, s);
-            rc = sync_state(ws, s);
-            if (rc != BELLA_OK) return rc;
-            double rnorm = sqrt(ws->ks_host->dot_aux2);
-            st.matvecs = 1;
+            double rnorm = bnorm;
+            if (o.x0_zero) {                          // r = b - A 0 = b exactly: no stencil
+                BELLA_CUDA(cudaMemcpyAsync(ws->r64, b, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            } else {
+                op_resid(ws, 0, x, b, ws->r64, s);
+                rc = sync_state(ws, s);
+                if (rc != BELLA_OK) return rc;
+                rnorm = sqrt(ws->ks_host->dot_aux2);
+                st.matvecs = 1;
+            }
             st.status = BELLA_MAXITER;
             int total = 0;
             bool failed = false;
@@ -922,6 +931,13 @@ int bella_bicgstab(bella_ws *ws, const double *b, double *x, const bella_solve_o
                 k_ir_update<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->x32, rnorm, ws->z64, ns, ws->ks,
                                                      ws->partials, ws->counter);
                 ws->launches++;
+                // keep x in the operator's range (A e_k = 0 exactly), before the
+                // residual is measured: the shift's rounding moves the FP64 residual
+                // by about eps * cond(A), so the residual tested is the returned x's
+                if (proj) {
+                    k_null_shift<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->ks, ns);
+                    ws->launches++;
+                }
                 op_resid(ws, 0, x, b, ws->r64, s);
                 st.matvecs += 1;
                 rc = sync_state(ws, s);
@@ -933,29 +949,31 @@ int bella_bicgstab(bella_ws *ws, const double *b, double *x, const bella_solve_o
                     failed = true;
                     break;
                 }
-                if (proj) {   // keep x in the operator's range (A e_k = 0 exactly)
-                    k_null_shift<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->ks, ns);
-                    ws->launches++;
-                }
                 rnorm = rnew;
             }
             st.iterations = total;
             if (failed) {
-                // FP64 fallback from the FP64 iterate, reported in stats.fallback
+                // fallback from the FP64 iterate, reported in stats.fallback: double-float
+                // BiCGStab, which accepts convergence only on the FP64 true residual
                 st.fallback = 1;
                 const int left = o.maxiter - total;
-                rc = solve_fp64(ws, b, x, o, 1, left > 0 ? left : 0, &st, s, t0);
+                rc = solve_df(ws, b, x, o, 1, left > 0 ? left : 0, &st, s, t0);
                 if (rc != BELLA_OK) return rc;
+            } else {
+                rn_known = rnorm;                     // the loop measured the returned x's residual last
             }
         }
     }
 done:
     {
         // true FP64 residual of the returned x
-        op_resid(ws, 0, x, b, ws->r64, s);
-        rc = sync_state(ws, s);
-        if (rc != BELLA_OK) return rc;
-        const double rn = sqrt(ws->ks_host->dot_aux2);
+        double rn = rn_known;
+        if (!(rn >= 0.0)) {
+            op_resid(ws, 0, x, b, ws->r64, s);
+            rc = sync_state(ws, s);
+            if (rc != BELLA_OK) return rc;
+            rn = sqrt(ws->ks_host->dot_aux2);
+        }
         st.relres = st.bnorm > 0 ? rn / st.bnorm : rn;
         if (!isfinite(rn)) st.status = BELLA_NONFINITE;
     }
@@ -1427,20 +1445,26 @@ static int fbicgstab_impl(bella_ws *ws, const bella::Precond &pc, const double *
     double target = o.tol * bnorm;
     if (o.atol > target) target = o.atol;
     bool failed = false;
+    double rn_known = -1.0;                           // >= 0: ||b - A x|| of the current x, measured
     if (!isfinite(bnorm)) {
         st.status = BELLA_NONFINITE;
     } else if (o.x0_zero && (bnorm == 0.0 || bnorm <= o.tol)) {   // scipy 1.7 legacy exit
         BELLA_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
         st.status = BELLA_OK;
     } else {
-        if (o.x0_zero) BELLA_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
         NullSpace ns = ws->ns;
         if (!o.project_null) ns.nm = 0;
-        op_resid(ws, 0, x, b, ws->r64, s);
-        rc = sync_state(ws, s);
-        if (rc != BELLA_OK) return rc;
-        double rnorm = sqrt(ws->ks_host->dot_aux2);
-        st.matvecs = 1;
+        double rnorm = bnorm;
+        if (o.x0_zero) {                              // r = b - A 0 = b exactly: no stencil
+            BELLA_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
+            BELLA_CUDA(cudaMemcpyAsync(ws->r64, b, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        } else {
+            op_resid(ws, 0, x, b, ws->r64, s);
+            rc = sync_state(ws, s);
+            if (rc != BELLA_OK) return rc;
+            rnorm = sqrt(ws->ks_host->dot_aux2);
+            st.matvecs = 1;
+        }
         int total = 0;
         for (int outer = 0;; ++outer) {
             if (!isfinite(rnorm)) { st.status = BELLA_NONFINITE; failed = true; break; }
@@ -1481,6 +1505,10 @@ static int fbicgstab_impl(bella_ws *ws, const bella::Precond &pc, const double *
             k_ir_update<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->x32, rnorm, ws->z64, ns, ws->ks, ws->partials,
                                                  ws->counter);
             ws->launches++;
+            if (ns.nm > 0) {   // range projection before the residual is measured (as in the plain loop)
+                k_null_shift<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->ks, ns);
+                ws->launches++;
+            }
             op_resid(ws, 0, x, b, ws->r64, s);
             st.matvecs += 1;
             rc = sync_state(ws, s);
@@ -1490,10 +1518,6 @@ static int fbicgstab_impl(bella_ws *ws, const bella::Precond &pc, const double *
                 BELLA_CUDA(cudaMemcpyAsync(x, ws->x64v, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
                 failed = true;
                 break;
-            }
-            if (ns.nm > 0) {
-                k_null_shift<<<gv, VEC_BLOCK, 0, s>>>(n, x, ws->ks, ns);
-                ws->launches++;
             }
             rnorm = rnew;
         }
@@ -1510,12 +1534,17 @@ static int fbicgstab_impl(bella_ws *ws, const bella::Precond &pc, const double *
             st.iterations += fs.iterations;
             st.matvecs += fs.matvecs;
             st.detail = fs.detail;
+        } else {
+            rn_known = rnorm;                         // the loop measured the returned x's residual last
         }
     }
-    op_resid(ws, 0, x, b, ws->r64, s);
-    rc = sync_state(ws, s);
-    if (rc != BELLA_OK) return rc;
-    const double rn = sqrt(ws->ks_host->dot_aux2);
+    double rn = rn_known;
+    if (!(rn >= 0.0)) {                               // true FP64 residual of the returned x
+        op_resid(ws, 0, x, b, ws->r64, s);
+        rc = sync_state(ws, s);
+        if (rc != BELLA_OK) return rc;
+        rn = sqrt(ws->ks_host->dot_aux2);
+    }
     st.relres = st.bnorm > 0 ? rn / st.bnorm : rn;
     if (!isfinite(rn)) st.status = BELLA_NONFINITE;
     BELLA_CUDA(cudaGetLastError());

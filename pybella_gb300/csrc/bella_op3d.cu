@@ -22,8 +22,13 @@
 // (j0 + ty, k0 + tz)) and marches through a run of node planes [xs, xe).
 // Step i of a run stores u plane i+2 with its one-node y-z halo (10 x 34;
 // u is formed on the fly from the Krylov vectors), computes the 9 x 33 cell
-// fluxes of cell plane i+1 and finishes node plane i-1.  Four u planes and
-// three flux planes rotate in shared memory, so the three phases of a step
+// fluxes of cell plane i+1 and finishes node plane i-1.  The x direction is
+// summed once per plane and carried in registers: a cell's gradients are
+// differences and sums of its two u faces, each face's sums computed once
+// (Gx = S(face x) - S(face x-1), Gy = Y(x-1) + Y(x), Gz = Z(x-1) + Z(x)), and a
+// node's sums are differences and sums of its two cell planes' flux partials
+// (xs = X(n+1) - X(n), ys = Y(n) + Y(n+1), zs = Z(n) + Z(n+1)).  Four u planes
+// and two flux planes rotate in shared memory, so the three phases of a step
 // touch disjoint buffers and one barrier per step suffices.  Every global
 // load is issued two steps before its use (register sets A and B serve
 // alternate steps), which keeps enough bytes in flight per SM to cover the
@@ -38,7 +43,7 @@ constexpr int SUY = S3Y + 2, SUZ = S3Z + 2, SUN = SUY * SUZ;    // u plane with 
 constexpr int SCY = S3Y + 1, SCZ = S3Z + 1, SCN = SCY * SCZ;    // cell plane: 9 x 33
 constexpr int SU_EXTRA = SUN - 256;                             // 84 halo nodes beyond one per thread
 constexpr int SC_EXTRA = SCN - 256;                             // 41 edge cells beyond one per thread
-constexpr int SU_BUF = 4, SF_BUF = 3;                           // rotating u and flux planes
+constexpr int SU_BUF = 4, SF_BUF = 2;                           // rotating u and flux planes
 
 template <typename T>
 struct Op3D {
@@ -57,6 +62,8 @@ struct StArgs3 {
 
 template <typename T>
 size_t smem3d_bytes() { return sizeof(T) * (SU_BUF * SUN + SF_BUF * 3 * SCN); }
+
+template <bool B> struct Chk { static constexpr bool value = B; };
 
 // number of input vectors u is formed from: x (APPLY, RESID), r p v (PDIR), r v (SDIR)
 template <int MODE> struct In3 { static constexpr int n = MODE == M_PDIR ? 3 : MODE == M_SDIR ? 2 : 1; };
@@ -123,8 +130,13 @@ __device__ __forceinline__ int wrap3(int g, int n) {
 }
 
 // ---- fused stencil ---------------------------------------------------------------
+// double and double-float: at least 2 resident CTAs per SM (at most 128 registers
+// a thread; measured 0.74 vs 0.86 ms per double-float iteration at 257x129x257).
+// FP32: no minimum (0), where the compiler keeps the matvec at 64 registers and 4
+// CTAs per SM (69 us at 257x129x257); a minimum of 1 or 2 let it take 108
+// registers, 2 CTAs per SM and 89 us.
 template <typename T, int MODE, bool CROSS, bool HC>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 0 : 2)
 k_stencil3d(Op3D<T> op, StArgs3<T> a, KState *ks, double *partials, unsigned *counter) {
     using AccT = typename Acc<T>::type;
     constexpr int NI = In3<MODE>::n, NCF = CROSS ? 5 : 3;
@@ -132,17 +144,12 @@ k_stencil3d(Op3D<T> op, StArgs3<T> a, KState *ks, double *partials, unsigned *co
     T *su = reinterpret_cast<T *>(smem_raw);          // [SU_BUF][SUY][SUZ]
     T *sf = su + SU_BUF * SUN;                        // [SF_BUF][Fx, Fy, Fz][SCY][SCZ]
 
-    int par = 0;
-    bool first = false;
-    T alpha = 0, beta = 0, omega = 0;
-    if (MODE == M_PDIR || MODE == M_SDIR) {
-        if (ks->done) return;
-        par = ks->iter & 1;
-        first = (ks->iter == 0);
-        alpha = (T)ks->alpha;
-        beta = (T)ks->beta;
-        omega = (T)ks->omega;
-    }
+    constexpr bool KRYLOV = MODE == M_PDIR || MODE == M_SDIR;
+    if (KRYLOV && ks->done) return;
+    const int par = KRYLOV ? (ks->iter & 1) : 0;
+    const bool first = KRYLOV && ks->iter == 0;
+    const T alpha = KRYLOV ? (T)ks->alpha : T(0), beta = KRYLOV ? (T)ks->beta : T(0),
+            omega = KRYLOV ? (T)ks->omega : T(0);
     const int nx = op.nx, ny = op.ny, nz = op.nz;
     const int tyn = (ny + S3Y - 1) / S3Y, tzn = (nz + S3Z - 1) / S3Z;
     const long long work = (long long)tyn * tzn * nx;          // (y-z tile, node plane) pairs
@@ -153,8 +160,8 @@ k_stencil3d(Op3D<T> op, StArgs3<T> a, KState *ks, double *partials, unsigned *co
     T *vnew = par ? a.v0 : a.v1;
     const T *vin = (MODE == M_PDIR) ? vold : vnew;
     T *yout = (MODE == M_PDIR) ? vnew : a.y;
-    const long long nyz = (long long)ny * nz;
-    const long long cyz = (long long)(ny + 1) * (nz + 1);
+    const int nyz = ny * nz;                          // node and cell counts are below 2^31 (host check)
+    const int cyz = (ny + 1) * (nz + 1);
     const T *src[3] = {MODE == M_PDIR || MODE == M_SDIR ? a.r : a.x, MODE == M_PDIR ? pin : vin, vin};
     const T *coef[5] = {op.ax, op.ay, op.az, op.cxz, op.czx};
 
@@ -171,49 +178,59 @@ k_stencil3d(Op3D<T> op, StArgs3<T> a, KState *ks, double *partials, unsigned *co
         lo += xe - xs;
         const int j0 = (int)(tile / tzn) * S3Y, k0 = (int)(tile % tzn) * S3Z;
 
-        // this thread's halo nodes (own + one extra for tid < 84): shared-memory
-        // slot and y-z offset (-1: outside the domain, u = 0 there)
-        int uslot[2] = {(ty + 1) * SUZ + tz + 1, -1};
-        long long uoff[2] = {-1, -1};
+        // this thread's halo nodes: its own and, for tid < 84, one of the halo ring;
+        // shared-memory slot and y-z offset (-1: outside the domain, u = 0 there)
+        int uslot[2] = {(ty + 1) * SUZ + tz + 1, -1}, uoff[2] = {-1, -1};
         {
             int lb[2] = {ty + 1, 0}, ld[2] = {tz + 1, 0};
             if (tid < SU_EXTRA) {
                 const int e = tid;
-                if (e < SUZ)                { lb[1] = 0;                   ld[1] = e; }
-                else if (e < 2 * SUZ)       { lb[1] = SUY - 1;             ld[1] = e - SUZ; }
-                else if (e < 2 * SUZ + S3Y) { lb[1] = e - 2 * SUZ + 1;     ld[1] = 0; }
+                if (e < SUZ)                { lb[1] = 0;                     ld[1] = e; }
+                else if (e < 2 * SUZ)       { lb[1] = SUY - 1;               ld[1] = e - SUZ; }
+                else if (e < 2 * SUZ + S3Y) { lb[1] = e - 2 * SUZ + 1;       ld[1] = 0; }
                 else                        { lb[1] = e - 2 * SUZ - S3Y + 1; ld[1] = SUZ - 1; }
                 uslot[1] = lb[1] * SUZ + ld[1];
             }
 #pragma unroll
             for (int w = 0; w < 2; ++w) {
                 const int gj = wrap3(j0 - 1 + lb[w], ny), gk = wrap3(k0 - 1 + ld[w], nz);
-                if (uslot[w] >= 0 && gj < ny && gk < nz) uoff[w] = (long long)gj * nz + gk;
+                if (uslot[w] >= 0 && gj < ny && gk < nz) uoff[w] = gj * nz + gk;
             }
         }
-        // this thread's cells (own + one extra for tid < 41): slot and y-z offset
-        int cslot[2] = {ty * SCZ + tz, -1};
-        long long coff[2] = {-1, -1};
+        // this thread's cells: its own and, for the last 41 threads, one of the
+        // tile's far edges; flux slot, slot of the cell's (y, z) = (0, 0) corner
+        // node in the u plane, y-z offset of the cell (-1: outside, flux 0)
+        int cslot[2] = {ty * SCZ + tz, -1}, cu[2] = {ty * SUZ + tz, 0}, coff[2] = {-1, -1};
         {
             int cb[2] = {ty, 0}, cd[2] = {tz, 0};
-            if (tid < SC_EXTRA) {
-                if (tid < SCZ) { cb[1] = SCY - 1; cd[1] = tid; }
-                else           { cb[1] = tid - SCZ; cd[1] = SCZ - 1; }
+            if (tid >= 256 - SC_EXTRA) {
+                const int e = tid - (256 - SC_EXTRA);
+                if (e < SCZ) { cb[1] = SCY - 1; cd[1] = e; }
+                else         { cb[1] = e - SCZ; cd[1] = SCZ - 1; }
                 cslot[1] = cb[1] * SCZ + cd[1];
+                cu[1] = cb[1] * SUZ + cd[1];
             }
 #pragma unroll
             for (int w = 0; w < 2; ++w) {
                 const int cj = j0 + cb[w], ck = k0 + cd[w];
-                if (cslot[w] >= 0 && cj <= ny && ck <= nz) coff[w] = (long long)cj * (nz + 1) + ck;
+                if (cslot[w] >= 0 && cj <= ny && ck <= nz) coff[w] = cj * (nz + 1) + ck;
             }
         }
         const bool nvalid = (j0 + ty < ny) && (k0 + tz < nz);
-        const long long noff = (long long)(j0 + ty) * nz + (k0 + tz);
+        const int noff = (j0 + ty) * nz + (k0 + tz);
+        const int c0 = ty * SCZ + tz, uc = (ty + 1) * SUZ + tz + 1;
 
-        // loads of u plane p, cell plane c, node plane n into a register set
-        auto load_u = [&](Pref3<T, MODE, CROSS> &S, int p) {
-            if (p > xe) return;
-            const long long base = (long long)wrap3(p, nx) * nyz;
+        // sums carried from one plane to the next: per cell, the previous u plane's
+        // face sums (S: the four nodes, Y: the y+1 pair minus the y pair, Z: the
+        // z+1 pair minus the z pair); per node, the previous cell plane's flux
+        // partials (X: sum of the four cells' Fx, Y/Z: the upper minus the lower pair)
+        T fS[2], fY[2], fZ[2], nX, nY, nZ;
+
+        // the run's interior steps (xs+1 <= i <= xe-4) have every phase active and
+        // every plane in range: they are instantiated with CK = false and no checks
+        auto load_u = [&](Pref3<T, MODE, CROSS> &S, int p, auto CK) {
+            if (decltype(CK)::value && p > xe) return;
+            const int base = wrap3(p, nx) * nyz;
 #pragma unroll
             for (int w = 0; w < 2; ++w) {
                 if (uoff[w] < 0) continue;
@@ -224,9 +241,9 @@ k_stencil3d(Op3D<T> op, StArgs3<T> a, KState *ks, double *partials, unsigned *co
                 }
             }
         };
-        auto load_cf = [&](Pref3<T, MODE, CROSS> &S, int c) {
-            if (c < xs || c > xe) return;
-            const long long base = (long long)c * cyz;
+        auto load_cf = [&](Pref3<T, MODE, CROSS> &S, int c, auto CK) {
+            if (decltype(CK)::value && (c < xs || c > xe)) return;
+            const int base = c * cyz;
 #pragma unroll
             for (int w = 0; w < 2; ++w) {
                 if (coff[w] < 0) continue;
@@ -234,18 +251,20 @@ k_stencil3d(Op3D<T> op, StArgs3<T> a, KState *ks, double *partials, unsigned *co
                 for (int q = 0; q < NCF; ++q) S.cf[q][w] = coef[q][base + coff[w]];
             }
         };
-        auto load_nd = [&](Pref3<T, MODE, CROSS> &S, int n) {
-            if (n < xs || n >= xe || !nvalid) return;
-            const long long g = (long long)n * nyz + noff;
+        auto load_nd = [&](Pref3<T, MODE, CROSS> &S, int n, auto CK) {
+            if ((decltype(CK)::value && (n < xs || n >= xe)) || !nvalid) return;
+            const int g = n * nyz + noff;
             S.dinv = op.dinv[g];
             if (HC) S.hc = op.hc[g];
             if (MODE == M_RESID) S.aux = a.b[g];
             if (MODE == M_PDIR) S.aux = a.rh[g];
         };
-        // step i: u plane i+2 -> shared memory, cell plane i+1, node plane i-1
-        auto step = [&](Pref3<T, MODE, CROSS> &S, int i) {
+        // step i: u plane i+2 -> shared memory; face sums of u plane i+1 and the
+        // fluxes of cell plane i+1; flux partials of cell plane i and node plane i-1
+        auto step = [&](Pref3<T, MODE, CROSS> &S, int i, auto CK) {
+            constexpr bool chk = decltype(CK)::value;
             const int p = i + 2;
-            if (p >= xs - 1 && p <= xe) {
+            if (!chk || (p >= xs - 1 && p <= xe)) {
                 T *ub = su + ((p + 4) & 3) * SUN;
 #pragma unroll
                 for (int w = 0; w < 2; ++w) {
@@ -257,77 +276,89 @@ k_stencil3d(Op3D<T> op, StArgs3<T> a, KState *ks, double *partials, unsigned *co
                         else u = S.ui[0][w] - alpha * S.ui[NI - 1][w];
                     }
                     ub[uslot[w]] = u;
-                    if (MODE == M_PDIR && w == 0 && nvalid && p >= xs && p < xe) pout[(long long)p * nyz + noff] = u;
+                    if (MODE == M_PDIR && w == 0 && nvalid && (!chk || (p >= xs && p < xe))) pout[p * nyz + noff] = u;
                 }
             }
-            load_u(S, i + 4);
-            const int c = i + 1;
-            if (c >= xs && c <= xe) {
-                const T *u0 = su + ((c + 3) & 3) * SUN, *u1 = su + ((c + 4) & 3) * SUN;   // planes c-1, c
-                T *fb = sf + (c % SF_BUF) * (3 * SCN);
+            load_u(S, i + 4, CK);
+            const int q = i + 1;                      // u plane of the faces; cell plane q spans u planes q-1, q
+            if (!chk || (q >= xs - 1 && q <= xe)) {
+                const T *ub = su + ((q + 4) & 3) * SUN;
+                T *fb = sf + (q & 1) * (3 * SCN);
 #pragma unroll
                 for (int w = 0; w < 2; ++w) {
                     if (cslot[w] < 0) continue;
-                    T fx = 0, fy = 0, fz = 0;
-                    if (coff[w] >= 0) {
-                        const int cb = cslot[w] / SCZ, cd = cslot[w] - cb * SCZ;
-                        const int b0 = cb * SUZ + cd;
-                        const T c000 = u0[b0], c001 = u0[b0 + 1], c010 = u0[b0 + SUZ], c011 = u0[b0 + SUZ + 1];
-                        const T c100 = u1[b0], c101 = u1[b0 + 1], c110 = u1[b0 + SUZ], c111 = u1[b0 + SUZ + 1];
-                        const T gx = ((c100 + c110) + (c101 + c111)) - ((c000 + c010) + (c001 + c011));
-                        const T gy = ((c010 + c110) + (c011 + c111)) - ((c000 + c100) + (c001 + c101));
-                        const T gz = ((c001 + c101) + (c011 + c111)) - ((c000 + c100) + (c010 + c110));
-                        fx = S.cf[0][w] * gx;
-                        fy = S.cf[1][w] * gy;
-                        fz = S.cf[2][w] * gz;
-                        if (CROSS) {
-                            fx += S.cf[3][w] * gz;
-                            fz = fz - S.cf[NCF - 1][w] * gx;
+                    const int b0 = cu[w];
+                    const T u00 = ub[b0], u01 = ub[b0 + 1], u10 = ub[b0 + SUZ], u11 = ub[b0 + SUZ + 1];
+                    const T pj = u00 + u01, pj1 = u10 + u11;
+                    const T s_ = pj + pj1, y_ = pj1 - pj, z_ = (u01 + u11) - (u00 + u10);
+                    if (!chk || q >= xs) {
+                        T fx = 0, fy = 0, fz = 0;
+                        if (coff[w] >= 0) {
+                            const T gx = s_ - fS[w], gy = fY[w] + y_, gz = fZ[w] + z_;
+                            fx = S.cf[0][w] * gx;
+                            fy = S.cf[1][w] * gy;
+                            fz = S.cf[2][w] * gz;
+                            if (CROSS) {
+                                fx += S.cf[3][w] * gz;
+                                fz = fz - S.cf[NCF - 1][w] * gx;
+                            }
                         }
+                        fb[cslot[w]] = fx;
+                        fb[SCN + cslot[w]] = fy;
+                        fb[2 * SCN + cslot[w]] = fz;
                     }
-                    fb[cslot[w]] = fx;
-                    fb[SCN + cslot[w]] = fy;
-                    fb[2 * SCN + cslot[w]] = fz;
+                    fS[w] = s_; fY[w] = y_; fZ[w] = z_;
                 }
             }
-            load_cf(S, i + 3);
-            const int n = i - 1;
-            if (n >= xs && n < xe && nvalid) {
-                const T *fl = sf + (n % SF_BUF) * (3 * SCN), *fu = sf + ((n + 1) % SF_BUF) * (3 * SCN);
-                const T *flx = fl, *fly = fl + SCN, *flz = fl + 2 * SCN;
-                const T *fux = fu, *fuy = fu + SCN, *fuz = fu + 2 * SCN;
-                const int c0 = ty * SCZ + tz, dy_ = SCZ;
-                const T xs_ = ((fux[c0] + fux[c0 + dy_]) + (fux[c0 + 1] + fux[c0 + dy_ + 1])) -
-                              ((flx[c0] + flx[c0 + dy_]) + (flx[c0 + 1] + flx[c0 + dy_ + 1]));
-                const T ys_ = ((fly[c0 + dy_] + fuy[c0 + dy_]) + (fly[c0 + dy_ + 1] + fuy[c0 + dy_ + 1])) -
-                              ((fly[c0] + fuy[c0]) + (fly[c0 + 1] + fuy[c0 + 1]));
-                const T zs_ = ((flz[c0 + 1] + fuz[c0 + 1]) + (flz[c0 + dy_ + 1] + fuz[c0 + dy_ + 1])) -
-                              ((flz[c0] + fuz[c0]) + (flz[c0 + dy_] + fuz[c0 + dy_]));
-                const T u = su[((n + 4) & 3) * SUN + (ty + 1) * SUZ + tz + 1];
-                T s = (xs_ + ys_) + zs_;
-                if (HC) s += S.hc * u;
-                T yv = s * S.dinv;
-                if (MODE == M_RESID) {
-                    yv = S.aux - yv;
-                    acc0.add_prod(yv, yv);
-                } else if (MODE == M_PDIR) {
-                    acc0.add_prod(S.aux, yv);
-                } else if (MODE == M_SDIR) {
-                    acc0.add_prod(yv, u);
-                    acc1.add_prod(yv, yv);
-                    acc2.add_prod(u, u);
+            load_cf(S, i + 3, CK);
+            const int c = i;                          // cell plane of the partials; node plane c-1
+            if ((!chk || (c >= xs && c <= xe)) && nvalid) {
+                const T *fb = sf + (c & 1) * (3 * SCN);
+                const T *Fx = fb, *Fy = fb + SCN, *Fz = fb + 2 * SCN;
+                constexpr int dy_ = SCZ;
+                const T X = (Fx[c0] + Fx[c0 + 1]) + (Fx[c0 + dy_] + Fx[c0 + dy_ + 1]);
+                const T Y = (Fy[c0 + dy_] + Fy[c0 + dy_ + 1]) - (Fy[c0] + Fy[c0 + 1]);
+                const T Z = (Fz[c0 + 1] + Fz[c0 + dy_ + 1]) - (Fz[c0] + Fz[c0 + dy_]);
+                const int n = c - 1;
+                if (!chk || n >= xs) {
+                    const T u = su[((n + 4) & 3) * SUN + uc];
+                    T s = ((X - nX) + (nY + Y)) + (nZ + Z);
+                    if (HC) s += S.hc * u;
+                    T yv = s * S.dinv;
+                    if (MODE == M_RESID) {
+                        yv = S.aux - yv;
+                        acc0.add_prod(yv, yv);
+                    } else if (MODE == M_PDIR) {
+                        acc0.add_prod(S.aux, yv);
+                    } else if (MODE == M_SDIR) {
+                        acc0.add_prod(yv, u);
+                        acc1.add_prod(yv, yv);
+                        acc2.add_prod(u, u);
+                    }
+                    yout[n * nyz + noff] = yv;
                 }
-                yout[(long long)n * nyz + noff] = yv;
+                nX = X; nY = Y; nZ = Z;
             }
-            load_nd(S, i + 1);
+            load_nd(S, i + 1, CK);
             __syncthreads();
         };
 
-        load_u(A, xs - 1);
-        load_u(B, xs);
-        for (int i = xs - 3; i <= xe; i += 2) {
-            step(A, i);
-            if (i + 1 <= xe) step(B, i + 1);
+        const Chk<true> checked;
+        const Chk<false> steady;
+        load_u(A, xs - 1, checked);
+        load_u(B, xs, checked);
+        int i = xs - 3;                               // steps xs-3 .. xe; A serves xs-3, xs-1, ...
+        for (; i <= xe && i < xs + 1; i += 2) {
+            step(A, i, checked);
+            if (i + 1 <= xe) step(B, i + 1, checked);
+        }
+        for (; i + 1 <= xe - 4; i += 2) {
+            step(A, i, steady);
+            step(B, i + 1, steady);
+        }
+        for (; i <= xe; i += 2) {
+            step(A, i, checked);
+            if (i + 1 <= xe) step(B, i + 1, checked);
         }
     }
     if (MODE == M_APPLY) return;

@@ -441,11 +441,15 @@ extern "C" int bella_projection3d(bella_ws *ws, const bella_proj3d *a, const bel
     o.x0_zero = 1;
     int st;
     if (a->precond == 1) {
-        bella_spectral3d *sp = nullptr;
-        rc = bella_spectral3d_create(&sp, &op, ws->device, stream);
-        if (rc != BELLA_OK) return rc;
-        st = bella_fbicgstab_pc(ws, sp, nullptr, 0, bvec, xvec, &o, stats, stream);
-        bella_spectral3d_destroy(sp);
+        // the workspace's background solve, re-derived from this call's coefficients
+        // (made anew when the grid or a boundary kind changed)
+        if (!ws->sp_cache || bella_spectral3d_update(ws->sp_cache, &op, stream) != BELLA_OK) {
+            bella_spectral3d_destroy(ws->sp_cache);
+            ws->sp_cache = nullptr;
+            rc = bella_spectral3d_create(&ws->sp_cache, &op, ws->device, stream);
+            if (rc != BELLA_OK) return rc;
+        }
+        st = bella_fbicgstab_pc(ws, ws->sp_cache, nullptr, 0, bvec, xvec, &o, stats, stream);
     } else {
         st = bella_bicgstab(ws, bvec, xvec, &o, stats, stream);
     }

@@ -740,8 +740,37 @@ struct SpGeom {
     const double *dinv;
 };
 
+// the parts that depend on the operator's coefficients: y-line means, 1/diag_inv,
+// the singular-line flag and the Thomas factors of every mode line.  Stream-ordered;
+// it waits for the device only when the operator has an hcenter term (whose means
+// decide whether singular mode lines exist).
 template <typename F>
-static int sp_build(bella_spectral3d **out, const SpGeom &g, int device, cudaStream_t s, F launch_means) {
+static int sp_refresh(bella_spectral3d *sp, const SpGeom &g, cudaStream_t s, F launch_means, int has_hc) {
+    sp->idx2 = g.idx2;
+    sp->idy2 = g.idy2;
+    sp->idz2 = g.idz2;
+    launch_means(sp);
+    k_sp_recip<<<vec_grid(sp->n), VEC_BLOCK, 0, s>>>(sp->n, g.dinv, sp->dscale);
+    sp->hc_zero = 1;
+    if (has_hc) {
+        std::vector<double> hcm(sp->ny);
+        if (cudaMemcpyAsync(hcm.data(), sp->hcm, sp->ny * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return BELLA_ECUDA;
+        for (int j = 0; j < sp->ny; ++j)
+            if (hcm[j] != 0.0) sp->hc_zero = 0;
+    }
+    const long long nl = (long long)sp->Kx * sp->Kz;
+    k_sp_factor<<<(unsigned)((nl + 127) / 128), 128, 0, s>>>(sp->Kx, sp->ny, sp->Kz, sp->mux, sp->muz, sp->cx, sp->cy,
+                                                             sp->cz, sp->hcm, sp->hc_zero, sp->idx2, sp->idy2,
+                                                             sp->idz2, sp->la, sp->lc, sp->li);
+    sp->launches += 3;
+    return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
+}
+
+template <typename F>
+static int sp_build(bella_spectral3d **out, const SpGeom &g, int device, cudaStream_t s, F launch_means,
+                    int has_hc) {
     bella_spectral3d *sp = new bella_spectral3d;
     memset(sp, 0, sizeof(*sp));
     sp->device = device;
@@ -810,17 +839,6 @@ static int sp_build(bella_spectral3d **out, const SpGeom &g, int device, cudaStr
     }
     cudaMemcpyAsync(sp->mux, mux.data(), Kx * sizeof(double), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(sp->muz, muz.data(), Kz * sizeof(double), cudaMemcpyHostToDevice, s);
-    launch_means(sp);
-    k_sp_recip<<<vec_grid(sp->n), VEC_BLOCK, 0, s>>>(sp->n, g.dinv, sp->dscale);
-    std::vector<double> hcm(ny);
-    cudaMemcpyAsync(hcm.data(), sp->hcm, ny * sizeof(double), cudaMemcpyDeviceToHost, s);
-    if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
-        bella_spectral3d_destroy(sp);
-        return BELLA_ECUDA;
-    }
-    sp->hc_zero = 1;
-    for (int j = 0; j < ny; ++j)
-        if (hcm[j] != 0.0) sp->hc_zero = 0;
     auto twiddles = [&](int L, float2 **dst) {
         std::vector<float2> t(L);
         const double pi = 3.14159265358979323846;
@@ -843,16 +861,31 @@ static int sp_build(bella_spectral3d **out, const SpGeom &g, int device, cudaStr
         bella_spectral3d_destroy(sp);
         return BELLA_ECUDA;
     }
-    k_sp_factor<<<(unsigned)((nl + 127) / 128), 128, 0, s>>>(Kx, ny, Kz, sp->mux, sp->muz, sp->cx, sp->cy, sp->cz,
-                                                             sp->hcm, sp->hc_zero, sp->idx2, sp->idy2, sp->idz2,
-                                                             sp->la, sp->lc, sp->li);
-    if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+    if (sp_refresh(sp, g, s, launch_means, has_hc) != BELLA_OK ||
+        cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
         bella_spectral3d_destroy(sp);
         return BELLA_ECUDA;
     }
-    sp->launches = 3;
     *out = sp;
     return BELLA_OK;
+}
+
+// launchers of the y-line means of a 3D or 2D operator's coefficients
+static auto means3d(const bella_op3d *op, cudaStream_t s) {
+    return [op, s](bella_spectral3d *sp) {
+        k_sp_means<<<dim3(op->ny, SP_CHUNKS), 256, 0, s>>>(op->nx, op->ny, op->nz, op->hplusx, op->hplusy, op->hplusz,
+                                                           op->hcenter, sp->mpart);
+        k_sp_means_final<<<(op->ny + 127) / 128, 128, 0, s>>>(op->nx, op->ny, op->nz, op->hcenter ? 1 : 0, sp->mpart,
+                                                              sp->cx, sp->cy, sp->cz, sp->hcm);
+    };
+}
+static auto means2d(const bella_op2d *op, cudaStream_t s) {
+    return [op, s](bella_spectral3d *sp) {
+        k_sp2_means<<<dim3(op->ny, SP_CHUNKS), 256, 0, s>>>(op->nx, op->ny, op->hplusx, op->hplusy, op->cxx, op->cyy,
+                                                            op->hcenter, sp->mpart);
+        k_sp2_means_final<<<(op->ny + 127) / 128, 128, 0, s>>>(op->nx, op->ny, op->hcenter ? 1 : 0, sp->mpart, sp->cx,
+                                                               sp->cy, sp->cz, sp->hcm);
+    };
 }
 
 extern "C" {
@@ -868,12 +901,20 @@ int bella_spectral3d_create(bella_spectral3d **out, const bella_op3d *op, int de
     cudaStream_t s = (cudaStream_t)stream;
     const SpGeom g{op->nx, op->ny, op->nz, op->x_wall ? 0 : 1, op->z_wall ? 0 : 1, 0,
                    1.0 / (op->dx * op->dx), 1.0 / (op->dy * op->dy), 1.0 / (op->dz * op->dz), op->diag_inv};
-    return sp_build(out, g, device, s, [&](bella_spectral3d *sp) {
-        k_sp_means<<<dim3(op->ny, SP_CHUNKS), 256, 0, s>>>(op->nx, op->ny, op->nz, op->hplusx, op->hplusy, op->hplusz,
-                                                           op->hcenter, sp->mpart);
-        k_sp_means_final<<<(op->ny + 127) / 128, 128, 0, s>>>(op->nx, op->ny, op->nz, op->hcenter ? 1 : 0, sp->mpart,
-                                                              sp->cx, sp->cy, sp->cz, sp->hcm);
-    });
+    return sp_build(out, g, device, s, means3d(op, s), op->hcenter ? 1 : 0);
+}
+
+int bella_spectral3d_update(bella_spectral3d *sp, const bella_op3d *op, void *stream) {
+    if (!sp || !op) return BELLA_EINVAL;
+    if (sp->twod || op->nx != sp->nx || op->ny != sp->ny || op->nz != sp->nz || (op->x_wall ? 0 : 1) != sp->xper ||
+        (op->z_wall ? 0 : 1) != sp->zper || !op->y_wall || !op->hplusx || !op->hplusy || !op->hplusz ||
+        !op->diag_inv || !(op->dx > 0.0) || !(op->dy > 0.0) || !(op->dz > 0.0))
+        return BELLA_EINVAL;
+    if (cudaSetDevice(sp->device) != cudaSuccess) return BELLA_ECUDA;
+    cudaStream_t s = (cudaStream_t)stream;
+    const SpGeom g{op->nx, op->ny, op->nz, sp->xper, sp->zper, 0,
+                   1.0 / (op->dx * op->dx), 1.0 / (op->dy * op->dy), 1.0 / (op->dz * op->dz), op->diag_inv};
+    return sp_refresh(sp, g, s, means3d(op, s), op->hcenter ? 1 : 0);
 }
 
 int bella_spectral2d_create(bella_spectral3d **out, const bella_op2d *op, int device, void *stream) {
@@ -888,12 +929,19 @@ int bella_spectral2d_create(bella_spectral3d **out, const bella_op2d *op, int de
     // nodes [ny][nx] as the 3D layout [1][ny][nx]: x takes the role of z
     const SpGeom g{1, op->ny, op->nx, 1, op->x_wall ? 0 : 1, 1, 0.0, 1.0 / (op->dy * op->dy),
                    1.0 / (op->dx * op->dx), op->diag_inv};
-    return sp_build(out, g, device, s, [&](bella_spectral3d *sp) {
-        k_sp2_means<<<dim3(op->ny, SP_CHUNKS), 256, 0, s>>>(op->nx, op->ny, op->hplusx, op->hplusy, op->cxx, op->cyy,
-                                                            op->hcenter, sp->mpart);
-        k_sp2_means_final<<<(op->ny + 127) / 128, 128, 0, s>>>(op->nx, op->ny, op->hcenter ? 1 : 0, sp->mpart, sp->cx,
-                                                               sp->cy, sp->cz, sp->hcm);
-    });
+    return sp_build(out, g, device, s, means2d(op, s), op->hcenter ? 1 : 0);
+}
+
+int bella_spectral2d_update(bella_spectral3d *sp, const bella_op2d *op, void *stream) {
+    if (!sp || !op) return BELLA_EINVAL;
+    if (!sp->twod || op->nx != sp->nz || op->ny != sp->ny || (op->x_wall ? 0 : 1) != sp->zper || op->y_wall != 1 ||
+        !op->hplusx || !op->hplusy || !op->cxx || !op->cyy || !op->diag_inv || !(op->dx > 0.0) || !(op->dy > 0.0))
+        return BELLA_EINVAL;
+    if (cudaSetDevice(sp->device) != cudaSuccess) return BELLA_ECUDA;
+    cudaStream_t s = (cudaStream_t)stream;
+    const SpGeom g{1, op->ny, op->nx, 1, sp->zper, 1, 0.0, 1.0 / (op->dy * op->dy), 1.0 / (op->dx * op->dx),
+                   op->diag_inv};
+    return sp_refresh(sp, g, s, means2d(op, s), op->hcenter ? 1 : 0);
 }
 
 int bella_spectral3d_apply(bella_spectral3d *sp, const float *in, float *out, void *stream) {

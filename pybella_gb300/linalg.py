@@ -102,7 +102,9 @@ class _NodalOperator:
         control flow.  ``'mixed'`` runs FP32 BiCGStab inner solves inside FP64
         iterative refinement (FP64 residuals, FP64 accumulated solution); if an
         inner solve fails (non-finite, breakdown, no progress) the solve is
-        finished by FP64 BiCGStab and ``stats['fallback'] == 1``.  ``'df64'``
+        finished by double-float BiCGStab with FP64 reliable updates (its convergence
+        is accepted only on the FP64 true residual) and ``stats['fallback'] == 1``.
+        ``'df64'``
         is double-float BiCGStab with FP64 reliable updates.
 
         ``preconditioner`` (3D only) selects flexible BiCGStab right-

@@ -67,6 +67,18 @@ class BackgroundSolve:
 
     __call__ = apply
 
+    def update(self, op):
+        """Re-derive the background solve from ``op``'s coefficients in place (an
+        operator of the same shape and boundary kinds as the one it was made for,
+        e.g. the next time step's): nothing is allocated
+        (``bella_spectral3d_update`` / ``bella_spectral2d_update``)."""
+        upd = (self._lib.bella_spectral2d_update if isinstance(op._op, _lib.Op2D)
+               else self._lib.bella_spectral3d_update)
+        with torch.cuda.device(self.dev):
+            _lib.check(upd(self.handle, ctypes.byref(op._op), self._stream()), "bella_spectral_update")
+        self.op = op
+        return self
+
     def launches(self):
         return int(self._lib.bella_spectral3d_launches(self.handle))
 

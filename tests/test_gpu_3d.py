@@ -82,15 +82,29 @@ def test_null_modes_3d_exact_on_device():
 
 @pytest.mark.parametrize("precision", ["fp64", "df64", "mixed"])
 def test_solve3d_small_vs_scipy(precision):
-    w = cases.stratified_3d(1, 33, 17, 33)
+    """33x17x33 to rtol 1e-10 on every arithmetic path: the FP64 true residual
+    reaches the tolerance, and the solution's cell gradients are as close to the
+    converged FP64 solution (true residual 1e-13) as those of the oracle's
+    scipy-semantics BiCGStab at the same tolerance: within three times that
+    solve's own error, or 1e-8.  (Two solves stopped at rtol 1e-10 differ by up
+    to cond(A) * 1e-10, so they are compared through the converged solution, not
+    with each other.)"""
+    from test_gpu_fp64_oracle import _cell_grads_3d, _converged
+    shape = (33, 17, 33)
+    w = cases.stratified_3d(1, *shape)
     A = _dev_op(w["op"])
     x_ref, info_ref, _ = bicgstab_legacy(w["op"], w["b"], 1e-10, 20000)
+    assert info_ref == 0
+    xs = _converged(A, w["b"]).cpu().numpy()
     x, st = A.solve(w["b"], tol=1e-10, maxiter=20000, precision=precision)
     assert st["status"] == 0, st
     xn = x.cpu().numpy()
     assert true_relres(w["op"], xn, w["b"]) <= 1e-10
-    if precision != "mixed" or st["fallback"]:
-        assert _rel(xn, x_ref) < 1e-6
+    gs = _cell_grads_3d(xs, shape)
+    e_ref = [_rel(g, g0) for g, g0 in zip(_cell_grads_3d(x_ref, shape), gs)]
+    e = [_rel(g, g0) for g, g0 in zip(_cell_grads_3d(xn, shape), gs)]
+    for k in range(3):
+        assert e[k] <= max(1e-8, 3.0 * e_ref[k]), (precision, k, e, e_ref, st)
 
 
 def test_solve3d_mid_size_df64_converges():

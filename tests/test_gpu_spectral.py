@@ -233,6 +233,42 @@ def test_trained_correction_of_the_background_solve(capsys):
 # ---------------------------------------------------------------------------
 # the background solve of the 2D 9-point operator
 # ---------------------------------------------------------------------------
+def test_background_update_equals_a_fresh_set_up():
+    """bella_spectral3d_update / bella_spectral2d_update: a background solve made
+    for one operator and re-derived in place from another of the same shape (with
+    and without an hcenter term) applies exactly as one made for the second;
+    another shape, boundary kind or dimension is refused."""
+    import torch
+    from pybella_gb300 import _lib
+    from pybella_gb300.spectral import BackgroundSolve
+    rng = np.random.default_rng(5)
+    shape, walls = (33, 17, 29), (False, True, True)
+    a = cases.stratified_3d(1, *shape, walls=walls)["op"]
+    b = cases.stratified_3d(2, *shape, walls=walls)["op"]
+    r = torch.tensor(_seam_consistent(rng.standard_normal(int(np.prod(shape))), shape, walls),
+                     dtype=torch.float32, device="cuda")
+    for hc in (False, True):
+        if hc:
+            b = dict(b, hcenter=-rng.uniform(0.1, 1.0, shape).reshape(-1))
+        A, B = _dev_op(a), _dev_op(b)
+        bg = BackgroundSolve(A)
+        fresh = BackgroundSolve(B)
+        y_up = bg.update(B).apply(r).clone()
+        y_new = fresh.apply(r)
+        assert torch.equal(y_up, y_new), float((y_up - y_new).abs().max())
+    other = _dev_op(cases.stratified_3d(1, 33, 17, 33, walls=walls)["op"])
+    with pytest.raises(_lib.BellaError):
+        bg.update(other)
+    w2 = [cases.stratified_2d(s, 65, 33)["op"] for s in (3, 4)]
+    bg2 = BackgroundSolve(_op2d(w2[0]))
+    y_up = bg2.update(_op2d(w2[1])).apply(r[: 65 * 33]).clone()
+    assert torch.equal(y_up, BackgroundSolve(_op2d(w2[1])).apply(r[: 65 * 33]))
+    with pytest.raises(_lib.BellaError):
+        bg2.update(A)
+    with pytest.raises(_lib.BellaError):
+        bg.update(_op2d(w2[0]))
+
+
 def _op2d(op):
     from pybella_gb300.linalg import NodalHelmholtz2D
     return NodalHelmholtz2D(op["hplusx"], op["hplusy"], op["hcenter"], op["cor"], op["diag_inv"],
