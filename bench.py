@@ -49,6 +49,9 @@ METRIC = "solves/s to 1e-8 residual: learned-precond vs plain BiCGStab, 1 GB300"
 STENCIL3D_TRAFFIC = 211.3e6     # k_stencil3d<float, APPLY>, 257x129x257 nodes
 STENCIL2D_TRAFFIC = 134.4e6     # k_stencil2d<dfloat, PDIR>, 2049x1025 nodes
 CONV_TRAFFIC = 108.9e6          # k_conv3d_tc<32, 32>, one hidden layer at 257x129x257 nodes (2x2x2 blocked)
+# k_batch_bicgstab<dfloat, 64, 8>: 16.95 GB read + written by a 20-iteration launch of the
+# 48-member ensemble, whose algorithmic bytes are 20 x 4,327,728 nodes x 200 B = 17.31 GB
+ENSEMBLE_TRAFFIC_RATIO = 16.951e9 / 17.311e9
 WORKLOAD = "2D nodal Helmholtz 9-point solve, 2049x1025 nodes, pseudo-incompressible, rtol 1e-8, 64 seeds"
 
 
@@ -545,7 +548,11 @@ def ensemble_line(args, dev, local, rank, world, dist, steps, warmup, e2e_steps,
                 "d2h_bytes_per_step": d2h, "path": "pybella_gb300.ensemble.solve_ensemble on NumPy operands"},
         "gpu_launches": steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "k_batch_bicgstab (whole round, one launch)",
+                     "traffic": alg * ENSEMBLE_TRAFFIC_RATIO,
+                     "traffic_source": "ncu dram bytes read + written of one 20-iteration launch of the same 48 "
+                                       "members, 0.979 of its algorithmic bytes, scaled to this round by member "
+                                       "iterations x nodes",
+                     "kernel": "k_batch_bicgstab (whole round, one launch)",
                      "peak_source": peak_kind, "alg_bytes_per_launch": alg},
         "clocks": clk,
         "solver": {"iterations": [st["iterations"] for st in stats], "status": sorted(set(st["status"] for st in stats)),
@@ -1017,6 +1024,12 @@ def ensemble_steps_line(args, local, rank, world, nsteps, warmup, want_cpu):
     stats = E.stats[nstat0:]
     iters = np.array([[st["iterations"] for st in rnd] for rnd in stats], dtype=np.float64)
     status = sorted(set(st["status"] for rnd in stats for st in rnd))
+    status_counts = {}
+    for rnd in stats:
+        for st in rnd:
+            status_counts[str(st["status"])] = status_counts.get(str(st["status"]), 0) + 1
+    finished_alone = sum(1 for rnd in stats for st in rnd if st["fallback"] >= 256)
+    relres_max = max(st["relres"] for rnd in stats for st in rnd)
     sizes = np.array([int(m.adv.inx) * int(m.adv.iny) for m in members], dtype=np.float64)
     # algorithmic bytes of the batched solves: 25 words per node and iteration (two
     # 5-word matvecs and the 15-word vector chain), 8 bytes each (FP64 or FP32 pair)
@@ -1035,7 +1048,8 @@ def ensemble_steps_line(args, local, rank, world, nsteps, warmup, want_cpu):
         "solver": {"iterations_mean_per_grid": {
             "%dx%d" % (int(m.adv.inx) - 1, int(m.adv.iny) - 1): float(iters[:, k].mean())
             for k, m in enumerate(members) if k % 16 == 0},
-            "status": status, "solves": int(iters.size)},
+            "status": status, "status_counts": status_counts, "relres_max": relres_max,
+            "finished_alone": finished_alone, "solves": int(iters.size)},
         "roofline": {"bound": "hbm", "achieved": alg / (ms / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": alg / (ms / 1000.0) / 1e9 / peak, "traffic": None,
                      "kernel": "whole ensemble step (k_batch_bicgstab dominates)", "peak_source": peak_kind,

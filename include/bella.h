@@ -345,9 +345,13 @@ int bella_cfl_maxima(const double *rho, const double *rhou, const double *rhov, 
  * grid barrier); tol, atol, maxiter from opts; opts->precision 0: FP64
  * arithmetic, otherwise double-float on the FP32 pipe, whose members are
  * refined in FP64 (residual, batched correction solve, update) when their FP64
- * true residual misses the tolerance.  config: index of a launch configuration
+ * true residual misses the tolerance; members whose batched iteration broke
+ * down, or that still miss after four refinement rounds, are finished alone by
+ * the FP64 bella_bicgstab from their iterate within the iteration budget left
+ * (the batched iterate is kept unless that lowers its FP64 true residual).  config: index of a launch configuration
  * (tile shape, CTAs per SM), < 0 for the autotuned one.  stats[m].outer reports
- * the configuration used, stats[m].fallback the refinement rounds of member m.
+ * the configuration used, stats[m].fallback the refinement rounds of member m,
+ * plus 256 when it was finished alone.
  * Returns BELLA_OK when every member converged, else the first failing
  * member's status. */
 int bella_bicgstab_batched(bella_ws *const *ws, int nmembers, const double *const *b, double *const *x,

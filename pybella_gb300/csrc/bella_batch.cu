@@ -523,6 +523,8 @@ struct BatchCtx {
     double *part = nullptr;
     const double **bptr = nullptr;
     size_t mem_cap = 0, part_cap = 0;
+    double *save = nullptr;   // a member's iterate kept while it is finished alone
+    long long save_cap = 0;
     // autotuned choice per member-size signature
     std::vector<std::pair<std::string, int>> tuned;
     std::string err;
@@ -876,6 +878,59 @@ int bella_bicgstab_batched(bella_ws *const *ws, int nmembers, const double *cons
             if (!sub[q].done || sub[q].status != BELLA_OK) status[m] = sub[q].done ? sub[q].status : BELLA_MAXITER;
         }
     }
+    // double-float members whose batched iteration broke down, or whose FP64 true
+    // residual still misses the tolerance after the refinement rounds (the
+    // double-float floor of a hard system), are finished one by one by the FP64
+    // solve from their iterate, within the iteration budget left; the batched
+    // iterate is kept unless that lowers its FP64 true residual.  Reported in
+    // stats->fallback.
+    std::vector<int> single(nmembers, 0);
+    if (prec != 0) {
+        bool any = false;
+        for (int m = 0; m < nmembers; ++m) {
+            double target = o.tol * bnorm[m];
+            if (o.atol > target) target = o.atol;
+            const double rm = sqrt(ks[m].dot_aux2);
+            const bool missed = status[m] == BELLA_OK && isfinite(rm) && rm > target && !(bnorm[m] <= o.tol);
+            if (!(status[m] == BELLA_BREAKDOWN || missed) || !isfinite(bnorm[m]) || !isfinite(rm) ||
+                its[m] >= o.maxiter)
+                continue;
+            const long long nm_ = ws[m]->n;
+            if (c.save_cap < nm_) {
+                cudaFree(c.save);
+                c.save = nullptr;
+                c.save_cap = 0;
+                if (cudaMalloc(&c.save, nm_ * sizeof(double)) != cudaSuccess) return BELLA_ECUDA;
+                c.save_cap = nm_;
+            }
+            if (cudaMemcpyAsync(c.save, x[m], nm_ * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+                return BELLA_ECUDA;
+            bella_solve_opts os = o;
+            os.precision = 0;
+            os.x0_zero = 0;
+            os.maxiter = o.maxiter - its[m];
+            bella_solve_stats fs;
+            const int r = bella_bicgstab(ws[m], b[m], x[m], &os, &fs, stream);
+            if (r < 0) return r;
+            its[m] += fs.iterations;
+            if (isfinite(fs.relres) && fs.relres * bnorm[m] < rm) {
+                status[m] = fs.status;
+                single[m] = 1;
+            } else if (cudaMemcpyAsync(x[m], c.save, nm_ * sizeof(double), cudaMemcpyDeviceToDevice, s) !=
+                       cudaSuccess) {
+                return BELLA_ECUDA;
+            }
+            any = true;
+        }
+        if (any) {
+            for (int m = 0; m < nmembers; ++m)
+                if (single[m]) op2d_resid(ws[m], 0, x[m], b[m], ws[m]->r64, s);
+            for (int m = 0; m < nmembers; ++m)
+                if (single[m] && cudaMemcpyAsync(&ks[m], ws[m]->ks, sizeof(KState), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+                    return BELLA_ECUDA;
+            if (cudaStreamSynchronize(s) != cudaSuccess) return BELLA_ECUDA;
+        }
+    }
     const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     int worst = BELLA_OK;
     for (int m = 0; m < nmembers; ++m) {
@@ -897,7 +952,7 @@ int bella_bicgstab_batched(bella_ws *const *ws, int nmembers, const double *cons
             q.seconds = secs;
             q.detail = detail[m];
             q.outer = cfg;
-            q.fallback = rounds[m];   // FP64 refinement rounds of this member
+            q.fallback = rounds[m] + (single[m] ? 256 : 0);   // FP64 refinement rounds; +256: finished alone
         }
     }
     return worst;

@@ -315,6 +315,9 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, long long work, const __nv_bfloat1
             const __nv_bfloat16 *__restrict__ Wtc, const float *__restrict__ bias, void *out, float out_scale,
             int *err, const __nv_bfloat16 *__restrict__ mask) {
     static_assert(COUT == 32 || (COUT == 16 && OUTF32), "hidden layers: 32 channels; output layer: 16 (8 used)");
+    // the next layer, launched as a programmatic dependent, may start its prologue
+    // on the SMs this grid leaves (it waits for this grid before it touches activations)
+    asm volatile("griddepcontrol.launch_dependents;");
     constexpr int TMEM_COLS = TC_MB * TC_RING * COUT;     // 512 or 256: a power of two
     constexpr int NCH = CIN / 8;
     constexpr int NB = 3 * COUT;                          // B rows: the three dx taps
@@ -374,6 +377,10 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, long long work, const __nv_bfloat1
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
+    // the prologue above touches only this layer's weights and on-chip state; the
+    // input activations are the previous grid's output: wait for it to complete
+    // (a no-op when this grid was not launched as a programmatic dependent)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
 
     const int plane = PY * PZ;
     const int nblk = (plane + TC_ROWS - 1) / TC_ROWS;
@@ -642,25 +649,39 @@ __device__ __forceinline__ float rms_scale(const double *sumsq, long long nn) {
     return (q > 0.0 && isfinite(q)) ? (float)(1.0 / sqrt(q / (double)nn)) : 1.f;
 }
 
+// voxel v of the net grid -> (sample, ci, cj, ck); 32-bit (node and voxel counts
+// stay below 2^31: bella_cnn_create bounds the capacity)
+struct VoxIdx {
+    int s, ci, cj, ck;
+};
+__device__ __forceinline__ VoxIdx vox_index(const BlockMap &m, int v) {
+    VoxIdx r;
+    r.ck = v % m.cz;
+    const int t = v / m.cz;
+    r.cj = t % m.cy;
+    const int sx = t / m.cy;
+    r.s = sx / m.cx;
+    r.ci = sx - r.s * m.cx;
+    return r;
+}
+
 // node values (f32, times scale -- or 1/RMS from sumsq when given) -> channels-last
-// bf16 with 16 channels
+// bf16 with 16 channels; one thread per voxel, BB = m.b (1 or 2) at compile time
+template <int BB>
 __global__ void k_pack_in(BlockMap m, const float *in, float scale, __nv_bfloat16 *out, const double *sumsq) {
-    const long long n = m.nvox();
+    const int n = (int)m.nvox();
     if (sumsq) scale = rms_scale(sumsq, (long long)m.B * m.nx * m.ny * m.nz);
-    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
-        const int ck = (int)(v % m.cz);
-        const long long t = v / m.cz;
-        const int cj = (int)(t % m.cy);
-        const long long sx = t / m.cy;
-        const int s = (int)(sx / m.cx), ci = (int)(sx % m.cx);
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const VoxIdx x = vox_index(m, v);
         float c[16];
 #pragma unroll
         for (int q = 0; q < 16; ++q) c[q] = 0.f;
-        for (int q = 0; q < m.b * m.b * m.b; ++q) {
-            const int a = q / (m.b * m.b), bb = (q / m.b) % m.b, d = q % m.b;
-            const int i = ci * m.b + a, j = cj * m.b + bb, k = ck * m.b + d;
+#pragma unroll
+        for (int q = 0; q < BB * BB * BB; ++q) {
+            const int a = q / (BB * BB), bb = (q / BB) % BB, d = q % BB;
+            const int i = x.ci * BB + a, j = x.cj * BB + bb, k = x.ck * BB + d;
             if (i < m.nx && j < m.ny && k < m.nz)
-                c[q] = in[(((long long)s * m.nx + i) * m.ny + j) * m.nz + k] * scale;
+                c[q] = in[((x.s * m.nx + i) * m.ny + j) * m.nz + k] * scale;
         }
         uint32_t w[8];
 #pragma unroll
@@ -668,7 +689,7 @@ __global__ void k_pack_in(BlockMap m, const float *in, float scale, __nv_bfloat1
             const __nv_bfloat162 h = __floats2bfloat162_rn(c[2 * q], c[2 * q + 1]);
             w[q] = *reinterpret_cast<const uint32_t *>(&h);
         }
-        uint4 *o = reinterpret_cast<uint4 *>(out + v * 16);
+        uint4 *o = reinterpret_cast<uint4 *>(out + (long long)v * 16);
         o[0] = make_uint4(w[0], w[1], w[2], w[3]);
         o[1] = make_uint4(w[4], w[5], w[6], w[7]);
     }
@@ -699,29 +720,50 @@ __global__ void k_pack_f32(BlockMap m, const float *in, float scale, float *out)
 // net-grid f32 [nvox][8] -> node values (times RMS from sumsq when given), plus
 // omega * skip (the identity path of the preconditioner) when skip is given
 // seam: the network's reach in nodes; along an axis flagged in pmask (bit 0 x, 1 y,
-// 2 z) the output is 0 within that distance of the duplicated periodic seam
+// 2 z) the output is 0 within that distance of the duplicated periodic seam.
+// One thread per voxel: its 8 channels in two 16-byte loads, its BB^3 nodes
+// written as z pairs (coalesced across the warp); BB = m.b at compile time.
+template <int BB>
 __global__ void k_unpack(BlockMap m, const float *y8, float *out, const double *sumsq, const float *skip = nullptr,
                          float omega = 0.f, int pmask = 0, int seam = 0) {
-    const long long n = (long long)m.B * m.nx * m.ny * m.nz;
-    const float mul = sumsq ? 1.f / rms_scale(sumsq, n) : 1.f;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(e % m.nz);
-        const long long t = e / m.nz;
-        const int j = (int)(t % m.ny);
-        const long long si = t / m.ny;
-        const int s = (int)(si / m.nx), i = (int)(si % m.nx);
-        const long long v = (((long long)s * m.cx + i / m.b) * m.cy + j / m.b) * m.cz + k / m.b;
-        const int q = ((i % m.b) * m.b + j % m.b) * m.b + k % m.b;
-        float o = y8[v * 8 + q] * mul;
-        if (skip) o = fmaf(omega, skip[e], o);
-        if (pmask) {
-            const bool near = ((pmask & 1) && min(i, m.nx - 1 - i) < seam) ||
-                              ((pmask & 2) && min(j, m.ny - 1 - j) < seam) ||
-                              ((pmask & 4) && min(k, m.nz - 1 - k) < seam);
-            if (near) o = 0.f;
+    const int nv = (int)m.nvox();
+    const float mul = sumsq ? 1.f / rms_scale(sumsq, (long long)m.B * m.nx * m.ny * m.nz) : 1.f;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
+        const VoxIdx x = vox_index(m, v);
+        const float4 lo = reinterpret_cast<const float4 *>(y8)[2 * (long long)v];
+        const float4 hi = reinterpret_cast<const float4 *>(y8)[2 * (long long)v + 1];
+        const float yv[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+#pragma unroll
+        for (int q = 0; q < BB * BB * BB; ++q) {
+            const int a = q / (BB * BB), bb = (q / BB) % BB, d = q % BB;
+            const int i = x.ci * BB + a, j = x.cj * BB + bb, k = x.ck * BB + d;
+            if (i >= m.nx || j >= m.ny || k >= m.nz) continue;
+            const int e = ((x.s * m.nx + i) * m.ny + j) * m.nz + k;
+            float o = yv[q] * mul;
+            if (skip) o = fmaf(omega, skip[e], o);
+            if (pmask) {
+                const bool near = ((pmask & 1) && min(i, m.nx - 1 - i) < seam) ||
+                                  ((pmask & 2) && min(j, m.ny - 1 - j) < seam) ||
+                                  ((pmask & 4) && min(k, m.nz - 1 - k) < seam);
+                if (near) o = 0.f;
+            }
+            out[e] = o;
         }
-        out[e] = o;
     }
+}
+
+// host launchers of the two, for the map's blocking factor (1 or 2)
+static void pack_in(const BlockMap &m, const float *in, float scale, __nv_bfloat16 *out, const double *sumsq,
+                    cudaStream_t s) {
+    const int g = vec_grid(m.nvox());
+    if (m.b == 2) k_pack_in<2><<<g, 256, 0, s>>>(m, in, scale, out, sumsq);
+    else          k_pack_in<1><<<g, 256, 0, s>>>(m, in, scale, out, sumsq);
+}
+static void unpack(const BlockMap &m, const float *y8, float *out, const double *sumsq, const float *skip,
+                   float omega, int pmask, int seam, cudaStream_t s) {
+    const int g = vec_grid(m.nvox());
+    if (m.b == 2) k_unpack<2><<<g, 256, 0, s>>>(m, y8, out, sumsq, skip, omega, pmask, seam);
+    else          k_unpack<1><<<g, 256, 0, s>>>(m, y8, out, sumsq, skip, omega, pmask, seam);
 }
 
 // f32 [nvox][8] -> bf16 [nvox][16] (zero-padded), input of the last layer's gradient pass
@@ -1076,6 +1118,23 @@ static bool map_ok(const bella_cnn *net, const BlockMap &m) {
     return m.nvox() <= net->cap && (m.B == 1 || m.cx % CT_X == 0);
 }
 
+// a launch that may begin while the previous kernel in the stream is finishing
+// (programmatic dependent launch); the kernel orders itself with griddepcontrol.wait
+template <typename... P, typename... A>
+static void launch_dependent(void (*kernel)(P...), int grid, int block, size_t smem, cudaStream_t s, A... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, static_cast<P>(args)...);
+}
+
 static int tc_grid(long long nitems) {
     int nsm = num_sms();
     return (int)(nitems < nsm ? nitems : nsm);
@@ -1096,22 +1155,27 @@ static void forward_layers(bella_cnn *net, const BlockMap &m, float out_scale, c
         const int gt = tc_grid(items), pz = nz + 2;
         const long long work = (items + gt - 1) / gt;
         const float *b5 = net->linear ? nullptr : net->bias[5];
+        // layers 2..6 are programmatic dependents of the layer before (one CTA per SM
+        // each, so the whole previous grid is resident when they launch)
+        const __nv_bfloat16 *nomask = nullptr;
         if (net->linear) {
             k_conv3d_tc<16, 32, false, false><<<gt, TC_THREADS, tc_smem_bytes<16, 32>(pz), s>>>(
                 nx, ny, nz, xs, work, net->act[0], net->wtc[0], nullptr, net->act[1], 1.f, net->tc_err, nullptr);
             for (int l = 1; l <= 4; ++l)
-                k_conv3d_tc<32, 32, false, false><<<gt, TC_THREADS, tc_smem_bytes<32, 32>(pz), s>>>(
-                    nx, ny, nz, xs, work, net->act[l], net->wtc[l], nullptr, net->act[l + 1], 1.f, net->tc_err, nullptr);
+                launch_dependent(k_conv3d_tc<32, 32, false, false>, gt, TC_THREADS, tc_smem_bytes<32, 32>(pz), s,
+                                 nx, ny, nz, xs, work, net->act[l], net->wtc[l], (const float *)nullptr,
+                                 (void *)net->act[l + 1], 1.f, net->tc_err, nomask);
         } else {
             k_conv3d_tc<16, 32, true, false><<<gt, TC_THREADS, tc_smem_bytes<16, 32>(pz), s>>>(
                 nx, ny, nz, xs, work, net->act[0], net->wtc[0], net->bias[0], net->act[1], 1.f, net->tc_err, nullptr);
             for (int l = 1; l <= 4; ++l)
-                k_conv3d_tc<32, 32, true, false><<<gt, TC_THREADS, tc_smem_bytes<32, 32>(pz), s>>>(
-                    nx, ny, nz, xs, work, net->act[l], net->wtc[l], net->bias[l], net->act[l + 1], 1.f,
-                    net->tc_err, nullptr);
+                launch_dependent(k_conv3d_tc<32, 32, true, false>, gt, TC_THREADS, tc_smem_bytes<32, 32>(pz), s,
+                                 nx, ny, nz, xs, work, net->act[l], net->wtc[l], (const float *)net->bias[l],
+                                 (void *)net->act[l + 1], 1.f, net->tc_err, nomask);
         }
-        k_conv3d_tc<32, 16, false, true><<<gt, TC_THREADS, tc_smem_bytes<32, 16>(pz), s>>>(
-            nx, ny, nz, xs, work, net->act[5], net->wtc[5], b5, net->y8, out_scale, net->tc_err, nullptr);
+        launch_dependent(k_conv3d_tc<32, 16, false, true>, gt, TC_THREADS, tc_smem_bytes<32, 16>(pz), s,
+                         nx, ny, nz, xs, work, net->act[5], net->wtc[5], b5, (void *)net->y8, out_scale,
+                         net->tc_err, nomask);
         net->launches += 6;
         return;
     }
@@ -1226,11 +1290,11 @@ int cnn_apply_dev(bella_cnn *net, int nx, int ny, int nz, const float *in, float
                   cudaStream_t s, const int *per) {
     const BlockMap m = make_map(1, nx, ny, nz, net->block);
     if (!map_ok(net, m)) return BELLA_EINVAL;
-    k_pack_in<<<vec_grid(m.nvox()), 256, 0, s>>>(m, in, 1.f, net->act[0], sumsq);
+    pack_in(m, in, 1.f, net->act[0], sumsq, s);
     forward_layers(net, m, 1.f, s);
     const int pmask = per ? (per[0] ? 1 : 0) | (per[1] ? 2 : 0) | (per[2] ? 4 : 0) : 0;
     const int seam = 7 * net->block - 1;      // six 3x3x3 layers on b-node blocks: 6b + (b - 1) nodes
-    k_unpack<<<vec_grid((long long)nx * ny * nz), 256, 0, s>>>(m, net->y8, out, sumsq, in, net->omega, pmask, seam);
+    unpack(m, net->y8, out, sumsq, in, net->omega, pmask, seam, s);
     net->launches += 2;
     return BELLA_OK;
 }
@@ -1240,6 +1304,7 @@ extern "C" {
 
 int bella_cnn_create(bella_cnn **out, int device, int block, long long capacity) {
     if (!out || capacity <= 0 || (block != 1 && block != 2)) return BELLA_EINVAL;
+    if (capacity * 8 >= (1LL << 31)) return BELLA_EINVAL;   // the pack kernels index nodes in 32 bits
     if (cudaSetDevice(device) != cudaSuccess) return BELLA_ECUDA;
     bella_cnn *net = new bella_cnn();
     memset(net, 0, sizeof(*net));
@@ -1336,9 +1401,9 @@ int bella_cnn_forward(bella_cnn *net, int nx, int ny, int nz, const float *in, f
     const BlockMap m = make_map(1, nx, ny, nz, net->block);
     if (!map_ok(net, m)) return BELLA_EINVAL;
     cudaStream_t s = (cudaStream_t)stream;
-    k_pack_in<<<vec_grid(m.nvox()), 256, 0, s>>>(m, in, in_scale, net->act[0], nullptr);
+    pack_in(m, in, in_scale, net->act[0], nullptr, s);
     forward_layers(net, m, 1.f / in_scale, s);
-    k_unpack<<<vec_grid((long long)nx * ny * nz), 256, 0, s>>>(m, net->y8, out, nullptr, in, net->omega);
+    unpack(m, net->y8, out, nullptr, in, net->omega, 0, 0, s);
     net->launches += 2;
     return cudaGetLastError() == cudaSuccess ? BELLA_OK : BELLA_ECUDA;
 }
@@ -1352,9 +1417,9 @@ int bella_cnn_gradients(bella_cnn *net, int nx, int ny, int nz, const float *in,
     const BlockMap m = make_map(1, nx, ny, nz, net->block);
     if (!map_ok(net, m)) return BELLA_EINVAL;
     cudaStream_t s = (cudaStream_t)stream;
-    k_pack_in<<<vec_grid(m.nvox()), 256, 0, s>>>(m, in, 1.f, net->act[0], nullptr);
+    pack_in(m, in, 1.f, net->act[0], nullptr, s);
     forward_layers(net, m, 1.f, s);
-    if (out) k_unpack<<<vec_grid((long long)nx * ny * nz), 256, 0, s>>>(m, net->y8, out, nullptr, in, net->omega);
+    if (out) unpack(m, net->y8, out, nullptr, in, net->omega, 0, 0, s);
     k_pack_f32<<<vec_grid(m.nvox()), 256, 0, s>>>(m, gout, 1.f, net->g8);
     backward_layers(net, m, s);
     cudaMemcpyAsync(grads, net->grads, net->nparams * sizeof(float), cudaMemcpyDeviceToDevice, s);
@@ -1379,7 +1444,7 @@ int bella_cnn_train_step(bella_cnn *net, int nsamples, int nx, int ny, int nz, c
     cudaStream_t s = (cudaStream_t)stream;
     const long long n = m.nvox();
     const long long nsv = (long long)m.cx * m.cy * m.cz * 8;
-    k_pack_in<<<vec_grid(n), 256, 0, s>>>(m, in, 1.f, net->act[0], nullptr);
+    pack_in(m, in, 1.f, net->act[0], nullptr, s);
     k_pack_f32<<<vec_grid(n), 256, 0, s>>>(m, target, 1.f, net->t8);
     k_sample_norm<<<nsamples, 256, 0, s>>>(nsv, net->t8, net->inv_e2);
     forward_layers(net, m, 1.f, s);
@@ -1455,9 +1520,9 @@ int bella_cnn_train_step_op(bella_cnn *net, int nsamples, int S, const float *in
         net->flux_cap = nc;
     }
     const float ox = (float)(1.0 / (dx * dx)), oy = (float)(1.0 / (dy * dy)), oz = (float)(1.0 / (dz * dz));
-    k_pack_in<<<vec_grid(m.nvox()), 256, 0, s>>>(m, in, 1.f, net->act[0], nullptr);
+    pack_in(m, in, 1.f, net->act[0], nullptr, s);
     forward_layers(net, m, 1.f, s);
-    k_unpack<<<vec_grid(nn), 256, 0, s>>>(m, net->y8, net->yf, nullptr, in, net->omega);
+    unpack(m, net->y8, net->yf, nullptr, in, net->omega, 0, 0, s);
     k_sub<<<vec_grid(nn), 256, 0, s>>>(nn, net->yf, target, net->gf);
     // q = interior(A (y - e))
     k_crop_flux<<<vec_grid(nc), 256, 0, s>>>(nsamples, S, net->gf, nullptr, hcell, net->flux);

@@ -81,15 +81,32 @@ struct NullSpace {
     double ginv[MAXNULL * MAXNULL];
 };
 
-__device__ __forceinline__ double null_mode(const NullSpace &ns, int m, long long g) {
-    long long i, j, k;
-    if (ns.ndim == 2) { j = g / ns.nx; i = g - j * ns.nx; k = 0; }
-    else { k = g % ns.nz; long long t = g / ns.nz; j = t % ns.ny; i = t / ns.ny; }
+// parities of node g's grid indices (bit 0: i, bit 1: j, bit 2: k); 32-bit
+// division (operators have fewer than 2^31 nodes: checked when they are set)
+__device__ __forceinline__ int node_parity(const NullSpace &ns, long long g) {
+    const unsigned gg = (unsigned)g;
+    unsigned i, j, k;
+    if (ns.ndim == 2) { j = gg / (unsigned)ns.nx; i = gg - j * (unsigned)ns.nx; k = 0u; }
+    else {
+        const unsigned t = gg / (unsigned)ns.nz;
+        k = gg - t * (unsigned)ns.nz;
+        i = t / (unsigned)ns.ny;
+        j = t - i * (unsigned)ns.ny;
+    }
+    return (int)((i & 1u) | ((j & 1u) << 1) | ((k & 1u) << 2));
+}
+
+// value (+1 / -1) of null mode m at a node of parities p
+__device__ __forceinline__ double null_mode_p(const NullSpace &ns, int m, int p) {
     int par = 0;
-    if (ns.sx[m] < 0) par ^= (int)(i & 1);
-    if (ns.sy[m] < 0) par ^= (int)(j & 1);
-    if (ns.sz[m] < 0) par ^= (int)(k & 1);
+    if (ns.sx[m] < 0) par ^= p & 1;
+    if (ns.sy[m] < 0) par ^= (p >> 1) & 1;
+    if (ns.sz[m] < 0) par ^= (p >> 2) & 1;
     return par ? -1.0 : 1.0;
+}
+
+__device__ __forceinline__ double null_mode(const NullSpace &ns, int m, long long g) {
+    return null_mode_p(ns, m, node_parity(ns, g));
 }
 
 // --------------------------------------------------------------------------

@@ -285,28 +285,38 @@ k_init32(long long n, const double *r64, double inv_scale, float *r, float *rh, 
     if (threadIdx.x == 0) init_state(ks, tot[0], atol, 4.930380657631324e-32, maxiter);
 }
 
-// x64 += scale * x32, and <z_k, x64> for every null mode (projection).
+// The null modes are sign patterns of a node's index parities p (bit 0: i, 1: j,
+// 2: k), so every sum over nodes weighted by a mode is a signed combination of the
+// 8 parity-class sums, and every shift by a combination of modes is one constant
+// per class: one FP64 operation per node instead of one per mode (GB300's FP64
+// pipe bounds these passes).  The class sums live in shared memory, one slot per
+// class and thread.
+
+// x64 += scale * x32, and <z e_k, x64> for every null mode (projection)
 __global__ void __launch_bounds__(VEC_BLOCK)
 k_ir_update(long long n, double *x64, const float *x32, double scale, const double *z, NullSpace ns,
             KState *ks, double *partials, unsigned *counter) {
-    double acc[MAXNULL];
+    __shared__ double cls[8][VEC_BLOCK];
+    const int tid = threadIdx.x;
 #pragma unroll
-    for (int m = 0; m < MAXNULL; ++m) acc[m] = 0.0;
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
-         g += (long long)gridDim.x * blockDim.x) {
+    for (int q = 0; q < 8; ++q) cls[q][tid] = 0.0;
+    for (long long g = blockIdx.x * (long long)blockDim.x + tid; g < n; g += (long long)gridDim.x * blockDim.x) {
         const double xn = x64[g] + scale * (double)x32[g];
         x64[g] = xn;
-        if (ns.nm) {
-            const double zx = z[g] * xn;
-#pragma unroll
-            for (int m = 0; m < MAXNULL; ++m)
-                if (m < ns.nm) acc[m] += null_mode(ns, m, g) * zx;
-        }
+        if (ns.nm) cls[node_parity(ns, g)][tid] += z[g] * xn;
     }
     if (!ns.nm) return;
+    double acc[MAXNULL];
+#pragma unroll
+    for (int m = 0; m < MAXNULL; ++m) {
+        acc[m] = 0.0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (m < ns.nm) acc[m] += null_mode_p(ns, m, q) * cls[q][tid];
+    }
     double tot[MAXNULL];
     if (!grid_sum<MAXNULL>(acc, partials, counter, tot)) return;
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
         for (int k = 0; k < ns.nm; ++k) {
             ks->nd[k] = tot[k];
             double c = 0.0;
@@ -317,32 +327,37 @@ k_ir_update(long long n, double *x64, const float *x32, double scale, const doub
 }
 
 // x64 -= sum_l c_l e_l: removes the null-space component, keeping x in the
-// operator's range where the exact Krylov solution from x0 = 0 lies.
+// operator's range where the exact Krylov solution from x0 = 0 lies
 __global__ void k_null_shift(long long n, double *x64, const KState *ks, NullSpace ns) {
-    double c[MAXNULL];
-#pragma unroll
-    for (int m = 0; m < MAXNULL; ++m) c[m] = (m < ns.nm) ? ks->cnull[m] : 0.0;
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
-         g += (long long)gridDim.x * blockDim.x) {
+    __shared__ double D[8];                       // the shift of each parity class
+    if (threadIdx.x < 8) {
         double d = 0.0;
-#pragma unroll
-        for (int m = 0; m < MAXNULL; ++m)
-            if (m < ns.nm) d += c[m] * null_mode(ns, m, g);
-        x64[g] -= d;
+        for (int m = 0; m < ns.nm; ++m) d += ks->cnull[m] * null_mode_p(ns, m, threadIdx.x);
+        D[threadIdx.x] = d;
     }
-}
-
-// Gram entry G_kl = <z, e_k e_l> -> ks->dot_aux
-__global__ void __launch_bounds__(VEC_BLOCK)
-k_null_gram(long long n, const double *z, NullSpace ns, int k, int l, KState *ks, double *partials,
-            unsigned *counter) {
-    double a[1] = {0.0};
+    __syncthreads();
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
          g += (long long)gridDim.x * blockDim.x)
-        a[0] += z[g] * null_mode(ns, k, g) * null_mode(ns, l, g);
-    double tot[1];
-    if (!grid_sum<1>(a, partials, counter, tot)) return;
-    if (threadIdx.x == 0) ks->dot_aux = tot[0];
+        x64[g] -= D[node_parity(ns, g)];
+}
+
+// the 8 parity-class sums of z -> ks->nd[0..7]; the Gram matrix of the modes
+// follows from them, G_kl = sum_p e_k(p) e_l(p) Z_p
+__global__ void __launch_bounds__(VEC_BLOCK)
+k_null_classes(long long n, const double *z, NullSpace ns, KState *ks, double *partials, unsigned *counter) {
+    __shared__ double cls[8][VEC_BLOCK];
+    const int tid = threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) cls[q][tid] = 0.0;
+    for (long long g = blockIdx.x * (long long)blockDim.x + tid; g < n; g += (long long)gridDim.x * blockDim.x)
+        cls[node_parity(ns, g)][tid] += z[g];
+    double a[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) a[q] = cls[q][tid];
+    double tot[8];
+    if (!grid_sum<8>(a, partials, counter, tot)) return;
+    if (tid == 0)
+        for (int q = 0; q < 8; ++q) ks->nd[q] = tot[q];
 }
 
 // generic FP64 dot -> ks->dot_aux
@@ -487,15 +502,23 @@ static int setup_null_space(bella_ws *ws, cudaStream_t s, int xper, int yper, in
     }
     const int nm = ns.nm;
     double G[MAXNULL * MAXNULL];
+    k_null_classes<<<ws->grid_vec, VEC_BLOCK, 0, s>>>(ws->n, ws->z64, ns, ws->ks, ws->partials, ws->counter);
+    ws->launches++;
+    BELLA_CUDA(cudaGetLastError());
+    BELLA_CUDA(cudaMemcpyAsync(ws->ks_host, ws->ks, sizeof(KState), cudaMemcpyDeviceToHost, s));
+    BELLA_CUDA(cudaStreamSynchronize(s));
+    auto sign = [&](int m, int p) {                   // null_mode_p on the host
+        int par = 0;
+        if (ns.sx[m] < 0) par ^= p & 1;
+        if (ns.sy[m] < 0) par ^= (p >> 1) & 1;
+        if (ns.sz[m] < 0) par ^= (p >> 2) & 1;
+        return par ? -1.0 : 1.0;
+    };
     for (int k = 0; k < nm; ++k)
         for (int l = 0; l < nm; ++l) {
-            k_null_gram<<<ws->grid_vec, VEC_BLOCK, 0, s>>>(ws->n, ws->z64, ns, k, l, ws->ks, ws->partials,
-                                                           ws->counter);
-            ws->launches++;
-            BELLA_CUDA(cudaGetLastError());
-            BELLA_CUDA(cudaMemcpyAsync(ws->ks_host, ws->ks, sizeof(KState), cudaMemcpyDeviceToHost, s));
-            BELLA_CUDA(cudaStreamSynchronize(s));
-            G[k * nm + l] = ws->ks_host->dot_aux;
+            double g = 0.0;
+            for (int q = 0; q < 8; ++q) g += sign(k, q) * sign(l, q) * ws->ks_host->nd[q];
+            G[k * nm + l] = g;
         }
     // Gauss-Jordan inverse with partial pivoting (nm <= 8)
     double A[MAXNULL][2 * MAXNULL];
@@ -525,6 +548,8 @@ int bella_op2d_set(bella_ws *ws, const bella_op2d *op, void *stream) {
     if (!op->hplusx || !op->hplusy || !op->cxx || !op->cyy || !op->diag_inv)
         return set_err(BELLA_EINVAL, "bella_op2d_set: hplusx, hplusy, cxx, cyy, diag_inv are required");
     if (!(op->dx > 0.0) || !(op->dy > 0.0)) return set_err(BELLA_EINVAL, "bella_op2d_set: dx, dy must be > 0");
+    if ((long long)(op->nx + 1) * (op->ny + 1) >= (1LL << 31))   // node indices are 32-bit in the null space
+        return set_err(BELLA_EINVAL, "bella_op2d_set: (nx+1)(ny+1) must be below 2^31");
     if (op->x_wall < 0 || op->x_wall > 1 || op->y_wall < 0 || op->y_wall > BELLA_Y_MIRROR)
         return set_err(BELLA_EINVAL, "bella_op2d_set: x_wall must be 0 or 1, y_wall 0, 1 or BELLA_Y_MIRROR");
     if (op->y_wall == BELLA_Y_MIRROR && op->x_wall)
@@ -1092,10 +1117,24 @@ k_flex_corr_in(long long n, const float *in, float *Ay, KState *ks, double *part
     if (ks->done) return;
     DF d0;
     d0.zero();
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
-        const float d = in[g] - Ay[g];
-        Ay[g] = d;
-        d0.add_prod(d, d);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long g0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; g0 < n; g0 += 4 * stride) {
+        float a[4], b[4];                             // four elements, loads first
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const long long g = g0 + u * stride;
+            a[u] = g < n ? in[g] : 0.f;
+            b[u] = g < n ? Ay[g] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const long long g = g0 + u * stride;
+            if (g < n) {
+                const float d = a[u] - b[u];
+                Ay[g] = d;
+                d0.add_prod(d, d);
+            }
+        }
     }
     double a[1] = {d0.value()}, tot[1];
     if (!grid_sum<1>(a, partials, counter, tot)) return;
@@ -1105,8 +1144,21 @@ k_flex_corr_in(long long n, const float *in, float *Ay, KState *ks, double *part
 __global__ void __launch_bounds__(VEC_BLOCK)
 k_flex_add(long long n, float *out, const float *add, const KState *ks) {
     if (ks->done) return;
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x)
-        out[g] += add[g];
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long g0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; g0 < n; g0 += 4 * stride) {
+        float a[4], b[4];                             // four elements, loads first
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const long long g = g0 + u * stride;
+            a[u] = g < n ? out[g] : 0.f;
+            b[u] = g < n ? add[g] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const long long g = g0 + u * stride;
+            if (g < n) out[g] = a[u] + b[u];
+        }
+    }
 }
 
 // the preconditioner of the flexible solver: the network, the background
@@ -1221,6 +1273,12 @@ constexpr int FG_MAXV = FG_MAXM + 1;
 static int fg_xblk() { return num_sms() * 8; }
 constexpr int FG_GROUP = 8;         // inner products per block
 
+// The Arnoldi vectors are columns of leading dimension fg_ld(n), a multiple of 4,
+// so every column starts on a 16-byte boundary: the Gram-Schmidt kernels read
+// four consecutive elements at a time (float4), the n mod 4 last ones in block 0.
+__device__ __forceinline__ float4 ld4(const float *p, long long i4) { return reinterpret_cast<const float4 *>(p)[i4]; }
+__device__ __forceinline__ void st4(float *p, long long i4, float4 v) { reinterpret_cast<float4 *>(p)[i4] = v; }
+
 // block (bx, gy): partial sums of <V_i, w> for the FG_GROUP vectors i of group gy
 // over a grid-stride share -> part[i * gridDim.x + bx]; w is read once per group.
 // With FG_XBLK x 256 threads each thread adds a few tens of products (FP32, on
@@ -1233,12 +1291,26 @@ k_fg_mdot(long long n, const float *__restrict__ V, long long ld, int nv, const 
     float acc[FG_GROUP];
 #pragma unroll
     for (int q = 0; q < FG_GROUP; ++q) acc[q] = 0.f;
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
-        const float wg = w[g];
+    const long long n4 = n >> 2;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x) {
+        const float4 wv = ld4(w, i);
 #pragma unroll
         for (int q = 0; q < FG_GROUP; ++q)
-            if (q < cnt) acc[q] = fmaf(V[(i0 + q) * ld + g], wg, acc[q]);
+            if (q < cnt) {
+                const float4 v = ld4(V + (i0 + q) * ld, i);
+                acc[q] = fmaf(v.x, wv.x, acc[q]);
+                acc[q] = fmaf(v.y, wv.y, acc[q]);
+                acc[q] = fmaf(v.z, wv.z, acc[q]);
+                acc[q] = fmaf(v.w, wv.w, acc[q]);
+            }
     }
+    if (blockIdx.x == 0)
+        for (long long g = 4 * n4 + threadIdx.x; g < n; g += blockDim.x) {
+            const float wg = w[g];
+#pragma unroll
+            for (int q = 0; q < FG_GROUP; ++q)
+                if (q < cnt) acc[q] = fmaf(V[(i0 + q) * ld + g], wg, acc[q]);
+        }
     __shared__ double red[FG_GROUP][VEC_BLOCK / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
@@ -1273,18 +1345,39 @@ __global__ void __launch_bounds__(256) k_fg_reduce(int nblk, const double *part,
 
 // w -= sum_i h[i] V_i, and with norm per-block partial sums of the new <w, w> (slot 0)
 __global__ void __launch_bounds__(VEC_BLOCK)
-k_fg_update(long long n, const float *V, long long ld, int nv, const double *h, float *w, int norm, double *part) {
+k_fg_update(long long n, const float *__restrict__ V, long long ld, int nv, const double *__restrict__ h,
+            float *__restrict__ w, int norm, double *__restrict__ part) {
     __shared__ float hs[FG_MAXV];
     if ((int)threadIdx.x < nv) hs[threadIdx.x] = (float)h[threadIdx.x];
     __syncthreads();
     DF acc;
     acc.zero();
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
-        float wg = w[g];
-        for (int i = 0; i < nv; ++i) wg = fmaf(-hs[i], V[i * ld + g], wg);
-        w[g] = wg;
-        if (norm) acc.add_prod(wg, wg);
+    const long long n4 = n >> 2;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x) {
+        float4 wv = ld4(w, i);
+        for (int q = 0; q < nv; ++q) {
+            const float4 v = ld4(V + q * ld, i);
+            const float hq = -hs[q];
+            wv.x = fmaf(hq, v.x, wv.x);
+            wv.y = fmaf(hq, v.y, wv.y);
+            wv.z = fmaf(hq, v.z, wv.z);
+            wv.w = fmaf(hq, v.w, wv.w);
+        }
+        st4(w, i, wv);
+        if (norm) {
+            acc.add_prod(wv.x, wv.x);
+            acc.add_prod(wv.y, wv.y);
+            acc.add_prod(wv.z, wv.z);
+            acc.add_prod(wv.w, wv.w);
+        }
     }
+    if (blockIdx.x == 0)
+        for (long long g = 4 * n4 + threadIdx.x; g < n; g += blockDim.x) {
+            float wg = w[g];
+            for (int q = 0; q < nv; ++q) wg = fmaf(-hs[q], V[q * ld + g], wg);
+            w[g] = wg;
+            if (norm) acc.add_prod(wg, wg);
+        }
     if (!norm) return;
     __shared__ double red[VEC_BLOCK / 32];
     const double v = warp_sum(acc.value());
@@ -1297,25 +1390,47 @@ k_fg_update(long long n, const float *V, long long ld, int nv, const double *h, 
     }
 }
 
-// out = w / sqrt(*nrm2) (in place allowed); zero when the norm is not positive
+// out = w / sqrt(*nrm2) (in place allowed); zero when the norm is not positive;
+// both 16-byte aligned (Arnoldi columns, the workspace's r32)
 __global__ void k_fg_scale(long long n, const float *w, const double *nrm2, float *out) {
     const double q = *nrm2;
     const float inv = (q > 0.0 && isfinite(q)) ? (float)(1.0 / sqrt(q)) : 0.f;
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x)
-        out[g] = w[g] * inv;
+    const long long n4 = n >> 2;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x) {
+        const float4 v = ld4(w, i);
+        st4(out, i, make_float4(v.x * inv, v.y * inv, v.z * inv, v.w * inv));
+    }
+    if (blockIdx.x == 0)
+        for (long long g = 4 * n4 + threadIdx.x; g < n; g += blockDim.x) out[g] = w[g] * inv;
 }
 
-// x += sum_i y[i] Z_i
+// x += sum_i y[i] Z_i (x: the workspace's x32, 16-byte aligned)
 __global__ void k_fg_combine(long long n, const float *Z, long long ld, int nz, const double *y, float *x) {
     __shared__ float ys[FG_MAXM];
     if ((int)threadIdx.x < nz) ys[threadIdx.x] = (float)y[threadIdx.x];
     __syncthreads();
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
-        float xg = x[g];
-        for (int i = 0; i < nz; ++i) xg = fmaf(ys[i], Z[i * ld + g], xg);
-        x[g] = xg;
+    const long long n4 = n >> 2;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x) {
+        float4 xv = ld4(x, i);
+        for (int q = 0; q < nz; ++q) {
+            const float4 v = ld4(Z + q * ld, i);
+            xv.x = fmaf(ys[q], v.x, xv.x);
+            xv.y = fmaf(ys[q], v.y, xv.y);
+            xv.z = fmaf(ys[q], v.z, xv.z);
+            xv.w = fmaf(ys[q], v.w, xv.w);
+        }
+        st4(x, i, xv);
     }
+    if (blockIdx.x == 0)
+        for (long long g = 4 * n4 + threadIdx.x; g < n; g += blockDim.x) {
+            float xg = x[g];
+            for (int q = 0; q < nz; ++q) xg = fmaf(ys[q], Z[q * ld + g], xg);
+            x[g] = xg;
+        }
 }
+
+// leading dimension of the Arnoldi columns: n rounded up to a multiple of 4
+static long long fg_ld(long long n) { return (n + 3) & ~3LL; }
 
 static int fg_ensure(bella_ws *ws, int m) {
     const long long n = ws->n;
@@ -1324,8 +1439,8 @@ static int fg_ensure(bella_ws *ws, int m) {
     ws->fg_v = ws->fg_z = nullptr;
     ws->fg_part = ws->fg_dev = nullptr;
     ws->fg_m = 0;
-    BELLA_CUDA(cudaMalloc(&ws->fg_v, (size_t)(m + 1) * n * sizeof(float)));
-    BELLA_CUDA(cudaMalloc(&ws->fg_z, (size_t)m * n * sizeof(float)));
+    BELLA_CUDA(cudaMalloc(&ws->fg_v, (size_t)(m + 1) * fg_ld(n) * sizeof(float)));
+    BELLA_CUDA(cudaMalloc(&ws->fg_z, (size_t)m * fg_ld(n) * sizeof(float)));
     BELLA_CUDA(cudaMalloc(&ws->fg_part, (size_t)MAXGRID * (FG_MAXV + 1) *
                                         sizeof(double)));
     BELLA_CUDA(cudaMalloc(&ws->fg_dev, 4 * (FG_MAXV + 1) * sizeof(double)));
@@ -1347,6 +1462,7 @@ static int fgmres_cycle(bella_ws *ws, const Precond &pc, int m, double rel, cuda
     double *h1 = ws->fg_dev, *h2 = ws->fg_dev + (FG_MAXV + 1), *nrm = ws->fg_dev + 2 * (FG_MAXV + 1);
     double *unit = ws->fg_dev + 3 * (FG_MAXV + 1);   // 1.0: sum of squares of a basis vector
     float *V = ws->fg_v, *Z = ws->fg_z;
+    const long long ld = fg_ld(n);
     int rc = sync_state(ws, s);
     if (rc != BELLA_OK) return rc;
     const double beta = sqrt(ws->ks_host->rr);
@@ -1362,18 +1478,18 @@ static int fgmres_cycle(bella_ws *ws, const Precond &pc, int m, double rel, cuda
     double hhost[3 * (FG_MAXV + 1)];
     int j = 0, k = 0;
     for (j = 0; j < m; ++j) {
-        float *vj = V + (size_t)j * n, *zj = Z + (size_t)j * n, *w = V + (size_t)(j + 1) * n;
+        float *vj = V + (size_t)j * ld, *zj = Z + (size_t)j * ld, *w = V + (size_t)(j + 1) * ld;
         rc = precond_apply(ws, pc, vj, zj, unit, s);
         if (rc != BELLA_OK) return rc;
         op_apply(ws, 1, zj, w, s);
         const int nv = j + 1;
         const unsigned ng = (unsigned)((nv + FG_GROUP - 1) / FG_GROUP);
-        k_fg_mdot<<<dim3(xb, ng), VEC_BLOCK, 0, s>>>(n, V, n, nv, w, ws->fg_part);
+        k_fg_mdot<<<dim3(xb, ng), VEC_BLOCK, 0, s>>>(n, V, ld, nv, w, ws->fg_part);
         k_fg_reduce<<<nv, 256, 0, s>>>(xb, ws->fg_part, nv, h1);
-        k_fg_update<<<gv, VEC_BLOCK, 0, s>>>(n, V, n, nv, h1, w, 0, ws->fg_part);
-        k_fg_mdot<<<dim3(xb, ng), VEC_BLOCK, 0, s>>>(n, V, n, nv, w, ws->fg_part);
+        k_fg_update<<<gv, VEC_BLOCK, 0, s>>>(n, V, ld, nv, h1, w, 0, ws->fg_part);
+        k_fg_mdot<<<dim3(xb, ng), VEC_BLOCK, 0, s>>>(n, V, ld, nv, w, ws->fg_part);
         k_fg_reduce<<<nv, 256, 0, s>>>(xb, ws->fg_part, nv, h2);
-        k_fg_update<<<gv, VEC_BLOCK, 0, s>>>(n, V, n, nv, h2, w, 1, ws->fg_part);
+        k_fg_update<<<gv, VEC_BLOCK, 0, s>>>(n, V, ld, nv, h2, w, 1, ws->fg_part);
         k_fg_reduce<<<1, 256, 0, s>>>(gv, ws->fg_part, 1, nrm);
         k_fg_scale<<<gv, VEC_BLOCK, 0, s>>>(n, w, nrm, w);
         ws->launches += 10;
@@ -1410,7 +1526,7 @@ static int fgmres_cycle(bella_ws *ws, const Precond &pc, int m, double rel, cuda
         y[i] = H[i][i] != 0.0 ? t / H[i][i] : 0.0;
     }
     BELLA_CUDA(cudaMemcpyAsync(ws->fg_dev, y, k * sizeof(double), cudaMemcpyHostToDevice, s));
-    k_fg_combine<<<gv, VEC_BLOCK, 0, s>>>(n, Z, n, k, ws->fg_dev, ws->x32);
+    k_fg_combine<<<gv, VEC_BLOCK, 0, s>>>(n, Z, ld, k, ws->fg_dev, ws->x32);
     ws->launches += 1;
     BELLA_CUDA(cudaStreamSynchronize(s));   // y lives on this stack frame until the copy is done
     *iters = k;
