@@ -500,7 +500,18 @@ k_sp_factor(int Kx, int ny, int Kz, const double *mux, const double *muz, const 
     for (int j = j0; j < ny; ++j) {
         const double a = j > j0 ? off(j - 1) : 0.0;
         const double c = j < ny - 1 ? off(j) : 0.0;
-        const double inv = 1.0 / (diag(j) - a * cprev);
+        // 1 / den by Newton-Raphson from an FP32 seed: each step x <- x (2 - den x)
+        // squares the relative error (2^-23 -> 2^-46 -> below FP64 rounding), four
+        // FP64 FMAs instead of an FP64 division (GB300's FP64 pipe bounds this loop)
+        const double den = diag(j) - a * cprev;
+        double inv;
+        if (fabs(den) > 1e-30 && fabs(den) < 1e30) {   // the seed within FP32's range
+            inv = (double)(1.0f / (float)den);
+            inv = inv * fma(-den, inv, 2.0);
+            inv = inv * fma(-den, inv, 2.0);
+        } else {
+            inv = 1.0 / den;
+        }
         cprev = c * inv;
         la[(long long)j * nl + line] = (float)a;
         lc[(long long)j * nl + line] = (float)cprev;
