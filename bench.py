@@ -217,8 +217,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "rtol": TOL,
-                                           "l2": "inputs resident on host"},
+            "data": "synthetic", "config": solve2d_config(args, _dist()[0], args.seeds),
             "cpu_baseline": {"value": value, "unit": "solves/s", "cores": 1, "kind": "port",
                              "sample": "NumPy lap2D_gather_new restatement + scipy bicgstab (FP64), "
                                        "bounded iteration samples on seed 0; solves/s = 1/(s per iteration x "
@@ -383,9 +382,7 @@ def solve2d_line(args, dev, local, rank, world, dist, steps, warmup, nseeds, e2e
         "warmup": warmup, "ms_per_step": ms / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": {"fp64": "f64", "mixed": "f32+f64", "df64": "f32x2 (double-float)"}[args.precision],
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "rtol": TOL, "precision": args.precision,
-                   "l2": "flushed (256 MB write) before every step", "seeds": nseeds,
-                   "parallelism": "replicas" if world > 1 else "single"},
+        "config": solve2d_config(args, world, nseeds),
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "path": "pybella_gb300.linalg.bicgstab on NumPy operands"},
         "gpu_launches": launches,
@@ -764,12 +761,15 @@ def run_learned3d(args):
     h2d = sum(t.numel() * t.element_size() for t in host.values())
     e2e_ms = []
     ws_e2e = _lib.Workspace(local)
+    bg_e2e = []                                      # one background solve per grid, as a time loop keeps it
     for i in range(0 if args.no_e2e else args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         Ah = NodalHelmholtz3D(host["hplusx"], host["hplusy"], host["hplusz"], None, host["diag_inv"], *shape,
                               w["dx"], w["dy"], w["dz"], walls=w["walls"], ws=ws_e2e)
-        bg = BackgroundSolve(Ah)
+        if not bg_e2e:                               # made in the first (warm-up) call
+            bg_e2e.append(BackgroundSolve(Ah))
+        bg = bg_e2e[0].update(Ah)                    # from this call's coefficients
         with warnings.catch_warnings():
             warnings.simplefilter("ignore", RuntimeWarning)
             x, _ = Ah.solve(host["b"], tol=TOL, maxiter=20000,
@@ -778,8 +778,9 @@ def run_learned3d(args):
         torch.cuda.synchronize()
         if i >= args.warmup:
             e2e_ms.append((time.perf_counter() - t0) * 1000.0)
-        bg.close()
         del Ah
+    for b_ in bg_e2e:
+        b_.close()
     # the learned solve's kernels: network application and background solve, timed alone
     bg = BackgroundSolve(A)
     r32 = torch.randn(A.n, device=dev)
@@ -847,7 +848,10 @@ def run_learned3d(args):
                                                 / max(L["stats"][-1]["iterations"], 1),
                                                 "what": "the same flexible GMRES with the background solve alone"},
         "e2e": ({"value": 1000.0 / statistics.median(e2e_ms), "unit": "solves/s", "h2d_bytes_per_step": h2d,
-                 "d2h_bytes_per_step": A.n * 8} if e2e_ms else None),
+                 "d2h_bytes_per_step": A.n * 8,
+                 "path": "NodalHelmholtz3D from pinned host planes, BackgroundSolve.update, solve(preconditioner="
+                         "LearnedPreconditioner, method='fgmres'), x to the host; median of the timed calls"}
+                if e2e_ms else None),
         "gpu_launches": L["launches"],
         "roofline": {"bound": "tensor", "achieved": ach, "peak": tpeak, "unit": "TFLOP/s", "frac": ach / tpeak,
                      "traffic": CONV_TRAFFIC,
@@ -978,9 +982,7 @@ def run_step2d(args):
                           "value": world * 1000.0 / ms, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
                           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                           "vs_baseline": None, "dtype": "f64 state, %s solves" % args.precision, "data": "synthetic",
-                          "config": {"workload": "2D time step, rising bubble 160x80 cells", "parallelism":
-                                     "replicas" if world > 1 else "single GPU",
-                                     "l2": "state of 1 MB, L2-resident (a launch-bound workload)"},
+                          "config": step2d_config(world),
                           "solve_iterations": its, "clocks": clocks, "cpu_baseline": cpu,
                           "gpu_launches": None}), flush=True)
 
@@ -988,6 +990,31 @@ def run_step2d(args):
 ENS_STEPS_WORKLOAD = ("ensemble time steps: 48 rising-bubble members (16 each at 160x80, 320x160, 640x320 cells, "
                       "amplitude N(2 K, 0.2 K), centre N(0, 200 m)), each step's two projections of all members "
                       "solved in one persistent launch (rtol 1e-10)")
+
+
+def solve2d_config(args, world, nseeds):
+    """config of the 2049x1025 standalone-solve lines (both arms)."""
+    return {"workload": WORKLOAD, "nx": NX, "ny": NY, "rtol": TOL, "precision": args.precision,
+            "l2": "GPU arm: flushed (256 MB write) before every step; CPU arm: host-resident inputs",
+            "seeds": nseeds, "parallelism": "replicas" if world > 1 else "single"}
+
+
+def step2d_config(world):
+    """config of the 2D time-step lines (both arms, so the driver sees the same config)."""
+    return {"workload": "2D time step, rising bubble 160x80 cells",
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "l2": "state of 1 MB, L2-resident (a launch-bound workload)"}
+
+
+def ens_steps_config(world):
+    """config of the ensemble time-step lines (both arms): 16 members on each grid."""
+    from pybella_gb300.workloads import ENSEMBLE_GRIDS
+    nodes = [(cx + 1, cy + 1) for cx, cy in ENSEMBLE_GRIDS]
+    return {"workload": ENS_STEPS_WORKLOAD, "members": 16 * len(nodes),
+            "unknowns": int(sum(16 * nx * ny for nx, ny in nodes)),
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "l2": "state of %.0f MB resident (larger than L2 across the ensemble)"
+                  % (sum(16 * 6 * 8 * (nx + 3) * (ny + 3) for nx, ny in nodes) / 1e6)}
 
 
 def ensemble_steps_line(args, local, rank, world, nsteps, warmup, want_cpu):
@@ -1040,10 +1067,7 @@ def ensemble_steps_line(args, local, rank, world, nsteps, warmup, want_cpu):
         "value": 2.0 * nmem * nsteps / (ms / 1000.0), "unit": "solves/s", "n_gpus": world, "steps": nsteps,
         "warmup": warmup, "ms_per_step": ms / nsteps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64 state, %s solves" % prec, "data": "synthetic",
-        "config": {"workload": ENS_STEPS_WORKLOAD, "members": nmem, "unknowns": int(sizes.sum()),
-                   "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2": "state of %.0f MB resident (larger than L2 across the ensemble)" % (
-                       sum(6 * 8 * (int(m.adv.inx) + 3) * (int(m.adv.iny) + 3) for m in members) / 1e6)},
+        "config": ens_steps_config(world),
         "member_steps_per_s": nmem * nsteps / (ms / 1000.0),
         "solver": {"iterations_mean_per_grid": {
             "%dx%d" % (int(m.adv.inx) - 1, int(m.adv.iny) - 1): float(iters[:, k].mean())
@@ -1144,7 +1168,7 @@ def main():
                 print(json.dumps({"impl": "reference", "metric": "2D time steps/s (rising bubble 160x80, "
                                   "projections to 1e-10)", "value": v, "unit": "steps/s", "n_gpus": 1,
                                   "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-                                  "config": {"workload": "2D time step, rising bubble 160x80 cells"},
+                                  "config": step2d_config(_dist()[0]),
                                   "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
                                                    "sample": "%d steps of the oracle's time step" % k},
                                   "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0,
@@ -1161,7 +1185,7 @@ def main():
                 print(json.dumps({"impl": "reference", "metric": "ensemble time steps: projection solves/s "
                                   "(48 uneven members, batched)", "value": ref, "unit": "solves/s",
                                   "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-                                  "config": {"workload": ENS_STEPS_WORKLOAD},
+                                  "config": ens_steps_config(_dist()[0]),
                                   "cpu_baseline": {"value": ref, "unit": "solves/s", "cores": 1,
                                                    "kind": "port",
                                                    "sample": "%d steps of the oracle's time step on a 160x80 member, "

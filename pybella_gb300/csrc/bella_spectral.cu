@@ -545,10 +545,10 @@ k_sp_lines(int Kx, int ny, int Kz, float *__restrict__ W, const double *__restri
         for (int j = 0; j < ny; ++j) ps += (L.cat == 2 && (j & 1)) ? -(double)w[(long long)j * Kz] : (double)w[(long long)j * Kz];
         proj = (float)(ps / ny);
     }
-    // sweeps in batches of 8 rows: the 8 loads of a batch are issued before its
+    // sweeps in batches of 12 rows: the loads of a batch are issued before its
     // dependent arithmetic, and its stores after it (the in-place rows would
     // otherwise serialise every load behind the previous row's store)
-    constexpr int B = 8;
+    constexpr int B = 12;
     const int j0 = L.cat ? 1 : 0;
     float d = 0.f;
     for (int jb = j0; jb < ny; jb += B) {
