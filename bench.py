@@ -762,6 +762,7 @@ def run_learned3d(args):
     e2e_ms = []
     ws_e2e = _lib.Workspace(local)
     bg_e2e = []                                      # one background solve per grid, as a time loop keeps it
+    xh = torch.empty(A.n, dtype=torch.float64, pin_memory=True)   # the caller's pinned result buffer
     for i in range(0 if args.no_e2e else args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -774,7 +775,7 @@ def run_learned3d(args):
             warnings.simplefilter("ignore", RuntimeWarning)
             x, _ = Ah.solve(host["b"], tol=TOL, maxiter=20000,
                             preconditioner=learned.LearnedPreconditioner(bg, net, "post"), **kw_learned)
-        xh = x.cpu()
+        xh.copy_(x)
         torch.cuda.synchronize()
         if i >= args.warmup:
             e2e_ms.append((time.perf_counter() - t0) * 1000.0)
@@ -850,7 +851,8 @@ def run_learned3d(args):
         "e2e": ({"value": 1000.0 / statistics.median(e2e_ms), "unit": "solves/s", "h2d_bytes_per_step": h2d,
                  "d2h_bytes_per_step": A.n * 8,
                  "path": "NodalHelmholtz3D from pinned host planes, BackgroundSolve.update, solve(preconditioner="
-                         "LearnedPreconditioner, method='fgmres'), x to the host; median of the timed calls"}
+                         "LearnedPreconditioner, method='fgmres'), x into a pinned host buffer; median of the "
+                         "timed calls"}
                 if e2e_ms else None),
         "gpu_launches": L["launches"],
         "roofline": {"bound": "tensor", "achieved": ach, "peak": tpeak, "unit": "TFLOP/s", "frac": ach / tpeak,
