@@ -1294,15 +1294,16 @@ k_fg_mdot(long long n, const float *__restrict__ V, long long ld, int nv, const 
     const long long n4 = n >> 2;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x) {
         const float4 wv = ld4(w, i);
+        float4 v[FG_GROUP];                           // every vector's load issued before the products
 #pragma unroll
-        for (int q = 0; q < FG_GROUP; ++q)
-            if (q < cnt) {
-                const float4 v = ld4(V + (i0 + q) * ld, i);
-                acc[q] = fmaf(v.x, wv.x, acc[q]);
-                acc[q] = fmaf(v.y, wv.y, acc[q]);
-                acc[q] = fmaf(v.z, wv.z, acc[q]);
-                acc[q] = fmaf(v.w, wv.w, acc[q]);
-            }
+        for (int q = 0; q < FG_GROUP; ++q) v[q] = q < cnt ? ld4(V + (i0 + q) * ld, i) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < FG_GROUP; ++q) {
+            acc[q] = fmaf(v[q].x, wv.x, acc[q]);
+            acc[q] = fmaf(v[q].y, wv.y, acc[q]);
+            acc[q] = fmaf(v[q].z, wv.z, acc[q]);
+            acc[q] = fmaf(v[q].w, wv.w, acc[q]);
+        }
     }
     if (blockIdx.x == 0)
         for (long long g = 4 * n4 + threadIdx.x; g < n; g += blockDim.x) {
