@@ -1269,8 +1269,11 @@ static int run_flex(bella_ws *ws, const Precond &pc, const bella_solve_opts *o, 
 constexpr int FG_MAXM = 64;
 constexpr int FG_MAXV = FG_MAXM + 1;
 
-// blocks per group of inner products: 8 per SM (enough warps to cover memory latency)
-static int fg_xblk() { return num_sms() * 8; }
+// blocks of the Gram-Schmidt kernels: 4 per SM, one resident wave (at 40-52
+// registers a thread 4-6 blocks of 256 fit an SM; 8 per SM ran a second, partial
+// wave that cost ~10 us a launch: 41 -> 30 us for the inner products with one
+// basis vector at 257x129x257)
+static int fg_xblk() { return num_sms() * 4; }
 constexpr int FG_GROUP = 8;         // inner products per block
 
 // The Arnoldi vectors are columns of leading dimension fg_ld(n), a multiple of 4,
@@ -1459,7 +1462,7 @@ static int fg_ensure(bella_ws *ws, int m) {
 static int fgmres_cycle(bella_ws *ws, const Precond &pc, int m, double rel, cudaStream_t s, int *iters,
                         int *status) {
     const long long n = ws->n;
-    const int gv = ws->grid_vec;
+    const int gv = fg_xblk();                          // one resident wave (see fg_xblk)
     double *h1 = ws->fg_dev, *h2 = ws->fg_dev + (FG_MAXV + 1), *nrm = ws->fg_dev + 2 * (FG_MAXV + 1);
     double *unit = ws->fg_dev + 3 * (FG_MAXV + 1);   // 1.0: sum of squares of a basis vector
     float *V = ws->fg_v, *Z = ws->fg_z;
