@@ -9,7 +9,8 @@ theta = rhoY / rho is compared every 0.1 against
 * the oracle's run of the same case (``fullrun_oracle_kat.npz``; the oracle's
   step and loop are pinned bit for bit to the reference's ``do``), and
 * the reference's own run (``fullrun_kat.npz``, generated by running pyBELLA
-  here as plain Python; it holds the output times that run had reached).
+  as plain Python through ``tests/golden/make_fullrun.py``: all ten output times
+  0.1 ... 1.0, 216 steps, about five hours on the host).
 
 The bar is relative L2 <= 1e-6 at every output time, t_end included; the
 errors are also printed relative to the bubble's perturbation theta - 1.
