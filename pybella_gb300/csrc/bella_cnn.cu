@@ -863,6 +863,217 @@ k_wgrad(int nx, int ny, int nz, int xseg, const __nv_bfloat16 *__restrict__ in, 
 template <int CINR, int COUTR>
 constexpr size_t wgrad_smem() { return sizeof(float) * ((size_t)CH_VOX * CINR + 256 * COUTR); }
 
+// ---- weight gradients on tcgen05 ---------------------------------------------------
+// dW[t][ci][co] = sum_v in[v + off(t)][ci] g[v][co] as a GEMM whose K runs over voxels.
+// Items are (x-plane q of the gradient, block of TC_ROWS padded (y, z) rows); each CTA
+// (one per SM) takes a contiguous share.  Per item, a stage holds input planes q-1, q,
+// q+1 in the forward kernel's layout ([16-byte channel chunk][row][8 channels], rows
+// f0-PZ-1 .. f0+TC_ROWS+PZ of the zero-padded plane, zeros outside the plane and the
+// sample's x-segment) and, next in the same chunk sequence, the gradient rows f0 ..
+// f0+TC_ROWS-1 of plane q.  Read MN-major (a chunk's 8 channels contiguous, rows 16
+// bytes apart), the stage's 16 chunks are one A operand of 128 rows (plane q-1+s,
+// channel) -- rows past plane q+1 read the gradient or unused chunks and are
+// discarded -- and the gradient chunks are B (N = COUT).  For tap (dy, dz) A starts
+// dy*PZ + dz rows later, so the nine (dy, dz) accumulators of COUT tensor-memory
+// columns take the same B; they collect every item of the CTA and are added into dW
+// once.  Two stages: the copies of the next item overlap the MMAs of this one.
+constexpr int WG_THREADS = 128;
+constexpr int WG_CHUNKS = 16;               // 16-byte chunks per stage (A reads all 16)
+
+__host__ __device__ constexpr size_t wg_smem_bytes(int pz) {
+    return (size_t)2 * WG_CHUNKS * (TC_ROWS + 2 * pz + 2) * 16;
+}
+
+template <int CIN, int COUT, int CINR, int COUTR>
+__global__ void __launch_bounds__(WG_THREADS, 1)
+k_wgrad_tc(int nx, int ny, int nz, int xseg, long long work, const __nv_bfloat16 *__restrict__ in,
+           const __nv_bfloat16 *__restrict__ g, float *dW, int *err) {
+    static_assert(CIN == 16 || CIN == 32, "input channels: 16 or 32");
+    static_assert(COUT == 16 || COUT == 32, "gradient channels: 16 or 32");
+    constexpr int NCH = CIN / 8, NCG = COUT / 8;
+    static_assert(3 * NCH + NCG <= WG_CHUNKS, "three input planes and the gradient fit a stage");
+    constexpr int TMEM_COLS = 9 * COUT <= 256 ? 256 : 512;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bar_mma[2];
+    __shared__ __align__(8) uint64_t bar_done;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int never;                                 // the waits here are not cut short by another role
+    const int PZ = nz + 2, PY = ny + 2;
+    const int L = TC_ROWS + 2 * PZ + 2;                   // staged rows per chunk
+    const uint32_t CS = (uint32_t)L * 16, SS = (uint32_t)WG_CHUNKS * CS;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    auto sa = [](const void *p) { return (uint32_t)__cvta_generic_to_shared(p); };
+    const uint32_t s0 = sa(smem);
+    if (tid == 0) {
+        for (int k = 0; k < 2; ++k) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sa(&bar_mma[k])));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sa(&bar_done)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+        never = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sa(&tmem_slot)),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_slot;
+    const int plane = PY * PZ;
+    const int nblk = (plane + TC_ROWS - 1) / TC_ROWS;
+    const long long lo = (long long)blockIdx.x * work;
+    const long long n_it = max(0LL, min(lo + work, (long long)nblk * nx) - lo);
+
+    auto stage = [&](long long it, int buf) {
+        const int q = (int)(it / nblk), f0 = (int)(it - (long long)q * nblk) * TC_ROWS;
+        const int seg = q / xseg;
+        const uint32_t base = s0 + (uint32_t)buf * SS;
+        for (int e = tid; e < 3 * L; e += WG_THREADS) {   // input planes q-1, q, q+1
+            const int s = e / L, rb = e - s * L;
+            const int p = q - 1 + s, f = f0 - PZ - 1 + rb;
+            const __nv_bfloat16 *src = in;
+            uint32_t bytes = 0;
+            if (p >= 0 && p < nx && p / xseg == seg && f >= 0 && f < plane) {
+                const int yq = f / PZ;
+                const int y = yq - 1, z = f - yq * PZ - 1;
+                if (y >= 0 && y < ny && z >= 0 && z < nz) {
+                    src = in + (((size_t)p * ny + y) * nz + z) * CIN;
+                    bytes = 16;
+                }
+            }
+#pragma unroll
+            for (int ch = 0; ch < NCH; ++ch)
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
+                             ::"r"(base + (uint32_t)(((s * NCH + ch) * L + rb) * 16)), "l"(src + (bytes ? ch * 8 : 0)),
+                               "r"(bytes));
+        }
+        for (int rb = tid; rb < TC_ROWS; rb += WG_THREADS) {   // gradient rows of plane q
+            const int f = f0 + rb;
+            const __nv_bfloat16 *src = g;
+            uint32_t bytes = 0;
+            if (f < plane) {
+                const int yq = f / PZ;
+                const int y = yq - 1, z = f - yq * PZ - 1;
+                if (y >= 0 && y < ny && z >= 0 && z < nz) {
+                    src = g + (((size_t)q * ny + y) * nz + z) * COUT;
+                    bytes = 16;
+                }
+            }
+#pragma unroll
+            for (int ch = 0; ch < NCG; ++ch)
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
+                             ::"r"(base + (uint32_t)(((3 * NCH + ch) * L + rb) * 16)), "l"(src + (bytes ? ch * 8 : 0)),
+                               "r"(bytes));
+        }
+        asm volatile("cp.async.commit_group;");
+    };
+    // MN-major, no swizzle: 8-row K groups 128 bytes apart (LBO), 8-channel chunks CS apart (SBO)
+    const uint32_t idesc = tc_idesc_n(COUT) | (1u << 15) | (1u << 16);
+    auto issue = [&](int buf, bool first) {
+        const uint32_t base = s0 + (uint32_t)buf * SS;
+        for (int kk = 0; kk < TC_ROWS / 16; ++kk) {
+            const uint64_t bd = tc_sdesc(base + (uint32_t)((3 * NCH * L + kk * 16) * 16), 128, CS);
+#pragma unroll
+            for (int j = 0; j < 9; ++j) {
+                const int dy = j / 3 - 1, dz = j % 3 - 1;
+                const uint64_t ad = tc_sdesc(base + (uint32_t)((PZ + 1 + kk * 16 + dy * PZ + dz) * 16), 128, CS);
+                const uint32_t acc = (first && kk == 0) ? 0u : 1u;
+                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                             ::"r"(tmem + (uint32_t)(j * COUT)), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+        }
+    };
+
+    bool ok = true;
+    if (n_it > 0) stage(lo, 0);
+    for (long long i = 0; i < n_it; ++i) {
+        const int b = (int)(i & 1);
+        asm volatile("cp.async.wait_group 0;");
+        asm volatile("fence.proxy.async.shared::cta;");   // the stage is read by the tensor cores
+        if (!__syncthreads_and(ok)) {
+            ok = false;
+            break;
+        }
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            issue(b, i == 0);
+            tc_commit(sa(&bar_mma[b]));
+        }
+        if (i + 1 < n_it) {
+            // the other stage was read by the previous item's MMAs
+            if (i >= 1 && !tc_wait(sa(&bar_mma[(i - 1) & 1]), (uint32_t)(((i - 1) >> 1) & 1), &never)) ok = false;
+            if (ok) stage(lo + i + 1, b ^ 1);
+        }
+    }
+    asm volatile("cp.async.wait_all;");
+    __syncthreads();
+    if (tid == 0 && n_it > 0) tc_commit(sa(&bar_done));   // every MMA issued above
+    if (n_it > 0 && !tc_wait(sa(&bar_done), 0u, &never)) ok = false;
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (__syncthreads_and(ok)) {
+        if (n_it > 0) {
+            // lane m of the accumulators: plane q-1+s, channel ci with m = s*CIN + ci
+            const int m = warp * 32 + lane;
+            const int s = m / CIN, ci = m - s * CIN;
+#pragma unroll 1
+            for (int j = 0; j < 9; ++j) {
+                const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(j * COUT);
+                uint32_t r[32];
+                if (COUT == 32)
+                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+                                   "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+                                   "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+                                   "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+                                   "=r"(r[31])
+                                 : "r"(taddr));
+                else
+                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+                                   "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                                 : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;");
+                if (s < 3 && ci < CINR) {
+                    float *d = dW + ((size_t)(s * 9 + j) * CINR + ci) * COUTR;   // tap (dx = s-1, dy, dz)
+#pragma unroll
+                    for (int co = 0; co < COUTR; ++co) atomicAdd(d + co, __uint_as_float(r[co]));
+                }
+            }
+        }
+    } else if (tid == 0) {
+        atomicExch(err, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+}
+
+// bias gradients db[co] = sum_v g[v][co] for co < CR of C-channel rows (C divides 256)
+template <typename GT>
+__global__ void k_bias_grad(long long n, int C, int CR, const GT *__restrict__ g, float *db) {
+    __shared__ float red[256];
+    float acc = 0.f;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n * C;
+         e += (long long)gridDim.x * blockDim.x) {   // a thread's channel stays threadIdx.x % C
+        if constexpr (sizeof(GT) == 2) acc += __bfloat162float(g[e]); else acc += (float)g[e];
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    if ((int)threadIdx.x < CR) {
+        float s = 0.f;
+        for (int t = threadIdx.x; t < 256; t += C) s += red[t];
+        atomicAdd(&db[threadIdx.x], s);
+    }
+}
+
 // per-sample squared norms of the targets: one block per sample of nsv values
 __global__ void k_sample_norm(long long nsv, const float *e, float *inv_e2) {
     __shared__ double red[32 * NQ];
@@ -1211,21 +1422,41 @@ static void backward_layers(bella_cnn *net, const BlockMap &m, cudaStream_t s) {
         dW[l] = net->grads + w_off(net, l);
         db[l] = dW[l] + 27LL * net->cin[l] * net->cout[l];
     }
-    // layer 5 (32 -> block^3): weight gradient from the FP32 output gradient
-    if (net->block == 2)
-        k_wgrad<32, 32, 8, 8, float><<<gw, 256, wgrad_smem<32, 8>(), s>>>(nx, ny, nz, xs, net->act[5], net->g8, dW[5], db[5]);
-    else
-        k_wgrad<32, 32, 8, 1, float><<<gw, 256, wgrad_smem<32, 1>(), s>>>(nx, ny, nz, xs, net->act[5], net->g8, dW[5], db[5]);
-    k_g8_to_bf16<<<vec_grid(n), 256, 0, s>>>(n, net->g8, net->gact[1]);
-    // input gradients (masked by ReLU' of the layer's input when the network has ReLUs):
-    // on tcgen05 -- the forward kernel with the mirrored, transposed weights -- where
-    // the staged planes fit, else on mma.sync
+    // the tcgen05 kernels (input gradients: the forward kernel with the mirrored,
+    // transposed weights and, with ReLUs, the ReLU derivative in its epilogue; weight
+    // gradients: k_wgrad_tc) where the staged planes fit, else mma.sync and FP32 loops
     const bool relu = !net->linear;
     const bool tc = net->use_tc && tc_fits(m);
+    const bool wtc = net->use_tc && wg_smem_bytes(nz + 2) <= TC_SMEM_MAX;
+    const bool bias = !(net->linear || net->bias_free);
     const long long plane = (long long)(ny + 2) * (nz + 2);
     const long long items = ((plane + TC_ROWS - 1) / TC_ROWS) * (long long)nx;
     const int gt = tc_grid(items), pz = nz + 2;
     const long long work = (items + gt - 1) / gt;
+    const size_t wsm = wg_smem_bytes(pz);
+    const int gb = vec_grid(n);
+    long long launches = 0;
+    // layer 5 (32 -> block^3)
+    if (wtc) {
+        k_g8_to_bf16<<<vec_grid(n), 256, 0, s>>>(n, net->g8, net->gact[1]);
+        if (net->block == 2)
+            k_wgrad_tc<32, 16, 32, 8><<<gt, WG_THREADS, wsm, s>>>(nx, ny, nz, xs, work, net->act[5], net->gact[1],
+                                                                 dW[5], net->tc_err);
+        else
+            k_wgrad_tc<32, 16, 32, 1><<<gt, WG_THREADS, wsm, s>>>(nx, ny, nz, xs, work, net->act[5], net->gact[1],
+                                                                 dW[5], net->tc_err);
+        if (bias) k_bias_grad<float><<<gb, 256, 0, s>>>(n, 8, net->block == 2 ? 8 : 1, net->g8, db[5]);
+        launches += 2 + (bias ? 1 : 0);
+    } else {
+        if (net->block == 2)
+            k_wgrad<32, 32, 8, 8, float><<<gw, 256, wgrad_smem<32, 8>(), s>>>(nx, ny, nz, xs, net->act[5], net->g8,
+                                                                              dW[5], db[5]);
+        else
+            k_wgrad<32, 32, 8, 1, float><<<gw, 256, wgrad_smem<32, 1>(), s>>>(nx, ny, nz, xs, net->act[5], net->g8,
+                                                                              dW[5], db[5]);
+        k_g8_to_bf16<<<vec_grid(n), 256, 0, s>>>(n, net->g8, net->gact[1]);
+        launches += 2;
+    }
     if (tc)
         k_conv3d_tc<16, 32, false, false><<<gt, TC_THREADS, tc_smem_bytes<16, 32>(pz), s>>>(
             nx, ny, nz, xs, work, net->gact[1], net->wtcT[5], nullptr, net->gact[0], 1.f, net->tc_err,
@@ -1233,10 +1464,19 @@ static void backward_layers(bella_cnn *net, const BlockMap &m, cudaStream_t s) {
     else
         k_conv3d<16, 32, false, false, true><<<g, CNN_THREADS, conv_smem<16, 32>(), s>>>(
             nx, ny, nz, xs, net->gact[1], net->wkT[5], nullptr, net->gact[0], 1.f, relu ? net->act[5] : nullptr);
+    launches += 1;
     int cur = 0;
     for (int l = 4; l >= 1; --l) {
-        k_wgrad<32, 32, 32, 32, __nv_bfloat16><<<gw, 256, wgrad_smem<32, 32>(), s>>>(
-            nx, ny, nz, xs, net->act[l], net->gact[cur], dW[l], db[l]);
+        if (wtc) {
+            k_wgrad_tc<32, 32, 32, 32><<<gt, WG_THREADS, wsm, s>>>(nx, ny, nz, xs, work, net->act[l], net->gact[cur],
+                                                                  dW[l], net->tc_err);
+            if (bias) k_bias_grad<__nv_bfloat16><<<gb, 256, 0, s>>>(n, 32, 32, net->gact[cur], db[l]);
+            launches += 1 + (bias ? 1 : 0);
+        } else {
+            k_wgrad<32, 32, 32, 32, __nv_bfloat16><<<gw, 256, wgrad_smem<32, 32>(), s>>>(
+                nx, ny, nz, xs, net->act[l], net->gact[cur], dW[l], db[l]);
+            launches += 1;
+        }
         if (tc)
             k_conv3d_tc<32, 32, false, false><<<gt, TC_THREADS, tc_smem_bytes<32, 32>(pz), s>>>(
                 nx, ny, nz, xs, work, net->gact[cur], net->wtcT[l], nullptr, net->gact[cur ^ 1], 1.f, net->tc_err,
@@ -1245,16 +1485,29 @@ static void backward_layers(bella_cnn *net, const BlockMap &m, cudaStream_t s) {
             k_conv3d<32, 32, false, false, true><<<g, CNN_THREADS, conv_smem<32, 32>(), s>>>(
                 nx, ny, nz, xs, net->gact[cur], net->wkT[l], nullptr, net->gact[cur ^ 1], 1.f,
                 relu ? net->act[l] : nullptr);
+        launches += 1;
         cur ^= 1;
     }
-    if (net->block == 2)
-        k_wgrad<16, 8, 32, 32, __nv_bfloat16><<<gw, 256, wgrad_smem<8, 32>(), s>>>(
-            nx, ny, nz, xs, net->act[0], net->gact[cur], dW[0], db[0]);
-    else
-        k_wgrad<16, 1, 32, 32, __nv_bfloat16><<<gw, 256, wgrad_smem<1, 32>(), s>>>(
-            nx, ny, nz, xs, net->act[0], net->gact[cur], dW[0], db[0]);
-    net->launches += 2 + 2 + 2 * 4 + 1;
-    if (net->linear || net->bias_free) {   // biases stay at zero: no gradient, no Adam motion
+    if (wtc) {
+        if (net->block == 2)
+            k_wgrad_tc<16, 32, 8, 32><<<gt, WG_THREADS, wsm, s>>>(nx, ny, nz, xs, work, net->act[0], net->gact[cur],
+                                                                 dW[0], net->tc_err);
+        else
+            k_wgrad_tc<16, 32, 1, 32><<<gt, WG_THREADS, wsm, s>>>(nx, ny, nz, xs, work, net->act[0], net->gact[cur],
+                                                                 dW[0], net->tc_err);
+        if (bias) k_bias_grad<__nv_bfloat16><<<gb, 256, 0, s>>>(n, 32, 32, net->gact[cur], db[0]);
+        launches += 1 + (bias ? 1 : 0);
+    } else {
+        if (net->block == 2)
+            k_wgrad<16, 8, 32, 32, __nv_bfloat16><<<gw, 256, wgrad_smem<8, 32>(), s>>>(
+                nx, ny, nz, xs, net->act[0], net->gact[cur], dW[0], db[0]);
+        else
+            k_wgrad<16, 1, 32, 32, __nv_bfloat16><<<gw, 256, wgrad_smem<1, 32>(), s>>>(
+                nx, ny, nz, xs, net->act[0], net->gact[cur], dW[0], db[0]);
+        launches += 1;
+    }
+    net->launches += launches;
+    if (!bias) {   // biases stay at zero: no gradient, no Adam motion
         for (int l = 0; l < 6; ++l) cudaMemsetAsync(db[l], 0, net->cout[l] * sizeof(float), s);
     }
 }
@@ -1350,7 +1603,10 @@ int bella_cnn_create(bella_cnn **out, int device, int block, long long capacity)
          big_smem(k_conv3d_tc<16, 32, false, false>, TC_SMEM_MAX) &&
          big_smem(k_conv3d_tc<16, 32, true, false>, TC_SMEM_MAX) &&
          big_smem(k_conv3d_tc<32, 32, false, false>, TC_SMEM_MAX) &&
-         big_smem(k_conv3d_tc<32, 32, true, false>, TC_SMEM_MAX) && big_smem(k_conv3d_tc<32, 16, false, true>, TC_SMEM_MAX);
+         big_smem(k_conv3d_tc<32, 32, true, false>, TC_SMEM_MAX) && big_smem(k_conv3d_tc<32, 16, false, true>, TC_SMEM_MAX) &&
+         big_smem(k_wgrad_tc<32, 16, 32, 8>, TC_SMEM_MAX) && big_smem(k_wgrad_tc<32, 16, 32, 1>, TC_SMEM_MAX) &&
+         big_smem(k_wgrad_tc<32, 32, 32, 32>, TC_SMEM_MAX) && big_smem(k_wgrad_tc<16, 32, 8, 32>, TC_SMEM_MAX) &&
+         big_smem(k_wgrad_tc<16, 32, 1, 32>, TC_SMEM_MAX);
     if (ok) ok = cnn_sync_weights(net, 0) == BELLA_OK && cudaDeviceSynchronize() == cudaSuccess;
     if (!ok) {
         g_cnn_err = "bella_cnn_create: allocation or attribute failed";

@@ -39,10 +39,11 @@ def test_cnn_forward_matches_oracle(block, shape):
     np.testing.assert_allclose(y2.reshape(shape), 3.0 * y, rtol=1e-5, atol=1e-6)
 
 
-@pytest.mark.parametrize("block,shape", [(1, (6, 5, 18)), (2, (11, 8, 34))])
+@pytest.mark.parametrize("block,shape", [(1, (6, 5, 18)), (2, (11, 8, 34)), (1, (7, 20, 30)), (2, (20, 38, 62))])
 def test_cnn_gradients_match_oracle(block, shape):
-    """Backward kernels (mirrored tensor-core input gradients, FP32 weight gradients)
-    against the oracle's float64 backward on the same BF16 activations."""
+    """Backward kernels (tcgen05 input gradients with the mirrored weights, tcgen05
+    weight gradients) against the oracle's float64 backward on the same BF16
+    activations; the last two shapes span three 256-row blocks of the padded plane."""
     import torch
     from pybella_gb300.learned import CNN
     rng = np.random.default_rng(11 + block)
@@ -196,3 +197,58 @@ def test_tcgen05_forward_matches_mma_sync_and_oracle(mode, block, shape):
     if shape[0] * shape[1] * shape[2] < 40000:
         ref, _ = ocnn.forward(r, params, block, linear=(mode == "linear"))
         assert _rel(y_tc.reshape(shape), ref) < 2e-2
+
+
+@pytest.mark.parametrize("mode", ["relu", "linear"])
+@pytest.mark.parametrize("block,shape", [(2, (11, 8, 34)), (2, (20, 38, 62)), (1, (7, 20, 30))])
+def test_tcgen05_gradients_match_cuda_core_gradients(mode, block, shape):
+    """Weight and bias gradients on tcgen05 (GEMM over voxels, MN-major operands from the
+    staged planes) against the FP32 CUDA-core loops and mma.sync input gradients."""
+    import torch
+    from pybella_gb300.learned import CNN
+    rng = np.random.default_rng(31 + sum(shape))
+    params = _params(block, 5)
+    if mode == "linear":
+        for l in range(6):
+            params["b%d" % l] = np.zeros_like(params["b%d" % l])
+    r = torch.tensor(rng.standard_normal(shape).astype(np.float32).ravel(), device="cuda")
+    gout = torch.tensor(rng.standard_normal(shape).astype(np.float32).ravel(), device="cuda")
+    net = CNN(shape, block=block, mode=mode)
+    net.set_params(params)
+    net.set_tensor_cores(False)
+    g_cc = ocnn.unflatten(net.gradients(r, gout, shape)[0].cpu().numpy(), block)
+    net.set_tensor_cores(True)
+    g_tc = ocnn.unflatten(net.gradients(r, gout, shape)[0].cpu().numpy(), block)
+    assert not net.tensor_core_error()
+    for k in g_cc:
+        if not np.any(g_cc[k]):
+            assert not np.any(g_tc[k]), k
+            continue
+        # the same BF16 operands up to the input gradients' own rounding (and the last
+        # layer's output gradient in BF16 instead of FP32)
+        assert _rel(g_tc[k], g_cc[k]) < 1e-2, (k, _rel(g_tc[k], g_cc[k]))
+
+
+@pytest.mark.parametrize("block", [1, 2])
+def test_tcgen05_batched_training_tracks_cuda_cores(block):
+    """Adam on a batch of samples stacked along x (one x-segment each): the tensor-core
+    backward and the CUDA-core backward give the same loss curve."""
+    import torch
+    from pybella_gb300.learned import CNN
+    torch.manual_seed(1)
+    ns, S = 4, 24
+    x = torch.randn(ns, S, S, S, device="cuda")
+    t = x.clone()
+    for ax in (1, 2, 3):
+        t = (torch.roll(t, 1, ax) + t + torch.roll(t, -1, ax)) / 3.0
+    curves = []
+    for tc in (False, True):
+        net = CNN((S, S, S), block=block, nsamples=ns)
+        net.init(0)
+        net.set_tensor_cores(tc)
+        curves.append(np.array([net.train_step(x, t, 1e-3) for _ in range(12)]))
+        assert not net.tensor_core_error()
+    cc, tcv = curves
+    assert np.all(np.isfinite(tcv))
+    assert tcv[-1] < tcv[0]
+    np.testing.assert_allclose(tcv, cc, rtol=2e-2)
