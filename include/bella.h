@@ -383,9 +383,10 @@ int       bella_cnn_set_mode(bella_cnn *net, int mode);
 /* identity path: every map (forward, gradients, training, solver) returns omega*in + CNN(in);
  * default 0 */
 int       bella_cnn_set_skip(bella_cnn *net, float omega);
-/* all six forward layers on the tcgen05 tensor-core path (1, the default) or mma.sync (0); tcgen05
- * is used when the z extent of the grid the net runs on is at most 142 (staged planes fit in
- * shared memory), mma.sync otherwise */
+/* the tensor-core path (1, the default): all six forward layers and the input-gradient passes on
+ * tcgen05 when the z extent of the grid the net runs on is at most 142 (staged planes fit in
+ * shared memory, mma.sync otherwise), the weight gradients on tcgen05 when it is at most 151
+ * (FP32 CUDA-core loops otherwise); 0: mma.sync and the CUDA-core loops throughout */
 int       bella_cnn_set_tc(bella_cnn *net, int on);
 /* 1 if a tensor-core completion wait gave up since the last call (synchronises) */
 int       bella_cnn_tc_error(bella_cnn *net);

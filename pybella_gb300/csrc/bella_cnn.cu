@@ -865,47 +865,66 @@ constexpr size_t wgrad_smem() { return sizeof(float) * ((size_t)CH_VOX * CINR + 
 
 // ---- weight gradients on tcgen05 ---------------------------------------------------
 // dW[t][ci][co] = sum_v in[v + off(t)][ci] g[v][co] as a GEMM whose K runs over voxels.
-// Items are (x-plane q of the gradient, block of TC_ROWS padded (y, z) rows); each CTA
-// (one per SM) takes a contiguous share.  Per item, a stage holds input planes q-1, q,
-// q+1 in the forward kernel's layout ([16-byte channel chunk][row][8 channels], rows
-// f0-PZ-1 .. f0+TC_ROWS+PZ of the zero-padded plane, zeros outside the plane and the
-// sample's x-segment) and, next in the same chunk sequence, the gradient rows f0 ..
-// f0+TC_ROWS-1 of plane q.  Read MN-major (a chunk's 8 channels contiguous, rows 16
-// bytes apart), the stage's 16 chunks are one A operand of 128 rows (plane q-1+s,
-// channel) -- rows past plane q+1 read the gradient or unused chunks and are
-// discarded -- and the gradient chunks are B (N = COUT).  For tap (dy, dz) A starts
-// dy*PZ + dz rows later, so the nine (dy, dz) accumulators of COUT tensor-memory
-// columns take the same B; they collect every item of the CTA and are added into dW
-// once.  Two stages: the copies of the next item overlap the MMAs of this one.
-constexpr int WG_THREADS = 128;
-constexpr int WG_CHUNKS = 16;               // 16-byte chunks per stage (A reads all 16)
+// Items are (x-plane q of the gradient, block of WG_ROWS padded (y, z) rows f0 ..);
+// each CTA (one per SM) takes a contiguous share.  With w = f + dz the in-plane sum
+// is sum_w in[w + dy*PZ][ci] g[w - dz][co], so per item a stage holds
+//   * A: input planes q-1, q, q+1 in the forward kernel's layout ([16-byte channel
+//     chunk][row][8 channels]), rows f0-8-PZ .. f0+WG_K-8+PZ-1 of the zero-padded
+//     plane, zeros outside the plane and the sample's x-segment.  Read MN-major (a
+//     chunk's 8 channels contiguous, rows 16 bytes apart), 16 consecutive chunks are
+//     one operand of 128 rows (plane q-1+s, channel); rows past plane q+1 read other
+//     data and are discarded.  For dy the operand starts dy*PZ rows later.
+//   * B: three copies of the gradient rows of plane q, copy dz shifted by dz rows
+//     (row w of copy dz is g[f0-8+w-dz], zero outside the item's rows): with the
+//     copies' chunks in sequence, one MN-major operand of N = 3*COUT covers dz = -1..1.
+// K = WG_K rows (WG_ROWS and 8 on either side), so three MMAs (dy) of N = 3*COUT per
+// 16 rows; their accumulators (tap (dy, dz) at column ((dy+1)*3 + dz+1)*COUT) collect
+// every item of the CTA and are added into dW once.  Three stages where they fit in
+// shared memory (else two): the copies of the next items overlap the MMAs of this one.
+constexpr int WG_THREADS = 256;
+constexpr int WG_ROWS = 128;                // gradient rows per item
+constexpr int WG_K = WG_ROWS + 16;          // K rows per item
+constexpr int WG_CHUNKS = 16;               // 16-byte chunks of one A operand
+constexpr int WG_MAX_STAGES = 3;
 
-__host__ __device__ constexpr size_t wg_smem_bytes(int pz) {
-    return (size_t)2 * WG_CHUNKS * (TC_ROWS + 2 * pz + 2) * 16;
+__host__ __device__ constexpr uint32_t wg_stage_bytes(int cin, int cout, int pz) {
+    return (uint32_t)(((3 * (cin / 8) * (WG_K + 2 * pz) * 16 + 3 * (cout / 8) * WG_K * 16) >
+                               WG_CHUNKS * (WG_K + 2 * pz) * 16
+                           ? 3 * (cin / 8) * (WG_K + 2 * pz) * 16 + 3 * (cout / 8) * WG_K * 16
+                           : WG_CHUNKS * (WG_K + 2 * pz) * 16) + 127) & ~127u;
+}
+// stages that fit the shared memory (at least two are needed)
+__host__ __device__ constexpr int wg_stages(int cin, int cout, int pz) {
+    return (size_t)WG_MAX_STAGES * wg_stage_bytes(cin, cout, pz) <= TC_SMEM_MAX ? WG_MAX_STAGES : 2;
+}
+__host__ __device__ constexpr size_t wg_smem_bytes(int cin, int cout, int pz) {
+    return (size_t)wg_stages(cin, cout, pz) * wg_stage_bytes(cin, cout, pz);
 }
 
 template <int CIN, int COUT, int CINR, int COUTR>
 __global__ void __launch_bounds__(WG_THREADS, 1)
-k_wgrad_tc(int nx, int ny, int nz, int xseg, long long work, const __nv_bfloat16 *__restrict__ in,
+k_wgrad_tc(int nx, int ny, int nz, int xseg, long long work, int nst, const __nv_bfloat16 *__restrict__ in,
            const __nv_bfloat16 *__restrict__ g, float *dW, int *err) {
     static_assert(CIN == 16 || CIN == 32, "input channels: 16 or 32");
     static_assert(COUT == 16 || COUT == 32, "gradient channels: 16 or 32");
     constexpr int NCH = CIN / 8, NCG = COUT / 8;
-    static_assert(3 * NCH + NCG <= WG_CHUNKS, "three input planes and the gradient fit a stage");
     constexpr int TMEM_COLS = 9 * COUT <= 256 ? 256 : 512;
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t bar_mma[2];
+    __shared__ __align__(8) uint64_t bar_mma[WG_MAX_STAGES];
     __shared__ __align__(8) uint64_t bar_done;
     __shared__ uint32_t tmem_slot;
     __shared__ int never;                                 // the waits here are not cut short by another role
     const int PZ = nz + 2, PY = ny + 2;
-    const int L = TC_ROWS + 2 * PZ + 2;                   // staged rows per chunk
-    const uint32_t CS = (uint32_t)L * 16, SS = (uint32_t)WG_CHUNKS * CS;
+    const int L = WG_K + 2 * PZ;                          // staged input rows per chunk
+    const uint32_t CS = (uint32_t)L * 16, CSB = (uint32_t)WG_K * 16;
+    const uint32_t SS = wg_stage_bytes(CIN, COUT, PZ);
+    const uint32_t BOFF = 3u * NCH * CS;                  // B after the three input planes
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     auto sa = [](const void *p) { return (uint32_t)__cvta_generic_to_shared(p); };
     const uint32_t s0 = sa(smem);
     if (tid == 0) {
-        for (int k = 0; k < 2; ++k) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sa(&bar_mma[k])));
+        for (int k = 0; k < WG_MAX_STAGES; ++k)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sa(&bar_mma[k])));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sa(&bar_done)));
         asm volatile("fence.mbarrier_init.release.cluster;");
         never = 0;
@@ -920,76 +939,95 @@ k_wgrad_tc(int nx, int ny, int nz, int xseg, long long work, const __nv_bfloat16
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_slot;
     const int plane = PY * PZ;
-    const int nblk = (plane + TC_ROWS - 1) / TC_ROWS;
+    const int nblk = (plane + WG_ROWS - 1) / WG_ROWS;
     const long long lo = (long long)blockIdx.x * work;
     const long long n_it = max(0LL, min(lo + work, (long long)nblk * nx) - lo);
 
+    // row f of the padded plane -> (y, z) of the grid, false on the padding ring or outside
+    const float inv_pz = 1.0f / (float)PZ;
+    auto interior = [&](int f, int &y, int &z) {
+        if (f < 0 || f >= plane) return false;
+        int yq = __float2int_rz((float)f * inv_pz);       // exact to within one (f < 2^24)
+        int r = f - yq * PZ;
+        if (r < 0) { --yq; r += PZ; } else if (r >= PZ) { ++yq; r -= PZ; }
+        y = yq - 1;
+        z = r - 1;
+        return y >= 0 && y < ny && z >= 0 && z < nz;
+    };
+    // rows of the B copies outside an item's gradient rows (w < 8+dz, w >= WG_ROWS+8+dz)
+    // are zero in every item: written once, in every stage
+    for (int e = tid; e < nst * 3 * 16 * NCG; e += WG_THREADS) {
+        const int ch = e % NCG, k = (e / NCG) % 16, jz = (e / (16 * NCG)) % 3, buf = e / (3 * 16 * NCG);
+        const int w = k < 7 + jz ? k : k + WG_ROWS;
+        *reinterpret_cast<uint4 *>(smem + (size_t)buf * SS + BOFF + (size_t)(jz * NCG + ch) * CSB + (size_t)w * 16) =
+            make_uint4(0u, 0u, 0u, 0u);
+    }
     auto stage = [&](long long it, int buf) {
-        const int q = (int)(it / nblk), f0 = (int)(it - (long long)q * nblk) * TC_ROWS;
-        const int seg = q / xseg;
+        const int q = (int)(it / nblk), f0 = (int)(it - (long long)q * nblk) * WG_ROWS;
+        const int slo = (q / xseg) * xseg, shi = min(slo + xseg, nx);   // this sample's x-segment
         const uint32_t base = s0 + (uint32_t)buf * SS;
-        for (int e = tid; e < 3 * L; e += WG_THREADS) {   // input planes q-1, q, q+1
-            const int s = e / L, rb = e - s * L;
-            const int p = q - 1 + s, f = f0 - PZ - 1 + rb;
-            const __nv_bfloat16 *src = in;
-            uint32_t bytes = 0;
-            if (p >= 0 && p < nx && p / xseg == seg && f >= 0 && f < plane) {
-                const int yq = f / PZ;
-                const int y = yq - 1, z = f - yq * PZ - 1;
-                if (y >= 0 && y < ny && z >= 0 && z < nz) {
-                    src = in + (((size_t)p * ny + y) * nz + z) * CIN;
-                    bytes = 16;
-                }
-            }
+        // A: input planes q-1, q, q+1 (a row's grid position found once for the three)
+        for (int rb = tid; rb < L; rb += WG_THREADS) {
+            int y = 0, z = 0;
+            const bool rv = interior(f0 - 8 - PZ + rb, y, z);
+            const size_t off = ((size_t)y * nz + z) * CIN;
 #pragma unroll
-            for (int ch = 0; ch < NCH; ++ch)
-                asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
-                             ::"r"(base + (uint32_t)(((s * NCH + ch) * L + rb) * 16)), "l"(src + (bytes ? ch * 8 : 0)),
-                               "r"(bytes));
+            for (int sp = 0; sp < 3; ++sp) {
+                const int p = q - 1 + sp;
+                const bool v = rv && p >= slo && p < shi;
+                const __nv_bfloat16 *src = v ? in + (size_t)p * ny * nz * CIN + off : in;
+                const uint32_t bytes = v ? 16u : 0u;
+#pragma unroll
+                for (int ch = 0; ch < NCH; ++ch)
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
+                                 ::"r"(base + (uint32_t)(sp * NCH + ch) * CS + (uint32_t)rb * 16),
+                                   "l"(src + (v ? ch * 8 : 0)), "r"(bytes));
+            }
         }
-        for (int rb = tid; rb < TC_ROWS; rb += WG_THREADS) {   // gradient rows of plane q
-            const int f = f0 + rb;
-            const __nv_bfloat16 *src = g;
-            uint32_t bytes = 0;
-            if (f < plane) {
-                const int yq = f / PZ;
-                const int y = yq - 1, z = f - yq * PZ - 1;
-                if (y >= 0 && y < ny && z >= 0 && z < nz) {
-                    src = g + (((size_t)q * ny + y) * nz + z) * COUT;
-                    bytes = 16;
-                }
-            }
+        // B: gradient row f0 + r of plane q into copy dz = jz-1 at row w = r + 8 + dz
+        for (int r = tid; r < WG_ROWS; r += WG_THREADS) {
+            int y = 0, z = 0;
+            const bool v = interior(f0 + r, y, z);
+            const __nv_bfloat16 *src = v ? g + (((size_t)q * ny + y) * nz + z) * COUT : g;
+            const uint32_t bytes = v ? 16u : 0u;
 #pragma unroll
-            for (int ch = 0; ch < NCG; ++ch)
-                asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
-                             ::"r"(base + (uint32_t)(((3 * NCH + ch) * L + rb) * 16)), "l"(src + (bytes ? ch * 8 : 0)),
-                               "r"(bytes));
+            for (int jz = 0; jz < 3; ++jz)
+#pragma unroll
+                for (int ch = 0; ch < NCG; ++ch)
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
+                                 ::"r"(base + BOFF + (uint32_t)(jz * NCG + ch) * CSB + (uint32_t)(r + 7 + jz) * 16),
+                                   "l"(src + (v ? ch * 8 : 0)), "r"(bytes));
         }
         asm volatile("cp.async.commit_group;");
     };
-    // MN-major, no swizzle: 8-row K groups 128 bytes apart (LBO), 8-channel chunks CS apart (SBO)
-    const uint32_t idesc = tc_idesc_n(COUT) | (1u << 15) | (1u << 16);
+    // MN-major, no swizzle: 8-row K groups 128 bytes apart (LBO), 8-channel chunks CS or CSB apart (SBO)
+    const uint32_t idesc = tc_idesc_n(3 * COUT) | (1u << 15) | (1u << 16);
     auto issue = [&](int buf, bool first) {
         const uint32_t base = s0 + (uint32_t)buf * SS;
-        for (int kk = 0; kk < TC_ROWS / 16; ++kk) {
-            const uint64_t bd = tc_sdesc(base + (uint32_t)((3 * NCH * L + kk * 16) * 16), 128, CS);
+        for (int kk = 0; kk < WG_K / 16; ++kk) {
+            const uint64_t bd = tc_sdesc(base + BOFF + (uint32_t)(kk * 16 * 16), 128, CSB);
 #pragma unroll
-            for (int j = 0; j < 9; ++j) {
-                const int dy = j / 3 - 1, dz = j % 3 - 1;
-                const uint64_t ad = tc_sdesc(base + (uint32_t)((PZ + 1 + kk * 16 + dy * PZ + dz) * 16), 128, CS);
+            for (int dyi = 0; dyi < 3; ++dyi) {
+                const uint64_t ad = tc_sdesc(base + (uint32_t)((kk * 16 + dyi * PZ) * 16), 128, CS);
                 const uint32_t acc = (first && kk == 0) ? 0u : 1u;
                 asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
                              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                             ::"r"(tmem + (uint32_t)(j * COUT)), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+                             ::"r"(tmem + (uint32_t)(dyi * 3 * COUT)), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
             }
         }
     };
 
     bool ok = true;
-    if (n_it > 0) stage(lo, 0);
+    // nst stages: the copies of items i+1 .. i+nst-1 are in flight while item i's MMAs
+    // run; one copy group per item (empty past the share) keeps the group count uniform
+    for (int k = 0; k < nst - 1; ++k) {
+        if (k < n_it) stage(lo + k, k);
+        else asm volatile("cp.async.commit_group;");
+    }
     for (long long i = 0; i < n_it; ++i) {
-        const int b = (int)(i & 1);
-        asm volatile("cp.async.wait_group 0;");
+        const int b = (int)(i % nst);
+        if (nst == 3) asm volatile("cp.async.wait_group 1;");   // item i's copies have landed
+        else          asm volatile("cp.async.wait_group 0;");
         asm volatile("fence.proxy.async.shared::cta;");   // the stage is read by the tensor cores
         if (!__syncthreads_and(ok)) {
             ok = false;
@@ -1000,11 +1038,13 @@ k_wgrad_tc(int nx, int ny, int nz, int xseg, long long work, const __nv_bfloat16
             issue(b, i == 0);
             tc_commit(sa(&bar_mma[b]));
         }
-        if (i + 1 < n_it) {
-            // the other stage was read by the previous item's MMAs
-            if (i >= 1 && !tc_wait(sa(&bar_mma[(i - 1) & 1]), (uint32_t)(((i - 1) >> 1) & 1), &never)) ok = false;
-            if (ok) stage(lo + i + 1, b ^ 1);
-        }
+        // item i+nst-1 goes to the stage the previous item's MMAs read
+        const long long nxt = i + nst - 1;
+        if (i >= 1 && nxt < n_it &&
+            !tc_wait(sa(&bar_mma[(i - 1) % nst]), (uint32_t)(((i - 1) / nst) & 1), &never))
+            ok = false;
+        if (ok && nxt < n_it) stage(lo + nxt, (int)(nxt % nst));
+        else asm volatile("cp.async.commit_group;");
     }
     asm volatile("cp.async.wait_all;");
     __syncthreads();
@@ -1013,12 +1053,13 @@ k_wgrad_tc(int nx, int ny, int nz, int xseg, long long work, const __nv_bfloat16
     asm volatile("tcgen05.fence::after_thread_sync;");
     if (__syncthreads_and(ok)) {
         if (n_it > 0) {
-            // lane m of the accumulators: plane q-1+s, channel ci with m = s*CIN + ci
-            const int m = warp * 32 + lane;
+            // lane m of the accumulators: plane q-1+s, channel ci with m = s*CIN + ci; warps
+            // w and w+4 read the same lanes and share the nine accumulators
+            const int m = (warp & 3) * 32 + lane;
             const int s = m / CIN, ci = m - s * CIN;
 #pragma unroll 1
-            for (int j = 0; j < 9; ++j) {
-                const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(j * COUT);
+            for (int j = warp >> 2; j < 9; j += WG_THREADS / 128) {
+                const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(j * COUT);
                 uint32_t r[32];
                 if (COUT == 32)
                     asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
@@ -1199,18 +1240,25 @@ __global__ void k_sub(long long n, const float *a, const float *b, float *d) {
 
 // per-sample weights 1/||core(r_s)||^2 (one block per sample; core: nodes at least
 // `margin` nodes inside the crop)
-__global__ void k_crop_rnorm(int S, int margin, const float *r, float *w) {
+__global__ void k_crop_rnorm(int S, int margin, const float *r, double *acc) {
+    // one block per (x-plane of the core, sample): partial sums of r^2 over the core
     __shared__ double red[32 * NQ];
-    const long long nsv = (long long)S * S * S;
-    const float *p = r + (long long)blockIdx.x * nsv;
-    double acc[1] = {0.0};
-    for (long long e = threadIdx.x; e < nsv; e += blockDim.x) {
-        const int k = (int)(e % S), j = (int)((e / S) % S), i = (int)(e / ((long long)S * S));
-        if (i < margin || j < margin || k < margin || i >= S - margin || j >= S - margin || k >= S - margin) continue;
-        acc[0] += (double)p[e] * p[e];
+    const int W = S - 2 * margin;
+    const float *p = r + ((long long)blockIdx.y * S + margin + blockIdx.x) * S * S;
+    double a[1] = {0.0};
+    for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
+        const int jj = e / W;
+        const float v = p[(margin + jj) * S + margin + (e - jj * W)];
+        a[0] += (double)v * v;
     }
-    block_sum<1>(acc, red);
-    if (threadIdx.x == 0) w[blockIdx.x] = acc[0] > 0.0 ? (float)(1.0 / acc[0]) : 0.f;
+    block_sum<1>(a, red);
+    if (threadIdx.x == 0) atomicAdd(&acc[blockIdx.y], a[0]);
+}
+
+// w_s = 1 / sum over the core of r^2 (0 for an all-zero core)
+__global__ void k_crop_rinv(int B, const double *acc, float *w) {
+    const int smp = blockIdx.x * blockDim.x + threadIdx.x;
+    if (smp < B) w[smp] = acc[smp] > 0.0 ? (float)(1.0 / acc[smp]) : 0.f;
 }
 
 // loss += w_s ||q||^2 / B and q *= 2 w_s / B (q becomes dL/d(Ad) before the adjoint)
@@ -1258,7 +1306,7 @@ struct bella_cnn {
     float *inv_e2;            // per-sample 1/||target||^2 [cap]
     double *loss;
     // operator-loss scratch (node grid of a batch of crops), allocated on first use
-    float *yf, *qf, *gf, *flux, *wcrop;
+    float *yf, *qf, *gf, *flux, *wcrop;   // wcrop: per-sample loss weights, then their FP64 sums
     long long fine_cap, flux_cap;
     long long launches;
 };
@@ -1427,24 +1475,26 @@ static void backward_layers(bella_cnn *net, const BlockMap &m, cudaStream_t s) {
     // gradients: k_wgrad_tc) where the staged planes fit, else mma.sync and FP32 loops
     const bool relu = !net->linear;
     const bool tc = net->use_tc && tc_fits(m);
-    const bool wtc = net->use_tc && wg_smem_bytes(nz + 2) <= TC_SMEM_MAX;
+    const bool wtc = net->use_tc && 2 * (size_t)wg_stage_bytes(32, 32, nz + 2) <= TC_SMEM_MAX;
     const bool bias = !(net->linear || net->bias_free);
     const long long plane = (long long)(ny + 2) * (nz + 2);
     const long long items = ((plane + TC_ROWS - 1) / TC_ROWS) * (long long)nx;
     const int gt = tc_grid(items), pz = nz + 2;
     const long long work = (items + gt - 1) / gt;
-    const size_t wsm = wg_smem_bytes(pz);
+    const long long witems = ((plane + WG_ROWS - 1) / WG_ROWS) * (long long)nx;
+    const int gwt = tc_grid(witems);
+    const long long wwork = (witems + gwt - 1) / gwt;
     const int gb = vec_grid(n);
     long long launches = 0;
     // layer 5 (32 -> block^3)
     if (wtc) {
         k_g8_to_bf16<<<vec_grid(n), 256, 0, s>>>(n, net->g8, net->gact[1]);
         if (net->block == 2)
-            k_wgrad_tc<32, 16, 32, 8><<<gt, WG_THREADS, wsm, s>>>(nx, ny, nz, xs, work, net->act[5], net->gact[1],
-                                                                 dW[5], net->tc_err);
+            k_wgrad_tc<32, 16, 32, 8><<<gwt, WG_THREADS, wg_smem_bytes(32, 16, pz), s>>>(
+                nx, ny, nz, xs, wwork, wg_stages(32, 16, pz), net->act[5], net->gact[1], dW[5], net->tc_err);
         else
-            k_wgrad_tc<32, 16, 32, 1><<<gt, WG_THREADS, wsm, s>>>(nx, ny, nz, xs, work, net->act[5], net->gact[1],
-                                                                 dW[5], net->tc_err);
+            k_wgrad_tc<32, 16, 32, 1><<<gwt, WG_THREADS, wg_smem_bytes(32, 16, pz), s>>>(
+                nx, ny, nz, xs, wwork, wg_stages(32, 16, pz), net->act[5], net->gact[1], dW[5], net->tc_err);
         if (bias) k_bias_grad<float><<<gb, 256, 0, s>>>(n, 8, net->block == 2 ? 8 : 1, net->g8, db[5]);
         launches += 2 + (bias ? 1 : 0);
     } else {
@@ -1468,8 +1518,8 @@ static void backward_layers(bella_cnn *net, const BlockMap &m, cudaStream_t s) {
     int cur = 0;
     for (int l = 4; l >= 1; --l) {
         if (wtc) {
-            k_wgrad_tc<32, 32, 32, 32><<<gt, WG_THREADS, wsm, s>>>(nx, ny, nz, xs, work, net->act[l], net->gact[cur],
-                                                                  dW[l], net->tc_err);
+            k_wgrad_tc<32, 32, 32, 32><<<gwt, WG_THREADS, wg_smem_bytes(32, 32, pz), s>>>(
+                nx, ny, nz, xs, wwork, wg_stages(32, 32, pz), net->act[l], net->gact[cur], dW[l], net->tc_err);
             if (bias) k_bias_grad<__nv_bfloat16><<<gb, 256, 0, s>>>(n, 32, 32, net->gact[cur], db[l]);
             launches += 1 + (bias ? 1 : 0);
         } else {
@@ -1490,11 +1540,11 @@ static void backward_layers(bella_cnn *net, const BlockMap &m, cudaStream_t s) {
     }
     if (wtc) {
         if (net->block == 2)
-            k_wgrad_tc<16, 32, 8, 32><<<gt, WG_THREADS, wsm, s>>>(nx, ny, nz, xs, work, net->act[0], net->gact[cur],
-                                                                 dW[0], net->tc_err);
+            k_wgrad_tc<16, 32, 8, 32><<<gwt, WG_THREADS, wg_smem_bytes(16, 32, pz), s>>>(
+                nx, ny, nz, xs, wwork, wg_stages(16, 32, pz), net->act[0], net->gact[cur], dW[0], net->tc_err);
         else
-            k_wgrad_tc<16, 32, 1, 32><<<gt, WG_THREADS, wsm, s>>>(nx, ny, nz, xs, work, net->act[0], net->gact[cur],
-                                                                 dW[0], net->tc_err);
+            k_wgrad_tc<16, 32, 1, 32><<<gwt, WG_THREADS, wg_smem_bytes(16, 32, pz), s>>>(
+                nx, ny, nz, xs, wwork, wg_stages(16, 32, pz), net->act[0], net->gact[cur], dW[0], net->tc_err);
         if (bias) k_bias_grad<__nv_bfloat16><<<gb, 256, 0, s>>>(n, 32, 32, net->gact[cur], db[0]);
         launches += 1 + (bias ? 1 : 0);
     } else {
@@ -1764,7 +1814,7 @@ int bella_cnn_train_step_op(bella_cnn *net, int nsamples, int S, const float *in
         net->yf = net->qf = net->gf = net->wcrop = nullptr;
         net->fine_cap = 0;
         if (cudaMalloc(&net->yf, nn * 4) != cudaSuccess || cudaMalloc(&net->qf, nn * 4) != cudaSuccess ||
-            cudaMalloc(&net->gf, nn * 4) != cudaSuccess || cudaMalloc(&net->wcrop, (nn / 64 + 1) * 4) != cudaSuccess)
+            cudaMalloc(&net->gf, nn * 4) != cudaSuccess || cudaMalloc(&net->wcrop, (nn / 64 + 1) * 16) != cudaSuccess)
             return BELLA_ECUDA;
         net->fine_cap = nn;
     }
@@ -1783,7 +1833,10 @@ int bella_cnn_train_step_op(bella_cnn *net, int nsamples, int S, const float *in
     // q = interior(A (y - e))
     k_crop_flux<<<vec_grid(nc), 256, 0, s>>>(nsamples, S, net->gf, nullptr, hcell, net->flux);
     k_crop_node<<<vec_grid(nn), 256, 0, s>>>(nsamples, S, net->flux, dinv, ox, oy, oz, margin, net->qf);
-    k_crop_rnorm<<<nsamples, 256, 0, s>>>(S, margin, in, net->wcrop);
+    double *rsum = reinterpret_cast<double *>(net->wcrop + 2 * ((nsamples + 1) / 2));   // after the nsamples weights
+    cudaMemsetAsync(rsum, 0, nsamples * sizeof(double), s);
+    k_crop_rnorm<<<dim3(S - 2 * margin, nsamples), 256, 0, s>>>(S, margin, in, rsum);
+    k_crop_rinv<<<(nsamples + 255) / 256, 256, 0, s>>>(nsamples, rsum, net->wcrop);
     cudaMemsetAsync(net->loss, 0, sizeof(double), s);
     k_crop_loss<<<vec_grid(nn), 256, 0, s>>>(nn, (long long)S * S * S, nsamples, net->qf, net->wcrop, net->loss);
     // g = A^T q = L (dinv * q)
@@ -1796,7 +1849,7 @@ int bella_cnn_train_step_op(bella_cnn *net, int nsamples, int S, const float *in
     const float bc1 = 1.f - powf(b1, (float)net->adam_t), bc2 = 1.f - powf(b2, (float)net->adam_t);
     k_adam<<<vec_grid(net->nparams), 256, 0, s>>>(net->nparams, net->params, net->grads, net->adam_m, net->adam_v, lr,
                                                   b1, b2, 1e-8f, bc1, bc2);
-    net->launches += 13;
+    net->launches += 14;
     const int rc = cnn_sync_weights(net, s);
     if (rc != BELLA_OK) return rc;
     if (loss) {
@@ -1818,7 +1871,8 @@ int bella_cnn_set_skip(bella_cnn *net, float omega) {
     return BELLA_OK;
 }
 
-// the forward layers on the tcgen05 tensor-core path (1) or on mma.sync (0)
+// the forward, input-gradient and weight-gradient passes on tcgen05 where the staged planes
+// fit (1) or on mma.sync and the FP32 CUDA-core loops (0)
 int bella_cnn_set_tc(bella_cnn *net, int on) {
     if (!net) return BELLA_EINVAL;
     net->use_tc = on ? 1 : 0;

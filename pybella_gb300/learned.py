@@ -114,7 +114,8 @@ class CNN:
         return loss.value
 
     def set_tensor_cores(self, on):
-        """Forward layers on tcgen05 (True) or mma.sync (False)."""
+        """Forward, input-gradient and weight-gradient passes on tcgen05 (True) or on
+        mma.sync and FP32 CUDA-core loops (False)."""
         _lib.check(self._lib.bella_cnn_set_tc(self.handle, int(bool(on))), "bella_cnn_set_tc")
 
     def tensor_core_error(self):
