@@ -225,8 +225,8 @@ constexpr int TC_DRING = 32;                // completion barriers of input plan
 constexpr long long TC_SPIN_LIMIT = 1LL << 24;
 constexpr size_t TC_SMEM_MAX = 225 * 1024;   // dynamic part; the kernel's static shared variables come on top
 constexpr int TC_EPI_WARPS = 4 * TC_MB;      // warps 0 .. 7: epilogue, row block w / 4, lanes 32 * (w % 4)
-constexpr int TC_PROD_WARPS = 2;             // warps 8, 9: producers
-constexpr int TC_MMA_WARP = TC_EPI_WARPS + TC_PROD_WARPS;   // warp 10: tensor memory and the MMAs
+constexpr int TC_PROD_WARPS = 3;             // warps 8 .. 10: producers
+constexpr int TC_MMA_WARP = TC_EPI_WARPS + TC_PROD_WARPS;   // warp 11: tensor memory and the MMAs
 constexpr int TC_THREADS = 32 * (TC_MMA_WARP + 1);
 
 __device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
@@ -391,6 +391,7 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, long long work, const __nv_bfloat1
     if (warp >= TC_EPI_WARPS && warp < TC_MMA_WARP) {
         // ---------------- producers: input planes into the slot ring ----------------
         const int ptid = tid - 32 * TC_EPI_WARPS;
+        const float inv_pz = 1.0f / (float)PZ;
         long long i = 0;                                  // input planes staged so far (this CTA)
         bool ok = true;
         long long idx = share_lo;
@@ -412,8 +413,10 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, long long work, const __nv_bfloat1
                         const __nv_bfloat16 *src = in;
                         uint32_t bytes = 0;
                         if (f >= 0 && f < plane) {
-                            const int yq = f / PZ;
-                            const int y = yq - 1, z = f - yq * PZ - 1;
+                            int yq = __float2int_rz((float)f * inv_pz);   // f / PZ to within one (f < 2^24)
+                            int zr = f - yq * PZ;
+                            if (zr < 0) { --yq; zr += PZ; } else if (zr >= PZ) { ++yq; zr -= PZ; }
+                            const int y = yq - 1, z = zr - 1;
                             if (y >= 0 && y < ny && z >= 0 && z < nz) {
                                 src = in + (((size_t)p * ny + y) * nz + z) * CIN;
                                 bytes = 16;

@@ -36,7 +36,7 @@ def _const(name):
 
 
 S, D, R = _const("TC_SLOTS"), _const("TC_DRING"), _const("TC_RING")
-NPROD, NEPI = 2, 8
+NPROD, NEPI = _const("TC_PROD_WARPS"), 8
 
 
 class Bar:
