@@ -27,6 +27,7 @@ ranks.  ``--impl reference`` times the reference algorithm on the host cores
 BiCGStab) on the same configuration.
 """
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -86,18 +87,63 @@ def _dist():
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed region."""
+    """SM clock and clock-event (throttle) reasons sampled during the timed region:
+    NVML through ctypes every 5 ms (the device matched by the CUDA device's UUID),
+    else nvidia-smi every 200 ms.  Only samples taken between start() and stop() count;
+    reading these values changes no setting of the GPU."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # NVML clock-event reason bits (nvml.h): SW power cap, HW slowdown, SW thermal, HW thermal, HW power brake
+    BITS = ((0x4, "sw_power_cap"), (0x8, "hw_slowdown"), (0x20, "sw_thermal_slowdown"),
+            (0x40, "hw_thermal_slowdown"), (0x80, "hw_power_brake_slowdown"))
+    PERIOD_S = 0.005
 
     def __init__(self, index):
         self.index = index
         self.rows = []
         self.proc = None
+        self.nvml = None
+        self.stop_evt = threading.Event()
+
+    def _nvml_handle(self):
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            return None
+        h = ctypes.c_void_p()
+        try:
+            import torch
+            u = str(torch.cuda.get_device_properties(self.index).uuid)
+            u = u if u.startswith("GPU-") else "GPU-" + u
+            if lib.nvmlDeviceGetHandleByUUID(u.encode(), ctypes.byref(h)) == 0:
+                return lib, h
+        except Exception:
+            pass
+        if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.index), ctypes.byref(h)) == 0:
+            return lib, h
+        return None
+
+    def _nvml_loop(self):
+        lib, h = self.nvml
+        sm, mx, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        get_r = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        while not self.stop_evt.is_set():
+            if lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(sm)) == 0 and \
+                    lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0 and get_r(h, ctypes.byref(rs)) == 0:
+                self.rows.append((float(sm.value), float(mx.value), int(rs.value)))
+            self.stop_evt.wait(self.PERIOD_S)
 
     def start(self):
+        try:
+            self.nvml = self._nvml_handle()
+        except OSError:
+            self.nvml = None
+        if self.nvml is not None:
+            self.thread = threading.Thread(target=self._nvml_loop, daemon=True)
+            self.thread.start()
+            return
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -112,6 +158,14 @@ class ClockSampler:
             self.rows.append([c.strip() for c in line.split(",")])
 
     def stop(self):
+        if self.nvml is not None:
+            self.stop_evt.set()
+            self.thread.join(timeout=5)
+            sm = [r[0] for r in self.rows]
+            reasons = {name for r in self.rows for bit, name in self.BITS if r[2] & bit}
+            return {"sm_mhz": statistics.median(sm) if sm else None,
+                    "sm_max_mhz": max(r[1] for r in self.rows) if self.rows else None,
+                    "reasons": sorted(reasons), "samples": len(sm), "source": "nvml, 5 ms"}
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -132,7 +186,7 @@ class ClockSampler:
                     reasons.add(name)
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi, 200 ms"}
 
 
 def _peaks():
