@@ -220,8 +220,8 @@ constexpr int TC_MB = 2;                    // 128-row accumulators per output p
 constexpr int TC_ROWS = 128 * TC_MB;
 constexpr int TC_SLOTS = 5;                 // ring of staged input planes
 constexpr int TC_DRING = 32;                // completion barriers of input planes: longer than any
-                                            // waiter lags (input slots 5, accumulator ring 8 outputs
-                                            // of up to 3 inputs each), so no phase parity aliases
+                                            // waiter lags (input slots 5, 6 outputs in flight of up
+                                            // to 3 inputs each), so no phase parity aliases
 constexpr long long TC_SPIN_LIMIT = 1LL << 24;
 constexpr size_t TC_SMEM_MAX = 225 * 1024;   // dynamic part; the kernel's static shared variables come on top
 constexpr int TC_EPI_WARPS = 4 * TC_MB;      // warps 0 .. 7: epilogue, row block w / 4, lanes 32 * (w % 4)
@@ -298,13 +298,30 @@ __device__ __forceinline__ bool tc_next(long long &idx, long long hi, int nx, Tc
 // Input plane p feeds output planes p+1, p, p-1 through the weights of taps dx = 0, 1, 2:
 // with the three taps side by side in B (N = 96) one MMA per (dy, dz, K-step) serves
 // all three output planes.  Output planes are numbered o = 0, 1, ... in the order the
-// CTA produces them; their accumulators live in a ring of TC_RING planes of COUT
-// tensor-memory columns per row block, in descending order (o at column
-// COUT * (TC_RING - 1 - o % TC_RING)), so the three are adjacent unless the ring wraps
-// between them (then two MMAs).  Every slot is zeroed by its epilogue and every MMA
+// CTA produces them; a row block's accumulators are TC_RING blocks of COUT
+// tensor-memory columns, and at most TC_LIVE output planes hold accumulators at a
+// time.  The MMAs of the input plane whose output window is w, w-1, w-2 (w the index
+// of plane p+1) write blocks b, b+1, b+2 with b = tc_win(w) = (1 - w) mod TC_LIVE, so a
+// window never wraps (b + 2 <= 7) and every input plane is one MMA per (tap, K-step).
+// Output o, a = -o mod TC_LIVE, then collects its contributions in block a+1, except
+// for a = 0 (block 1 from planes o-1 and o, block 7 from o+1) and a = TC_LIVE-1 (block 0
+// from o-1, block 6 from o and o+1): the epilogue adds the two blocks (tc_blocks).
+// Only outputs o +- k*TC_LIVE share blocks, so output o may start once the epilogue has
+// released output o - TC_LIVE.  Every block is zeroed by its epilogue and every MMA
 // accumulates.  Output planes outside the run or in another sample's x-segment are
-// left out of an MMA's column range.
-constexpr int TC_RING = 8;                   // accumulator planes per row block
+// left out of an MMA's column range (a sub-range of the window).
+constexpr int TC_RING = 8;                   // accumulator blocks per row block
+constexpr int TC_LIVE = 6;                   // output planes holding accumulators at a time
+
+__host__ __device__ __forceinline__ int tc_win(long long w) {
+    return (int)(((1 - w) % TC_LIVE + TC_LIVE) % TC_LIVE);
+}
+// the accumulator blocks of output o: primary, and the second one or -1
+__host__ __device__ __forceinline__ void tc_blocks(long long o, int &pb, int &sb) {
+    const int a = (int)(((-o) % TC_LIVE + TC_LIVE) % TC_LIVE);
+    pb = a == TC_LIVE - 1 ? TC_LIVE : a + 1;
+    sb = a == 0 ? TC_LIVE + 1 : (a == TC_LIVE - 1 ? 0 : -1);
+}
 
 // COUT = 32: hidden layers, BF16 output with bias and optional ReLU.  COUT = 16 with
 // OUTF32: the output layer (8 channels padded to 16), FP32 output (acc + bias) *
@@ -322,7 +339,7 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, long long work, const __nv_bfloat1
     constexpr int NCH = CIN / 8;
     constexpr int NB = 3 * COUT;                          // B rows: the three dx taps
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t bar_full[TC_SLOTS], bar_mma[TC_DRING], bar_free[TC_RING];
+    __shared__ __align__(8) uint64_t bar_full[TC_SLOTS], bar_mma[TC_DRING], bar_free[TC_LIVE];
     __shared__ __align__(8) uint64_t bar_done;
     __shared__ uint32_t tmem_slot;
     __shared__ int abort_flag;
@@ -343,7 +360,7 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, long long work, const __nv_bfloat1
         for (int k = 0; k < TC_SLOTS; ++k)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sa(&bar_full[k])), "r"(32 * TC_PROD_WARPS));
         for (int k = 0; k < TC_DRING; ++k) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sa(&bar_mma[k])));
-        for (int k = 0; k < TC_RING; ++k)
+        for (int k = 0; k < TC_LIVE; ++k)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sa(&bar_free[k])), "r"(TC_EPI_WARPS));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sa(&bar_done)));
         asm volatile("fence.mbarrier_init.release.cluster;");
@@ -444,11 +461,10 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, long long work, const __nv_bfloat1
             const uint64_t a0 = tc_sdesc(sA_a, (uint32_t)L * 16, 128), b0 = tc_sdesc(sW_a, NB * 16, 128);
             long long i = 0, obase = 0, acq = 0;
             bool ok = true;
-            // the MMAs of input plane p (ring slot `slot`) into output planes ohi .. olo,
-            // descending columns from ohi; plane ohi uses the dx tap d0
-            auto mma_range = [&](int slot, long long ohi, long long olo, int d0) {
-                const int n = (int)(ohi - olo + 1);       // 1..3 output planes
-                const uint32_t col = (uint32_t)(COUT * (TC_RING - 1 - (int)(ohi % TC_RING)));
+            // the MMAs of input plane p (ring slot `slot`) into n output planes from ohi
+            // down, at accumulator blocks blk, blk+1, ...; plane ohi uses the dx tap d0
+            auto mma_range = [&](int slot, int blk, int n, int d0) {
+                const uint32_t col = (uint32_t)(COUT * blk);
                 const uint32_t idesc = tc_idesc_n(n * COUT);
                 const uint64_t abase = a0 + (uint64_t)(slot * NCH * L + PZ + 1);
 #pragma unroll
@@ -487,20 +503,15 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, long long work, const __nv_bfloat1
                         const int qlo = max(max(p - 1, R.ia), s0), qhi = min(min(p + 1, R.ib - 1), s0 + xseg - 1);
                         if (qlo <= qhi) {
                             const long long olo = obase + (qlo - R.ia), ohi = obase + (qhi - R.ia);
-                            for (; acq <= ohi && ok; ++acq)   // accumulators of ohi free again?
-                                if (acq >= TC_RING &&
-                                    !tc_wait(sa(&bar_free[acq % TC_RING]), (uint32_t)((acq / TC_RING - 1) & 1), abort))
+                            for (; acq <= ohi && ok; ++acq)   // output acq - TC_LIVE released its blocks?
+                                if (acq >= TC_LIVE &&
+                                    !tc_wait(sa(&bar_free[acq % TC_LIVE]), (uint32_t)((acq / TC_LIVE - 1) & 1), abort))
                                     ok = false;
                             if (!ok) break;
                             asm volatile("tcgen05.fence::after_thread_sync;");
                             const int d0 = p + 1 - qhi;           // dx tap of plane qhi
-                            const long long cut = (ohi / TC_RING) * TC_RING;   // ring boundary below ohi
-                            if (olo >= cut) {
-                                mma_range(slot, ohi, olo, d0);
-                            } else {
-                                mma_range(slot, ohi, cut, d0);
-                                mma_range(slot, cut - 1, olo, d0 + (int)(ohi - cut) + 1);
-                            }
+                            const long long w = obase + (p + 1 - R.ia);   // the window's first output
+                            mma_range(slot, tc_win(w) + (int)(w - ohi), (int)(ohi - olo + 1), d0);
                         }
                     }
                     // one commit: the slot is free and output plane p-1 complete once these MMAs are done
@@ -532,7 +543,9 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, long long work, const __nv_bfloat1
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;");
-                const uint32_t taddr = tlane + (uint32_t)(COUT * (TC_RING - 1 - (int)(o % TC_RING)));
+                int pb, sb;
+                tc_blocks(o, pb, sb);
+                const uint32_t taddr = tlane + (uint32_t)(COUT * pb);
                 uint32_t r[32];
                 if (COUT == 32)
                     asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
@@ -553,7 +566,25 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, long long work, const __nv_bfloat1
                                    "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
                                  : "r"(taddr));
                 asm volatile("tcgen05.wait::ld.sync.aligned;");
-                zero_cols(taddr);                           // the slot's next plane accumulates from zero
+                zero_cols(taddr);                           // the block's next plane accumulates from zero
+                if (sb >= 0) {                              // the contributions in the second block
+                    const uint32_t saddr = tlane + (uint32_t)(COUT * sb);
+#pragma unroll
+                    for (int h = 0; h < COUT; h += 16) {
+                        uint32_t t[16];
+                        asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                                     "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                                     : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]), "=r"(t[5]),
+                                       "=r"(t[6]), "=r"(t[7]), "=r"(t[8]), "=r"(t[9]), "=r"(t[10]), "=r"(t[11]),
+                                       "=r"(t[12]), "=r"(t[13]), "=r"(t[14]), "=r"(t[15])
+                                     : "r"(saddr + (uint32_t)h));
+                        asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+                        for (int c = 0; c < 16; ++c)
+                            r[h + c] = __float_as_uint(__uint_as_float(r[h + c]) + __uint_as_float(t[c]));
+                    }
+                    zero_cols(saddr);
+                }
                 const int f = R.fb * TC_ROWS + mb * 128 + (warp & 3) * 32 + lane;
                 if (f < plane) {
                     const int yq = f / PZ;
@@ -602,7 +633,7 @@ k_conv3d_tc(int nx, int ny, int nz, int xseg, long long work, const __nv_bfloat1
                 asm volatile("tcgen05.wait::st.sync.aligned;");
                 asm volatile("tcgen05.fence::before_thread_sync;");
                 __syncwarp();
-                if (lane == 0) tc_arrive(sa(&bar_free[o % TC_RING]));
+                if (lane == 0) tc_arrive(sa(&bar_free[o % TC_LIVE]));
             }
             ibase += R.ib - R.ia + 2;                     // the run read input planes ia-1 .. ib
         }

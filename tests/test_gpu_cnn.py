@@ -203,30 +203,40 @@ def test_tcgen05_forward_matches_mma_sync_and_oracle(mode, block, shape):
 @pytest.mark.parametrize("block,shape", [(2, (11, 8, 34)), (2, (20, 38, 62)), (1, (7, 20, 30))])
 def test_tcgen05_gradients_match_cuda_core_gradients(mode, block, shape):
     """Weight and bias gradients on tcgen05 (GEMM over voxels, MN-major operands from the
-    staged planes) against the FP32 CUDA-core loops and mma.sync input gradients."""
+    staged planes) against the FP32 CUDA-core loops with mma.sync input gradients: both
+    against the oracle's float64 backward, the tensor-core path at least as accurate.
+    The two paths sum the same BF16 products in different orders, so BF16 activations
+    and, with ReLUs, their masks differ in a few places; without ReLUs the gradients
+    agree directly."""
     import torch
     from pybella_gb300.learned import CNN
     rng = np.random.default_rng(31 + sum(shape))
     params = _params(block, 5)
-    if mode == "linear":
+    linear = mode == "linear"
+    if linear:
         for l in range(6):
             params["b%d" % l] = np.zeros_like(params["b%d" % l])
-    r = torch.tensor(rng.standard_normal(shape).astype(np.float32).ravel(), device="cuda")
-    gout = torch.tensor(rng.standard_normal(shape).astype(np.float32).ravel(), device="cuda")
+    r = rng.standard_normal(shape).astype(np.float32)
+    gout = rng.standard_normal(shape).astype(np.float32)
+    _, acts = ocnn.forward(r, params, block, linear=linear)
+    ref = ocnn.backward(acts, params, gout, block, linear=linear)
     net = CNN(shape, block=block, mode=mode)
     net.set_params(params)
-    net.set_tensor_cores(False)
-    g_cc = ocnn.unflatten(net.gradients(r, gout, shape)[0].cpu().numpy(), block)
-    net.set_tensor_cores(True)
-    g_tc = ocnn.unflatten(net.gradients(r, gout, shape)[0].cpu().numpy(), block)
+    got = {}
+    for tc in (False, True):
+        net.set_tensor_cores(tc)
+        g = net.gradients(torch.tensor(r.ravel(), device="cuda"), torch.tensor(gout.ravel(), device="cuda"), shape)[0]
+        got[tc] = ocnn.unflatten(g.cpu().numpy(), block)
     assert not net.tensor_core_error()
-    for k in g_cc:
-        if not np.any(g_cc[k]):
-            assert not np.any(g_tc[k]), k
+    for k in ref:
+        if linear and k.startswith("b"):           # biases are held at zero in linear mode
+            assert not np.any(got[True][k]) and not np.any(got[False][k]), k
             continue
-        # the same BF16 operands up to the input gradients' own rounding (and the last
-        # layer's output gradient in BF16 instead of FP32)
-        assert _rel(g_tc[k], g_cc[k]) < 1e-2, (k, _rel(g_tc[k], g_cc[k]))
+        e_tc, e_cc = _rel(got[True][k], ref[k]), _rel(got[False][k], ref[k])
+        # the output layer's gradient enters the tensor-core weight gradient in BF16
+        assert e_tc <= max(1.5 * e_cc, 1e-2), (k, e_tc, e_cc)
+        if linear:
+            assert _rel(got[True][k], got[False][k]) < 1e-2, (k, _rel(got[True][k], got[False][k]))
 
 
 @pytest.mark.parametrize("block", [1, 2])

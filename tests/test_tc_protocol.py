@@ -11,15 +11,19 @@ its hand-offs:
 * producers stage input plane i into slot i % TC_SLOTS once the MMAs of plane
   i - TC_SLOTS are complete (completion ring entry (i - TC_SLOTS) % TC_DRING);
   the copies' completion arrives on the slot's ``full`` barrier later, in order;
-* the MMA thread waits for ``full``, acquires the accumulator planes it starts
-  (waiting for the epilogue to release plane o - TC_RING), issues, commits to
-  completion entry i % TC_DRING (completions happen later, in issue order);
+* the MMA thread waits for ``full``, acquires the accumulators of the output
+  planes it starts (waiting for the epilogue to release plane o - TC_LIVE), issues
+  one MMA window per input plane -- TC_RING accumulator blocks, the window of
+  outputs w, w-1, w-2 at blocks tc_win(w) + 0, 1, 2 -- and commits to completion
+  entry i % TC_DRING (completions happen later, in issue order);
 * epilogue warps wait for the completion of input plane q+1 of the run, read
-  output plane q, release its accumulators.
+  output plane q from its blocks (``tc_blocks``: one, or two at the wrap),
+  release them.
 
-Checked: no deadlock, no parity alias, an output plane is read only after all
-its contributions are complete, a slot or accumulator is reused only after its
-last reader is done.
+Checked: no deadlock, no parity alias, a window never wraps, every contribution
+lands in one of its output's blocks, an output plane is read only after all
+its contributions are complete, a slot or accumulator block is reused only
+after its last reader is done.
 """
 import os
 import random
@@ -35,7 +39,18 @@ def _const(name):
     return int(re.search(r"constexpr int %s = (\d+);" % name, src).group(1))
 
 
-S, D, R = _const("TC_SLOTS"), _const("TC_DRING"), _const("TC_RING")
+S, D, R, LIVE = _const("TC_SLOTS"), _const("TC_DRING"), _const("TC_RING"), _const("TC_LIVE")
+
+
+def tc_win(w):
+    """First accumulator block of the window whose first output is w (the kernel's tc_win)."""
+    return (1 - w) % LIVE
+
+
+def tc_blocks(o):
+    """The accumulator blocks of output o (the kernel's tc_blocks)."""
+    a = (-o) % LIVE
+    return [LIVE if a == LIVE - 1 else a + 1] + ([LIVE + 1] if a == 0 else [0] if a == LIVE - 1 else [])
 NPROD, NEPI = _const("TC_PROD_WARPS"), 8
 
 
@@ -71,7 +86,7 @@ def _simulate(nx, xseg, work, nblk, cta, seed):
     runs = _runs(cta, work, nx, nblk)
     full = [Bar(NPROD, "full%d" % k) for k in range(S)]
     done = [Bar(1, "done%d" % k) for k in range(D)]
-    free = [Bar(NEPI, "free%d" % k) for k in range(R)]
+    free = [Bar(NEPI, "free%d" % k) for k in range(LIVE)]
     inputs = [p for (_, ia, ib) in runs for p in range(ia - 1, ib + 1)]
     owner, contrib, slot_data = {}, {}, {}
     commits, landings = [], [[] for _ in range(NPROD)]
@@ -100,14 +115,20 @@ def _simulate(nx, xseg, work, nblk, cta, seed):
                     if qlo <= qhi:
                         olo, ohi = obase + qlo - ia, obase + qhi - ia
                         while acq <= ohi:
-                            if acq >= R:
-                                while not free[acq % R].ready(acq // R - 1):
+                            if acq >= LIVE:
+                                while not free[acq % LIVE].ready(acq // LIVE - 1):
                                     yield
                             acq += 1
+                        w = obase + p + 1 - ia                  # the window's first output
+                        assert tc_win(w) + (w - olo) <= R - 1, "window wraps"
                         for o in range(olo, ohi + 1):
-                            if owner.get(o % R) != o:
-                                assert o % R not in owner or contrib[owner[o % R]] == "done", "reused too early"
-                                owner[o % R], contrib[o] = o, 0
+                            if o not in contrib:                # first contribution: claim the blocks
+                                for b in tc_blocks(o):
+                                    assert b not in owner or contrib[owner[b]] == "done", "reused too early"
+                                    owner[b] = o
+                                contrib[o] = 0
+                            blk = tc_win(w) + (w - o)
+                            assert blk in tc_blocks(o) and owner[blk] == o, ("contribution in a foreign block", o, blk)
                             contrib[o] += 1
                 commits.append(i % D)
                 i += 1
@@ -121,12 +142,12 @@ def _simulate(nx, xseg, work, nblk, cta, seed):
                 j = ibase + (q - ia + 2)
                 while not done[j % D].ready(j // D):
                     yield
-                assert owner[o % R] == o
+                assert all(owner[b] == o for b in tc_blocks(o))
                 want = sum(1 for pp in (q - 1, q, q + 1) if 0 <= pp < nx and pp // xseg == q // xseg)
                 assert contrib[o] == want, ("incomplete plane", q, contrib[o], want)
                 yield
-                free[o % R].arrive()
-                if free[o % R].pending == free[o % R].count:
+                free[o % LIVE].arrive()
+                if free[o % LIVE].pending == free[o % LIVE].count:
                     contrib[o] = "done"
                 o += 1
             ibase += ib - ia + 2
