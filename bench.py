@@ -49,7 +49,7 @@ METRIC = "solves/s to 1e-8 residual: learned-precond vs plain BiCGStab, 1 GB300"
 # each (the summaries in profiles/ give the commands); per launch, like `achieved`
 STENCIL3D_TRAFFIC = 211.3e6     # k_stencil3d<float, APPLY>, 257x129x257 nodes
 STENCIL2D_TRAFFIC = 134.4e6     # k_stencil2d<dfloat, PDIR>, 2049x1025 nodes
-CONV_TRAFFIC = 108.9e6          # k_conv3d_tc<32, 32>, one hidden layer at 257x129x257 nodes (2x2x2 blocked)
+CONV_TRAFFIC = 107.1e6          # k_conv3d_tc<32, 32>, one hidden layer at 257x129x257 nodes (2x2x2 blocked)
 # k_batch_bicgstab<dfloat, 64, 8>: 16.95 GB read + written by a 20-iteration launch of the
 # 48-member ensemble, whose algorithmic bytes are 20 x 4,327,728 nodes x 200 B = 17.31 GB
 ENSEMBLE_TRAFFIC_RATIO = 16.951e9 / 17.311e9
