@@ -5,7 +5,7 @@
 
 namespace bella {
 
-enum { M_APPLY = 0, M_RESID = 1, M_PDIR = 2, M_SDIR = 3 };
+enum { M_APPLY = 0, M_RESID = 1, M_PDIR = 2, M_SDIR = 3, M_RESX = 4 };   // M_RESX: FP64 vectors, double-float arithmetic
 
 // ---- last-block finalisers of one BiCGStab iteration -----------------------
 // The control flow follows scipy's bicgstab, which the reference calls
@@ -119,6 +119,8 @@ int  stencil3d_grid(int nx, int ny, int nz);
 int  op3d_pack(bella_ws *ws, const bella_op3d *op, cudaStream_t s);
 void op3d_apply(bella_ws *ws, int prec, const void *x, void *y, cudaStream_t s);
 void op3d_resid(bella_ws *ws, int prec, const void *x, const void *b, void *r, cudaStream_t s);
+// r = b - A x and ||r||^2 of FP64 vectors, formed in double-float arithmetic (~1e-14 of |A||x|)
+void op3d_resid_df(bella_ws *ws, const double *x, const double *b, double *r, cudaStream_t s);
 void op3d_iteration(bella_ws *ws, int prec, cudaStream_t s);
 
 // dimension dispatch of the prepared operator

@@ -63,6 +63,17 @@ struct StArgs3 {
 template <typename T>
 size_t smem3d_bytes() { return sizeof(T) * (SU_BUF * SUN + SF_BUF * 3 * SCN); }
 
+// vector loads and stores; M_RESX reads and writes FP64 values (8 bytes, the size of a
+// double-float) and computes in double-float
+template <typename T, int MODE> __device__ __forceinline__ T ld3(const T *p) {
+    if constexpr (MODE == M_RESX) return T(*reinterpret_cast<const double *>(p));
+    else return *p;
+}
+template <typename T, int MODE> __device__ __forceinline__ void st3(T *p, T v) {
+    if constexpr (MODE == M_RESX) *reinterpret_cast<double *>(p) = v.to_double();
+    else *p = v;
+}
+
 template <bool B> struct Chk { static constexpr bool value = B; };
 
 // number of input vectors u is formed from: x (APPLY, RESID), r p v (PDIR), r v (SDIR)
@@ -234,7 +245,7 @@ k_stencil3d(Op3D<T> op, StArgs3<T> a, KState *ks, double *partials, unsigned *co
 #pragma unroll
             for (int w = 0; w < 2; ++w) {
                 if (uoff[w] < 0) continue;
-                S.ui[0][w] = src[0][base + uoff[w]];
+                S.ui[0][w] = ld3<T, MODE>(src[0] + base + uoff[w]);
                 if (NI > 1 && !(MODE == M_PDIR && first)) {
 #pragma unroll
                     for (int q = 1; q < NI; ++q) S.ui[q][w] = src[q][base + uoff[w]];
@@ -256,7 +267,7 @@ k_stencil3d(Op3D<T> op, StArgs3<T> a, KState *ks, double *partials, unsigned *co
             const int g = n * nyz + noff;
             S.dinv = op.dinv[g];
             if (HC) S.hc = op.hc[g];
-            if (MODE == M_RESID) S.aux = a.b[g];
+            if (MODE == M_RESID || MODE == M_RESX) S.aux = ld3<T, MODE>(a.b + g);
             if (MODE == M_PDIR) S.aux = a.rh[g];
         };
         // step i: u plane i+2 -> shared memory; face sums of u plane i+1 and the
@@ -271,7 +282,7 @@ k_stencil3d(Op3D<T> op, StArgs3<T> a, KState *ks, double *partials, unsigned *co
                     if (uslot[w] < 0) continue;
                     T u = 0;
                     if (uoff[w] >= 0) {
-                        if (MODE == M_APPLY || MODE == M_RESID) u = S.ui[0][w];
+                        if (MODE == M_APPLY || MODE == M_RESID || MODE == M_RESX) u = S.ui[0][w];
                         else if (MODE == M_PDIR) u = first ? S.ui[0][w] : S.ui[0][w] + beta * (S.ui[1][w] - omega * S.ui[2][w]);
                         else u = S.ui[0][w] - alpha * S.ui[NI - 1][w];
                     }
@@ -325,7 +336,7 @@ k_stencil3d(Op3D<T> op, StArgs3<T> a, KState *ks, double *partials, unsigned *co
                     T s = ((X - nX) + (nY + Y)) + (nZ + Z);
                     if (HC) s += S.hc * u;
                     T yv = s * S.dinv;
-                    if (MODE == M_RESID) {
+                    if (MODE == M_RESID || MODE == M_RESX) {
                         yv = S.aux - yv;
                         acc0.add_prod(yv, yv);
                     } else if (MODE == M_PDIR) {
@@ -335,7 +346,7 @@ k_stencil3d(Op3D<T> op, StArgs3<T> a, KState *ks, double *partials, unsigned *co
                         acc1.add_prod(yv, yv);
                         acc2.add_prod(u, u);
                     }
-                    yout[n * nyz + noff] = yv;
+                    st3<T, MODE>(yout + n * nyz + noff, yv);
                 }
                 nX = X; nY = Y; nZ = Z;
             }
@@ -366,7 +377,7 @@ k_stencil3d(Op3D<T> op, StArgs3<T> a, KState *ks, double *partials, unsigned *co
     double tot[3];
     if (!grid_sum<3>(v, partials, counter, tot)) return;
     if (tid != 0) return;
-    if (MODE == M_RESID) ks->dot_aux2 = tot[0];
+    if (MODE == M_RESID || MODE == M_RESX) ks->dot_aux2 = tot[0];
     else if (MODE == M_PDIR) finalize_pdir(ks, tot[0]);
     else finalize_sdir(ks, tot[0], tot[1], tot[2]);
 }
@@ -417,7 +428,7 @@ static void launch3_one(bella_ws *ws, const StArgs3<T> &a, cudaStream_t s) {
 
 template <typename T, int MODE>
 static void launch3(bella_ws *ws, const StArgs3<T> &a, cudaStream_t s) {
-    const int pk = MODE == M_PDIR ? PK_PDIR : MODE == M_SDIR ? PK_SDIR : MODE == M_RESID ? PK_RESID : -1;
+    const int pk = MODE == M_PDIR ? PK_PDIR : MODE == M_SDIR ? PK_SDIR : MODE == M_RESID || MODE == M_RESX ? PK_RESID : -1;
     if (pk >= 0) prof_begin(ws, pk, s);
     if (ws->cross) {
         if (ws->has_hc) launch3_one<T, MODE, true, true>(ws, a, s);
@@ -463,6 +474,14 @@ void op3d_resid(bella_ws *ws, int prec, const void *x, const void *b, void *r, c
         a.x = (const float *)x; a.b = (const float *)b; a.y = (float *)r;
         launch3<float, M_RESID>(ws, a, s);
     }
+}
+
+void op3d_resid_df(bella_ws *ws, const double *x, const double *b, double *r, cudaStream_t s) {
+    StArgs3<dfloat> a = {};
+    a.x = reinterpret_cast<const dfloat *>(x);
+    a.b = reinterpret_cast<const dfloat *>(b);
+    a.y = reinterpret_cast<dfloat *>(r);
+    launch3<dfloat, M_RESX>(ws, a, s);
 }
 
 void op3d_iteration(bella_ws *ws, int prec, cudaStream_t s) {
