@@ -423,7 +423,9 @@ long long bella_cnn_launches(const bella_cnn *net);
 /* Flexible BiCGStab on the 3D operator of ws, right-preconditioned by net: the
  * preconditioner slot of scipy's bicgstab (its M argument), which the reference
  * leaves empty at second_projection.py:230.  FP32 inner iterations (FP32 stencil,
- * FP64 reductions) inside FP64 iterative refinement on the true residual; tol,
+ * FP64 reductions) inside FP64 iterative refinement on the true residual (the
+ * residual of the FP64 iterate formed in double-float arithmetic, about 1e-14 of
+ * |A||x|, when tol >= 1e-11; in FP64 below that and after a fallback); tol,
  * atol, maxiter, x0_zero, project_null, inner_tol, max_outer, check_every and
  * timeout_s as for bella_bicgstab (precision is ignored); each inner solve is
  * capped at maxiter/max_outer iterations (at least 100).  When the learned

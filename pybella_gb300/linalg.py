@@ -111,8 +111,9 @@ class _NodalOperator:
         preconditioned by a :class:`pybella_gb300.learned.CNN`, a
         :class:`pybella_gb300.spectral.BackgroundSolve` or a
         :class:`pybella_gb300.learned.LearnedPreconditioner` (background solve
-        corrected by the network): FP32 inner iterations in FP64 refinement,
-        ``precision`` ignored; a failed preconditioned solve is finished by the
+        corrected by the network): FP32 inner iterations in FP64 refinement
+        (its residual formed in double-float arithmetic, about 1e-14 of
+        |A||x|, when ``tol >= 1e-11``), ``precision`` ignored; a failed preconditioned solve is finished by the
         plain double-float method, reported in ``stats['fallback']`` and by a
         warning.  ``method='fgmres'`` runs the preconditioned inner solves as
         flexible GMRES cycles of at most ``restart`` iterations (exact for a
