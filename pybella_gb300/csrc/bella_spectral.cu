@@ -488,22 +488,23 @@ k_sp_factor(int Kx, int ny, int Kz, const double *mux, const double *muz, const 
     if (line >= nl) return;
     const LineCoef L = line_coef((int)(line / Kz), (int)(line % Kz), mux, muz, hc_zero, idx2, idy2, idz2);
     if (L.cat == 3) return;
-    auto off = [&](int j) { return L.al * cx[j] - L.be * cy[j] + L.ga * cz[j]; };   // between nodes j, j+1
-    auto diag = [&](int j) {
-        double d = hcm[j];
-        if (j > 0) d += L.al * cx[j - 1] + L.be * cy[j - 1] + L.ga * cz[j - 1];
-        if (j < ny - 1) d += L.al * cx[j] + L.be * cy[j] + L.ga * cz[j];
-        return d;
-    };
+    // row j couples nodes j-1, j, j+1 through the cells j-1 and j (cx, cy, cz per cell
+    // row, ny-1 of them): off-diagonal al cx - be cy + ga cz of a cell, diagonal hcm plus
+    // al cx + be cy + ga cz of both cells.  A row's cell coefficients and off-diagonal
+    // carry over to the next row, so each row costs one new cell (12 FP64 operations
+    // with the reciprocal; GB300's FP64 pipe bounds this loop)
     const int j0 = L.cat ? 1 : 0;
-    double cprev = 0.0;
+    double px = j0 > 0 ? cx[j0 - 1] : 0.0, py = j0 > 0 ? cy[j0 - 1] : 0.0, pz = j0 > 0 ? cz[j0 - 1] : 0.0;
+    double a = 0.0, cprev = 0.0;                      // no sub-diagonal in the first solved row
     for (int j = j0; j < ny; ++j) {
-        const double a = j > j0 ? off(j - 1) : 0.0;
-        const double c = j < ny - 1 ? off(j) : 0.0;
+        const bool last = j == ny - 1;
+        const double qx = last ? 0.0 : cx[j], qy = last ? 0.0 : cy[j], qz = last ? 0.0 : cz[j];
+        const double c = L.al * qx - L.be * qy + L.ga * qz;                       // 0 on the last row
+        const double d = hcm[j] + L.al * (px + qx) + L.be * (py + qy) + L.ga * (pz + qz);
         // 1 / den by Newton-Raphson from an FP32 seed: each step x <- x (2 - den x)
         // squares the relative error (2^-23 -> 2^-46 -> below FP64 rounding), four
-        // FP64 FMAs instead of an FP64 division (GB300's FP64 pipe bounds this loop)
-        const double den = diag(j) - a * cprev;
+        // FP64 FMAs instead of an FP64 division
+        const double den = d - a * cprev;
         double inv;
         if (fabs(den) > 1e-30 && fabs(den) < 1e30) {   // the seed within FP32's range
             inv = (double)(1.0f / (float)den);
@@ -516,6 +517,8 @@ k_sp_factor(int Kx, int ny, int Kz, const double *mux, const double *muz, const 
         la[(long long)j * nl + line] = (float)a;
         lc[(long long)j * nl + line] = (float)cprev;
         li[(long long)j * nl + line] = (float)inv;
+        a = c;
+        px = qx; py = qy; pz = qz;
     }
 }
 
