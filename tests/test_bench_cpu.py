@@ -52,3 +52,29 @@ def test_step2d_workload_inputs_and_cpu_sample(monkeypatch):
     np.testing.assert_array_equal(st["mpv"].HydroState_n.S0, hn["S0"])
     v, k = bench._cpu_step2d_sample(0.0)
     assert k == 1 and v > 0
+
+
+def test_clock_sampler_decodes_nvml_reasons_and_keeps_only_its_samples():
+    """The NVML path of bench.ClockSampler: clock-event reason bits map to the names
+    the bench line reports (sw_power_cap kept, slowdowns named), the median SM clock
+    and the maximum are taken over the samples of the timed region only; without
+    NVML or nvidia-smi the line says so instead of inventing a clock."""
+    import threading
+    import bench
+    c = bench.ClockSampler(0)
+    c.nvml = ("lib", "handle")                 # as after a successful start()
+    c.thread = threading.Thread(target=lambda: None)
+    c.thread.start()
+    c.rows = [(2070.0, 2070.0, 0x0), (2055.0, 2070.0, 0x4), (1800.0, 2070.0, 0x8 | 0x1)]
+    out = c.stop()
+    assert out["samples"] == 3 and out["sm_mhz"] == 2055.0 and out["sm_max_mhz"] == 2070.0
+    assert out["reasons"] == ["hw_slowdown", "sw_power_cap"]
+    assert out["source"].startswith("nvml")
+    c2 = bench.ClockSampler(0)
+    c2.rows = [(2070.0, 2070.0, 0x20 | 0x40 | 0x80)]
+    c2.nvml = ("lib", "handle")
+    c2.thread = threading.Thread(target=lambda: None)
+    c2.thread.start()
+    assert c2.stop()["reasons"] == ["hw_power_brake_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown"]
+    c3 = bench.ClockSampler(0)                 # neither NVML nor nvidia-smi started
+    assert c3.stop()["reasons"] == ["nvidia-smi unavailable"]
